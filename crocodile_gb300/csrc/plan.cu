@@ -1,0 +1,537 @@
+// Plan construction: bit-exact cell assignment of every visibility (K1),
+// counting sort into grid tiles or kernel groups (K2), and the work list of
+// the persistent gridding kernels.
+//
+// Replaces the per-visibility coordinate work of convgrid/convdegrid
+// (crocodile/synthesis.py:476-479, 497-499 via frac_coords :438-449) and the
+// w ordering of sort_vis_w (:506-515).
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+
+#include "cg_internal.cuh"
+
+namespace cg {
+
+static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// ---------------------------------------------------------------- scan
+// Exclusive scan of int32 counts (bucket histograms).  Three phases:
+// per-block scan + block totals, scan of the totals, add-back.
+static constexpr int SCAN_THREADS = 1024;
+static constexpr int SCAN_PER_THREAD = 4;
+static constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER_THREAD;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *s_warp,
+                                                    int &total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) s_warp[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    int nw = blockDim.x >> 5;
+    int w = lane < nw ? s_warp[lane] : 0;
+    int winc = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, winc, o);
+      if (lane >= o) winc += t;
+    }
+    if (lane < nw) s_warp[lane] = winc - w;
+    if (lane == 31) s_warp[32] = winc;
+  }
+  __syncthreads();
+  total = s_warp[32];
+  int r = s_warp[warp] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+__global__ void k_scan_tiles(const int32_t *__restrict__ in,
+                             int32_t *__restrict__ out, int n,
+                             int32_t *__restrict__ block_sums) {
+  __shared__ int s_warp[33];
+  const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+  int v[SCAN_PER_THREAD];
+  int sum = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+    v[k] = (base + k < n) ? in[base + k] : 0;
+    sum += v[k];
+  }
+  int total;
+  int run = block_exclusive_scan(sum, s_warp, total);
+#pragma unroll
+  for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+    if (base + k < n) out[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 0 && block_sums) block_sums[blockIdx.x] = total;
+}
+
+__global__ void k_scan_add(int32_t *__restrict__ out, int n,
+                           const int32_t *__restrict__ block_offsets) {
+  const int i = blockIdx.x * SCAN_TILE + threadIdx.x;
+  const int add = block_offsets[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+    int j = i + k * SCAN_THREADS;
+    if (j < n && j < (blockIdx.x + 1) * SCAN_TILE) out[j] += add;
+  }
+}
+
+size_t scan_scratch_words(int n) {
+  int nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  return 2 * (size_t)(nb + 1);
+}
+
+int launch_scan(const int32_t *in, int32_t *out, int n, int32_t *scratch,
+                cudaStream_t s) {
+  if (n <= 0) return CG_OK;
+  int nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (nb == 1) {
+    k_scan_tiles<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr);
+    CG_LAUNCH("scan");
+    return CG_OK;
+  }
+  CG_REQUIRE(nb <= SCAN_TILE, "scan of %d buckets exceeds the two-level limit", n);
+  int32_t *sums = scratch, *sums_off = scratch + nb + 1;
+  k_scan_tiles<<<nb, SCAN_THREADS, 0, s>>>(in, out, n, sums);
+  k_scan_tiles<<<1, SCAN_THREADS, 0, s>>>(sums, sums_off, nb, nullptr);
+  k_scan_add<<<nb, SCAN_THREADS, 0, s>>>(out, n, sums_off);
+  CG_LAUNCH("scan");
+  return CG_OK;
+}
+
+// ---------------------------------------------------------------- K1 coordinates
+struct CoordParams {
+  const double *uvw;
+  int64_t stride;
+  double lam;
+  int64_t n;
+  int H, W, Q, S, G, sep;
+  const int32_t *kidx;
+  int mode, T, ntx, nbuckets;
+  VisRec *rec;
+  int32_t *key;
+  int32_t *rank;
+  int32_t *hist;
+  int32_t *status;
+};
+
+// Warp-aggregated increment of hist[key]; returns this lane's slot.  All 32
+// lanes of the warp must call it (invalid lanes pass valid = false).
+__device__ __forceinline__ int aggregated_slot(int32_t *hist, int key,
+                                               bool valid) {
+  const int lane = threadIdx.x & 31;
+  unsigned peers = __match_any_sync(0xffffffffu, valid ? key : -1);
+  int leader = __ffs(peers) - 1;
+  int base = 0;
+  if (valid && lane == leader) base = atomicAdd(&hist[key], __popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+__global__ void k_plan_coords(CoordParams P) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool live = i < P.n;
+  bool ok = live;
+  int key = -1;
+  VisRec r = {0, 0, 0, 0};
+  if (live) {
+    double pu = vis_coord(P.uvw, P.stride, i, 0, P.lam);
+    double pv = vis_coord(P.uvw, P.stride, i, 1, P.lam);
+    if (!(in_unit_range(pu) && in_unit_range(pv))) {
+      atomicAdd(&P.status[ST_RANGE], 1);
+      ok = false;
+    } else {
+      int x, xf, y, yf;
+      frac_coord(pu, P.W, P.Q, x, xf);
+      frac_coord(pv, P.H, P.Q, y, yf);
+      int x0 = x - P.S / 2, y0 = y - P.S / 2;
+      if (x0 < 0 || y0 < 0 || x0 + P.S > P.W || y0 + P.S > P.H) {
+        atomicAdd(&P.status[ST_BOUNDS], 1);
+        ok = false;
+      }
+      int g = P.kidx ? P.kidx[i] : 0;
+      if (g < 0 || g >= P.G) {
+        atomicAdd(&P.status[ST_INDEX], 1);
+        ok = false;
+      }
+      r.x0 = x0;
+      r.y0 = y0;
+      if (P.sep) {
+        r.k0 = g * P.Q + yf;
+        r.k1 = g * P.Q + xf;
+      } else {
+        r.k0 = g;
+        r.k1 = yf * P.Q + xf;
+      }
+      if (ok)
+        key = (P.mode == CG_PLAN_TILED) ? (y0 / P.T) * P.ntx + (x0 / P.T) : g;
+    }
+  }
+  int slot = aggregated_slot(P.hist, key, ok);
+  if (live) {
+    P.rec[i] = r;
+    P.key[i] = ok ? key : -1;
+    P.rank[i] = slot;
+  }
+}
+
+__global__ void k_plan_scatter(int64_t n, const VisRec *__restrict__ rec,
+                               const int32_t *__restrict__ key,
+                               const int32_t *__restrict__ rank,
+                               const int32_t *__restrict__ offsets,
+                               VisRec *__restrict__ out, int32_t *__restrict__ perm) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int k = key[i];
+  if (k < 0) return;
+  int pos = offsets[k] + rank[i];
+  out[pos] = rec[i];
+  perm[pos] = (int32_t)i;
+}
+
+__global__ void k_plan_items(int nb, const int32_t *__restrict__ counts,
+                             const int32_t *__restrict__ offsets, int chunk,
+                             WorkItem *__restrict__ items,
+                             int32_t *__restrict__ nitems) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  int c = counts[b];
+  if (c == 0) return;
+  int nch = (c + chunk - 1) / chunk;
+  int base = atomicAdd(nitems, nch);
+  int off = offsets[b];
+  for (int j = 0; j < nch; ++j) {
+    WorkItem w;
+    w.tile = b;
+    w.start = off + j * chunk;
+    w.count = min(chunk, c - j * chunk);
+    w.pad = 0;
+    items[base + j] = w;
+  }
+}
+
+__global__ void k_frac_coords(const double *uvw, int64_t stride, double lam,
+                              int64_t n, int H, int W, int Q, int32_t *x,
+                              int32_t *xf, int32_t *y, int32_t *yf,
+                              int32_t *status) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double pu = vis_coord(uvw, stride, i, 0, lam);
+  double pv = vis_coord(uvw, stride, i, 1, lam);
+  if (!(in_unit_range(pu) && in_unit_range(pv))) atomicAdd(&status[ST_RANGE], 1);
+  int a, b, c, d;
+  frac_coord(pu, W, Q, a, b);
+  frac_coord(pv, H, Q, c, d);
+  x[i] = a;
+  xf[i] = b;
+  y[i] = c;
+  yf[i] = d;
+}
+
+// ---------------------------------------------------------------- w bins
+// w_cache_imaging's bin (synthesis.py:793): wbin = wstep * round(w / wstep),
+// half-to-even.  k = rint(w / wstep) is the bin number.
+__global__ void k_w_bins(const double *uvw, int64_t stride, int64_t n, double wstep,
+                         int32_t *kidx, int32_t *minmax, int32_t *status) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double k = rint(__ddiv_rn(uvw[i * stride + 2], wstep));
+  if (!(k > -1.0e9 && k < 1.0e9)) {
+    atomicAdd(&status[ST_RANGE], 1);
+    kidx[i] = 0;
+    return;
+  }
+  const int ki = (int)k;
+  kidx[i] = ki;
+  atomicMin(&minmax[0], ki);
+  atomicMax(&minmax[1], ki);
+}
+
+__global__ void k_w_bins_rebase(int32_t *kidx, int64_t n, const int32_t *minmax) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) kidx[i] -= minmax[0];
+}
+
+// Bins against a known table range [kmin, kmin + nk): no host round trip.
+__global__ void k_w_bins_fixed(const double *uvw, int64_t stride, int64_t n, double wstep,
+                               int kmin, int nk, int32_t *kidx, int32_t *status) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double k = rint(__ddiv_rn(uvw[i * stride + 2], wstep));
+  const double j = k - (double)kmin;
+  if (!(j >= 0.0 && j < (double)nk)) {
+    atomicAdd(&status[ST_INDEX], 1);
+    kidx[i] = 0;
+    return;
+  }
+  kidx[i] = (int32_t)j;
+}
+
+__global__ void k_minmax_init(int32_t *mm) {
+  mm[0] = INT32_MAX;
+  mm[1] = INT32_MIN;
+}
+
+// ---------------------------------------------------------------- sizing
+struct Layout {
+  size_t rec_tmp, key, rank, recs, perm, counts, offsets, scan, items, ctr, total;
+};
+
+static int tile_edge(int S) {
+  if (S <= 8) return 32;
+  if (S <= 16) return 48;
+  return 64;
+}
+
+static void plan_geometry(cg_plan &p) {
+  if (p.mode == CG_PLAN_TILED) {
+    p.T = tile_edge(p.kd.S);
+    p.ntx = (p.W + p.T - 1) / p.T;
+    p.nty = (p.H + p.T - 1) / p.T;
+    p.nbuckets = p.ntx * p.nty;
+    p.win = p.T + p.kd.S - 1;
+    p.pitch = (p.win + 1) & ~1;
+    int64_t want = p.n / (int64_t)(num_sms() * 16) + 1;
+    p.chunk = (int)std::min<int64_t>(2048, std::max<int64_t>(256, want));
+    p.max_items = (p.n + p.chunk - 1) / p.chunk + p.nbuckets;
+  } else {
+    p.T = 0;
+    p.ntx = p.nty = 0;
+    p.nbuckets = p.kd.G;
+    p.win = p.pitch = 0;
+    p.chunk = 0;
+    p.max_items = 0;
+  }
+}
+
+static Layout layout_of(const cg_plan &p) {
+  Layout L;
+  size_t o = 0;
+  size_t n = (size_t)std::max<int64_t>(p.n, 1);
+  L.rec_tmp = o; o = align256(o + n * sizeof(VisRec));
+  L.key = o;     o = align256(o + n * 4);
+  L.rank = o;    o = align256(o + n * 4);
+  L.recs = o;    o = align256(o + n * sizeof(VisRec));
+  L.perm = o;    o = align256(o + n * 4);
+  L.counts = o;  o = align256(o + (size_t)p.nbuckets * 4);
+  L.offsets = o; o = align256(o + (size_t)p.nbuckets * 4);
+  L.scan = o;    o = align256(o + scan_scratch_words(p.nbuckets) * 4);
+  L.items = o;   o = align256(o + (size_t)std::max<int64_t>(p.max_items, 1) * sizeof(WorkItem));
+  L.ctr = o;     o = align256(o + 4 * 4);
+  L.total = o;
+  return L;
+}
+
+static int check_desc(const cg_kernel_desc *kd, int H, int W) {
+  CG_REQUIRE(kd, "kernel descriptor is NULL");
+  CG_REQUIRE(kd->Q >= 1 && kd->S >= 1 && kd->G >= 1,
+             "bad kernel descriptor Q=%d S=%d G=%d", kd->Q, kd->S, kd->G);
+  CG_REQUIRE(kd->S <= 32, "support %d exceeds the supported maximum 32", kd->S);
+  CG_REQUIRE(H >= 1 && W >= 1 && H <= 65536 && W <= 65536, "bad grid %dx%d", H, W);
+  return CG_OK;
+}
+
+}  // namespace cg
+
+using namespace cg;
+
+extern "C" {
+
+size_t cg_plan_workspace_bytes(int mode, int64_t n, int H, int W,
+                               const cg_kernel_desc *kd) {
+  if (check_desc(kd, H, W) != CG_OK) return 0;
+  cg_plan p;
+  memset(&p, 0, sizeof(p));
+  p.mode = mode;
+  p.kd = *kd;
+  p.H = H;
+  p.W = W;
+  p.n = n;
+  plan_geometry(p);
+  return layout_of(p).total;
+}
+
+int cg_plan_create(cg_plan **out, int mode, const cg_kernel_desc *kd, int H,
+                   int W, const double *uvw, int64_t stride, double lam,
+                   const int32_t *kidx, int64_t n, void *workspace,
+                   size_t workspace_bytes, int32_t *d_status,
+                   cg_stream_t stream) {
+  CG_REQUIRE(out, "plan output pointer is NULL");
+  *out = nullptr;
+  int rc = check_desc(kd, H, W);
+  if (rc) return rc;
+  CG_REQUIRE(mode == CG_PLAN_TILED || mode == CG_PLAN_GROUPS, "bad plan mode %d", mode);
+  CG_REQUIRE(n >= 0 && n < (int64_t)INT32_MAX, "visibility count %lld unsupported",
+             (long long)n);
+  CG_REQUIRE(n == 0 || (uvw && stride >= 2), "uvw is NULL or stride < 2");
+  CG_REQUIRE(d_status, "status block is NULL");
+  CG_REQUIRE(kd->G == 1 || kidx || n == 0, "G > 1 needs per-visibility kernel indices");
+  cudaStream_t s = (cudaStream_t)stream;
+
+  cg_plan *p = new (std::nothrow) cg_plan;
+  CG_REQUIRE(p, "out of host memory");
+  memset(p, 0, sizeof(*p));
+  p->mode = mode;
+  p->kd = *kd;
+  p->H = H;
+  p->W = W;
+  p->n = n;
+  plan_geometry(*p);
+  Layout L = layout_of(*p);
+  if (!workspace || workspace_bytes < L.total) {
+    delete p;
+    return set_error(CG_ERR_WORKSPACE, "plan needs %zu workspace bytes, got %zu",
+                     L.total, workspace_bytes);
+  }
+  char *ws = (char *)workspace;
+  VisRec *rec_tmp = (VisRec *)(ws + L.rec_tmp);
+  int32_t *key = (int32_t *)(ws + L.key);
+  int32_t *rank = (int32_t *)(ws + L.rank);
+  p->recs = (VisRec *)(ws + L.recs);
+  p->perm = (int32_t *)(ws + L.perm);
+  p->counts = (int32_t *)(ws + L.counts);
+  p->offsets = (int32_t *)(ws + L.offsets);
+  p->items = (WorkItem *)(ws + L.items);
+  int32_t *ctr = (int32_t *)(ws + L.ctr);
+  p->nitems = ctr;
+  p->ticket = ctr + 1;
+  p->status = d_status;
+
+  auto fail = [&](int code) {
+    delete p;
+    return code;
+  };
+  if (cudaMemsetAsync(p->counts, 0, (size_t)p->nbuckets * 4, s) != cudaSuccess ||
+      cudaMemsetAsync(ctr, 0, 16, s) != cudaSuccess)
+    return fail(cuda_error(cudaGetLastError(), "plan memset"));
+  if (n > 0) {
+    CoordParams P;
+    P.uvw = uvw;
+    P.stride = stride;
+    P.lam = lam;
+    P.n = n;
+    P.H = H;
+    P.W = W;
+    P.Q = kd->Q;
+    P.S = kd->S;
+    P.G = kd->G;
+    P.sep = kd->sep;
+    P.kidx = kidx;
+    P.mode = mode;
+    P.T = p->T;
+    P.ntx = p->ntx;
+    P.nbuckets = p->nbuckets;
+    P.rec = rec_tmp;
+    P.key = key;
+    P.rank = rank;
+    P.hist = p->counts;
+    P.status = d_status;
+    int blocks = (int)((n + 255) / 256);
+    k_plan_coords<<<blocks, 256, 0, s>>>(P);
+    if (cudaGetLastError() != cudaSuccess) return fail(cuda_error(cudaGetLastError(), "coords"));
+    int rc2 = launch_scan(p->counts, p->offsets, p->nbuckets,
+                          (int32_t *)(ws + L.scan), s);
+    if (rc2) return fail(rc2);
+    k_plan_scatter<<<blocks, 256, 0, s>>>(n, rec_tmp, key, rank, p->offsets,
+                                          p->recs, p->perm);
+    if (mode == CG_PLAN_TILED)
+      k_plan_items<<<(p->nbuckets + 255) / 256, 256, 0, s>>>(
+          p->nbuckets, p->counts, p->offsets, p->chunk, p->items, p->nitems);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(cuda_error(e, "plan sort"));
+  }
+  if (mode == CG_PLAN_GROUPS) {
+    p->h_counts = (int32_t *)malloc((size_t)p->nbuckets * 4);
+    p->h_offsets = (int32_t *)malloc((size_t)p->nbuckets * 4);
+    if (!p->h_counts || !p->h_offsets) {
+      free(p->h_counts);
+      free(p->h_offsets);
+      return fail(set_error(CG_ERR_ARG, "out of host memory"));
+    }
+    cudaError_t e1 = cudaMemcpyAsync(p->h_counts, p->counts, (size_t)p->nbuckets * 4,
+                                     cudaMemcpyDeviceToHost, s);
+    cudaError_t e2 = cudaMemcpyAsync(p->h_offsets, p->offsets, (size_t)p->nbuckets * 4,
+                                     cudaMemcpyDeviceToHost, s);
+    cudaError_t e3 = cudaStreamSynchronize(s);
+    if (e1 || e2 || e3) {
+      free(p->h_counts);
+      free(p->h_offsets);
+      return fail(cuda_error(e1 ? e1 : e2 ? e2 : e3, "plan group readback"));
+    }
+    if (n == 0) memset(p->h_counts, 0, (size_t)p->nbuckets * 4);
+  }
+  *out = p;
+  return CG_OK;
+}
+
+int cg_plan_destroy(cg_plan *p) {
+  if (p) {
+    free(p->h_counts);
+    free(p->h_offsets);
+    delete p;
+  }
+  return CG_OK;
+}
+
+int cg_plan_info(const cg_plan *p, int64_t *info) {
+  CG_REQUIRE(p && info, "NULL argument");
+  info[0] = p->T;
+  info[1] = p->max_items;
+  info[2] = p->chunk;
+  info[3] = p->nbuckets;
+  return CG_OK;
+}
+
+int cg_w_bins(const double *uvw, int64_t stride, int64_t n, double wstep, int32_t *kidx,
+              int32_t *d_minmax, int32_t *h_minmax, int32_t *d_status, cg_stream_t stream) {
+  CG_REQUIRE(n >= 1 && uvw && stride >= 3 && kidx && d_minmax && h_minmax && d_status,
+             "bad w_bins arguments");
+  CG_REQUIRE(wstep != 0.0, "wstep must be non-zero");
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  k_minmax_init<<<1, 1, 0, s>>>(d_minmax);
+  k_w_bins<<<blocks, 256, 0, s>>>(uvw, stride, n, wstep, kidx, d_minmax, d_status);
+  k_w_bins_rebase<<<blocks, 256, 0, s>>>(kidx, n, d_minmax);
+  CG_LAUNCH("w_bins");
+  CG_CUDA(cudaMemcpyAsync(h_minmax, d_minmax, 8, cudaMemcpyDeviceToHost, s));
+  CG_CUDA(cudaStreamSynchronize(s));
+  return CG_OK;
+}
+
+int cg_w_bins_fixed(const double *uvw, int64_t stride, int64_t n, double wstep, int kmin,
+                    int nk, int32_t *kidx, int32_t *d_status, cg_stream_t stream) {
+  CG_REQUIRE(n >= 0 && (n == 0 || (uvw && stride >= 3 && kidx && d_status)) && nk >= 1,
+             "bad w_bins_fixed arguments");
+  CG_REQUIRE(wstep != 0.0, "wstep must be non-zero");
+  if (n == 0) return CG_OK;
+  k_w_bins_fixed<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      uvw, stride, n, wstep, kmin, nk, kidx, d_status);
+  CG_LAUNCH("w_bins_fixed");
+  return CG_OK;
+}
+
+int cg_frac_coords(const double *uvw, int64_t stride, double lam, int64_t n,
+                   int H, int W, int Q, int32_t *x, int32_t *xf, int32_t *y,
+                   int32_t *yf, int32_t *d_status, cg_stream_t stream) {
+  CG_REQUIRE(Q >= 1 && H >= 1 && W >= 1, "bad frac_coords arguments");
+  CG_REQUIRE(n == 0 || (uvw && x && xf && y && yf && d_status && stride >= 2),
+             "NULL argument");
+  if (n == 0) return CG_OK;
+  k_frac_coords<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      uvw, stride, lam, n, H, W, Q, x, xf, y, yf, d_status);
+  CG_LAUNCH("frac_coords");
+  return CG_OK;
+}
+
+}  // extern "C"

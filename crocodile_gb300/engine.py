@@ -1,0 +1,366 @@
+"""Device-level engine: HBM-resident torch tensors in, C-ABI kernels underneath.
+
+PyTorch only provides device memory, streams and the current device here;
+every computation on the gridding path is a kernel of libcrocodile_gb300.so.
+All functions take and return CUDA tensors and run on the current stream.
+"""
+
+import ctypes
+import weakref
+
+import numpy
+import torch
+
+from . import _lib as L
+
+CF = torch.complex64
+CD = torch.complex128
+
+
+def _p(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("crocodile_gb300 needs a CUDA GPU (sm_103a); none is visible")
+    L.lib()
+
+
+def cuda_tensor(x, dtype):
+    """x (numpy array or tensor) as a contiguous CUDA tensor of dtype."""
+    if isinstance(x, torch.Tensor):
+        t = x.to(device="cuda", dtype=dtype)
+    else:
+        a = numpy.asarray(x)
+        if dtype.is_complex:
+            a = a.astype(numpy.complex128 if dtype == CD else numpy.complex64, copy=False)
+        t = torch.as_tensor(numpy.ascontiguousarray(a)).to(device="cuda", dtype=dtype)
+    return t.contiguous()
+
+
+class Status:
+    """The CG_STATUS_WORDS device counters shared by a sequence of calls."""
+
+    def __init__(self):
+        self.t = torch.zeros(L.CG_STATUS_WORDS, dtype=torch.int32, device="cuda")
+
+    def reset(self):
+        L.call("cg_status_reset", _p(self.t), stream())
+
+    def check(self):
+        """Synchronise and raise the reference's exception for any counted error."""
+        L.raise_for(L.lib().cg_status_check(_p(self.t), None, stream()))
+
+    def counts(self):
+        return self.t.cpu().tolist()
+
+
+# --------------------------------------------------------------------------
+# kernel tables
+
+class KernelTable:
+    """A GCF table on the device, flattened to [G, Q, (Q,) S(, S)] (synthesis.py:451-461)."""
+
+    def __init__(self, table, sep, Q, S):
+        self.table = table.contiguous()
+        self.sep = bool(sep)
+        self.Q, self.S = int(Q), int(S)
+        per = Q * S if sep else Q * Q * S * S
+        self.G = self.table.numel() // per
+        if self.G * per != self.table.numel():
+            raise ValueError("kernel table size does not match Q=%d S=%d" % (Q, S))
+
+    @property
+    def dtype(self):
+        return self.table.dtype
+
+    def desc(self):
+        return L.KernelDesc(int(self.sep), self.Q, self.S, self.G)
+
+    def to(self, dtype):
+        return self if dtype == self.dtype else KernelTable(self.table.to(dtype), self.sep,
+                                                            self.Q, self.S)
+
+    @classmethod
+    def from_gcf(cls, gcf, nsrc, dtype=CF):
+        """Layout from the kernel rank against the src columns, as make_gcf decides it."""
+        shape = tuple(gcf.shape)
+        extra = len(shape) - nsrc
+        if extra == 2:
+            sep, Q, S = True, shape[-2], shape[-1]
+        elif extra == 4:
+            if shape[-1] != shape[-2]:
+                raise ValueError("non-square kernels are not supported")
+            sep, Q, S = False, shape[-3], shape[-1]
+        else:
+            raise AssertionError("kernel rank %d does not match %d src columns"
+                                 % (len(shape), nsrc))
+        if not sep and shape[-3] != shape[-4]:
+            raise ValueError("kernel oversampling must be equal along both axes")
+        return cls(cuda_tensor(gcf, dtype).reshape(-1), sep, Q, S)
+
+
+def kernel_groups(lead_shape, src, n):
+    """Flat group index of each src row into the kernel's leading dims (numpy indexing,
+    negative indices wrap); int32 numpy array, or None when there are no src columns."""
+    if src is None:
+        return None
+    src = numpy.asarray(src)
+    if src.ndim != 2 or src.shape[1] == 0:
+        return None
+    if src.shape[1] != len(lead_shape):
+        raise AssertionError("src has %d columns, kernel has %d leading dims"
+                             % (src.shape[1], len(lead_shape)))
+    idx = src.astype(numpy.int64)
+    for k, d in enumerate(lead_shape):
+        col = idx[:, k]
+        if ((col < -d) | (col >= d)).any():
+            raise IndexError("src column %d out of range for kernel dimension %d" % (k, d))
+        idx[:, k] = numpy.where(col < 0, col + d, col)
+    return numpy.ravel_multi_index(tuple(idx.T), lead_shape).astype(numpy.int32)
+
+
+# --------------------------------------------------------------------------
+# plans and gridding
+
+class Plan:
+    """Sorted, bit-exact cell assignment of a visibility set (cg_plan_create).
+
+    ``uvw`` is a float64 CUDA tensor [n, >=2] (rows in units such that
+    uvw / lam is the fraction of the grid), ``shape`` the grid (H, W)."""
+
+    def __init__(self, uvw, lam, shape, ktab, kidx=None, mode=L.CG_PLAN_TILED, status=None):
+        require_cuda()
+        self.uvw = cuda_tensor(uvw, torch.float64)
+        if self.uvw.dim() != 2 or self.uvw.shape[1] < 2:
+            raise ValueError("uvw must be [n, >=2]")
+        self.n = self.uvw.shape[0]
+        self.kidx = None if kidx is None else cuda_tensor(kidx, torch.int32)
+        self.shape = (int(shape[0]), int(shape[1]))
+        self.mode = mode
+        self.sep, self.Q, self.S, self.G = ktab.sep, ktab.Q, ktab.S, ktab.G
+        kd = ktab.desc()
+        self._kd = kd
+        nbytes = L.lib().cg_plan_workspace_bytes(mode, self.n, self.shape[0], self.shape[1],
+                                                 ctypes.byref(kd))
+        if nbytes == 0:
+            L.raise_for(L.CG_ERR_ARG, "cg_plan_workspace_bytes")
+        self.ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+        self.status = status or Status()
+        if status is None:
+            self.status.reset()
+        h = ctypes.c_void_p()
+        L.call("cg_plan_create", ctypes.byref(h), mode, ctypes.byref(kd), self.shape[0],
+               self.shape[1], _p(self.uvw), self.uvw.stride(0), float(lam), _p(self.kidx),
+               self.n, _p(self.ws), nbytes, _p(self.status.t), stream())
+        self.handle = h
+        self._fin = weakref.finalize(self, L.lib().cg_plan_destroy, h)
+
+    def info(self):
+        out = (ctypes.c_int64 * 4)()
+        L.call("cg_plan_info", self.handle, out)
+        return {"tile": out[0], "max_items": out[1], "chunk": out[2], "buckets": out[3]}
+
+    def check(self):
+        self.status.check()
+
+    def _table(self, ktab, dtype):
+        if (ktab.sep, ktab.Q, ktab.S, ktab.G) != (self.sep, self.Q, self.S, self.G):
+            raise ValueError("kernel table does not match the plan's kernel layout")
+        return ktab.to(dtype).table
+
+    def grid(self, ktab, vis, grid):
+        """grid (c64 [H, W]) += convgrid of vis (c64 [n])."""
+        t = self._table(ktab, CF)
+        L.call("cg_grid", self.handle, _p(t), _p(vis), _p(grid), stream())
+        return grid
+
+    def grid_weighted(self, ktab, vis, weight, grid):
+        """grid += convgrid of vis * weight (vis None: weight alone, the PSF pass)."""
+        t = self._table(ktab, CF)
+        L.call("cg_grid_weighted", self.handle, _p(t), _p(vis), _p(weight), _p(grid), stream())
+        return grid
+
+    def degrid(self, ktab, grid, out=None):
+        t = self._table(ktab, CF)
+        if out is None:
+            out = torch.empty(self.n, dtype=CF, device="cuda")
+        L.call("cg_degrid", self.handle, _p(t), _p(grid), _p(out), stream())
+        return out
+
+    def grid_fp64(self, ktab, vis, grid):
+        t = self._table(ktab, CD)
+        L.call("cg_grid_fp64", self.handle, _p(t), _p(vis), _p(grid), stream())
+        return grid
+
+    def degrid_fp64(self, ktab, grid, out=None):
+        t = self._table(ktab, CD)
+        if out is None:
+            out = torch.empty(self.n, dtype=CD, device="cuda")
+        L.call("cg_degrid_fp64", self.handle, _p(t), _p(grid), _p(out), stream())
+        return out
+
+
+def frac_coords(uvw, lam, shape, Q, status):
+    uvw = cuda_tensor(uvw, torch.float64)
+    n = uvw.shape[0]
+    outs = [torch.empty(n, dtype=torch.int32, device="cuda") for _ in range(4)]
+    L.call("cg_frac_coords", _p(uvw), uvw.stride(0), float(lam), n, int(shape[0]),
+           int(shape[1]), int(Q), *[_p(o) for o in outs], _p(status.t), stream())
+    return outs
+
+
+def w_bins(uvw, wstep, status):
+    """(kidx int32 [n] = bin - min bin, min bin, max bin) of w_cache_imaging's bins."""
+    uvw = cuda_tensor(uvw, torch.float64)
+    n = uvw.shape[0]
+    kidx = torch.empty(n, dtype=torch.int32, device="cuda")
+    dmm = torch.empty(2, dtype=torch.int32, device="cuda")
+    hmm = (ctypes.c_int32 * 2)()
+    L.call("cg_w_bins", _p(uvw), uvw.stride(0), n, float(wstep), _p(kidx), _p(dmm), hmm,
+           _p(status.t), stream())
+    return kidx, int(hmm[0]), int(hmm[1])
+
+
+def grid_boxcar(uvw, lam, vis, grid, status):
+    L.call("cg_grid_boxcar", _p(uvw), uvw.stride(0), float(lam), uvw.shape[0], _p(vis),
+           _p(grid), grid.shape[0], grid.shape[1], _p(status.t), stream())
+    return grid
+
+
+def degrid_boxcar(uvw, lam, grid, status):
+    out = torch.empty(uvw.shape[0], dtype=CD, device="cuda")
+    L.call("cg_degrid_boxcar", _p(uvw), uvw.stride(0), float(lam), uvw.shape[0], _p(grid),
+           _p(out), grid.shape[0], grid.shape[1], _p(status.t), stream())
+    return out
+
+
+# --------------------------------------------------------------------------
+# imaging helpers
+
+def weights(uvw, lam, N, status, v_in=None):
+    """doweight on the device: float64 [n] weights."""
+    n = uvw.shape[0]
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    counts = torch.empty(N * N, dtype=torch.int32, device="cuda")
+    L.call("cg_weights", _p(uvw), uvw.stride(0), float(lam), n, int(N), _p(v_in), _p(out),
+           _p(counts), _p(status.t), stream())
+    return out
+
+
+def mirror_uvw(uvw, vis):
+    """In place on the device tensors (mirror_uvw)."""
+    L.call("cg_mirror_uvw", _p(uvw), uvw.stride(0), uvw.shape[0], _p(vis),
+           int(vis is not None and vis.dtype == CF), stream())
+
+
+def make_hermitian(grid):
+    L.call("cg_make_hermitian", _p(grid), grid.shape[-2], grid.shape[-1],
+           int(grid.dtype == CF), stream())
+    return grid
+
+
+def fft_(t, inverse):
+    """Centred (i)fft of the last one or two dims of t, in place."""
+    if t.dim() == 1:
+        H, W, batch = 1, t.shape[0], 1
+    else:
+        H, W = t.shape[-2], t.shape[-1]
+        batch = t.numel() // (H * W)
+    ws = None
+    if not ((H == 1 or H % 2 == 0) and W % 2 == 0):
+        ws = torch.empty_like(t)
+    L.call("cg_fft", _p(t), batch, H, W, int(t.dtype == CF), int(inverse), _p(ws), stream())
+    return t
+
+
+def image_from_grid(grid, want_max=False):
+    """Re(ifft(make_grid_hermitian(grid))) as float32; consumes grid (c64, even sizes)."""
+    H, W = grid.shape
+    img = torch.empty((H, W), dtype=torch.float32, device="cuda")
+    mx = torch.empty(1, dtype=torch.float32, device="cuda") if want_max else None
+    L.call("cg_image_from_grid", _p(grid), H, W, _p(img), _p(mx), stream())
+    return img, mx
+
+
+def scale_image(img, d_scale):
+    L.call("cg_scale_image", _p(img), img.numel(), _p(d_scale), stream())
+    return img
+
+
+# --------------------------------------------------------------------------
+# kernel generation
+
+def kernel_oversample(ff, Qpx, s=None, dtype=CD, ndim=None):
+    """kernel_oversample of one far field, or of a batch along leading dims
+    (then ``ndim`` says whether each far field is 1-D or 2-D), on the device."""
+    ff = cuda_tensor(ff, CD)
+    if ndim is None:
+        ndim = ff.dim()
+    if ndim not in (1, 2) or ff.dim() < ndim:
+        raise AssertionError("Unsupported grid shape for kernel_oversample")
+    if ndim == 2 and ff.shape[-1] != ff.shape[-2]:
+        raise AssertionError("2-D far fields must be square")
+    N0 = ff.shape[-1]
+    s = N0 if s is None else int(s)
+    batch_shape = tuple(ff.shape[:-ndim])
+    batch = int(numpy.prod(batch_shape)) if batch_shape else 1
+    nbytes = L.lib().cg_kernel_oversample_workspace_bytes(batch, ndim, N0, int(Qpx))
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    tail = (Qpx, Qpx, s, s) if ndim == 2 else (Qpx, s)
+    out = torch.empty(batch_shape + tail, dtype=dtype, device="cuda")
+    L.call("cg_kernel_oversample", _p(ff), batch, ndim, N0, int(Qpx), s, _p(out),
+           int(dtype == CF), _p(ws), nbytes, stream())
+    return out
+
+
+def w_kernels(theta, ws_list, NpixFF, NpixKern, Qpx, invert=True, dl=0.0, dm=0.0, T=None,
+              dtype=CF, status=None, max_workspace=1 << 31):
+    """w_kernel for every w in ws_list: [nw, Q, Q, S, S] on the device."""
+    assert NpixFF > NpixKern or (NpixFF == NpixKern and Qpx == 1)
+    w = numpy.ascontiguousarray(numpy.asarray(ws_list, dtype=numpy.float64).ravel())
+    nw = len(w)
+    st = status or Status()
+    if status is None:
+        st.reset()
+    per = L.lib().cg_w_kernels_workspace_bytes(1, int(NpixFF), int(Qpx))
+    full = L.lib().cg_w_kernels_workspace_bytes(nw, int(NpixFF), int(Qpx))
+    nbytes = int(min(full, max(per + 256 + 8 * nw, max_workspace)))
+    wsb = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = torch.empty((nw, Qpx, Qpx, NpixKern, NpixKern), dtype=dtype, device="cuda")
+    Tm = None
+    if T is not None:
+        Tm = numpy.ascontiguousarray(numpy.asarray(T, dtype=numpy.float64).reshape(4))
+    L.call("cg_w_kernels", float(theta), w.ctypes.data_as(ctypes.c_void_p), nw, int(NpixFF),
+           int(NpixKern), int(Qpx), int(bool(invert)), float(dl), float(dm),
+           None if Tm is None else Tm.ctypes.data_as(ctypes.c_void_p), _p(out),
+           int(dtype == CF), _p(wsb), nbytes, _p(st.t), stream())
+    if status is None:
+        st.check()
+    return out
+
+
+def aw_kernels(A, Wk, a1, a2, wi, dtype=CF, status=None):
+    """AW kernels [nk, Q, Q, SA, SA] from A kernels [nA, SA, SA] and w kernels [nW, Q, Q, S, S]."""
+    A = cuda_tensor(A, CD)
+    Wk = cuda_tensor(Wk, CD)
+    a1, a2, wi = (cuda_tensor(x, torch.int32) for x in (a1, a2, wi))
+    nA, SA = A.shape[0], A.shape[-1]
+    nW, Q, S = Wk.shape[0], Wk.shape[1], Wk.shape[-1]
+    nk = a1.shape[0]
+    st = status or Status()
+    if status is None:
+        st.reset()
+    nbytes = L.lib().cg_aw_kernels_workspace_bytes(nk, SA)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = torch.empty((nk, Q, Q, SA, SA), dtype=dtype, device="cuda")
+    L.call("cg_aw_kernels", _p(A), nA, SA, _p(Wk), nW, Q, S, _p(a1), _p(a2), _p(wi), nk,
+           _p(out), int(dtype == CF), _p(ws), nbytes, _p(st.t), stream())
+    if status is None:
+        st.check()
+    return out

@@ -1,0 +1,760 @@
+"""Drop-in replacement for crocodile.synthesis on a GB300.
+
+Same function names, argument meanings, defaults and exceptions as the
+reference module (crocodile/synthesis.py; cited per function).  Grids,
+visibilities and kernels given as numpy arrays come back as numpy arrays of
+the reference's dtypes (complex128 / float64 / int64); given as CUDA torch
+tensors they stay on the device.  The visibility hot path -- coordinates,
+binning, sorting, convolutional gridding and degridding, weighting,
+hermitian symmetry, FFTs and kernel generation -- runs in the hand-written
+sm_103a kernels of libcrocodile_gb300.so; there is no CPU fallback.
+
+Precision: the default ``precision="fp32"`` grids complex64 visibilities with
+FP32 products and accumulation in the tiled persistent kernels, while cell
+assignment and w binning stay bit-exact FP64 and kernels are generated in
+FP64.  ``precision="fp64"`` selects the plain complex128 form (FP64 atomics,
+one launch per kernel group).  Drivers accept ``precision=`` as an extra
+keyword; ``set_precision`` changes the module default.
+
+Small host-side helpers that only reshape or describe arrays (coordinates,
+pad/extract, the prolate spheroidal taper from scipy, slicing) are plain
+numpy, as in the reference.
+"""
+
+import functools
+
+import numpy
+import scipy.special
+import torch
+
+from . import _lib
+from . import engine as E
+
+_PRECISION = "fp32"
+
+
+def set_precision(p):
+    """Module default for the gridding precision: "fp32" (tiled) or "fp64" (plain)."""
+    global _PRECISION
+    if p not in ("fp32", "fp64"):
+        raise ValueError("precision must be 'fp32' or 'fp64'")
+    _PRECISION = p
+
+
+def _prec(p):
+    p = _PRECISION if p is None else p
+    if p not in ("fp32", "fp64"):
+        raise ValueError("precision must be 'fp32' or 'fp64'")
+    return p
+
+
+def _is_dev(x):
+    return isinstance(x, torch.Tensor) and x.is_cuda
+
+
+def _host(t, like=None, dtype=None):
+    """Device tensor -> numpy (complex128 / float64 / int64 as the reference returns)."""
+    if like is not None and _is_dev(like):
+        return t
+    a = t.detach().cpu().numpy()
+    if dtype is not None:
+        return a.astype(dtype)
+    if numpy.iscomplexobj(a):
+        return a.astype(numpy.complex128)
+    if a.dtype.kind == "f":
+        return a.astype(numpy.float64)
+    if a.dtype.kind == "i":
+        return a.astype(numpy.int64)
+    return a
+
+
+def _nrows(x):
+    return x.shape[0]
+
+
+def _src_cols(src, n):
+    if src is None:
+        return 0
+    if isinstance(src, torch.Tensor):
+        src = src.cpu().numpy()
+    s = numpy.asarray(src)
+    if s.size == 0:
+        return 0
+    return s.reshape(n, -1).shape[1]
+
+
+# --------------------------------------------------------------------------
+# coordinates, FFT conventions, padding (synthesis.py:38-197)
+
+def coordinateBounds(N):
+    """Lowest and highest coordinate of an N grid (synthesis.py:38-55)."""
+    if N % 2 == 0:
+        return -0.5, 0.5 * (N - 2) / N
+    return -0.5 * (N - 1) / N, 0.5 * (N - 1) / N
+
+
+def coordinates(N):
+    """1-D coordinates spanning [-0.5, 0.5) with 0 at N//2 (synthesis.py:57-63)."""
+    lo = -(N // 2)
+    return numpy.arange(lo, lo + N) / N
+
+
+def coordinates2(N):
+    """(x, y) coordinate grids with (0, 0) at (N//2, N//2) (synthesis.py:66-80)."""
+    c = numpy.arange(-(N // 2), -(N // 2) + N)
+    rows, cols = numpy.meshgrid(c, c, indexing="ij")
+    return numpy.array([cols, rows]) / N
+
+
+def _centred_fft(a, inverse):
+    dev = _is_dev(a)
+    if not dev:
+        a = numpy.asarray(a)
+        if a.ndim not in (1, 2):
+            raise AssertionError("Unsupported shape for FFT!")
+    t = E.cuda_tensor(a, E.CD if not dev or a.dtype != E.CF else E.CF)
+    if t.dim() not in (1, 2):
+        raise AssertionError("Unsupported shape for FFT!")
+    E.fft_(t, inverse)
+    return t if dev else _host(t)
+
+
+def fft(a):
+    """Image -> grid: fftshift(fft2(ifftshift(a))) on the device (synthesis.py:83-93)."""
+    return _centred_fft(a, False)
+
+
+def ifft(a):
+    """Grid -> image, normalised by 1/N^2, on the device (synthesis.py:96-106)."""
+    return _centred_fft(a, True)
+
+
+def pad_mid(ff, N):
+    """Zero-pad a far field to N around its middle (synthesis.py:109-129)."""
+    N0 = ff.shape[0]
+    if N == N0:
+        return ff
+    assert N > N0
+    lo, hi = N // 2 - N0 // 2, (N + 1) // 2 - (N0 + 1) // 2
+    if ff.ndim == 2:
+        assert N0 == ff.shape[1]
+        return numpy.pad(ff, [(lo, hi), (lo, hi)], mode="constant")
+    return numpy.pad(ff, [(lo, hi)], mode="constant")
+
+
+def extract_mid(a, N):
+    """Centre section of size N (synthesis.py:131-158)."""
+    assert N <= a.shape[0]
+    h, odd, cx = N // 2, N % 2, a.shape[0] // 2
+    if a.ndim == 2:
+        assert N <= a.shape[1]
+        cy = a.shape[1] // 2
+        return a[cx - h:cx + h + odd, cy - h:cy + h + odd]
+    assert a.ndim == 1, "Unsupported grid shape for extract_mid!"
+    return a[cx - h:cx + h + odd]
+
+
+def extract_oversampled(a, Qpx, N):
+    """Sub-kernels of an oversampled pattern (synthesis.py:160-197)."""
+    Na = a.shape[0]
+    start = Na // 2 - Qpx * (N // 2)
+    if a.ndim == 1:
+        return numpy.array([a[start + f:start + f + Qpx * N:Qpx] for f in range(Qpx)],
+                           dtype=complex)
+    assert a.ndim == 2, "Unsupported grid shape for extract_oversampled!"
+    out = numpy.empty((Qpx, Qpx, N, N), dtype=complex)
+    for fy in range(Qpx):
+        for fx in range(Qpx):
+            out[fy, fx] = a[start + fy:start + fy + Qpx * N:Qpx,
+                            start + fx:start + fx + Qpx * N:Qpx]
+    return out
+
+
+# --------------------------------------------------------------------------
+# kernels (synthesis.py:199-377, 682-734)
+
+def anti_aliasing_function(shape, m, c):
+    """Prolate spheroidal taper via scipy.special.pro_ang1 (synthesis.py:199-218).
+
+    Host-side kernel preparation, as in the reference."""
+    if numpy.ndim(shape) == 0:
+        return scipy.special.pro_ang1(m, m, c, (2 - 1 / shape / 4) * coordinates(shape))[0]
+    return numpy.outer(anti_aliasing_function(shape[0], m, c),
+                       anti_aliasing_function(shape[1], m, c))
+
+
+def kernel_transform(dl, dm):
+    """2x2 transform keeping w-kernel coordinates stable under a shift (synthesis.py:220-248)."""
+    dn = numpy.sqrt(1 - dl ** 2 - dm ** 2)
+    f = (dn - 1) / (dl ** 2 + dm ** 2) if (dl != 0 or dm != 0) else 0
+    return numpy.array([[dn - dm * dm * f, dl * dm * f],
+                        [dl * dm * f, dn - dl * dl * f]])
+
+
+def kernel_coordinates(N, theta, dl=0, dm=0, T=None):
+    """(l, m) far-field coordinates, optionally transformed and shifted (synthesis.py:250-270)."""
+    l, m = coordinates2(N) * theta
+    if T is not None:
+        l, m = T[0, 0] * l + T[1, 0] * m, T[0, 1] * l + T[1, 1] * m
+    return l + dl, m + dm
+
+
+def w_kernel_function(l, m, w):
+    """Fresnel pattern exp(2 pi i w (1 - sqrt(1 - l^2 - m^2))) (synthesis.py:273-293)."""
+    r2 = l ** 2 + m ** 2
+    assert numpy.all(r2 < 1.0), "Error in image coordinate system: l %s, m %s" % (l, m)
+    return numpy.exp(2j * numpy.pi * w * (1 - numpy.sqrt(1.0 - r2)))
+
+
+def kernel_recentre(cp, theta, w, dl, dm):
+    """Phase ramp re-centring a kernel in grid space (synthesis.py:296-311)."""
+    l, m = coordinates2(cp.shape[0]) * theta
+    return cp * numpy.exp(-2j * numpy.pi * w * (dl * l + dm * m))
+
+
+def visibility_recentre(uvw, dl, dm):
+    """Counterpart of kernel_recentre on visibility coordinates (synthesis.py:314-327)."""
+    u, v, w = numpy.hsplit(uvw, 3)
+    return numpy.hstack([u - w * dl, v - w * dm, w])
+
+
+def invert_kernel(a):
+    """Pseudo-inverse conj(a)/|a|^2 (synthesis.py:380-386; unused by the reference)."""
+    return numpy.conj(a) / (numpy.abs(a) ** 2)
+
+
+def kernel_oversample(ff, Qpx, s=None):
+    """Oversampled convolution kernel from a far field, FP64 on the device (synthesis.py:330-354)."""
+    dev = _is_dev(ff)
+    ffa = ff if dev else numpy.asarray(ff)
+    if ffa.ndim not in (1, 2):
+        raise AssertionError("Unsupported grid shape for kernel_oversample!")
+    out = E.kernel_oversample(ffa, int(Qpx), s, dtype=E.CD)
+    return out if dev else _host(out)
+
+
+def w_kernel(theta, w, NpixFF, NpixKern, Qpx, invert=True, **kwargs):
+    """[Qpx, Qpx, S, S] w-kernel, FP64 phase + cuFFT on the device (synthesis.py:357-377)."""
+    assert NpixFF > NpixKern or (NpixFF == NpixKern and Qpx == 1)
+    out = E.w_kernels(theta, [w], NpixFF, NpixKern, Qpx, invert=invert,
+                      dl=kwargs.get("dl", 0.0), dm=kwargs.get("dm", 0.0), T=kwargs.get("T"),
+                      dtype=E.CD)
+    return _host(out[0])
+
+
+def w_conj_kernel_fn(kernel_fn):
+    """Kernel function using K(-w) = conj(K(w)) (synthesis.py:682-699)."""
+    def fn(theta, w, *args, **kw):
+        if w < 0:
+            return numpy.conj(kernel_fn(theta, -w, *args, **kw))
+        return kernel_fn(theta, w, *args, **kw)
+    return fn
+
+
+def aw_kernel_fn(a_kernel_fn, w_kernel_fn=w_kernel):
+    """AW kernel function: (A1 conv A2) conv W[yf, xf] on the device (synthesis.py:701-734)."""
+    def fn(theta, w, a1, a2, *src):
+        A = numpy.array([a_kernel_fn(theta, a1, *src), a_kernel_fn(theta, a2, *src)])
+        Wk = numpy.asarray(w_kernel_fn(theta, w))[None]
+        one = numpy.zeros(1, dtype=numpy.int32)
+        out = E.aw_kernels(A, Wk, one, one + 1, one, dtype=E.CD)
+        return _host(out[0])
+    return fn
+
+
+# --------------------------------------------------------------------------
+# visibility coordinates (synthesis.py:419-449)
+
+def frac_coord(N, Qpx, p):
+    """Whole and fractional grid coordinate, bit-exact on the device (synthesis.py:419-435)."""
+    scalar = numpy.ndim(p) == 0
+    pa = numpy.atleast_1d(numpy.asarray(p, dtype=numpy.float64))
+    uv = numpy.column_stack([pa, pa])
+    st = E.Status()
+    x, xf, _, _ = E.frac_coords(uv, 1.0, (N, N), Qpx, st)
+    st.check()
+    x, xf = _host(x), _host(xf)
+    return (x[0], xf[0]) if scalar else (x.reshape(numpy.shape(p)), xf.reshape(numpy.shape(p)))
+
+
+def frac_coords(shape, Qpx, p):
+    """(x, xf, y, yf) with x over the width and y over the height (synthesis.py:438-449)."""
+    st = E.Status()
+    out = E.frac_coords(p, 1.0, shape, Qpx, st)
+    st.check()
+    return tuple(_host(o) for o in out)
+
+
+# --------------------------------------------------------------------------
+# boxcar gridding (synthesis.py:389-416)
+
+def grid(a, p, v):
+    """Boxcar gridding into a, in place, FP64 on the device (synthesis.py:389-401)."""
+    st = E.Status()
+    uvw = E.cuda_tensor(p, torch.float64)
+    g = a if (_is_dev(a) and a.dtype == E.CD) else E.cuda_tensor(a, E.CD)
+    E.grid_boxcar(uvw, 1.0, E.cuda_tensor(v, E.CD), g, st)
+    st.check()
+    if g is not a:
+        if _is_dev(a):
+            a.copy_(g)
+        else:
+            a[...] = g.cpu().numpy()
+
+
+def degrid(a, p):
+    """Boxcar degridding (synthesis.py:404-416)."""
+    st = E.Status()
+    out = E.degrid_boxcar(E.cuda_tensor(p, torch.float64), 1.0, E.cuda_tensor(a, E.CD), st)
+    st.check()
+    return _host(out, like=a)
+
+
+# --------------------------------------------------------------------------
+# convolutional gridding (synthesis.py:451-503)
+
+def _table_and_groups(gcf, src, n, dtype):
+    nsrc = _src_cols(src, n)
+    ktab = E.KernelTable.from_gcf(gcf, nsrc, dtype)
+    kidx = None
+    if nsrc:
+        s = src.cpu().numpy() if isinstance(src, torch.Tensor) else numpy.asarray(src)
+        kidx = E.kernel_groups(tuple(gcf.shape[:nsrc]), s.reshape(n, nsrc), n)
+    return ktab, kidx
+
+
+def _grid_into(ktab, kidx, uvw, lam, shape, vis, prec, weight=None, out=None, status=None):
+    """Grid on the device; returns the device grid (c64 or c128)."""
+    mode = _lib.CG_PLAN_TILED if prec == "fp32" else _lib.CG_PLAN_GROUPS
+    plan = E.Plan(uvw, lam, shape, ktab, kidx, mode, status)
+    if prec == "fp32":
+        g = out if out is not None else torch.zeros(shape, dtype=E.CF, device="cuda")
+        if weight is None:
+            plan.grid(ktab, E.cuda_tensor(vis, E.CF), g)
+        else:
+            plan.grid_weighted(ktab, None if vis is None else E.cuda_tensor(vis, E.CF),
+                               E.cuda_tensor(weight, torch.float32), g)
+    else:
+        g = out if out is not None else torch.zeros(shape, dtype=E.CD, device="cuda")
+        v = E.cuda_tensor(vis, E.CD) if vis is not None else None
+        if weight is not None:
+            w = E.cuda_tensor(weight, torch.float64)
+            v = w.to(E.CD) if v is None else v * w
+        plan.grid_fp64(ktab, v, g)
+    return g, plan
+
+
+def _degrid_from(ktab, kidx, uvw, lam, guv, prec):
+    mode = _lib.CG_PLAN_TILED if prec == "fp32" else _lib.CG_PLAN_GROUPS
+    dt = E.CF if prec == "fp32" else E.CD
+    g = E.cuda_tensor(guv, dt)
+    plan = E.Plan(uvw, lam, tuple(g.shape), ktab, kidx, mode)
+    out = plan.degrid(ktab, g) if prec == "fp32" else plan.degrid_fp64(ktab, g)
+    plan.check()
+    return out
+
+
+def convgrid(gcf, a, p, src, v, precision=None):
+    """Convolutional gridding into a, in place (synthesis.py:464-481)."""
+    prec = _prec(precision)
+    n = _nrows(p)
+    ktab, kidx = _table_and_groups(gcf, src, n, E.CF if prec == "fp32" else E.CD)
+    shape = tuple(a.shape)
+    dev_inplace = _is_dev(a) and a.dtype == (E.CF if prec == "fp32" else E.CD)
+    g, plan = _grid_into(ktab, kidx, p, 1.0, shape, v, prec, out=a if dev_inplace else None)
+    plan.check()
+    if not dev_inplace:
+        if _is_dev(a):
+            a += g.to(a.dtype)
+        else:
+            a += g.cpu().numpy()
+
+
+def convdegrid(gcf, a, p, src=None, precision=None):
+    """Convolutional degridding (synthesis.py:484-503)."""
+    prec = _prec(precision)
+    n = _nrows(p)
+    ktab, kidx = _table_and_groups(gcf, src, n, E.CF if prec == "fp32" else E.CD)
+    return _host(_degrid_from(ktab, kidx, p, 1.0, a, prec), like=a)
+
+
+# --------------------------------------------------------------------------
+# ordering and weighting (synthesis.py:506-549, 831-852)
+
+def sort_vis_w(p, v=None):
+    """Sort by w; stable order for ties (synthesis.py:506-515)."""
+    zs = numpy.argsort(p[:, 2], kind="stable")
+    return (p[zs], v[zs]) if v is not None else p[zs]
+
+
+def slice_vis(step, uvw, v=None):
+    """Chunks of at most step rows (synthesis.py:518-532)."""
+    ii = range(0, len(uvw), step)
+    if v is None:
+        return [uvw[i:i + step] for i in ii]
+    return [(uvw[i:i + step], v[i:i + step]) for i in ii]
+
+
+def doweight(theta, lam, p, v):
+    """Uniform re-weighting v / count(cell), counted on the device (synthesis.py:535-549)."""
+    N = int(round(theta * lam))
+    assert N > 1
+    st = E.Status()
+    uvw = E.cuda_tensor(p, torch.float64)
+    vt = v if _is_dev(v) else numpy.asarray(v)
+    if numpy.iscomplexobj(vt) if not _is_dev(vt) else vt.is_complex():
+        w = E.weights(uvw, lam, N, st)
+        st.check()
+        out = E.cuda_tensor(vt, E.CD) * w
+    else:
+        out = E.weights(uvw, lam, N, st, E.cuda_tensor(vt, torch.float64))
+        st.check()
+    return _host(out, like=v)
+
+
+def mirror_uvw(uvw, vis):
+    """Flip baselines with v < 0 and conjugate their visibilities (synthesis.py:831-852)."""
+    u = E.cuda_tensor(uvw, torch.float64).clone()
+    cplx = torch.is_tensor(vis) and vis.is_complex() or (not torch.is_tensor(vis)
+                                                        and numpy.iscomplexobj(vis))
+    vt = E.cuda_tensor(vis, E.CD if not (_is_dev(vis) and vis.dtype == E.CF) else E.CF).clone() \
+        if cplx else E.cuda_tensor(vis, torch.float64).clone()
+    E.mirror_uvw(u, vt if cplx else None)
+    if _is_dev(uvw):
+        return u, vt
+    return _host(u), _host(vt, dtype=numpy.asarray(vis).dtype)
+
+
+def make_grid_hermitian(guv):
+    """guv + conj(mirrored guv), in place, on the device (synthesis.py:855-880)."""
+    if _is_dev(guv):
+        return E.make_hermitian(guv)
+    t = E.cuda_tensor(guv, E.CD)
+    E.make_hermitian(t)
+    guv[...] = t.cpu().numpy()
+    return guv
+
+
+# --------------------------------------------------------------------------
+# kernel specifications of the imaging drivers
+#
+# A "spec" turns (uvw, src) into a device kernel table and per-visibility
+# table rows.  All drivers share it, so imaging, PSF and predict on the same
+# visibilities reuse one plan.
+
+class _DeviceWKernels:
+    """Device-resident w-kernel tables keyed by their parameters (LRU).
+
+    Replaces pylru.FunctionCacheManager(w_kernel, size) of w_cache_imaging
+    (synthesis.py:785-788) with whole tables generated in one batched pass."""
+
+    def __init__(self, size=8):
+        self.size = size
+        self.tables = {}
+
+    def get(self, theta, wstep, kmin, kmax, NpixFF, NpixKern, Qpx, invert, dl, dm, T, dtype):
+        key = (float(theta), float(wstep), kmin, kmax, NpixFF, NpixKern, Qpx, bool(invert),
+               float(dl), float(dm), None if T is None else numpy.asarray(T, float).tobytes(),
+               dtype)
+        if key in self.tables:
+            t = self.tables.pop(key)
+            self.tables[key] = t
+            return t
+        ws = wstep * numpy.arange(kmin, kmax + 1).astype(numpy.float64)
+        t = E.w_kernels(theta, ws, NpixFF, NpixKern, Qpx, invert=invert, dl=dl, dm=dm, T=T,
+                        dtype=dtype)
+        self.tables[key] = t
+        while len(self.tables) > self.size:
+            self.tables.pop(next(iter(self.tables)))
+        return t
+
+
+W_KERNEL_TABLES = _DeviceWKernels()
+
+
+def _is_w_kernel(fn):
+    return fn is w_kernel
+
+
+def _wkw(kwargs):
+    kw = dict(kwargs)
+    NpixFF, NpixKern, Qpx = kw.pop("NpixFF"), kw.pop("NpixKern"), kw.pop("Qpx")
+    invert = kw.pop("invert", True)
+    dl, dm, T = kw.pop("dl", 0.0), kw.pop("dm", 0.0), kw.pop("T", None)
+    if kw:
+        raise TypeError("unexpected w_kernel arguments %s" % sorted(kw))
+    return NpixFF, NpixKern, Qpx, invert, dl, dm, T
+
+
+def _spec_w_cache(theta, uvw_t, uvw_host, src, wstep, kernel_cache, kernel_fn, kwargs, dtype):
+    n = uvw_t.shape[0]
+    nsrc = _src_cols(src, n)
+    if kernel_cache is None and _is_w_kernel(kernel_fn) and nsrc == 0:
+        st = E.Status()
+        kidx, kmin, kmax = E.w_bins(uvw_t, wstep, st)
+        st.check()
+        NpixFF, NpixKern, Qpx, invert, dl, dm, T = _wkw(kwargs)
+        t = W_KERNEL_TABLES.get(theta, wstep, kmin, kmax, NpixFF, NpixKern, Qpx, invert, dl,
+                                dm, T, dtype)
+        return E.KernelTable(t.reshape(-1), False, Qpx, NpixKern), kidx
+    # Generic kernel callables are host functions: call each once per distinct
+    # (wbin, *src_row) key, in first-use order, and upload the table.
+    fn = kernel_cache if kernel_cache is not None else kernel_fn
+    uh = uvw_host if uvw_host is not None else uvw_t.cpu().numpy()
+    wbin = wstep * numpy.round(uh[:, 2] / wstep)
+    s = numpy.zeros((n, 0)) if nsrc == 0 else numpy.asarray(
+        src.cpu().numpy() if isinstance(src, torch.Tensor) else src).reshape(n, nsrc)
+    keys = numpy.column_stack([wbin, s]) if nsrc else wbin[:, None]
+    _, first, inv = numpy.unique(keys, axis=0, return_index=True, return_inverse=True)
+    order = numpy.argsort(first)
+    rank = numpy.empty_like(order)
+    rank[order] = numpy.arange(len(order))
+    kerns = [numpy.asarray(fn(theta, wbin[first[k]], *s[first[k]], **kwargs)) for k in order]
+    table = numpy.array(kerns)
+    Q, S = table.shape[1], table.shape[-1]
+    return (E.KernelTable(E.cuda_tensor(table, dtype).reshape(-1), False, Q, S),
+            rank[inv.ravel()].astype(numpy.int32))
+
+
+def _spec_w_slice(theta, uvw_t, uvw_host, wstep, kernel_fn, kwargs, dtype):
+    uh = uvw_host if uvw_host is not None else uvw_t.cpu().numpy()
+    n = len(uh)
+    order = numpy.argsort(uh[:, 2], kind="stable")
+    nsl = (n + wstep - 1) // wstep
+    means = numpy.array([numpy.mean(uh[order[i:i + wstep], 2]) for i in range(0, n, wstep)])
+    kidx = numpy.empty(n, dtype=numpy.int32)
+    kidx[order] = numpy.arange(n) // wstep
+    if _is_w_kernel(kernel_fn):
+        NpixFF, NpixKern, Qpx, invert, dl, dm, T = _wkw(kwargs)
+        t = E.w_kernels(theta, means, NpixFF, NpixKern, Qpx, invert=invert, dl=dl, dm=dm, T=T,
+                        dtype=dtype)
+    else:
+        t = E.cuda_tensor(numpy.array([numpy.asarray(kernel_fn(theta, w, **kwargs))
+                                       for w in means]), dtype)
+    assert t.shape[0] == nsl
+    return E.KernelTable(t.reshape(-1), False, t.shape[1], t.shape[-1]), kidx
+
+
+def _grid_size(theta, lam):
+    N = int(round(theta * lam))
+    assert N > 1
+    return N
+
+
+# --------------------------------------------------------------------------
+# imaging / predict drivers (synthesis.py:552-679, 757-828, 883-927)
+
+def simple_imaging(theta, lam, uvw, src, vis):
+    """Boxcar imaging (synthesis.py:552-562)."""
+    N = _grid_size(theta, lam)
+    st = E.Status()
+    g = torch.zeros((N, N), dtype=E.CD, device="cuda")
+    E.grid_boxcar(E.cuda_tensor(uvw, torch.float64), lam, E.cuda_tensor(vis, E.CD), g, st)
+    st.check()
+    return _host(g, like=uvw)
+
+
+def simple_predict(theta, lam, uvw, src, guv):
+    """Boxcar predict (synthesis.py:565-580)."""
+    _grid_size(theta, lam)
+    st = E.Status()
+    out = E.degrid_boxcar(E.cuda_tensor(uvw, torch.float64), lam, E.cuda_tensor(guv, E.CD), st)
+    st.check()
+    return _host(out, like=uvw)
+
+
+def conv_imaging(theta, lam, uvw, src, vis, kv, precision=None):
+    """Convolve and grid with a user kernel (synthesis.py:583-598)."""
+    prec = _prec(precision)
+    N = _grid_size(theta, lam)
+    ktab, kidx = _table_and_groups(kv, src, _nrows(uvw), E.CF if prec == "fp32" else E.CD)
+    g, plan = _grid_into(ktab, kidx, uvw, lam, (N, N), vis, prec)
+    plan.check()
+    return _host(g, like=uvw)
+
+
+def conv_predict(theta, lam, uvw, src, guv, kv, precision=None):
+    """Convolutional predict (synthesis.py:600-613)."""
+    prec = _prec(precision)
+    ktab, kidx = _table_and_groups(kv, src, _nrows(uvw), E.CF if prec == "fp32" else E.CD)
+    return _host(_degrid_from(ktab, kidx, uvw, lam, guv, prec), like=uvw)
+
+
+def w_slice_imaging(theta, lam, uvw, src, vis, wstep=2000, kernel_fn=w_kernel, precision=None,
+                    **kwargs):
+    """w-sliced imaging (synthesis.py:616-644), with the reference's undefined names
+    (``p, v`` at :638) read as ``uvw, vis``.  All slices grid in one launch."""
+    prec = _prec(precision)
+    N = _grid_size(theta, lam)
+    uh = None if _is_dev(uvw) else numpy.asarray(uvw)
+    uvw_t = E.cuda_tensor(uvw, torch.float64)
+    ktab, kidx = _spec_w_slice(theta, uvw_t, uh, wstep, kernel_fn, kwargs,
+                               E.CF if prec == "fp32" else E.CD)
+    g, plan = _grid_into(ktab, kidx, uvw_t, lam, (N, N), vis, prec)
+    plan.check()
+    return _host(g, like=uvw)
+
+
+def w_slice_predict(theta, lam, uvw, src, guv, wstep=2000, kernel_fn=w_kernel, precision=None,
+                    **kwargs):
+    """w-sliced predict (synthesis.py:647-679), undefined ``p`` (:672) read as ``uvw``."""
+    prec = _prec(precision)
+    _grid_size(theta, lam)
+    uh = None if _is_dev(uvw) else numpy.asarray(uvw)
+    uvw_t = E.cuda_tensor(uvw, torch.float64)
+    ktab, kidx = _spec_w_slice(theta, uvw_t, uh, wstep, kernel_fn, kwargs,
+                               E.CF if prec == "fp32" else E.CD)
+    return _host(_degrid_from(ktab, kidx, uvw_t, lam, guv, prec), like=uvw)
+
+
+def w_cache_imaging(theta, lam, uvw, src, vis, wstep=2000, kernel_cache=None, kernel_fn=w_kernel,
+                    precision=None, **kwargs):
+    """w-projection with one kernel per w-bin (synthesis.py:757-796).
+
+    With the default kernel function the bins are found and the kernels
+    generated on the device, and every visibility grids in one persistent
+    launch; other kernel callables are evaluated once per distinct key."""
+    prec = _prec(precision)
+    N = int(round(theta * lam))
+    uh = None if _is_dev(uvw) else numpy.asarray(uvw)
+    uvw_t = E.cuda_tensor(uvw, torch.float64)
+    ktab, kidx = _spec_w_cache(theta, uvw_t, uh, src, wstep, kernel_cache, kernel_fn, kwargs,
+                               E.CF if prec == "fp32" else E.CD)
+    g, plan = _grid_into(ktab, kidx, uvw_t, lam, (N, N), vis, prec)
+    plan.check()
+    return _host(g, like=uvw)
+
+
+def w_cache_predict(theta, lam, uvw, src, guv, wstep=2000, kernel_cache=None, kernel_fn=w_kernel,
+                    precision=None, **kwargs):
+    """w-projection predict (synthesis.py:799-828), with the reference's undefined
+    ``nv``/``ixs`` (:823, :827) read as the number of rows and the row index."""
+    prec = _prec(precision)
+    uh = None if _is_dev(uvw) else numpy.asarray(uvw)
+    uvw_t = E.cuda_tensor(uvw, torch.float64)
+    ktab, kidx = _spec_w_cache(theta, uvw_t, uh, src, wstep, kernel_cache, kernel_fn, kwargs,
+                               E.CF if prec == "fp32" else E.CD)
+    return _host(_degrid_from(ktab, kidx, uvw_t, lam, guv, prec), like=uvw)
+
+
+def _device_spec(imgfn, theta, uvw_t, uvw_host, src, kwargs, dtype):
+    """(ktab, kidx) for one of this module's imaging/predict functions, or None."""
+    n = uvw_t.shape[0]
+    if imgfn in (conv_imaging, conv_predict):
+        return _table_and_groups(kwargs["kv"], src, n, dtype)
+    if imgfn in (w_cache_imaging, w_cache_predict):
+        kw = dict(kwargs)
+        wstep = kw.pop("wstep", 2000)
+        cache = kw.pop("kernel_cache", None)
+        fn = kw.pop("kernel_fn", w_kernel)
+        return _spec_w_cache(theta, uvw_t, uvw_host, src, wstep, cache, fn, kw, dtype)
+    if imgfn in (w_slice_imaging, w_slice_predict):
+        kw = dict(kwargs)
+        wstep = kw.pop("wstep", 2000)
+        fn = kw.pop("kernel_fn", w_kernel)
+        return _spec_w_slice(theta, uvw_t, uvw_host, wstep, fn, kw, dtype)
+    return None
+
+
+def do_imaging(theta, lam, uvw, src, vis, imgfn, **kwargs):
+    """Dirty image and PSF (synthesis.py:883-911).
+
+    For this module's imaging functions the whole chain runs on the device
+    with one plan shared by the image and the PSF pass."""
+    prec = _prec(kwargs.pop("precision", None))
+    n = len(vis)
+    if src is None:
+        src = numpy.ndarray((n, 0))
+    uvw_t = E.cuda_tensor(uvw, torch.float64).clone()
+    cplx = E.CF if prec == "fp32" else E.CD
+    vis_t = E.cuda_tensor(vis, E.CD).clone()
+    E.mirror_uvw(uvw_t, vis_t)
+    N = _grid_size(theta, lam)
+    st = E.Status()
+    wt = E.weights(uvw_t, lam, N, st)
+    st.check()
+    spec = None
+    if imgfn is not simple_imaging:
+        spec = _device_spec(imgfn, theta, uvw_t, None if _is_dev(uvw) else uvw_t.cpu().numpy(),
+                            src, kwargs, cplx)
+    if spec is None and imgfn is not simple_imaging:
+        # a caller-supplied imaging function: run it as the reference does
+        uh = uvw_t.cpu().numpy()
+        wh = wt.cpu().numpy()
+        vh = vis_t.cpu().numpy()
+        cdrt = numpy.asarray(imgfn(theta, lam, uh, src, wh * vh, **kwargs))
+        c = numpy.asarray(imgfn(theta, lam, uh, src, wh, **kwargs))
+        drt = numpy.real(ifft(make_grid_hermitian(cdrt)))
+        psf = numpy.real(ifft(make_grid_hermitian(c)))
+        pmax = psf.max()
+        assert pmax > 0.0
+        return drt / pmax, psf / pmax, pmax
+    if imgfn is simple_imaging:
+        g1 = torch.zeros((N, N), dtype=E.CD, device="cuda")
+        g2 = torch.zeros((N, N), dtype=E.CD, device="cuda")
+        E.grid_boxcar(uvw_t, lam, vis_t * wt, g1, st)
+        E.grid_boxcar(uvw_t, lam, wt.to(E.CD), g2, st)
+        st.check()
+        if prec == "fp32":
+            g1, g2 = g1.to(E.CF), g2.to(E.CF)
+    else:
+        ktab, kidx = spec
+        g1, plan = _grid_into(ktab, kidx, uvw_t, lam, (N, N), vis_t, prec, weight=wt)
+        g2, _ = _grid_into(ktab, kidx, uvw_t, lam, (N, N), None, prec, weight=wt) \
+            if prec == "fp64" else (None, None)
+        if prec == "fp32":
+            g2 = torch.zeros((N, N), dtype=E.CF, device="cuda")
+            plan.grid_weighted(ktab, None, wt.to(torch.float32), g2)
+        plan.check()
+    if prec == "fp32" and N % 2 == 0:
+        img, _ = E.image_from_grid(g1)
+        psf, pmax = E.image_from_grid(g2, want_max=True)
+        pm = float(pmax.item())
+        assert pm > 0.0
+        E.scale_image(img, pmax)
+        E.scale_image(psf, pmax)
+        return img.double().cpu().numpy(), psf.double().cpu().numpy(), pm
+    # complex128 (or odd-sized) images: hermitian + centred ifft + real part
+    g1, g2 = g1.to(E.CD), g2.to(E.CD)
+    for g in (g1, g2):
+        E.make_hermitian(g)
+        E.fft_(g, True)
+    drt, psf = g1.real.cpu().numpy(), g2.real.cpu().numpy()
+    pmax = psf.max()
+    assert pmax > 0.0
+    return drt / pmax, psf / pmax, pmax
+
+
+def do_predict(theta, lam, uvw, src, modelimage, predfn, **kwargs):
+    """Predict visibilities of a model image (synthesis.py:914-927)."""
+    prec = _prec(kwargs.pop("precision", None))
+    img = modelimage if _is_dev(modelimage) else numpy.asarray(modelimage)
+    ximage = E.cuda_tensor(img, E.CD)
+    E.fft_(ximage, False)
+    uvw_t = E.cuda_tensor(uvw, torch.float64)
+    if predfn is simple_predict:
+        st = E.Status()
+        out = E.degrid_boxcar(uvw_t, lam, ximage, st)
+        st.check()
+        return _host(out, like=uvw)
+    cplx = E.CF if prec == "fp32" else E.CD
+    spec = _device_spec(predfn, theta, uvw_t, None if _is_dev(uvw) else numpy.asarray(uvw),
+                        src, kwargs, cplx)
+    if spec is None:
+        return predfn(theta, lam, uvw, src, _host(ximage), **kwargs)
+    ktab, kidx = spec
+    return _host(_degrid_from(ktab, kidx, uvw_t, lam, ximage, prec), like=uvw)
+
+
+def sample_image(image, x, y):
+    """Bilinear sample relative to the image middle (synthesis.py:736-755)."""
+    x = x + image.shape[0] / 2
+    y = y + image.shape[1] / 2
+    ix = numpy.floor(x).astype(int)
+    dx = x - ix
+    iy = numpy.floor(y).astype(int)
+    dy = y - iy
+    return numpy.sum([image[iy, ix] * ((1 - dx) * (1 - dy)),
+                      image[iy, ix + 1] * (dx * (1 - dy)),
+                      image[iy + 1, ix] * ((1 - dx) * dy),
+                      image[iy + 1, ix + 1] * (dx * dy)], axis=0)

@@ -1,0 +1,222 @@
+/*
+ * crocodile_gb300 -- C ABI of the GB300 (sm_103a) convolutional gridding path.
+ *
+ * Each entry point replaces one function of crocodile's gridding path
+ * (crocodile/synthesis.py in the SKA-ScienceDataProcessor/crocodile
+ * reference); the replaced function is cited beside it.  All array
+ * arguments are DEVICE pointers owned by the caller unless stated
+ * otherwise; the library never frees caller memory.  Complex arrays are
+ * interleaved (re, im): "c64" = 2 x float32, "c128" = 2 x float64.
+ * Every call is ordered on the given stream (NULL = legacy default stream).
+ *
+ * Return value: CG_OK (0) or a negative CG_ERR_* code; cg_last_error()
+ * gives a message for the calling thread.  No exception crosses the ABI
+ * and no kernel traps: data errors found on the device (coordinates out of
+ * range, footprints outside the grid, bad kernel indices) are counted in a
+ * caller-visible status block and every later kernel of the same call
+ * leaves its outputs untouched.  cg_status_check() reads the block.
+ */
+#ifndef CROCODILE_GB300_H
+#define CROCODILE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *cg_stream_t; /* == cudaStream_t */
+
+#define CG_OK 0
+#define CG_ERR_ARG (-1)       /* bad argument: shape, null pointer, unsupported size */
+#define CG_ERR_RANGE (-2)     /* p outside [-0.5, 0.5): AssertionError at synthesis.py:432 */
+#define CG_ERR_BOUNDS (-3)    /* footprint outside the grid: ValueError at synthesis.py:480 */
+#define CG_ERR_INDEX (-4)     /* kernel group / weighting cell out of range: IndexError */
+#define CG_ERR_CUDA (-5)      /* CUDA or cuFFT error */
+#define CG_ERR_WORKSPACE (-6) /* workspace smaller than the *_workspace_bytes query */
+#define CG_ERR_TIMEOUT (-7)   /* a bounded device wait gave up */
+
+/* Status block: CG_STATUS_WORDS int32 counters in device memory, zeroed by
+ * cg_status_reset.  [0] range errors, [1] footprint errors, [2] index
+ * errors, [3] timeouts. */
+#define CG_STATUS_WORDS 4
+
+const char *cg_last_error(void);
+int cg_version(void);
+int cg_status_reset(int32_t *d_status, cg_stream_t stream);
+/* Synchronises the stream, copies the block to counts_out (may be NULL)
+ * and returns the CG_ERR_* code of the first non-zero counter. */
+int cg_status_check(const int32_t *d_status, int32_t *counts_out, cg_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Visibility coordinates.  Throughout, visibility i has coordinates
+ * p = (uvw[i*stride+0], uvw[i*stride+1]) / lam as a fraction of the grid
+ * (pass lam = 1 for coordinates already in grid fractions). */
+
+/* frac_coords (synthesis.py:419-449): x, xf from p[:,0] over the width W,
+ * y, yf from p[:,1] over the height H; bit-exact with numpy (FP64, IEEE
+ * rounding, half-to-even, floor division).  Outputs are int32 device
+ * arrays of length n.  Range errors are counted in d_status[0]. */
+int cg_frac_coords(const double *uvw, int64_t stride, double lam, int64_t n,
+                   int H, int W, int Q, int32_t *x, int32_t *xf, int32_t *y,
+                   int32_t *yf, int32_t *d_status, cg_stream_t stream);
+
+/* w bins of w_cache_imaging / w_cache_predict (synthesis.py:793, 825):
+ * k_i = round(w_i / wstep) (half-to-even; w = uvw[i*stride+2], stride >= 3).
+ * Writes kidx[i] = k_i - min(k) (a kernel-table row), stores (min k, max k)
+ * in h_minmax (host, 2 ints) and synchronises the stream.  d_minmax is a
+ * 2-int device scratch.  The kernel of row j is the one for
+ * w = wstep * (min k + j). */
+int cg_w_bins(const double *uvw, int64_t stride, int64_t n, double wstep,
+              int32_t *kidx, int32_t *d_minmax, int32_t *h_minmax,
+              int32_t *d_status, cg_stream_t stream);
+/* Same bins against a kernel table that already covers k in [kmin, kmin+nk):
+ * kidx[i] = k_i - kmin, bins outside the table are index errors.  Fully
+ * stream-ordered (no synchronisation), for steady-state imaging loops. */
+int cg_w_bins_fixed(const double *uvw, int64_t stride, int64_t n, double wstep,
+                    int kmin, int nk, int32_t *kidx, int32_t *d_status,
+                    cg_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Kernel (GCF) tables, as built by make_gcf (synthesis.py:451-461):
+ *   sep = 1: [G, Q, S] table, footprint = outer(K[g,yf], K[g,xf])
+ *   sep = 0: [G, Q, Q, S, S] table, footprint = K[g, yf, xf]
+ * G counts the flattened leading "src" dimensions; the per-visibility
+ * group index kidx (int32, may be NULL for G = 1) selects one. */
+typedef struct {
+  int sep;
+  int Q;
+  int S;
+  int G;
+} cg_kernel_desc;
+
+/* A plan holds the visibilities' bit-exact cell assignment, their order
+ * (sorted into grid tiles, or into kernel groups for the plain FP64 form)
+ * and the work list of the gridding kernels.  It lives in a caller-owned
+ * workspace and is reused by any number of grid/degrid calls on the same
+ * coordinates (imaging and its PSF, predict, the adjoint pair). */
+typedef struct cg_plan cg_plan;
+
+#define CG_PLAN_TILED 0  /* FP32 tiled gridder/degridder (cg_grid, cg_degrid) */
+#define CG_PLAN_GROUPS 1 /* plain FP64 form, one launch per kernel group */
+
+size_t cg_plan_workspace_bytes(int mode, int64_t n, int H, int W,
+                               const cg_kernel_desc *kd);
+/* Builds the plan on `stream`.  CG_PLAN_GROUPS synchronises once to learn
+ * the group sizes.  A data error leaves the plan marked failed (see
+ * cg_status_check); grid/degrid then do nothing. */
+int cg_plan_create(cg_plan **plan, int mode, const cg_kernel_desc *kd, int H,
+                   int W, const double *uvw, int64_t stride, double lam,
+                   const int32_t *kidx, int64_t n, void *workspace,
+                   size_t workspace_bytes, int32_t *d_status,
+                   cg_stream_t stream);
+int cg_plan_destroy(cg_plan *plan);
+/* Tile edge (cells) and number of work items upper bound, for reports. */
+int cg_plan_info(const cg_plan *plan, int64_t *info_out /* [4] */);
+
+/* convgrid (synthesis.py:464-481): grid[H,W] (c64) += K * vis (c64).
+ * FP32 products and accumulation; persistent tiled kernel; CG_PLAN_TILED. */
+int cg_grid(const cg_plan *plan, const void *ktab_c64, const void *vis_c64,
+            void *grid_c64, cg_stream_t stream);
+/* Same, with the visibilities multiplied by a real per-visibility weight
+ * (do_imaging's wt * vis, synthesis.py:901-906); vis_c64 may be NULL for
+ * the PSF pass (vis = 1). */
+int cg_grid_weighted(const cg_plan *plan, const void *ktab_c64,
+                     const void *vis_c64, const float *weight,
+                     void *grid_c64, cg_stream_t stream);
+/* convdegrid (synthesis.py:484-503): out[i] = sum(grid[footprint] * K). */
+int cg_degrid(const cg_plan *plan, const void *ktab_c64, const void *grid_c64,
+              void *vis_out_c64, cg_stream_t stream);
+/* Plain FP64 form of the same two operations (c128 data, FP64 atomics,
+ * one launch per kernel group): the accuracy and speed comparator.
+ * Needs a CG_PLAN_GROUPS plan. */
+int cg_grid_fp64(const cg_plan *plan, const void *ktab_c128,
+                 const void *vis_c128, void *grid_c128, cg_stream_t stream);
+int cg_degrid_fp64(const cg_plan *plan, const void *ktab_c128,
+                   const void *grid_c128, void *vis_out_c128,
+                   cg_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Boxcar gridding, grid/degrid (synthesis.py:389-416): nearest cell
+ * N//2 + floor(0.5 + N*p), N = H (as the reference uses a.shape[0]).
+ * Coordinates not below 0.5 in any of the first min(stride, 3) columns are
+ * range errors (the reference asserts max(p) < 0.5 over u, v and w).
+ * c128 data, FP64. */
+int cg_grid_boxcar(const double *uvw, int64_t stride, double lam, int64_t n,
+                   const void *vis_c128, void *grid_c128, int H, int W,
+                   int32_t *d_status, cg_stream_t stream);
+int cg_degrid_boxcar(const double *uvw, int64_t stride, double lam, int64_t n,
+                     const void *grid_c128, void *vis_out_c128, int H, int W,
+                     int32_t *d_status, cg_stream_t stream);
+
+/* doweight (synthesis.py:535-549): w_out[i] = v_in[i] / count(cell(i)) on
+ * an N x N grid (v_in NULL = ones).  counts is an int32 N*N scratch array. */
+int cg_weights(const double *uvw, int64_t stride, double lam, int64_t n,
+               int N, const double *v_in, double *w_out, int32_t *counts,
+               int32_t *d_status, cg_stream_t stream);
+
+/* mirror_uvw (synthesis.py:831-852), in place: rows with v < 0 become
+ * (-u, -v, -w) and their visibility is conjugated (vis may be NULL). */
+int cg_mirror_uvw(double *uvw, int64_t stride, int64_t n, void *vis,
+                  int vis_is_c64, cg_stream_t stream);
+
+/* make_grid_hermitian (synthesis.py:855-880), in place. */
+int cg_make_hermitian(void *grid, int H, int W, int is_c64,
+                      cg_stream_t stream);
+
+/* fft / ifft (synthesis.py:83-106): centred 2-D transform of `batch`
+ * H x W arrays (H = 1: 1-D), in place; the inverse includes 1/(H*W).
+ * Grids with H and W even need no workspace; otherwise workspace must hold
+ * one array of the same size. */
+int cg_fft(void *data, int batch, int H, int W, int is_c64, int inverse,
+           void *workspace, cg_stream_t stream);
+
+/* Dirty image / PSF of a grid (synthesis.py:904-907): image = Re(ifft(
+ * make_grid_hermitian(grid))), written as float32 H x W; the grid is
+ * consumed (overwritten).  If max_out is not NULL the image maximum is
+ * stored there (float, device).  Even H and W only. */
+int cg_image_from_grid(void *grid_c64, int H, int W, float *image_out,
+                       float *max_out, cg_stream_t stream);
+/* image *= 1 / *d_scale (do_imaging's normalisation, synthesis.py:909-911) */
+int cg_scale_image(float *image, int64_t count, const float *d_scale,
+                   cg_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Kernel generation (FP64 arithmetic; outputs c64 or c128). */
+
+/* kernel_oversample (synthesis.py:330-354) of `batch` far fields ff
+ * (c128, batch x N0 (ndim 1) or batch x N0 x N0 (ndim 2)) into
+ * batch x [Q, s] or batch x [Q, Q, s, s]. */
+size_t cg_kernel_oversample_workspace_bytes(int batch, int ndim, int N0, int Q);
+int cg_kernel_oversample(const void *ff_c128, int batch, int ndim, int N0,
+                         int Q, int s, void *out, int out_c64, void *workspace,
+                         size_t workspace_bytes, cg_stream_t stream);
+
+/* w_kernel (synthesis.py:357-377) for nw w values (host array): each
+ * output is [Q, Q, S, S].  T (host, row-major 2x2) may be NULL. */
+size_t cg_w_kernels_workspace_bytes(int nw, int NpixFF, int Q);
+int cg_w_kernels(double theta, const double *w_host, int nw, int NpixFF,
+                 int S, int Q, int invert, double dl, double dm,
+                 const double *T_host, void *out, int out_c64,
+                 void *workspace, size_t workspace_bytes, int32_t *d_status,
+                 cg_stream_t stream);
+
+/* aw_kernel_fn (synthesis.py:701-734): for each of nk AW kernels k,
+ *   akern = convolve2d(A[a1[k]], A[a2[k]], 'same')        (SA x SA)
+ *   out[k, yf, xf] = convolve2d(akern, W[wi[k], yf, xf], 'same')
+ * A: [nA, SA, SA] c128, W: [nW, Q, Q, S, S] c128, out: [nk, Q, Q, SA, SA]
+ * c64 or c128.  a1, a2, wi: int32 device arrays.  A kernels are combined
+ * in FP64; the Q*Q sub-kernel convolutions use FP32 products and sums. */
+size_t cg_aw_kernels_workspace_bytes(int nk, int SA);
+int cg_aw_kernels(const void *A_c128, int nA, int SA, const void *W_c128,
+                  int nW, int Q, int S, const int32_t *a1, const int32_t *a2,
+                  const int32_t *wi, int nk, void *out, int out_c64,
+                  void *workspace, size_t workspace_bytes, int32_t *d_status,
+                  cg_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CROCODILE_GB300_H */

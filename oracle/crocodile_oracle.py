@@ -1,0 +1,535 @@
+"""CPU oracle of crocodile's convolutional gridding path -- TEST INFRASTRUCTURE ONLY.
+
+A numpy (complex128) restatement of ``crocodile/synthesis.py`` written for
+this project.  It is the parity checker for the CUDA product: only
+``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+may import it.  The product never routes through it.
+
+Parity pin: ``tests/golden/make_golden.py`` imports the real reference
+(Python, importable in the build container) and stores its outputs as
+``tests/golden/*.npz``; ``tests/test_oracle_golden.py`` checks every
+function here against those fixtures and against the C golden table of
+``examples/grid/test_recombine.c:378-412``.
+
+Each function cites the reference lines whose behaviour it restates.  Three
+reference functions are broken as shipped (NameError) and are restated with
+the minimal fix, documented at each one: ``w_slice_imaging``,
+``w_slice_predict``, ``w_cache_predict``.
+
+Vectorisation note: ``convgrid`` here adds the S x S footprints with
+``numpy.add.at`` in visibility order, which performs exactly the same
+sequence of complex128 additions per grid cell as the reference's per-row
+Python loop (``synthesis.py:479-481``), so grids agree bit for bit.
+"""
+
+import numpy
+import scipy.special
+import scipy.signal
+
+
+# --------------------------------------------------------------------------
+# coordinates and FFT conventions (synthesis.py:38-106)
+
+def coordinateBounds(N):
+    """Lowest/highest coordinate of an N grid (synthesis.py:38-55)."""
+    if N % 2 == 0:
+        return -0.5, 0.5 * (N - 2) / N
+    return -0.5 * (N - 1) / N, 0.5 * (N - 1) / N
+
+
+def coordinates(N):
+    """1-D coordinates, zero at N//2, step 1/N (synthesis.py:57-63)."""
+    lo = -(N // 2)
+    return numpy.arange(lo, lo + N) / N
+
+
+def coordinates2(N):
+    """(x, y) 2-D coordinate grids, x varying along axis 1 (synthesis.py:66-80)."""
+    c = numpy.arange(-(N // 2), -(N // 2) + N)
+    cy, cx = numpy.meshgrid(c, c, indexing="ij")
+    return numpy.array([cx, cy]) / N
+
+
+def fft(a):
+    """Centred forward FFT: fftshift(fft(ifftshift(a))) (synthesis.py:83-93)."""
+    if a.ndim == 1:
+        return numpy.fft.fftshift(numpy.fft.fft(numpy.fft.ifftshift(a)))
+    assert a.ndim == 2, "Unsupported image shape for FFT!"
+    return numpy.fft.fftshift(numpy.fft.fft2(numpy.fft.ifftshift(a)))
+
+
+def ifft(a):
+    """Centred inverse FFT incl. 1/N normalisation (synthesis.py:96-106)."""
+    if a.ndim == 1:
+        return numpy.fft.fftshift(numpy.fft.ifft(numpy.fft.ifftshift(a)))
+    assert a.ndim == 2, "Unsupported grid shape for iFFT!"
+    return numpy.fft.fftshift(numpy.fft.ifft2(numpy.fft.ifftshift(a)))
+
+
+# --------------------------------------------------------------------------
+# padding / extraction (synthesis.py:109-197)
+
+def pad_mid(ff, N):
+    """Zero-pad a far field to N (per axis) around N//2 (synthesis.py:109-129)."""
+    N0 = ff.shape[0]
+    if N == N0:
+        return ff
+    assert N > N0
+    before = N // 2 - N0 // 2
+    after = (N + 1) // 2 - (N0 + 1) // 2
+    if ff.ndim == 2:
+        assert ff.shape[1] == N0
+        return numpy.pad(ff, [(before, after)] * 2, mode="constant")
+    return numpy.pad(ff, [(before, after)], mode="constant")
+
+
+def extract_mid(a, N):
+    """Centre crop of size N around shape//2 (synthesis.py:131-158)."""
+    assert N <= a.shape[0]
+    h = N // 2
+    odd = N % 2
+    cx = a.shape[0] // 2
+    if a.ndim == 2:
+        assert N <= a.shape[1]
+        cy = a.shape[1] // 2
+        return a[cx - h:cx + h + odd, cy - h:cy + h + odd]
+    assert a.ndim == 1, "Unsupported grid shape for extract_mid!"
+    return a[cx - h:cx + h + odd]
+
+
+def extract_oversampled(a, Qpx, N):
+    """Every Qpx-th sample from offset Na//2 - Qpx*(N//2) + f (synthesis.py:160-197)."""
+    Na = a.shape[0]
+    base = Na // 2 - Qpx * (N // 2)
+    taps = Qpx * numpy.arange(N)
+    if a.ndim == 1:
+        out = numpy.empty((Qpx, N), dtype=complex)
+        for f in range(Qpx):
+            out[f] = a[base + f + taps]
+        return out
+    assert a.ndim == 2, "Unsupported grid shape for extract_oversampled!"
+    out = numpy.empty((Qpx, Qpx, N, N), dtype=complex)
+    for fy in range(Qpx):
+        rows = base + fy + taps
+        for fx in range(Qpx):
+            cols = base + fx + taps
+            out[fy, fx] = a[numpy.ix_(rows, cols)]
+    return out
+
+
+# --------------------------------------------------------------------------
+# kernels (synthesis.py:199-377, 682-734)
+
+def anti_aliasing_function(shape, m, c):
+    """PSWF pro_ang1(m, m, c, (2 - 1/N/4) * coordinates(N)) (synthesis.py:199-218)."""
+    if numpy.ndim(shape) == 0:
+        mult = 2 - 1 / shape / 4
+        return scipy.special.pro_ang1(m, m, c, mult * coordinates(shape))[0]
+    return numpy.outer(anti_aliasing_function(shape[0], m, c),
+                       anti_aliasing_function(shape[1], m, c))
+
+
+def kernel_coordinates(N, theta, dl=0, dm=0, T=None):
+    """(l, m) of an N far field, optionally transformed by T and shifted (synthesis.py:250-270)."""
+    l, m = coordinates2(N) * theta
+    if T is not None:
+        l, m = T[0, 0] * l + T[1, 0] * m, T[0, 1] * l + T[1, 1] * m
+    return l + dl, m + dm
+
+
+def w_kernel_function(l, m, w):
+    """Fresnel pattern exp(2 pi i w (1 - sqrt(1 - l^2 - m^2))) (synthesis.py:273-293)."""
+    r2 = l ** 2 + m ** 2
+    assert numpy.all(r2 < 1.0), "Error in image coordinate system"
+    ph = 1 - numpy.sqrt(1.0 - r2)
+    return numpy.exp(2j * numpy.pi * w * ph)
+
+
+def kernel_oversample(ff, Qpx, s=None):
+    """Oversampled GCF: extract_oversampled(fft(pad_mid(ff, N*Qpx)), Qpx, s) (synthesis.py:330-354)."""
+    N = ff.shape[0]
+    if s is None:
+        s = N
+    return extract_oversampled(fft(pad_mid(ff, N * Qpx)), Qpx, s)
+
+
+def w_kernel(theta, w, NpixFF, NpixKern, Qpx, invert=True, **kwargs):
+    """[Qpx,Qpx,S,S] w-kernel, inverted for imaging by default (synthesis.py:357-377)."""
+    assert NpixFF > NpixKern or (NpixFF == NpixKern and Qpx == 1)
+    l, m = kernel_coordinates(NpixFF, theta, **kwargs)
+    kern = w_kernel_function(l, m, w)
+    if invert:
+        kern = 1 / kern
+    return kernel_oversample(kern, Qpx, NpixKern)
+
+
+def w_conj_kernel_fn(kernel_fn):
+    """K(-w) = conj(K(w)) wrapper (synthesis.py:682-699)."""
+    def fn(theta, w, *args, **kw):
+        if w < 0:
+            return numpy.conj(kernel_fn(theta, -w, *args, **kw))
+        return kernel_fn(theta, w, *args, **kw)
+    return fn
+
+
+def aw_kernel_fn(a_kernel_fn, w_kernel_fn=w_kernel):
+    """AW kernel = (A1 conv A2) conv W[yf,xf], 'same' crops (synthesis.py:701-734)."""
+    def fn(theta, w, a1, a2, *src):
+        akern = scipy.signal.convolve2d(a_kernel_fn(theta, a1, *src),
+                                        a_kernel_fn(theta, a2, *src), mode="same")
+        wkern = w_kernel_fn(theta, w)
+        return numpy.array([[scipy.signal.convolve2d(akern, wk, mode="same")
+                             for wk in row] for row in wkern])
+    return fn
+
+
+# --------------------------------------------------------------------------
+# coordinates of visibilities (synthesis.py:419-449)
+
+def frac_coord(N, Qpx, p):
+    """Whole and fractional (1/Qpx) grid coordinate, banker's rounding (synthesis.py:419-435)."""
+    p = numpy.asarray(p)
+    assert (p >= -0.5).all() and (p < 0.5).all()
+    x = N // 2 + p * N
+    fx = numpy.around(-x * Qpx).astype(int)
+    return -(fx // Qpx), fx % Qpx
+
+
+def frac_coords(shape, Qpx, p):
+    """x from p[:,0] over the width, y from p[:,1] over the height (synthesis.py:438-449)."""
+    h, w = shape
+    x, xf = frac_coord(w, Qpx, p[:, 0])
+    y, yf = frac_coord(h, Qpx, p[:, 1])
+    return x, xf, y, yf
+
+
+# --------------------------------------------------------------------------
+# boxcar gridding (synthesis.py:389-416)
+
+def grid(a, p, v):
+    """Nearest-cell gridding N//2 + floor(0.5 + N p) (synthesis.py:389-401)."""
+    assert numpy.max(p) < 0.5
+    N = a.shape[0]
+    xy = N // 2 + numpy.floor(0.5 + N * p[:, 0:2]).astype(int)
+    numpy.add.at(a, (xy[:, 1], xy[:, 0]), v)
+
+
+def degrid(a, p):
+    """Nearest-cell degridding (synthesis.py:404-416)."""
+    assert numpy.max(p) < 0.5
+    N = a.shape[0]
+    xy = N // 2 + numpy.floor(0.5 + p[:, 0:2] * N).astype(int)
+    return a[xy[:, 1], xy[:, 0]]
+
+
+# --------------------------------------------------------------------------
+# convolutional gridding (synthesis.py:451-503)
+
+def gcf_layout(gcf, nsrc):
+    """(separable?, Qpx, S) from the kernel rank vs the src columns (synthesis.py:451-461)."""
+    extra = gcf.ndim - nsrc
+    if extra == 2:
+        return True, gcf.shape[-2], gcf.shape[-1]
+    if extra == 4:
+        assert gcf.shape[-1] == gcf.shape[-2], "non-square kernels are not supported"
+        return False, gcf.shape[-3], gcf.shape[-1]
+    raise AssertionError("kernel rank does not match the src columns")
+
+
+def kernel_groups(gcf, src, n):
+    """Flat kernel-group index of each row of src into gcf's leading dims."""
+    src = numpy.zeros((n, 0)) if src is None else numpy.asarray(src)
+    lead = gcf.shape[:src.shape[1]]
+    if src.shape[1] == 0:
+        return src, numpy.zeros(n, dtype=numpy.int64)
+    idx = src.astype(numpy.int64)
+    for k, d in enumerate(lead):
+        col = idx[:, k]
+        if ((col < -d) | (col >= d)).any():
+            raise IndexError("src column %d out of range for kernel dimension %d" % (k, d))
+        idx[:, k] = numpy.where(col < 0, col + d, col)
+    return src, numpy.ravel_multi_index(tuple(idx.T), lead)
+
+
+def _footprints(shape, S, x, y):
+    x0 = x - S // 2
+    y0 = y - S // 2
+    bad = (x0 < 0) | (y0 < 0) | (x0 + S > shape[1]) | (y0 + S > shape[0])
+    if bad.any():
+        raise ValueError("%d visibilities have footprints outside the %dx%d grid"
+                         % (int(bad.sum()), shape[0], shape[1]))
+    return x0, y0
+
+
+def _kernel_block(kt, sep, g, xf, yf):
+    if sep:
+        return kt[g, yf][:, :, None] * kt[g, xf][:, None, :]
+    return kt[g, yf, xf]
+
+
+def convgrid_indexed(kt, sep, a, x, xf, y, yf, g, v, chunk=1 << 14):
+    """a[y-S//2 : y+(S+1)//2, x-S//2 : x+(S+1)//2] += K[g,yf,xf] * v, in visibility order.
+
+    kt is the kernel table flattened to [G, Q, (Q,) S(, S)].  Restates the
+    loop of synthesis.py:479-481.
+    """
+    S = kt.shape[-1]
+    x0, y0 = _footprints(a.shape, S, x, y)
+    taps = numpy.arange(S)
+    for s in range(0, len(x), chunk):
+        e = s + chunk
+        vals = _kernel_block(kt, sep, g[s:e], xf[s:e], yf[s:e]) * v[s:e, None, None]
+        iy = y0[s:e, None, None] + taps[None, :, None]
+        ix = x0[s:e, None, None] + taps[None, None, :]
+        numpy.add.at(a, (iy, ix), vals)
+
+
+def convdegrid_indexed(kt, sep, a, x, xf, y, yf, g, chunk=1 << 14):
+    """sum(a[footprint] * K[g,yf,xf]) per visibility (restates synthesis.py:500-503)."""
+    S = kt.shape[-1]
+    x0, y0 = _footprints(a.shape, S, x, y)
+    taps = numpy.arange(S)
+    out = numpy.empty(len(x), dtype=complex)
+    for s in range(0, len(x), chunk):
+        e = s + chunk
+        iy = y0[s:e, None, None] + taps[None, :, None]
+        ix = x0[s:e, None, None] + taps[None, None, :]
+        prod = a[iy, ix] * _kernel_block(kt, sep, g[s:e], xf[s:e], yf[s:e])
+        out[s:e] = prod.reshape(prod.shape[0], -1).sum(axis=1)
+    return out
+
+
+def _flat_table(gcf, nsrc):
+    sep, Q, S = gcf_layout(gcf, nsrc)
+    tail = (Q, S) if sep else (Q, Q, S, S)
+    return gcf.reshape((-1,) + tail), sep, Q
+
+
+def convgrid(gcf, a, p, src, v):
+    """Convolutional gridding into a, in place (synthesis.py:464-481)."""
+    n = p.shape[0]
+    src, g = kernel_groups(gcf, src, n)
+    kt, sep, Q = _flat_table(gcf, src.shape[1])
+    x, xf, y, yf = frac_coords(a.shape, Q, p)
+    convgrid_indexed(kt, sep, a, x, xf, y, yf, g, numpy.asarray(v))
+
+
+def convdegrid(gcf, a, p, src=None):
+    """Convolutional degridding (synthesis.py:484-503)."""
+    n = p.shape[0]
+    src, g = kernel_groups(gcf, src, n)
+    kt, sep, Q = _flat_table(gcf, src.shape[1])
+    x, xf, y, yf = frac_coords(a.shape, Q, p)
+    return convdegrid_indexed(kt, sep, a, x, xf, y, yf, g)
+
+
+# --------------------------------------------------------------------------
+# ordering and weighting (synthesis.py:506-549, 831-852)
+
+def sort_vis_w(p, v=None):
+    """Order by w (stable argsort; the reference's default sort ties arbitrarily) (synthesis.py:506-515)."""
+    zs = numpy.argsort(p[:, 2], kind="stable")
+    return (p[zs], v[zs]) if v is not None else p[zs]
+
+
+def slice_vis(step, uvw, v=None):
+    """Fixed-size chunks (synthesis.py:518-532)."""
+    starts = range(0, len(uvw), step)
+    if v is None:
+        return [uvw[i:i + step] for i in starts]
+    return [(uvw[i:i + step], v[i:i + step]) for i in starts]
+
+
+def doweight(theta, lam, p, v):
+    """Uniform weighting: v / count(cell) on an N = round(theta*lam) grid (synthesis.py:535-549)."""
+    N = int(round(theta * lam))
+    assert N > 1
+    x, _, y, _ = frac_coords((N, N), 1, p / lam)
+    if ((x >= N) | (y >= N)).any():
+        raise IndexError("visibility falls outside the weighting grid")
+    counts = numpy.zeros((N, N))
+    numpy.add.at(counts, (x, y), 1)
+    return v / counts[x, y]
+
+
+def mirror_uvw(uvw, vis):
+    """Flip rows with v < 0 to (-uvw, conj(vis)) (synthesis.py:831-852)."""
+    flip = uvw[:, 1] < 0
+    uvw = numpy.copy(uvw)
+    vis = numpy.copy(vis)
+    uvw[flip] = -uvw[flip]
+    vis[flip] = numpy.conj(vis[flip])
+    return uvw, vis
+
+
+def make_grid_hermitian(guv):
+    """guv + conj(mirror(guv)), mirrored on the zero point (synthesis.py:855-880).
+
+    Out-of-place right-hand side, as numpy buffers the overlapping operands
+    of the reference's in-place update."""
+    if guv.shape[0] % 2 == 0:
+        guv[1:, 1:] += numpy.conj(guv[:0:-1, :0:-1]).copy()
+    else:
+        guv += numpy.conj(guv[::-1, ::-1]).copy()
+    return guv
+
+
+# --------------------------------------------------------------------------
+# imaging / predict drivers (synthesis.py:552-679, 757-828, 883-927)
+
+def grid_size(theta, lam):
+    N = int(round(theta * lam))
+    assert N > 1
+    return N
+
+
+def simple_imaging(theta, lam, uvw, src, vis):
+    """Boxcar imaging (synthesis.py:552-562)."""
+    N = grid_size(theta, lam)
+    guv = numpy.zeros([N, N], dtype=complex)
+    grid(guv, uvw / lam, vis)
+    return guv
+
+
+def simple_predict(theta, lam, uvw, src, guv):
+    """Boxcar predict (synthesis.py:565-580)."""
+    grid_size(theta, lam)
+    return degrid(guv, uvw / lam)
+
+
+def conv_imaging(theta, lam, uvw, src, vis, kv):
+    """Convolutional imaging (synthesis.py:583-598)."""
+    N = grid_size(theta, lam)
+    guv = numpy.zeros([N, N], dtype=complex)
+    convgrid(kv, guv, uvw / lam, src, vis)
+    return guv
+
+
+def conv_predict(theta, lam, uvw, src, guv, kv):
+    """Convolutional predict (synthesis.py:600-613)."""
+    return convdegrid(kv, guv, uvw / lam, src)
+
+
+def w_slice_imaging(theta, lam, uvw, src, vis, wstep=2000, kernel_fn=w_kernel, **kwargs):
+    """w-sliced imaging (synthesis.py:616-644).
+
+    Minimal fix: the reference sorts undefined names ``p, v`` (:638); this
+    sorts ``uvw, vis``.  ``src`` is ignored per slice as in the reference's
+    kernel call (``kernel_fn(theta, w, **kwargs)``, :642) and convgrid gets
+    ``None`` (the reference passes the full ``src``, which only works when it
+    has no columns)."""
+    N = grid_size(theta, lam)
+    guv = numpy.zeros([N, N], dtype=complex)
+    for ps, vs in slice_vis(wstep, *sort_vis_w(uvw, vis)):
+        wg = kernel_fn(theta, numpy.mean(ps[:, 2]), **kwargs)
+        convgrid(wg, guv, ps / lam, None, vs)
+    return guv
+
+
+def w_slice_predict(theta, lam, uvw, src, guv, wstep=2000, kernel_fn=w_kernel, **kwargs):
+    """w-sliced predict (synthesis.py:647-679).  Minimal fix: ``p`` -> ``uvw`` (:672-673)."""
+    grid_size(theta, lam)
+    nv = len(uvw)
+    v = numpy.ndarray(nv, dtype=complex)
+    for ps, ixs in slice_vis(wstep, *sort_vis_w(uvw, numpy.arange(nv))):
+        wg = kernel_fn(theta, numpy.mean(ps[:, 2]), **kwargs)
+        v[ixs] = convdegrid(wg, guv, ps / lam)
+    return v
+
+
+def _w_cache_table(theta, uvw, src, wstep, kernel_cache, kernel_fn, kwargs):
+    """Kernel table over the distinct (wbin, *src_row) keys, in first-use order,
+    and the per-visibility table index.  wbin = wstep * round(w / wstep)
+    (synthesis.py:793)."""
+    if kernel_cache is None:
+        kernel_cache = kernel_fn
+    src = numpy.zeros((len(uvw), 0)) if src is None else numpy.asarray(src)
+    wbin = wstep * numpy.round(uvw[:, 2] / wstep)
+    keys = numpy.column_stack([wbin, src]) if src.shape[1] else wbin[:, None]
+    uniq, first, inv = numpy.unique(keys, axis=0, return_index=True, return_inverse=True)
+    order = numpy.argsort(first)
+    rank = numpy.empty_like(order)
+    rank[order] = numpy.arange(len(order))
+    kerns = []
+    for k in order:
+        i = first[k]
+        kerns.append(numpy.asarray(kernel_cache(theta, wbin[i], *src[i], **kwargs)))
+    return numpy.array(kerns), rank[inv.ravel()]
+
+
+def w_cache_imaging(theta, lam, uvw, src, vis, wstep=2000, kernel_cache=None,
+                    kernel_fn=w_kernel, **kwargs):
+    """w-projection with one kernel per w-bin (and src key) (synthesis.py:757-796).
+
+    The reference grids one visibility at a time; here the kernels of all
+    keys are gathered first and one convgrid pass runs in visibility order,
+    which performs the same additions in the same order."""
+    N = int(round(theta * lam))
+    guv = numpy.zeros([N, N], dtype=complex)
+    kt, g = _w_cache_table(theta, uvw, src, wstep, kernel_cache, kernel_fn, kwargs)
+    Q = kt.shape[1]
+    x, xf, y, yf = frac_coords(guv.shape, Q, uvw / lam)
+    convgrid_indexed(kt, False, guv, x, xf, y, yf, g, numpy.asarray(vis))
+    return guv
+
+
+def w_cache_predict(theta, lam, uvw, src, guv, wstep=2000, kernel_cache=None,
+                    kernel_fn=w_kernel, **kwargs):
+    """w-projection predict (synthesis.py:799-828).
+
+    Minimal fix: the reference uses undefined ``nv`` (:823) and ``ixs``
+    (:827); this sizes the output by ``len(uvw)`` and writes row i."""
+    kt, g = _w_cache_table(theta, uvw, src, wstep, kernel_cache, kernel_fn, kwargs)
+    Q = kt.shape[1]
+    x, xf, y, yf = frac_coords(guv.shape, Q, uvw / lam)
+    return convdegrid_indexed(kt, False, guv, x, xf, y, yf, g)
+
+
+def do_imaging(theta, lam, uvw, src, vis, imgfn, **kwargs):
+    """Mirror, weight, grid, hermitian, FFT; PSF likewise; normalise (synthesis.py:883-911)."""
+    if src is None:
+        src = numpy.ndarray((len(vis), 0))
+    uvw, vis = mirror_uvw(uvw, vis)
+    wt = doweight(theta, lam, uvw, numpy.ones(len(uvw)))
+    cdrt = imgfn(theta, lam, uvw, src, wt * vis, **kwargs)
+    drt = numpy.real(ifft(make_grid_hermitian(cdrt)))
+    c = imgfn(theta, lam, uvw, src, wt, **kwargs)
+    psf = numpy.real(ifft(make_grid_hermitian(c)))
+    pmax = psf.max()
+    assert pmax > 0.0
+    return drt / pmax, psf / pmax, pmax
+
+
+def do_predict(theta, lam, uvw, src, modelimage, predfn, **kwargs):
+    """FFT of the model image, then predfn (synthesis.py:914-927)."""
+    return predfn(theta, lam, uvw, src, fft(modelimage.astype(complex)), **kwargs)
+
+
+# --------------------------------------------------------------------------
+# w-stacking (examples/notebooks/wstacking.ipynb, code cell 10), with
+# convolutional gridding in place of the notebook's boxcar gridding.
+
+def w_stack_imaging(theta, lam, uvw, src, vis, kv, plane):
+    """Sum over planes of ifft(conv_imaging(plane vis)) / w_kernel_function(l, m, mean w).
+
+    ``plane`` is each visibility's w-plane index; w-planes without
+    visibilities are skipped, as in the notebook."""
+    N = grid_size(theta, lam)
+    l, m = theta * coordinates2(N)
+    image = numpy.zeros((N, N), dtype=complex)
+    src = numpy.zeros((len(uvw), 0)) if src is None else src
+    for wp in numpy.unique(plane):
+        sel = plane == wp
+        midw = numpy.mean(uvw[sel, 2])
+        g = conv_imaging(theta, lam, uvw[sel], src[sel], vis[sel], kv)
+        image += ifft(g) / w_kernel_function(l, m, midw)
+    return image
+
+
+# --------------------------------------------------------------------------
+# point-source visibilities (crocodile/simulate.py:210-230)
+
+def simulate_point(dist_uvw, l, m):
+    """exp(-2 pi i (u l + v m + w (sqrt(1 - l^2 - m^2) - 1))) (simulate.py:210-230)."""
+    s = numpy.array([l, m, numpy.sqrt(1 - l ** 2 - m ** 2) - 1.0])
+    return numpy.exp(-2j * numpy.pi * numpy.dot(dist_uvw, s))
