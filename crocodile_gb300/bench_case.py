@@ -1,0 +1,114 @@
+"""A small, self-contained run of the w-projection grid + degrid step, for profiling.
+
+    python -m crocodile_gb300.bench_case [--nvis N] [--steps K] [--workload wproj|plain]
+
+Sets up the seeded workload (kernels generated once), then runs K steps of
+w binning + plan + FP32 gridding + FP32 degridding on the current GPU and
+prints the per-step time.  Meant to run under ncu with a visibility count
+that keeps the capture small.
+"""
+
+import argparse
+import ctypes
+import time
+
+import numpy
+import torch
+
+from . import _lib as L
+from . import configs
+from . import engine as E
+from . import synthesis
+
+
+def setup(workload="wproj", nvis=500_000, seed=None):
+    if workload == "wproj":
+        w = configs.wproj(n=nvis) if seed is None else configs.wproj(seed=seed, n=nvis)
+        wstep, npixff = w.params["wstep"], w.params["NpixFF"]
+    else:
+        w = configs.plain(n=nvis) if seed is None else configs.plain(seed=seed, n=nvis)
+        wstep, npixff = None, None
+    dev = torch.device("cuda", torch.cuda.current_device())
+    uvw = torch.from_numpy(w.uvw).to(dev)
+    vis = torch.from_numpy(w.vis.astype(numpy.complex64)).to(dev)
+    st = E.Status()
+    if wstep is not None:
+        _, kmin, kmax = E.w_bins(uvw, wstep, st)
+        table = E.w_kernels(w.theta, wstep * numpy.arange(kmin, kmax + 1).astype(float), npixff,
+                            w.S, w.Q, dtype=E.CF)
+        kt = E.KernelTable(table.reshape(-1), False, w.Q, w.S)
+    else:
+        kmin = kmax = 0
+        aa = synthesis.anti_aliasing_function(w.N, 0, w.params["aa_c"])
+        k1 = synthesis.kernel_oversample(aa, w.Q, w.S)
+        kt = E.KernelTable.from_gcf(numpy.asarray(k1), 0, E.CF)
+    return dict(w=w, uvw=uvw, vis=vis, st=st, kt=kt, kmin=kmin, nk=kmax - kmin + 1, wstep=wstep)
+
+
+class Step:
+    """One grid + degrid step through the C ABI, reusing one workspace."""
+
+    def __init__(self, ctx):
+        self.c = ctx
+        w = ctx["w"]
+        self.n = w.uvw.shape[0]
+        self.N = w.N
+        dev = ctx["uvw"].device
+        self.kd = ctx["kt"].desc()
+        lib = L.lib()
+        self.ws_bytes = lib.cg_plan_workspace_bytes(L.CG_PLAN_TILED, self.n, self.N, self.N,
+                                                    ctypes.byref(self.kd))
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
+        self.kidx = torch.zeros(self.n, dtype=torch.int32, device=dev)
+        self.grid = torch.zeros((self.N, self.N), dtype=torch.complex64, device=dev)
+        self.out = torch.empty(self.n, dtype=torch.complex64, device=dev)
+
+    def __call__(self, uvw=None, vis=None, events=None):
+        c = self.c
+        P = lambda t: ctypes.c_void_p(t.data_ptr())
+        sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        uvw = c["uvw"] if uvw is None else uvw
+        vis = c["vis"] if vis is None else vis
+        kidx = None
+        if c["wstep"] is not None:
+            L.call("cg_w_bins_fixed", P(uvw), uvw.stride(0), self.n, c["wstep"], c["kmin"],
+                   c["nk"], P(self.kidx), P(c["st"].t), sp)
+            kidx = P(self.kidx)
+        h = ctypes.c_void_p()
+        L.call("cg_plan_create", ctypes.byref(h), L.CG_PLAN_TILED, ctypes.byref(self.kd), self.N,
+               self.N, P(uvw), uvw.stride(0), c["w"].lam, kidx, self.n, P(self.ws),
+               self.ws_bytes, P(c["st"].t), sp)
+        try:
+            self.grid.zero_()
+            if events:
+                events[0].record()
+            L.call("cg_grid", h, P(c["kt"].table), P(vis), P(self.grid), sp)
+            if events:
+                events[1].record()
+            L.call("cg_degrid", h, P(c["kt"].table), P(self.grid), P(self.out), sp)
+            if events:
+                events[2].record()
+        finally:
+            L.lib().cg_plan_destroy(h)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--nvis", type=int, default=500_000)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--workload", default="wproj", choices=["wproj", "plain"])
+    a = ap.parse_args()
+    ctx = setup(a.workload, a.nvis)
+    step = Step(ctx)
+    step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        step()
+    torch.cuda.synchronize()
+    ctx["st"].check()
+    print("%s n=%d: %.3f ms/step" % (a.workload, a.nvis, 1e3 * (time.perf_counter() - t0) / a.steps))
+
+
+if __name__ == "__main__":
+    main()

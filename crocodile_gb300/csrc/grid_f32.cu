@@ -251,10 +251,10 @@ static TiledArgs tiled_args(const cg_plan *p) {
 static int grid_launch(const cg_plan *p, const void *ktab, const void *vis,
                        const float *weight, int mode, void *grid, cudaStream_t s) {
   CG_REQUIRE(p && p->mode == CG_PLAN_TILED, "cg_grid needs a CG_PLAN_TILED plan");
+  if (p->n == 0) return CG_OK;
   CG_REQUIRE(ktab && grid, "NULL kernel table or grid");
   CG_REQUIRE(mode == 2 || vis, "NULL visibilities");
   CG_REQUIRE(mode == 0 || weight, "NULL weights");
-  if (p->n == 0) return CG_OK;
   TiledArgs A = tiled_args(p);
   const int SS = p->kd.S * p->kd.S;
   const int threads = (SS + 31) / 32 * 32;
@@ -296,8 +296,8 @@ int cg_grid_weighted(const cg_plan *p, const void *ktab, const void *vis,
 int cg_degrid(const cg_plan *p, const void *ktab, const void *grid, void *out,
               cg_stream_t stream) {
   CG_REQUIRE(p && p->mode == CG_PLAN_TILED, "cg_degrid needs a CG_PLAN_TILED plan");
-  CG_REQUIRE(ktab && grid && out, "NULL argument");
   if (p->n == 0) return CG_OK;
+  CG_REQUIRE(ktab && grid && out, "NULL argument");
   cudaStream_t s = (cudaStream_t)stream;
   TiledArgs A = tiled_args(p);
   const int SS = p->kd.S * p->kd.S;

@@ -163,6 +163,7 @@ extern "C" {
 int cg_grid_fp64(const cg_plan *p, const void *ktab, const void *vis, void *grid,
                  cg_stream_t stream) {
   CG_REQUIRE(p && p->mode == CG_PLAN_GROUPS, "cg_grid_fp64 needs a CG_PLAN_GROUPS plan");
+  if (p->n == 0) return CG_OK;
   CG_REQUIRE(ktab && vis && grid, "NULL argument");
   PlainArgs A = plain_args(p);
   const int SS = p->kd.S * p->kd.S;
@@ -180,6 +181,7 @@ int cg_grid_fp64(const cg_plan *p, const void *ktab, const void *vis, void *grid
 int cg_degrid_fp64(const cg_plan *p, const void *ktab, const void *grid, void *out,
                    cg_stream_t stream) {
   CG_REQUIRE(p && p->mode == CG_PLAN_GROUPS, "cg_degrid_fp64 needs a CG_PLAN_GROUPS plan");
+  if (p->n == 0) return CG_OK;
   CG_REQUIRE(ktab && grid && out, "NULL argument");
   PlainArgs A = plain_args(p);
   for (int g = 0; g < p->nbuckets; ++g) {
