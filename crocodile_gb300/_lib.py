@@ -25,6 +25,7 @@ CG_ERR_CUDA = -5
 CG_ERR_WORKSPACE = -6
 CG_ERR_TIMEOUT = -7
 CG_STATUS_WORDS = 4
+CG_NOALLOC_SCRATCH_BYTES = 16 << 20  # include/crocodile_gb300.h
 CG_PLAN_TILED = 0
 CG_PLAN_GROUPS = 1
 
@@ -50,6 +51,8 @@ SIGNATURES = {
     "cg_grid": (c_int, [P, P, P, P, P]),
     "cg_grid_weighted": (c_int, [P, P, P, P, P, P]),
     "cg_degrid": (c_int, [P, P, P, P, P]),
+    "cg_grid_noalloc": (c_int, [ctypes.POINTER(KernelDesc), c_int, c_int, P, c_int64, c_double,
+                                P, c_int64, P, P, P, P, P]),
     "cg_grid_fp64": (c_int, [P, P, P, P, P]),
     "cg_degrid_fp64": (c_int, [P, P, P, P, P]),
     "cg_grid_boxcar": (c_int, [P, c_int64, c_double, c_int64, P, P, c_int, c_int, P, P]),

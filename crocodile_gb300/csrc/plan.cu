@@ -342,6 +342,80 @@ static int check_desc(const cg_kernel_desc *kd, int H, int W) {
   return CG_OK;
 }
 
+// Tiled plan built into a caller-provided struct: no host or device
+// allocation.  Used by the entry point for callers that cannot allocate.
+int plan_build_tiled_into(cg_plan *p, const cg_kernel_desc *kd, int H, int W,
+                          const double *uvw, int64_t stride, double lam,
+                          const int32_t *kidx, int64_t n, void *workspace,
+                          size_t workspace_bytes, int32_t *d_status, cudaStream_t s) {
+  int rc = check_desc(kd, H, W);
+  if (rc) return rc;
+  CG_REQUIRE(n >= 0 && n < (int64_t)INT32_MAX, "visibility count %lld unsupported",
+             (long long)n);
+  CG_REQUIRE(n == 0 || (uvw && stride >= 2), "uvw is NULL or stride < 2");
+  CG_REQUIRE(d_status, "status block is NULL");
+  CG_REQUIRE(kd->G == 1 || kidx || n == 0, "G > 1 needs per-visibility kernel indices");
+  memset(p, 0, sizeof(*p));
+  p->mode = CG_PLAN_TILED;
+  p->kd = *kd;
+  p->H = H;
+  p->W = W;
+  p->n = n;
+  plan_geometry(*p);
+  const Layout L = layout_of(*p);
+  if (!workspace || workspace_bytes < L.total)
+    return set_error(CG_ERR_WORKSPACE, "plan needs %zu workspace bytes, got %zu", L.total,
+                     workspace_bytes);
+  char *ws = (char *)workspace;
+  VisRec *rec_tmp = (VisRec *)(ws + L.rec_tmp);
+  int32_t *key = (int32_t *)(ws + L.key);
+  int32_t *rank = (int32_t *)(ws + L.rank);
+  p->recs = (VisRec *)(ws + L.recs);
+  p->perm = (int32_t *)(ws + L.perm);
+  p->counts = (int32_t *)(ws + L.counts);
+  p->offsets = (int32_t *)(ws + L.offsets);
+  p->items = (WorkItem *)(ws + L.items);
+  int32_t *ctr = (int32_t *)(ws + L.ctr);
+  p->nitems = ctr;
+  p->ticket = ctr + 1;
+  p->status = d_status;
+  // everything later kernels accumulate into starts at zero on every call
+  CG_CUDA(cudaMemsetAsync(p->counts, 0, (size_t)p->nbuckets * 4, s));
+  CG_CUDA(cudaMemsetAsync(ctr, 0, 16, s));
+  if (n == 0) return CG_OK;
+  CoordParams P;
+  P.uvw = uvw;
+  P.stride = stride;
+  P.lam = lam;
+  P.n = n;
+  P.H = H;
+  P.W = W;
+  P.Q = kd->Q;
+  P.S = kd->S;
+  P.G = kd->G;
+  P.sep = kd->sep;
+  P.kidx = kidx;
+  P.mode = CG_PLAN_TILED;
+  P.T = p->T;
+  P.ntx = p->ntx;
+  P.nbuckets = p->nbuckets;
+  P.rec = rec_tmp;
+  P.key = key;
+  P.rank = rank;
+  P.hist = p->counts;
+  P.status = d_status;
+  const int blocks = (int)((n + 255) / 256);
+  k_plan_coords<<<blocks, 256, 0, s>>>(P);
+  CG_LAUNCH("coords");
+  rc = launch_scan(p->counts, p->offsets, p->nbuckets, (int32_t *)(ws + L.scan), s);
+  if (rc) return rc;
+  k_plan_scatter<<<blocks, 256, 0, s>>>(n, rec_tmp, key, rank, p->offsets, p->recs, p->perm);
+  k_plan_items<<<(p->nbuckets + 255) / 256, 256, 0, s>>>(p->nbuckets, p->counts, p->offsets,
+                                                         p->chunk, p->items, p->nitems);
+  CG_LAUNCH("plan sort");
+  return CG_OK;
+}
+
 }  // namespace cg
 
 using namespace cg;

@@ -128,6 +128,28 @@ int cg_grid_weighted(const cg_plan *plan, const void *ktab_c64,
 /* convdegrid (synthesis.py:484-503): out[i] = sum(grid[footprint] * K). */
 int cg_degrid(const cg_plan *plan, const void *ktab_c64, const void *grid_c64,
               void *vis_out_c64, cg_stream_t stream);
+/* cg_grid_noalloc: no counterpart in the reference.  For callers that
+ * cannot allocate device memory (a pipeline that owns all GPU memory in its
+ * own pool and may not call cudaMalloc/cudaFree while it runs, or an FFI
+ * host with nothing but its input and output buffers to pass): the same
+ * result as cg_plan_create + cg_grid (FP32, grid += K * vis), with the
+ * plan's scratch in a static device array of CG_NOALLOC_SCRATCH_BYTES that
+ * the library holds on every GPU that loads it until the process exits.
+ * Allocates nothing, on the host or the device.  Inputs and outputs are the
+ * caller's device buffers, as for cg_grid; d_status is the caller's status
+ * block.  Returns CG_ERR_WORKSPACE, writing nothing, when n visibilities on
+ * an H x W grid need more scratch than that (cg_plan_workspace_bytes gives
+ * the need; about 16 MiB / 44 B = 380 000 visibilities).
+ * The first call on a device looks up the array's device address, once per
+ * device, with that device current; make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller. */
+#define CG_NOALLOC_SCRATCH_BYTES (16u << 20)
+int cg_grid_noalloc(const cg_kernel_desc *kd, int H, int W, const double *uvw,
+                    int64_t stride, double lam, const int32_t *kidx, int64_t n,
+                    const void *ktab_c64, const void *vis_c64, void *grid_c64,
+                    int32_t *d_status, cg_stream_t stream);
+
 /* Plain FP64 form of the same two operations (c128 data, FP64 atomics,
  * one launch per kernel group): the accuracy and speed comparator.
  * Needs a CG_PLAN_GROUPS plan. */
