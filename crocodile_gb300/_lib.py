@@ -28,10 +28,17 @@ CG_STATUS_WORDS = 4
 CG_NOALLOC_SCRATCH_BYTES = 16 << 20  # include/crocodile_gb300.h
 CG_PLAN_TILED = 0
 CG_PLAN_GROUPS = 1
+CG_LAYOUT_WARP = 1
+CG_LAYOUT_OWNER = 2
 
 
 class KernelDesc(ctypes.Structure):
     _fields_ = [("sep", c_int), ("Q", c_int), ("S", c_int), ("G", c_int)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("tile", c_int), ("chunk", c_int), ("rows", c_int), ("groups", c_int),
+                ("layout", c_int)]
 
 
 # name -> (restype, argtypes); the declarations of include/crocodile_gb300.h
@@ -46,7 +53,12 @@ SIGNATURES = {
                                            ctypes.POINTER(KernelDesc)]),
     "cg_plan_create": (c_int, [ctypes.POINTER(P), c_int, ctypes.POINTER(KernelDesc), c_int, c_int,
                                P, c_int64, c_double, P, c_int64, P, c_size_t, P, P]),
+    "cg_plan_create_wbins": (c_int, [ctypes.POINTER(P), c_int, ctypes.POINTER(KernelDesc), c_int,
+                                     c_int, P, c_int64, c_double, c_double, c_int, c_int64, P,
+                                     c_size_t, P, P]),
     "cg_plan_destroy": (c_int, [P]),
+    "cg_set_tuning": (c_int, [ctypes.POINTER(Tuning)]),
+    "cg_get_tuning": (c_int, [ctypes.POINTER(Tuning)]),
     "cg_plan_info": (c_int, [P, P]),
     "cg_grid": (c_int, [P, P, P, P, P]),
     "cg_grid_weighted": (c_int, [P, P, P, P, P, P]),

@@ -3,8 +3,8 @@
     python -m crocodile_gb300.bench_case [--nvis N] [--steps K] [--workload wproj|plain]
 
 Sets up the seeded workload (kernels generated once), then runs K steps of
-w binning + plan + FP32 gridding + FP32 degridding on the current GPU and
-prints the per-step time.  Meant to run under ncu with a visibility count
+plan (with fused w binning) + FP32 gridding + FP32 degridding on the current
+GPU and prints the per-step time.  --tune runs the autotuner first.  Meant to run under ncu with a visibility count
 that keeps the capture small.
 """
 
@@ -46,7 +46,7 @@ def setup(workload="wproj", nvis=500_000, seed=None):
 
 
 class Step:
-    """One grid + degrid step through the C ABI, reusing one workspace."""
+    """One plan + grid + degrid step through the C ABI, reusing one workspace."""
 
     def __init__(self, ctx):
         self.c = ctx
@@ -59,7 +59,6 @@ class Step:
         self.ws_bytes = lib.cg_plan_workspace_bytes(L.CG_PLAN_TILED, self.n, self.N, self.N,
                                                     ctypes.byref(self.kd))
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
-        self.kidx = torch.zeros(self.n, dtype=torch.int32, device=dev)
         self.grid = torch.zeros((self.N, self.N), dtype=torch.complex64, device=dev)
         self.out = torch.empty(self.n, dtype=torch.complex64, device=dev)
 
@@ -69,15 +68,15 @@ class Step:
         sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         uvw = c["uvw"] if uvw is None else uvw
         vis = c["vis"] if vis is None else vis
-        kidx = None
-        if c["wstep"] is not None:
-            L.call("cg_w_bins_fixed", P(uvw), uvw.stride(0), self.n, c["wstep"], c["kmin"],
-                   c["nk"], P(self.kidx), P(c["st"].t), sp)
-            kidx = P(self.kidx)
         h = ctypes.c_void_p()
-        L.call("cg_plan_create", ctypes.byref(h), L.CG_PLAN_TILED, ctypes.byref(self.kd), self.N,
-               self.N, P(uvw), uvw.stride(0), c["w"].lam, kidx, self.n, P(self.ws),
-               self.ws_bytes, P(c["st"].t), sp)
+        if c["wstep"] is not None:
+            L.call("cg_plan_create_wbins", ctypes.byref(h), L.CG_PLAN_TILED,
+                   ctypes.byref(self.kd), self.N, self.N, P(uvw), uvw.stride(0), c["w"].lam,
+                   c["wstep"], c["kmin"], self.n, P(self.ws), self.ws_bytes, P(c["st"].t), sp)
+        else:
+            L.call("cg_plan_create", ctypes.byref(h), L.CG_PLAN_TILED, ctypes.byref(self.kd),
+                   self.N, self.N, P(uvw), uvw.stride(0), c["w"].lam, None, self.n, P(self.ws),
+                   self.ws_bytes, P(c["st"].t), sp)
         try:
             self.grid.zero_()
             if events:
@@ -97,8 +96,18 @@ def main():
     ap.add_argument("--nvis", type=int, default=500_000)
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--workload", default="wproj", choices=["wproj", "plain"])
+    ap.add_argument("--tune", action="store_true", help="autotune the launch shape first")
     a = ap.parse_args()
     ctx = setup(a.workload, a.nvis)
+    if a.tune:
+        from . import autotune
+        w = ctx["w"]
+        kidx = None
+        if ctx["wstep"] is not None:
+            kidx, _, _ = E.w_bins(ctx["uvw"], ctx["wstep"], ctx["st"])
+        best, _ = autotune.tune(ctx["uvw"], w.lam, (w.N, w.N), ctx["kt"], kidx, ctx["vis"],
+                                cands=autotune.candidates(w.S, quick=True), use_cache=False)
+        print("tuning", best)
     step = Step(ctx)
     step()
     torch.cuda.synchronize()

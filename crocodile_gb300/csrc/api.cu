@@ -34,9 +34,36 @@ int num_sms() {
   return sms;
 }
 
+static std::mutex g_tuning_mu;
+static cg_tuning g_tuning = {0, 0, 0, 0, 0};
+
+cg_tuning tuning() {
+  std::lock_guard<std::mutex> lock(g_tuning_mu);
+  return g_tuning;
+}
+
 }  // namespace cg
 
 extern "C" {
+
+int cg_set_tuning(const cg_tuning *t) {
+  CG_REQUIRE(t, "tuning is NULL");
+  CG_REQUIRE(t->tile >= 0 && t->tile <= 64 && t->tile % 4 == 0, "tile %d must be a multiple of 4 "
+             "in [0, 64]", t->tile);
+  CG_REQUIRE(t->chunk >= 0 && t->chunk <= (1 << 20), "chunk %d out of range", t->chunk);
+  CG_REQUIRE(t->rows >= 0 && t->rows <= 8, "rows %d out of range [0, 8]", t->rows);
+  CG_REQUIRE(t->groups >= 0 && t->groups <= 8, "groups %d out of range [0, 8]", t->groups);
+  CG_REQUIRE(t->layout >= 0 && t->layout <= CG_LAYOUT_OWNER, "layout %d unknown", t->layout);
+  std::lock_guard<std::mutex> lock(cg::g_tuning_mu);
+  cg::g_tuning = *t;
+  return CG_OK;
+}
+
+int cg_get_tuning(cg_tuning *out) {
+  CG_REQUIRE(out, "output is NULL");
+  *out = cg::tuning();
+  return CG_OK;
+}
 
 const char *cg_last_error(void) { return cg::g_msg; }
 

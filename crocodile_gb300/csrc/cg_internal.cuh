@@ -31,6 +31,7 @@ int cuda_error(cudaError_t e, const char *where);
 enum { ST_RANGE = 0, ST_BOUNDS = 1, ST_INDEX = 2, ST_TIMEOUT = 3 };
 
 int num_sms();
+cg_tuning tuning();  // current process-wide launch-shape tuning
 
 // ---------------------------------------------------------------- device helpers
 // Python-style floor division / modulo of an integer by a positive divisor.
@@ -60,6 +61,67 @@ __device__ __forceinline__ void frac_coord(double p, int N, int Q, int &xi,
 
 __device__ __forceinline__ bool in_unit_range(double p) {
   return p >= -0.5 && p < 0.5;  // false for NaN, as numpy's assert
+}
+
+// Filtered exact evaluation.  GB300 runs FP64 at a small fraction of its FP32
+// rate and an IEEE division costs many FP64 operations, so coordinates are
+// first estimated with one FMA from constants prepared on the host, and the
+// exact sequence above runs only when the estimate cannot decide:
+//   c~ = fma(-u, NQ_over_lam, -(N//2)*Q)   estimates (-(N//2 + (u/lam)*N)) * Q
+// Each of the two evaluations is within a few ulp of the real value, i.e.
+// within ~2^-49 * N * Q (< 1e-9 for N*Q <= 2^20) of each other, so rint()
+// agrees whenever c~ is further than 1e-6 from a half-integer.  The range
+// test p in [-0.5, 0.5) likewise uses u * (1/lam) except within 1e-9 of the
+// ends.  Results are bit-identical to frac_coord/in_unit_range on u / lam.
+struct AxisConst {
+  double nq_over_lam;  // N * Q / lam
+  double n2q;          // (N // 2) * Q
+  double inv_lam;      // 1 / lam
+};
+
+__device__ __forceinline__ bool near_half(double c) {
+  const double f = c - floor(c);
+  return fabs(f - 0.5) < 1e-6;
+}
+
+// p = u / lam in range?  (exact decision)
+__device__ __forceinline__ bool unit_range_fast(double u, double lam, double inv_lam) {
+  const double pe = u * inv_lam;
+  if (pe > -0.5 + 1e-9 && pe < 0.5 - 1e-9) return true;
+  if (!(pe > -0.5 - 1e-9 && pe < 0.5 + 1e-9)) return false;  // NaN lands here too
+  return in_unit_range(__ddiv_rn(u, lam));
+}
+
+__device__ __forceinline__ void frac_coord_fast(double u, double lam, const AxisConst &k, int N,
+                                                int Q, int &xi, int &xf) {
+  const double ce = fma(-u, k.nq_over_lam, -k.n2q);
+  long long fx;
+  if (!near_half(ce)) {
+    fx = (long long)rint(ce);
+  } else {
+    const double p = __ddiv_rn(u, lam);
+    const double x = __dadd_rn((double)(N / 2), __dmul_rn(p, (double)N));
+    fx = (long long)rint(__dmul_rn(-x, (double)Q));
+  }
+  long long q, r;
+  floordivmod(fx, Q, q, r);
+  xi = (int)(-q);
+  xf = (int)r;
+}
+
+// w bin k = rint(w / wstep) (w_cache_imaging, synthesis.py:793), filtered likewise.
+__device__ __forceinline__ double w_bin_fast(double w, double wstep, double inv_wstep) {
+  const double ke = w * inv_wstep;
+  if (!near_half(ke)) return rint(ke);
+  return rint(__ddiv_rn(w, wstep));
+}
+
+inline AxisConst axis_const(int N, int Q, double lam) {
+  AxisConst k;
+  k.nq_over_lam = ((double)N * (double)Q) / lam;
+  k.n2q = (double)(N / 2) * (double)Q;
+  k.inv_lam = 1.0 / lam;
+  return k;
 }
 
 // Visibility coordinate p = uvw[i*stride + axis] / lam (IEEE division).
@@ -92,6 +154,8 @@ struct cg_plan {
   int win;      // window edge = T + S - 1
   int pitch;    // smem row pitch (even)
   int nbuckets;
+  int ntiles;   // tiled mode: tiles; each tile holds 4^sublog sub-tile buckets
+  int sublog;   // sub-tiles are 4x4 cells, ordered along a Morton curve in the tile
   int64_t max_items;
   int chunk;    // visibilities per work item
   // device arrays inside the caller's workspace

@@ -2,22 +2,21 @@
 //
 // Gridder, replacing convgrid (crocodile/synthesis.py:464-481):
 //   grid[y0+dy, x0+dx] += K[g, yf, xf, dy, dx] * v   for each visibility.
-// Visibilities arrive sorted by the grid tile of their footprint origin.  A
-// persistent CTA takes one work item (<= chunk visibilities of one tile),
-// accumulates into a shared-memory window of (T+S-1)^2 cells and flushes the
-// window to HBM with vectorised float2 atomics once per item.  Inside the
-// window, thread (tx, ty) of the S x S thread group owns every cell whose
-// window coordinates are congruent to (tx, ty) mod S: each visibility's
-// footprint holds exactly one such cell, so every thread updates exactly
-// one cell per visibility, no two threads ever touch the same cell, and the
-// running sum stays in registers while consecutive visibilities hit the
-// same cell (it is written back to shared memory only when the cell
-// changes).  No shared-memory atomics are needed.
+// Visibilities arrive sorted by grid tile, and inside a tile by 4x4 sub-tile
+// along a Morton curve.  A persistent CTA takes one work item (<= chunk
+// visibilities of one tile), accumulates into a shared-memory window of
+// (T+S-1)^2 cells and flushes the window to HBM with vectorised float2
+// atomics once per item.  Inside the window every cell belongs to one thread
+// of a thread group (ownership by position mod S), which keeps a running sum
+// in registers while consecutive visibilities hit the same cell and writes it
+// back only when the cell changes; spatially sorted visibilities make that
+// rare.
 //
 // Degridder, replacing convdegrid (synthesis.py:484-503):
 //   out[i] = sum_{dy,dx} grid[y0+dy, x0+dx] * K[g, yf, xf, dy, dx]
 // A persistent CTA stages the item's grid window in shared memory; one warp
-// per visibility sums its S*S taps (fixed per lane) and reduces with shuffles.
+// per visibility pair sums the S*S taps (fixed per lane) and reduces with
+// shuffles.
 #include <algorithm>
 
 #include "cg_internal.cuh"
@@ -60,24 +59,35 @@ __device__ __forceinline__ int next_item(const TiledArgs &A, int *s_item) {
 // ---------------------------------------------------------------- gridder
 static constexpr int GRID_STAGE = 256;  // visibilities staged per batch
 
-template <bool SEP, int MODE>  // MODE 0: vis, 1: vis * weight, 2: weight only
-__global__ void __launch_bounds__(1024) k_grid_tiled(
-    TiledArgs A, const float2 *__restrict__ ktab, const float2 *__restrict__ vis,
+// A thread group has S * ceil(S / R) threads: thread (tx, yg) owns window
+// column residue tx and row residues yg*R + r (r < R), i.e. for every
+// visibility it updates the R cells of its residues inside the footprint,
+// decoding the visibility once for R updates.  With one group per CTA each
+// window cell has a single owner and the running sums are written back with
+// plain read-modify-writes; with several groups sharing the window
+// (shared = true) the write-backs are shared-memory atomics.
+// mode 0: vis, 1: vis * weight, 2: weight only (the PSF pass).
+template <bool SEP, int R>
+__global__ void __launch_bounds__(256) k_grid_tiled(
+    TiledArgs A, int gsize, int ngroups, int mode, bool shared,
+    const float2 *__restrict__ ktab, const float2 *__restrict__ vis,
     const float *__restrict__ weight, float2 *__restrict__ grid) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_item;
   if (status_failed(A.status)) return;
   const int S = A.S, SS = S * S, pitch = A.pitch;
   float2 *win = (float2 *)smem;
-  int *s_lxy = (int *)(win + (size_t)pitch * A.win);
-  int *s_mxy = s_lxy + GRID_STAGE;
+  int *s_base = (int *)(win + (size_t)pitch * A.win);
+  int *s_mxy = s_base + GRID_STAGE;
   long long *s_k0 = (long long *)(s_mxy + GRID_STAGE);
   long long *s_k1 = s_k0 + GRID_STAGE;
   float2 *s_v = (float2 *)(s_k1 + GRID_STAGE);
 
   const int tid = threadIdx.x;
-  const bool active = tid < SS;
-  const int tx = tid % S, ty = tid / S;
+  const int gpad = (gsize + 31) & ~31;  // groups start on warp boundaries
+  const int grp = tid / gpad, lt = tid - grp * gpad;
+  const bool active = grp < ngroups && lt < gsize;
+  const int tx = lt % S, yg = lt / S;
   const int wcells = A.win * A.win;
   const long long KSZ = (long long)A.Q * A.Q * SS;
 
@@ -87,31 +97,35 @@ __global__ void __launch_bounds__(1024) k_grid_tiled(
     const int wx0 = (w.tile % A.ntx) * A.T, wy0 = (w.tile / A.ntx) * A.T;
     for (int c = tid; c < pitch * A.win; c += blockDim.x) win[c] = make_float2(0.f, 0.f);
 
-    int cur = -1;
-    float2 acc = make_float2(0.f, 0.f);
+    int cur[R];
+    float2 acc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      cur[r] = -1;
+      acc[r] = make_float2(0.f, 0.f);
+    }
     for (int b = 0; b < w.count; b += GRID_STAGE) {
       const int nb = min(GRID_STAGE, w.count - b);
       __syncthreads();
       for (int j = tid; j < nb; j += blockDim.x) {
         const int pos = w.start + b + j;
-        const VisRec r = A.recs[pos];
-        const int lx0 = r.x0 - wx0, ly0 = r.y0 - wy0;
-        s_lxy[j] = lx0 | (ly0 << 16);
+        const VisRec rec = A.recs[pos];
+        const int lx0 = rec.x0 - wx0, ly0 = rec.y0 - wy0;
+        s_base[j] = ly0 * pitch + lx0;
         s_mxy[j] = (lx0 % S) | ((ly0 % S) << 16);
         if (SEP) {
-          s_k0[j] = (long long)r.k0 * S;
-          s_k1[j] = (long long)r.k1 * S;
+          s_k0[j] = (long long)rec.k0 * S;
+          s_k1[j] = (long long)rec.k1 * S;
         } else {
-          s_k0[j] = (long long)r.k0 * KSZ + (long long)r.k1 * SS;
-          s_k1[j] = 0;
+          s_k0[j] = (long long)rec.k0 * KSZ + (long long)rec.k1 * SS;
         }
         const int src = A.perm[pos];
         float2 v;
-        if (MODE == 2) {
+        if (mode == 2) {
           v = make_float2(weight[src], 0.f);
         } else {
           v = vis[src];
-          if (MODE == 1) {
+          if (mode == 1) {
             const float wt = weight[src];
             v.x *= wt;
             v.y *= wt;
@@ -121,39 +135,158 @@ __global__ void __launch_bounds__(1024) k_grid_tiled(
       }
       __syncthreads();
       if (active) {
-#pragma unroll 4
-        for (int j = 0; j < nb; ++j) {
-          const int lxy = s_lxy[j], mxy = s_mxy[j];
-          const int lx0 = lxy & 0xffff, ly0 = lxy >> 16;
+        for (int j = grp; j < nb; j += ngroups) {
+          const int base = s_base[j], mxy = s_mxy[j];
+          const float2 v = s_v[j];
           int dx = tx - (mxy & 0xffff);
           dx += (dx >> 31) & S;
-          int dy = ty - (mxy >> 16);
-          dy += (dy >> 31) & S;
-          const int cell = (ly0 + dy) * pitch + lx0 + dx;
-          float2 k;
-          if (SEP)
-            k = cmul(__ldg(&ktab[s_k0[j] + dy]), __ldg(&ktab[s_k1[j] + dx]));
-          else
-            k = __ldg(&ktab[s_k0[j] + dy * S + dx]);
-          if (cell != cur) {
-            if (cur >= 0) {
-              float2 o = win[cur];
-              o.x += acc.x;
-              o.y += acc.y;
-              win[cur] = o;
-            }
-            cur = cell;
-            acc = make_float2(0.f, 0.f);
+          const int my = mxy >> 16;
+          const int cb = base + dx;
+          const float2 *kp;
+          float2 kx = make_float2(0.f, 0.f);
+          if (SEP) {
+            kp = ktab + s_k0[j];
+            kx = __ldg(&ktab[s_k1[j] + dx]);
+          } else {
+            kp = ktab + s_k0[j] + dx;
           }
-          cfma(acc, k, s_v[j]);
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const int res = yg * R + r;
+            if (res < S) {
+              int dy = res - my;
+              dy += (dy >> 31) & S;
+              const int cell = cb + dy * pitch;
+              const float2 k = SEP ? cmul(__ldg(&kp[dy]), kx) : __ldg(&kp[dy * S]);
+              if (cell != cur[r]) {
+                if (cur[r] >= 0) {
+                  if (shared) {
+                    atomicAdd(&win[cur[r]].x, acc[r].x);
+                    atomicAdd(&win[cur[r]].y, acc[r].y);
+                  } else {
+                    float2 o = win[cur[r]];
+                    o.x += acc[r].x;
+                    o.y += acc[r].y;
+                    win[cur[r]] = o;
+                  }
+                }
+                cur[r] = cell;
+                acc[r] = make_float2(0.f, 0.f);
+              }
+              cfma(acc[r], k, v);
+            }
+          }
         }
       }
     }
-    if (active && cur >= 0) {
-      float2 o = win[cur];
-      o.x += acc.x;
-      o.y += acc.y;
-      win[cur] = o;
+    if (active) {
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        if (cur[r] >= 0) {
+          if (shared) {
+            atomicAdd(&win[cur[r]].x, acc[r].x);
+            atomicAdd(&win[cur[r]].y, acc[r].y);
+          } else {
+            float2 o = win[cur[r]];
+            o.x += acc[r].x;
+            o.y += acc[r].y;
+            win[cur[r]] = o;
+          }
+        }
+    }
+    __syncthreads();
+    for (int c = tid; c < wcells; c += blockDim.x) {
+      const int r = c / A.win, q = c - r * A.win;
+      const float2 val = win[r * pitch + q];
+      if (val.x != 0.f || val.y != 0.f) {
+        const int gy = wy0 + r, gx = wx0 + q;
+        if (gy < A.H && gx < A.W) atomicAdd(&grid[(size_t)gy * A.W + gx], val);
+      }
+    }
+  }
+}
+
+// Warp layout: one warp per visibility; lane l adds taps l, l+32, ... of the
+// S x S footprint (kernel taps read coalesced) into the shared window with
+// shared-memory atomic adds, so the warps of a CTA share one window freely.
+template <bool SEP, int MAXT>
+__global__ void __launch_bounds__(256) k_grid_warp(
+    TiledArgs A, int mode, const float2 *__restrict__ ktab, const float2 *__restrict__ vis,
+    const float *__restrict__ weight, float2 *__restrict__ grid) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_item;
+  if (status_failed(A.status)) return;
+  const int S = A.S, SS = S * S, pitch = A.pitch;
+  float2 *win = (float2 *)smem;
+  int *s_base = (int *)(win + (size_t)pitch * A.win);
+  long long *s_k0 = (long long *)(s_base + 2 * GRID_STAGE);
+  long long *s_k1 = s_k0 + GRID_STAGE;
+  float2 *s_v = (float2 *)(s_k1 + GRID_STAGE);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const int wcells = A.win * A.win;
+  const long long KSZ = (long long)A.Q * A.Q * SS;
+
+  int soff[MAXT], kdy[MAXT], kdx[MAXT];
+#pragma unroll
+  for (int i = 0; i < MAXT; ++i) {
+    const int t = lane + 32 * i;
+    const int dy = t / S, dx = t - (t / S) * S;
+    soff[i] = (t < SS) ? dy * pitch + dx : -1;
+    kdy[i] = dy;
+    kdx[i] = dx;
+  }
+
+  int it;
+  while ((it = next_item(A, &s_item)) >= 0) {
+    const WorkItem w = A.items[it];
+    const int wx0 = (w.tile % A.ntx) * A.T, wy0 = (w.tile / A.ntx) * A.T;
+    for (int c = tid; c < pitch * A.win; c += blockDim.x) win[c] = make_float2(0.f, 0.f);
+    for (int b = 0; b < w.count; b += GRID_STAGE) {
+      const int nb = min(GRID_STAGE, w.count - b);
+      __syncthreads();
+      for (int j = tid; j < nb; j += blockDim.x) {
+        const int pos = w.start + b + j;
+        const VisRec rec = A.recs[pos];
+        s_base[j] = (rec.y0 - wy0) * pitch + (rec.x0 - wx0);
+        if (SEP) {
+          s_k0[j] = (long long)rec.k0 * S;
+          s_k1[j] = (long long)rec.k1 * S;
+        } else {
+          s_k0[j] = (long long)rec.k0 * KSZ + (long long)rec.k1 * SS;
+        }
+        const int src = A.perm[pos];
+        float2 v;
+        if (mode == 2) {
+          v = make_float2(weight[src], 0.f);
+        } else {
+          v = vis[src];
+          if (mode == 1) {
+            const float wt = weight[src];
+            v.x *= wt;
+            v.y *= wt;
+          }
+        }
+        s_v[j] = v;
+      }
+      __syncthreads();
+      for (int j = warp; j < nb; j += nwarps) {
+        const int base = s_base[j];
+        const float2 v = s_v[j];
+        const float2 *kk = ktab + s_k0[j];
+        const float2 *kx = ktab + s_k1[j];
+        float2 k[MAXT];
+#pragma unroll
+        for (int i = 0; i < MAXT; ++i)
+          if (soff[i] >= 0)
+            k[i] = SEP ? cmul(__ldg(&kk[kdy[i]]), __ldg(&kx[kdx[i]])) : __ldg(&kk[lane + 32 * i]);
+#pragma unroll
+        for (int i = 0; i < MAXT; ++i)
+          if (soff[i] >= 0) {
+            const float2 u = cmul(k[i], v);
+            atomicAdd(&win[base + soff[i]].x, u.x);
+            atomicAdd(&win[base + soff[i]].y, u.y);
+          }
+      }
     }
     __syncthreads();
     for (int c = tid; c < wcells; c += blockDim.x) {
@@ -168,6 +301,9 @@ __global__ void __launch_bounds__(1024) k_grid_tiled(
 }
 
 // ---------------------------------------------------------------- degridder
+// Each warp sums the S*S taps of two visibilities at a time (taps fixed per
+// lane, interleaved so that both visibilities' kernel loads are in flight
+// together) and reduces both with shuffles.
 template <bool SEP, int MAXT>
 __global__ void __launch_bounds__(256) k_degrid_tiled(
     TiledArgs A, const float2 *__restrict__ ktab, const float2 *__restrict__ grid,
@@ -202,29 +338,42 @@ __global__ void __launch_bounds__(256) k_degrid_tiled(
                                                   : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    for (int j = warp; j < w.count; j += nwarps) {
-      const VisRec r = A.recs[w.start + j];
-      const int base = (r.y0 - wy0) * pitch + (r.x0 - wx0);
-      float2 sum = make_float2(0.f, 0.f);
-      if (SEP) {
-        const float2 *ky = ktab + (long long)r.k0 * S;
-        const float2 *kx = ktab + (long long)r.k1 * S;
+    for (int j = 2 * warp; j < w.count; j += 2 * nwarps) {
+      const bool two = j + 1 < w.count;
+      const VisRec r1 = A.recs[w.start + j];
+      const VisRec r2 = two ? A.recs[w.start + j + 1] : r1;
+      const int b1 = (r1.y0 - wy0) * pitch + (r1.x0 - wx0);
+      const int b2 = (r2.y0 - wy0) * pitch + (r2.x0 - wx0);
+      const float2 *k1 = ktab + (SEP ? 0 : (long long)r1.k0 * KSZ + (long long)r1.k1 * SS);
+      const float2 *k2 = ktab + (SEP ? 0 : (long long)r2.k0 * KSZ + (long long)r2.k1 * SS);
+      const float2 *ky1 = ktab + (long long)r1.k0 * S, *kx1 = ktab + (long long)r1.k1 * S;
+      const float2 *ky2 = ktab + (long long)r2.k0 * S, *kx2 = ktab + (long long)r2.k1 * S;
+      float2 s1 = make_float2(0.f, 0.f), s2 = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int i = 0; i < MAXT; ++i)
-          if (soff[i] >= 0)
-            cfma(sum, win[base + soff[i]], cmul(__ldg(&ky[kdy[i]]), __ldg(&kx[kdx[i]])));
-      } else {
-        const float2 *kk = ktab + (long long)r.k0 * KSZ + (long long)r.k1 * SS;
-#pragma unroll
-        for (int i = 0; i < MAXT; ++i)
-          if (soff[i] >= 0) cfma(sum, win[base + soff[i]], __ldg(&kk[lane + 32 * i]));
-      }
+      for (int i = 0; i < MAXT; ++i)
+        if (soff[i] >= 0) {
+          float2 ka, kb;
+          if (SEP) {
+            ka = cmul(__ldg(&ky1[kdy[i]]), __ldg(&kx1[kdx[i]]));
+            kb = cmul(__ldg(&ky2[kdy[i]]), __ldg(&kx2[kdx[i]]));
+          } else {
+            ka = __ldg(&k1[lane + 32 * i]);
+            kb = __ldg(&k2[lane + 32 * i]);
+          }
+          cfma(s1, win[b1 + soff[i]], ka);
+          cfma(s2, win[b2 + soff[i]], kb);
+        }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        sum.x += __shfl_xor_sync(0xffffffffu, sum.x, o);
-        sum.y += __shfl_xor_sync(0xffffffffu, sum.y, o);
+        s1.x += __shfl_xor_sync(0xffffffffu, s1.x, o);
+        s1.y += __shfl_xor_sync(0xffffffffu, s1.y, o);
+        s2.x += __shfl_xor_sync(0xffffffffu, s2.x, o);
+        s2.y += __shfl_xor_sync(0xffffffffu, s2.y, o);
       }
-      if (lane == 0) out[A.perm[w.start + j]] = sum;
+      if (lane == 0) {
+        out[A.perm[w.start + j]] = s1;
+        if (two) out[A.perm[w.start + j + 1]] = s2;
+      }
     }
   }
 }
@@ -248,6 +397,44 @@ static TiledArgs tiled_args(const cg_plan *p) {
   return A;
 }
 
+// Row residues per thread: the smallest R in {2, 3, 4} dividing S, else 4
+// (1 for S = 1); overridable by the tuning.
+static int pick_rows(int S) {
+  const cg_tuning t = tuning();
+  if (t.rows > 0) return t.rows;
+  if (S == 1) return 1;
+  for (int r = 2; r <= 4; ++r)
+    if (S % r == 0) return r;
+  return S < 4 ? S : 4;
+}
+
+template <bool SEP>
+static void *grid_kernel_for(int R) {
+  switch (R) {
+    case 1: return (void *)k_grid_tiled<SEP, 1>;
+    case 2: return (void *)k_grid_tiled<SEP, 2>;
+    case 3: return (void *)k_grid_tiled<SEP, 3>;
+    case 4: return (void *)k_grid_tiled<SEP, 4>;
+    case 5: return (void *)k_grid_tiled<SEP, 5>;
+    case 6: return (void *)k_grid_tiled<SEP, 6>;
+    case 8: return (void *)k_grid_tiled<SEP, 8>;
+    default: return nullptr;
+  }
+}
+
+template <bool SEP>
+static void *grid_warp_kernel_for(int maxt) {
+  switch (maxt) {
+    case 1: return (void *)k_grid_warp<SEP, 1>;
+    case 2: return (void *)k_grid_warp<SEP, 2>;
+    case 4: return (void *)k_grid_warp<SEP, 4>;
+    case 8: return (void *)k_grid_warp<SEP, 8>;
+    case 16: return (void *)k_grid_warp<SEP, 16>;
+    case 32: return (void *)k_grid_warp<SEP, 32>;
+    default: return nullptr;
+  }
+}
+
 static int grid_launch(const cg_plan *p, const void *ktab, const void *vis,
                        const float *weight, int mode, void *grid, cudaStream_t s) {
   CG_REQUIRE(p && p->mode == CG_PLAN_TILED, "cg_grid needs a CG_PLAN_TILED plan");
@@ -256,24 +443,65 @@ static int grid_launch(const cg_plan *p, const void *ktab, const void *vis,
   CG_REQUIRE(mode == 2 || vis, "NULL visibilities");
   CG_REQUIRE(mode == 0 || weight, "NULL weights");
   TiledArgs A = tiled_args(p);
-  const int SS = p->kd.S * p->kd.S;
-  const int threads = (SS + 31) / 32 * 32;
-  const size_t smem = (size_t)p->pitch * p->win * sizeof(float2) +
-                      (size_t)GRID_STAGE * (4 + 4 + 8 + 8 + 8);
-  void (*fn)(TiledArgs, const float2 *, const float2 *, const float *, float2 *);
-  if (p->kd.sep)
-    fn = mode == 0 ? k_grid_tiled<true, 0> : mode == 1 ? k_grid_tiled<true, 1> : k_grid_tiled<true, 2>;
-  else
-    fn = mode == 0 ? k_grid_tiled<false, 0> : mode == 1 ? k_grid_tiled<false, 1> : k_grid_tiled<false, 2>;
+  const int S = p->kd.S;
+  const cg_tuning t = tuning();
+  const float2 *kt = (const float2 *)ktab;
+  const float2 *vv = (const float2 *)vis;
+  float2 *gg = (float2 *)grid;
+  const size_t wbytes = (size_t)p->pitch * p->win * sizeof(float2);
+  void *fn = nullptr;
+  int threads = 0;
+  size_t smem = 0;
+  void *args[12];
+  int gsize = 0, ngroups = 0;
+  bool shared = false;
+  const int layout = t.layout > 0 ? t.layout : CG_LAYOUT_WARP;
+  if (layout == CG_LAYOUT_WARP) {
+    const int need = (S * S + 31) / 32;
+    int maxt = 1;
+    while (maxt < need) maxt *= 2;
+    fn = p->kd.sep ? grid_warp_kernel_for<true>(maxt) : grid_warp_kernel_for<false>(maxt);
+    CG_REQUIRE(fn, "no warp gridder for support %d", S);
+    threads = 32 * (t.groups > 0 ? t.groups : 8);
+    smem = wbytes + (size_t)GRID_STAGE * (8 + 8 + 8 + 8);
+    args[0] = &A;
+    args[1] = &mode;
+    args[2] = &kt;
+    args[3] = &vv;
+    args[4] = (void *)&weight;
+    args[5] = &gg;
+  } else {
+    int R = t.rows > 0 ? t.rows : pick_rows(S);
+    if (R > S) R = S;
+    if (R == 7) R = 8;
+    gsize = S * ((S + R - 1) / R);
+    const int gpad = (gsize + 31) & ~31;
+    ngroups = t.groups > 0 ? t.groups : std::max(1, 256 / gpad);
+    ngroups = std::max(1, std::min(ngroups, 256 / gpad));
+    threads = gpad * ngroups;
+    CG_REQUIRE(threads <= 256 && threads > 0,
+               "gridder thread group too large (S=%d, rows=%d)", S, R);
+    smem = wbytes + (size_t)GRID_STAGE * (4 + 4 + 8 + 8 + 8);
+    fn = p->kd.sep ? grid_kernel_for<true>(R) : grid_kernel_for<false>(R);
+    CG_REQUIRE(fn, "no gridder for %d rows per thread", R);
+    shared = ngroups > 1;
+    args[0] = &A;
+    args[1] = &gsize;
+    args[2] = &ngroups;
+    args[3] = &mode;
+    args[4] = &shared;
+    args[5] = &kt;
+    args[6] = &vv;
+    args[7] = (void *)&weight;
+    args[8] = &gg;
+  }
   CG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
   CG_REQUIRE(per_sm > 0, "gridder does not fit on an SM (smem %zu)", smem);
   int64_t blocks = std::min<int64_t>((int64_t)per_sm * num_sms(), p->max_items);
   CG_CUDA(cudaMemsetAsync(p->ticket, 0, sizeof(int32_t), s));
-  fn<<<(unsigned)blocks, threads, smem, s>>>(A, (const float2 *)ktab, (const float2 *)vis,
-                                              weight, (float2 *)grid);
-  CG_LAUNCH("grid");
+  CG_CUDA(cudaLaunchKernel(fn, dim3((unsigned)blocks), dim3(threads), args, smem, s));
   return CG_OK;
 }
 

@@ -69,19 +69,18 @@ __device__ __forceinline__ C cconj_add(C a, C b) {  // a + conj(b)
 }
 
 // ---------------------------------------------------------------- weights
-__global__ void k_weight_count(const double *uvw, int64_t stride, double lam,
+__global__ void k_weight_count(const double *uvw, int64_t stride, double lam, AxisConst k,
                                int64_t n, int N, int32_t *counts, int32_t *status) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double pu = vis_coord(uvw, stride, i, 0, lam);
-  const double pv = vis_coord(uvw, stride, i, 1, lam);
-  if (!(in_unit_range(pu) && in_unit_range(pv))) {
+  const double u = uvw[i * stride], v = uvw[i * stride + 1];
+  if (!(unit_range_fast(u, lam, k.inv_lam) && unit_range_fast(v, lam, k.inv_lam))) {
     atomicAdd(&status[ST_RANGE], 1);
     return;
   }
   int x, xf, y, yf;
-  frac_coord(pu, N, 1, x, xf);
-  frac_coord(pv, N, 1, y, yf);
+  frac_coord_fast(u, lam, k, N, 1, x, xf);
+  frac_coord_fast(v, lam, k, N, 1, y, yf);
   if (x < 0 || x >= N || y < 0 || y >= N) {
     atomicAdd(&status[ST_INDEX], 1);
     return;
@@ -89,7 +88,7 @@ __global__ void k_weight_count(const double *uvw, int64_t stride, double lam,
   atomicAdd(&counts[(size_t)x * N + y], 1);  // gw[x, y] as the reference indexes it
 }
 
-__global__ void k_weight_apply(const double *uvw, int64_t stride, double lam,
+__global__ void k_weight_apply(const double *uvw, int64_t stride, double lam, AxisConst k,
                                int64_t n, int N, const int32_t *counts,
                                const double *v_in, double *w_out,
                                const int32_t *status) {
@@ -97,8 +96,8 @@ __global__ void k_weight_apply(const double *uvw, int64_t stride, double lam,
   if (i >= n) return;
   if ((status[ST_RANGE] | status[ST_INDEX]) != 0) return;
   int x, xf, y, yf;
-  frac_coord(vis_coord(uvw, stride, i, 0, lam), N, 1, x, xf);
-  frac_coord(vis_coord(uvw, stride, i, 1, lam), N, 1, y, yf);
+  frac_coord_fast(uvw[i * stride], lam, k, N, 1, x, xf);
+  frac_coord_fast(uvw[i * stride + 1], lam, k, N, 1, y, yf);
   const double v = v_in ? v_in[i] : 1.0;
   w_out[i] = v / (double)counts[(size_t)x * N + y];
 }
@@ -293,8 +292,10 @@ int cg_weights(const double *uvw, int64_t stride, double lam, int64_t n, int N,
   if (n == 0) return CG_OK;
   CG_CUDA(cudaMemsetAsync(counts, 0, (size_t)N * N * sizeof(int32_t), s));
   const unsigned blocks = (unsigned)((n + 255) / 256);
-  k_weight_count<<<blocks, 256, 0, s>>>(uvw, stride, lam, n, N, counts, d_status);
-  k_weight_apply<<<blocks, 256, 0, s>>>(uvw, stride, lam, n, N, counts, v_in, w_out, d_status);
+  const AxisConst k = axis_const(N, 1, lam);
+  k_weight_count<<<blocks, 256, 0, s>>>(uvw, stride, lam, k, n, N, counts, d_status);
+  k_weight_apply<<<blocks, 256, 0, s>>>(uvw, stride, lam, k, n, N, counts, v_in, w_out,
+                                        d_status);
   CG_LAUNCH("weights");
   return CG_OK;
 }

@@ -118,7 +118,10 @@ struct CoordParams {
   int64_t n;
   int H, W, Q, S, G, sep;
   const int32_t *kidx;
-  int mode, T, ntx, nbuckets;
+  int mode, T, ntx, nbuckets, sublog;
+  AxisConst ax, ay;    // filtered-exact constants for x (width W) and y (height H)
+  double wstep, inv_wstep;  // wstep != 0: the kernel group is the w bin - kmin
+  int kmin, nk;
   VisRec *rec;
   int32_t *key;
   int32_t *rank;
@@ -139,6 +142,27 @@ __device__ __forceinline__ int aggregated_slot(int32_t *hist, int key,
   return base + __popc(peers & ((1u << lane) - 1u));
 }
 
+// Interleave the low 8 bits of x and y (Morton / Z order).
+__device__ __forceinline__ int morton2(int x, int y) {
+  unsigned a = (unsigned)x & 0xffu, b = (unsigned)y & 0xffu;
+  a = (a | (a << 4)) & 0x0f0fu;
+  a = (a | (a << 2)) & 0x3333u;
+  a = (a | (a << 1)) & 0x5555u;
+  b = (b | (b << 4)) & 0x0f0fu;
+  b = (b | (b << 2)) & 0x3333u;
+  b = (b | (b << 1)) & 0x5555u;
+  return (int)(a | (b << 1));
+}
+
+// Tiled-mode bucket: tile, then the 4x4-cell sub-tile of the footprint
+// origin along a Morton curve, so that consecutive visibilities of a work
+// item are spatial neighbours.
+__device__ __forceinline__ int tile_bucket(const CoordParams &P, int x0, int y0) {
+  const int ty = y0 / P.T, tx = x0 / P.T;
+  const int ly = y0 - ty * P.T, lx = x0 - tx * P.T;
+  return ((ty * P.ntx + tx) << (2 * P.sublog)) | morton2(lx >> 2, ly >> 2);
+}
+
 __global__ void k_plan_coords(CoordParams P) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool live = i < P.n;
@@ -146,21 +170,26 @@ __global__ void k_plan_coords(CoordParams P) {
   int key = -1;
   VisRec r = {0, 0, 0, 0};
   if (live) {
-    double pu = vis_coord(P.uvw, P.stride, i, 0, P.lam);
-    double pv = vis_coord(P.uvw, P.stride, i, 1, P.lam);
-    if (!(in_unit_range(pu) && in_unit_range(pv))) {
+    const double u = P.uvw[i * P.stride], v = P.uvw[i * P.stride + 1];
+    if (!(unit_range_fast(u, P.lam, P.ax.inv_lam) && unit_range_fast(v, P.lam, P.ay.inv_lam))) {
       atomicAdd(&P.status[ST_RANGE], 1);
       ok = false;
     } else {
       int x, xf, y, yf;
-      frac_coord(pu, P.W, P.Q, x, xf);
-      frac_coord(pv, P.H, P.Q, y, yf);
+      frac_coord_fast(u, P.lam, P.ax, P.W, P.Q, x, xf);
+      frac_coord_fast(v, P.lam, P.ay, P.H, P.Q, y, yf);
       int x0 = x - P.S / 2, y0 = y - P.S / 2;
       if (x0 < 0 || y0 < 0 || x0 + P.S > P.W || y0 + P.S > P.H) {
         atomicAdd(&P.status[ST_BOUNDS], 1);
         ok = false;
       }
-      int g = P.kidx ? P.kidx[i] : 0;
+      int g = 0;
+      if (P.wstep != 0.0) {
+        const double j = w_bin_fast(P.uvw[i * P.stride + 2], P.wstep, P.inv_wstep) - P.kmin;
+        g = (j >= 0.0 && j < (double)P.nk) ? (int)j : -1;
+      } else if (P.kidx) {
+        g = P.kidx[i];
+      }
       if (g < 0 || g >= P.G) {
         atomicAdd(&P.status[ST_INDEX], 1);
         ok = false;
@@ -174,8 +203,7 @@ __global__ void k_plan_coords(CoordParams P) {
         r.k0 = g;
         r.k1 = yf * P.Q + xf;
       }
-      if (ok)
-        key = (P.mode == CG_PLAN_TILED) ? (y0 / P.T) * P.ntx + (x0 / P.T) : g;
+      if (ok) key = (P.mode == CG_PLAN_TILED) ? tile_bucket(P, x0, y0) : g;
     }
   }
   int slot = aggregated_slot(P.hist, key, ok);
@@ -200,20 +228,23 @@ __global__ void k_plan_scatter(int64_t n, const VisRec *__restrict__ rec,
   perm[pos] = (int32_t)i;
 }
 
-__global__ void k_plan_items(int nb, const int32_t *__restrict__ counts,
+// Work items: each tile's sorted range (its 4^sublog sub-tile buckets are
+// contiguous) cut into pieces of at most `chunk` visibilities.
+__global__ void k_plan_items(int ntiles, int sublog, const int32_t *__restrict__ counts,
                              const int32_t *__restrict__ offsets, int chunk,
                              WorkItem *__restrict__ items,
                              int32_t *__restrict__ nitems) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nb) return;
-  int c = counts[b];
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const int b0 = t << (2 * sublog), b1 = b0 + (1 << (2 * sublog)) - 1;
+  const int off = offsets[b0];
+  const int c = offsets[b1] + counts[b1] - off;
   if (c == 0) return;
   int nch = (c + chunk - 1) / chunk;
   int base = atomicAdd(nitems, nch);
-  int off = offsets[b];
   for (int j = 0; j < nch; ++j) {
     WorkItem w;
-    w.tile = b;
+    w.tile = t;
     w.start = off + j * chunk;
     w.count = min(chunk, c - j * chunk);
     w.pad = 0;
@@ -222,17 +253,17 @@ __global__ void k_plan_items(int nb, const int32_t *__restrict__ counts,
 }
 
 __global__ void k_frac_coords(const double *uvw, int64_t stride, double lam,
-                              int64_t n, int H, int W, int Q, int32_t *x,
-                              int32_t *xf, int32_t *y, int32_t *yf,
+                              int64_t n, int H, int W, int Q, AxisConst ax, AxisConst ay,
+                              int32_t *x, int32_t *xf, int32_t *y, int32_t *yf,
                               int32_t *status) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double pu = vis_coord(uvw, stride, i, 0, lam);
-  double pv = vis_coord(uvw, stride, i, 1, lam);
-  if (!(in_unit_range(pu) && in_unit_range(pv))) atomicAdd(&status[ST_RANGE], 1);
+  const double u = uvw[i * stride], v = uvw[i * stride + 1];
+  if (!(unit_range_fast(u, lam, ax.inv_lam) && unit_range_fast(v, lam, ay.inv_lam)))
+    atomicAdd(&status[ST_RANGE], 1);
   int a, b, c, d;
-  frac_coord(pu, W, Q, a, b);
-  frac_coord(pv, H, Q, c, d);
+  frac_coord_fast(u, lam, ax, W, Q, a, b);
+  frac_coord_fast(v, lam, ay, H, Q, c, d);
   x[i] = a;
   xf[i] = b;
   y[i] = c;
@@ -243,10 +274,10 @@ __global__ void k_frac_coords(const double *uvw, int64_t stride, double lam,
 // w_cache_imaging's bin (synthesis.py:793): wbin = wstep * round(w / wstep),
 // half-to-even.  k = rint(w / wstep) is the bin number.
 __global__ void k_w_bins(const double *uvw, int64_t stride, int64_t n, double wstep,
-                         int32_t *kidx, int32_t *minmax, int32_t *status) {
+                         double inv_wstep, int32_t *kidx, int32_t *minmax, int32_t *status) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double k = rint(__ddiv_rn(uvw[i * stride + 2], wstep));
+  const double k = w_bin_fast(uvw[i * stride + 2], wstep, inv_wstep);
   if (!(k > -1.0e9 && k < 1.0e9)) {
     atomicAdd(&status[ST_RANGE], 1);
     kidx[i] = 0;
@@ -265,10 +296,11 @@ __global__ void k_w_bins_rebase(int32_t *kidx, int64_t n, const int32_t *minmax)
 
 // Bins against a known table range [kmin, kmin + nk): no host round trip.
 __global__ void k_w_bins_fixed(const double *uvw, int64_t stride, int64_t n, double wstep,
-                               int kmin, int nk, int32_t *kidx, int32_t *status) {
+                               double inv_wstep, int kmin, int nk, int32_t *kidx,
+                               int32_t *status) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double k = rint(__ddiv_rn(uvw[i * stride + 2], wstep));
+  const double k = w_bin_fast(uvw[i * stride + 2], wstep, inv_wstep);
   const double j = k - (double)kmin;
   if (!(j >= 0.0 && j < (double)nk)) {
     atomicAdd(&status[ST_INDEX], 1);
@@ -289,6 +321,8 @@ struct Layout {
 };
 
 static int tile_edge(int S) {
+  const cg_tuning t = tuning();
+  if (t.tile > 0) return std::max(4, std::min(64, t.tile & ~3));
   if (S <= 8) return 32;
   if (S <= 16) return 48;
   return 64;
@@ -299,12 +333,20 @@ static void plan_geometry(cg_plan &p) {
     p.T = tile_edge(p.kd.S);
     p.ntx = (p.W + p.T - 1) / p.T;
     p.nty = (p.H + p.T - 1) / p.T;
-    p.nbuckets = p.ntx * p.nty;
+    p.ntiles = p.ntx * p.nty;
+    p.sublog = 0;
+    while ((4 << p.sublog) < p.T) ++p.sublog;  // 4x4 sub-tiles, 2^sublog per tile edge
+    p.nbuckets = p.ntiles << (2 * p.sublog);
     p.win = p.T + p.kd.S - 1;
-    p.pitch = (p.win + 1) & ~1;
+    // pitch = S (mod 16): the taps t = dy*S + dx of consecutive lanes fall on
+    // consecutive 8-byte bank pairs of the window (no bank conflicts)
+    p.pitch = p.win;
+    while ((p.pitch - p.kd.S) % 16 != 0) ++p.pitch;
+    const cg_tuning t = tuning();
     int64_t want = p.n / (int64_t)(num_sms() * 16) + 1;
-    p.chunk = (int)std::min<int64_t>(2048, std::max<int64_t>(256, want));
-    p.max_items = (p.n + p.chunk - 1) / p.chunk + p.nbuckets;
+    p.chunk = t.chunk > 0 ? t.chunk
+                          : (int)std::min<int64_t>(2048, std::max<int64_t>(256, want));
+    p.max_items = (p.n + p.chunk - 1) / p.chunk + p.ntiles;
   } else {
     p.T = 0;
     p.ntx = p.nty = 0;
@@ -342,21 +384,25 @@ static int check_desc(const cg_kernel_desc *kd, int H, int W) {
   return CG_OK;
 }
 
-// Tiled plan built into a caller-provided struct: no host or device
-// allocation.  Used by the entry point for callers that cannot allocate.
-int plan_build_tiled_into(cg_plan *p, const cg_kernel_desc *kd, int H, int W,
-                          const double *uvw, int64_t stride, double lam,
-                          const int32_t *kidx, int64_t n, void *workspace,
-                          size_t workspace_bytes, int32_t *d_status, cudaStream_t s) {
+// Plan built into a caller-provided struct (no host or device allocation):
+// geometry, workspace layout, coordinates + histogram, scan, scatter and (tiled
+// mode) the work list.  wstep != 0 derives each visibility's kernel group
+// from its w bin (round(w / wstep) - kmin, synthesis.py:793) in the same pass.
+int plan_build_into(cg_plan *p, int mode, const cg_kernel_desc *kd, int H, int W,
+                    const double *uvw, int64_t stride, double lam, const int32_t *kidx,
+                    double wstep, int kmin, int64_t n, void *workspace, size_t workspace_bytes,
+                    int32_t *d_status, cudaStream_t s) {
   int rc = check_desc(kd, H, W);
   if (rc) return rc;
+  CG_REQUIRE(mode == CG_PLAN_TILED || mode == CG_PLAN_GROUPS, "bad plan mode %d", mode);
   CG_REQUIRE(n >= 0 && n < (int64_t)INT32_MAX, "visibility count %lld unsupported",
              (long long)n);
-  CG_REQUIRE(n == 0 || (uvw && stride >= 2), "uvw is NULL or stride < 2");
+  CG_REQUIRE(n == 0 || (uvw && stride >= (wstep != 0.0 ? 3 : 2)), "uvw is NULL or stride too small");
   CG_REQUIRE(d_status, "status block is NULL");
-  CG_REQUIRE(kd->G == 1 || kidx || n == 0, "G > 1 needs per-visibility kernel indices");
+  CG_REQUIRE(kd->G == 1 || kidx || wstep != 0.0 || n == 0,
+             "G > 1 needs per-visibility kernel indices");
   memset(p, 0, sizeof(*p));
-  p->mode = CG_PLAN_TILED;
+  p->mode = mode;
   p->kd = *kd;
   p->H = H;
   p->W = W;
@@ -395,10 +441,17 @@ int plan_build_tiled_into(cg_plan *p, const cg_kernel_desc *kd, int H, int W,
   P.G = kd->G;
   P.sep = kd->sep;
   P.kidx = kidx;
-  P.mode = CG_PLAN_TILED;
+  P.mode = mode;
   P.T = p->T;
   P.ntx = p->ntx;
   P.nbuckets = p->nbuckets;
+  P.sublog = p->sublog;
+  P.ax = axis_const(W, kd->Q, lam);
+  P.ay = axis_const(H, kd->Q, lam);
+  P.wstep = wstep;
+  P.inv_wstep = wstep != 0.0 ? 1.0 / wstep : 0.0;
+  P.kmin = kmin;
+  P.nk = kd->G;
   P.rec = rec_tmp;
   P.key = key;
   P.rank = rank;
@@ -410,9 +463,61 @@ int plan_build_tiled_into(cg_plan *p, const cg_kernel_desc *kd, int H, int W,
   rc = launch_scan(p->counts, p->offsets, p->nbuckets, (int32_t *)(ws + L.scan), s);
   if (rc) return rc;
   k_plan_scatter<<<blocks, 256, 0, s>>>(n, rec_tmp, key, rank, p->offsets, p->recs, p->perm);
-  k_plan_items<<<(p->nbuckets + 255) / 256, 256, 0, s>>>(p->nbuckets, p->counts, p->offsets,
-                                                         p->chunk, p->items, p->nitems);
+  if (mode == CG_PLAN_TILED)
+    k_plan_items<<<(p->ntiles + 255) / 256, 256, 0, s>>>(p->ntiles, p->sublog, p->counts,
+                                                          p->offsets, p->chunk, p->items,
+                                                          p->nitems);
   CG_LAUNCH("plan sort");
+  return CG_OK;
+}
+
+int plan_build_tiled_into(cg_plan *p, const cg_kernel_desc *kd, int H, int W,
+                          const double *uvw, int64_t stride, double lam,
+                          const int32_t *kidx, int64_t n, void *workspace,
+                          size_t workspace_bytes, int32_t *d_status, cudaStream_t s) {
+  return plan_build_into(p, CG_PLAN_TILED, kd, H, W, uvw, stride, lam, kidx, 0.0, 0, n,
+                         workspace, workspace_bytes, d_status, s);
+}
+
+// Heap plan; the groups form also copies the group ranges to the host.
+static int plan_create_heap(cg_plan **out, int mode, const cg_kernel_desc *kd, int H, int W,
+                            const double *uvw, int64_t stride, double lam, const int32_t *kidx,
+                            double wstep, int kmin, int64_t n, void *workspace,
+                            size_t workspace_bytes, int32_t *d_status, cudaStream_t s) {
+  CG_REQUIRE(out, "plan output pointer is NULL");
+  *out = nullptr;
+  cg_plan *p = new (std::nothrow) cg_plan;
+  CG_REQUIRE(p, "out of host memory");
+  int rc = plan_build_into(p, mode, kd, H, W, uvw, stride, lam, kidx, wstep, kmin, n, workspace,
+                           workspace_bytes, d_status, s);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  if (mode == CG_PLAN_GROUPS) {
+    p->h_counts = (int32_t *)malloc((size_t)p->nbuckets * 4);
+    p->h_offsets = (int32_t *)malloc((size_t)p->nbuckets * 4);
+    cudaError_t e = cudaSuccess;
+    if (!p->h_counts || !p->h_offsets) {
+      rc = set_error(CG_ERR_ARG, "out of host memory");
+    } else if (n == 0) {
+      memset(p->h_counts, 0, (size_t)p->nbuckets * 4);
+      memset(p->h_offsets, 0, (size_t)p->nbuckets * 4);
+    } else if ((e = cudaMemcpyAsync(p->h_counts, p->counts, (size_t)p->nbuckets * 4,
+                                    cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+               (e = cudaMemcpyAsync(p->h_offsets, p->offsets, (size_t)p->nbuckets * 4,
+                                    cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+               (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+      rc = cuda_error(e, "plan group readback");
+    }
+    if (rc) {
+      free(p->h_counts);
+      free(p->h_offsets);
+      delete p;
+      return rc;
+    }
+  }
+  *out = p;
   return CG_OK;
 }
 
@@ -441,112 +546,17 @@ int cg_plan_create(cg_plan **out, int mode, const cg_kernel_desc *kd, int H,
                    const int32_t *kidx, int64_t n, void *workspace,
                    size_t workspace_bytes, int32_t *d_status,
                    cg_stream_t stream) {
-  CG_REQUIRE(out, "plan output pointer is NULL");
-  *out = nullptr;
-  int rc = check_desc(kd, H, W);
-  if (rc) return rc;
-  CG_REQUIRE(mode == CG_PLAN_TILED || mode == CG_PLAN_GROUPS, "bad plan mode %d", mode);
-  CG_REQUIRE(n >= 0 && n < (int64_t)INT32_MAX, "visibility count %lld unsupported",
-             (long long)n);
-  CG_REQUIRE(n == 0 || (uvw && stride >= 2), "uvw is NULL or stride < 2");
-  CG_REQUIRE(d_status, "status block is NULL");
-  CG_REQUIRE(kd->G == 1 || kidx || n == 0, "G > 1 needs per-visibility kernel indices");
-  cudaStream_t s = (cudaStream_t)stream;
+  return plan_create_heap(out, mode, kd, H, W, uvw, stride, lam, kidx, 0.0, 0, n, workspace,
+                          workspace_bytes, d_status, (cudaStream_t)stream);
+}
 
-  cg_plan *p = new (std::nothrow) cg_plan;
-  CG_REQUIRE(p, "out of host memory");
-  memset(p, 0, sizeof(*p));
-  p->mode = mode;
-  p->kd = *kd;
-  p->H = H;
-  p->W = W;
-  p->n = n;
-  plan_geometry(*p);
-  Layout L = layout_of(*p);
-  if (!workspace || workspace_bytes < L.total) {
-    delete p;
-    return set_error(CG_ERR_WORKSPACE, "plan needs %zu workspace bytes, got %zu",
-                     L.total, workspace_bytes);
-  }
-  char *ws = (char *)workspace;
-  VisRec *rec_tmp = (VisRec *)(ws + L.rec_tmp);
-  int32_t *key = (int32_t *)(ws + L.key);
-  int32_t *rank = (int32_t *)(ws + L.rank);
-  p->recs = (VisRec *)(ws + L.recs);
-  p->perm = (int32_t *)(ws + L.perm);
-  p->counts = (int32_t *)(ws + L.counts);
-  p->offsets = (int32_t *)(ws + L.offsets);
-  p->items = (WorkItem *)(ws + L.items);
-  int32_t *ctr = (int32_t *)(ws + L.ctr);
-  p->nitems = ctr;
-  p->ticket = ctr + 1;
-  p->status = d_status;
-
-  auto fail = [&](int code) {
-    delete p;
-    return code;
-  };
-  if (cudaMemsetAsync(p->counts, 0, (size_t)p->nbuckets * 4, s) != cudaSuccess ||
-      cudaMemsetAsync(ctr, 0, 16, s) != cudaSuccess)
-    return fail(cuda_error(cudaGetLastError(), "plan memset"));
-  if (n > 0) {
-    CoordParams P;
-    P.uvw = uvw;
-    P.stride = stride;
-    P.lam = lam;
-    P.n = n;
-    P.H = H;
-    P.W = W;
-    P.Q = kd->Q;
-    P.S = kd->S;
-    P.G = kd->G;
-    P.sep = kd->sep;
-    P.kidx = kidx;
-    P.mode = mode;
-    P.T = p->T;
-    P.ntx = p->ntx;
-    P.nbuckets = p->nbuckets;
-    P.rec = rec_tmp;
-    P.key = key;
-    P.rank = rank;
-    P.hist = p->counts;
-    P.status = d_status;
-    int blocks = (int)((n + 255) / 256);
-    k_plan_coords<<<blocks, 256, 0, s>>>(P);
-    if (cudaGetLastError() != cudaSuccess) return fail(cuda_error(cudaGetLastError(), "coords"));
-    int rc2 = launch_scan(p->counts, p->offsets, p->nbuckets,
-                          (int32_t *)(ws + L.scan), s);
-    if (rc2) return fail(rc2);
-    k_plan_scatter<<<blocks, 256, 0, s>>>(n, rec_tmp, key, rank, p->offsets,
-                                          p->recs, p->perm);
-    if (mode == CG_PLAN_TILED)
-      k_plan_items<<<(p->nbuckets + 255) / 256, 256, 0, s>>>(
-          p->nbuckets, p->counts, p->offsets, p->chunk, p->items, p->nitems);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(cuda_error(e, "plan sort"));
-  }
-  if (mode == CG_PLAN_GROUPS) {
-    p->h_counts = (int32_t *)malloc((size_t)p->nbuckets * 4);
-    p->h_offsets = (int32_t *)malloc((size_t)p->nbuckets * 4);
-    if (!p->h_counts || !p->h_offsets) {
-      free(p->h_counts);
-      free(p->h_offsets);
-      return fail(set_error(CG_ERR_ARG, "out of host memory"));
-    }
-    cudaError_t e1 = cudaMemcpyAsync(p->h_counts, p->counts, (size_t)p->nbuckets * 4,
-                                     cudaMemcpyDeviceToHost, s);
-    cudaError_t e2 = cudaMemcpyAsync(p->h_offsets, p->offsets, (size_t)p->nbuckets * 4,
-                                     cudaMemcpyDeviceToHost, s);
-    cudaError_t e3 = cudaStreamSynchronize(s);
-    if (e1 || e2 || e3) {
-      free(p->h_counts);
-      free(p->h_offsets);
-      return fail(cuda_error(e1 ? e1 : e2 ? e2 : e3, "plan group readback"));
-    }
-    if (n == 0) memset(p->h_counts, 0, (size_t)p->nbuckets * 4);
-  }
-  *out = p;
-  return CG_OK;
+int cg_plan_create_wbins(cg_plan **out, int mode, const cg_kernel_desc *kd, int H, int W,
+                         const double *uvw, int64_t stride, double lam, double wstep, int kmin,
+                         int64_t n, void *workspace, size_t workspace_bytes,
+                         int32_t *d_status, cg_stream_t stream) {
+  CG_REQUIRE(wstep != 0.0, "wstep must be non-zero");
+  return plan_create_heap(out, mode, kd, H, W, uvw, stride, lam, nullptr, wstep, kmin, n,
+                          workspace, workspace_bytes, d_status, (cudaStream_t)stream);
 }
 
 int cg_plan_destroy(cg_plan *p) {
@@ -575,7 +585,7 @@ int cg_w_bins(const double *uvw, int64_t stride, int64_t n, double wstep, int32_
   cudaStream_t s = (cudaStream_t)stream;
   const unsigned blocks = (unsigned)((n + 255) / 256);
   k_minmax_init<<<1, 1, 0, s>>>(d_minmax);
-  k_w_bins<<<blocks, 256, 0, s>>>(uvw, stride, n, wstep, kidx, d_minmax, d_status);
+  k_w_bins<<<blocks, 256, 0, s>>>(uvw, stride, n, wstep, 1.0 / wstep, kidx, d_minmax, d_status);
   k_w_bins_rebase<<<blocks, 256, 0, s>>>(kidx, n, d_minmax);
   CG_LAUNCH("w_bins");
   CG_CUDA(cudaMemcpyAsync(h_minmax, d_minmax, 8, cudaMemcpyDeviceToHost, s));
@@ -590,7 +600,7 @@ int cg_w_bins_fixed(const double *uvw, int64_t stride, int64_t n, double wstep, 
   CG_REQUIRE(wstep != 0.0, "wstep must be non-zero");
   if (n == 0) return CG_OK;
   k_w_bins_fixed<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-      uvw, stride, n, wstep, kmin, nk, kidx, d_status);
+      uvw, stride, n, wstep, 1.0 / wstep, kmin, nk, kidx, d_status);
   CG_LAUNCH("w_bins_fixed");
   return CG_OK;
 }
@@ -603,7 +613,8 @@ int cg_frac_coords(const double *uvw, int64_t stride, double lam, int64_t n,
              "NULL argument");
   if (n == 0) return CG_OK;
   k_frac_coords<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-      uvw, stride, lam, n, H, W, Q, x, xf, y, yf, d_status);
+      uvw, stride, lam, n, H, W, Q, axis_const(W, Q, lam), axis_const(H, Q, lam), x, xf, y,
+      yf, d_status);
   CG_LAUNCH("frac_coords");
   return CG_OK;
 }

@@ -134,7 +134,10 @@ class Plan:
     ``uvw`` is a float64 CUDA tensor [n, >=2] (rows in units such that
     uvw / lam is the fraction of the grid), ``shape`` the grid (H, W)."""
 
-    def __init__(self, uvw, lam, shape, ktab, kidx=None, mode=L.CG_PLAN_TILED, status=None):
+    def __init__(self, uvw, lam, shape, ktab, kidx=None, mode=L.CG_PLAN_TILED, status=None,
+                 wbins=None):
+        """wbins=(wstep, kmin): take each visibility's kernel group from its w bin
+        (round(w / wstep) - kmin) inside the plan's coordinate pass."""
         require_cuda()
         self.uvw = cuda_tensor(uvw, torch.float64)
         if self.uvw.dim() != 2 or self.uvw.shape[1] < 2:
@@ -155,9 +158,15 @@ class Plan:
         if status is None:
             self.status.reset()
         h = ctypes.c_void_p()
-        L.call("cg_plan_create", ctypes.byref(h), mode, ctypes.byref(kd), self.shape[0],
-               self.shape[1], _p(self.uvw), self.uvw.stride(0), float(lam), _p(self.kidx),
-               self.n, _p(self.ws), nbytes, _p(self.status.t), stream())
+        if wbins is not None:
+            L.call("cg_plan_create_wbins", ctypes.byref(h), mode, ctypes.byref(kd),
+                   self.shape[0], self.shape[1], _p(self.uvw), self.uvw.stride(0), float(lam),
+                   float(wbins[0]), int(wbins[1]), self.n, _p(self.ws), nbytes,
+                   _p(self.status.t), stream())
+        else:
+            L.call("cg_plan_create", ctypes.byref(h), mode, ctypes.byref(kd), self.shape[0],
+                   self.shape[1], _p(self.uvw), self.uvw.stride(0), float(lam), _p(self.kidx),
+                   self.n, _p(self.ws), nbytes, _p(self.status.t), stream())
         self.handle = h
         self._fin = weakref.finalize(self, L.lib().cg_plan_destroy, h)
 

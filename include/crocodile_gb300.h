@@ -91,6 +91,27 @@ typedef struct {
   int G;
 } cg_kernel_desc;
 
+/* Launch-shape tuning of the tiled kernels (no reference counterpart; the
+ * autotuner in crocodile_gb300/autotune.py sets it).  Zero fields mean
+ * "automatic".  tile: grid tile edge in cells (multiple of 4, <= 64; read
+ * when a plan is created); chunk: visibilities per work item (plan
+ * creation); layout: gridder layout, CG_LAYOUT_WARP (one warp per
+ * visibility, shared-memory atomics) or CG_LAYOUT_OWNER (threads own window
+ * cells by position mod S and keep running sums in registers); rows: row
+ * residues per owner-layout thread (1..8); groups: owner-layout thread
+ * groups, or warp-layout warps, per CTA (1..8).  Process-wide. */
+#define CG_LAYOUT_WARP 1
+#define CG_LAYOUT_OWNER 2
+typedef struct {
+  int tile;
+  int chunk;
+  int rows;
+  int groups;
+  int layout;
+} cg_tuning;
+int cg_set_tuning(const cg_tuning *t);
+int cg_get_tuning(cg_tuning *out);
+
 /* A plan holds the visibilities' bit-exact cell assignment, their order
  * (sorted into grid tiles, or into kernel groups for the plain FP64 form)
  * and the work list of the gridding kernels.  It lives in a caller-owned
@@ -111,6 +132,16 @@ int cg_plan_create(cg_plan **plan, int mode, const cg_kernel_desc *kd, int H,
                    const int32_t *kidx, int64_t n, void *workspace,
                    size_t workspace_bytes, int32_t *d_status,
                    cg_stream_t stream);
+/* Same, with each visibility's kernel group taken from its w bin:
+ * g = round(w / wstep) - kmin (w = uvw[i*stride+2], stride >= 3), the
+ * binning of w_cache_imaging (synthesis.py:793) fused into the plan's
+ * coordinate pass; kd->G is the number of bins in the kernel table and bins
+ * outside [kmin, kmin + G) are index errors. */
+int cg_plan_create_wbins(cg_plan **plan, int mode, const cg_kernel_desc *kd,
+                         int H, int W, const double *uvw, int64_t stride,
+                         double lam, double wstep, int kmin, int64_t n,
+                         void *workspace, size_t workspace_bytes,
+                         int32_t *d_status, cg_stream_t stream);
 int cg_plan_destroy(cg_plan *plan);
 /* Tile edge (cells) and number of work items upper bound, for reports. */
 int cg_plan_info(const cg_plan *plan, int64_t *info_out /* [4] */);

@@ -97,3 +97,23 @@ def test_host_helpers_match_oracle():
     lo, mo = O.kernel_coordinates(16, 0.1, 0.01, -0.02, numpy.array([[1, .1], [.2, 1]]))
     assert numpy.array_equal(l, lo) and numpy.array_equal(m, mo)
     assert numpy.array_equal(S.anti_aliasing_function(16, 0, 5), O.anti_aliasing_function(16, 0, 5))
+
+
+def test_tuning_roundtrip_and_validation(libpath):
+    from crocodile_gb300 import _lib, autotune
+    try:
+        autotune.set_tuning(tile=32, chunk=700, rows=3, groups=2, layout=_lib.CG_LAYOUT_OWNER)
+        assert autotune.get_tuning() == {"tile": 32, "chunk": 700, "rows": 3, "groups": 2,
+                                         "layout": 2}
+        for bad in ({"tile": 30}, {"tile": 68}, {"rows": 9}, {"groups": 9}, {"layout": 3}):
+            with pytest.raises(ValueError):
+                autotune.set_tuning(**bad)
+    finally:
+        autotune.set_tuning()
+    assert autotune.get_tuning() == {"tile": 0, "chunk": 0, "rows": 0, "groups": 0, "layout": 0}
+    cands = autotune.candidates(15)
+    assert any(c["layout"] == 1 for c in cands) and any(c["layout"] == 2 for c in cands)
+    for c in cands:
+        if c["layout"] == 2:
+            gpad = (15 * ((15 + c["rows"] - 1) // c["rows"]) + 31) // 32 * 32
+            assert gpad * c["groups"] <= 256

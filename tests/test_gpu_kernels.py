@@ -1,0 +1,157 @@
+"""GPU checks of the kernels' internal choices: the filtered-exact coordinate
+path at rounding boundaries, every gridder launch shape, and the fused w-bin
+plan, each against the CPU oracle."""
+
+import ctypes
+
+import numpy
+import pytest
+from numpy.testing import assert_array_equal
+
+pytestmark = pytest.mark.gpu
+
+FP32_TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def env():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from crocodile_gb300 import autotune, engine, synthesis
+    from oracle import crocodile_oracle
+    yield torch, engine, synthesis, autotune, crocodile_oracle
+    autotune.set_tuning()
+
+
+def rel(a, b):
+    return numpy.linalg.norm(numpy.asarray(a) - numpy.asarray(b)) / numpy.linalg.norm(b)
+
+
+def test_frac_coord_at_rounding_boundaries(env):
+    """Coordinates whose scaled value (-(N//2 + p*N))*Q lies exactly on, or one ulp
+    around, a half-integer: the fast estimate must defer to the exact sequence."""
+    torch, E, S, A, O = env
+    for N, Q, lam in ((1024, 8, 12800.0), (4096, 8, 40960.0), (8192, 16, 163840.0),
+                      (97, 3, 1212.5), (5, 4, 6.0)):
+        k = numpy.arange(-N * Q // 2, N * Q // 2, max(1, N * Q // 4096))
+        p = (k + 0.5) / (N * Q)          # exact half-steps of the oversampled grid
+        p = numpy.concatenate([p, numpy.nextafter(p, 1), numpy.nextafter(p, -1), k / (N * Q)])
+        p = p[(p >= -0.5) & (p < 0.5)]
+        q = numpy.random.default_rng(N).permutation(p)
+        pq = numpy.column_stack([p, q, numpy.zeros_like(p)])
+        got = S.frac_coords((N, N), Q, pq)
+        exp = O.frac_coords((N, N), Q, pq)
+        for g, e in zip(got, exp):
+            assert_array_equal(g, e)
+        # and through lam (device division) in the plan path, for the rows whose
+        # u / lam and v / lam stay inside [-0.5, 0.5)
+        uvw = pq * lam
+        inside = ((uvw[:, :2] / lam >= -0.5) & (uvw[:, :2] / lam < 0.5)).all(axis=1)
+        uvw = uvw[inside]
+        st = E.Status()
+        got = E.frac_coords(uvw, lam, (N, N), Q, st)
+        st.check()
+        exp = O.frac_coords((N, N), Q, uvw / lam)
+        for g, e in zip(got, exp):
+            assert_array_equal(g.cpu().numpy(), e)
+
+
+def test_w_bins_at_rounding_boundaries(env):
+    torch, E, S, A, O = env
+    wstep = 10.0
+    w = numpy.concatenate([(numpy.arange(-60, 60) + 0.5) * wstep,
+                           numpy.nextafter((numpy.arange(-60, 60) + 0.5) * wstep, 1e9),
+                           numpy.random.default_rng(1).uniform(-600, 600, 1000)])
+    uvw = numpy.column_stack([numpy.zeros_like(w), numpy.zeros_like(w), w])
+    st = E.Status()
+    kidx, kmin, kmax = E.w_bins(uvw, wstep, st)
+    st.check()
+    k = numpy.round(w / wstep).astype(int)
+    assert (kmin, kmax) == (k.min(), k.max())
+    assert_array_equal(kidx.cpu().numpy(), k - k.min())
+
+
+def _wproj_case(O, n=20000, N=256, seed=5):
+    rng = numpy.random.default_rng(seed)
+    theta = 0.1
+    lam = N / theta
+    r = rng.uniform(0, 0.45 * lam, n)
+    ph = rng.uniform(0, 2 * numpy.pi, n)
+    uvw = numpy.column_stack([r * numpy.cos(ph), r * numpy.sin(ph), rng.uniform(-200, 200, n)])
+    vis = rng.normal(size=n) + 1j * rng.normal(size=n)
+    return theta, lam, uvw, vis
+
+
+@pytest.mark.parametrize("cfg", [
+    {"layout": 1, "groups": 8, "tile": 32},
+    {"layout": 1, "groups": 4, "tile": 16, "chunk": 64},
+    {"layout": 2, "rows": 1, "groups": 1, "tile": 48},
+    {"layout": 2, "rows": 3, "groups": 2, "tile": 32},
+    {"layout": 2, "rows": 4, "groups": 4, "tile": 24, "chunk": 100},
+    {"layout": 2, "rows": 5, "groups": 1, "tile": 64},
+    {"layout": 2, "rows": 8, "groups": 1, "tile": 32},
+])
+def test_gridder_shapes_match_oracle(env, cfg):
+    torch, E, S, A, O = env
+    theta, lam, uvw, vis = _wproj_case(O)
+    kw = dict(NpixFF=32, NpixKern=15, Qpx=4)
+    ref = O.w_cache_imaging(theta, lam, uvw, None, vis, wstep=20.0, **kw)
+    vref = O.w_cache_predict(theta, lam, uvw, None, ref, wstep=20.0, **kw)
+    A.set_tuning(**cfg)
+    try:
+        got = S.w_cache_imaging(theta, lam, uvw, None, vis, wstep=20.0, **kw)
+        vgot = S.w_cache_predict(theta, lam, uvw, None, ref, wstep=20.0, **kw)
+    finally:
+        A.set_tuning()
+    assert rel(got, ref) < FP32_TOL
+    assert rel(vgot, vref) < FP32_TOL
+
+
+@pytest.mark.parametrize("S_,sep", [(8, True), (8, False), (7, False), (16, False)])
+def test_supports_and_separable(env, S_, sep):
+    torch, E, S, A, O = env
+    rng = numpy.random.default_rng(S_)
+    N, n, theta, Q = 128, 5000, 0.1, 4
+    lam = N / theta
+    uvw = numpy.column_stack([rng.uniform(-0.4, 0.4, (n, 2)) * lam, numpy.zeros(n)])
+    vis = rng.normal(size=n) + 1j * rng.normal(size=n)
+    aa = O.anti_aliasing_function(N, 0, 6)
+    kv = O.kernel_oversample(aa, Q, S_) if sep else \
+        O.kernel_oversample(numpy.outer(aa, aa), Q, S_)
+    for layout in (1, 2):
+        A.set_tuning(layout=layout)
+        try:
+            g = S.conv_imaging(theta, lam, uvw, None, vis, kv)
+            v = S.conv_predict(theta, lam, uvw, None, g, kv)
+        finally:
+            A.set_tuning()
+        assert rel(g, O.conv_imaging(theta, lam, uvw, None, vis, kv)) < FP32_TOL
+        assert rel(v, O.conv_predict(theta, lam, uvw, None, g, kv)) < FP32_TOL
+
+
+def test_fused_wbin_plan(env):
+    torch, E, S, A, O = env
+    theta, lam, uvw, vis = _wproj_case(O, n=30000, N=512, seed=9)
+    kw = dict(NpixFF=32, NpixKern=9, Qpx=4)
+    N = int(round(theta * lam))
+    ref = O.w_cache_imaging(theta, lam, uvw, None, vis, wstep=15.0, **kw)
+    st = E.Status()
+    uvw_t = E.cuda_tensor(uvw, torch.float64)
+    kidx, kmin, kmax = E.w_bins(uvw_t, 15.0, st)
+    table = E.w_kernels(theta, 15.0 * numpy.arange(kmin, kmax + 1).astype(float), 32, 9, 4)
+    kt = E.KernelTable(table.reshape(-1), False, 4, 9)
+    plan = E.Plan(uvw_t, lam, (N, N), kt, status=st, wbins=(15.0, kmin))
+    g = torch.zeros((N, N), dtype=E.CF, device="cuda")
+    plan.grid(kt, E.cuda_tensor(vis, E.CF), g)
+    plan.check()
+    assert rel(g.cpu().numpy(), ref) < FP32_TOL
+    # a table that misses bins is an index error and leaves the grid untouched
+    st2 = E.Status()
+    small = E.KernelTable(table[1:].reshape(-1), False, 4, 9)
+    plan = E.Plan(uvw_t, lam, (N, N), small, status=st2, wbins=(15.0, kmin + 1))
+    g2 = torch.zeros((N, N), dtype=E.CF, device="cuda")
+    plan.grid(small, E.cuda_tensor(vis, E.CF), g2)
+    with pytest.raises(IndexError):
+        plan.check()
+    assert float(g2.abs().sum()) == 0.0
