@@ -32,6 +32,10 @@ CG_LAYOUT_WARP = 1
 CG_LAYOUT_OWNER = 2
 
 
+class PlanOpts(ctypes.Structure):
+    _fields_ = [("layers", c_int), ("layer", c_void_p), ("wstep", c_double), ("kmin", c_int)]
+
+
 class KernelDesc(ctypes.Structure):
     _fields_ = [("sep", c_int), ("Q", c_int), ("S", c_int), ("G", c_int)]
 
@@ -56,6 +60,13 @@ SIGNATURES = {
     "cg_plan_create_wbins": (c_int, [ctypes.POINTER(P), c_int, ctypes.POINTER(KernelDesc), c_int,
                                      c_int, P, c_int64, c_double, c_double, c_int, c_int64, P,
                                      c_size_t, P, P]),
+    "cg_plan_workspace_bytes_ex": (c_size_t, [c_int, c_int64, c_int, c_int,
+                                              ctypes.POINTER(KernelDesc), ctypes.POINTER(PlanOpts)]),
+    "cg_plan_create_ex": (c_int, [ctypes.POINTER(P), c_int, ctypes.POINTER(KernelDesc), c_int,
+                                  c_int, P, c_int64, c_double, P, c_int64,
+                                  ctypes.POINTER(PlanOpts), P, c_size_t, P, P]),
+    "cg_plan_layer_mean_w": (c_int, [P, P, c_int64, P, P, P]),
+    "cg_wstack_combine": (c_int, [P, c_int, c_int, c_double, P, P, P, P, P]),
     "cg_plan_destroy": (c_int, [P]),
     "cg_set_tuning": (c_int, [ctypes.POINTER(Tuning)]),
     "cg_get_tuning": (c_int, [ctypes.POINTER(Tuning)]),

@@ -154,8 +154,11 @@ struct cg_plan {
   int win;      // window edge = T + S - 1
   int pitch;    // smem row pitch (even)
   int nbuckets;
-  int ntiles;   // tiled mode: tiles; each tile holds 4^sublog sub-tile buckets
-  int sublog;   // sub-tiles are 4x4 cells, ordered along a Morton curve in the tile
+  int layers;   // stacked grids (w-stacking planes); a grid of H*W cells each
+  int tpl;      // tiles per layer (ntx * nty)
+  int ntiles;   // tiled mode: tiles of all layers; each holds 4^sublog sub-tile buckets
+  int sublog;   // 2^sublog sub-tiles per tile edge, ordered along a Morton curve
+  int subshift; // sub-tile edge = 1 << subshift cells (4, or more for huge grid stacks)
   int64_t max_items;
   int chunk;    // visibilities per work item
   // device arrays inside the caller's workspace

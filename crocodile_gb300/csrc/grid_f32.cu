@@ -30,8 +30,22 @@ struct TiledArgs {
   const int32_t *nitems;
   int32_t *ticket;
   const int32_t *status;
-  int H, W, S, Q, T, ntx, win, pitch;
+  int H, W, S, Q, T, ntx, tpl, win, pitch;
 };
+
+// Window origin of a work item's tile and the offset of its layer's grid.
+struct TileOrigin {
+  int wx0, wy0;
+  size_t layer_off;
+};
+__device__ __forceinline__ TileOrigin tile_origin(const TiledArgs &A, int tile) {
+  const int lyr = tile / A.tpl, t = tile - lyr * A.tpl;
+  TileOrigin o;
+  o.wx0 = (t % A.ntx) * A.T;
+  o.wy0 = (t / A.ntx) * A.T;
+  o.layer_off = (size_t)lyr * A.H * A.W;
+  return o;
+}
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -94,7 +108,8 @@ __global__ void __launch_bounds__(256) k_grid_tiled(
   int it;
   while ((it = next_item(A, &s_item)) >= 0) {
     const WorkItem w = A.items[it];
-    const int wx0 = (w.tile % A.ntx) * A.T, wy0 = (w.tile / A.ntx) * A.T;
+    const TileOrigin org = tile_origin(A, w.tile);
+    const int wx0 = org.wx0, wy0 = org.wy0;
     for (int c = tid; c < pitch * A.win; c += blockDim.x) win[c] = make_float2(0.f, 0.f);
 
     int cur[R];
@@ -200,7 +215,7 @@ __global__ void __launch_bounds__(256) k_grid_tiled(
       const float2 val = win[r * pitch + q];
       if (val.x != 0.f || val.y != 0.f) {
         const int gy = wy0 + r, gx = wx0 + q;
-        if (gy < A.H && gx < A.W) atomicAdd(&grid[(size_t)gy * A.W + gx], val);
+        if (gy < A.H && gx < A.W) atomicAdd(&grid[org.layer_off + (size_t)gy * A.W + gx], val);
       }
     }
   }
@@ -239,7 +254,8 @@ __global__ void __launch_bounds__(256) k_grid_warp(
   int it;
   while ((it = next_item(A, &s_item)) >= 0) {
     const WorkItem w = A.items[it];
-    const int wx0 = (w.tile % A.ntx) * A.T, wy0 = (w.tile / A.ntx) * A.T;
+    const TileOrigin org = tile_origin(A, w.tile);
+    const int wx0 = org.wx0, wy0 = org.wy0;
     for (int c = tid; c < pitch * A.win; c += blockDim.x) win[c] = make_float2(0.f, 0.f);
     for (int b = 0; b < w.count; b += GRID_STAGE) {
       const int nb = min(GRID_STAGE, w.count - b);
@@ -294,7 +310,7 @@ __global__ void __launch_bounds__(256) k_grid_warp(
       const float2 val = win[r * pitch + q];
       if (val.x != 0.f || val.y != 0.f) {
         const int gy = wy0 + r, gx = wx0 + q;
-        if (gy < A.H && gx < A.W) atomicAdd(&grid[(size_t)gy * A.W + gx], val);
+        if (gy < A.H && gx < A.W) atomicAdd(&grid[org.layer_off + (size_t)gy * A.W + gx], val);
       }
     }
   }
@@ -330,12 +346,14 @@ __global__ void __launch_bounds__(256) k_degrid_tiled(
   int it;
   while ((it = next_item(A, &s_item)) >= 0) {
     const WorkItem w = A.items[it];
-    const int wx0 = (w.tile % A.ntx) * A.T, wy0 = (w.tile / A.ntx) * A.T;
+    const TileOrigin org = tile_origin(A, w.tile);
+    const int wx0 = org.wx0, wy0 = org.wy0;
     for (int c = threadIdx.x; c < A.win * A.win; c += blockDim.x) {
       const int r = c / A.win, q = c - r * A.win;
       const int gy = wy0 + r, gx = wx0 + q;
-      win[r * pitch + q] = (gy < A.H && gx < A.W) ? __ldg(&grid[(size_t)gy * A.W + gx])
-                                                  : make_float2(0.f, 0.f);
+      win[r * pitch + q] = (gy < A.H && gx < A.W)
+                               ? __ldg(&grid[org.layer_off + (size_t)gy * A.W + gx])
+                               : make_float2(0.f, 0.f);
     }
     __syncthreads();
     for (int j = 2 * warp; j < w.count; j += 2 * nwarps) {
@@ -392,6 +410,7 @@ static TiledArgs tiled_args(const cg_plan *p) {
   A.Q = p->kd.Q;
   A.T = p->T;
   A.ntx = p->ntx;
+  A.tpl = p->tpl;
   A.win = p->win;
   A.pitch = p->pitch;
   return A;

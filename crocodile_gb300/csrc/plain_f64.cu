@@ -40,7 +40,7 @@ __device__ __forceinline__ double2 plain_kernel(const PlainArgs &A,
 __global__ void k_grid_plain(PlainArgs A, int start, int count,
                              const double2 *__restrict__ ktab,
                              const double2 *__restrict__ vis,
-                             double *__restrict__ grid) {
+                             double *__restrict__ grid) {  // grid of this bucket's layer
   if (any_failed(A.status)) return;
   const int SS = A.S * A.S;
   int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -171,8 +171,9 @@ int cg_grid_fp64(const cg_plan *p, const void *ktab, const void *vis, void *grid
     const int c = p->h_counts[g];
     if (!c) continue;
     const int64_t threads = (int64_t)c * SS;
+    double *layer_grid = (double *)grid + 2 * (size_t)(g / p->kd.G) * p->H * p->W;
     k_grid_plain<<<(unsigned)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-        A, p->h_offsets[g], c, (const double2 *)ktab, (const double2 *)vis, (double *)grid);
+        A, p->h_offsets[g], c, (const double2 *)ktab, (const double2 *)vis, layer_grid);
   }
   CG_LAUNCH("grid_fp64");
   return CG_OK;
@@ -187,8 +188,9 @@ int cg_degrid_fp64(const cg_plan *p, const void *ktab, const void *grid, void *o
   for (int g = 0; g < p->nbuckets; ++g) {
     const int c = p->h_counts[g];
     if (!c) continue;
+    const double2 *layer_grid = (const double2 *)grid + (size_t)(g / p->kd.G) * p->H * p->W;
     k_degrid_plain<<<(unsigned)((c + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
-        A, p->h_offsets[g], c, (const double2 *)ktab, (const double2 *)grid, (double2 *)out);
+        A, p->h_offsets[g], c, (const double2 *)ktab, layer_grid, (double2 *)out);
   }
   CG_LAUNCH("degrid_fp64");
   return CG_OK;

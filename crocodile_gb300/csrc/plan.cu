@@ -87,24 +87,27 @@ __global__ void k_scan_add(int32_t *__restrict__ out, int n,
   }
 }
 
+// Scratch of the recursive scan: per level the block totals and their scan.
 size_t scan_scratch_words(int n) {
-  int nb = (n + SCAN_TILE - 1) / SCAN_TILE;
-  return 2 * (size_t)(nb + 1);
+  const int nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (nb <= 1) return 0;
+  return 2 * (size_t)(nb + 1) + scan_scratch_words(nb);
 }
 
 int launch_scan(const int32_t *in, int32_t *out, int n, int32_t *scratch,
                 cudaStream_t s) {
   if (n <= 0) return CG_OK;
-  int nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  const int nb = (n + SCAN_TILE - 1) / SCAN_TILE;
   if (nb == 1) {
     k_scan_tiles<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr);
     CG_LAUNCH("scan");
     return CG_OK;
   }
-  CG_REQUIRE(nb <= SCAN_TILE, "scan of %d buckets exceeds the two-level limit", n);
   int32_t *sums = scratch, *sums_off = scratch + nb + 1;
   k_scan_tiles<<<nb, SCAN_THREADS, 0, s>>>(in, out, n, sums);
-  k_scan_tiles<<<1, SCAN_THREADS, 0, s>>>(sums, sums_off, nb, nullptr);
+  CG_LAUNCH("scan");
+  const int rc = launch_scan(sums, sums_off, nb, scratch + 2 * (nb + 1), s);
+  if (rc) return rc;
   k_scan_add<<<nb, SCAN_THREADS, 0, s>>>(out, n, sums_off);
   CG_LAUNCH("scan");
   return CG_OK;
@@ -118,7 +121,9 @@ struct CoordParams {
   int64_t n;
   int H, W, Q, S, G, sep;
   const int32_t *kidx;
-  int mode, T, ntx, nbuckets, sublog;
+  int mode, T, ntx, nbuckets, sublog, subshift;
+  const int32_t *layer;  // per-visibility layer (grid of the stack), or NULL
+  int layers, tpl;
   AxisConst ax, ay;    // filtered-exact constants for x (width W) and y (height H)
   double wstep, inv_wstep;  // wstep != 0: the kernel group is the w bin - kmin
   int kmin, nk;
@@ -157,10 +162,11 @@ __device__ __forceinline__ int morton2(int x, int y) {
 // Tiled-mode bucket: tile, then the 4x4-cell sub-tile of the footprint
 // origin along a Morton curve, so that consecutive visibilities of a work
 // item are spatial neighbours.
-__device__ __forceinline__ int tile_bucket(const CoordParams &P, int x0, int y0) {
+__device__ __forceinline__ int tile_bucket(const CoordParams &P, int lyr, int x0, int y0) {
   const int ty = y0 / P.T, tx = x0 / P.T;
   const int ly = y0 - ty * P.T, lx = x0 - tx * P.T;
-  return ((ty * P.ntx + tx) << (2 * P.sublog)) | morton2(lx >> 2, ly >> 2);
+  return ((lyr * P.tpl + ty * P.ntx + tx) << (2 * P.sublog)) |
+         morton2(lx >> P.subshift, ly >> P.subshift);
 }
 
 __global__ void k_plan_coords(CoordParams P) {
@@ -194,6 +200,11 @@ __global__ void k_plan_coords(CoordParams P) {
         atomicAdd(&P.status[ST_INDEX], 1);
         ok = false;
       }
+      const int lyr = P.layer ? P.layer[i] : 0;
+      if (lyr < 0 || lyr >= P.layers) {
+        atomicAdd(&P.status[ST_INDEX], 1);
+        ok = false;
+      }
       r.x0 = x0;
       r.y0 = y0;
       if (P.sep) {
@@ -203,7 +214,7 @@ __global__ void k_plan_coords(CoordParams P) {
         r.k0 = g;
         r.k1 = yf * P.Q + xf;
       }
-      if (ok) key = (P.mode == CG_PLAN_TILED) ? tile_bucket(P, x0, y0) : g;
+      if (ok) key = (P.mode == CG_PLAN_TILED) ? tile_bucket(P, lyr, x0, y0) : lyr * P.G + g;
     }
   }
   int slot = aggregated_slot(P.hist, key, ok);
@@ -333,9 +344,17 @@ static void plan_geometry(cg_plan &p) {
     p.T = tile_edge(p.kd.S);
     p.ntx = (p.W + p.T - 1) / p.T;
     p.nty = (p.H + p.T - 1) / p.T;
-    p.ntiles = p.ntx * p.nty;
+    p.tpl = p.ntx * p.nty;
+    p.ntiles = p.tpl * p.layers;
     p.sublog = 0;
     while ((4 << p.sublog) < p.T) ++p.sublog;  // 4x4 sub-tiles, 2^sublog per tile edge
+    // keep the histogram (4 B per bucket) within 2^24 buckets: coarser sub-tiles
+    // for very large grid stacks
+    p.subshift = 2;  // sub-tile edge 1 << subshift cells
+    while (p.sublog > 0 && ((int64_t)p.ntiles << (2 * p.sublog)) > (1 << 24)) {
+      --p.sublog;
+      ++p.subshift;
+    }
     p.nbuckets = p.ntiles << (2 * p.sublog);
     p.win = p.T + p.kd.S - 1;
     // pitch = S (mod 16): the taps t = dy*S + dx of consecutive lanes fall on
@@ -350,7 +369,8 @@ static void plan_geometry(cg_plan &p) {
   } else {
     p.T = 0;
     p.ntx = p.nty = 0;
-    p.nbuckets = p.kd.G;
+    p.tpl = 1;
+    p.nbuckets = p.kd.G * p.layers;
     p.win = p.pitch = 0;
     p.chunk = 0;
     p.max_items = 0;
@@ -390,10 +410,13 @@ static int check_desc(const cg_kernel_desc *kd, int H, int W) {
 // from its w bin (round(w / wstep) - kmin, synthesis.py:793) in the same pass.
 int plan_build_into(cg_plan *p, int mode, const cg_kernel_desc *kd, int H, int W,
                     const double *uvw, int64_t stride, double lam, const int32_t *kidx,
-                    double wstep, int kmin, int64_t n, void *workspace, size_t workspace_bytes,
-                    int32_t *d_status, cudaStream_t s) {
+                    double wstep, int kmin, int layers, const int32_t *layer, int64_t n,
+                    void *workspace, size_t workspace_bytes, int32_t *d_status,
+                    cudaStream_t s) {
   int rc = check_desc(kd, H, W);
   if (rc) return rc;
+  CG_REQUIRE(layers >= 1 && (layers == 1 || layer || n == 0), "bad layer arguments");
+  CG_REQUIRE((int64_t)layers * H * W < ((int64_t)1 << 40), "grid stack too large");
   CG_REQUIRE(mode == CG_PLAN_TILED || mode == CG_PLAN_GROUPS, "bad plan mode %d", mode);
   CG_REQUIRE(n >= 0 && n < (int64_t)INT32_MAX, "visibility count %lld unsupported",
              (long long)n);
@@ -407,7 +430,9 @@ int plan_build_into(cg_plan *p, int mode, const cg_kernel_desc *kd, int H, int W
   p->H = H;
   p->W = W;
   p->n = n;
+  p->layers = layers;
   plan_geometry(*p);
+  CG_REQUIRE((int64_t)p->nbuckets < (int64_t)INT32_MAX / 2, "too many tiles");
   const Layout L = layout_of(*p);
   if (!workspace || workspace_bytes < L.total)
     return set_error(CG_ERR_WORKSPACE, "plan needs %zu workspace bytes, got %zu", L.total,
@@ -446,6 +471,10 @@ int plan_build_into(cg_plan *p, int mode, const cg_kernel_desc *kd, int H, int W
   P.ntx = p->ntx;
   P.nbuckets = p->nbuckets;
   P.sublog = p->sublog;
+  P.subshift = p->subshift;
+  P.layer = layer;
+  P.layers = layers;
+  P.tpl = p->tpl;
   P.ax = axis_const(W, kd->Q, lam);
   P.ay = axis_const(H, kd->Q, lam);
   P.wstep = wstep;
@@ -475,21 +504,22 @@ int plan_build_tiled_into(cg_plan *p, const cg_kernel_desc *kd, int H, int W,
                           const double *uvw, int64_t stride, double lam,
                           const int32_t *kidx, int64_t n, void *workspace,
                           size_t workspace_bytes, int32_t *d_status, cudaStream_t s) {
-  return plan_build_into(p, CG_PLAN_TILED, kd, H, W, uvw, stride, lam, kidx, 0.0, 0, n,
-                         workspace, workspace_bytes, d_status, s);
+  return plan_build_into(p, CG_PLAN_TILED, kd, H, W, uvw, stride, lam, kidx, 0.0, 0, 1, nullptr,
+                         n, workspace, workspace_bytes, d_status, s);
 }
 
 // Heap plan; the groups form also copies the group ranges to the host.
 static int plan_create_heap(cg_plan **out, int mode, const cg_kernel_desc *kd, int H, int W,
                             const double *uvw, int64_t stride, double lam, const int32_t *kidx,
-                            double wstep, int kmin, int64_t n, void *workspace,
-                            size_t workspace_bytes, int32_t *d_status, cudaStream_t s) {
+                            double wstep, int kmin, int layers, const int32_t *layer, int64_t n,
+                            void *workspace, size_t workspace_bytes, int32_t *d_status,
+                            cudaStream_t s) {
   CG_REQUIRE(out, "plan output pointer is NULL");
   *out = nullptr;
   cg_plan *p = new (std::nothrow) cg_plan;
   CG_REQUIRE(p, "out of host memory");
-  int rc = plan_build_into(p, mode, kd, H, W, uvw, stride, lam, kidx, wstep, kmin, n, workspace,
-                           workspace_bytes, d_status, s);
+  int rc = plan_build_into(p, mode, kd, H, W, uvw, stride, lam, kidx, wstep, kmin, layers, layer,
+                           n, workspace, workspace_bytes, d_status, s);
   if (rc) {
     delete p;
     return rc;
@@ -537,6 +567,7 @@ size_t cg_plan_workspace_bytes(int mode, int64_t n, int H, int W,
   p.H = H;
   p.W = W;
   p.n = n;
+  p.layers = 1;
   plan_geometry(p);
   return layout_of(p).total;
 }
@@ -546,8 +577,45 @@ int cg_plan_create(cg_plan **out, int mode, const cg_kernel_desc *kd, int H,
                    const int32_t *kidx, int64_t n, void *workspace,
                    size_t workspace_bytes, int32_t *d_status,
                    cg_stream_t stream) {
-  return plan_create_heap(out, mode, kd, H, W, uvw, stride, lam, kidx, 0.0, 0, n, workspace,
-                          workspace_bytes, d_status, (cudaStream_t)stream);
+  return plan_create_heap(out, mode, kd, H, W, uvw, stride, lam, kidx, 0.0, 0, 1, nullptr, n,
+                          workspace, workspace_bytes, d_status, (cudaStream_t)stream);
+}
+
+static void opts_or_default(const cg_plan_opts *o, cg_plan_opts &r) {
+  r.layers = 1;
+  r.layer = nullptr;
+  r.wstep = 0.0;
+  r.kmin = 0;
+  if (o) r = *o;
+  if (r.layers < 1) r.layers = 1;
+}
+
+size_t cg_plan_workspace_bytes_ex(int mode, int64_t n, int H, int W, const cg_kernel_desc *kd,
+                                  const cg_plan_opts *opts) {
+  if (check_desc(kd, H, W) != CG_OK) return 0;
+  cg_plan_opts o;
+  opts_or_default(opts, o);
+  cg_plan p;
+  memset(&p, 0, sizeof(p));
+  p.mode = mode;
+  p.kd = *kd;
+  p.H = H;
+  p.W = W;
+  p.n = n;
+  p.layers = o.layers;
+  plan_geometry(p);
+  return layout_of(p).total;
+}
+
+int cg_plan_create_ex(cg_plan **out, int mode, const cg_kernel_desc *kd, int H, int W,
+                      const double *uvw, int64_t stride, double lam, const int32_t *kidx,
+                      int64_t n, const cg_plan_opts *opts, void *workspace,
+                      size_t workspace_bytes, int32_t *d_status, cg_stream_t stream) {
+  cg_plan_opts o;
+  opts_or_default(opts, o);
+  return plan_create_heap(out, mode, kd, H, W, uvw, stride, lam, kidx, o.wstep, o.kmin, o.layers,
+                          o.layer, n, workspace, workspace_bytes, d_status,
+                          (cudaStream_t)stream);
 }
 
 int cg_plan_create_wbins(cg_plan **out, int mode, const cg_kernel_desc *kd, int H, int W,
@@ -555,8 +623,8 @@ int cg_plan_create_wbins(cg_plan **out, int mode, const cg_kernel_desc *kd, int 
                          int64_t n, void *workspace, size_t workspace_bytes,
                          int32_t *d_status, cg_stream_t stream) {
   CG_REQUIRE(wstep != 0.0, "wstep must be non-zero");
-  return plan_create_heap(out, mode, kd, H, W, uvw, stride, lam, nullptr, wstep, kmin, n,
-                          workspace, workspace_bytes, d_status, (cudaStream_t)stream);
+  return plan_create_heap(out, mode, kd, H, W, uvw, stride, lam, nullptr, wstep, kmin, 1, nullptr,
+                          n, workspace, workspace_bytes, d_status, (cudaStream_t)stream);
 }
 
 int cg_plan_destroy(cg_plan *p) {

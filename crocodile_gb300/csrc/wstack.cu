@@ -1,0 +1,133 @@
+// w-stacking (K9): the per-plane loop of examples/notebooks/wstacking.ipynb
+// (code cell 10) with convolutional gridding, batched over all planes.
+//
+//   for each w-plane p with visibilities:
+//       midw = mean(w of the plane's visibilities)
+//       image += ifft(grid_p) / w_kernel_function(l, m, midw)
+//
+// The planes are gridded in one launch into a stack of grids (a layered
+// plan), transformed by one batched cuFFT, and combined here in one pass over
+// the stack.  w_kernel_function (crocodile/synthesis.py:273-293) is
+// exp(2 pi i w ph) with ph = 1 - sqrt(1 - l^2 - m^2); ph is computed in FP64
+// once per pixel, the turns w ph of each plane are formed in double-float
+// arithmetic and reduced to a fraction of a turn before the FP32 sincospi,
+// so the FP32 factor is accurate to ~1e-7 for any w.
+#include "cg_internal.cuh"
+
+namespace cg {
+
+// One block per layer: mean of w over the layer's visibilities, summed in the
+// plan's sorted order (deterministic).  Empty layers get mean 0 and count 0.
+__global__ void k_layer_mean_w(const double *__restrict__ uvw, int64_t stride,
+                               const int32_t *__restrict__ perm,
+                               const int32_t *__restrict__ counts,
+                               const int32_t *__restrict__ offsets, int buckets_per_layer,
+                               double *__restrict__ mean_out, int32_t *__restrict__ count_out) {
+  const int l = blockIdx.x;
+  const int b0 = l * buckets_per_layer, b1 = b0 + buckets_per_layer - 1;
+  const int start = offsets[b0], end = offsets[b1] + counts[b1];
+  double sum = 0.0;
+  for (int j = start + threadIdx.x; j < end; j += blockDim.x) sum += uvw[(int64_t)perm[j] * stride + 2];
+  __shared__ double s[32];
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = threadIdx.x < (blockDim.x >> 5) ? s[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) {
+      const int c = end - start;
+      mean_out[l] = c ? t / (double)c : 0.0;
+      if (count_out) count_out[l] = c;
+    }
+  }
+}
+
+// image[i, j] = sum_p planes[p, i, j] / exp(2 pi i midw_p ph(i, j)).
+// The turns t = midw_p * ph are formed as a double-float product (midw and ph
+// split into FP32 hi + lo parts, exact FMA residual), so their fraction keeps
+// ~2^-44 relative precision for any w without 32 FP64 products per pixel.
+__global__ void k_wstack_combine(const float2 *__restrict__ planes, int layers, int N,
+                                 double theta, const double *__restrict__ midw,
+                                 const int32_t *__restrict__ counts, float2 *__restrict__ out,
+                                 int32_t *status) {
+  extern __shared__ float2 s_w[];  // (hi, lo) of midw per layer; lo = NaN marks empty layers
+  for (int p = threadIdx.x; p < layers; p += blockDim.x) {
+    const double w = midw[p];
+    const float hi = (float)w;
+    s_w[p] = make_float2(hi, counts[p] ? (float)(w - (double)hi) : __int_as_float(0x7fc00000));
+  }
+  __syncthreads();
+  const int64_t total = (int64_t)N * N;
+  int bad = 0;
+  for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total;
+       L += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(L / N), j = (int)(L - (int64_t)i * N);
+    // theta * coordinates2(N): l along columns (x), m along rows (y)
+    const double l = __dmul_rn(theta, __ddiv_rn((double)(j - N / 2), (double)N));
+    const double m = __dmul_rn(theta, __ddiv_rn((double)(i - N / 2), (double)N));
+    const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
+    if (!(r2 < 1.0)) bad = 1;
+    const double ph = 1.0 - sqrt(1.0 - r2);
+    const float ph_h = (float)ph, ph_l = (float)(ph - (double)ph_h);
+    float ax = 0.f, ay = 0.f;
+    for (int p = 0; p < layers; ++p) {
+      const float2 w = s_w[p];
+      if (w.y != w.y) continue;  // empty plane
+      const float hi = w.x * ph_h;
+      const float lo = fmaf(w.x, ph_h, -hi) + fmaf(w.x, ph_l, w.y * ph_h);
+      const float f = (hi - rintf(hi)) + lo;
+      float sn, cs;
+      sincospif(2.0f * f, &sn, &cs);
+      const float2 g = planes[(int64_t)p * total + L];
+      // g / (cs + i sn) = g * (cs - i sn) for |e| = 1
+      ax += g.x * cs + g.y * sn;
+      ay += g.y * cs - g.x * sn;
+    }
+    out[L] = make_float2(ax, ay);
+  }
+  if (bad && status) atomicAdd(&status[ST_RANGE], 1);
+}
+
+}  // namespace cg
+
+using namespace cg;
+
+extern "C" {
+
+int cg_plan_layer_mean_w(const cg_plan *p, const double *uvw, int64_t stride, double *mean_out,
+                         int32_t *count_out, cg_stream_t stream) {
+  CG_REQUIRE(p && p->mode == CG_PLAN_TILED, "needs a CG_PLAN_TILED plan");
+  CG_REQUIRE(uvw && stride >= 3 && mean_out, "NULL argument");
+  if (p->n == 0) {
+    CG_CUDA(cudaMemsetAsync(mean_out, 0, sizeof(double) * p->layers, (cudaStream_t)stream));
+    if (count_out)
+      CG_CUDA(cudaMemsetAsync(count_out, 0, sizeof(int32_t) * p->layers, (cudaStream_t)stream));
+    return CG_OK;
+  }
+  const int bpl = p->tpl << (2 * p->sublog);
+  k_layer_mean_w<<<p->layers, 256, 0, (cudaStream_t)stream>>>(uvw, stride, p->perm, p->counts,
+                                                               p->offsets, bpl, mean_out,
+                                                               count_out);
+  CG_LAUNCH("layer mean w");
+  return CG_OK;
+}
+
+int cg_wstack_combine(const void *planes_c64, int layers, int N, double theta,
+                      const double *mean_w, const int32_t *counts, void *image_c64,
+                      int32_t *d_status, cg_stream_t stream) {
+  CG_REQUIRE(planes_c64 && mean_w && counts && image_c64 && layers >= 1 && N >= 1,
+             "bad w-stacking arguments");
+  const int64_t total = (int64_t)N * N;
+  int64_t blocks = (total + 255) / 256;
+  const int64_t cap = (int64_t)num_sms() * 8;
+  if (blocks > cap) blocks = cap;
+  CG_REQUIRE(layers <= 4096, "at most 4096 w-planes");
+  k_wstack_combine<<<(unsigned)blocks, 256, layers * sizeof(float2), (cudaStream_t)stream>>>(
+      (const float2 *)planes_c64, layers, N, theta, mean_w, counts, (float2 *)image_c64,
+      d_status);
+  CG_LAUNCH("w-stack combine");
+  return CG_OK;
+}
+
+}  // extern "C"

@@ -135,9 +135,10 @@ class Plan:
     uvw / lam is the fraction of the grid), ``shape`` the grid (H, W)."""
 
     def __init__(self, uvw, lam, shape, ktab, kidx=None, mode=L.CG_PLAN_TILED, status=None,
-                 wbins=None):
+                 wbins=None, layers=None):
         """wbins=(wstep, kmin): take each visibility's kernel group from its w bin
-        (round(w / wstep) - kmin) inside the plan's coordinate pass."""
+        (round(w / wstep) - kmin) inside the plan's coordinate pass.
+        layers=(L, layer): grid visibility i into grid layer[i] of a stack of L grids."""
         require_cuda()
         self.uvw = cuda_tensor(uvw, torch.float64)
         if self.uvw.dim() != 2 or self.uvw.shape[1] < 2:
@@ -149,24 +150,23 @@ class Plan:
         self.sep, self.Q, self.S, self.G = ktab.sep, ktab.Q, ktab.S, ktab.G
         kd = ktab.desc()
         self._kd = kd
-        nbytes = L.lib().cg_plan_workspace_bytes(mode, self.n, self.shape[0], self.shape[1],
-                                                 ctypes.byref(kd))
+        self.layers = 1 if layers is None else int(layers[0])
+        self.layer = None if layers is None else cuda_tensor(layers[1], torch.int32)
+        opts = L.PlanOpts(self.layers, None if self.layer is None else self.layer.data_ptr(),
+                          0.0 if wbins is None else float(wbins[0]),
+                          0 if wbins is None else int(wbins[1]))
+        nbytes = L.lib().cg_plan_workspace_bytes_ex(mode, self.n, self.shape[0], self.shape[1],
+                                                    ctypes.byref(kd), ctypes.byref(opts))
         if nbytes == 0:
-            L.raise_for(L.CG_ERR_ARG, "cg_plan_workspace_bytes")
+            L.raise_for(L.CG_ERR_ARG, "cg_plan_workspace_bytes_ex")
         self.ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
         self.status = status or Status()
         if status is None:
             self.status.reset()
         h = ctypes.c_void_p()
-        if wbins is not None:
-            L.call("cg_plan_create_wbins", ctypes.byref(h), mode, ctypes.byref(kd),
-                   self.shape[0], self.shape[1], _p(self.uvw), self.uvw.stride(0), float(lam),
-                   float(wbins[0]), int(wbins[1]), self.n, _p(self.ws), nbytes,
-                   _p(self.status.t), stream())
-        else:
-            L.call("cg_plan_create", ctypes.byref(h), mode, ctypes.byref(kd), self.shape[0],
-                   self.shape[1], _p(self.uvw), self.uvw.stride(0), float(lam), _p(self.kidx),
-                   self.n, _p(self.ws), nbytes, _p(self.status.t), stream())
+        L.call("cg_plan_create_ex", ctypes.byref(h), mode, ctypes.byref(kd), self.shape[0],
+               self.shape[1], _p(self.uvw), self.uvw.stride(0), float(lam), _p(self.kidx),
+               self.n, ctypes.byref(opts), _p(self.ws), nbytes, _p(self.status.t), stream())
         self.handle = h
         self._fin = weakref.finalize(self, L.lib().cg_plan_destroy, h)
 
@@ -183,8 +183,16 @@ class Plan:
             raise ValueError("kernel table does not match the plan's kernel layout")
         return ktab.to(dtype).table
 
+    def layer_mean_w(self):
+        """(mean w [layers] float64, visibility count [layers] int32) per grid layer."""
+        mean = torch.empty(self.layers, dtype=torch.float64, device="cuda")
+        count = torch.empty(self.layers, dtype=torch.int32, device="cuda")
+        L.call("cg_plan_layer_mean_w", self.handle, _p(self.uvw), self.uvw.stride(0), _p(mean),
+               _p(count), stream())
+        return mean, count
+
     def grid(self, ktab, vis, grid):
-        """grid (c64 [H, W]) += convgrid of vis (c64 [n])."""
+        """grid (c64 [H, W], or [layers, H, W]) += convgrid of vis (c64 [n])."""
         t = self._table(ktab, CF)
         L.call("cg_grid", self.handle, _p(t), _p(vis), _p(grid), stream())
         return grid
@@ -246,6 +254,15 @@ def degrid_boxcar(uvw, lam, grid, status):
     out = torch.empty(uvw.shape[0], dtype=CD, device="cuda")
     L.call("cg_degrid_boxcar", _p(uvw), uvw.stride(0), float(lam), uvw.shape[0], _p(grid),
            _p(out), grid.shape[0], grid.shape[1], _p(status.t), stream())
+    return out
+
+
+def wstack_combine(planes, theta, mean_w, counts, status):
+    """sum_p planes[p] / w_kernel_function(l, m, mean_w[p]) as a complex64 image."""
+    layers, N = planes.shape[0], planes.shape[-1]
+    out = torch.empty((N, N), dtype=CF, device="cuda")
+    L.call("cg_wstack_combine", _p(planes), layers, N, float(theta), _p(mean_w), _p(counts),
+           _p(out), _p(status.t), stream())
     return out
 
 

@@ -746,6 +746,51 @@ def do_predict(theta, lam, uvw, src, modelimage, predfn, **kwargs):
     return _host(_degrid_from(ktab, kidx, uvw_t, lam, ximage, prec), like=uvw)
 
 
+def w_stack_imaging(theta, lam, uvw, src, vis, kv, plane, precision=None, per_plane=False):
+    """w-stacking (examples/notebooks/wstacking.ipynb, code cell 10, with conv_imaging in
+    place of the notebook's boxcar gridding): for each w-plane p holding visibilities,
+    ifft(grid_p) / w_kernel_function(l, m, mean w of the plane), summed; returns the
+    complex image (the notebook shows 2 Re of it).  ``plane`` is each visibility's plane
+    index.  All planes grid in one launch into a stack of grids and transform in one
+    batched FFT; ``per_plane=True`` grids and transforms one plane per launch instead
+    (the comparator).  FP32 only."""
+    if _prec(precision) != "fp32":
+        raise ValueError("w_stack_imaging runs the FP32 tiled path only")
+    N = _grid_size(theta, lam)
+    n = _nrows(uvw)
+    ptab = numpy.asarray(plane.cpu().numpy() if isinstance(plane, torch.Tensor) else plane)
+    layers = int(ptab.max()) + 1 if n else 1
+    ktab, kidx = _table_and_groups(kv, src, n, E.CF)
+    uvw_t = E.cuda_tensor(uvw, torch.float64)
+    vis_t = E.cuda_tensor(vis, E.CF)
+    planes = torch.zeros((layers, N, N), dtype=E.CF, device="cuda")
+    st = E.Status()
+    if not per_plane:
+        plan = E.Plan(uvw_t, lam, (N, N), ktab, kidx, status=st,
+                      layers=(layers, ptab.astype(numpy.int32)))
+        plan.grid(ktab, vis_t, planes)
+        mean_w, counts = plan.layer_mean_w()
+        E.fft_(planes, True)
+    else:
+        mean_w = torch.zeros(layers, dtype=torch.float64, device="cuda")
+        counts = torch.zeros(layers, dtype=torch.int32, device="cuda")
+        for p in range(layers):
+            sel = numpy.nonzero(ptab == p)[0]
+            if len(sel) == 0:
+                continue
+            idx = torch.from_numpy(sel).cuda()
+            sub = E.Plan(uvw_t[idx], lam, (N, N), ktab,
+                         None if kidx is None else kidx[sel], status=st,
+                         layers=(1, numpy.zeros(len(sel), numpy.int32)))
+            sub.grid(ktab, vis_t[idx], planes[p])
+            m, c = sub.layer_mean_w()
+            mean_w[p], counts[p] = m[0], c[0]
+            E.fft_(planes[p], True)
+    image = E.wstack_combine(planes, theta, mean_w, counts, st)
+    st.check()
+    return _host(image, like=uvw)
+
+
 def sample_image(image, x, y):
     """Bilinear sample relative to the image middle (synthesis.py:736-755)."""
     x = x + image.shape[0] / 2

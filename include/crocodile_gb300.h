@@ -142,6 +142,26 @@ int cg_plan_create_wbins(cg_plan **plan, int mode, const cg_kernel_desc *kd,
                          double lam, double wstep, int kmin, int64_t n,
                          void *workspace, size_t workspace_bytes,
                          int32_t *d_status, cg_stream_t stream);
+/* Extended plan options (no reference counterpart beyond the functions
+ * cited): layers > 1 grids each visibility into grid layer[i] of a stack of
+ * `layers` H x W grids laid out one after another (the per-plane grids of
+ * w-stacking, examples/notebooks/wstacking.ipynb cell 10), all in one launch;
+ * wstep != 0 takes kernel groups from w bins as cg_plan_create_wbins. */
+typedef struct {
+  int layers;
+  const int32_t *layer; /* device int32 [n], or NULL when layers == 1 */
+  double wstep;
+  int kmin;
+} cg_plan_opts;
+size_t cg_plan_workspace_bytes_ex(int mode, int64_t n, int H, int W,
+                                  const cg_kernel_desc *kd,
+                                  const cg_plan_opts *opts);
+int cg_plan_create_ex(cg_plan **plan, int mode, const cg_kernel_desc *kd,
+                      int H, int W, const double *uvw, int64_t stride,
+                      double lam, const int32_t *kidx, int64_t n,
+                      const cg_plan_opts *opts, void *workspace,
+                      size_t workspace_bytes, int32_t *d_status,
+                      cg_stream_t stream);
 int cg_plan_destroy(cg_plan *plan);
 /* Tile edge (cells) and number of work items upper bound, for reports. */
 int cg_plan_info(const cg_plan *plan, int64_t *info_out /* [4] */);
@@ -234,6 +254,22 @@ int cg_image_from_grid(void *grid_c64, int H, int W, float *image_out,
 /* image *= 1 / *d_scale (do_imaging's normalisation, synthesis.py:909-911) */
 int cg_scale_image(float *image, int64_t count, const float *d_scale,
                    cg_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* w-stacking (examples/notebooks/wstacking.ipynb code cell 10, with
+ * convolutional gridding): after gridding every plane into one layer of a
+ * layered plan (cg_plan_create_ex) and an inverse centred cg_fft of the
+ * stack, image = sum_p plane_p / w_kernel_function(l, m, mean w of plane p)
+ * (synthesis.py:273-293).  cg_plan_layer_mean_w writes the mean w (double)
+ * and visibility count (int32, may be NULL) of each layer, summed in the
+ * plan's order; cg_wstack_combine forms the complex64 N x N image (planes
+ * without visibilities are skipped, as in the notebook). */
+int cg_plan_layer_mean_w(const cg_plan *plan, const double *uvw, int64_t stride,
+                         double *mean_out, int32_t *count_out,
+                         cg_stream_t stream);
+int cg_wstack_combine(const void *planes_c64, int layers, int N, double theta,
+                      const double *mean_w, const int32_t *counts,
+                      void *image_c64, int32_t *d_status, cg_stream_t stream);
 
 /* ------------------------------------------------------------------ */
 /* Kernel generation (FP64 arithmetic; outputs c64 or c128). */
