@@ -33,7 +33,8 @@ CG_LAYOUT_OWNER = 2
 
 
 class PlanOpts(ctypes.Structure):
-    _fields_ = [("layers", c_int), ("layer", c_void_p), ("wstep", c_double), ("kmin", c_int)]
+    _fields_ = [("layers", c_int), ("layer", c_void_p), ("wstep", c_double), ("kmin", c_int),
+                ("group", c_void_p), ("ngroups", c_int)]
 
 
 class KernelDesc(ctypes.Structure):
@@ -66,6 +67,9 @@ SIGNATURES = {
                                   c_int, P, c_int64, c_double, P, c_int64,
                                   ctypes.POINTER(PlanOpts), P, c_size_t, P, P]),
     "cg_plan_layer_mean_w": (c_int, [P, P, c_int64, P, P, P]),
+    "cg_compact_keys_workspace_bytes": (c_size_t, [c_int]),
+    "cg_compact_keys": (c_int, [P, c_int64, c_int, P, P, P, P, c_size_t, P, P]),
+    "cg_aw_keys": (c_int, [P, c_int64, P, P, c_int64, c_int, c_double, c_int, c_int, P, P, P]),
     "cg_wstack_combine": (c_int, [P, c_int, c_int, c_double, P, P, P, P, P]),
     "cg_plan_destroy": (c_int, [P]),
     "cg_set_tuning": (c_int, [ctypes.POINTER(Tuning)]),

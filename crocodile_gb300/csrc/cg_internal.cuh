@@ -155,6 +155,7 @@ struct cg_plan {
   int pitch;    // smem row pitch (even)
   int nbuckets;
   int layers;   // stacked grids (w-stacking planes); a grid of H*W cells each
+  int gper;     // groups mode: buckets per layer (launch groups, or kernel groups)
   int tpl;      // tiles per layer (ntx * nty)
   int ntiles;   // tiled mode: tiles of all layers; each holds 4^sublog sub-tile buckets
   int sublog;   // 2^sublog sub-tiles per tile edge, ordered along a Morton curve

@@ -171,7 +171,7 @@ int cg_grid_fp64(const cg_plan *p, const void *ktab, const void *vis, void *grid
     const int c = p->h_counts[g];
     if (!c) continue;
     const int64_t threads = (int64_t)c * SS;
-    double *layer_grid = (double *)grid + 2 * (size_t)(g / p->kd.G) * p->H * p->W;
+    double *layer_grid = (double *)grid + 2 * (size_t)(g / p->gper) * p->H * p->W;
     k_grid_plain<<<(unsigned)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
         A, p->h_offsets[g], c, (const double2 *)ktab, (const double2 *)vis, layer_grid);
   }
@@ -188,7 +188,7 @@ int cg_degrid_fp64(const cg_plan *p, const void *ktab, const void *grid, void *o
   for (int g = 0; g < p->nbuckets; ++g) {
     const int c = p->h_counts[g];
     if (!c) continue;
-    const double2 *layer_grid = (const double2 *)grid + (size_t)(g / p->kd.G) * p->H * p->W;
+    const double2 *layer_grid = (const double2 *)grid + (size_t)(g / p->gper) * p->H * p->W;
     k_degrid_plain<<<(unsigned)((c + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
         A, p->h_offsets[g], c, (const double2 *)ktab, layer_grid, (double2 *)out);
   }

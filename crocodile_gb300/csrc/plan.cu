@@ -124,6 +124,8 @@ struct CoordParams {
   int mode, T, ntx, nbuckets, sublog, subshift;
   const int32_t *layer;  // per-visibility layer (grid of the stack), or NULL
   int layers, tpl;
+  const int32_t *group;  // groups mode: per-visibility launch group, or NULL (= kernel group)
+  int ngroups;
   AxisConst ax, ay;    // filtered-exact constants for x (width W) and y (height H)
   double wstep, inv_wstep;  // wstep != 0: the kernel group is the w bin - kmin
   int kmin, nk;
@@ -214,7 +216,16 @@ __global__ void k_plan_coords(CoordParams P) {
         r.k0 = g;
         r.k1 = yf * P.Q + xf;
       }
-      if (ok) key = (P.mode == CG_PLAN_TILED) ? tile_bucket(P, lyr, x0, y0) : lyr * P.G + g;
+      int grp = g, gper = P.G;
+      if (P.mode == CG_PLAN_GROUPS && P.group) {
+        grp = P.group[i];
+        gper = P.ngroups;
+        if (grp < 0 || grp >= gper) {
+          atomicAdd(&P.status[ST_INDEX], 1);
+          ok = false;
+        }
+      }
+      if (ok) key = (P.mode == CG_PLAN_TILED) ? tile_bucket(P, lyr, x0, y0) : lyr * gper + grp;
     }
   }
   int slot = aggregated_slot(P.hist, key, ok);
@@ -326,6 +337,52 @@ __global__ void k_minmax_init(int32_t *mm) {
   mm[1] = INT32_MIN;
 }
 
+// ---------------------------------------------------------------- key compaction
+__global__ void k_key_flags(const int32_t *__restrict__ key, int64_t n, int nkeys,
+                            int32_t *__restrict__ flags, int32_t *status) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k = key[i];
+  if (k < 0 || k >= nkeys) {
+    atomicAdd(&status[ST_INDEX], 1);
+    return;
+  }
+  flags[k] = 1;  // benign race: every writer stores 1
+}
+
+__global__ void k_key_rows(const int32_t *__restrict__ key, int64_t n, int nkeys,
+                           const int32_t *__restrict__ rank, int32_t *__restrict__ row) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k = key[i];
+  row[i] = (k >= 0 && k < nkeys) ? rank[k] : 0;
+}
+
+__global__ void k_key_of_row(int nkeys, const int32_t *__restrict__ flags,
+                             const int32_t *__restrict__ rank, int32_t *__restrict__ key_of_row) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nkeys && flags[k]) key_of_row[rank[k]] = k;
+}
+
+// AW kernel key of every visibility: (a1 * nant + a2) * nbins + w bin - kmin, the
+// (wbin, a1, a2) key of the AW kernel cache (scripts/image_dataset.py:153-171,
+// synthesis.py:793).
+__global__ void k_aw_keys(const double *__restrict__ uvw, int64_t stride,
+                          const int32_t *__restrict__ a1, const int32_t *__restrict__ a2,
+                          int64_t n, int nant, double wstep, double inv_wstep, int kmin,
+                          int nbins, int32_t *__restrict__ key, int32_t *status) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double j = w_bin_fast(uvw[i * stride + 2], wstep, inv_wstep) - (double)kmin;
+  const int p = a1[i], q = a2[i];
+  if (!(j >= 0.0 && j < (double)nbins) || p < 0 || p >= nant || q < 0 || q >= nant) {
+    atomicAdd(&status[ST_INDEX], 1);
+    key[i] = 0;
+    return;
+  }
+  key[i] = (p * nant + q) * nbins + (int)j;
+}
+
 // ---------------------------------------------------------------- sizing
 struct Layout {
   size_t rec_tmp, key, rank, recs, perm, counts, offsets, scan, items, ctr, total;
@@ -370,7 +427,7 @@ static void plan_geometry(cg_plan &p) {
     p.T = 0;
     p.ntx = p.nty = 0;
     p.tpl = 1;
-    p.nbuckets = p.kd.G * p.layers;
+    p.nbuckets = p.gper * p.layers;
     p.win = p.pitch = 0;
     p.chunk = 0;
     p.max_items = 0;
@@ -410,10 +467,12 @@ static int check_desc(const cg_kernel_desc *kd, int H, int W) {
 // from its w bin (round(w / wstep) - kmin, synthesis.py:793) in the same pass.
 int plan_build_into(cg_plan *p, int mode, const cg_kernel_desc *kd, int H, int W,
                     const double *uvw, int64_t stride, double lam, const int32_t *kidx,
-                    double wstep, int kmin, int layers, const int32_t *layer, int64_t n,
-                    void *workspace, size_t workspace_bytes, int32_t *d_status,
-                    cudaStream_t s) {
+                    double wstep, int kmin, int layers, const int32_t *layer,
+                    const int32_t *group, int ngroups, int64_t n, void *workspace,
+                    size_t workspace_bytes, int32_t *d_status, cudaStream_t s) {
   int rc = check_desc(kd, H, W);
+  CG_REQUIRE(!group || (mode == CG_PLAN_GROUPS && ngroups >= 1),
+             "launch groups need a CG_PLAN_GROUPS plan and ngroups >= 1");
   if (rc) return rc;
   CG_REQUIRE(layers >= 1 && (layers == 1 || layer || n == 0), "bad layer arguments");
   CG_REQUIRE((int64_t)layers * H * W < ((int64_t)1 << 40), "grid stack too large");
@@ -431,6 +490,7 @@ int plan_build_into(cg_plan *p, int mode, const cg_kernel_desc *kd, int H, int W
   p->W = W;
   p->n = n;
   p->layers = layers;
+  p->gper = group ? ngroups : kd->G;
   plan_geometry(*p);
   CG_REQUIRE((int64_t)p->nbuckets < (int64_t)INT32_MAX / 2, "too many tiles");
   const Layout L = layout_of(*p);
@@ -474,6 +534,8 @@ int plan_build_into(cg_plan *p, int mode, const cg_kernel_desc *kd, int H, int W
   P.subshift = p->subshift;
   P.layer = layer;
   P.layers = layers;
+  P.group = group;
+  P.ngroups = ngroups;
   P.tpl = p->tpl;
   P.ax = axis_const(W, kd->Q, lam);
   P.ay = axis_const(H, kd->Q, lam);
@@ -505,21 +567,21 @@ int plan_build_tiled_into(cg_plan *p, const cg_kernel_desc *kd, int H, int W,
                           const int32_t *kidx, int64_t n, void *workspace,
                           size_t workspace_bytes, int32_t *d_status, cudaStream_t s) {
   return plan_build_into(p, CG_PLAN_TILED, kd, H, W, uvw, stride, lam, kidx, 0.0, 0, 1, nullptr,
-                         n, workspace, workspace_bytes, d_status, s);
+                         nullptr, 0, n, workspace, workspace_bytes, d_status, s);
 }
 
 // Heap plan; the groups form also copies the group ranges to the host.
 static int plan_create_heap(cg_plan **out, int mode, const cg_kernel_desc *kd, int H, int W,
                             const double *uvw, int64_t stride, double lam, const int32_t *kidx,
-                            double wstep, int kmin, int layers, const int32_t *layer, int64_t n,
-                            void *workspace, size_t workspace_bytes, int32_t *d_status,
-                            cudaStream_t s) {
+                            double wstep, int kmin, int layers, const int32_t *layer,
+                            const int32_t *group, int ngroups, int64_t n, void *workspace,
+                            size_t workspace_bytes, int32_t *d_status, cudaStream_t s) {
   CG_REQUIRE(out, "plan output pointer is NULL");
   *out = nullptr;
   cg_plan *p = new (std::nothrow) cg_plan;
   CG_REQUIRE(p, "out of host memory");
   int rc = plan_build_into(p, mode, kd, H, W, uvw, stride, lam, kidx, wstep, kmin, layers, layer,
-                           n, workspace, workspace_bytes, d_status, s);
+                           group, ngroups, n, workspace, workspace_bytes, d_status, s);
   if (rc) {
     delete p;
     return rc;
@@ -568,6 +630,7 @@ size_t cg_plan_workspace_bytes(int mode, int64_t n, int H, int W,
   p.W = W;
   p.n = n;
   p.layers = 1;
+  p.gper = kd->G;
   plan_geometry(p);
   return layout_of(p).total;
 }
@@ -577,8 +640,8 @@ int cg_plan_create(cg_plan **out, int mode, const cg_kernel_desc *kd, int H,
                    const int32_t *kidx, int64_t n, void *workspace,
                    size_t workspace_bytes, int32_t *d_status,
                    cg_stream_t stream) {
-  return plan_create_heap(out, mode, kd, H, W, uvw, stride, lam, kidx, 0.0, 0, 1, nullptr, n,
-                          workspace, workspace_bytes, d_status, (cudaStream_t)stream);
+  return plan_create_heap(out, mode, kd, H, W, uvw, stride, lam, kidx, 0.0, 0, 1, nullptr, nullptr,
+                          0, n, workspace, workspace_bytes, d_status, (cudaStream_t)stream);
 }
 
 static void opts_or_default(const cg_plan_opts *o, cg_plan_opts &r) {
@@ -586,6 +649,8 @@ static void opts_or_default(const cg_plan_opts *o, cg_plan_opts &r) {
   r.layer = nullptr;
   r.wstep = 0.0;
   r.kmin = 0;
+  r.group = nullptr;
+  r.ngroups = 0;
   if (o) r = *o;
   if (r.layers < 1) r.layers = 1;
 }
@@ -603,6 +668,7 @@ size_t cg_plan_workspace_bytes_ex(int mode, int64_t n, int H, int W, const cg_ke
   p.W = W;
   p.n = n;
   p.layers = o.layers;
+  p.gper = o.group ? o.ngroups : kd->G;
   plan_geometry(p);
   return layout_of(p).total;
 }
@@ -614,7 +680,7 @@ int cg_plan_create_ex(cg_plan **out, int mode, const cg_kernel_desc *kd, int H, 
   cg_plan_opts o;
   opts_or_default(opts, o);
   return plan_create_heap(out, mode, kd, H, W, uvw, stride, lam, kidx, o.wstep, o.kmin, o.layers,
-                          o.layer, n, workspace, workspace_bytes, d_status,
+                          o.layer, o.group, o.ngroups, n, workspace, workspace_bytes, d_status,
                           (cudaStream_t)stream);
 }
 
@@ -624,7 +690,8 @@ int cg_plan_create_wbins(cg_plan **out, int mode, const cg_kernel_desc *kd, int 
                          int32_t *d_status, cg_stream_t stream) {
   CG_REQUIRE(wstep != 0.0, "wstep must be non-zero");
   return plan_create_heap(out, mode, kd, H, W, uvw, stride, lam, nullptr, wstep, kmin, 1, nullptr,
-                          n, workspace, workspace_bytes, d_status, (cudaStream_t)stream);
+                          nullptr, 0, n, workspace, workspace_bytes, d_status,
+                          (cudaStream_t)stream);
 }
 
 int cg_plan_destroy(cg_plan *p) {
@@ -670,6 +737,51 @@ int cg_w_bins_fixed(const double *uvw, int64_t stride, int64_t n, double wstep, 
   k_w_bins_fixed<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
       uvw, stride, n, wstep, 1.0 / wstep, kmin, nk, kidx, d_status);
   CG_LAUNCH("w_bins_fixed");
+  return CG_OK;
+}
+
+size_t cg_compact_keys_workspace_bytes(int nkeys) {
+  return (2 * (size_t)std::max(nkeys, 1) + scan_scratch_words(std::max(nkeys, 1)) + 64) * 4;
+}
+
+int cg_compact_keys(const int32_t *key, int64_t n, int nkeys, int32_t *row, int32_t *key_of_row,
+                    int32_t *h_nrows, void *ws, size_t ws_bytes, int32_t *d_status,
+                    cg_stream_t stream) {
+  CG_REQUIRE(nkeys >= 1 && h_nrows && d_status && (n == 0 || (key && row && key_of_row)),
+             "bad compact_keys arguments");
+  if (!ws || ws_bytes < cg_compact_keys_workspace_bytes(nkeys))
+    return set_error(CG_ERR_WORKSPACE, "compact_keys needs %zu workspace bytes",
+                     cg_compact_keys_workspace_bytes(nkeys));
+  cudaStream_t s = (cudaStream_t)stream;
+  int32_t *flags = (int32_t *)ws, *rank = flags + nkeys, *scratch = rank + nkeys;
+  CG_CUDA(cudaMemsetAsync(flags, 0, (size_t)nkeys * 4, s));
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  if (n > 0) k_key_flags<<<blocks, 256, 0, s>>>(key, n, nkeys, flags, d_status);
+  CG_LAUNCH("key flags");
+  int rc = launch_scan(flags, rank, nkeys, scratch, s);
+  if (rc) return rc;
+  if (n > 0) k_key_rows<<<blocks, 256, 0, s>>>(key, n, nkeys, rank, row);
+  k_key_of_row<<<(nkeys + 255) / 256, 256, 0, s>>>(nkeys, flags, rank, key_of_row);
+  CG_LAUNCH("key rows");
+  int32_t last[2];
+  CG_CUDA(cudaMemcpyAsync(&last[0], rank + nkeys - 1, 4, cudaMemcpyDeviceToHost, s));
+  CG_CUDA(cudaMemcpyAsync(&last[1], flags + nkeys - 1, 4, cudaMemcpyDeviceToHost, s));
+  CG_CUDA(cudaStreamSynchronize(s));
+  *h_nrows = last[0] + last[1];
+  return CG_OK;
+}
+
+int cg_aw_keys(const double *uvw, int64_t stride, const int32_t *a1, const int32_t *a2, int64_t n,
+               int nant, double wstep, int kmin, int nbins, int32_t *key, int32_t *d_status,
+               cg_stream_t stream) {
+  CG_REQUIRE(nant >= 1 && nbins >= 1 && wstep != 0.0 && d_status &&
+                 (n == 0 || (uvw && stride >= 3 && a1 && a2 && key)),
+             "bad aw_keys arguments");
+  CG_REQUIRE((int64_t)nant * nant * nbins < (int64_t)INT32_MAX, "too many AW keys");
+  if (n == 0) return CG_OK;
+  k_aw_keys<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      uvw, stride, a1, a2, n, nant, wstep, 1.0 / wstep, kmin, nbins, key, d_status);
+  CG_LAUNCH("aw keys");
   return CG_OK;
 }
 

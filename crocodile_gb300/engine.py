@@ -135,10 +135,11 @@ class Plan:
     uvw / lam is the fraction of the grid), ``shape`` the grid (H, W)."""
 
     def __init__(self, uvw, lam, shape, ktab, kidx=None, mode=L.CG_PLAN_TILED, status=None,
-                 wbins=None, layers=None):
+                 wbins=None, layers=None, groups=None):
         """wbins=(wstep, kmin): take each visibility's kernel group from its w bin
         (round(w / wstep) - kmin) inside the plan's coordinate pass.
-        layers=(L, layer): grid visibility i into grid layer[i] of a stack of L grids."""
+        layers=(L, layer): grid visibility i into grid layer[i] of a stack of L grids.
+        groups=(G, group): plain form only, one launch per group[i] in [0, G)."""
         require_cuda()
         self.uvw = cuda_tensor(uvw, torch.float64)
         if self.uvw.dim() != 2 or self.uvw.shape[1] < 2:
@@ -152,9 +153,12 @@ class Plan:
         self._kd = kd
         self.layers = 1 if layers is None else int(layers[0])
         self.layer = None if layers is None else cuda_tensor(layers[1], torch.int32)
+        self.group = None if groups is None else cuda_tensor(groups[1], torch.int32)
         opts = L.PlanOpts(self.layers, None if self.layer is None else self.layer.data_ptr(),
                           0.0 if wbins is None else float(wbins[0]),
-                          0 if wbins is None else int(wbins[1]))
+                          0 if wbins is None else int(wbins[1]),
+                          None if self.group is None else self.group.data_ptr(),
+                          0 if groups is None else int(groups[0]))
         nbytes = L.lib().cg_plan_workspace_bytes_ex(mode, self.n, self.shape[0], self.shape[1],
                                                     ctypes.byref(kd), ctypes.byref(opts))
         if nbytes == 0:
@@ -242,6 +246,29 @@ def w_bins(uvw, wstep, status):
     L.call("cg_w_bins", _p(uvw), uvw.stride(0), n, float(wstep), _p(kidx), _p(dmm), hmm,
            _p(status.t), stream())
     return kidx, int(hmm[0]), int(hmm[1])
+
+
+def compact_keys(key, nkeys, status):
+    """(row per element, distinct keys ascending) of int32 keys in [0, nkeys)."""
+    key = cuda_tensor(key, torch.int32)
+    n = key.shape[0]
+    row = torch.empty(n, dtype=torch.int32, device="cuda")
+    kor = torch.empty(nkeys, dtype=torch.int32, device="cuda")
+    nbytes = L.lib().cg_compact_keys_workspace_bytes(int(nkeys))
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    nrows = ctypes.c_int32()
+    L.call("cg_compact_keys", _p(key), n, int(nkeys), _p(row), _p(kor), ctypes.byref(nrows),
+           _p(ws), nbytes, _p(status.t), stream())
+    return row, kor[:nrows.value]
+
+
+def aw_keys(uvw, a1, a2, nant, wstep, kmin, nbins, status):
+    uvw = cuda_tensor(uvw, torch.float64)
+    a1, a2 = cuda_tensor(a1, torch.int32), cuda_tensor(a2, torch.int32)
+    key = torch.empty(uvw.shape[0], dtype=torch.int32, device="cuda")
+    L.call("cg_aw_keys", _p(uvw), uvw.stride(0), _p(a1), _p(a2), uvw.shape[0], int(nant),
+           float(wstep), int(kmin), int(nbins), _p(key), _p(status.t), stream())
+    return key
 
 
 def grid_boxcar(uvw, lam, vis, grid, status):

@@ -152,6 +152,11 @@ typedef struct {
   const int32_t *layer; /* device int32 [n], or NULL when layers == 1 */
   double wstep;
   int kmin;
+  /* CG_PLAN_GROUPS only: launch group per visibility (device int32 [n]) in
+   * [0, ngroups), e.g. the w-plane, when each visibility's kernel row (kidx)
+   * is finer than the launches (AW kernels: one launch per w-plane). */
+  const int32_t *group;
+  int ngroups;
 } cg_plan_opts;
 size_t cg_plan_workspace_bytes_ex(int mode, int64_t n, int H, int W,
                                   const cg_kernel_desc *kd,
@@ -254,6 +259,23 @@ int cg_image_from_grid(void *grid_c64, int H, int W, float *image_out,
 /* image *= 1 / *d_scale (do_imaging's normalisation, synthesis.py:909-911) */
 int cg_scale_image(float *image, int64_t count, const float *d_scale,
                    cg_stream_t stream);
+
+/* Distinct keys: for keys in [0, nkeys), row[i] = rank of key[i] among the
+ * distinct keys present (ascending), key_of_row[r] = the r-th distinct key,
+ * *h_nrows (host) = their number; synchronises the stream.  Replaces the
+ * kernel cache lookup of w_cache_imaging (synthesis.py:788, 794) with one
+ * table row per distinct cache key. */
+size_t cg_compact_keys_workspace_bytes(int nkeys);
+int cg_compact_keys(const int32_t *key, int64_t n, int nkeys, int32_t *row,
+                    int32_t *key_of_row, int32_t *h_nrows, void *workspace,
+                    size_t workspace_bytes, int32_t *d_status,
+                    cg_stream_t stream);
+/* AW cache keys (the (wbin, a1, a2) arguments of aw_kernel_fn through
+ * w_cache_imaging, synthesis.py:719, 793-794; scripts/image_dataset.py:153-171):
+ * key[i] = (a1[i] * nant + a2[i]) * nbins + round(w_i / wstep) - kmin. */
+int cg_aw_keys(const double *uvw, int64_t stride, const int32_t *a1,
+               const int32_t *a2, int64_t n, int nant, double wstep, int kmin,
+               int nbins, int32_t *key, int32_t *d_status, cg_stream_t stream);
 
 /* ------------------------------------------------------------------ */
 /* w-stacking (examples/notebooks/wstacking.ipynb code cell 10, with
