@@ -50,7 +50,7 @@ class AWProjection:
                 wi.astype(numpy.int32))
         self.ktab = E.KernelTable(E.aw_kernels(*args, dtype=E.CF, status=st).reshape(-1), False,
                                   Q, SA)
-        self.plan = E.Plan(self.uvw, lam, (self.N, self.N), self.ktab, rows, status=st)
+        self.replan()
         self.ktab64 = self.plan64 = None
         if fp64:
             self.ktab64 = E.KernelTable(E.aw_kernels(*args, dtype=E.CD, status=st).reshape(-1),
@@ -59,12 +59,33 @@ class AWProjection:
                                  mode=L.CG_PLAN_GROUPS, status=st, groups=(nb, wbin))
         st.check()
 
+    def replan(self):
+        """(Re)build the tiled plan, e.g. after the launch-shape tuning changed."""
+        self.plan = E.Plan(self.uvw, self.lam, (self.N, self.N), self.ktab, self.rows,
+                           status=self.status)
+
+    def tune(self, vis, quick=True):
+        """Autotune the tiled kernels on these visibilities and rebuild the plan."""
+        from . import autotune
+        best, table = autotune.tune(self.uvw, self.lam, (self.N, self.N), self.ktab, self.rows,
+                                    E.cuda_tensor(vis, E.CF),
+                                    cands=autotune.candidates(self.ktab.S, quick=quick),
+                                    use_cache=False)
+        self.replan()
+        return best
+
     def grid(self, vis, out=None):
         g = out if out is not None else torch.zeros((self.N, self.N), dtype=E.CF, device="cuda")
         return self.plan.grid(self.ktab, E.cuda_tensor(vis, E.CF), g)
 
     def degrid(self, grid):
         return self.plan.degrid(self.ktab, E.cuda_tensor(grid, E.CF))
+
+    def degrid_grid(self, grid_in, vis_in, grid_out, residual=False, vis_out=None):
+        """Fused pass: each AW kernel slice is read once for both directions."""
+        return self.plan.degrid_grid(self.ktab, E.cuda_tensor(grid_in, E.CF),
+                                     None if vis_in is None else E.cuda_tensor(vis_in, E.CF),
+                                     grid_out, residual, vis_out)
 
     def grid_fp64(self, vis, out=None):
         g = out if out is not None else torch.zeros((self.N, self.N), dtype=E.CD, device="cuda")

@@ -1,0 +1,209 @@
+"""Throughput and accuracy of every benchmark configuration on the current GPU.
+
+    python -m crocodile_gb300.bench_configs [--only plain,diff,wstack,aw] [--steps K]
+
+For each configuration (see configs.py) it times, with CUDA events on the
+current stream after warm-up, the FP32 batched form and the plain FP64 form
+(or the one-plane-per-launch form for w-stacking), and reports the relative
+L2 error of the FP32 result against the FP64 one.  Prints one JSON object.
+"""
+
+import argparse
+import json
+import statistics
+import time
+
+import numpy
+import torch
+
+from . import _lib as L
+from . import autotune
+from . import configs
+from . import engine as E
+
+
+def _time(fn, steps, warmup=2):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return statistics.median(times)
+
+
+def _rel(a, b):
+    a, b = a.to(torch.complex128), b.to(torch.complex128)
+    return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+
+
+def _aa_kernel(N, Q=8, S=8, c=8):
+    from . import synthesis
+    return synthesis.kernel_oversample(synthesis.anti_aliasing_function(N, 0, c), Q, S)
+
+
+def measure_plain(steps=20):
+    """conv_imaging + conv_predict, 1024^2, 200k visibilities, separable AA kernel S 8 Q 8."""
+    w = configs.plain()
+    n, N = len(w.uvw), w.N
+    kv = _aa_kernel(N)
+    kt, kt64 = E.KernelTable.from_gcf(kv, 0, E.CF), E.KernelTable.from_gcf(kv, 0, E.CD)
+    uvw = E.cuda_tensor(w.uvw, torch.float64)
+    vis, vis64 = E.cuda_tensor(w.vis, E.CF), E.cuda_tensor(w.vis, E.CD)
+    autotune.tune(uvw, w.lam, (N, N), kt, None, vis, cands=autotune.candidates(8, quick=True),
+                  use_cache=False)
+    g = torch.zeros((N, N), dtype=E.CF, device="cuda")
+    g64 = torch.zeros((N, N), dtype=E.CD, device="cuda")
+    out = {}
+
+    def fp32():
+        plan = E.Plan(uvw, w.lam, (N, N), kt)
+        g.zero_()
+        plan.grid(kt, vis, g)
+        out["v"] = plan.degrid(kt, g)
+
+    def fp64():
+        plan = E.Plan(uvw, w.lam, (N, N), kt64, mode=L.CG_PLAN_GROUPS)
+        g64.zero_()
+        plan.grid_fp64(kt64, vis64, g64)
+        out["v64"] = plan.degrid_fp64(kt64, g64)
+
+    ms, ms64 = _time(fp32, steps), _time(fp64, max(3, steps // 4))
+    return {"workload": w.name, "n_vis": n, "ms": ms, "mvis_s": n / ms / 1e3,
+            "plain_fp64_ms": ms64, "plain_fp64_mvis_s": n / ms64 / 1e3, "speedup": ms64 / ms,
+            "rel_err_grid": _rel(g, g64), "rel_err_degrid": _rel(out["v"], out["v64"])}
+
+
+def measure_diff(steps=20):
+    """Predict (FFT + degrid) and its adjoint (grid + N^2 ifft) of a 2048^2 image, 1M vis."""
+    from . import autograd as AG
+    w = configs.diff()
+    n, N = len(w.uvw), w.N
+    kv = _aa_kernel(N)
+    op = AG.GriddingOperator(w.uvw, w.lam, (N, N), E.KernelTable.from_gcf(kv, 0, E.CF))
+    img = torch.from_numpy(w.params["image"]).cuda().requires_grad_(True)
+    obs = op.predict(img).detach() * 1.01
+
+    def step():
+        loss = (torch.abs(op.predict(img) - obs) ** 2).sum()
+        torch.autograd.grad(loss, img)
+
+    ms = _time(step, steps)
+    return {"workload": w.name, "n_vis": n, "ms_forward_backward": ms,
+            "mvis_s": n / ms / 1e3}
+
+
+def measure_wstack(steps=5):
+    """All 32 w-planes in one gridding launch + one batched FFT vs one plane per launch."""
+    from . import synthesis as S
+    w = configs.wstack()
+    n = len(w.uvw)
+    kv = _aa_kernel(w.N)
+    uvw = torch.from_numpy(w.uvw).cuda()
+    vis = torch.from_numpy(w.vis).cuda()
+    plane = w.params["plane"]
+    res = {}
+
+    def batched():
+        res["a"] = S.w_stack_imaging(w.theta, w.lam, uvw, None, vis, kv, plane)
+
+    def per_plane():
+        res["b"] = S.w_stack_imaging(w.theta, w.lam, uvw, None, vis, kv, plane, per_plane=True)
+
+    ms, ms1 = _time(batched, steps, 1), _time(per_plane, steps, 1)
+    return {"workload": w.name, "n_vis": n, "planes": int(plane.max()) + 1, "ms": ms,
+            "mvis_s": n / ms / 1e3, "per_plane_ms": ms1, "per_plane_mvis_s": n / ms1 / 1e3,
+            "speedup": ms1 / ms, "rel_err_batched_vs_per_plane": _rel(res["a"], res["b"]),
+            "note": "times include gridding, FFTs of all planes and the Fresnel combine"}
+
+
+def measure_aw(steps=5, nvis=None, fp64=True):
+    """AW gridding + degridding, 8192^2, 16.1M visibilities, S 16 Q 16 (nvis: only the
+    first nvis visibilities, for profiling)."""
+    from . import awproj
+    w = configs.aw()
+    if nvis:
+        w = configs.wproj_subset(w, nvis)
+        w.params = dict(w.params, a1=w.params["a1"][:nvis], a2=w.params["a2"][:nvis])
+    n = len(w.uvw)
+    t0 = time.perf_counter()
+    op = awproj.AWProjection(w.theta, w.lam, w.uvw, w.params["a1"], w.params["a2"],
+                             w.params["beams"], w.params["wstep"], w.params["NpixFF"], fp64=fp64)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    vis = torch.from_numpy(w.vis.astype(numpy.complex64)).cuda()
+    tuned = op.tune(vis)
+    vis64 = torch.from_numpy(w.vis).cuda() if fp64 else None
+    N = w.N
+    g = torch.zeros((N, N), dtype=E.CF, device="cuda")
+    g64 = torch.zeros((N, N), dtype=E.CD, device="cuda") if fp64 else None
+    out = {}
+
+    def run32():
+        g.zero_()
+        op.grid(vis, g)
+        out["v"] = op.degrid(g)
+
+    def run64():
+        g64.zero_()
+        op.grid_fp64(vis64, g64)
+        out["v64"] = op.degrid_fp64(g64)
+
+    ms = _time(run32, steps)
+    gf = torch.zeros((N, N), dtype=E.CF, device="cuda")
+
+    def fused():
+        gf.zero_()
+        out["vf"] = op.degrid_grid(g, vis, gf)
+
+    ms_fused = _time(fused, steps)
+    if not fp64:
+        return {"workload": w.name, "n_vis": n, "aw_kernels": op.nkernels, "ms": ms,
+                "mvis_s": n / ms / 1e3, "tuning": tuned}
+    ms64 = _time(run64, max(2, steps // 2), 1)
+    return {"workload": w.name, "n_vis": n, "aw_kernels": op.nkernels, "tuning": tuned,
+            "kernel_table_gb": op.ktab.table.numel() * 8 / 1e9, "setup_s": setup_s,
+            "ms": ms, "mvis_s": n / ms / 1e3, "plain_fp64_ms": ms64,
+            "plain_fp64_mvis_s": n / ms64 / 1e3, "speedup": ms64 / ms,
+            "fused_ms": ms_fused, "fused_mvis_s": n / ms_fused / 1e3,
+            "fused_speedup": ms64 / ms_fused,
+            "plain_form": "complex128, FP64 atomics, one launch per w-plane (%d)" % op.nbins,
+            "rel_err_grid": _rel(g, g64), "rel_err_degrid": _rel(out["v"], out["v64"])}
+
+
+MEASURES = {"plain": measure_plain, "diff": measure_diff, "wstack": measure_wstack,
+            "aw": measure_aw}
+
+
+def run(only=None, steps=None):
+    res = {}
+    for name, fn in MEASURES.items():
+        if only and name not in only:
+            continue
+        autotune.set_tuning()
+        res[name] = fn() if steps is None else fn(steps)
+        torch.cuda.empty_cache()
+    autotune.set_tuning()
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", default="")
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--aw-nvis", type=int, default=0,
+                    help="AW only: the first N visibilities, FP32 only (profiling runs)")
+    a = ap.parse_args()
+    if a.aw_nvis:
+        print(json.dumps(measure_aw(a.steps or 2, nvis=a.aw_nvis, fp64=False)))
+        return
+    print(json.dumps(run([s for s in a.only.split(",") if s] or None, a.steps)))
+
+
+if __name__ == "__main__":
+    main()

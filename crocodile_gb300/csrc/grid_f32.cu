@@ -285,20 +285,30 @@ __global__ void __launch_bounds__(256) k_grid_warp(
         s_v[j] = v;
       }
       __syncthreads();
-      for (int j = warp; j < nb; j += nwarps) {
-        const int base = s_base[j];
-        const float2 v = s_v[j];
+      // Software pipeline: the taps of the warp's next visibility are loaded
+      // before the current one's are added, so two slices are in flight.
+      float2 k[MAXT];
+      auto load_taps = [&](int j) {
         const float2 *kk = ktab + s_k0[j];
         const float2 *kx = ktab + s_k1[j];
-        float2 k[MAXT];
 #pragma unroll
         for (int i = 0; i < MAXT; ++i)
           if (soff[i] >= 0)
             k[i] = SEP ? cmul(__ldg(&kk[kdy[i]]), __ldg(&kx[kdx[i]])) : __ldg(&kk[lane + 32 * i]);
+      };
+      int j = warp;
+      if (j < nb) load_taps(j);
+      for (; j < nb; j += nwarps) {
+        float2 kc[MAXT];
+#pragma unroll
+        for (int i = 0; i < MAXT; ++i) kc[i] = k[i];
+        if (j + nwarps < nb) load_taps(j + nwarps);
+        const int base = s_base[j];
+        const float2 v = s_v[j];
 #pragma unroll
         for (int i = 0; i < MAXT; ++i)
           if (soff[i] >= 0) {
-            const float2 u = cmul(k[i], v);
+            const float2 u = cmul(kc[i], v);
             atomicAdd(&win[base + soff[i]].x, u.x);
             atomicAdd(&win[base + soff[i]].y, u.y);
           }
@@ -311,6 +321,130 @@ __global__ void __launch_bounds__(256) k_grid_warp(
       if (val.x != 0.f || val.y != 0.f) {
         const int gy = wy0 + r, gx = wx0 + q;
         if (gy < A.H && gx < A.W) atomicAdd(&grid[org.layer_off + (size_t)gy * A.W + gx], val);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- fused pass
+// Degridding and gridding of the same visibilities in one traversal: every
+// kernel tap is read once for both directions.  Per work item the CTA stages
+// the input grid's window (for degridding) and accumulates an output window;
+// one warp per visibility forms out[i] = sum(grid_in[footprint] * K) and adds
+// K * u into the output window, with u = vis_in[i] (mode 0) or the residual
+// vis_in[i] - out[i] (mode 1, the predict-subtract-invert step of an imaging
+// major cycle).  Both windows are conflict-free thanks to the plan's pitch.
+template <bool SEP, int MAXT>
+__global__ void __launch_bounds__(256) k_degrid_grid_warp(
+    TiledArgs A, int mode, const float2 *__restrict__ ktab, const float2 *__restrict__ grid_in,
+    const float2 *__restrict__ vis_in, float2 *__restrict__ vis_out,
+    float2 *__restrict__ grid_out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_item;
+  if (status_failed(A.status)) return;
+  const int S = A.S, SS = S * S, pitch = A.pitch;
+  const size_t wsz = (size_t)pitch * A.win;
+  float2 *win_in = (float2 *)smem;
+  float2 *win_out = win_in + wsz;
+  int *s_base = (int *)(win_out + wsz);
+  int *s_dst = s_base + GRID_STAGE;
+  long long *s_k0 = (long long *)(s_dst + GRID_STAGE);
+  long long *s_k1 = s_k0 + GRID_STAGE;
+  float2 *s_v = (float2 *)(s_k1 + GRID_STAGE);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const int wcells = A.win * A.win;
+  const long long KSZ = (long long)A.Q * A.Q * SS;
+
+  int soff[MAXT], kdy[MAXT], kdx[MAXT];
+#pragma unroll
+  for (int i = 0; i < MAXT; ++i) {
+    const int t = lane + 32 * i;
+    const int dy = t / S, dx = t - (t / S) * S;
+    soff[i] = (t < SS) ? dy * pitch + dx : -1;
+    kdy[i] = dy;
+    kdx[i] = dx;
+  }
+
+  int it;
+  while ((it = next_item(A, &s_item)) >= 0) {
+    const WorkItem w = A.items[it];
+    const TileOrigin org = tile_origin(A, w.tile);
+    const int wx0 = org.wx0, wy0 = org.wy0;
+    for (int c = tid; c < (int)wsz; c += blockDim.x) win_out[c] = make_float2(0.f, 0.f);
+    for (int c = tid; c < wcells; c += blockDim.x) {
+      const int r = c / A.win, q = c - r * A.win;
+      const int gy = wy0 + r, gx = wx0 + q;
+      win_in[r * pitch + q] = (gy < A.H && gx < A.W)
+                                  ? __ldg(&grid_in[org.layer_off + (size_t)gy * A.W + gx])
+                                  : make_float2(0.f, 0.f);
+    }
+    for (int b = 0; b < w.count; b += GRID_STAGE) {
+      const int nb = min(GRID_STAGE, w.count - b);
+      __syncthreads();
+      for (int j = tid; j < nb; j += blockDim.x) {
+        const int pos = w.start + b + j;
+        const VisRec rec = A.recs[pos];
+        s_base[j] = (rec.y0 - wy0) * pitch + (rec.x0 - wx0);
+        if (SEP) {
+          s_k0[j] = (long long)rec.k0 * S;
+          s_k1[j] = (long long)rec.k1 * S;
+        } else {
+          s_k0[j] = (long long)rec.k0 * KSZ + (long long)rec.k1 * SS;
+        }
+        const int src = A.perm[pos];
+        s_dst[j] = src;
+        s_v[j] = vis_in ? vis_in[src] : make_float2(0.f, 0.f);
+      }
+      __syncthreads();
+      float2 k[MAXT];
+      auto load_taps = [&](int j) {
+        const float2 *kk = ktab + s_k0[j];
+        const float2 *kx = ktab + s_k1[j];
+#pragma unroll
+        for (int i = 0; i < MAXT; ++i)
+          if (soff[i] >= 0)
+            k[i] = SEP ? cmul(__ldg(&kk[kdy[i]]), __ldg(&kx[kdx[i]])) : __ldg(&kk[lane + 32 * i]);
+      };
+      int j = warp;
+      if (j < nb) load_taps(j);
+      for (; j < nb; j += nwarps) {
+        float2 kc[MAXT];
+#pragma unroll
+        for (int i = 0; i < MAXT; ++i) kc[i] = k[i];
+        if (j + nwarps < nb) load_taps(j + nwarps);
+        const int base = s_base[j];
+        float2 sum = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i < MAXT; ++i)
+          if (soff[i] >= 0) cfma(sum, win_in[base + soff[i]], kc[i]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          sum.x += __shfl_xor_sync(0xffffffffu, sum.x, o);
+          sum.y += __shfl_xor_sync(0xffffffffu, sum.y, o);
+        }
+        if (lane == 0 && vis_out) vis_out[s_dst[j]] = sum;
+        float2 u = s_v[j];
+        if (mode == 1) {
+          u.x -= sum.x;
+          u.y -= sum.y;
+        }
+#pragma unroll
+        for (int i = 0; i < MAXT; ++i)
+          if (soff[i] >= 0) {
+            const float2 c = cmul(kc[i], u);
+            atomicAdd(&win_out[base + soff[i]].x, c.x);
+            atomicAdd(&win_out[base + soff[i]].y, c.y);
+          }
+      }
+    }
+    __syncthreads();
+    for (int c = tid; c < wcells; c += blockDim.x) {
+      const int r = c / A.win, q = c - r * A.win;
+      const float2 val = win_out[r * pitch + q];
+      if (val.x != 0.f || val.y != 0.f) {
+        const int gy = wy0 + r, gx = wx0 + q;
+        if (gy < A.H && gx < A.W)
+          atomicAdd(&grid_out[org.layer_off + (size_t)gy * A.W + gx], val);
       }
     }
   }
@@ -566,6 +700,45 @@ int cg_degrid(const cg_plan *p, const void *ktab, const void *grid, void *out,
   fn<<<(unsigned)blocks, threads, smem, s>>>(A, (const float2 *)ktab, (const float2 *)grid,
                                               (float2 *)out);
   CG_LAUNCH("degrid");
+  return CG_OK;
+}
+
+int cg_degrid_grid(const cg_plan *p, const void *ktab, const void *grid_in, const void *vis_in,
+                   int residual, void *vis_out, void *grid_out, cg_stream_t stream) {
+  CG_REQUIRE(p && p->mode == CG_PLAN_TILED, "cg_degrid_grid needs a CG_PLAN_TILED plan");
+  if (p->n == 0) return CG_OK;
+  CG_REQUIRE(ktab && grid_in && grid_out, "NULL kernel table or grid");
+  CG_REQUIRE(vis_in || !residual, "the residual mode needs input visibilities");
+  CG_REQUIRE(grid_in != grid_out, "input and output grids must differ");
+  cudaStream_t s = (cudaStream_t)stream;
+  TiledArgs A = tiled_args(p);
+  const int S = p->kd.S;
+  const int need = (S * S + 31) / 32;
+  int maxt = 1;
+  while (maxt < need) maxt *= 2;
+  void *fn = nullptr;
+#define PICK(M)                                                                      \
+  if (maxt == M) fn = p->kd.sep ? (void *)k_degrid_grid_warp<true, M>                 \
+                                : (void *)k_degrid_grid_warp<false, M>;
+  PICK(1) PICK(2) PICK(4) PICK(8) PICK(16) PICK(32)
+#undef PICK
+  CG_REQUIRE(fn, "no fused kernel for support %d", S);
+  const cg_tuning t = tuning();
+  const int threads = 32 * (t.groups > 0 ? t.groups : 8);
+  const size_t smem = 2 * (size_t)p->pitch * p->win * sizeof(float2) +
+                      (size_t)GRID_STAGE * (4 + 4 + 8 + 8 + 8);
+  CG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+  CG_REQUIRE(per_sm > 0, "fused kernel does not fit on an SM (smem %zu)", smem);
+  int64_t blocks = std::min<int64_t>((int64_t)per_sm * num_sms(), p->max_items);
+  CG_CUDA(cudaMemsetAsync(p->ticket, 0, sizeof(int32_t), s));
+  int mode = residual ? 1 : 0;
+  const float2 *kt = (const float2 *)ktab, *gi = (const float2 *)grid_in,
+               *vi = (const float2 *)vis_in;
+  float2 *vo = (float2 *)vis_out, *go = (float2 *)grid_out;
+  void *args[] = {&A, &mode, &kt, &gi, &vi, &vo, &go};
+  CG_CUDA(cudaLaunchKernel(fn, dim3((unsigned)blocks), dim3(threads), args, smem, s));
   return CG_OK;
 }
 

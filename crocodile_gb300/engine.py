@@ -214,6 +214,16 @@ class Plan:
         L.call("cg_degrid", self.handle, _p(t), _p(grid), _p(out), stream())
         return out
 
+    def degrid_grid(self, ktab, grid_in, vis_in, grid_out, residual=False, vis_out=None):
+        """One pass: vis_out = degrid(grid_in); grid_out += grid(vis_in, or vis_in - vis_out
+        when residual).  Returns vis_out."""
+        t = self._table(ktab, CF)
+        if vis_out is None:
+            vis_out = torch.empty(self.n, dtype=CF, device="cuda")
+        L.call("cg_degrid_grid", self.handle, _p(t), _p(grid_in), _p(vis_in), int(bool(residual)),
+               _p(vis_out), _p(grid_out), stream())
+        return vis_out
+
     def grid_fp64(self, ktab, vis, grid):
         t = self._table(ktab, CD)
         L.call("cg_grid_fp64", self.handle, _p(t), _p(vis), _p(grid), stream())

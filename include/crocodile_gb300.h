@@ -184,6 +184,17 @@ int cg_grid_weighted(const cg_plan *plan, const void *ktab_c64,
 /* convdegrid (synthesis.py:484-503): out[i] = sum(grid[footprint] * K). */
 int cg_degrid(const cg_plan *plan, const void *ktab_c64, const void *grid_c64,
               void *vis_out_c64, cg_stream_t stream);
+/* Degridding and gridding in one pass over the plan (each kernel tap read
+ * once for both): vis_out = convdegrid(grid_in) (synthesis.py:484-503) and
+ * grid_out += convgrid of u (:464-481) with u = vis_in, or, with
+ * residual != 0, u = vis_in - vis_out (predict, subtract and invert: the
+ * major-cycle step of do_predict followed by do_imaging's gridding).
+ * vis_in may be NULL without residual (grids zeros); vis_out may be NULL.
+ * grid_in and grid_out must differ.  FP32, c64 data. */
+int cg_degrid_grid(const cg_plan *plan, const void *ktab_c64,
+                   const void *grid_in_c64, const void *vis_in_c64, int residual,
+                   void *vis_out_c64, void *grid_out_c64, cg_stream_t stream);
+
 /* cg_grid_noalloc: no counterpart in the reference.  For callers that
  * cannot allocate device memory (a pipeline that owns all GPU memory in its
  * own pool and may not call cudaMalloc/cudaFree while it runs, or an FFI

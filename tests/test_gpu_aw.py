@@ -68,4 +68,13 @@ def test_aw_full_size_fp32_vs_fp64(aw_workload):
     err = float(torch.linalg.vector_norm(v32.to(torch.complex128) - v64) /
                 torch.linalg.vector_norm(v64))
     assert err < 1e-5, err
+    # the fused pass (each AW slice read once) gives both results at once
+    gf = torch.zeros_like(g32)
+    vf = op.degrid_grid(g64.to(torch.complex64), vis, gf)
+    err = float(torch.linalg.vector_norm(gf.to(torch.complex128) - g64) /
+                torch.linalg.vector_norm(g64))
+    assert err < 1e-5, err
+    err = float(torch.linalg.vector_norm(vf.to(torch.complex128) - v64) /
+                torch.linalg.vector_norm(v64))
+    assert err < 1e-5, err
     op.status.check()

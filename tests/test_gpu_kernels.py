@@ -155,3 +155,30 @@ def test_fused_wbin_plan(env):
     with pytest.raises(IndexError):
         plan.check()
     assert float(g2.abs().sum()) == 0.0
+
+
+@pytest.mark.parametrize("sep", [False, True])
+def test_fused_degrid_grid_matches_separate(env, sep):
+    torch, E, S, A, O = env
+    theta, lam, uvw, vis = _wproj_case(O, n=30000, N=256, seed=13)
+    N = int(round(theta * lam))
+    aa = O.anti_aliasing_function(N, 0, 7)
+    kv = O.kernel_oversample(aa, 4, 7) if sep else O.kernel_oversample(numpy.outer(aa, aa), 4, 7)
+    kt = E.KernelTable.from_gcf(kv, 0, E.CF)
+    plan = E.Plan(uvw, lam, (N, N), kt)
+    rng = numpy.random.default_rng(3)
+    model = E.cuda_tensor(rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N)), E.CF)
+    v_in = E.cuda_tensor(vis, E.CF)
+    ref_v = plan.degrid(kt, model)
+    ref_g = plan.grid(kt, v_in, torch.zeros((N, N), dtype=E.CF, device="cuda"))
+    g = torch.zeros((N, N), dtype=E.CF, device="cuda")
+    v = plan.degrid_grid(kt, model, v_in, g)
+    plan.check()
+    r = lambda a, b: float(torch.linalg.vector_norm((a - b).to(torch.complex128)) /
+                           torch.linalg.vector_norm(b.to(torch.complex128)))
+    assert r(v, ref_v) < 1e-6 and r(g, ref_g) < 1e-6
+    # residual mode: grid(vis - degrid(model))
+    ref_res = plan.grid(kt, v_in - ref_v, torch.zeros((N, N), dtype=E.CF, device="cuda"))
+    g2 = torch.zeros((N, N), dtype=E.CF, device="cuda")
+    plan.degrid_grid(kt, model, v_in, g2, residual=True)
+    assert r(g2, ref_res) < 1e-5
