@@ -1,19 +1,27 @@
 #!/usr/bin/env python
-"""Benchmark: grid + degrid throughput (Mvis/s) of the w-projection workload on GB300.
+"""Benchmark: convolutional grid + degrid throughput (Mvis/s) on one GB300.
 
-Workload (seeded synthetic, the w_cache_imaging configuration): 4096^2 grid,
-theta 0.1, 2M visibilities with 1/r radial uv density inside 0.45 lam and
-|w| <= 500, w-kernels support 15, oversampling 8, w-step 10 (101 kernels,
-NpixFF 64).  One step = w binning + plan (bit-exact coordinates, tile sort,
-work list) + FP32 tiled gridding (w_cache_imaging) + FP32 tiled degridding
-(w_cache_predict) of all visibilities, inputs resident in HBM.  Kernels are
-generated once (a kernel cache, as the reference's pylru cache) and reported
-separately.
+Default workload (--workload aw, the AW-projection configuration the target
+is stated on): 8192^2 grid, theta 0.05, 16,128,000 visibilities of 64
+antennas (2016 baselines x 125 hour angles x 64 channels, Earth-rotation
+uvw), AW kernels = (A1 conv A2) conv W (support 16, oversampling 16) for
+every distinct (w bin, antenna pair) -- 27,751 kernels, 14.5 GB resident in
+HBM, generated once as the reference's kernel cache does and reported
+separately.  --workload wproj: 4096^2 w-projection, 2M visibilities, S 15,
+Q 8, 101 w-kernels.
+
+One step = plan (bit-exact FP64 cell assignment, tile sort, work list) + FP32
+tiled gridding + FP32 tiled degridding of all visibilities, inputs resident
+in HBM.  The same line reports the plain FP64 form (complex128, FP64
+atomics, one launch per w-plane), FP32-vs-FP64 errors, the fused
+degrid+grid pass, end to end with host buffers, the roofline of the dominant
+kernel, the other configurations and a single-core CPU baseline.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload aw|wproj]
 
 --impl reference times the CPU oracle (a numpy restatement of the
-reference's algorithm) on the host cores over a bounded sample.
+reference's algorithm) on the host cores over bounded samples.
 Prints one JSON line (rank 0).
 """
 
@@ -33,19 +41,19 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "grid+degrid Mvis/s per GB300, FP32 batched vs plain, at <=1e-5 rel err vs FP64"
-WSTEP, NPIXFF = 10.0, 64
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--nvis", type=int, default=2_000_000)
+    ap.add_argument("--workload", default="aw", choices=["aw", "wproj"])
     ap.add_argument("--plain-steps", type=int, default=2)
-    ap.add_argument("--cpu-sample", type=int, default=400_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other configurations' measurements")
     return ap.parse_args()
 
 
@@ -56,58 +64,96 @@ def dist_env():
     return world, rank, local
 
 
+def make_workload(name, rank=0):
+    from crocodile_gb300 import configs
+    if name == "aw":
+        return configs.aw(seed=20261207 + rank)
+    return configs.wproj(seed=20261204 + rank)
+
+
 # --------------------------------------------------------------------------- CPU (oracle) arm
 
 _CPU = {}
 
 
-def _cpu_init(table, kmin, theta, lam, shared, lock):
+def _cpu_init(table, theta, lam, shared, lock):
     os.environ["OMP_NUM_THREADS"] = "1"
-    _CPU.update(table=table, kmin=kmin, theta=theta, lam=lam, shared=shared, lock=lock)
+    _CPU.update(table=table, theta=theta, lam=lam, shared=shared, lock=lock)
 
 
 def _cpu_shard(job):
-    """Oracle grid + degrid of one visibility shard; the shard grid is added into
-    the shared grid under its lock (the pattern of scripts/image_dataset.py:190-219)."""
-    uvw, vis = job
+    """Oracle grid + degrid of one visibility shard with a prepared kernel table; the
+    shard grid is added into the shared grid under its lock (the pattern of
+    scripts/image_dataset.py:190-219)."""
+    uvw, vis, rows = job
     from oracle import crocodile_oracle as O
-    table, kmin, lam = _CPU["table"], _CPU["kmin"], _CPU["lam"]
+    table, lam = _CPU["table"], _CPU["lam"]
     N = int(round(_CPU["theta"] * lam))
     g = numpy.zeros((N, N), dtype=complex)
-    k = numpy.round(uvw[:, 2] / WSTEP).astype(int) - kmin
     x, xf, y, yf = O.frac_coords(g.shape, table.shape[1], uvw / lam)
-    O.convgrid_indexed(table, False, g, x, xf, y, yf, k, vis)
-    v = O.convdegrid_indexed(table, False, g, x, xf, y, yf, k)
+    O.convgrid_indexed(table, False, g, x, xf, y, yf, rows, vis)
+    v = O.convdegrid_indexed(table, False, g, x, xf, y, yf, rows)
     if _CPU["shared"] is not None:
         with _CPU["lock"]:
             numpy.frombuffer(_CPU["shared"].get_obj(), dtype=complex).reshape(N, N)[...] += g
     return len(v)
 
 
+def oracle_sample(name, w, sample):
+    """(uvw, vis, rows, kernel table) of a bounded sample, kernels from the oracle.
+
+    wproj: the first `sample` visibilities, one w-kernel per bin.  aw: all
+    visibilities of the first baselines up to `sample`, one AW kernel per
+    distinct (w bin, a1, a2) from the oracle's aw_kernel_fft (equal to
+    aw_kernel_fn to rounding, batched over sub-kernels so large samples are
+    affordable)."""
+    from oracle import crocodile_oracle as O
+    if name == "wproj":
+        wstep, npff = w.params["wstep"], w.params["NpixFF"]
+        uvw, vis = w.uvw[:sample], w.vis[:sample]
+        k = numpy.round(uvw[:, 2] / wstep).astype(int)
+        table = numpy.array([O.w_kernel(w.theta, wstep * kk, npff, w.S, w.Q)
+                             for kk in range(k.min(), k.max() + 1)])
+        return uvw, vis, k - k.min(), table
+    a1, a2 = w.params["a1"], w.params["a2"]
+    bl = a1.astype(numpy.int64) * w.params["nant"] + a2
+    order = numpy.unique(bl)
+    take = numpy.zeros(len(bl), bool)
+    for b in order:
+        take |= bl == b
+        if take.sum() >= sample:
+            break
+    uvw, vis = w.uvw[take], w.vis[take]
+    wstep, npff, beams = w.params["wstep"], w.params["NpixFF"], w.params["beams"]
+    wbin = wstep * numpy.round(uvw[:, 2] / wstep)
+    keys = numpy.column_stack([wbin, a1[take], a2[take]])
+    uniq, rows = numpy.unique(keys, axis=0, return_inverse=True)
+    akern = {a: O.kernel_oversample(beams[a], 1, 16)[0, 0]
+             for a in numpy.unique(numpy.concatenate([a1[take], a2[take]]))}
+    wkern = {kw: O.w_kernel(w.theta, kw, npff, 16, 16) for kw in numpy.unique(wbin)}
+    table = numpy.array([O.aw_kernel_fft(akern[int(p)], akern[int(q)], wkern[kw])
+                         for kw, p, q in uniq])
+    return uvw, vis, rows.ravel(), table
+
+
 class CpuArm:
     """The numpy oracle on `procs` host processes (spawned once, before timing)."""
 
-    def __init__(self, w, sample, procs):
-        from oracle import crocodile_oracle as O
-        self.w, self.sample, self.procs = w, sample, procs
-        self.uvw, self.vis = w.uvw[:sample], w.vis[:sample]
-        k = numpy.round(self.uvw[:, 2] / WSTEP).astype(int)
-        self.kmin, kmax = int(k.min()), int(k.max())
-        self.table = numpy.array([O.w_kernel(w.theta, WSTEP * kk, NPIXFF, w.S, w.Q)
-                                  for kk in range(self.kmin, kmax + 1)])
+    def __init__(self, name, w, sample, procs):
+        self.uvw, self.vis, self.rows, table = oracle_sample(name, w, sample)
+        self.sample, self.procs = len(self.uvw), procs
         self.pool = None
         if procs > 1:
             ctx = mp.get_context("spawn")
-            self.shared = ctx.Array(ctypes.c_double, 2 * w.N * w.N)
-            self.pool = ctx.Pool(procs, _cpu_init, (self.table, self.kmin, w.theta, w.lam,
-                                                     self.shared, ctx.Lock()))
-            self.pool.map(_cpu_shard, [(self.uvw[:8], self.vis[:8])] * procs)
+            shared = ctx.Array(ctypes.c_double, 2 * w.N * w.N)
+            self.pool = ctx.Pool(procs, _cpu_init, (table, w.theta, w.lam, shared, ctx.Lock()))
+            self.pool.map(_cpu_shard, [(self.uvw[:8], self.vis[:8], self.rows[:8])] * procs)
         else:
-            _cpu_init(self.table, self.kmin, w.theta, w.lam, None, None)
+            _cpu_init(table, w.theta, w.lam, None, None)
 
     def measure(self):
         shards = numpy.array_split(numpy.arange(self.sample), self.procs)
-        jobs = [(self.uvw[s], self.vis[s]) for s in shards]
+        jobs = [(self.uvw[s], self.vis[s], self.rows[s]) for s in shards]
         t0 = time.perf_counter()
         if self.pool is None:
             _cpu_shard(jobs[0])
@@ -122,30 +168,22 @@ class CpuArm:
             self.pool.join()
 
 
-def cpu_measure(w, sample, procs):
-    arm = CpuArm(w, sample, procs)
-    try:
-        return arm.measure()
-    finally:
-        arm.close()
-
-
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    from crocodile_gb300 import configs
-    w = configs.wproj(n=args.nvis)
+    w = make_workload(args.workload)
+    n = len(w.uvw)
     procs = os.cpu_count() or 1
-    # size each step's sample so that all K steps take about 90 s of host time
-    probe = CpuArm(w, min(args.nvis, 4000 * procs), procs)
+    # size each step's sample so that all steps take about 90 s of host time
+    probe = CpuArm(args.workload, w, min(n, 8000 * procs), procs)
     probe.measure()
     rate, _ = probe.measure()
     probe.close()
-    sample = int(min(args.nvis, max(2000 * procs, rate * 1e6 * 90.0 / max(args.steps, 1))))
-    arm = CpuArm(w, sample, procs)
+    sample = int(min(n, max(2000 * procs, rate * 1e6 * 90.0 / max(min(args.steps, 20), 1))))
+    arm = CpuArm(args.workload, w, sample, procs)
     rates, secs = [], []
-    for i in range(args.steps + 1):
+    for i in range(min(args.steps, 20) + 1):
         r, dt = arm.measure()
         if i:  # the first pass is a warm-up
             rates.append(r)
@@ -154,17 +192,19 @@ def run_reference(args):
     value = statistics.median(rates)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mvis/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * statistics.median(secs) * args.nvis / sample,
+        "n_gpus": args.gpus, "steps": len(rates), "warmup": 1,
+        "ms_per_step": 1e3 * statistics.median(secs) * n / arm.sample,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
         "data": "synthetic (seeded)",
-        "config": {"workload": w.name, "n_vis": args.nvis, "N": w.N, "S": w.S, "Q": w.Q,
-                   "wstep": WSTEP, "NpixFF": NPIXFF},
+        "config": {"workload": w.name, "n_vis": n, "N": w.N, "S": w.S, "Q": w.Q},
         "cpu_baseline": {"value": value, "unit": "Mvis/s", "cores": procs, "kind": "port",
-                         "sample": "%d of %d visibilities per step, grid+degrid, numpy oracle, "
-                                   "%d spawned processes over visibility shards, shard grids "
-                                   "summed into a shared grid under a lock"
-                                   % (sample, args.nvis, procs)},
+                         "sample": "%d of %d visibilities per step (%s), grid+degrid, numpy "
+                                   "oracle, %d spawned processes over visibility shards, shard "
+                                   "grids summed into a shared grid under a lock; kernels "
+                                   "generated once before timing"
+                                   % (arm.sample, n, "all visibilities of the first baselines"
+                                      if args.workload == "aw" else "first visibilities",
+                                      procs)},
         "e2e": {"value": value, "unit": "Mvis/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -217,6 +257,186 @@ class Clocks:
                 "samples": len(sm)}
 
 
+class GpuWorkload:
+    """Device-resident inputs, kernel table and the step closures of one workload."""
+
+    def __init__(self, name, w):
+        import torch
+        from crocodile_gb300 import _lib as L
+        from crocodile_gb300 import engine as E
+        self.torch, self.L, self.E = torch, L, E
+        self.name, self.w = name, w
+        self.n, self.N, self.S, self.Q = len(w.uvw), w.N, w.S, w.Q
+        self.dev = torch.device("cuda", torch.cuda.current_device())
+        self.uvw = torch.from_numpy(w.uvw).to(self.dev)
+        self.vis = torch.from_numpy(w.vis.astype(numpy.complex64)).to(self.dev)
+        self.st = E.Status()
+        self.stream = torch.cuda.current_stream()
+        self.sp = ctypes.c_void_p(self.stream.cuda_stream)
+        t0 = time.perf_counter()
+        self._prepare()
+        torch.cuda.synchronize()
+        self.kgen_ms = 1e3 * (time.perf_counter() - t0)
+        self.grid = torch.zeros((self.N, self.N), dtype=torch.complex64, device=self.dev)
+        self.grid_out = torch.zeros_like(self.grid)
+        self.out = torch.empty(self.n, dtype=torch.complex64, device=self.dev)
+
+    @staticmethod
+    def P(t):
+        return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+    def _alloc_ws(self):
+        kd = self.kt.desc()
+        self.kd = kd
+        self.ws_bytes = self.L.lib().cg_plan_workspace_bytes(self.L.CG_PLAN_TILED, self.n, self.N,
+                                                             self.N, ctypes.byref(kd))
+        self.ws = self.torch.empty(self.ws_bytes, dtype=self.torch.uint8, device=self.dev)
+
+    def tune(self):
+        from crocodile_gb300 import autotune
+        t0 = time.perf_counter()
+        self.tuned, _ = autotune.tune(self.uvw, self.w.lam, (self.N, self.N), self.kt,
+                                      self.tune_kidx(), self.vis,
+                                      cands=autotune.candidates(self.S, quick=True),
+                                      use_cache=False)
+        self.tune_s = time.perf_counter() - t0
+        self._alloc_ws()
+
+    def step(self, uvw, vis, kev=None):
+        """plan + grid + degrid, all stream-ordered (no host synchronisation)."""
+        L, P = self.L, self.P
+        h = ctypes.c_void_p()
+        self.create_plan(h, uvw)
+        self.grid.zero_()
+        if kev:
+            kev[0].record(self.stream)
+        L.call("cg_grid", h, P(self.kt.table), P(vis), P(self.grid), self.sp)
+        if kev:
+            kev[1].record(self.stream)
+        L.call("cg_degrid", h, P(self.kt.table), P(self.grid), P(self.out), self.sp)
+        if kev:
+            kev[2].record(self.stream)
+        L.lib().cg_plan_destroy(h)
+
+    def fused_step(self):
+        L, P = self.L, self.P
+        h = ctypes.c_void_p()
+        self.create_plan(h, self.uvw)
+        self.grid_out.zero_()
+        L.call("cg_degrid_grid", h, P(self.kt.table), P(self.grid), P(self.vis), 0, P(self.out),
+               P(self.grid_out), self.sp)
+        L.lib().cg_plan_destroy(h)
+
+    def kernel_bytes_per_vis(self):
+        return 0
+
+
+class WProjGpu(GpuWorkload):
+    def _prepare(self):
+        E, w = self.E, self.w
+        self.wstep, npff = w.params["wstep"], w.params["NpixFF"]
+        _, self.kmin, kmax = E.w_bins(self.uvw, self.wstep, self.st)
+        self.nk = kmax - self.kmin + 1
+        self.wlist = self.wstep * numpy.arange(self.kmin, kmax + 1).astype(float)
+        self.kt = E.KernelTable(E.w_kernels(w.theta, self.wlist, npff, self.S, self.Q,
+                                            dtype=E.CF).reshape(-1), False, self.Q, self.S)
+        self._alloc_ws()
+        self.groups_desc = "one launch per w-plane (%d)" % self.nk
+
+    def tune_kidx(self):
+        return self.E.w_bins(self.uvw, self.wstep, self.st)[0]
+
+    def create_plan(self, h, uvw):
+        P = self.P
+        self.L.call("cg_plan_create_wbins", ctypes.byref(h), self.L.CG_PLAN_TILED,
+                    ctypes.byref(self.kd), self.N, self.N, P(uvw), 3, self.w.lam, self.wstep,
+                    self.kmin, self.n, P(self.ws), self.ws_bytes, P(self.st.t), self.sp)
+
+    def plain(self, steps):
+        """(ms per plain FP64 step, FP32-vs-FP64 errors)."""
+        E, torch = self.E, self.torch
+        kt64 = E.KernelTable(E.w_kernels(self.w.theta, self.wlist, self.w.params["NpixFF"],
+                                         self.S, self.Q, dtype=E.CD).reshape(-1), False, self.Q,
+                             self.S)
+        vis64 = torch.from_numpy(self.w.vis).to(self.dev)
+        g64 = torch.zeros((self.N, self.N), dtype=torch.complex128, device=self.dev)
+        kidx = self.tune_kidx()
+        ms = []
+        for i in range(steps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            plan = E.Plan(self.uvw, self.w.lam, (self.N, self.N), kt64, kidx,
+                          self.L.CG_PLAN_GROUPS, status=self.st)
+            g64.zero_()
+            plan.grid_fp64(kt64, vis64, g64)
+            o64 = plan.degrid_fp64(kt64, g64)
+            torch.cuda.synchronize()
+            if i:
+                ms.append(1e3 * (time.perf_counter() - t0))
+        self.step(self.uvw, self.vis)
+        o32 = E.Plan(self.uvw, self.w.lam, (self.N, self.N), self.kt, kidx,
+                     status=self.st).degrid(self.kt, g64.to(torch.complex64))
+        torch.cuda.synchronize()
+        return statistics.mean(ms), _rel(self.grid, g64), _rel(o32, o64)
+
+
+class AWGpu(GpuWorkload):
+    def _prepare(self):
+        from crocodile_gb300 import awproj
+        w = self.w
+        self.op = awproj.AWProjection(w.theta, w.lam, self.uvw, w.params["a1"], w.params["a2"],
+                                      w.params["beams"], w.params["wstep"], w.params["NpixFF"])
+        self.kt, self.rows = self.op.ktab, self.op.rows
+        self._alloc_ws()
+        self.groups_desc = "one launch per w-plane (%d)" % self.op.nbins
+
+    def tune_kidx(self):
+        return self.rows
+
+    def create_plan(self, h, uvw):
+        P = self.P
+        self.L.call("cg_plan_create", ctypes.byref(h), self.L.CG_PLAN_TILED, ctypes.byref(self.kd),
+                    self.N, self.N, P(uvw), 3, self.w.lam, P(self.rows), self.n, P(self.ws),
+                    self.ws_bytes, P(self.st.t), self.sp)
+
+    def kernel_bytes_per_vis(self):
+        return self.S * self.S * 8  # each visibility's AW kernel slice
+
+    def plain(self, steps):
+        """(ms per plain FP64 step, FP32-vs-FP64 errors): the same AW kernels held as
+        complex128, FP64 atomics, one launch per w-plane."""
+        E, torch, op, w = self.E, self.torch, self.op, self.w
+        op.enable_fp64()
+        vis64 = torch.from_numpy(w.vis).to(self.dev)
+        g64 = torch.zeros((self.N, self.N), dtype=torch.complex128, device=self.dev)
+        ms = []
+        for i in range(steps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            plan = E.Plan(self.uvw, w.lam, (self.N, self.N), op.ktab64, op.rows,
+                          mode=self.L.CG_PLAN_GROUPS, status=self.st, groups=(op.nbins, op.wbin))
+            g64.zero_()
+            plan.grid_fp64(op.ktab64, vis64, g64)
+            o64 = plan.degrid_fp64(op.ktab64, g64)
+            torch.cuda.synchronize()
+            if i:
+                ms.append(1e3 * (time.perf_counter() - t0))
+        self.step(self.uvw, self.vis)
+        o32 = op.degrid(g64.to(torch.complex64))
+        torch.cuda.synchronize()
+        errs = (_rel(self.grid, g64), _rel(o32, o64))
+        del g64, vis64, plan
+        op.disable_fp64()
+        torch.cuda.empty_cache()
+        return (statistics.mean(ms),) + errs
+
+
+def _rel(a, b):
+    import torch
+    a, b = a.to(torch.complex128), b.to(torch.complex128)
+    return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+
+
 def run_ours(args):
     import torch
     import __graft_entry__
@@ -229,69 +449,21 @@ def run_ours(args):
         torch.cuda.set_device(0)
     __graft_entry__.build()
     from crocodile_gb300 import _lib as L
-    from crocodile_gb300 import configs
-    from crocodile_gb300 import engine as E
-
-    lib = L.lib()
-    dev = torch.device("cuda", torch.cuda.current_device())
-    w = configs.wproj(seed=20261204 + rank, n=args.nvis)
-    n = w.uvw.shape[0]
-    stream = torch.cuda.current_stream()
-    sp = ctypes.c_void_p(stream.cuda_stream)
-    P = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
-
-    uvw = torch.from_numpy(w.uvw).to(dev)
-    vis = torch.from_numpy(w.vis.astype(numpy.complex64)).to(dev)
-    st = E.Status()
-    # kernel table for the bins present (generated once, reported separately)
-    _, kmin, kmax = E.w_bins(uvw, WSTEP, st)
-    nk = kmax - kmin + 1
-    t0 = time.perf_counter()
-    table = E.w_kernels(w.theta, WSTEP * numpy.arange(kmin, kmax + 1).astype(float), NPIXFF, w.S,
-                        w.Q, dtype=E.CF)
-    torch.cuda.synchronize()
-    kgen_ms = 1e3 * (time.perf_counter() - t0)
-    kt = E.KernelTable(table.reshape(-1), False, w.Q, w.S)
-    kd = kt.desc()
-    N = w.N
-    kidx = torch.empty(n, dtype=torch.int32, device=dev)
-    grid = torch.zeros((N, N), dtype=torch.complex64, device=dev)
-    out = torch.empty(n, dtype=torch.complex64, device=dev)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    ev = lambda: torch.cuda.Event(enable_timing=True)
-
-    # launch-shape autotuning on this workload (outside the timed region)
     from crocodile_gb300 import autotune
-    kidx_t, _, _ = E.w_bins(uvw, WSTEP, st)
-    t0 = time.perf_counter()
-    tuned, _ = autotune.tune(uvw, w.lam, (w.N, w.N), kt, kidx_t, vis,
-                             cands=autotune.candidates(w.S, quick=True), use_cache=False)
-    tune_s = time.perf_counter() - t0
-    del kidx_t
-    ws_bytes = lib.cg_plan_workspace_bytes(L.CG_PLAN_TILED, n, N, N, ctypes.byref(kd))
-    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
 
-    def step(uvw_t, vis_t, kev=None):
-        h = ctypes.c_void_p()
-        L.call("cg_plan_create_wbins", ctypes.byref(h), L.CG_PLAN_TILED, ctypes.byref(kd), N, N,
-               P(uvw_t), 3, w.lam, WSTEP, kmin, n, P(ws), ws_bytes, P(st.t), sp)
-        grid.zero_()
-        if kev:
-            kev[0].record(stream)
-        L.call("cg_grid", h, P(kt.table), P(vis_t), P(grid), sp)
-        if kev:
-            kev[1].record(stream)
-        L.call("cg_degrid", h, P(kt.table), P(grid), P(out), sp)
-        if kev:
-            kev[2].record(stream)
-        lib.cg_plan_destroy(h)
-
-    info_plan = E.Plan(uvw, w.lam, (N, N), kt, status=st, wbins=(WSTEP, kmin)).info()
-    st.reset()
+    w = make_workload(args.workload, rank)
+    G = (AWGpu if args.workload == "aw" else WProjGpu)(args.workload, w)
+    G.tune()
+    n, N, S, Q = G.n, G.N, G.S, G.Q
+    stream = G.stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=G.dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    info_plan = G.E.Plan(G.uvw, w.lam, (N, N), G.kt, G.tune_kidx(), status=G.st).info()
+    G.st.reset()
     for _ in range(max(args.warmup, 3)):
-        step(uvw, vis)
+        G.step(G.uvw, G.vis)
     torch.cuda.synchronize()
-    st.check()
+    G.st.check()
 
     # ---- timed region (device-resident inputs)
     if world > 1:
@@ -304,7 +476,7 @@ def run_ours(args):
         e0, e1 = ev(), ev()
         kev = [ev(), ev(), ev()]
         e0.record(stream)
-        step(uvw, vis, kev)
+        G.step(G.uvw, G.vis, kev)
         e1.record(stream)
         times.append((e0, e1))
         tg.append((kev[0], kev[1]))
@@ -316,9 +488,9 @@ def run_ours(args):
     ms = statistics.mean(a.elapsed_time(b) for a, b in times)
     ms_grid = statistics.mean(a.elapsed_time(b) for a, b in tg)
     ms_degrid = statistics.mean(a.elapsed_time(b) for a, b in td)
-    st.check()
+    G.st.check()
     if world > 1:
-        t = torch.tensor([ms], device=dev)
+        t = torch.tensor([ms], device=G.dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = world * n / (ms * 1e-3) / 1e6
@@ -328,8 +500,7 @@ def run_ours(args):
     h_vis = torch.from_numpy(w.vis.astype(numpy.complex64)).pin_memory()
     h_grid = torch.empty((N, N), dtype=torch.complex64).pin_memory()
     h_out = torch.empty(n, dtype=torch.complex64).pin_memory()
-    d_uvw = torch.empty_like(uvw)
-    d_vis = torch.empty_like(vis)
+    d_uvw, d_vis = torch.empty_like(G.uvw), torch.empty_like(G.vis)
     e2e_times = []
     for i in range(min(args.steps, 20) + 1):
         flush.zero_()
@@ -337,9 +508,9 @@ def run_ours(args):
         e0.record(stream)
         d_uvw.copy_(h_uvw, non_blocking=True)
         d_vis.copy_(h_vis, non_blocking=True)
-        step(d_uvw, d_vis)
-        h_grid.copy_(grid, non_blocking=True)
-        h_out.copy_(out, non_blocking=True)
+        G.step(d_uvw, d_vis)
+        h_grid.copy_(G.grid, non_blocking=True)
+        h_out.copy_(G.out, non_blocking=True)
         e1.record(stream)
         if i:
             e2e_times.append((e0, e1))
@@ -348,94 +519,108 @@ def run_ours(args):
     e2e = {"value": world * n / (ms_e2e * 1e-3) / 1e6, "unit": "Mvis/s",
            "h2d_bytes_per_step": h_uvw.numel() * 8 + h_vis.numel() * 8,
            "d2h_bytes_per_step": h_grid.numel() * 8 + h_out.numel() * 8}
+    del d_uvw, d_vis
 
-    # ---- plain FP64 form (one launch per w-plane) and accuracy of FP32 vs FP64
-    kt64 = E.KernelTable(E.w_kernels(w.theta, WSTEP * numpy.arange(kmin, kmax + 1).astype(float),
-                                     NPIXFF, w.S, w.Q, dtype=E.CD).reshape(-1), False, w.Q, w.S)
-    vis64 = torch.from_numpy(w.vis).to(dev)
-    g64 = torch.zeros((N, N), dtype=torch.complex128, device=dev)
-    plain_ms = []
-    for i in range(args.plain_steps + 1):
-        e0, e1 = ev(), ev()
+    # ---- fused form: plan + one pass that degrids the grid and grids the visibilities
+    for _ in range(3):
+        G.fused_step()
+    fused_times = []
+    for _ in range(min(args.steps, 50)):
         flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        e0, e1 = ev(), ev()
         e0.record(stream)
-        L.call("cg_w_bins_fixed", P(uvw), 3, n, WSTEP, kmin, nk, P(kidx), P(st.t), sp)
-        plan64 = E.Plan(uvw, w.lam, (N, N), kt64, kidx, L.CG_PLAN_GROUPS, status=st)
-        g64.zero_()
-        plan64.grid_fp64(kt64, vis64, g64)
-        o64 = plan64.degrid_fp64(kt64, g64)
+        G.fused_step()
         e1.record(stream)
-        torch.cuda.synchronize()
-        if i:
-            plain_ms.append(1e3 * (time.perf_counter() - t0))
-    st.check()
-    plain_value = n / (statistics.mean(plain_ms) * 1e-3) / 1e6
-    step(uvw, vis)
+        fused_times.append((e0, e1))
     torch.cuda.synchronize()
-    err_grid = float(torch.linalg.vector_norm(grid.to(torch.complex128) - g64) /
-                     torch.linalg.vector_norm(g64))
-    o_ref = plan64.degrid_fp64(kt64, g64)
-    o32 = E.Plan(uvw, w.lam, (N, N), kt, kidx, status=st).degrid(kt, g64.to(torch.complex64))
-    err_degrid = float(torch.linalg.vector_norm(o32.to(torch.complex128) - o_ref) /
-                       torch.linalg.vector_norm(o_ref))
+    G.st.check()
+    ms_fused = statistics.mean(a.elapsed_time(b) for a, b in fused_times)
 
-    # ---- roofline of the gridder (dominant kernel): algorithmic bytes per launch
-    S, Q = w.S, w.Q
-    table_bytes = nk * Q * Q * S * S * 8
-    grid_bytes = n * (16 + 4 + 8) + N * N * 8 + table_bytes
-    degrid_bytes = n * (16 + 4 + 8) + N * N * 8 + table_bytes
+    # ---- plain FP64 form and accuracy of FP32 vs FP64 (full size)
+    del flush
+    torch.cuda.empty_cache()
+    ms_plain, err_grid, err_degrid = G.plain(args.plain_steps)
+    plain_value = n / (ms_plain * 1e-3) / 1e6
+
+    # ---- roofline of the dominant kernel: algorithmic bytes per launch
+    kbytes = G.kernel_bytes_per_vis()
+    table_bytes = 0 if kbytes else G.kt.table.numel() * 8
+    alg = n * (16 + 4 + 8 + kbytes) + N * N * 8 + table_bytes
     dom = "grid" if ms_grid >= ms_degrid else "degrid"
     dom_ms = max(ms_grid, ms_degrid)
-    dom_bytes = grid_bytes if dom == "grid" else degrid_bytes
+    tuned = G.tuned
+    if dom == "grid":
+        kname = "k_grid_warp" if tuned.get("layout") in (0, L.CG_LAYOUT_WARP) else "k_grid_tiled"
+    else:
+        kname = "k_degrid_tiled"
     peaks = {}
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk):
         peaks = json.load(open(pk))
     peak = peaks.get("hbm_gbs", 6800.0)
-    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    achieved = alg / (dom_ms * 1e-3) / 1e9
     traffic = None
     tf = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tf):
-        traffic = json.load(open(tf)).get("k_%s_tiled" % dom)
+        entry = json.load(open(tf)).get(args.workload, {}).get(kname)
+        if entry:
+            traffic = entry["bytes_per_launch"]
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rate, dt = cpu_measure(w, min(args.cpu_sample, n), 1)
+        arm = CpuArm(args.workload, w, 200_000, 1)
+        arm.measure()
+        rate, dt = arm.measure()
+        arm.close()
         cpu = {"value": rate, "unit": "Mvis/s", "cores": 1, "kind": "port",
-               "sample": "%d of %d visibilities, grid+degrid, numpy oracle, 1 process, %.1f s"
-                         % (min(args.cpu_sample, n), n, dt)}
+               "sample": "%d of %d visibilities (%s), grid+degrid, numpy oracle, 1 process, "
+                         "%.2f s; kernels generated once before timing"
+                         % (arm.sample, n, "all visibilities of the first baselines"
+                            if args.workload == "aw" else "first visibilities", dt)}
 
-    # kernels of ours per step: coords (with w bins), scan (1 or 3), scatter, work items,
-    # grid, degrid
+    # the other configurations (each its own workload, timed the same way)
+    cfg_results = None
+    if rank == 0 and world == 1 and not args.no_configs:
+        from crocodile_gb300 import bench_configs
+        del G.ws
+        torch.cuda.empty_cache()
+        skip = {"aw"} if args.workload == "aw" else {"wproj"}
+        cfg_results = bench_configs.run([k for k in bench_configs.MEASURES if k not in skip])
+        autotune.set_tuning(**tuned)
+
+    # kernels of ours per step: coords, scan (1 or 3), scatter, work items, grid, degrid
     per_step = 1 + (3 if info_plan["buckets"] > 4096 else 1) + 1 + 1 + 2
     line = {
         "metric": METRIC, "value": value, "unit": "Mvis/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic (seeded numpy point-source visibilities)",
-        "config": {"workload": w.name, "n_vis": n, "N": N, "S": S, "Q": Q, "wstep": WSTEP,
-                   "NpixFF": NPIXFF, "w_kernels": nk, "coordinates": "fp64 bit-exact",
+        "config": {"workload": w.name, "n_vis": n, "N": N, "S": S, "Q": Q,
+                   "kernels": G.kt.G, "kernel_table_gb": round(G.kt.table.numel() * 8 / 1e9, 3),
+                   "coordinates": "fp64 bit-exact",
                    "l2": "256 MiB written between timed steps (outside the step events)",
                    "tile": info_plan["tile"], "chunk": info_plan["chunk"],
-                   "tuning": tuned, "tuning_seconds": round(tune_s, 2)},
+                   "tuning": tuned, "tuning_seconds": round(G.tune_s, 2)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "kernel": "k_%s_tiled" % dom,
-                     "algorithmic_bytes": dom_bytes, "ms": dom_ms,
+                     "frac": achieved / peak, "traffic": traffic, "kernel": kname,
+                     "algorithmic_bytes": alg, "ms": dom_ms,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks
                      else "fallback 6800 GB/s"},
-        "kernel_ms": {"grid": ms_grid, "degrid": ms_degrid, "plan_and_bins": ms - ms_grid - ms_degrid,
-                      "kernel_generation_once": kgen_ms},
+        "kernel_ms": {"grid": ms_grid, "degrid": ms_degrid, "plan": ms - ms_grid - ms_degrid,
+                      "kernel_generation_once": G.kgen_ms},
         "updates_per_s": 2 * n * S * S / (ms * 1e-3),
-        "plain_fp64": {"value": plain_value, "unit": "Mvis/s", "ms_per_step": statistics.mean(plain_ms),
-                       "form": "complex128, FP64 atomics, one launch per w-plane (%d)" % nk},
+        "plain_fp64": {"value": plain_value, "unit": "Mvis/s", "ms_per_step": ms_plain,
+                       "form": "complex128, FP64 atomics, " + G.groups_desc},
         "speedup_vs_plain": value / plain_value,
         "rel_err_vs_fp64": {"grid": err_grid, "degrid": err_degrid},
+        "fused": {"value": n / (ms_fused * 1e-3) / 1e6, "unit": "Mvis/s", "ms_per_step": ms_fused,
+                  "form": "plan + one degrid+grid pass (cg_degrid_grid), each kernel tap read "
+                          "once", "speedup_vs_plain": ms_plain / ms_fused},
         "e2e": e2e,
         "gpu_launches": args.steps * per_step,
         "clocks": clk,
         "cpu_baseline": cpu,
+        "configs": cfg_results,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

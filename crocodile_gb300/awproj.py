@@ -48,16 +48,28 @@ class AWProjection:
         self.A, self.Wk = A, Wk
         args = (A, Wk, (pair // nant).astype(numpy.int32), (pair % nant).astype(numpy.int32),
                 wi.astype(numpy.int32))
+        self._aw_args = args
         self.ktab = E.KernelTable(E.aw_kernels(*args, dtype=E.CF, status=st).reshape(-1), False,
                                   Q, SA)
         self.replan()
         self.ktab64 = self.plan64 = None
         if fp64:
-            self.ktab64 = E.KernelTable(E.aw_kernels(*args, dtype=E.CD, status=st).reshape(-1),
-                                        False, Q, SA)
-            self.plan64 = E.Plan(self.uvw, lam, (self.N, self.N), self.ktab64, rows,
-                                 mode=L.CG_PLAN_GROUPS, status=st, groups=(nb, wbin))
+            self.enable_fp64()
         st.check()
+
+    def enable_fp64(self):
+        """Prepare the plain FP64 form: the same AW kernels held as complex128 and a
+        groups plan with one launch per w-plane."""
+        st = self.status
+        Q, SA = self.ktab.Q, self.ktab.S
+        self.ktab64 = E.KernelTable(E.aw_kernels(*self._aw_args, dtype=E.CD,
+                                                 status=st).reshape(-1), False, Q, SA)
+        self.plan64 = E.Plan(self.uvw, self.lam, (self.N, self.N), self.ktab64, self.rows,
+                             mode=L.CG_PLAN_GROUPS, status=st, groups=(self.nbins, self.wbin))
+        st.check()
+
+    def disable_fp64(self):
+        self.ktab64 = self.plan64 = None
 
     def replan(self):
         """(Re)build the tiled plan, e.g. after the launch-shape tuning changed."""

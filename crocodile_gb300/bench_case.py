@@ -1,6 +1,6 @@
 """A small, self-contained run of the w-projection grid + degrid step, for profiling.
 
-    python -m crocodile_gb300.bench_case [--nvis N] [--steps K] [--workload wproj|plain]
+    python -m crocodile_gb300.bench_case [--nvis N] [--steps K] [--workload wproj|plain|aw]
 
 Sets up the seeded workload (kernels generated once), then runs K steps of
 plan (with fused w binning) + FP32 gridding + FP32 degridding on the current
@@ -22,6 +22,17 @@ from . import synthesis
 
 
 def setup(workload="wproj", nvis=500_000, seed=None):
+    if workload == "aw":
+        from . import awproj
+        w = configs.aw() if seed is None else configs.aw(seed=seed)
+        if nvis and nvis < len(w.uvw):
+            w = configs.wproj_subset(w, nvis)
+            w.params = dict(w.params, a1=w.params["a1"][:nvis], a2=w.params["a2"][:nvis])
+        op = awproj.AWProjection(w.theta, w.lam, w.uvw, w.params["a1"], w.params["a2"],
+                                 w.params["beams"], w.params["wstep"], w.params["NpixFF"])
+        vis = torch.from_numpy(w.vis.astype(numpy.complex64)).to(op.uvw.device)
+        return dict(w=w, uvw=op.uvw, vis=vis, st=op.status, kt=op.ktab, kmin=0, nk=0,
+                    wstep=None, rows=op.rows)
     if workload == "wproj":
         w = configs.wproj(n=nvis) if seed is None else configs.wproj(seed=seed, n=nvis)
         wstep, npixff = w.params["wstep"], w.params["NpixFF"]
@@ -74,9 +85,11 @@ class Step:
                    ctypes.byref(self.kd), self.N, self.N, P(uvw), uvw.stride(0), c["w"].lam,
                    c["wstep"], c["kmin"], self.n, P(self.ws), self.ws_bytes, P(c["st"].t), sp)
         else:
+            rows = c.get("rows")
             L.call("cg_plan_create", ctypes.byref(h), L.CG_PLAN_TILED, ctypes.byref(self.kd),
-                   self.N, self.N, P(uvw), uvw.stride(0), c["w"].lam, None, self.n, P(self.ws),
-                   self.ws_bytes, P(c["st"].t), sp)
+                   self.N, self.N, P(uvw), uvw.stride(0), c["w"].lam,
+                   None if rows is None else P(rows), self.n, P(self.ws), self.ws_bytes,
+                   P(c["st"].t), sp)
         try:
             self.grid.zero_()
             if events:
@@ -95,14 +108,20 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--nvis", type=int, default=500_000)
     ap.add_argument("--steps", type=int, default=2)
-    ap.add_argument("--workload", default="wproj", choices=["wproj", "plain"])
+    ap.add_argument("--workload", default="wproj", choices=["wproj", "plain", "aw"])
     ap.add_argument("--tune", action="store_true", help="autotune the launch shape first")
+    ap.add_argument("--tuning", default="",
+                    help="explicit launch shape tile,chunk,rows,groups,layout (no autotuning)")
     a = ap.parse_args()
     ctx = setup(a.workload, a.nvis)
-    if a.tune:
+    if a.tuning:
+        from . import autotune
+        tile, chunk, rows, groups, layout = (int(x) for x in a.tuning.split(","))
+        autotune.set_tuning(tile, chunk, rows, groups, layout)
+    elif a.tune:
         from . import autotune
         w = ctx["w"]
-        kidx = None
+        kidx = ctx.get("rows")
         if ctx["wstep"] is not None:
             kidx, _, _ = E.w_bins(ctx["uvw"], ctx["wstep"], ctx["st"])
         best, _ = autotune.tune(ctx["uvw"], w.lam, (w.N, w.N), ctx["kt"], kidx, ctx["vis"],

@@ -1,6 +1,6 @@
 """Throughput and accuracy of every benchmark configuration on the current GPU.
 
-    python -m crocodile_gb300.bench_configs [--only plain,diff,wstack,aw] [--steps K]
+    python -m crocodile_gb300.bench_configs [--only plain,wproj,diff,wstack,aw] [--steps K]
 
 For each configuration (see configs.py) it times, with CUDA events on the
 current stream after warm-up, the FP32 batched form and the plain FP64 form
@@ -77,6 +77,45 @@ def measure_plain(steps=20):
     return {"workload": w.name, "n_vis": n, "ms": ms, "mvis_s": n / ms / 1e3,
             "plain_fp64_ms": ms64, "plain_fp64_mvis_s": n / ms64 / 1e3, "speedup": ms64 / ms,
             "rel_err_grid": _rel(g, g64), "rel_err_degrid": _rel(out["v"], out["v64"])}
+
+
+def measure_wproj(steps=20):
+    """w_cache_imaging + w_cache_predict, 4096^2, 2M visibilities, S 15 Q 8, 101 w-kernels:
+    plan (fused w binning) + grid + degrid, and the plain FP64 form."""
+    w = configs.wproj()
+    n, N = len(w.uvw), w.N
+    wstep, npff = w.params["wstep"], w.params["NpixFF"]
+    uvw = E.cuda_tensor(w.uvw, torch.float64)
+    vis, vis64 = E.cuda_tensor(w.vis, E.CF), E.cuda_tensor(w.vis, E.CD)
+    st = E.Status()
+    kidx, kmin, kmax = E.w_bins(uvw, wstep, st)
+    ws_ = wstep * numpy.arange(kmin, kmax + 1).astype(float)
+    kt = E.KernelTable(E.w_kernels(w.theta, ws_, npff, w.S, w.Q).reshape(-1), False, w.Q, w.S)
+    kt64 = E.KernelTable(E.w_kernels(w.theta, ws_, npff, w.S, w.Q, dtype=E.CD).reshape(-1),
+                         False, w.Q, w.S)
+    tuned, _ = autotune.tune(uvw, w.lam, (N, N), kt, kidx, vis,
+                             cands=autotune.candidates(w.S, quick=True), use_cache=False)
+    g = torch.zeros((N, N), dtype=E.CF, device="cuda")
+    g64 = torch.zeros((N, N), dtype=E.CD, device="cuda")
+    out = {}
+
+    def fp32():
+        plan = E.Plan(uvw, w.lam, (N, N), kt, status=st, wbins=(wstep, kmin))
+        g.zero_()
+        plan.grid(kt, vis, g)
+        out["v"] = plan.degrid(kt, g)
+
+    def fp64():
+        plan = E.Plan(uvw, w.lam, (N, N), kt64, kidx, mode=L.CG_PLAN_GROUPS, status=st)
+        g64.zero_()
+        plan.grid_fp64(kt64, vis64, g64)
+        out["v64"] = plan.degrid_fp64(kt64, g64)
+
+    ms, ms64 = _time(fp32, steps), _time(fp64, 2, 1)
+    st.check()
+    return {"workload": w.name, "n_vis": n, "ms": ms, "mvis_s": n / ms / 1e3, "tuning": tuned,
+            "plain_fp64_ms": ms64, "plain_fp64_mvis_s": n / ms64 / 1e3, "speedup": ms64 / ms,
+            "rel_err_grid": _rel(g, g64)}
 
 
 def measure_diff(steps=20):
@@ -176,8 +215,8 @@ def measure_aw(steps=5, nvis=None, fp64=True):
             "rel_err_grid": _rel(g, g64), "rel_err_degrid": _rel(out["v"], out["v64"])}
 
 
-MEASURES = {"plain": measure_plain, "diff": measure_diff, "wstack": measure_wstack,
-            "aw": measure_aw}
+MEASURES = {"plain": measure_plain, "wproj": measure_wproj, "diff": measure_diff,
+            "wstack": measure_wstack, "aw": measure_aw}
 
 
 def run(only=None, steps=None):

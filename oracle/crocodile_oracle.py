@@ -183,6 +183,16 @@ def aw_kernel_fn(a_kernel_fn, w_kernel_fn=w_kernel):
     return fn
 
 
+def aw_kernel_fft(akern_a, akern_b, wkern):
+    """aw_kernel_fn's result for one key, computed with scipy.signal.fftconvolve
+    batched over the Q x Q sub-kernels (same 'same' crops as convolve2d, equal to
+    aw_kernel_fn to rounding).  Used to prepare large CPU-baseline kernel tables;
+    tests/test_oracle_golden.py pins it against aw_kernel_fn."""
+    akern = scipy.signal.convolve2d(akern_a, akern_b, mode="same")
+    akern = numpy.broadcast_to(akern, wkern.shape[:-2] + akern.shape)
+    return scipy.signal.fftconvolve(akern, wkern, mode="same", axes=(-2, -1))
+
+
 # --------------------------------------------------------------------------
 # coordinates of visibilities (synthesis.py:419-449)
 

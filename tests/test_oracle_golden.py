@@ -132,3 +132,11 @@ def test_fixed_functions_agree_with_cache_path(golden):
     assert_allclose(v1, golden["cd_vis4"], rtol=1e-12)
     v2 = O.w_cache_predict(theta, lam, uvw, None, golden["cg_model"], wstep=1e9, kernel_fn=kfn)
     assert_allclose(v2, golden["cd_vis4"], rtol=1e-12)
+
+
+def test_aw_kernel_fft_equals_aw_kernel_fn(golden):
+    ak = golden["aw_akerns"]
+    wk = O.w_kernel(0.1, 25.0, 16, 6, 2)
+    ref = O.aw_kernel_fn(lambda th, a: ak[a], lambda th, w: wk)(0.1, 25.0, 0, 1)
+    assert_allclose(O.aw_kernel_fft(ak[0], ak[1], wk), ref, rtol=1e-12, atol=1e-12)
+    assert_allclose(ref, golden["aw_k01"], rtol=1e-13)
