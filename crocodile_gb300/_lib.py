@@ -30,6 +30,7 @@ CG_PLAN_TILED = 0
 CG_PLAN_GROUPS = 1
 CG_LAYOUT_WARP = 1
 CG_LAYOUT_OWNER = 2
+CG_LAYOUT_LANE = 3
 
 
 class PlanOpts(ctypes.Structure):

@@ -52,8 +52,10 @@ int cg_set_tuning(const cg_tuning *t) {
              "in [0, 64]", t->tile);
   CG_REQUIRE(t->chunk >= 0 && t->chunk <= (1 << 20), "chunk %d out of range", t->chunk);
   CG_REQUIRE(t->rows >= 0 && t->rows <= 8, "rows %d out of range [0, 8]", t->rows);
-  CG_REQUIRE(t->groups >= 0 && t->groups <= 8, "groups %d out of range [0, 8]", t->groups);
-  CG_REQUIRE(t->layout >= 0 && t->layout <= CG_LAYOUT_OWNER, "layout %d unknown", t->layout);
+  CG_REQUIRE(t->layout >= 0 && t->layout <= CG_LAYOUT_LANE, "layout %d unknown", t->layout);
+  const int gmax = t->layout == CG_LAYOUT_LANE ? 16 : 8;
+  CG_REQUIRE(t->groups >= 0 && t->groups <= gmax, "groups %d out of range [0, %d]", t->groups,
+             gmax);
   std::lock_guard<std::mutex> lock(cg::g_tuning_mu);
   cg::g_tuning = *t;
   return CG_OK;

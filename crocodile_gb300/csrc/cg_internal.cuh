@@ -64,63 +64,112 @@ __device__ __forceinline__ bool in_unit_range(double p) {
 }
 
 // Filtered exact evaluation.  GB300 runs FP64 at a small fraction of its FP32
-// rate and an IEEE division costs many FP64 operations, so coordinates are
-// first estimated with one FMA from constants prepared on the host, and the
-// exact sequence above runs only when the estimate cannot decide:
-//   c~ = fma(-u, NQ_over_lam, -(N//2)*Q)   estimates (-(N//2 + (u/lam)*N)) * Q
-// Each of the two evaluations is within a few ulp of the real value, i.e.
-// within ~2^-49 * N * Q (< 1e-9 for N*Q <= 2^20) of each other, so rint()
-// agrees whenever c~ is further than 1e-6 from a half-integer.  The range
-// test p in [-0.5, 0.5) likewise uses u * (1/lam) except within 1e-9 of the
-// ends.  Results are bit-identical to frac_coord/in_unit_range on u / lam.
+// rate (and an IEEE division costs many FP64 operations), so each coordinate
+// costs ONE FP64 operation on the fast path:
+//   t = fma(-u, N*Q/lam, M - (N//2)*Q),  M = 1.5 * 2^32
+// For |c| < 2^31 the sum lies in [2^32, 2^33), where doubles are spaced 2^-20
+// apart, so the single rounding of the FMA leaves F = bits(t) - bits(M) =
+// round(c * 2^20), c = -(N//2 + (u/lam)*N) * Q, as a fixed-point integer.
+// F is within 2^-21 (+ a few ulp of N*Q) of the value the exact sequence of
+// frac_coord rounds, so rint() of the exact value is known unless the
+// fraction of F lies within FIX_MARGIN units (2.9e-6) of one half, and the
+// range test p in [-0.5, 0.5) (c in (-(N//2 + N/2)*Q, (N/2 - N//2)*Q]) is
+// known unless F lies within FIX_MARGIN of an end.  Only those undecided
+// cases run the exact IEEE sequence, so results are bit-identical to
+// frac_coord/in_unit_range on u / lam.  Non-finite t maps to |F| >= 2^51 and
+// tests out of range, as NaN/inf do in the exact test.
+constexpr int FIX_BITS = 20;
+constexpr long long FIX_ONE = 1ll << FIX_BITS;
+constexpr long long FIX_HALF = FIX_ONE >> 1;
+constexpr long long FIX_MARGIN = 3;
+constexpr unsigned long long FIX_MAGIC_BITS = 0x41F8000000000000ull;  // bits of 1.5 * 2^32
+constexpr double FIX_MAGIC = 6442450944.0;                          // 1.5 * 2^32
+
 struct AxisConst {
   double nq_over_lam;  // N * Q / lam
-  double n2q;          // (N // 2) * Q
-  double inv_lam;      // 1 / lam
+  double c0;           // M - (N//2) * Q  (exact)
+  long long lo, hi;    // range ends in fixed point: p < 0.5 <=> F > lo, p >= -0.5 <=> F <= hi
+  int qshift;          // log2(Q) when Q is a power of two, else -1
+  int fast;            // 0: |c| may reach 2^31 (N*Q >= 2^30); exact sequence only
 };
 
-__device__ __forceinline__ bool near_half(double c) {
-  const double f = c - floor(c);
-  return fabs(f - 0.5) < 1e-6;
+__device__ __forceinline__ long long fixed_coord(double u, const AxisConst &k) {
+  const double t = fma(-u, k.nq_over_lam, k.c0);
+  return (long long)((unsigned long long)__double_as_longlong(t) - FIX_MAGIC_BITS);
 }
 
-// p = u / lam in range?  (exact decision)
-__device__ __forceinline__ bool unit_range_fast(double u, double lam, double inv_lam) {
-  const double pe = u * inv_lam;
-  if (pe > -0.5 + 1e-9 && pe < 0.5 - 1e-9) return true;
-  if (!(pe > -0.5 - 1e-9 && pe < 0.5 + 1e-9)) return false;  // NaN lands here too
-  return in_unit_range(__ddiv_rn(u, lam));
-}
-
-__device__ __forceinline__ void frac_coord_fast(double u, double lam, const AxisConst &k, int N,
-                                                int Q, int &xi, int &xf) {
-  const double ce = fma(-u, k.nq_over_lam, -k.n2q);
-  long long fx;
-  if (!near_half(ce)) {
-    fx = (long long)rint(ce);
+// floor division / modulo of fx (|fx| < 2^31) by Q
+__device__ __forceinline__ void split_q(long long fx, int Q, int qshift, int &xi, int &xf) {
+  if (qshift >= 0) {
+    const int f = (int)fx;
+    xi = -(f >> qshift);
+    xf = f & (Q - 1);
   } else {
-    const double p = __ddiv_rn(u, lam);
-    const double x = __dadd_rn((double)(N / 2), __dmul_rn(p, (double)N));
-    fx = (long long)rint(__dmul_rn(-x, (double)Q));
+    long long q, r;
+    floordivmod(fx, Q, q, r);
+    xi = (int)(-q);
+    xf = (int)r;
   }
-  long long q, r;
-  floordivmod(fx, Q, q, r);
-  xi = (int)(-q);
-  xf = (int)r;
 }
 
-// w bin k = rint(w / wstep) (w_cache_imaging, synthesis.py:793), filtered likewise.
+// Range test and frac_coord of one axis.  Returns false (and leaves xi, xf
+// unset) when p = u / lam is outside [-0.5, 0.5) or NaN.
+__device__ __forceinline__ bool coord_fast(double u, double lam, const AxisConst &k, int N, int Q,
+                                           int &xi, int &xf) {
+  long long fx;
+  if (k.fast) {
+    const long long F = fixed_coord(u, k);
+    if (F > k.hi + FIX_MARGIN || F < k.lo - FIX_MARGIN) return false;
+    if (F > k.hi - FIX_MARGIN || F < k.lo + FIX_MARGIN) {
+      if (!in_unit_range(__ddiv_rn(u, lam))) return false;
+    }
+    const long long fr = F & (FIX_ONE - 1);
+    if (fr < FIX_HALF - FIX_MARGIN || fr > FIX_HALF + FIX_MARGIN) {
+      fx = (F >> FIX_BITS) + (fr > FIX_HALF ? 1 : 0);
+      split_q(fx, Q, k.qshift, xi, xf);
+      return true;
+    }
+  } else if (!in_unit_range(__ddiv_rn(u, lam))) {
+    return false;
+  }
+  const double p = __ddiv_rn(u, lam);
+  const double x = __dadd_rn((double)(N / 2), __dmul_rn(p, (double)N));
+  fx = (long long)rint(__dmul_rn(-x, (double)Q));
+  split_q(fx, Q, k.qshift, xi, xf);
+  return true;
+}
+
+// w bin k = rint(w / wstep) (w_cache_imaging, synthesis.py:793), filtered the
+// same way: F = round(w * (1/wstep) * 2^20) from one FMA; the estimate is within
+// 2^-21 + 2^-22 of w / wstep while |w / wstep| < 2^31 (|F| < 2^51).
 __device__ __forceinline__ double w_bin_fast(double w, double wstep, double inv_wstep) {
-  const double ke = w * inv_wstep;
-  if (!near_half(ke)) return rint(ke);
+  const double t = fma(w, inv_wstep, FIX_MAGIC);
+  const long long F =
+      (long long)((unsigned long long)__double_as_longlong(t) - FIX_MAGIC_BITS);
+  if (F > -(1ll << 50) && F < (1ll << 50)) {
+    const long long fr = F & (FIX_ONE - 1);
+    if (fr < FIX_HALF - FIX_MARGIN || fr > FIX_HALF + FIX_MARGIN)
+      return (double)((F >> FIX_BITS) + (fr > FIX_HALF ? 1 : 0));
+  }
   return rint(__ddiv_rn(w, wstep));
 }
 
 inline AxisConst axis_const(int N, int Q, double lam) {
   AxisConst k;
   k.nq_over_lam = ((double)N * (double)Q) / lam;
-  k.n2q = (double)(N / 2) * (double)Q;
-  k.inv_lam = 1.0 / lam;
+  k.c0 = FIX_MAGIC - (double)(N / 2) * (double)Q;
+  // p = 0.5 <=> c = -(N//2 + N/2) * Q ; p = -0.5 <=> c = (N/2 - N//2) * Q
+  const double half_n = 0.5 * (double)N;
+  k.lo = (long long)(-((double)(N / 2) + half_n) * (double)Q * (double)FIX_ONE);
+  k.hi = (long long)((half_n - (double)(N / 2)) * (double)Q * (double)FIX_ONE);
+  k.qshift = -1;
+  for (int b = 0; b < 31; ++b)
+    if (Q == (1 << b)) k.qshift = b;
+  // fixed point needs |c| < 2^31 for every in-range u and a finite, non-zero
+  // scale; otherwise every coordinate takes the exact sequence
+  const double nq = (double)N * (double)Q;
+  k.fast = (nq < (double)(1 << 30) && lam == lam && lam != 0.0 &&
+            k.nq_over_lam - k.nq_over_lam == 0.0) ? 1 : 0;
   return k;
 }
 

@@ -20,55 +20,9 @@
 #include <algorithm>
 
 #include "cg_internal.cuh"
+#include "tiled.cuh"
 
 namespace cg {
-
-struct TiledArgs {
-  const VisRec *recs;
-  const int32_t *perm;
-  const WorkItem *items;
-  const int32_t *nitems;
-  int32_t *ticket;
-  const int32_t *status;
-  int H, W, S, Q, T, ntx, tpl, win, pitch;
-};
-
-// Window origin of a work item's tile and the offset of its layer's grid.
-struct TileOrigin {
-  int wx0, wy0;
-  size_t layer_off;
-};
-__device__ __forceinline__ TileOrigin tile_origin(const TiledArgs &A, int tile) {
-  const int lyr = tile / A.tpl, t = tile - lyr * A.tpl;
-  TileOrigin o;
-  o.wx0 = (t % A.ntx) * A.T;
-  o.wy0 = (t / A.ntx) * A.T;
-  o.layer_off = (size_t)lyr * A.H * A.W;
-  return o;
-}
-
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ void cfma(float2 &acc, float2 a, float2 b) {
-  acc.x = fmaf(a.x, b.x, acc.x);
-  acc.x = fmaf(-a.y, b.y, acc.x);
-  acc.y = fmaf(a.x, b.y, acc.y);
-  acc.y = fmaf(a.y, b.x, acc.y);
-}
-
-__device__ __forceinline__ bool status_failed(const int32_t *st) {
-  return (st[ST_RANGE] | st[ST_BOUNDS] | st[ST_INDEX]) != 0;
-}
-
-// Next work item for the whole CTA, or -1.
-__device__ __forceinline__ int next_item(const TiledArgs &A, int *s_item) {
-  __syncthreads();
-  if (threadIdx.x == 0) *s_item = atomicAdd(A.ticket, 1);
-  __syncthreads();
-  int it = *s_item;
-  return it < *A.nitems ? it : -1;
-}
 
 // ---------------------------------------------------------------- gridder
 static constexpr int GRID_STAGE = 256;  // visibilities staged per batch
@@ -530,25 +484,6 @@ __global__ void __launch_bounds__(256) k_degrid_tiled(
   }
 }
 
-static TiledArgs tiled_args(const cg_plan *p) {
-  TiledArgs A;
-  A.recs = p->recs;
-  A.perm = p->perm;
-  A.items = p->items;
-  A.nitems = p->nitems;
-  A.ticket = p->ticket;
-  A.status = p->status;
-  A.H = p->H;
-  A.W = p->W;
-  A.S = p->kd.S;
-  A.Q = p->kd.Q;
-  A.T = p->T;
-  A.ntx = p->ntx;
-  A.tpl = p->tpl;
-  A.win = p->win;
-  A.pitch = p->pitch;
-  return A;
-}
 
 // Row residues per thread: the smallest R in {2, 3, 4} dividing S, else 4
 // (1 for S = 1); overridable by the tuning.
@@ -609,13 +544,15 @@ static int grid_launch(const cg_plan *p, const void *ktab, const void *vis,
   int gsize = 0, ngroups = 0;
   bool shared = false;
   const int layout = t.layout > 0 ? t.layout : CG_LAYOUT_WARP;
-  if (layout == CG_LAYOUT_WARP) {
+  if (layout == CG_LAYOUT_LANE && S <= 16)
+    return lane_launch(p, kt, vv, weight, mode, gg, nullptr, nullptr, 0, false, s);
+  if (layout != CG_LAYOUT_OWNER) {
     const int need = (S * S + 31) / 32;
     int maxt = 1;
     while (maxt < need) maxt *= 2;
     fn = p->kd.sep ? grid_warp_kernel_for<true>(maxt) : grid_warp_kernel_for<false>(maxt);
     CG_REQUIRE(fn, "no warp gridder for support %d", S);
-    threads = 32 * (t.groups > 0 ? t.groups : 8);
+    threads = 32 * (t.groups > 0 ? std::min(t.groups, 8) : 8);
     smem = wbytes + (size_t)GRID_STAGE * (8 + 8 + 8 + 8);
     args[0] = &A;
     args[1] = &mode;
@@ -711,8 +648,13 @@ int cg_degrid_grid(const cg_plan *p, const void *ktab, const void *grid_in, cons
   CG_REQUIRE(vis_in || !residual, "the residual mode needs input visibilities");
   CG_REQUIRE(grid_in != grid_out, "input and output grids must differ");
   cudaStream_t s = (cudaStream_t)stream;
-  TiledArgs A = tiled_args(p);
   const int S = p->kd.S;
+  const cg_tuning t = tuning();
+  if (t.layout == CG_LAYOUT_LANE && S <= 16)
+    return lane_launch(p, (const float2 *)ktab, (const float2 *)vis_in, nullptr, 0,
+                       (float2 *)grid_out, (const float2 *)grid_in, (float2 *)vis_out, residual,
+                       true, s);
+  TiledArgs A = tiled_args(p);
   const int need = (S * S + 31) / 32;
   int maxt = 1;
   while (maxt < need) maxt *= 2;
@@ -723,8 +665,7 @@ int cg_degrid_grid(const cg_plan *p, const void *ktab, const void *grid_in, cons
   PICK(1) PICK(2) PICK(4) PICK(8) PICK(16) PICK(32)
 #undef PICK
   CG_REQUIRE(fn, "no fused kernel for support %d", S);
-  const cg_tuning t = tuning();
-  const int threads = 32 * (t.groups > 0 ? t.groups : 8);
+  const int threads = 32 * (t.groups > 0 ? std::min(t.groups, 8) : 8);
   const size_t smem = 2 * (size_t)p->pitch * p->win * sizeof(float2) +
                       (size_t)GRID_STAGE * (4 + 4 + 8 + 8 + 8);
   CG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

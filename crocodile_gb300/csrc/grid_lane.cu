@@ -1,0 +1,427 @@
+// Lane-layout FP32 gridder and fused degrid+grid pass: no shared-memory atomics.
+//
+// Gridding replaces convgrid (crocodile/synthesis.py:464-481); the fused pass
+// is convdegrid (synthesis.py:484-503) followed by convgrid of the same
+// visibilities, reading every kernel tap once for both.
+//
+// One warp takes one work item (<= chunk visibilities of one grid tile) at a
+// time and owns a private (T+S-1)^2 window in shared memory, so no other warp
+// ever writes its cells.  Lane l owns the kernel taps t = l + 32 i of every
+// visibility (footprint cell (t / S, t mod S)); the taps of one visibility are
+// distinct cells, so each lane adds its products with a plain read-modify-write
+// and the warp synchronises once per visibility: no shared-memory atomics.
+// Each item's window is flushed to HBM with float2 atomics and left zeroed for
+// the next one.
+//
+// Non-separable tables whose S x S slices are a multiple of 16 bytes stream
+// every visibility's slice into a per-warp ring of LANE_DEPTH shared-memory
+// stages with bulk asynchronous copies (cp.async.bulk; completion counted in
+// bytes on one mbarrier per stage), issued LANE_DEPTH - 1 visibilities ahead by
+// lane 0, so that ~LANE_DEPTH slices per warp are in flight without holding
+// registers.  Other tables load their taps from global memory one visibility
+// ahead.  Visibility records are staged 32 at a time in a per-warp ring of 64,
+// the next batch being loaded while the current one runs.  Every mbarrier
+// wait is bounded (about two seconds); on expiry the warp sets the timeout
+// status word, waits (bounded) for its copies in flight and stops.
+#include <algorithm>
+
+#include "tiled.cuh"
+
+namespace cg {
+
+static constexpr int LANE_DEPTH = 4;                          // bulk-copy stages per warp
+static constexpr int LANE_RING = 64;                          // staged visibility records per warp
+static constexpr long long LANE_WAIT_CYCLES = 4000000000ll;   // ~2 s at 2 GHz
+static constexpr unsigned FULL_MASK = 0xffffffffu;
+
+struct LaneArgs {
+  const float2 *ktab;
+  const float2 *vis;      // gridding: values to grid; fused: input visibilities (may be NULL)
+  const float *weight;    // gridding modes 1 and 2
+  float2 *grid;           // output grid
+  const float2 *grid_in;  // fused: grid to degrid
+  float2 *vis_out;        // fused: degridded visibilities (may be NULL)
+  int mode;               // gridding: 0 vis, 1 vis * weight, 2 weight; fused: 0 plain, 1 residual
+  int warp_bytes;         // shared memory per warp
+  int stage_off, meta_off, val_off, bar_off;  // byte offsets inside a warp's region
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+// Makes initialised mbarriers visible to the bulk-copy (async) proxy.
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// On lanes with p set: order the warp's earlier shared-memory reads before
+// the async proxy, then one bulk copy of `bytes` (multiple of 16, both
+// addresses 16-byte aligned) from global to shared memory completing on `bar`.
+// Predicated rather than branched, so the warp does not diverge.
+__device__ __forceinline__ void bulk_load_if(bool p, void *dst, const void *src, uint32_t bytes,
+                                             uint64_t *bar) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "@p fence.proxy.async.shared::cta;\n\t"
+      "@p mbarrier.arrive.expect_tx.shared::cta.b64 _, [%3], %2;\n\t"
+      "@p cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      "\n\t}" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "r"((int)p)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for the phase of `bar` with the given parity; false after ~2 s.
+__device__ __noinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try(bar, parity))
+    if (clock64() - t0 > LANE_WAIT_CYCLES) return false;
+  return true;
+}
+
+// FULLT: S * S == 32 * MAXT, every lane owns MAXT taps (no per-tap checks).
+// SC, PC: support and window pitch fixed at compile time (0: read at run
+// time); with S dividing 32 a lane's taps then sit at immediate offsets.
+template <bool SEP, bool BULK, bool FUSED, int MAXT, bool FULLT, int SC = 0, int PC = 0>
+__global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  if (status_failed(A.status)) return;
+  const int S = SC ? SC : A.S, SS = S * S, pitch = PC ? PC : A.pitch, win = A.win;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned char *region = smem + (size_t)warp * P.warp_bytes;
+  float2 *wbuf = (float2 *)region;
+  float2 *stages = (float2 *)(region + P.stage_off);
+  int4 *meta = (int4 *)(region + P.meta_off);
+  float2 *mval = (float2 *)(region + P.val_off);
+  uint64_t *bar = (uint64_t *)(region + P.bar_off);
+  const int QQ = A.Q * A.Q;
+  const float2 zero = make_float2(0.f, 0.f);
+  const uint32_t slice_bytes = (uint32_t)SS * 8u;
+
+  // lane l owns taps t = l + 32 i: footprint cell (dy, dx) = (t / S, t % S)
+  int soff[MAXT], goff[MAXT], tdy[MAXT], tdx[MAXT];
+  bool own[MAXT];
+  constexpr bool STEP = SC > 0 && 32 % (SC > 0 ? SC : 1) == 0;  // t + 32 is 32 / S rows down
+#pragma unroll
+  for (int i = 0; i < MAXT; ++i) {
+    const int t = lane + 32 * i;
+    tdy[i] = STEP ? lane / S + i * (32 / S) : t / S;
+    tdx[i] = STEP ? lane % S : t - tdy[i] * S;
+    own[i] = FULLT || t < SS;
+    soff[i] = STEP ? (lane / S) * pitch + lane % S + i * (32 / S) * pitch : tdy[i] * pitch + tdx[i];
+    goff[i] = tdy[i] * A.W + tdx[i];
+  }
+
+  for (int c = lane; c < pitch * win; c += 32) wbuf[c] = zero;
+  if (BULK && lane == 0) {
+    for (int d = 0; d < LANE_DEPTH; ++d) mbar_init(&bar[d], 1);
+    mbar_fence_init();
+  }
+  __syncwarp();
+
+  // consumer position in the stage ring: stage and phase parity of the next
+  // visibility this warp reads (persisting across items)
+  int cst = 0;
+  uint32_t cpar = 0;
+  for (;;) {
+    int it = 0;
+    if (lane == 0) it = atomicAdd(A.ticket, 1);
+    it = __shfl_sync(FULL_MASK, it, 0);
+    if (it >= *A.nitems) break;
+    const WorkItem w = A.items[it];
+    const TileOrigin org = tile_origin(A, w.tile);
+    const int n = w.count;
+    const float2 *gin = FUSED ? P.grid_in + org.layer_off + (size_t)org.wy0 * A.W + org.wx0
+                              : nullptr;
+
+    // Record of item visibility j, packed for the ring: x = lx0 | ly0 << 16 (the
+    // footprint origin in the window), y = slice (or kernel row k0), z = k1
+    // (separable), w = original index.
+    auto pack = [&](const VisRec &rec, int src) {
+      int4 m;
+      m.x = (rec.x0 - org.wx0) | ((rec.y0 - org.wy0) << 16);
+      m.y = SEP ? rec.k0 : rec.k0 * QQ + rec.k1;
+      m.z = rec.k1;
+      m.w = src;
+      return m;
+    };
+    auto value = [&](int src) {
+      if (FUSED) return P.vis ? P.vis[src] : zero;
+      if (P.mode == 2) return make_float2(P.weight[src], 0.f);
+      float2 v = P.vis[src];
+      if (P.mode == 1) {
+        const float wt = P.weight[src];
+        v.x *= wt;
+        v.y *= wt;
+      }
+      return v;
+    };
+
+    if (lane < n) {
+      const int src = A.perm[w.start + lane];
+      meta[lane] = pack(A.recs[w.start + lane], src);
+      mval[lane] = value(src);
+    }
+    __syncwarp();
+
+    // Bulk copies run LANE_DEPTH - 1 visibilities ahead of the consumer: the
+    // copy of visibility j + LANE_DEPTH - 1 goes into the stage that visibility
+    // j - 1 used.
+    int issued = 0;
+    if (BULK) {
+      int ist = cst;
+      for (; issued < min(n, LANE_DEPTH - 1); ++issued) {
+        const int4 m = meta[issued];
+        bulk_load_if(lane == 0, stages + (size_t)ist * SS, P.ktab + (size_t)m.y * SS,
+                     slice_bytes, &bar[ist]);
+        ist = ist + 1 == LANE_DEPTH ? 0 : ist + 1;
+      }
+    }
+
+    // taps from global memory (tables that are not streamed) and, fused, the
+    // input grid under the footprint: loaded one visibility ahead
+    float2 kn[MAXT], gn[MAXT];
+#pragma unroll
+    for (int i = 0; i < MAXT; ++i) kn[i] = gn[i] = zero;
+    auto load_global = [&](int j) {
+      const int4 m = meta[j & (LANE_RING - 1)];
+      const int lx0 = m.x & 0xffff, ly0 = m.x >> 16;
+      const float2 *kk = SEP ? P.ktab + (size_t)m.y * S : P.ktab + (size_t)m.y * SS;
+      const float2 *kx = P.ktab + (size_t)m.z * S;
+#pragma unroll
+      for (int i = 0; i < MAXT; ++i)
+        if (own[i]) {
+          if (!BULK)
+            kn[i] = SEP ? cmul(__ldg(&kk[tdy[i]]), __ldg(&kx[tdx[i]]))
+                        : __ldg(&kk[lane + 32 * i]);
+          if (FUSED) gn[i] = __ldg(&gin[(size_t)ly0 * A.W + lx0 + goff[i]]);
+        }
+    };
+    if (!BULK || FUSED) load_global(0);
+
+    bool failed = false;
+    // one visibility; false when a bulk copy did not arrive in time
+    auto body = [&](int j) -> bool {
+      float2 kc[MAXT], gc[MAXT];
+      if (BULK) {
+        if (issued < n) {
+          const int4 mi = meta[issued & (LANE_RING - 1)];
+          const int ist = cst == 0 ? LANE_DEPTH - 1 : cst - 1;
+          bulk_load_if(lane == 0, stages + (size_t)ist * SS, P.ktab + (size_t)mi.y * SS,
+                       slice_bytes, &bar[ist]);
+          ++issued;
+        }
+        bool ok = mbar_try(&bar[cst], cpar);
+        if (!__all_sync(FULL_MASK, ok)) {  // warp-uniform slow path, bounded
+          const long long t0 = clock64();
+          while (!ok && clock64() - t0 <= LANE_WAIT_CYCLES) ok = mbar_try(&bar[cst], cpar);
+          if (__any_sync(FULL_MASK, !ok)) return false;
+        }
+        const float2 *kp = stages + (size_t)cst * SS + lane;
+#pragma unroll
+        for (int i = 0; i < MAXT; ++i) kc[i] = own[i] ? kp[32 * i] : zero;
+        if (++cst == LANE_DEPTH) {
+          cst = 0;
+          cpar ^= 1u;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < MAXT; ++i) kc[i] = kn[i];
+      }
+#pragma unroll
+      for (int i = 0; i < MAXT; ++i) gc[i] = gn[i];
+      if ((!BULK || FUSED) && j + 1 < n) load_global(j + 1);
+
+      const int4 m = meta[j & (LANE_RING - 1)];
+      float2 u = mval[j & (LANE_RING - 1)];
+      const int base = (m.x >> 16) * pitch + (m.x & 0xffff);
+      if (FUSED) {
+        float2 sum = zero;
+#pragma unroll
+        for (int i = 0; i < MAXT; ++i) cfma(sum, gc[i], kc[i]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          sum.x += __shfl_xor_sync(FULL_MASK, sum.x, o);
+          sum.y += __shfl_xor_sync(FULL_MASK, sum.y, o);
+        }
+        if (lane == 0 && P.vis_out) P.vis_out[m.w] = sum;
+        if (P.mode == 1) {
+          u.x -= sum.x;
+          u.y -= sum.y;
+        }
+      }
+      // distinct taps of one visibility are distinct cells: plain read-modify-write
+#pragma unroll
+      for (int i = 0; i < MAXT; ++i)
+        if (own[i]) {
+          float2 *c = &wbuf[base + soff[i]];
+          float2 o = *c;
+          cfma(o, kc[i], u);
+          *c = o;
+        }
+      __syncwarp();  // this visibility's updates (and stage reads) before the next one
+      return true;
+    };
+
+    // Batches of 32 records: the next batch's indices are loaded before the
+    // first 8 visibilities, its values before the next 8, and it enters the
+    // ring before the last 16 (which may issue copies from it).
+    int j = 0;
+    for (int b0 = 0; b0 < n && !failed; b0 += 32) {
+      const int nb = min(32, n - b0);
+      const bool more = b0 + 32 < n;
+      const int jn = b0 + 32 + lane;
+      VisRec nrec;
+      int nsrc = 0;
+      float2 nval = zero;
+      if (more && jn < n) {
+        nrec = A.recs[w.start + jn];
+        nsrc = A.perm[w.start + jn];
+      }
+      for (int seg = 0; seg < 3 && !failed; ++seg) {
+        const int jend = b0 + min(nb, seg == 0 ? 8 : seg == 1 ? 16 : 32);
+        for (; j < jend; ++j)
+          if (!body(j)) {
+            failed = true;
+            break;
+          }
+        if (seg == 0 && more && jn < n) nval = value(nsrc);
+        if (seg == 1 && more) {
+          if (jn < n) {
+            meta[jn & (LANE_RING - 1)] = pack(nrec, nsrc);
+            mval[jn & (LANE_RING - 1)] = nval;
+          }
+          __syncwarp();
+        }
+      }
+    }
+    if (failed) {
+      // record the timeout, let this warp's copies in flight land, stop
+      if (lane == 0) {
+        atomicAdd((int32_t *)&A.status[ST_TIMEOUT], 1);
+        int st = cst;
+        uint32_t par = cpar;
+        for (int jx = j; jx < issued; ++jx) {
+          mbar_wait(&bar[st], par);
+          if (++st == LANE_DEPTH) {
+            st = 0;
+            par ^= 1u;
+          }
+        }
+      }
+      __syncwarp();
+      return;
+    }
+    for (int row = 0; row < win; ++row) {
+      const int gy = org.wy0 + row;
+      for (int q = lane; q < win; q += 32) {
+        const int c = row * pitch + q;
+        const float2 val = wbuf[c];
+        if (val.x != 0.f || val.y != 0.f) {
+          const int gx = org.wx0 + q;
+          if (gy < A.H && gx < A.W)
+            atomicAdd(&P.grid[org.layer_off + (size_t)gy * A.W + gx], val);
+          wbuf[c] = zero;
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+template <bool SEP, bool BULK, bool FUSED>
+static void *lane_kernel_for(int maxt, int SS, int pitch) {
+  if (maxt == 8 && SS == 256 && pitch == 32) return (void *)k_lane<SEP, BULK, FUSED, 8, true, 16, 32>;
+  if (maxt == 8 && SS == 256 && pitch == 48) return (void *)k_lane<SEP, BULK, FUSED, 8, true, 16, 48>;
+  if (maxt == 8 && SS == 256) return (void *)k_lane<SEP, BULK, FUSED, 8, true>;
+  if (maxt == 2 && SS == 64) return (void *)k_lane<SEP, BULK, FUSED, 2, true>;
+  switch (maxt) {
+    case 1: return (void *)k_lane<SEP, BULK, FUSED, 1, false>;
+    case 2: return (void *)k_lane<SEP, BULK, FUSED, 2, false>;
+    case 4: return (void *)k_lane<SEP, BULK, FUSED, 4, false>;
+    case 8: return (void *)k_lane<SEP, BULK, FUSED, 8, false>;
+    default: return nullptr;
+  }
+}
+
+int lane_launch(const cg_plan *p, const float2 *ktab, const float2 *vis, const float *weight,
+                int gmode, float2 *grid, const float2 *grid_in, float2 *vis_out, int residual,
+                bool fused, cudaStream_t s) {
+  const int S = p->kd.S, SS = S * S;
+  CG_REQUIRE(S <= 16, "the lane layout supports S <= 16 (S = %d)", S);
+  CG_REQUIRE(p->kd.sep || (int64_t)p->kd.G * p->kd.Q * p->kd.Q < (int64_t)1 << 31,
+             "kernel table has too many slices for the lane layout");
+  const int need = (SS + 31) / 32;
+  int maxt = 1;
+  while (maxt < need) maxt *= 2;
+  const bool bulk = !p->kd.sep && (SS * 8) % 16 == 0 && ((uintptr_t)ktab & 15) == 0;
+
+  LaneArgs P;
+  P.ktab = ktab;
+  P.vis = vis;
+  P.weight = weight;
+  P.grid = grid;
+  P.grid_in = grid_in;
+  P.vis_out = vis_out;
+  P.mode = fused ? (residual ? 1 : 0) : gmode;
+  auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+  size_t off = up16((size_t)p->pitch * p->win * sizeof(float2));
+  P.stage_off = (int)off;
+  if (bulk) off += (size_t)LANE_DEPTH * SS * sizeof(float2);
+  P.meta_off = (int)off;
+  off += LANE_RING * sizeof(int4);
+  P.val_off = (int)off;
+  off += LANE_RING * sizeof(float2);
+  P.bar_off = (int)off;
+  off = up16(off + LANE_DEPTH * sizeof(uint64_t));
+  P.warp_bytes = (int)off;
+
+  const cg_tuning t = tuning();
+  // warps per CTA: as asked (or as many as fill ~220 KB), at most what fits in 227 KB
+  const int fit = (int)std::min<size_t>(16, (227u << 10) / off);
+  CG_REQUIRE(fit >= 1, "lane-layout window does not fit in shared memory (%zu bytes per warp)",
+             off);
+  const int warps = std::min(fit, t.groups > 0 ? t.groups
+                                               : (int)std::max<size_t>(1, (220u << 10) / off));
+  void *fn = p->kd.sep ? (fused ? lane_kernel_for<true, false, true>(maxt, SS, p->pitch)
+                                : lane_kernel_for<true, false, false>(maxt, SS, p->pitch))
+                       : bulk ? (fused ? lane_kernel_for<false, true, true>(maxt, SS, p->pitch)
+                                       : lane_kernel_for<false, true, false>(maxt, SS, p->pitch))
+                              : (fused ? lane_kernel_for<false, false, true>(maxt, SS, p->pitch)
+                                       : lane_kernel_for<false, false, false>(maxt, SS, p->pitch));
+  CG_REQUIRE(fn, "no lane-layout kernel for support %d", S);
+  const size_t smem = (size_t)warps * off;
+  const int threads = 32 * warps;
+  CG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+  CG_REQUIRE(per_sm > 0, "lane-layout kernel does not fit on an SM (smem %zu)", smem);
+  const int64_t need_blocks = (p->max_items + warps - 1) / warps;
+  const int64_t blocks = std::max<int64_t>(
+      1, std::min<int64_t>((int64_t)per_sm * num_sms(), need_blocks));
+  TiledArgs A = tiled_args(p);
+  CG_CUDA(cudaMemsetAsync(p->ticket, 0, sizeof(int32_t), s));
+  void *args[] = {&A, &P};
+  CG_CUDA(cudaLaunchKernel(fn, dim3((unsigned)blocks), dim3(threads), args, smem, s));
+  return CG_OK;
+}
+
+}  // namespace cg

@@ -74,13 +74,13 @@ __global__ void k_weight_count(const double *uvw, int64_t stride, double lam, Ax
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double u = uvw[i * stride], v = uvw[i * stride + 1];
-  if (!(unit_range_fast(u, lam, k.inv_lam) && unit_range_fast(v, lam, k.inv_lam))) {
+  int x, xf, y, yf;
+  const bool inx = coord_fast(u, lam, k, N, 1, x, xf);
+  const bool iny = coord_fast(v, lam, k, N, 1, y, yf);
+  if (!(inx && iny)) {
     atomicAdd(&status[ST_RANGE], 1);
     return;
   }
-  int x, xf, y, yf;
-  frac_coord_fast(u, lam, k, N, 1, x, xf);
-  frac_coord_fast(v, lam, k, N, 1, y, yf);
   if (x < 0 || x >= N || y < 0 || y >= N) {
     atomicAdd(&status[ST_INDEX], 1);
     return;
@@ -96,8 +96,9 @@ __global__ void k_weight_apply(const double *uvw, int64_t stride, double lam, Ax
   if (i >= n) return;
   if ((status[ST_RANGE] | status[ST_INDEX]) != 0) return;
   int x, xf, y, yf;
-  frac_coord_fast(uvw[i * stride], lam, k, N, 1, x, xf);
-  frac_coord_fast(uvw[i * stride + 1], lam, k, N, 1, y, yf);
+  if (!(coord_fast(uvw[i * stride], lam, k, N, 1, x, xf) &&
+        coord_fast(uvw[i * stride + 1], lam, k, N, 1, y, yf)))
+    return;
   const double v = v_in ? v_in[i] : 1.0;
   w_out[i] = v / (double)counts[(size_t)x * N + y];
 }

@@ -179,13 +179,13 @@ __global__ void k_plan_coords(CoordParams P) {
   VisRec r = {0, 0, 0, 0};
   if (live) {
     const double u = P.uvw[i * P.stride], v = P.uvw[i * P.stride + 1];
-    if (!(unit_range_fast(u, P.lam, P.ax.inv_lam) && unit_range_fast(v, P.lam, P.ay.inv_lam))) {
+    int x, xf, y, yf;
+    const bool inx = coord_fast(u, P.lam, P.ax, P.W, P.Q, x, xf);
+    const bool iny = coord_fast(v, P.lam, P.ay, P.H, P.Q, y, yf);
+    if (!(inx && iny)) {
       atomicAdd(&P.status[ST_RANGE], 1);
       ok = false;
     } else {
-      int x, xf, y, yf;
-      frac_coord_fast(u, P.lam, P.ax, P.W, P.Q, x, xf);
-      frac_coord_fast(v, P.lam, P.ay, P.H, P.Q, y, yf);
       int x0 = x - P.S / 2, y0 = y - P.S / 2;
       if (x0 < 0 || y0 < 0 || x0 + P.S > P.W || y0 + P.S > P.H) {
         atomicAdd(&P.status[ST_BOUNDS], 1);
@@ -226,6 +226,11 @@ __global__ void k_plan_coords(CoordParams P) {
         }
       }
       if (ok) key = (P.mode == CG_PLAN_TILED) ? tile_bucket(P, lyr, x0, y0) : lyr * gper + grp;
+      if (ok && (unsigned)key >= (unsigned)P.nbuckets) {  // never: a bucket outside the histogram
+        atomicAdd(&P.status[ST_INDEX], 1);
+        ok = false;
+        key = -1;
+      }
     }
   }
   int slot = aggregated_slot(P.hist, key, ok);
@@ -281,11 +286,10 @@ __global__ void k_frac_coords(const double *uvw, int64_t stride, double lam,
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double u = uvw[i * stride], v = uvw[i * stride + 1];
-  if (!(unit_range_fast(u, lam, ax.inv_lam) && unit_range_fast(v, lam, ay.inv_lam)))
-    atomicAdd(&status[ST_RANGE], 1);
-  int a, b, c, d;
-  frac_coord_fast(u, lam, ax, W, Q, a, b);
-  frac_coord_fast(v, lam, ay, H, Q, c, d);
+  int a = 0, b = 0, c = 0, d = 0;
+  const bool inx = coord_fast(u, lam, ax, W, Q, a, b);
+  const bool iny = coord_fast(v, lam, ay, H, Q, c, d);
+  if (!(inx && iny)) atomicAdd(&status[ST_RANGE], 1);
   x[i] = a;
   xf[i] = b;
   y[i] = c;
@@ -403,11 +407,17 @@ static void plan_geometry(cg_plan &p) {
     p.nty = (p.H + p.T - 1) / p.T;
     p.tpl = p.ntx * p.nty;
     p.ntiles = p.tpl * p.layers;
-    p.sublog = 0;
-    while ((4 << p.sublog) < p.T) ++p.sublog;  // 4x4 sub-tiles, 2^sublog per tile edge
+    const cg_tuning t = tuning();
+    // 4x4-cell sub-tiles, 2^sublog per tile edge (4 << full >= T), except for the
+    // lane layout, whose private windows need no order inside a tile (tile
+    // buckets only).  The sub-tile edge is 1 << subshift cells, so that an
+    // in-tile coordinate shifted by subshift is always below 2^sublog.
+    int full = 0;
+    while ((4 << full) < p.T) ++full;
+    p.sublog = t.layout == CG_LAYOUT_LANE ? 0 : full;
+    p.subshift = 2 + full - p.sublog;
     // keep the histogram (4 B per bucket) within 2^24 buckets: coarser sub-tiles
     // for very large grid stacks
-    p.subshift = 2;  // sub-tile edge 1 << subshift cells
     while (p.sublog > 0 && ((int64_t)p.ntiles << (2 * p.sublog)) > (1 << 24)) {
       --p.sublog;
       ++p.subshift;
@@ -418,7 +428,6 @@ static void plan_geometry(cg_plan &p) {
     // consecutive 8-byte bank pairs of the window (no bank conflicts)
     p.pitch = p.win;
     while ((p.pitch - p.kd.S) % 16 != 0) ++p.pitch;
-    const cg_tuning t = tuning();
     int64_t want = p.n / (int64_t)(num_sms() * 16) + 1;
     p.chunk = t.chunk > 0 ? t.chunk
                           : (int)std::min<int64_t>(2048, std::max<int64_t>(256, want));

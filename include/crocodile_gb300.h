@@ -96,12 +96,17 @@ typedef struct {
  * "automatic".  tile: grid tile edge in cells (multiple of 4, <= 64; read
  * when a plan is created); chunk: visibilities per work item (plan
  * creation); layout: gridder layout, CG_LAYOUT_WARP (one warp per
- * visibility, shared-memory atomics) or CG_LAYOUT_OWNER (threads own window
- * cells by position mod S and keep running sums in registers); rows: row
- * residues per owner-layout thread (1..8); groups: owner-layout thread
- * groups, or warp-layout warps, per CTA (1..8).  Process-wide. */
+ * visibility, shared-memory atomics), CG_LAYOUT_OWNER (threads own window
+ * cells by position mod S and keep running sums in registers) or
+ * CG_LAYOUT_LANE (one warp per work item with a private window, lanes own
+ * cells by position mod S, kernel slices streamed by bulk copies; S <= 16;
+ * also selects the lane form of cg_degrid_grid); rows: row residues per
+ * owner-layout thread (1..8); groups: owner-layout thread groups, or
+ * warp-layout warps, per CTA (1..8), or lane-layout warps per CTA (1..16).
+ * Process-wide. */
 #define CG_LAYOUT_WARP 1
 #define CG_LAYOUT_OWNER 2
+#define CG_LAYOUT_LANE 3
 typedef struct {
   int tile;
   int chunk;

@@ -105,7 +105,8 @@ def test_tuning_roundtrip_and_validation(libpath):
         autotune.set_tuning(tile=32, chunk=700, rows=3, groups=2, layout=_lib.CG_LAYOUT_OWNER)
         assert autotune.get_tuning() == {"tile": 32, "chunk": 700, "rows": 3, "groups": 2,
                                          "layout": 2}
-        for bad in ({"tile": 30}, {"tile": 68}, {"rows": 9}, {"groups": 9}, {"layout": 3}):
+        for bad in ({"tile": 30}, {"tile": 68}, {"rows": 9}, {"groups": 9}, {"layout": 4},
+                    {"layout": 3, "groups": 17}):
             with pytest.raises(ValueError):
                 autotune.set_tuning(**bad)
     finally:

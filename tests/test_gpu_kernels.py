@@ -91,6 +91,9 @@ def _wproj_case(O, n=20000, N=256, seed=5):
     {"layout": 2, "rows": 4, "groups": 4, "tile": 24, "chunk": 100},
     {"layout": 2, "rows": 5, "groups": 1, "tile": 64},
     {"layout": 2, "rows": 8, "groups": 1, "tile": 32},
+    {"layout": 3, "tile": 32},
+    {"layout": 3, "groups": 3, "tile": 16, "chunk": 40},
+    {"layout": 3, "groups": 16, "tile": 24},
 ])
 def test_gridder_shapes_match_oracle(env, cfg):
     torch, E, S, A, O = env
@@ -108,7 +111,8 @@ def test_gridder_shapes_match_oracle(env, cfg):
     assert rel(vgot, vref) < FP32_TOL
 
 
-@pytest.mark.parametrize("S_,sep", [(8, True), (8, False), (7, False), (16, False)])
+@pytest.mark.parametrize("S_,sep", [(8, True), (8, False), (7, False), (16, False), (16, True),
+                                    (3, False), (12, False)])
 def test_supports_and_separable(env, S_, sep):
     torch, E, S, A, O = env
     rng = numpy.random.default_rng(S_)
@@ -119,7 +123,7 @@ def test_supports_and_separable(env, S_, sep):
     aa = O.anti_aliasing_function(N, 0, 6)
     kv = O.kernel_oversample(aa, Q, S_) if sep else \
         O.kernel_oversample(numpy.outer(aa, aa), Q, S_)
-    for layout in (1, 2):
+    for layout in (1, 2, 3):
         A.set_tuning(layout=layout)
         try:
             g = S.conv_imaging(theta, lam, uvw, None, vis, kv)
@@ -157,14 +161,24 @@ def test_fused_wbin_plan(env):
     assert float(g2.abs().sum()) == 0.0
 
 
-@pytest.mark.parametrize("sep", [False, True])
-def test_fused_degrid_grid_matches_separate(env, sep):
+@pytest.mark.parametrize("sep,S_,layout", [(False, 7, 1), (True, 7, 1), (False, 7, 3),
+                                           (True, 7, 3), (False, 8, 3), (False, 16, 3)])
+def test_fused_degrid_grid_matches_separate(env, sep, S_, layout):
     torch, E, S, A, O = env
     theta, lam, uvw, vis = _wproj_case(O, n=30000, N=256, seed=13)
     N = int(round(theta * lam))
     aa = O.anti_aliasing_function(N, 0, 7)
-    kv = O.kernel_oversample(aa, 4, 7) if sep else O.kernel_oversample(numpy.outer(aa, aa), 4, 7)
+    kv = O.kernel_oversample(aa, 4, S_) if sep else \
+        O.kernel_oversample(numpy.outer(aa, aa), 4, S_)
     kt = E.KernelTable.from_gcf(kv, 0, E.CF)
+    A.set_tuning(layout=layout)
+    try:
+        _fused_checks(torch, E, kt, uvw, lam, N, vis)
+    finally:
+        A.set_tuning()
+
+
+def _fused_checks(torch, E, kt, uvw, lam, N, vis):
     plan = E.Plan(uvw, lam, (N, N), kt)
     rng = numpy.random.default_rng(3)
     model = E.cuda_tensor(rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N)), E.CF)
@@ -182,3 +196,31 @@ def test_fused_degrid_grid_matches_separate(env, sep):
     g2 = torch.zeros((N, N), dtype=E.CF, device="cuda")
     plan.degrid_grid(kt, model, v_in, g2, residual=True)
     assert r(g2, ref_res) < 1e-5
+
+
+@pytest.mark.parametrize("S_", [8, 15, 16])
+def test_lane_layout_weighted_modes(env, S_):
+    """Weighted gridding (vis * weight) and the weights-only PSF pass in the lane
+    layout against the warp layout on the same plan."""
+    torch, E, S, A, O = env
+    theta, lam, uvw, vis = _wproj_case(O, n=20000, N=256, seed=21)
+    N = int(round(theta * lam))
+    aa = O.anti_aliasing_function(N, 0, 7)
+    kt = E.KernelTable.from_gcf(O.kernel_oversample(numpy.outer(aa, aa), 4, S_), 0, E.CF)
+    plan = E.Plan(uvw, lam, (N, N), kt)
+    v = E.cuda_tensor(vis, E.CF)
+    wt = torch.rand(len(vis), device="cuda", dtype=torch.float32) + 0.5
+    out = {}
+    for layout in (1, 3):
+        A.set_tuning(layout=layout)
+        try:
+            g1 = plan.grid_weighted(kt, v, wt, torch.zeros((N, N), dtype=E.CF, device="cuda"))
+            g2 = plan.grid_weighted(kt, None, wt, torch.zeros((N, N), dtype=E.CF, device="cuda"))
+        finally:
+            A.set_tuning()
+        out[layout] = (g1, g2)
+    plan.check()
+    for a, b in zip(out[3], out[1]):
+        err = float(torch.linalg.vector_norm((a - b).to(torch.complex128)) /
+                    torch.linalg.vector_norm(b.to(torch.complex128)))
+        assert err < 1e-6, err
