@@ -72,10 +72,16 @@ def _store(sig, entry):
 
 def candidates(S, quick=False):
     """Launch shapes to try: the warp layout over tile edge, work-item size and
-    warps per CTA; the owner layout over tile edge, rows per thread and groups."""
+    warps per CTA; the owner layout over tile edge, rows per thread and groups;
+    the lane layout (S <= 16) over tile edge and work-item size."""
     tiles = [t for t in ((32, 48) if quick else (16, 24, 32, 48, 64)) if t >= min(S, 16)]
     chunks = (0, 1024) if quick else (0, 512, 2048)
     out = []
+    if S <= 16:
+        for tile, chunk in itertools.product((16, 32) if quick else (16, 24, 32),
+                                             (512, 1024) if quick else (0, 512, 1024)):
+            out.append({"tile": tile, "chunk": chunk, "rows": 0, "groups": 0,
+                        "layout": L.CG_LAYOUT_LANE})
     for tile, chunk in itertools.product(tiles, chunks):
         for warps in ((8,) if quick else (4, 8)):
             out.append({"tile": tile, "chunk": chunk, "rows": 0, "groups": warps,
@@ -93,31 +99,33 @@ def candidates(S, quick=False):
 
 
 def time_config(cfg, uvw, lam, shape, ktab, kidx, vis, repeats=3):
-    """Median device ms of grid + degrid (CUDA events around the two launches)
-    with this tuning, or None if the shape does not run."""
+    """Median device ms of plan + grid + degrid (CUDA events around plan creation
+    and the two launches) with this tuning, or None if the shape does not run."""
     set_tuning(**cfg)
     grid = torch.zeros(shape, dtype=E.CF, device="cuda")
     out = torch.empty(uvw.shape[0], dtype=E.CF, device="cuda")
     times = []
     try:
-        plan = E.Plan(uvw, lam, shape, ktab, kidx)
         for i in range(repeats + 1):
             grid.zero_()
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
             ev[0].record()
-            plan.grid(ktab, vis, grid)
+            plan = E.Plan(uvw, lam, shape, ktab, kidx)
             ev[1].record()
-            plan.degrid(ktab, grid, out)
+            plan.grid(ktab, vis, grid)
             ev[2].record()
+            plan.degrid(ktab, grid, out)
+            ev[3].record()
             torch.cuda.synchronize()
+            plan.check()
             if i:
-                times.append((ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])))
-        plan.check()
+                times.append(tuple(ev[k].elapsed_time(ev[k + 1]) for k in range(3)))
+            del plan
     except (RuntimeError, ValueError):
         return None
-    times.sort(key=lambda t: t[0] + t[1])
-    g, d = times[len(times) // 2]
-    return {"grid": g, "degrid": d, "total": g + d}
+    times.sort(key=sum)
+    p, g, d = times[len(times) // 2]
+    return {"plan": p, "grid": g, "degrid": d, "total": p + g + d}
 
 
 def tune(uvw, lam, shape, ktab, kidx, vis, cands=None, repeats=3, use_cache=True, verbose=False):

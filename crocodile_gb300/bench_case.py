@@ -59,8 +59,10 @@ def setup(workload="wproj", nvis=500_000, seed=None):
 class Step:
     """One plan + grid + degrid step through the C ABI, reusing one workspace."""
 
-    def __init__(self, ctx):
+    def __init__(self, ctx, fused=False):
         self.c = ctx
+        self.fused = fused
+        self.model = None
         w = ctx["w"]
         self.n = w.uvw.shape[0]
         self.N = w.N
@@ -92,6 +94,12 @@ class Step:
                    P(c["st"].t), sp)
         try:
             self.grid.zero_()
+            if self.fused:
+                if self.model is None:
+                    self.model = torch.randn_like(self.grid)
+                L.call("cg_degrid_grid", h, P(c["kt"].table), P(self.model), P(vis), 0,
+                       P(self.out), P(self.grid), sp)
+                return
             if events:
                 events[0].record()
             L.call("cg_grid", h, P(c["kt"].table), P(vis), P(self.grid), sp)
@@ -110,6 +118,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--workload", default="wproj", choices=["wproj", "plain", "aw"])
     ap.add_argument("--tune", action="store_true", help="autotune the launch shape first")
+    ap.add_argument("--fused", action="store_true",
+                    help="one degrid+grid pass (cg_degrid_grid) instead of two calls")
     ap.add_argument("--tuning", default="",
                     help="explicit launch shape tile,chunk,rows,groups,layout (no autotuning)")
     a = ap.parse_args()
@@ -127,7 +137,7 @@ def main():
         best, _ = autotune.tune(ctx["uvw"], w.lam, (w.N, w.N), ctx["kt"], kidx, ctx["vis"],
                                 cands=autotune.candidates(w.S, quick=True), use_cache=False)
         print("tuning", best)
-    step = Step(ctx)
+    step = Step(ctx, a.fused)
     step()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -135,7 +145,8 @@ def main():
         step()
     torch.cuda.synchronize()
     ctx["st"].check()
-    print("%s n=%d: %.3f ms/step" % (a.workload, a.nvis, 1e3 * (time.perf_counter() - t0) / a.steps))
+    print("%s%s n=%d: %.3f ms/step" % (a.workload, " fused" if a.fused else "", a.nvis,
+                                        1e3 * (time.perf_counter() - t0) / a.steps))
 
 
 if __name__ == "__main__":

@@ -114,6 +114,8 @@ def test_tuning_roundtrip_and_validation(libpath):
     assert autotune.get_tuning() == {"tile": 0, "chunk": 0, "rows": 0, "groups": 0, "layout": 0}
     cands = autotune.candidates(15)
     assert any(c["layout"] == 1 for c in cands) and any(c["layout"] == 2 for c in cands)
+    assert any(c["layout"] == 3 for c in cands)
+    assert not any(c["layout"] == 3 for c in autotune.candidates(24))
     for c in cands:
         if c["layout"] == 2:
             gpad = (15 * ((15 + c["rows"] - 1) // c["rows"]) + 31) // 32 * 32
