@@ -42,6 +42,16 @@ cg_tuning tuning() {
   return g_tuning;
 }
 
+// The tuned layout, or automatically the lane layout for tables whose S x S
+// slices stream by bulk copies (non-separable, even S <= 16) and the warp
+// layout otherwise.  The lane layout needs S <= 16.
+int layout_for(const cg_kernel_desc &kd) {
+  const int l = tuning().layout;
+  if (l == CG_LAYOUT_LANE) return kd.S <= 16 ? CG_LAYOUT_LANE : CG_LAYOUT_WARP;
+  if (l > 0) return l;
+  return (!kd.sep && kd.S <= 16 && kd.S % 2 == 0) ? CG_LAYOUT_LANE : CG_LAYOUT_WARP;
+}
+
 }  // namespace cg
 
 extern "C" {

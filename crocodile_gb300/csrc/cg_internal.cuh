@@ -32,6 +32,7 @@ enum { ST_RANGE = 0, ST_BOUNDS = 1, ST_INDEX = 2, ST_TIMEOUT = 3 };
 
 int num_sms();
 cg_tuning tuning();  // current process-wide launch-shape tuning
+int layout_for(const cg_kernel_desc &kd);  // gridder layout used for this kernel table
 
 // ---------------------------------------------------------------- device helpers
 // Python-style floor division / modulo of an integer by a positive divisor.

@@ -543,8 +543,8 @@ static int grid_launch(const cg_plan *p, const void *ktab, const void *vis,
   void *args[12];
   int gsize = 0, ngroups = 0;
   bool shared = false;
-  const int layout = t.layout > 0 ? t.layout : CG_LAYOUT_WARP;
-  if (layout == CG_LAYOUT_LANE && S <= 16)
+  const int layout = layout_for(p->kd);
+  if (layout == CG_LAYOUT_LANE)
     return lane_launch(p, kt, vv, weight, mode, gg, nullptr, nullptr, 0, false, s);
   if (layout != CG_LAYOUT_OWNER) {
     const int need = (S * S + 31) / 32;
@@ -650,7 +650,7 @@ int cg_degrid_grid(const cg_plan *p, const void *ktab, const void *grid_in, cons
   cudaStream_t s = (cudaStream_t)stream;
   const int S = p->kd.S;
   const cg_tuning t = tuning();
-  if (t.layout == CG_LAYOUT_LANE && S <= 16)
+  if (layout_for(p->kd) == CG_LAYOUT_LANE)
     return lane_launch(p, (const float2 *)ktab, (const float2 *)vis_in, nullptr, 0,
                        (float2 *)grid_out, (const float2 *)grid_in, (float2 *)vis_out, residual,
                        true, s);

@@ -392,9 +392,11 @@ struct Layout {
   size_t rec_tmp, key, rank, recs, perm, counts, offsets, scan, items, ctr, total;
 };
 
-static int tile_edge(int S) {
+static int tile_edge(const cg_kernel_desc &kd) {
   const cg_tuning t = tuning();
+  const int S = kd.S;
   if (t.tile > 0) return std::max(4, std::min(64, t.tile & ~3));
+  if (layout_for(kd) == CG_LAYOUT_LANE) return 16;  // per-warp windows stay small
   if (S <= 8) return 32;
   if (S <= 16) return 48;
   return 64;
@@ -402,7 +404,7 @@ static int tile_edge(int S) {
 
 static void plan_geometry(cg_plan &p) {
   if (p.mode == CG_PLAN_TILED) {
-    p.T = tile_edge(p.kd.S);
+    p.T = tile_edge(p.kd);
     p.ntx = (p.W + p.T - 1) / p.T;
     p.nty = (p.H + p.T - 1) / p.T;
     p.tpl = p.ntx * p.nty;
@@ -414,7 +416,7 @@ static void plan_geometry(cg_plan &p) {
     // in-tile coordinate shifted by subshift is always below 2^sublog.
     int full = 0;
     while ((4 << full) < p.T) ++full;
-    p.sublog = t.layout == CG_LAYOUT_LANE ? 0 : full;
+    p.sublog = layout_for(p.kd) == CG_LAYOUT_LANE ? 0 : full;
     p.subshift = 2 + full - p.sublog;
     // keep the histogram (4 B per bucket) within 2^24 buckets: coarser sub-tiles
     // for very large grid stacks

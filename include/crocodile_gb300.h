@@ -103,7 +103,9 @@ typedef struct {
  * also selects the lane form of cg_degrid_grid); rows: row residues per
  * owner-layout thread (1..8); groups: owner-layout thread groups, or
  * warp-layout warps, per CTA (1..8), or lane-layout warps per CTA (1..16).
- * Process-wide. */
+ * layout 0 picks CG_LAYOUT_LANE (with 16-cell tiles) for non-separable tables
+ * with even S <= 16, whose slices stream by bulk copies, and CG_LAYOUT_WARP
+ * otherwise.  Process-wide. */
 #define CG_LAYOUT_WARP 1
 #define CG_LAYOUT_OWNER 2
 #define CG_LAYOUT_LANE 3
