@@ -550,7 +550,9 @@ def run_ours(args):
     dom_ms = max(ms_grid, ms_degrid)
     tuned = G.tuned
     if dom == "grid":
-        kname = "k_grid_warp" if tuned.get("layout") in (0, L.CG_LAYOUT_WARP) else "k_grid_tiled"
+        lay = autotune.effective_layout(G.kt)
+        kname = {L.CG_LAYOUT_LANE: "k_lane", L.CG_LAYOUT_OWNER: "k_grid_tiled"}.get(lay,
+                                                                                   "k_grid_warp")
     else:
         kname = "k_degrid_tiled"
     peaks = {}
@@ -606,7 +608,8 @@ def run_ours(args):
                      "algorithmic_bytes": alg, "ms": dom_ms,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks
                      else "fallback 6800 GB/s"},
-        "kernel_ms": {"grid": ms_grid, "degrid": ms_degrid, "plan": ms - ms_grid - ms_degrid,
+        "kernel_ms": {"grid": ms_grid, "degrid": ms_degrid,
+                      "plan_and_grid_zeroing": ms - ms_grid - ms_degrid,
                       "kernel_generation_once": G.kgen_ms},
         "updates_per_s": 2 * n * S * S / (ms * 1e-3),
         "plain_fp64": {"value": plain_value, "unit": "Mvis/s", "ms_per_step": ms_plain,

@@ -37,6 +37,20 @@ def get_tuning():
             "layout": t.layout}
 
 
+def effective_layout(ktab):
+    """The gridder layout the library uses for this kernel table under the
+    current tuning (the rule of layout_for in csrc/api.cu): the tuned layout
+    (the lane layout only for S <= 16), or automatically the lane layout for
+    non-separable tables with even S <= 16 and the warp layout otherwise."""
+    lay = get_tuning()["layout"]
+    if lay == L.CG_LAYOUT_LANE:
+        return lay if ktab.S <= 16 else L.CG_LAYOUT_WARP
+    if lay:
+        return lay
+    return L.CG_LAYOUT_LANE if (not ktab.sep and ktab.S <= 16 and ktab.S % 2 == 0) \
+        else L.CG_LAYOUT_WARP
+
+
 def signature(shape, ktab, n):
     n2 = 1 << max(0, int(n - 1).bit_length())
     return "H%d_W%d_S%d_Q%d_%s_n%d" % (shape[0], shape[1], ktab.S, ktab.Q,
