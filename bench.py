@@ -302,18 +302,21 @@ class GpuWorkload:
         self.tune_s = time.perf_counter() - t0
         self._alloc_ws()
 
-    def step(self, uvw, vis, kev=None):
-        """plan + grid + degrid, all stream-ordered (no host synchronisation)."""
+    def step(self, uvw, vis, kev=None, grid=None, out=None):
+        """plan + grid + degrid, all stream-ordered (no host synchronisation), into
+        self.grid / self.out or the given buffers."""
         L, P = self.L, self.P
+        grid = self.grid if grid is None else grid
+        out = self.out if out is None else out
         h = ctypes.c_void_p()
         self.create_plan(h, uvw)
-        self.grid.zero_()
+        grid.zero_()
         if kev:
             kev[0].record(self.stream)
-        L.call("cg_grid", h, P(self.kt.table), P(vis), P(self.grid), self.sp)
+        L.call("cg_grid", h, P(self.kt.table), P(vis), P(grid), self.sp)
         if kev:
             kev[1].record(self.stream)
-        L.call("cg_degrid", h, P(self.kt.table), P(self.grid), P(self.out), self.sp)
+        L.call("cg_degrid", h, P(self.kt.table), P(grid), P(out), self.sp)
         if kev:
             kev[2].record(self.stream)
         L.lib().cg_plan_destroy(h)
@@ -498,28 +501,60 @@ def run_ours(args):
     # ---- end to end through the C ABI with host buffers (pinned), copies timed
     h_uvw = torch.from_numpy(w.uvw).pin_memory()
     h_vis = torch.from_numpy(w.vis.astype(numpy.complex64)).pin_memory()
-    h_grid = torch.empty((N, N), dtype=torch.complex64).pin_memory()
-    h_out = torch.empty(n, dtype=torch.complex64).pin_memory()
-    d_uvw, d_vis = torch.empty_like(G.uvw), torch.empty_like(G.vis)
-    e2e_times = []
-    for i in range(min(args.steps, 20) + 1):
-        flush.zero_()
-        e0, e1 = ev(), ev()
-        e0.record(stream)
-        d_uvw.copy_(h_uvw, non_blocking=True)
-        d_vis.copy_(h_vis, non_blocking=True)
-        G.step(d_uvw, d_vis)
-        h_grid.copy_(G.grid, non_blocking=True)
-        h_out.copy_(G.out, non_blocking=True)
-        e1.record(stream)
-        if i:
-            e2e_times.append((e0, e1))
-    torch.cuda.synchronize()
-    ms_e2e = statistics.mean(a.elapsed_time(b) for a, b in e2e_times)
+    h_grid = [torch.empty((N, N), dtype=torch.complex64).pin_memory() for _ in range(2)]
+    h_out = [torch.empty(n, dtype=torch.complex64).pin_memory() for _ in range(2)]
+    # Pipelined over steps: step i's inputs are copied in on one copy stream and
+    # its grid and predicted visibilities copied out on another, each step into
+    # and out of its own (double-buffered) device buffers, so that copies of
+    # neighbouring steps overlap step i's kernels.  Every step still moves its
+    # own inputs and results; the time is first copy-in to last copy-out.
+    d_uvw = [G.uvw, torch.empty_like(G.uvw)]
+    d_vis = [G.vis, torch.empty_like(G.vis)]
+    d_grid = [G.grid, torch.empty_like(G.grid)]
+    d_out = [G.out, torch.empty_like(G.out)]
+    s_in, s_outs = torch.cuda.Stream(), torch.cuda.Stream()
+    k_steps = min(args.steps, 20)
+
+    def pipeline(k):
+        in_ready = [ev(), ev()]
+        done = [None, None]
+        copied = [None, None]
+        t0, t1 = ev(), ev()
+        t0.record(s_in)
+        for i in range(k):
+            b = i % 2
+            if done[b] is not None:
+                s_in.wait_event(done[b])  # step i - 2 finished reading buffer b
+            with torch.cuda.stream(s_in):
+                d_uvw[b].copy_(h_uvw, non_blocking=True)
+                d_vis[b].copy_(h_vis, non_blocking=True)
+            in_ready[b] = ev()
+            in_ready[b].record(s_in)
+            stream.wait_event(in_ready[b])
+            if copied[b] is not None:
+                stream.wait_event(copied[b])  # step i - 2's results are out
+            G.step(d_uvw[b], d_vis[b], grid=d_grid[b], out=d_out[b])
+            done[b] = ev()
+            done[b].record(stream)
+            s_outs.wait_event(done[b])
+            with torch.cuda.stream(s_outs):
+                h_grid[b].copy_(d_grid[b], non_blocking=True)
+                h_out[b].copy_(d_out[b], non_blocking=True)
+            copied[b] = ev()
+            copied[b].record(s_outs)
+        t1.record(s_outs)
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) / k
+
+    pipeline(2)  # warm-up
+    ms_e2e = pipeline(k_steps)
     e2e = {"value": world * n / (ms_e2e * 1e-3) / 1e6, "unit": "Mvis/s",
            "h2d_bytes_per_step": h_uvw.numel() * 8 + h_vis.numel() * 8,
-           "d2h_bytes_per_step": h_grid.numel() * 8 + h_out.numel() * 8}
-    del d_uvw, d_vis
+           "d2h_bytes_per_step": h_grid[0].numel() * 8 + h_out[0].numel() * 8,
+           "form": "pipelined over %d steps: copy-in, kernels and copy-out on three streams, "
+                   "double-buffered device inputs and results" % k_steps}
+    G.st.check()
+    del d_uvw, d_vis, d_grid, d_out
 
     # ---- fused form: plan + one pass that degrids the grid and grids the visibilities
     for _ in range(3):

@@ -431,8 +431,11 @@ static void plan_geometry(cg_plan &p) {
     p.pitch = p.win;
     while ((p.pitch - p.kd.S) % 16 != 0) ++p.pitch;
     int64_t want = p.n / (int64_t)(num_sms() * 16) + 1;
-    p.chunk = t.chunk > 0 ? t.chunk
-                          : (int)std::min<int64_t>(2048, std::max<int64_t>(256, want));
+    // lane layout: one warp per item, ~12 warps per SM, so shorter items
+    p.chunk = t.chunk > 0                              ? t.chunk
+              : layout_for(p.kd) == CG_LAYOUT_LANE ? 512
+                                                   : (int)std::min<int64_t>(
+                                                         2048, std::max<int64_t>(256, want));
     p.max_items = (p.n + p.chunk - 1) / p.chunk + p.ntiles;
   } else {
     p.T = 0;
