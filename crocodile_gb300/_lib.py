@@ -76,6 +76,7 @@ SIGNATURES = {
     "cg_set_tuning": (c_int, [ctypes.POINTER(Tuning)]),
     "cg_get_tuning": (c_int, [ctypes.POINTER(Tuning)]),
     "cg_plan_info": (c_int, [P, P]),
+    "cg_plan_export": (c_int, [P, P, P, P, P]),
     "cg_grid": (c_int, [P, P, P, P, P]),
     "cg_grid_weighted": (c_int, [P, P, P, P, P, P]),
     "cg_degrid": (c_int, [P, P, P, P, P]),

@@ -726,6 +726,21 @@ int cg_plan_info(const cg_plan *p, int64_t *info) {
   return CG_OK;
 }
 
+int cg_plan_export(const cg_plan *p, int32_t *recs, int32_t *perm, int32_t *counts,
+                   cg_stream_t stream) {
+  CG_REQUIRE(p, "NULL plan");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (recs && p->n > 0)
+    CG_CUDA(cudaMemcpyAsync(recs, p->recs, (size_t)p->n * sizeof(VisRec),
+                            cudaMemcpyDeviceToDevice, s));
+  if (perm && p->n > 0)
+    CG_CUDA(cudaMemcpyAsync(perm, p->perm, (size_t)p->n * 4, cudaMemcpyDeviceToDevice, s));
+  if (counts)
+    CG_CUDA(cudaMemcpyAsync(counts, p->counts, (size_t)p->nbuckets * 4, cudaMemcpyDeviceToDevice,
+                            s));
+  return CG_OK;
+}
+
 int cg_w_bins(const double *uvw, int64_t stride, int64_t n, double wstep, int32_t *kidx,
               int32_t *d_minmax, int32_t *h_minmax, int32_t *d_status, cg_stream_t stream) {
   CG_REQUIRE(n >= 1 && uvw && stride >= 3 && kidx && d_minmax && h_minmax && d_status,

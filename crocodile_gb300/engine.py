@@ -179,6 +179,16 @@ class Plan:
         L.call("cg_plan_info", self.handle, out)
         return {"tile": out[0], "max_items": out[1], "chunk": out[2], "buckets": out[3]}
 
+    def export(self):
+        """(recs [n, 4] int32 {x0, y0, k0, k1} in sorted order, perm [n] sorted
+        position -> input index, counts [buckets]) as CUDA tensors."""
+        nb = self.info()["buckets"]
+        recs = torch.empty((self.n, 4), dtype=torch.int32, device="cuda")
+        perm = torch.empty(self.n, dtype=torch.int32, device="cuda")
+        counts = torch.empty(nb, dtype=torch.int32, device="cuda")
+        L.call("cg_plan_export", self.handle, _p(recs), _p(perm), _p(counts), stream())
+        return recs, perm, counts
+
     def check(self):
         self.status.check()
 

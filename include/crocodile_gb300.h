@@ -177,6 +177,15 @@ int cg_plan_create_ex(cg_plan **plan, int mode, const cg_kernel_desc *kd,
 int cg_plan_destroy(cg_plan *plan);
 /* Tile edge (cells) and number of work items upper bound, for reports. */
 int cg_plan_info(const cg_plan *plan, int64_t *info_out /* [4] */);
+/* Copies of a plan's sort into caller device buffers, for checks (no
+ * reference counterpart; the reference grids in input order): recs_out [n x 4]
+ * int32 {x0, y0, k0, k1} (footprint origin and kernel rows, sorted by
+ * bucket), perm_out [n] (sorted position -> input index), counts_out
+ * [nbuckets] (visibilities per bucket: grid tile, or tile and sub-tile along a
+ * Morton curve; kernel group in CG_PLAN_GROUPS mode; nbuckets = info[3] of
+ * cg_plan_info).  Any output may be NULL.  Stream-ordered. */
+int cg_plan_export(const cg_plan *plan, int32_t *recs_out, int32_t *perm_out,
+                   int32_t *counts_out, cg_stream_t stream);
 
 /* convgrid (synthesis.py:464-481): grid[H,W] (c64) += K * vis (c64).
  * FP32 products and accumulation; persistent tiled kernel; CG_PLAN_TILED. */
