@@ -72,6 +72,9 @@ SIGNATURES = {
     "cg_compact_keys": (c_int, [P, c_int64, c_int, P, P, P, P, c_size_t, P, P]),
     "cg_aw_keys": (c_int, [P, c_int64, P, P, c_int64, c_int, c_double, c_int, c_int, P, P, P]),
     "cg_wstack_combine": (c_int, [P, c_int, c_int, c_double, P, P, P, P, P]),
+    "cg_tower_keys": (c_int, [P, c_int64, c_int64, c_double, c_int, c_double, P, P, P, P, P, P]),
+    "cg_towers_combine": (c_int, [P, c_int, c_int, c_double, P, P, c_int, P, P, P]),
+    "cg_towers_add": (c_int, [P, c_int, c_int, P, c_int, P, P]),
     "cg_plan_destroy": (c_int, [P]),
     "cg_set_tuning": (c_int, [ctypes.POINTER(Tuning)]),
     "cg_get_tuning": (c_int, [ctypes.POINTER(Tuning)]),

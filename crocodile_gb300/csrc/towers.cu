@@ -1,0 +1,215 @@
+// w-towers: w-stacking on sub-grids (examples/grid/grid.c:482-710,
+// examples/notebooks/wtowers.ipynb code cell 16), batched over every sub-grid.
+//
+// Visibilities fall into uv chunks of C = subgrid - margin cells and w-planes
+// of width wincrement:
+//   ub = floor(u*theta / C), vb = floor(v*theta / C), wp = rint(w / wincrement)
+// A chunk's sub-grid (s x s cells) is centred on xmid = (C*ub + C*(ub+1)) // 2
+// cells from the grid centre (likewise ymid).  Each (chunk, plane) pair with
+// visibilities becomes one layer of a stack of sub-grids, gridded in one
+// launch (a layered plan on the chunk-relative coordinates with the residual-w
+// kernels), inverse-transformed by one batched FFT; this file then forms, per
+// chunk, image = sum over its planes of layer / w_kernel_function(l, m,
+// wp*wincrement) (the Fresnel transfer between planes in closed form), and,
+// after a batched forward FFT, adds each chunk's sub-grid into the grid.
+//
+// The chunk and plane of a visibility and its chunk-relative coordinates are
+// IEEE double operations in the same order as the numpy restatement, so the
+// binning is bit-identical to it.
+#include <algorithm>
+
+#include "cg_internal.cuh"
+
+namespace cg {
+
+struct TowerBins {
+  int64_t ub, vb, wp;
+  double ru, rv, rw;  // coordinates relative to the chunk centre and the plane
+};
+
+__device__ __forceinline__ int64_t floor_div_ll(int64_t a, int64_t b) {
+  int64_t q, r;
+  q = a / b;
+  r = a - q * b;
+  if (r != 0 && ((r < 0) != (b < 0))) --q;
+  return q;
+}
+
+__device__ __forceinline__ bool tower_bins(const double *row, double theta, int C, double winc,
+                                           TowerBins &t) {
+  const double u = row[0], v = row[1], w = row[2];
+  const double fu = floor(__ddiv_rn(__dmul_rn(u, theta), (double)C));
+  const double fv = floor(__ddiv_rn(__dmul_rn(v, theta), (double)C));
+  const double fw = rint(__ddiv_rn(w, winc));
+  if (!(fabs(fu) < 1e9 && fabs(fv) < 1e9 && fabs(fw) < 1e9)) return false;  // NaN too
+  t.ub = (int64_t)fu;
+  t.vb = (int64_t)fv;
+  t.wp = (int64_t)fw;
+  const int64_t xmid = floor_div_ll((int64_t)C * t.ub + (int64_t)C * (t.ub + 1), 2);
+  const int64_t ymid = floor_div_ll((int64_t)C * t.vb + (int64_t)C * (t.vb + 1), 2);
+  t.ru = __dadd_rn(u, -__ddiv_rn((double)xmid, theta));
+  t.rv = __dadd_rn(v, -__ddiv_rn((double)ymid, theta));
+  t.rw = __dadd_rn(w, -__dmul_rn(fw, winc));
+  return true;
+}
+
+__global__ void k_tower_bounds(const double *__restrict__ uvw, int64_t stride, int64_t n,
+                               double theta, int C, double winc, int32_t *mm,
+                               int32_t *status) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  TowerBins t;
+  if (!tower_bins(uvw + i * stride, theta, C, winc, t)) {
+    atomicAdd(&status[ST_RANGE], 1);
+    return;
+  }
+  atomicMin(&mm[0], (int)t.ub);
+  atomicMax(&mm[1], (int)t.ub);
+  atomicMin(&mm[2], (int)t.vb);
+  atomicMax(&mm[3], (int)t.vb);
+  atomicMin(&mm[4], (int)t.wp);
+  atomicMax(&mm[5], (int)t.wp);
+}
+
+__global__ void k_tower_mm_init(int32_t *mm) {
+  if (threadIdx.x < 6) mm[threadIdx.x] = (threadIdx.x & 1) ? INT32_MIN : INT32_MAX;
+}
+
+// key = ((vb - vbmin) * nub + (ub - ubmin)) * nwp + (wp - wpmin): sorted keys
+// group a chunk's planes together, in increasing w.
+__global__ void k_tower_keys(const double *__restrict__ uvw, int64_t stride, int64_t n,
+                             double theta, int C, double winc, int ubmin, int vbmin, int wpmin,
+                             int nub, int nwp, int32_t *__restrict__ key,
+                             double *__restrict__ rel) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  TowerBins t;
+  if (!tower_bins(uvw + i * stride, theta, C, winc, t)) {
+    key[i] = 0;  // counted as a range error by the bounds pass
+    rel[3 * i] = rel[3 * i + 1] = rel[3 * i + 2] = 0.0;
+    return;
+  }
+  key[i] = (int32_t)((((int)t.vb - vbmin) * nub + ((int)t.ub - ubmin)) * nwp +
+                     ((int)t.wp - wpmin));
+  rel[3 * i] = t.ru;
+  rel[3 * i + 1] = t.rv;
+  rel[3 * i + 2] = t.rw;
+}
+
+// out[c, i, j] = sum over the layers L of chunk c of stack[L, i, j] /
+// exp(2 pi i w_L ph(i, j)), ph = 1 - sqrt(1 - l^2 - m^2) on the sub-grid's
+// l, m = theta * coordinates2(S).  The turns w_L * ph are a double-float
+// product reduced to a fraction of a turn before the FP32 sincospi.
+__global__ void k_towers_combine(const float2 *__restrict__ stack, int S, double theta,
+                                 const double *__restrict__ layer_w,
+                                 const int32_t *__restrict__ chunk_first,
+                                 float2 *__restrict__ out, int32_t *status) {
+  const int c = blockIdx.y;
+  const int L0 = chunk_first[c], L1 = chunk_first[c + 1];
+  const int64_t cells = (int64_t)S * S;
+  int bad = 0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cells;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k / S), j = (int)(k - (int64_t)i * S);
+    const double l = __dmul_rn(theta, __ddiv_rn((double)(j - S / 2), (double)S));
+    const double m = __dmul_rn(theta, __ddiv_rn((double)(i - S / 2), (double)S));
+    const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
+    if (!(r2 < 1.0)) bad = 1;
+    const double ph = 1.0 - sqrt(1.0 - r2);
+    const float ph_h = (float)ph, ph_l = (float)(ph - (double)ph_h);
+    float ax = 0.f, ay = 0.f;
+    for (int L = L0; L < L1; ++L) {
+      const double w = layer_w[L];
+      const float wh = (float)w, wl = (float)(w - (double)wh);
+      const float hi = wh * ph_h;
+      const float lo = fmaf(wh, ph_h, -hi) + fmaf(wh, ph_l, wl * ph_h);
+      const float f = (hi - rintf(hi)) + lo;
+      float sn, cs;
+      sincospif(2.0f * f, &sn, &cs);
+      const float2 g = stack[(int64_t)L * cells + k];
+      ax += g.x * cs + g.y * sn;
+      ay += g.y * cs - g.x * sn;
+    }
+    out[(int64_t)c * cells + k] = make_float2(ax, ay);
+  }
+  if (bad && status) atomicAdd(&status[ST_RANGE], 1);
+}
+
+// grid[y0 + i, x0 + j] += sub[c, i, j] inside the grid (sub-grids overlap by
+// the margin, hence the atomics).
+__global__ void k_towers_add(const float2 *__restrict__ sub, int S, const int32_t *__restrict__ origin,
+                             int N, float2 *__restrict__ grid) {
+  const int c = blockIdx.y;
+  const int x0 = origin[2 * c], y0 = origin[2 * c + 1];
+  const int64_t cells = (int64_t)S * S;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cells;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k / S), j = (int)(k - (int64_t)i * S);
+    const int y = y0 + i, x = x0 + j;
+    if (y < 0 || y >= N || x < 0 || x >= N) continue;
+    const float2 v = sub[(int64_t)c * cells + k];
+    if (v.x != 0.f || v.y != 0.f) atomicAdd(&grid[(int64_t)y * N + x], v);
+  }
+}
+
+}  // namespace cg
+
+using namespace cg;
+
+extern "C" {
+
+int cg_tower_keys(const double *uvw, int64_t stride, int64_t n, double theta, int chunk,
+                  double wincrement, int32_t *key_out, double *rel_out, int32_t *d_minmax,
+                  int32_t *h_bounds, int32_t *d_status, cg_stream_t stream) {
+  CG_REQUIRE(n >= 1 && uvw && stride >= 3 && key_out && rel_out && d_minmax && h_bounds &&
+                 d_status,
+             "bad tower key arguments");
+  CG_REQUIRE(chunk >= 1 && theta > 0.0 && wincrement > 0.0, "bad chunk, theta or wincrement");
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  k_tower_mm_init<<<1, 32, 0, s>>>(d_minmax);
+  k_tower_bounds<<<blocks, 256, 0, s>>>(uvw, stride, n, theta, chunk, wincrement, d_minmax,
+                                        d_status);
+  CG_LAUNCH("tower bounds");
+  CG_CUDA(cudaMemcpyAsync(h_bounds, d_minmax, 6 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  CG_CUDA(cudaStreamSynchronize(s));
+  if (h_bounds[0] > h_bounds[1]) return CG_OK;  // every coordinate out of range
+  const int64_t nub = (int64_t)h_bounds[1] - h_bounds[0] + 1;
+  const int64_t nvb = (int64_t)h_bounds[3] - h_bounds[2] + 1;
+  const int64_t nwp = (int64_t)h_bounds[5] - h_bounds[4] + 1;
+  CG_REQUIRE(nub * nvb * nwp < ((int64_t)1 << 31), "too many (chunk, plane) keys");
+  k_tower_keys<<<blocks, 256, 0, s>>>(uvw, stride, n, theta, chunk, wincrement, h_bounds[0],
+                                      h_bounds[2], h_bounds[4], (int)nub, (int)nwp, key_out,
+                                      rel_out);
+  CG_LAUNCH("tower keys");
+  return CG_OK;
+}
+
+int cg_towers_combine(const void *stack_c64, int layers, int S, double theta,
+                      const double *layer_w, const int32_t *chunk_first, int nchunks,
+                      void *out_c64, int32_t *d_status, cg_stream_t stream) {
+  CG_REQUIRE(stack_c64 && layer_w && chunk_first && out_c64 && layers >= 1 && S >= 1 &&
+                 nchunks >= 1 && nchunks <= 65535,
+             "bad w-towers combine arguments");
+  const int64_t cells = (int64_t)S * S;
+  const unsigned bx = (unsigned)std::min<int64_t>((cells + 255) / 256, 64);
+  k_towers_combine<<<dim3(bx, nchunks), 256, 0, (cudaStream_t)stream>>>(
+      (const float2 *)stack_c64, S, theta, layer_w, chunk_first, (float2 *)out_c64, d_status);
+  CG_LAUNCH("w-towers combine");
+  return CG_OK;
+}
+
+int cg_towers_add(const void *sub_c64, int nchunks, int S, const int32_t *origin, int N,
+                  void *grid_c64, cg_stream_t stream) {
+  CG_REQUIRE(sub_c64 && origin && grid_c64 && S >= 1 && N >= 1 && nchunks >= 1 &&
+                 nchunks <= 65535,
+             "bad w-towers add arguments");
+  const int64_t cells = (int64_t)S * S;
+  const unsigned bx = (unsigned)std::min<int64_t>((cells + 255) / 256, 64);
+  k_towers_add<<<dim3(bx, nchunks), 256, 0, (cudaStream_t)stream>>>(
+      (const float2 *)sub_c64, S, origin, N, (float2 *)grid_c64);
+  CG_LAUNCH("w-towers add");
+  return CG_OK;
+}
+
+}  // extern "C"

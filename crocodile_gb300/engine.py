@@ -462,3 +462,42 @@ class CapturedStep:
 
     def replay(self):
         self.graph.replay()
+
+
+# --------------------------------------------------------------------------
+# w-towers (examples/grid/grid.c:482-710)
+
+def tower_keys(uvw, theta, chunk, wincrement, status):
+    """(key int32 [n], chunk/plane-relative uvw float64 [n, 3], (ubmin, ubmax, vbmin,
+    vbmax, wpmin, wpmax)) of cg_tower_keys."""
+    uvw = cuda_tensor(uvw, torch.float64)
+    n = uvw.shape[0]
+    key = torch.empty(n, dtype=torch.int32, device="cuda")
+    rel = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    dmm = torch.empty(6, dtype=torch.int32, device="cuda")
+    hb = (ctypes.c_int32 * 6)()
+    L.call("cg_tower_keys", _p(uvw), uvw.stride(0), n, float(theta), int(chunk),
+           float(wincrement), _p(key), _p(rel), _p(dmm), hb, _p(status.t), stream())
+    return key, rel, tuple(int(x) for x in hb)
+
+
+def towers_combine(stack, theta, layer_w, chunk_first, status):
+    """Per chunk, the sum of its layers' images / w_kernel_function(l, m, layer_w)."""
+    S = stack.shape[-1]
+    # keep the uploaded tables referenced until the launch is queued: a freed
+    # temporary's block is handed to the next allocation
+    lw = cuda_tensor(layer_w, torch.float64)
+    cf = cuda_tensor(chunk_first, torch.int32)
+    nchunks = int(cf.shape[0]) - 1
+    out = torch.empty((nchunks, S, S), dtype=CF, device="cuda")
+    L.call("cg_towers_combine", _p(stack), int(stack.shape[0]), S, float(theta), _p(lw),
+           _p(cf), nchunks, _p(out), _p(status.t), stream())
+    return out
+
+
+def towers_add(sub, origin, grid):
+    """grid += each chunk's sub-grid at its origin (x0, y0), inside the grid."""
+    org = cuda_tensor(origin, torch.int32)
+    L.call("cg_towers_add", _p(sub), int(sub.shape[0]), int(sub.shape[-1]), _p(org),
+           int(grid.shape[-1]), _p(grid), stream())
+    return grid

@@ -791,6 +791,57 @@ def w_stack_imaging(theta, lam, uvw, src, vis, kv, plane, precision=None, per_pl
     return _host(image, like=uvw)
 
 
+def w_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wincrement, wstep=2000,
+                     kernel_cache=None, kernel_fn=w_kernel, precision=None, **kwargs):
+    """w-towers imaging: w-stacking on sub-grids (examples/grid/grid.c:482-710,
+    examples/notebooks/wtowers.ipynb code cell 16).  Visibilities are binned into uv
+    chunks of ``subgrid_size - margin`` cells and w-planes of width ``wincrement``;
+    each (chunk, plane) is w-projected relative to the chunk centre and the plane's w
+    with the kernels of w_cache_imaging (``wstep``, ``kernel_cache``/``kernel_fn``,
+    ``**kwargs``) into a ``subgrid_size``^2 sub-grid, the planes of a chunk are moved to
+    w = 0 in image space (division by w_kernel_function(l, m, w_plane)) and summed, and
+    the chunk's sub-grid is added into the grid.  Returns the grid, the quantity
+    w_cache_imaging returns.  All sub-grids grid in one launch and transform in batched
+    FFTs.  FP32 only; needs margin >= the kernel support."""
+    if _prec(precision) != "fp32":
+        raise ValueError("w_towers_imaging runs the FP32 tiled path only")
+    N = _grid_size(theta, lam)
+    s, C = int(subgrid_size), int(subgrid_size) - int(margin)
+    if C < 1 or margin < 0:
+        raise ValueError("need 0 <= margin < subgrid_size")
+    n = _nrows(uvw)
+    grid = torch.zeros((N, N), dtype=E.CF, device="cuda")
+    if n == 0:
+        return _host(grid, like=uvw)
+    uvw_t = E.cuda_tensor(uvw, torch.float64)
+    vis_t = E.cuda_tensor(vis, E.CF)
+    st = E.Status()
+    key, rel, (ubmin, ubmax, vbmin, vbmax, wpmin, wpmax) = E.tower_keys(uvw_t, theta, C,
+                                                                        wincrement, st)
+    st.check()
+    nub, nvb, nwp = ubmax - ubmin + 1, vbmax - vbmin + 1, wpmax - wpmin + 1
+    row, used = E.compact_keys(key, nub * nvb * nwp, st)
+    used = used.cpu().numpy().astype(numpy.int64)
+    plane = used % nwp + wpmin
+    chunk, first = numpy.unique(used // nwp, return_index=True)
+    chunk_first = numpy.append(first, len(used)).astype(numpy.int32)
+    ub, vb = chunk % nub + ubmin, chunk // nub + vbmin
+    xmid, ymid = (C * ub + C * (ub + 1)) // 2, (C * vb + C * (vb + 1)) // 2
+    origin = numpy.column_stack([N // 2 + xmid - s // 2, N // 2 + ymid - s // 2])
+    ktab, kidx = _spec_w_cache(theta, rel, None, src, wstep, kernel_cache, kernel_fn, kwargs,
+                               E.CF)
+    stack = torch.zeros((len(used), s, s), dtype=E.CF, device="cuda")
+    plan = E.Plan(rel, s / theta, (s, s), ktab, kidx, status=st, layers=(len(used), row))
+    plan.grid(ktab, vis_t, stack)
+    E.fft_(stack, True)
+    sub = E.towers_combine(stack, theta, plane * float(wincrement), chunk_first, st)
+    del stack
+    E.fft_(sub, False)
+    E.towers_add(sub, origin.astype(numpy.int32), grid)
+    st.check()
+    return _host(grid, like=uvw)
+
+
 def sample_image(image, x, y):
     """Bilinear sample relative to the image middle (synthesis.py:736-755)."""
     x = x + image.shape[0] / 2

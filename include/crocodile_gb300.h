@@ -320,6 +320,33 @@ int cg_wstack_combine(const void *planes_c64, int layers, int N, double theta,
                       const double *mean_w, const int32_t *counts,
                       void *image_c64, int32_t *d_status, cg_stream_t stream);
 
+/* w-towers: w-stacking on sub-grids (examples/grid/grid.c:482-710,
+ * examples/notebooks/wtowers.ipynb code cell 16).  Visibility i falls into
+ * the uv chunk ub = floor(u*theta / chunk), vb = floor(v*theta / chunk)
+ * (chunk = sub-grid size - margin) and the w-plane wp = rint(w / wincrement);
+ * the chunk's sub-grid is centred xmid = (chunk*ub + chunk*(ub+1)) // 2 cells
+ * from the grid centre (likewise ymid).
+ * cg_tower_keys writes key_out[i] = ((vb - vbmin)*nub + (ub - ubmin))*nwp +
+ * (wp - wpmin) and rel_out[i] = (u - xmid/theta, v - ymid/theta,
+ * w - wp*wincrement) (IEEE double, as numpy); h_bounds (host) = {ubmin,
+ * ubmax, vbmin, vbmax, wpmin, wpmax}; d_minmax is 6 int32 of device scratch;
+ * synchronises the stream.  The (chunk, plane) layers are then gridded with a
+ * layered plan on rel_out (lam = sub-grid size / theta, residual-w kernels)
+ * and inverse-transformed (cg_fft).
+ * cg_towers_combine: out[c] = sum over layers L in [chunk_first[c],
+ * chunk_first[c+1]) of stack[L] / w_kernel_function(l, m, layer_w[L]) on the
+ * sub-grid's l, m (the Fresnel transfer between w-planes, grid.c:598-622).
+ * cg_towers_add: after a forward cg_fft of out, grid[origin[2c+1] + i,
+ * origin[2c] + j] += out[c, i, j] inside the N x N grid (grid.c:640-656). */
+int cg_tower_keys(const double *uvw, int64_t stride, int64_t n, double theta, int chunk,
+                  double wincrement, int32_t *key_out, double *rel_out, int32_t *d_minmax,
+                  int32_t *h_bounds, int32_t *d_status, cg_stream_t stream);
+int cg_towers_combine(const void *stack_c64, int layers, int S, double theta,
+                      const double *layer_w, const int32_t *chunk_first, int nchunks,
+                      void *out_c64, int32_t *d_status, cg_stream_t stream);
+int cg_towers_add(const void *sub_c64, int nchunks, int S, const int32_t *origin, int N,
+                  void *grid_c64, cg_stream_t stream);
+
 /* ------------------------------------------------------------------ */
 /* Kernel generation (FP64 arithmetic; outputs c64 or c128). */
 

@@ -537,6 +537,67 @@ def w_stack_imaging(theta, lam, uvw, src, vis, kv, plane):
 
 
 # --------------------------------------------------------------------------
+# w-towers: w-stacking on sub-grids (examples/grid/grid.c:482-710,
+# examples/notebooks/wtowers.ipynb code cell 16), in crocodile's Python
+# conventions.  Neither reference form runs here (the C prototype needs
+# FFTW/HDF5 headers; the notebook grids nearest-cell with no last-mile
+# kernel), so this restatement defines the algorithm the GPU path matches:
+#
+#   chunk (ub, vb) = floor(u*theta / C), floor(v*theta / C)   C = subgrid - margin
+#   plane wp = around(w / wincrement)                            (notebook cell 16)
+#   chunk centre xmid = (C*ub + C*(ub+1)) // 2 cells, u_mid = xmid / theta
+#   per (chunk, plane): w_cache_imaging of the visibilities relative to
+#       (u_mid, v_mid, wp*wincrement) into an s x s sub-grid (lam_sub = s / theta),
+#       i.e. the last mile w-projected with w-kernels of the residual w (grid.c:277-305)
+#   per chunk: image = sum over planes of ifft(sub-grid) / w_kernel_function(l, m, wp*wincrement)
+#       on the sub-grid's l, m (the Fresnel transfer of grid.c:418-480, 598-622 in closed form)
+#   grid[N//2 + ymid - s//2 + i, N//2 + xmid - s//2 + j] += fft(image)[i, j], cells
+#       outside the grid dropped (grid.c:640-656)
+#
+# With one plane and every |w| < wincrement / 2 this is w_cache_imaging itself
+# (fft(ifft(x)) = x), which pins it to the reference (tests/test_oracle_golden.py).
+
+def tower_bins(theta, uvw, subgrid_size, margin, wincrement):
+    """(ub, vb, wp, xmid, ymid, uvw_rel) of every visibility."""
+    C = subgrid_size - margin
+    ub = numpy.floor(uvw[:, 0] * theta / C).astype(numpy.int64)
+    vb = numpy.floor(uvw[:, 1] * theta / C).astype(numpy.int64)
+    wp = numpy.around(uvw[:, 2] / wincrement)
+    xmid = (C * ub + C * (ub + 1)) // 2
+    ymid = (C * vb + C * (vb + 1)) // 2
+    rel = numpy.column_stack([uvw[:, 0] - xmid / theta, uvw[:, 1] - ymid / theta,
+                              uvw[:, 2] - wp * wincrement])
+    return ub, vb, wp.astype(numpy.int64), xmid, ymid, rel
+
+
+def w_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wincrement, wstep,
+                     kernel_fn=w_kernel, **kwargs):
+    """w-towers imaging: returns the N x N grid (the same quantity as w_cache_imaging)."""
+    N = int(round(theta * lam))
+    s = subgrid_size
+    guv = numpy.zeros((N, N), dtype=complex)
+    src = numpy.zeros((len(uvw), 0)) if src is None else src
+    ub, vb, wp, xmid, ymid, rel = tower_bins(theta, uvw, s, margin, wincrement)
+    l, m = theta * coordinates2(s)
+    chunks = sorted(set(zip(vb.tolist(), ub.tolist())))
+    for cv, cu in chunks:
+        in_chunk = (vb == cv) & (ub == cu)
+        image = numpy.zeros((s, s), dtype=complex)
+        for p in numpy.unique(wp[in_chunk]):
+            sel = in_chunk & (wp == p)
+            sub = w_cache_imaging(theta, s / theta, rel[sel], src[sel], vis[sel], wstep=wstep,
+                                  kernel_fn=kernel_fn, **kwargs)
+            image += ifft(sub) / w_kernel_function(l, m, p * wincrement)
+        sub = fft(image)
+        i = numpy.nonzero(in_chunk)[0][0]
+        y0, x0 = N // 2 + ymid[i] - s // 2, N // 2 + xmid[i] - s // 2
+        ya, yb, xa, xb = max(y0, 0), min(y0 + s, N), max(x0, 0), min(x0 + s, N)
+        if ya < yb and xa < xb:
+            guv[ya:yb, xa:xb] += sub[ya - y0:yb - y0, xa - x0:xb - x0]
+    return guv
+
+
+# --------------------------------------------------------------------------
 # point-source visibilities (crocodile/simulate.py:210-230)
 
 def simulate_point(dist_uvw, l, m):

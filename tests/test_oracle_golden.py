@@ -140,3 +140,33 @@ def test_aw_kernel_fft_equals_aw_kernel_fn(golden):
     ref = O.aw_kernel_fn(lambda th, a: ak[a], lambda th, w: wk)(0.1, 25.0, 0, 1)
     assert_allclose(O.aw_kernel_fft(ak[0], ak[1], wk), ref, rtol=1e-12, atol=1e-12)
     assert_allclose(ref, golden["aw_k01"], rtol=1e-13)
+
+
+def test_w_towers_single_plane_is_the_reference_w_cache_grid(golden):
+    """w-towers with one w-plane (every |w| < wincrement / 2) is w-projection itself:
+    the oracle's restatement reproduces the reference's own w_cache_imaging grid
+    (stored by tests/golden/make_golden.py) up to summation order, for several
+    sub-grid sizes and margins."""
+    uvw, vis = golden["wc_uvw"], golden["wc_vis"]
+    lam, theta = float(golden["wc_lam"]), float(golden["wc_theta"])
+    ref = golden["wc_grid"]
+    winc = 4 * float(numpy.abs(uvw[:, 2]).max()) + 1.0
+    for s, margin in ((32, 8), (48, 16), (40, 10)):
+        g = O.w_towers_imaging(theta, lam, uvw, None, vis, s, margin, winc, 10.0,
+                               NpixFF=16, NpixKern=7, Qpx=4)
+        assert numpy.linalg.norm(g - ref) <= 1e-12 * numpy.linalg.norm(ref)
+
+
+def test_w_towers_bins():
+    """Chunk, plane and relative coordinates of tower_bins on hand-picked values."""
+    theta, C, winc = 0.1, 48, 60.0
+    uvw = numpy.array([[0.0, 0.0, 0.0], [479.9, -480.0, 29.9], [-0.001, 960.0, -30.0],
+                       [4800.0, -4799.5, 90.0]])
+    ub, vb, wp, xmid, ymid, rel = O.tower_bins(theta, uvw, 64, 16, winc)
+    assert_array_equal(ub, [0, 0, -1, 10])
+    assert_array_equal(vb, [0, -1, 2, -10])
+    assert_array_equal(wp, [0, 0, -0, 2])     # around: half to even (-0.5 -> -0, 1.5 -> 2)
+    assert_array_equal(xmid, [24, 24, -24, 504])
+    assert_array_equal(ymid, [24, -24, 120, -456])
+    assert_allclose(rel[:, 0], uvw[:, 0] - xmid / theta)
+    assert_allclose(rel[:, 2], uvw[:, 2] - wp * winc)
