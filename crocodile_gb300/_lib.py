@@ -35,7 +35,7 @@ CG_LAYOUT_LANE = 3
 
 class PlanOpts(ctypes.Structure):
     _fields_ = [("layers", c_int), ("layer", c_void_p), ("wstep", c_double), ("kmin", c_int),
-                ("group", c_void_p), ("ngroups", c_int)]
+                ("group", c_void_p), ("ngroups", c_int), ("tile", c_int)]
 
 
 class KernelDesc(ctypes.Structure):
@@ -81,6 +81,7 @@ SIGNATURES = {
     "cg_plan_info": (c_int, [P, P]),
     "cg_plan_export": (c_int, [P, P, P, P, P]),
     "cg_grid": (c_int, [P, P, P, P, P]),
+    "cg_grid_sparse": (c_int, [P, P, P, P, P]),
     "cg_grid_weighted": (c_int, [P, P, P, P, P, P]),
     "cg_degrid": (c_int, [P, P, P, P, P]),
     "cg_degrid_grid": (c_int, [P, P, P, P, c_int, P, P, P]),
@@ -94,6 +95,7 @@ SIGNATURES = {
     "cg_mirror_uvw": (c_int, [P, c_int64, c_int64, P, c_int, P]),
     "cg_make_hermitian": (c_int, [P, c_int, c_int, c_int, P]),
     "cg_fft": (c_int, [P, c_int, c_int, c_int, c_int, c_int, P, P]),
+    "cg_fft_raw": (c_int, [P, c_int, c_int, c_int, c_int, c_int, P]),
     "cg_image_from_grid": (c_int, [P, c_int, c_int, P, P, P]),
     "cg_scale_image": (c_int, [P, c_int64, P, P]),
     "cg_kernel_oversample_workspace_bytes": (c_size_t, [c_int, c_int, c_int, c_int]),

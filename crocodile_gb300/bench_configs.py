@@ -215,8 +215,50 @@ def measure_aw(steps=5, nvis=None, fp64=True):
             "rel_err_grid": _rel(g, g64), "rel_err_degrid": _rel(out["v"], out["v64"])}
 
 
+def measure_wtowers(steps=5, variants=True):
+    """w-towers (examples/grid/grid.c:482-710) on the w-projection workload (4096^2,
+    2M visibilities, |w| <= 500): 256^2 sub-grids with a 16-cell margin, w-planes of
+    100 wavelengths, last-mile w-kernels S 8 Q 8 of the residual w (|w| <= 50), the
+    sparse gridder (with variants over gridder, tile and plane width).  Timed
+    end to end (binning, key compaction, plan, one gridder launch over every
+    sub-grid, batched FFTs, Fresnel combine, sub-grid add), next to w-projection
+    of the same visibilities with S 15 kernels over the full w range."""
+    from . import synthesis
+    w = configs.wproj()
+    n, N = len(w.uvw), w.N
+    s, margin, winc = 256, 16, 100.0
+    kw = dict(NpixFF=w.params["NpixFF"], NpixKern=8, Qpx=8)
+    uvw = E.cuda_tensor(w.uvw, torch.float64)
+    vis = E.cuda_tensor(w.vis, E.CF)
+    ms = _time(lambda: synthesis.w_towers_imaging(w.theta, w.lam, uvw, None, vis, s, margin,
+                                                  winc, 10.0, tile=32, gridder="sparse", **kw),
+               steps)
+    var = {}
+    for gridder, tile in ((("sparse", 32), ("tiled", 32), ("tiled", 64)) if variants else ()):
+        for wi in (50.0, 100.0):
+            var["%s_tile%d_winc%d" % (gridder, tile, wi)] = _time(
+                lambda: synthesis.w_towers_imaging(w.theta, w.lam, uvw, None, vis, s, margin,
+                                                   wi, 10.0, tile=tile, gridder=gridder, **kw),
+                steps)
+    st = E.Status()
+    key, _, b = E.tower_keys(uvw, w.theta, s - margin, winc, st)
+    row, used = E.compact_keys(key, (b[1] - b[0] + 1) * (b[3] - b[2] + 1) * (b[5] - b[4] + 1),
+                               st)
+    layers = int(used.shape[0])
+    chunks = len(numpy.unique(used.cpu().numpy() // (b[5] - b[4] + 1)))
+    kwp = dict(NpixFF=w.params["NpixFF"], NpixKern=w.S, Qpx=w.Q)
+    ms_wp = _time(lambda: synthesis.w_cache_imaging(w.theta, w.lam, uvw, None, vis,
+                                                    wstep=w.params["wstep"], **kwp), steps)
+    return {"workload": "w-towers 4096^2 2M vis, 256^2 sub-grids margin 16, w-planes of 100, "
+                        "S 8 Q 8 last mile, sparse gridder", "n_vis": n, "ms": ms, "mvis_s": n / ms / 1e3,
+            "chunks": chunks, "layers": layers, "ms_by_gridder_tile_and_plane_width": var,
+            "w_projection_s15_ms": ms_wp, "w_projection_s15_mvis_s": n / ms_wp / 1e3,
+            "note": "grid only (imaging); parity with the oracle's w-towers <= 1e-5 in "
+                    "tests/test_gpu_towers.py"}
+
+
 MEASURES = {"plain": measure_plain, "wproj": measure_wproj, "diff": measure_diff,
-            "wstack": measure_wstack, "aw": measure_aw}
+            "wstack": measure_wstack, "aw": measure_aw, "wtowers": measure_wtowers}
 
 
 def run(only=None, steps=None):
@@ -235,9 +277,14 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default="")
     ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--no-variants", action="store_true",
+                    help="w-towers only: time the measured shape alone (profiling runs)")
     ap.add_argument("--aw-nvis", type=int, default=0,
                     help="AW only: the first N visibilities, FP32 only (profiling runs)")
     a = ap.parse_args()
+    if a.no_variants:
+        print(json.dumps(measure_wtowers(a.steps or 5, variants=False)))
+        return
     if a.aw_nvis:
         print(json.dumps(measure_aw(a.steps or 2, nvis=a.aw_nvis, fp64=False)))
         return

@@ -199,6 +199,7 @@ struct cg_plan {
   cg_kernel_desc kd;
   int H, W;
   int64_t n;
+  int tile_req; // requested tile edge (0: tuning / automatic)
   int T;        // tile edge in cells (tiled mode)
   int ntx, nty; // tiles per row / column
   int win;      // window edge = T + S - 1

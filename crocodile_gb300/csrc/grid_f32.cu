@@ -510,6 +510,62 @@ static void *grid_kernel_for(int R) {
   }
 }
 
+// Sparse gridder: for stacks of grids holding few visibilities per tile (the
+// sub-grids of w-towers), where staging and flushing a window per work item
+// costs more than the visibilities' own taps.  No shared memory: each warp
+// takes work items in turn, loads 32 records at a time (one per lane) and, for
+// each visibility, lane l adds taps l + 32 i straight into the grid with
+// float2 atomics.  Full occupancy hides the latency of the small items.
+template <bool SEP, int MAXT>
+__global__ void __launch_bounds__(256) k_grid_sparse(TiledArgs A, const float2 *__restrict__ ktab,
+                                                     const float2 *__restrict__ vis,
+                                                     float2 *__restrict__ grid) {
+  if (status_failed(A.status)) return;
+  const int S = A.S, SS = S * S;
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const long long KSZ = (long long)A.Q * A.Q * SS;
+  int tdy[MAXT], tdx[MAXT];
+#pragma unroll
+  for (int i = 0; i < MAXT; ++i) {
+    const int t = lane + 32 * i;
+    tdy[i] = t / S;
+    tdx[i] = t - tdy[i] * S;
+  }
+  const int nitems = *A.nitems;
+  for (int64_t it = gw; it < nitems; it += nw) {
+    const WorkItem w = A.items[it];
+    const TileOrigin org = tile_origin(A, w.tile);
+    float2 *g0 = grid + org.layer_off;
+    for (int b = 0; b < w.count; b += 32) {
+      const int nb = min(32, w.count - b);
+      VisRec r = {0, 0, 0, 0};
+      float2 v = make_float2(0.f, 0.f);
+      if (lane < nb) {
+        r = A.recs[w.start + b + lane];
+        v = vis[A.perm[w.start + b + lane]];
+      }
+      for (int q = 0; q < nb; ++q) {
+        const int x0 = __shfl_sync(0xffffffffu, r.x0, q), y0 = __shfl_sync(0xffffffffu, r.y0, q);
+        const int k0 = __shfl_sync(0xffffffffu, r.k0, q), k1 = __shfl_sync(0xffffffffu, r.k1, q);
+        const float2 u = make_float2(__shfl_sync(0xffffffffu, v.x, q),
+                                     __shfl_sync(0xffffffffu, v.y, q));
+        const float2 *kk = SEP ? ktab + (long long)k0 * S : ktab + (long long)k0 * KSZ + (long long)k1 * SS;
+        const float2 *kx = ktab + (long long)k1 * S;
+        float2 *gp = g0 + (size_t)y0 * A.W + x0;
+#pragma unroll
+        for (int i = 0; i < MAXT; ++i) {
+          if (lane + 32 * i < SS) {
+            const float2 k = SEP ? cmul(__ldg(&kk[tdy[i]]), __ldg(&kx[tdx[i]])) : __ldg(&kk[lane + 32 * i]);
+            atomicAdd(&gp[(size_t)tdy[i] * A.W + tdx[i]], cmul(k, u));
+          }
+        }
+      }
+    }
+  }
+}
+
 template <bool SEP>
 static void *grid_warp_kernel_for(int maxt) {
   switch (maxt) {
@@ -609,6 +665,29 @@ int cg_grid(const cg_plan *p, const void *ktab, const void *vis, void *grid,
 int cg_grid_weighted(const cg_plan *p, const void *ktab, const void *vis,
                      const float *weight, void *grid, cg_stream_t stream) {
   return grid_launch(p, ktab, vis, weight, vis ? 1 : 2, grid, (cudaStream_t)stream);
+}
+
+int cg_grid_sparse(const cg_plan *p, const void *ktab, const void *vis, void *grid,
+                   cg_stream_t stream) {
+  CG_REQUIRE(p && p->mode == CG_PLAN_TILED, "cg_grid_sparse needs a CG_PLAN_TILED plan");
+  if (p->n == 0) return CG_OK;
+  CG_REQUIRE(ktab && vis && grid, "NULL argument");
+  const int SS = p->kd.S * p->kd.S;
+  const int need = (SS + 31) / 32;
+  void (*fn)(TiledArgs, const float2 *, const float2 *, float2 *) = nullptr;
+#define PICK(M)                                                                \
+  if (!fn && need <= M) fn = p->kd.sep ? k_grid_sparse<true, M> : k_grid_sparse<false, M>;
+  PICK(1) PICK(2) PICK(4) PICK(8) PICK(16) PICK(32)
+#undef PICK
+  CG_REQUIRE(fn, "support too large for the sparse gridder");
+  int per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0));
+  const int64_t blocks = std::max<int64_t>(
+      1, std::min<int64_t>((int64_t)std::max(per_sm, 1) * num_sms(), (p->max_items + 7) / 8));
+  fn<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(tiled_args(p), (const float2 *)ktab,
+                                                         (const float2 *)vis, (float2 *)grid);
+  CG_LAUNCH("sparse grid");
+  return CG_OK;
 }
 
 int cg_degrid(const cg_plan *p, const void *ktab, const void *grid, void *out,

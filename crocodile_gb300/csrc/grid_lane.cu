@@ -11,7 +11,8 @@
 // distinct cells, so each lane adds its products with a plain read-modify-write
 // and the warp synchronises once per visibility: no shared-memory atomics.
 // Each item's window is flushed to HBM with float2 atomics and left zeroed for
-// the next one.
+// the next one; an item with fewer taps than half its window's cells adds its
+// taps straight into the grid with float2 atomics instead.
 //
 // Non-separable tables whose S x S slices are a multiple of 16 bytes stream
 // every visibility's slice into a per-warp ring of LANE_DEPTH shared-memory
@@ -149,6 +150,10 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
     const WorkItem w = A.items[it];
     const TileOrigin org = tile_origin(A, w.tile);
     const int n = w.count;
+    // An item whose taps are fewer than half its window's cells skips the
+    // window: staging and flushing the window would cost more than per-tap
+    // global atomics (sparse tiles, e.g. the many small sub-grids of w-towers).
+    const bool direct = (int64_t)n * SS * 2 < (int64_t)win * win;
     const float2 *gin = FUSED ? P.grid_in + org.layer_off + (size_t)org.wy0 * A.W + org.wx0
                               : nullptr;
 
@@ -268,15 +273,24 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
           u.y -= sum.y;
         }
       }
-      // distinct taps of one visibility are distinct cells: plain read-modify-write
+      if (direct) {
+        // sparse item: the taps go straight to the grid (float2 atomics)
+        float2 *gp = P.grid + org.layer_off + (size_t)(org.wy0 + (m.x >> 16)) * A.W +
+                     org.wx0 + (m.x & 0xffff);
 #pragma unroll
-      for (int i = 0; i < MAXT; ++i)
-        if (own[i]) {
-          float2 *c = &wbuf[base + soff[i]];
-          float2 o = *c;
-          cfma(o, kc[i], u);
-          *c = o;
-        }
+        for (int i = 0; i < MAXT; ++i)
+          if (own[i]) atomicAdd(&gp[(size_t)tdy[i] * A.W + tdx[i]], cmul(kc[i], u));
+      } else {
+        // distinct taps of one visibility are distinct cells: plain read-modify-write
+#pragma unroll
+        for (int i = 0; i < MAXT; ++i)
+          if (own[i]) {
+            float2 *c = &wbuf[base + soff[i]];
+            float2 o = *c;
+            cfma(o, kc[i], u);
+            *c = o;
+          }
+      }
       __syncwarp();  // this visibility's updates (and stage reads) before the next one
       return true;
     };
@@ -330,7 +344,7 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
       __syncwarp();
       return;
     }
-    for (int row = 0; row < win; ++row) {
+    for (int row = 0; row < (direct ? 0 : win); ++row) {
       const int gy = org.wy0 + row;
       for (int q = lane; q < win; q += 32) {
         const int c = row * pitch + q;

@@ -331,6 +331,22 @@ int cg_fft(void *data, int batch, int H, int W, int is_c64, int inverse, void *w
                      (cudaStream_t)stream);
 }
 
+int cg_fft_raw(void *data, int batch, int H, int W, int is_c64, int inverse,
+               cg_stream_t stream) {
+  CG_REQUIRE(data && batch >= 1 && H >= 1 && W >= 1, "bad fft arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  cufftHandle plan;
+  int rc = fft_plan(batch, H, W, is_c64 ? CUFFT_C2C : CUFFT_Z2Z, &plan);
+  if (rc) return rc;
+  if (cufftSetStream(plan, s) != CUFFT_SUCCESS)
+    return set_error(CG_ERR_CUDA, "cufftSetStream failed");
+  const int dir = inverse ? CUFFT_INVERSE : CUFFT_FORWARD;
+  const cufftResult r =
+      is_c64 ? cufftExecC2C(plan, (cufftComplex *)data, (cufftComplex *)data, dir)
+             : cufftExecZ2Z(plan, (cufftDoubleComplex *)data, (cufftDoubleComplex *)data, dir);
+  return r == CUFFT_SUCCESS ? CG_OK : set_error(CG_ERR_CUDA, "cufftExec failed: %d", (int)r);
+}
+
 int cg_image_from_grid(void *grid, int H, int W, float *image, float *max_out,
                        cg_stream_t stream) {
   CG_REQUIRE(grid && image, "NULL argument");

@@ -392,9 +392,10 @@ struct Layout {
   size_t rec_tmp, key, rank, recs, perm, counts, offsets, scan, items, ctr, total;
 };
 
-static int tile_edge(const cg_kernel_desc &kd) {
+static int tile_edge(const cg_kernel_desc &kd, int req) {
   const cg_tuning t = tuning();
   const int S = kd.S;
+  if (req > 0) return std::max(4, std::min(64, req & ~3));
   if (t.tile > 0) return std::max(4, std::min(64, t.tile & ~3));
   if (layout_for(kd) == CG_LAYOUT_LANE) return 16;  // per-warp windows stay small
   if (S <= 8) return 32;
@@ -404,7 +405,7 @@ static int tile_edge(const cg_kernel_desc &kd) {
 
 static void plan_geometry(cg_plan &p) {
   if (p.mode == CG_PLAN_TILED) {
-    p.T = tile_edge(p.kd);
+    p.T = tile_edge(p.kd, p.tile_req);
     p.ntx = (p.W + p.T - 1) / p.T;
     p.nty = (p.H + p.T - 1) / p.T;
     p.tpl = p.ntx * p.nty;
@@ -483,7 +484,7 @@ int plan_build_into(cg_plan *p, int mode, const cg_kernel_desc *kd, int H, int W
                     const double *uvw, int64_t stride, double lam, const int32_t *kidx,
                     double wstep, int kmin, int layers, const int32_t *layer,
                     const int32_t *group, int ngroups, int64_t n, void *workspace,
-                    size_t workspace_bytes, int32_t *d_status, cudaStream_t s) {
+                    size_t workspace_bytes, int32_t *d_status, cudaStream_t s, int tile_req = 0) {
   int rc = check_desc(kd, H, W);
   CG_REQUIRE(!group || (mode == CG_PLAN_GROUPS && ngroups >= 1),
              "launch groups need a CG_PLAN_GROUPS plan and ngroups >= 1");
@@ -505,6 +506,7 @@ int plan_build_into(cg_plan *p, int mode, const cg_kernel_desc *kd, int H, int W
   p->n = n;
   p->layers = layers;
   p->gper = group ? ngroups : kd->G;
+  p->tile_req = tile_req;
   plan_geometry(*p);
   CG_REQUIRE((int64_t)p->nbuckets < (int64_t)INT32_MAX / 2, "too many tiles");
   const Layout L = layout_of(*p);
@@ -589,13 +591,13 @@ static int plan_create_heap(cg_plan **out, int mode, const cg_kernel_desc *kd, i
                             const double *uvw, int64_t stride, double lam, const int32_t *kidx,
                             double wstep, int kmin, int layers, const int32_t *layer,
                             const int32_t *group, int ngroups, int64_t n, void *workspace,
-                            size_t workspace_bytes, int32_t *d_status, cudaStream_t s) {
+                            size_t workspace_bytes, int32_t *d_status, cudaStream_t s, int tile_req = 0) {
   CG_REQUIRE(out, "plan output pointer is NULL");
   *out = nullptr;
   cg_plan *p = new (std::nothrow) cg_plan;
   CG_REQUIRE(p, "out of host memory");
   int rc = plan_build_into(p, mode, kd, H, W, uvw, stride, lam, kidx, wstep, kmin, layers, layer,
-                           group, ngroups, n, workspace, workspace_bytes, d_status, s);
+                           group, ngroups, n, workspace, workspace_bytes, d_status, s, tile_req);
   if (rc) {
     delete p;
     return rc;
@@ -665,6 +667,7 @@ static void opts_or_default(const cg_plan_opts *o, cg_plan_opts &r) {
   r.kmin = 0;
   r.group = nullptr;
   r.ngroups = 0;
+  r.tile = 0;
   if (o) r = *o;
   if (r.layers < 1) r.layers = 1;
 }
@@ -683,6 +686,7 @@ size_t cg_plan_workspace_bytes_ex(int mode, int64_t n, int H, int W, const cg_ke
   p.n = n;
   p.layers = o.layers;
   p.gper = o.group ? o.ngroups : kd->G;
+  p.tile_req = o.tile;
   plan_geometry(p);
   return layout_of(p).total;
 }
@@ -695,7 +699,7 @@ int cg_plan_create_ex(cg_plan **out, int mode, const cg_kernel_desc *kd, int H, 
   opts_or_default(opts, o);
   return plan_create_heap(out, mode, kd, H, W, uvw, stride, lam, kidx, o.wstep, o.kmin, o.layers,
                           o.layer, o.group, o.ngroups, n, workspace, workspace_bytes, d_status,
-                          (cudaStream_t)stream);
+                          (cudaStream_t)stream, o.tile);
 }
 
 int cg_plan_create_wbins(cg_plan **out, int mode, const cg_kernel_desc *kd, int H, int W,

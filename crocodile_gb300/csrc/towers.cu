@@ -96,58 +96,100 @@ __global__ void k_tower_keys(const double *__restrict__ uvw, int64_t stride, int
   rel[3 * i + 2] = t.rw;
 }
 
-// out[c, i, j] = sum over the layers L of chunk c of stack[L, i, j] /
-// exp(2 pi i w_L ph(i, j)), ph = 1 - sqrt(1 - l^2 - m^2) on the sub-grid's
-// l, m = theta * coordinates2(S).  The turns w_L * ph are a double-float
-// product reduced to a fraction of a turn before the FP32 sincospi.
+// out[c] = sum over the layers L of chunk c of image_L / exp(2 pi i w_L ph),
+// ph = 1 - sqrt(1 - l^2 - m^2) on the sub-grid's l, m = theta * coordinates2(S).
+// The layers arrive as unshifted, unnormalised inverse transforms F_L of the
+// sub-grids, and the centred image is image_L[k] = (-1)^(kx+ky) F_L[k + S/2] /
+// S^2 (indices mod S, S even); out is written rolled by S/2 (ifftshift), so an
+// unshifted forward transform of it is the centred fft up to the final roll,
+// which cg_towers_add applies.  The turns w_L * ph are a double-float product
+// reduced to a fraction of a turn before the FP32 sincospi.
+static constexpr int TOWER_CHUNKS_PER_BLOCK = 8;  // chunks sharing one cell's FP64 phase
+static constexpr int TOWER_SMEM_LAYERS = 2048;    // layers whose w split a block caches
+
+// w as an FP32 hi + lo pair (hi = w rounded, lo = the rest)
+__device__ __forceinline__ float2 split_w(double w) {
+  const float hi = (float)w;
+  return make_float2(hi, (float)(w - (double)hi));
+}
+
 __global__ void k_towers_combine(const float2 *__restrict__ stack, int S, double theta,
                                  const double *__restrict__ layer_w,
-                                 const int32_t *__restrict__ chunk_first,
+                                 const int32_t *__restrict__ chunk_first, int nchunks,
                                  float2 *__restrict__ out, int32_t *status) {
-  const int c = blockIdx.y;
-  const int L0 = chunk_first[c], L1 = chunk_first[c + 1];
+  extern __shared__ float2 s_w[];  // the block's layers' w, split once (FP64 is slow here)
+  const int c0 = blockIdx.y * TOWER_CHUNKS_PER_BLOCK;
+  const int c1 = min(nchunks, c0 + TOWER_CHUNKS_PER_BLOCK);
+  const int Lb0 = chunk_first[c0], Lb1 = chunk_first[c1];
+  const bool cached = Lb1 - Lb0 <= TOWER_SMEM_LAYERS;
+  if (cached)
+    for (int L = Lb0 + (int)threadIdx.x; L < Lb1; L += blockDim.x) s_w[L - Lb0] = split_w(layer_w[L]);
+  __syncthreads();
   const int64_t cells = (int64_t)S * S;
+  const int half = S / 2;
+  const float scale = 1.0f / (float)cells;
   int bad = 0;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cells;
        k += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(k / S), j = (int)(k - (int64_t)i * S);
-    const double l = __dmul_rn(theta, __ddiv_rn((double)(j - S / 2), (double)S));
-    const double m = __dmul_rn(theta, __ddiv_rn((double)(i - S / 2), (double)S));
+    // the cell's phase, once for every chunk of the block (FP64 is slow here)
+    const double l = __dmul_rn(theta, __ddiv_rn((double)(j - half), (double)S));
+    const double m = __dmul_rn(theta, __ddiv_rn((double)(i - half), (double)S));
     const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
     if (!(r2 < 1.0)) bad = 1;
     const double ph = 1.0 - sqrt(1.0 - r2);
     const float ph_h = (float)ph, ph_l = (float)(ph - (double)ph_h);
-    float ax = 0.f, ay = 0.f;
-    for (int L = L0; L < L1; ++L) {
-      const double w = layer_w[L];
-      const float wh = (float)w, wl = (float)(w - (double)wh);
-      const float hi = wh * ph_h;
-      const float lo = fmaf(wh, ph_h, -hi) + fmaf(wh, ph_l, wl * ph_h);
-      const float f = (hi - rintf(hi)) + lo;
-      float sn, cs;
-      sincospif(2.0f * f, &sn, &cs);
-      const float2 g = stack[(int64_t)L * cells + k];
-      ax += g.x * cs + g.y * sn;
-      ay += g.y * cs - g.x * sn;
+    const int ir = i + half >= S ? i + half - S : i + half;
+    const int jr = j + half >= S ? j + half - S : j + half;
+    const int64_t kr = (int64_t)ir * S + jr;  // rolled index, read and write
+    const float sg = ((i + j) & 1) ? -scale : scale;
+    for (int c = c0; c < c1; ++c) {
+      const int L0 = chunk_first[c], L1 = chunk_first[c + 1];
+      float ax = 0.f, ay = 0.f;
+      for (int L = L0; L < L1; L += 4) {
+        float2 g[4], w2[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {  // four layers' loads in flight
+          const bool in = L + q < L1;
+          g[q] = in ? stack[(int64_t)(L + q) * cells + kr] : make_float2(0.f, 0.f);
+          w2[q] = !in ? make_float2(0.f, 0.f) : cached ? s_w[L + q - Lb0] : split_w(layer_w[L + q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float wh = w2[q].x, wl = w2[q].y;
+          const float hi = wh * ph_h;
+          const float lo = fmaf(wh, ph_h, -hi) + fmaf(wh, ph_l, wl * ph_h);
+          const float f = (hi - rintf(hi)) + lo;
+          float sn, cs;
+          sincospif(2.0f * f, &sn, &cs);
+          ax += g[q].x * cs + g[q].y * sn;
+          ay += g[q].y * cs - g[q].x * sn;
+        }
+      }
+      out[(int64_t)c * cells + kr] = make_float2(ax * sg, ay * sg);
     }
-    out[(int64_t)c * cells + k] = make_float2(ax, ay);
   }
   if (bad && status) atomicAdd(&status[ST_RANGE], 1);
 }
 
-// grid[y0 + i, x0 + j] += sub[c, i, j] inside the grid (sub-grids overlap by
-// the margin, hence the atomics).
+// grid[y0 + i, x0 + j] += sub[c, i, j] inside the grid, where sub is the
+// centred transform: the unshifted forward transform G of the rolled image
+// read at the rolled index, sub[i, j] = G[i + S/2, j + S/2] (indices mod S).
+// Sub-grids overlap by the margin, hence the atomics.
 __global__ void k_towers_add(const float2 *__restrict__ sub, int S, const int32_t *__restrict__ origin,
                              int N, float2 *__restrict__ grid) {
   const int c = blockIdx.y;
   const int x0 = origin[2 * c], y0 = origin[2 * c + 1];
   const int64_t cells = (int64_t)S * S;
+  const int half = S / 2;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cells;
        k += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(k / S), j = (int)(k - (int64_t)i * S);
     const int y = y0 + i, x = x0 + j;
     if (y < 0 || y >= N || x < 0 || x >= N) continue;
-    const float2 v = sub[(int64_t)c * cells + k];
+    const int ir = i + half >= S ? i + half - S : i + half;
+    const int jr = j + half >= S ? j + half - S : j + half;
+    const float2 v = sub[(int64_t)c * cells + (int64_t)ir * S + jr];
     if (v.x != 0.f || v.y != 0.f) atomicAdd(&grid[(int64_t)y * N + x], v);
   }
 }
@@ -188,22 +230,25 @@ int cg_tower_keys(const double *uvw, int64_t stride, int64_t n, double theta, in
 int cg_towers_combine(const void *stack_c64, int layers, int S, double theta,
                       const double *layer_w, const int32_t *chunk_first, int nchunks,
                       void *out_c64, int32_t *d_status, cg_stream_t stream) {
-  CG_REQUIRE(stack_c64 && layer_w && chunk_first && out_c64 && layers >= 1 && S >= 1 &&
-                 nchunks >= 1 && nchunks <= 65535,
-             "bad w-towers combine arguments");
+  CG_REQUIRE(stack_c64 && layer_w && chunk_first && out_c64 && layers >= 1 && S >= 2 &&
+                 S % 2 == 0 && nchunks >= 1,
+             "bad w-towers combine arguments (even sub-grid size)");
   const int64_t cells = (int64_t)S * S;
-  const unsigned bx = (unsigned)std::min<int64_t>((cells + 255) / 256, 64);
-  k_towers_combine<<<dim3(bx, nchunks), 256, 0, (cudaStream_t)stream>>>(
-      (const float2 *)stack_c64, S, theta, layer_w, chunk_first, (float2 *)out_c64, d_status);
+  const unsigned bx = (unsigned)std::min<int64_t>((cells + 255) / 256, 1024);
+  const unsigned by = (unsigned)((nchunks + TOWER_CHUNKS_PER_BLOCK - 1) / TOWER_CHUNKS_PER_BLOCK);
+  k_towers_combine<<<dim3(bx, by), 256, TOWER_SMEM_LAYERS * sizeof(float2),
+                     (cudaStream_t)stream>>>(
+      (const float2 *)stack_c64, S, theta, layer_w, chunk_first, nchunks, (float2 *)out_c64,
+      d_status);
   CG_LAUNCH("w-towers combine");
   return CG_OK;
 }
 
 int cg_towers_add(const void *sub_c64, int nchunks, int S, const int32_t *origin, int N,
                   void *grid_c64, cg_stream_t stream) {
-  CG_REQUIRE(sub_c64 && origin && grid_c64 && S >= 1 && N >= 1 && nchunks >= 1 &&
-                 nchunks <= 65535,
-             "bad w-towers add arguments");
+  CG_REQUIRE(sub_c64 && origin && grid_c64 && S >= 2 && S % 2 == 0 && N >= 1 &&
+                 nchunks >= 1 && nchunks <= 65535,
+             "bad w-towers add arguments (even sub-grid size)");
   const int64_t cells = (int64_t)S * S;
   const unsigned bx = (unsigned)std::min<int64_t>((cells + 255) / 256, 64);
   k_towers_add<<<dim3(bx, nchunks), 256, 0, (cudaStream_t)stream>>>(

@@ -135,11 +135,12 @@ class Plan:
     uvw / lam is the fraction of the grid), ``shape`` the grid (H, W)."""
 
     def __init__(self, uvw, lam, shape, ktab, kidx=None, mode=L.CG_PLAN_TILED, status=None,
-                 wbins=None, layers=None, groups=None):
+                 wbins=None, layers=None, groups=None, tile=0):
         """wbins=(wstep, kmin): take each visibility's kernel group from its w bin
         (round(w / wstep) - kmin) inside the plan's coordinate pass.
         layers=(L, layer): grid visibility i into grid layer[i] of a stack of L grids.
-        groups=(G, group): plain form only, one launch per group[i] in [0, G)."""
+        groups=(G, group): plain form only, one launch per group[i] in [0, G).
+        tile: this plan's grid tile edge (0: the tuning / automatic choice)."""
         require_cuda()
         self.uvw = cuda_tensor(uvw, torch.float64)
         if self.uvw.dim() != 2 or self.uvw.shape[1] < 2:
@@ -158,7 +159,7 @@ class Plan:
                           0.0 if wbins is None else float(wbins[0]),
                           0 if wbins is None else int(wbins[1]),
                           None if self.group is None else self.group.data_ptr(),
-                          0 if groups is None else int(groups[0]))
+                          0 if groups is None else int(groups[0]), int(tile))
         nbytes = L.lib().cg_plan_workspace_bytes_ex(mode, self.n, self.shape[0], self.shape[1],
                                                     ctypes.byref(kd), ctypes.byref(opts))
         if nbytes == 0:
@@ -209,6 +210,13 @@ class Plan:
         """grid (c64 [H, W], or [layers, H, W]) += convgrid of vis (c64 [n])."""
         t = self._table(ktab, CF)
         L.call("cg_grid", self.handle, _p(t), _p(vis), _p(grid), stream())
+        return grid
+
+    def grid_sparse(self, ktab, vis, grid):
+        """grid += convgrid(vis) with per-tap atomics (cg_grid_sparse): for plans with
+        few visibilities per tile."""
+        t = self._table(ktab, CF)
+        L.call("cg_grid_sparse", self.handle, _p(t), _p(vis), _p(grid), stream())
         return grid
 
     def grid_weighted(self, ktab, vis, weight, grid):
@@ -349,6 +357,14 @@ def fft_(t, inverse):
     if not ((H == 1 or H % 2 == 0) and W % 2 == 0):
         ws = torch.empty_like(t)
     L.call("cg_fft", _p(t), batch, H, W, int(t.dtype == CF), int(inverse), _p(ws), stream())
+    return t
+
+
+def fft_raw(t, inverse):
+    """Unshifted, unnormalised (i)fft of the last two dims of t, in place."""
+    H, W = t.shape[-2], t.shape[-1]
+    L.call("cg_fft_raw", _p(t), t.numel() // (H * W), H, W, int(t.dtype == CF), int(inverse),
+           stream())
     return t
 
 

@@ -792,7 +792,8 @@ def w_stack_imaging(theta, lam, uvw, src, vis, kv, plane, precision=None, per_pl
 
 
 def w_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wincrement, wstep=2000,
-                     kernel_cache=None, kernel_fn=w_kernel, precision=None, **kwargs):
+                     kernel_cache=None, kernel_fn=w_kernel, precision=None, tile=32,
+                     gridder="auto", **kwargs):
     """w-towers imaging: w-stacking on sub-grids (examples/grid/grid.c:482-710,
     examples/notebooks/wtowers.ipynb code cell 16).  Visibilities are binned into uv
     chunks of ``subgrid_size - margin`` cells and w-planes of width ``wincrement``;
@@ -802,13 +803,16 @@ def w_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wincrement
     w = 0 in image space (division by w_kernel_function(l, m, w_plane)) and summed, and
     the chunk's sub-grid is added into the grid.  Returns the grid, the quantity
     w_cache_imaging returns.  All sub-grids grid in one launch and transform in batched
-    FFTs.  FP32 only; needs margin >= the kernel support."""
+    FFTs (``tile``: the gridder's tile edge inside the sub-grids; ``gridder``: "tiled"
+    (cg_grid), "sparse" (cg_grid_sparse, per-tap atomics) or "auto", sparse when the
+    sub-grids average fewer than 16 visibilities per tile).  FP32 only; needs an even
+    subgrid_size and margin >= the kernel support."""
     if _prec(precision) != "fp32":
         raise ValueError("w_towers_imaging runs the FP32 tiled path only")
     N = _grid_size(theta, lam)
     s, C = int(subgrid_size), int(subgrid_size) - int(margin)
-    if C < 1 or margin < 0:
-        raise ValueError("need 0 <= margin < subgrid_size")
+    if C < 1 or margin < 0 or s % 2:
+        raise ValueError("need an even subgrid_size and 0 <= margin < subgrid_size")
     n = _nrows(uvw)
     grid = torch.zeros((N, N), dtype=E.CF, device="cuda")
     if n == 0:
@@ -831,12 +835,21 @@ def w_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wincrement
     ktab, kidx = _spec_w_cache(theta, rel, None, src, wstep, kernel_cache, kernel_fn, kwargs,
                                E.CF)
     stack = torch.zeros((len(used), s, s), dtype=E.CF, device="cuda")
-    plan = E.Plan(rel, s / theta, (s, s), ktab, kidx, status=st, layers=(len(used), row))
-    plan.grid(ktab, vis_t, stack)
-    E.fft_(stack, True)
+    plan = E.Plan(rel, s / theta, (s, s), ktab, kidx, status=st, layers=(len(used), row),
+                  tile=tile)
+    tiles = len(used) * (-(-s // plan.info()["tile"])) ** 2
+    if gridder == "sparse" or (gridder == "auto" and n < 16 * tiles):
+        plan.grid_sparse(ktab, vis_t, stack)
+    elif gridder in ("auto", "tiled"):
+        plan.grid(ktab, vis_t, stack)
+    else:
+        raise ValueError("gridder must be 'auto', 'tiled' or 'sparse'")
+    # unshifted transforms: the centring rolls, signs and 1/s^2 are folded into
+    # the combine and add passes
+    E.fft_raw(stack, True)
     sub = E.towers_combine(stack, theta, plane * float(wincrement), chunk_first, st)
     del stack
-    E.fft_(sub, False)
+    E.fft_raw(sub, False)
     E.towers_add(sub, origin.astype(numpy.int32), grid)
     st.check()
     return _host(grid, like=uvw)

@@ -164,6 +164,10 @@ typedef struct {
    * is finer than the launches (AW kernels: one launch per w-plane). */
   const int32_t *group;
   int ngroups;
+  /* Tiled mode: grid tile edge for this plan (multiple of 4, <= 64), or 0 for
+   * the process-wide tuning / automatic choice.  Sparse stacks of small grids
+   * (the sub-grids of w-towers) want large tiles: more visibilities per item. */
+  int tile;
 } cg_plan_opts;
 size_t cg_plan_workspace_bytes_ex(int mode, int64_t n, int H, int W,
                                   const cg_kernel_desc *kd,
@@ -197,6 +201,12 @@ int cg_grid(const cg_plan *plan, const void *ktab_c64, const void *vis_c64,
 int cg_grid_weighted(const cg_plan *plan, const void *ktab_c64,
                      const void *vis_c64, const float *weight,
                      void *grid_c64, cg_stream_t stream);
+/* convgrid (synthesis.py:464-481) for sparse grid stacks: the same sums as
+ * cg_grid, without shared-memory windows — every tap is a float2 atomic into
+ * the grid.  For plans with few visibilities per tile (the many sub-grids of
+ * w-towers), where cg_grid's per-item window costs more than the taps. */
+int cg_grid_sparse(const cg_plan *plan, const void *ktab_c64, const void *vis_c64,
+                   void *grid_c64, cg_stream_t stream);
 /* convdegrid (synthesis.py:484-503): out[i] = sum(grid[footprint] * K). */
 int cg_degrid(const cg_plan *plan, const void *ktab_c64, const void *grid_c64,
               void *vis_out_c64, cg_stream_t stream);
@@ -276,6 +286,11 @@ int cg_make_hermitian(void *grid, int H, int W, int is_c64,
  * one array of the same size. */
 int cg_fft(void *data, int batch, int H, int W, int is_c64, int inverse,
            void *workspace, cg_stream_t stream);
+/* The same transforms unshifted and unnormalised (cuFFT's own convention):
+ * for callers that fold the centring shifts and the 1/(H W) of the inverse
+ * into neighbouring passes (the w-towers pipeline). */
+int cg_fft_raw(void *data, int batch, int H, int W, int is_c64, int inverse,
+               cg_stream_t stream);
 
 /* Dirty image / PSF of a grid (synthesis.py:904-907): image = Re(ifft(
  * make_grid_hermitian(grid))), written as float32 H x W; the grid is

@@ -224,3 +224,19 @@ def test_lane_layout_weighted_modes(env, S_):
         err = float(torch.linalg.vector_norm((a - b).to(torch.complex128)) /
                     torch.linalg.vector_norm(b.to(torch.complex128)))
         assert err < 1e-6, err
+
+
+@pytest.mark.parametrize("S_,sep", [(7, True), (8, False), (15, False), (16, False)])
+def test_sparse_gridder_matches_oracle(env, S_, sep):
+    """cg_grid_sparse (per-tap atomics, no windows) grids the same sums as convgrid."""
+    torch, E, S, A, O = env
+    theta, lam, uvw, vis = _wproj_case(O, n=20000, N=256, seed=61)
+    N = int(round(theta * lam))
+    aa = O.anti_aliasing_function(N, 0, 7)
+    kv = O.kernel_oversample(aa, 4, S_) if sep else O.kernel_oversample(numpy.outer(aa, aa), 4, S_)
+    kt = E.KernelTable.from_gcf(kv, 0, E.CF)
+    plan = E.Plan(uvw, lam, (N, N), kt)
+    g = plan.grid_sparse(kt, E.cuda_tensor(vis, E.CF), torch.zeros((N, N), dtype=E.CF,
+                                                                    device="cuda"))
+    plan.check()
+    assert rel(g.cpu().numpy(), O.conv_imaging(theta, lam, uvw, None, vis, kv)) < FP32_TOL

@@ -55,15 +55,19 @@ def test_tower_keys_bitexact(env):
     assert_array_equal(relt.cpu().numpy(), rel_ref)
 
 
-@pytest.mark.parametrize("s,margin,winc,kern", [(64, 16, 60.0, 7), (64, 16, 40.0, 8),
-                                                 (96, 24, 100.0, 15), (48, 16, 25.0, 4)])
-def test_w_towers_imaging_matches_oracle(env, s, margin, winc, kern):
+@pytest.mark.parametrize("s,margin,winc,kern,tile", [(64, 16, 60.0, 7, 32), (64, 16, 40.0, 8, 32),
+                                                      (96, 24, 100.0, 15, 32),
+                                                      (48, 16, 25.0, 4, 32), (64, 16, 40.0, 8, 16),
+                                                      (64, 16, 40.0, 8, 64), (96, 24, 60.0, 7, 64)])
+def test_w_towers_imaging_matches_oracle(env, s, margin, winc, kern, tile):
     torch, E, S, O = env
     theta, lam, uvw, vis = _case()
     kw = dict(NpixFF=32, NpixKern=kern, Qpx=4)
-    got = S.w_towers_imaging(theta, lam, uvw, None, vis, s, margin, winc, 10.0, **kw)
     ref = O.w_towers_imaging(theta, lam, uvw, None, vis, s, margin, winc, 10.0, **kw)
-    assert rel(got, ref) < TOL
+    for gridder in ("tiled", "sparse"):
+        got = S.w_towers_imaging(theta, lam, uvw, None, vis, s, margin, winc, 10.0, tile=tile,
+                                 gridder=gridder, **kw)
+        assert rel(got, ref) < TOL, gridder
 
 
 def test_w_towers_single_plane_is_w_projection(env):
