@@ -75,6 +75,8 @@ SIGNATURES = {
     "cg_tower_keys": (c_int, [P, c_int64, c_int64, c_double, c_int, c_double, P, P, P, P, P, P]),
     "cg_towers_combine": (c_int, [P, c_int, c_int, c_double, P, P, c_int, P, P, P]),
     "cg_towers_add": (c_int, [P, c_int, c_int, P, c_int, P, P]),
+    "cg_towers_cut": (c_int, [P, c_int, P, c_int, c_int, P, P]),
+    "cg_towers_expand": (c_int, [P, c_int, c_double, P, P, c_int, P, P, P]),
     "cg_plan_destroy": (c_int, [P]),
     "cg_set_tuning": (c_int, [ctypes.POINTER(Tuning)]),
     "cg_get_tuning": (c_int, [ctypes.POINTER(Tuning)]),

@@ -233,6 +233,10 @@ def measure_wtowers(steps=5, variants=True):
     ms = _time(lambda: synthesis.w_towers_imaging(w.theta, w.lam, uvw, None, vis, s, margin,
                                                   winc, 10.0, tile=32, gridder="sparse", **kw),
                steps)
+    grid = synthesis.w_towers_imaging(w.theta, w.lam, uvw, None, vis, s, margin, winc, 10.0,
+                                      tile=32, gridder="sparse", **kw)
+    ms_pred = _time(lambda: synthesis.w_towers_predict(w.theta, w.lam, uvw, None, grid, s,
+                                                       margin, winc, 10.0, tile=32, **kw), steps)
     var = {}
     for gridder, tile in ((("sparse", 32), ("tiled", 32), ("tiled", 64)) if variants else ()):
         for wi in (50.0, 100.0):
@@ -249,11 +253,16 @@ def measure_wtowers(steps=5, variants=True):
     kwp = dict(NpixFF=w.params["NpixFF"], NpixKern=w.S, Qpx=w.Q)
     ms_wp = _time(lambda: synthesis.w_cache_imaging(w.theta, w.lam, uvw, None, vis,
                                                     wstep=w.params["wstep"], **kwp), steps)
+    ms_wpp = _time(lambda: synthesis.w_cache_predict(w.theta, w.lam, uvw, None, grid,
+                                                     wstep=w.params["wstep"], **kwp), steps)
     return {"workload": "w-towers 4096^2 2M vis, 256^2 sub-grids margin 16, w-planes of 100, "
                         "S 8 Q 8 last mile, sparse gridder", "n_vis": n, "ms": ms, "mvis_s": n / ms / 1e3,
             "chunks": chunks, "layers": layers, "ms_by_gridder_tile_and_plane_width": var,
+            "predict_ms": ms_pred, "predict_mvis_s": n / ms_pred / 1e3,
             "w_projection_s15_ms": ms_wp, "w_projection_s15_mvis_s": n / ms_wp / 1e3,
-            "note": "grid only (imaging); parity with the oracle's w-towers <= 1e-5 in "
+            "w_projection_s15_predict_ms": ms_wpp,
+            "note": "ms = imaging (grid), predict_ms = predict (visibilities from the grid), "
+                    "each end to end; parity with the oracle's w-towers <= 1e-5 in "
                     "tests/test_gpu_towers.py"}
 
 

@@ -194,6 +194,80 @@ __global__ void k_towers_add(const float2 *__restrict__ sub, int S, const int32_
   }
 }
 
+// Predict, the reverse pass.  cut: out[c, roll(k)] = grid[origin_c + k] (zeros
+// outside the grid), roll(k) = (k + S/2) mod S per axis: the ifftshift, so an
+// unshifted inverse transform Y of it gives the centred image Y[roll(k)] / S^2.
+__global__ void k_towers_cut(const float2 *__restrict__ grid, int N,
+                             const int32_t *__restrict__ origin, int S,
+                             float2 *__restrict__ out) {
+  const int c = blockIdx.y;
+  const int x0 = origin[2 * c], y0 = origin[2 * c + 1];
+  const int64_t cells = (int64_t)S * S;
+  const int half = S / 2;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cells;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k / S), j = (int)(k - (int64_t)i * S);
+    const int y = y0 + i, x = x0 + j;
+    const int ir = i + half >= S ? i + half - S : i + half;
+    const int jr = j + half >= S ? j + half - S : j + half;
+    out[(int64_t)c * cells + (int64_t)ir * S + jr] =
+        (y >= 0 && y < N && x >= 0 && x < N) ? grid[(int64_t)y * N + x] : make_float2(0.f, 0.f);
+  }
+}
+
+// expand: layer L (chunk c, plane w_L) = image_c / exp(2 pi i w_L ph), written
+// at the rolled index times (-1)^(kx+ky), so that an unshifted forward
+// transform of it is the centred sub-grid in natural order; image_c[k] =
+// Y_c[roll(k)] / S^2.  Rolls are involutions for even S, so each thread reads
+// and writes index n = roll(k).
+__global__ void k_towers_expand(const float2 *__restrict__ images, int S, double theta,
+                                const double *__restrict__ layer_w,
+                                const int32_t *__restrict__ chunk_first, int nchunks,
+                                float2 *__restrict__ out, int32_t *status) {
+  extern __shared__ float2 s_w[];
+  const int c0 = blockIdx.y * TOWER_CHUNKS_PER_BLOCK;
+  const int c1 = min(nchunks, c0 + TOWER_CHUNKS_PER_BLOCK);
+  const int Lb0 = chunk_first[c0], Lb1 = chunk_first[c1];
+  const bool cached = Lb1 - Lb0 <= TOWER_SMEM_LAYERS;
+  if (cached)
+    for (int L = Lb0 + (int)threadIdx.x; L < Lb1; L += blockDim.x) s_w[L - Lb0] = split_w(layer_w[L]);
+  __syncthreads();
+  const int64_t cells = (int64_t)S * S;
+  const int half = S / 2;
+  const float scale = 1.0f / (float)cells;
+  int bad = 0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cells;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k / S), j = (int)(k - (int64_t)i * S);
+    const double l = __dmul_rn(theta, __ddiv_rn((double)(j - half), (double)S));
+    const double m = __dmul_rn(theta, __ddiv_rn((double)(i - half), (double)S));
+    const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
+    if (!(r2 < 1.0)) bad = 1;
+    const double ph = 1.0 - sqrt(1.0 - r2);
+    const float ph_h = (float)ph, ph_l = (float)(ph - (double)ph_h);
+    const int ir = i + half >= S ? i + half - S : i + half;
+    const int jr = j + half >= S ? j + half - S : j + half;
+    const int64_t kr = (int64_t)ir * S + jr;
+    const float sg = ((i + j) & 1) ? -scale : scale;
+    for (int c = c0; c < c1; ++c) {
+      float2 a = images[(int64_t)c * cells + kr];
+      a.x *= sg;
+      a.y *= sg;
+      for (int L = chunk_first[c]; L < chunk_first[c + 1]; ++L) {
+        const float2 w2 = cached ? s_w[L - Lb0] : split_w(layer_w[L]);
+        const float hi = w2.x * ph_h;
+        const float lo = fmaf(w2.x, ph_h, -hi) + fmaf(w2.x, ph_l, w2.y * ph_h);
+        const float f = (hi - rintf(hi)) + lo;
+        float sn, cs;
+        sincospif(2.0f * f, &sn, &cs);
+        // a / (cs + i sn) = a * (cs - i sn)
+        out[(int64_t)L * cells + kr] = make_float2(a.x * cs + a.y * sn, a.y * cs - a.x * sn);
+      }
+    }
+  }
+  if (bad && status) atomicAdd(&status[ST_RANGE], 1);
+}
+
 }  // namespace cg
 
 using namespace cg;
@@ -254,6 +328,35 @@ int cg_towers_add(const void *sub_c64, int nchunks, int S, const int32_t *origin
   k_towers_add<<<dim3(bx, nchunks), 256, 0, (cudaStream_t)stream>>>(
       (const float2 *)sub_c64, S, origin, N, (float2 *)grid_c64);
   CG_LAUNCH("w-towers add");
+  return CG_OK;
+}
+
+int cg_towers_cut(const void *grid_c64, int N, const int32_t *origin, int nchunks, int S,
+                  void *out_c64, cg_stream_t stream) {
+  CG_REQUIRE(grid_c64 && origin && out_c64 && N >= 1 && S >= 2 && S % 2 == 0 && nchunks >= 1 &&
+                 nchunks <= 65535,
+             "bad w-towers cut arguments (even sub-grid size)");
+  const int64_t cells = (int64_t)S * S;
+  const unsigned bx = (unsigned)std::min<int64_t>((cells + 255) / 256, 64);
+  k_towers_cut<<<dim3(bx, nchunks), 256, 0, (cudaStream_t)stream>>>(
+      (const float2 *)grid_c64, N, origin, S, (float2 *)out_c64);
+  CG_LAUNCH("w-towers cut");
+  return CG_OK;
+}
+
+int cg_towers_expand(const void *images_c64, int S, double theta, const double *layer_w,
+                     const int32_t *chunk_first, int nchunks, void *out_c64, int32_t *d_status,
+                     cg_stream_t stream) {
+  CG_REQUIRE(images_c64 && layer_w && chunk_first && out_c64 && S >= 2 && S % 2 == 0 &&
+                 nchunks >= 1,
+             "bad w-towers expand arguments (even sub-grid size)");
+  const int64_t cells = (int64_t)S * S;
+  const unsigned bx = (unsigned)std::min<int64_t>((cells + 255) / 256, 1024);
+  const unsigned by = (unsigned)((nchunks + TOWER_CHUNKS_PER_BLOCK - 1) / TOWER_CHUNKS_PER_BLOCK);
+  k_towers_expand<<<dim3(bx, by), 256, TOWER_SMEM_LAYERS * sizeof(float2),
+                    (cudaStream_t)stream>>>((const float2 *)images_c64, S, theta, layer_w,
+                                            chunk_first, nchunks, (float2 *)out_c64, d_status);
+  CG_LAUNCH("w-towers expand");
   return CG_OK;
 }
 

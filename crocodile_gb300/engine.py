@@ -517,3 +517,25 @@ def towers_add(sub, origin, grid):
     L.call("cg_towers_add", _p(sub), int(sub.shape[0]), int(sub.shape[-1]), _p(org),
            int(grid.shape[-1]), _p(grid), stream())
     return grid
+
+
+def towers_cut(grid, origin, S):
+    """Each chunk's S x S sub-grid of grid at its origin, rolled for cg_fft_raw."""
+    org = cuda_tensor(origin, torch.int32)
+    nchunks = int(org.shape[0])
+    out = torch.empty((nchunks, S, S), dtype=CF, device="cuda")
+    L.call("cg_towers_cut", _p(grid), int(grid.shape[-1]), _p(org), nchunks, int(S), _p(out),
+           stream())
+    return out
+
+
+def towers_expand(images, theta, layer_w, chunk_first, status):
+    """Per layer, its chunk's image / w_kernel_function(l, m, layer_w), ready for a
+    forward cg_fft_raw."""
+    S = images.shape[-1]
+    lw = cuda_tensor(layer_w, torch.float64)
+    cf = cuda_tensor(chunk_first, torch.int32)
+    out = torch.empty((int(lw.shape[0]), S, S), dtype=CF, device="cuda")
+    L.call("cg_towers_expand", _p(images), S, float(theta), _p(lw), _p(cf),
+           int(cf.shape[0]) - 1, _p(out), _p(status.t), stream())
+    return out

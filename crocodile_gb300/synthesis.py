@@ -791,6 +791,24 @@ def w_stack_imaging(theta, lam, uvw, src, vis, kv, plane, precision=None, per_pl
     return _host(image, like=uvw)
 
 
+def _tower_setup(theta, N, uvw_t, s, C, wincrement, st):
+    """(chunk/plane-relative uvw, layer per visibility, used (chunk, plane) keys, plane
+    of each layer, first layer of each chunk (+ end), sub-grid origin of each chunk)."""
+    key, rel, (ubmin, ubmax, vbmin, vbmax, wpmin, wpmax) = E.tower_keys(uvw_t, theta, C,
+                                                                        wincrement, st)
+    st.check()
+    nub, nvb, nwp = ubmax - ubmin + 1, vbmax - vbmin + 1, wpmax - wpmin + 1
+    row, used = E.compact_keys(key, nub * nvb * nwp, st)
+    used = used.cpu().numpy().astype(numpy.int64)
+    plane = used % nwp + wpmin
+    chunk, first = numpy.unique(used // nwp, return_index=True)
+    chunk_first = numpy.append(first, len(used)).astype(numpy.int32)
+    ub, vb = chunk % nub + ubmin, chunk // nub + vbmin
+    xmid, ymid = (C * ub + C * (ub + 1)) // 2, (C * vb + C * (vb + 1)) // 2
+    origin = numpy.column_stack([N // 2 + xmid - s // 2, N // 2 + ymid - s // 2])
+    return rel, row, used, plane, chunk_first, origin.astype(numpy.int32)
+
+
 def w_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wincrement, wstep=2000,
                      kernel_cache=None, kernel_fn=w_kernel, precision=None, tile=32,
                      gridder="auto", **kwargs):
@@ -820,18 +838,8 @@ def w_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wincrement
     uvw_t = E.cuda_tensor(uvw, torch.float64)
     vis_t = E.cuda_tensor(vis, E.CF)
     st = E.Status()
-    key, rel, (ubmin, ubmax, vbmin, vbmax, wpmin, wpmax) = E.tower_keys(uvw_t, theta, C,
-                                                                        wincrement, st)
-    st.check()
-    nub, nvb, nwp = ubmax - ubmin + 1, vbmax - vbmin + 1, wpmax - wpmin + 1
-    row, used = E.compact_keys(key, nub * nvb * nwp, st)
-    used = used.cpu().numpy().astype(numpy.int64)
-    plane = used % nwp + wpmin
-    chunk, first = numpy.unique(used // nwp, return_index=True)
-    chunk_first = numpy.append(first, len(used)).astype(numpy.int32)
-    ub, vb = chunk % nub + ubmin, chunk // nub + vbmin
-    xmid, ymid = (C * ub + C * (ub + 1)) // 2, (C * vb + C * (vb + 1)) // 2
-    origin = numpy.column_stack([N // 2 + xmid - s // 2, N // 2 + ymid - s // 2])
+    rel, row, used, plane, chunk_first, origin = _tower_setup(theta, N, uvw_t, s, C,
+                                                              wincrement, st)
     ktab, kidx = _spec_w_cache(theta, rel, None, src, wstep, kernel_cache, kernel_fn, kwargs,
                                E.CF)
     stack = torch.zeros((len(used), s, s), dtype=E.CF, device="cuda")
@@ -850,9 +858,45 @@ def w_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wincrement
     sub = E.towers_combine(stack, theta, plane * float(wincrement), chunk_first, st)
     del stack
     E.fft_raw(sub, False)
-    E.towers_add(sub, origin.astype(numpy.int32), grid)
+    E.towers_add(sub, origin, grid)
     st.check()
     return _host(grid, like=uvw)
+
+
+def w_towers_predict(theta, lam, uvw, src, guv, subgrid_size, margin, wincrement, wstep=2000,
+                     kernel_cache=None, kernel_fn=w_kernel, precision=None, tile=32, **kwargs):
+    """w-towers predict (examples/notebooks/wtowers-predict.ipynb), the reverse of
+    w_towers_imaging: each chunk's sub-grid of ``guv`` goes to image space, each of the
+    chunk's w-planes gets its image / w_kernel_function(l, m, w_plane) back in uv, and
+    the visibilities are degridded from their plane's sub-grid with the residual-w
+    kernels of w_cache_predict.  All sub-grids transform in batched FFTs and degrid in
+    one launch.  Returns the visibilities.  FP32 only."""
+    if _prec(precision) != "fp32":
+        raise ValueError("w_towers_predict runs the FP32 tiled path only")
+    s, C = int(subgrid_size), int(subgrid_size) - int(margin)
+    if C < 1 or margin < 0 or s % 2:
+        raise ValueError("need an even subgrid_size and 0 <= margin < subgrid_size")
+    grid_t = E.cuda_tensor(guv, E.CF)
+    N = grid_t.shape[-1]
+    n = _nrows(uvw)
+    if n == 0:
+        return _host(torch.zeros(0, dtype=E.CF, device="cuda"), like=uvw)
+    uvw_t = E.cuda_tensor(uvw, torch.float64)
+    st = E.Status()
+    rel, row, used, plane, chunk_first, origin = _tower_setup(theta, N, uvw_t, s, C,
+                                                              wincrement, st)
+    ktab, kidx = _spec_w_cache(theta, rel, None, src, wstep, kernel_cache, kernel_fn, kwargs,
+                               E.CF)
+    images = E.towers_cut(grid_t, origin, s)
+    E.fft_raw(images, True)
+    stack = E.towers_expand(images, theta, plane * float(wincrement), chunk_first, st)
+    del images
+    E.fft_raw(stack, False)
+    plan = E.Plan(rel, s / theta, (s, s), ktab, kidx, status=st, layers=(len(used), row),
+                  tile=tile)
+    out = plan.degrid(ktab, stack)
+    st.check()
+    return _host(out, like=uvw)
 
 
 def sample_image(image, x, y):

@@ -361,6 +361,18 @@ int cg_towers_combine(const void *stack_c64, int layers, int S, double theta,
                       void *out_c64, int32_t *d_status, cg_stream_t stream);
 int cg_towers_add(const void *sub_c64, int nchunks, int S, const int32_t *origin, int N,
                   void *grid_c64, cg_stream_t stream);
+/* w-towers predict (examples/notebooks/wtowers-predict.ipynb), the reverse:
+ * cg_towers_cut copies each chunk's S x S sub-grid of the N x N grid at origin
+ * (zeros outside), rolled by S/2 for an unshifted inverse cg_fft_raw;
+ * cg_towers_expand forms each layer's sub-grid image, chunk image /
+ * w_kernel_function(l, m, layer_w[L]), rolled and sign-modulated so that an
+ * unshifted forward cg_fft_raw of the stack gives the centred sub-grids, which a
+ * layered plan's cg_degrid then degrids with the residual-w kernels. */
+int cg_towers_cut(const void *grid_c64, int N, const int32_t *origin, int nchunks, int S,
+                  void *out_c64, cg_stream_t stream);
+int cg_towers_expand(const void *images_c64, int S, double theta, const double *layer_w,
+                     const int32_t *chunk_first, int nchunks, void *out_c64, int32_t *d_status,
+                     cg_stream_t stream);
 
 /* ------------------------------------------------------------------ */
 /* Kernel generation (FP64 arithmetic; outputs c64 or c128). */

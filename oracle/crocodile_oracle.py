@@ -597,6 +597,37 @@ def w_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wincrement
     return guv
 
 
+def w_towers_predict(theta, lam, uvw, src, guv, subgrid_size, margin, wincrement, wstep,
+                     kernel_fn=w_kernel, **kwargs):
+    """w-towers predict (examples/notebooks/wtowers-predict.ipynb; the reverse of
+    w_towers_imaging): for each chunk, the s x s sub-grid of guv at the chunk's
+    origin (zeros outside the grid) is taken to image space; for each w-plane of the
+    chunk, fft(image / w_kernel_function(l, m, wp*wincrement)) is degridded with the
+    residual-w kernels (w_cache_predict) at the chunk-relative coordinates.  With one
+    plane this is w_cache_predict itself."""
+    N = guv.shape[0]
+    s = subgrid_size
+    src = numpy.zeros((len(uvw), 0)) if src is None else src
+    out = numpy.zeros(len(uvw), dtype=complex)
+    ub, vb, wp, xmid, ymid, rel = tower_bins(theta, uvw, s, margin, wincrement)
+    l, m = theta * coordinates2(s)
+    for cv, cu in sorted(set(zip(vb.tolist(), ub.tolist()))):
+        in_chunk = (vb == cv) & (ub == cu)
+        i = numpy.nonzero(in_chunk)[0][0]
+        y0, x0 = N // 2 + ymid[i] - s // 2, N // 2 + xmid[i] - s // 2
+        crop = numpy.zeros((s, s), dtype=complex)
+        ya, yb, xa, xb = max(y0, 0), min(y0 + s, N), max(x0, 0), min(x0 + s, N)
+        if ya < yb and xa < xb:
+            crop[ya - y0:yb - y0, xa - x0:xb - x0] = guv[ya:yb, xa:xb]
+        image = ifft(crop)
+        for p in numpy.unique(wp[in_chunk]):
+            sel = in_chunk & (wp == p)
+            sub = fft(image / w_kernel_function(l, m, p * wincrement))
+            out[sel] = w_cache_predict(theta, s / theta, rel[sel], src[sel], sub, wstep=wstep,
+                                       kernel_fn=kernel_fn, **kwargs)
+    return out
+
+
 # --------------------------------------------------------------------------
 # point-source visibilities (crocodile/simulate.py:210-230)
 

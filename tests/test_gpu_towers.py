@@ -90,3 +90,28 @@ def test_w_towers_errors(env):
     bad[3, 0] = numpy.nan
     with pytest.raises(AssertionError):   # coordinates out of range, as the reference
         S.w_towers_imaging(theta, lam, bad, None, vis, 64, 16, 60.0, 10.0, **kw)
+
+
+@pytest.mark.parametrize("s,margin,winc,kern", [(64, 16, 60.0, 7), (64, 16, 40.0, 8),
+                                                 (96, 24, 100.0, 15)])
+def test_w_towers_predict_matches_oracle(env, s, margin, winc, kern):
+    torch, E, S, O = env
+    theta, lam, uvw, vis = _case(n=20000, seed=54)
+    N = int(round(theta * lam))
+    rng = numpy.random.default_rng(7)
+    guv = rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N))
+    kw = dict(NpixFF=32, NpixKern=kern, Qpx=4)
+    got = S.w_towers_predict(theta, lam, uvw, None, guv, s, margin, winc, 10.0, **kw)
+    ref = O.w_towers_predict(theta, lam, uvw, None, guv, s, margin, winc, 10.0, **kw)
+    assert rel(got, ref) < TOL
+
+
+def test_w_towers_predict_single_plane_is_w_cache_predict(env):
+    torch, E, S, O = env
+    theta, lam, uvw, vis = _case(n=20000, wmax=40.0, seed=55)
+    N = int(round(theta * lam))
+    guv = numpy.random.default_rng(8).normal(size=(N, N)).astype(complex)
+    kw = dict(NpixFF=32, NpixKern=8, Qpx=4)
+    got = S.w_towers_predict(theta, lam, uvw, None, guv, 64, 16, 100.0, 10.0, **kw)
+    ref = O.w_cache_predict(theta, lam, uvw, None, guv, wstep=10.0, **kw)
+    assert rel(got, ref) < TOL

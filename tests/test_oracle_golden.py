@@ -170,3 +170,18 @@ def test_w_towers_bins():
     assert_array_equal(ymid, [24, -24, 120, -456])
     assert_allclose(rel[:, 0], uvw[:, 0] - xmid / theta)
     assert_allclose(rel[:, 2], uvw[:, 2] - wp * winc)
+
+
+def test_w_towers_predict_single_plane_is_the_reference_predict(golden):
+    """One w-plane: the oracle's w-towers predict is w_cache_predict, which the
+    reference's fixed-kernel predict pins (cd_vis4, synthesis.py:484-503)."""
+    uvw, vis = golden["wc_uvw"], golden["wc_vis"]
+    lam, theta = float(golden["wc_lam"]), float(golden["wc_theta"])
+    N = golden["wc_grid"].shape[0]
+    guv = numpy.random.default_rng(4).normal(size=(N, N)) + 0j
+    winc = 4 * float(numpy.abs(uvw[:, 2]).max()) + 1.0
+    ref = O.w_cache_predict(theta, lam, uvw, None, guv, wstep=10.0, NpixFF=16, NpixKern=7, Qpx=4)
+    for s, margin in ((32, 8), (48, 16)):
+        got = O.w_towers_predict(theta, lam, uvw, None, guv, s, margin, winc, 10.0,
+                                 NpixFF=16, NpixKern=7, Qpx=4)
+        assert numpy.linalg.norm(got - ref) <= 1e-12 * numpy.linalg.norm(ref)
