@@ -37,6 +37,18 @@ def _time(fn, steps, warmup=2):
     return statistics.median(times)
 
 
+def _graph_time(fn, steps, ms_eager):
+    """(median ms of the step captured once in a CUDA graph and replayed, "CUDA graph"),
+    or the eager time if the capture is refused."""
+    try:
+        cap = E.CapturedStep(fn)
+    except RuntimeError as e:
+        return ms_eager, "eager (graph capture failed: %s)" % str(e).splitlines()[0][:100]
+    ms = _time(cap.replay, steps)
+    del cap
+    return ms, "CUDA graph"
+
+
 def _rel(a, b):
     a, b = a.to(torch.complex128), b.to(torch.complex128)
     return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
@@ -73,8 +85,10 @@ def measure_plain(steps=20):
         plan.grid_fp64(kt64, vis64, g64)
         out["v64"] = plan.degrid_fp64(kt64, g64)
 
-    ms, ms64 = _time(fp32, steps), _time(fp64, max(3, steps // 4))
-    return {"workload": w.name, "n_vis": n, "ms": ms, "mvis_s": n / ms / 1e3,
+    ms_eager, ms64 = _time(fp32, steps), _time(fp64, max(3, steps // 4))
+    ms, launch = _graph_time(fp32, steps, ms_eager)
+    return {"workload": w.name, "n_vis": n, "ms": ms, "mvis_s": n / ms / 1e3, "launch": launch,
+            "ms_eager": ms_eager,
             "plain_fp64_ms": ms64, "plain_fp64_mvis_s": n / ms64 / 1e3, "speedup": ms64 / ms,
             "rel_err_grid": _rel(g, g64), "rel_err_degrid": _rel(out["v"], out["v64"])}
 
@@ -111,9 +125,11 @@ def measure_wproj(steps=20):
         plan.grid_fp64(kt64, vis64, g64)
         out["v64"] = plan.degrid_fp64(kt64, g64)
 
-    ms, ms64 = _time(fp32, steps), _time(fp64, 2, 1)
+    ms_eager, ms64 = _time(fp32, steps), _time(fp64, 2, 1)
+    ms, launch = _graph_time(fp32, steps, ms_eager)
     st.check()
     return {"workload": w.name, "n_vis": n, "ms": ms, "mvis_s": n / ms / 1e3, "tuning": tuned,
+            "launch": launch, "ms_eager": ms_eager,
             "plain_fp64_ms": ms64, "plain_fp64_mvis_s": n / ms64 / 1e3, "speedup": ms64 / ms,
             "rel_err_grid": _rel(g, g64)}
 
