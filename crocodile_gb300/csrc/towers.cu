@@ -22,11 +22,6 @@
 
 namespace cg {
 
-struct TowerBins {
-  int64_t ub, vb, wp;
-  double ru, rv, rw;  // coordinates relative to the chunk centre and the plane
-};
-
 __device__ __forceinline__ int64_t floor_div_ll(int64_t a, int64_t b) {
   int64_t q, r;
   q = a / b;
@@ -35,65 +30,81 @@ __device__ __forceinline__ int64_t floor_div_ll(int64_t a, int64_t b) {
   return q;
 }
 
-__device__ __forceinline__ bool tower_bins(const double *row, double theta, int C, double winc,
-                                           TowerBins &t) {
-  const double u = row[0], v = row[1], w = row[2];
-  const double fu = floor(__ddiv_rn(__dmul_rn(u, theta), (double)C));
-  const double fv = floor(__ddiv_rn(__dmul_rn(v, theta), (double)C));
-  const double fw = rint(__ddiv_rn(w, winc));
-  if (!(fabs(fu) < 1e9 && fabs(fv) < 1e9 && fabs(fw) < 1e9)) return false;  // NaN too
-  t.ub = (int64_t)fu;
-  t.vb = (int64_t)fv;
-  t.wp = (int64_t)fw;
-  const int64_t xmid = floor_div_ll((int64_t)C * t.ub + (int64_t)C * (t.ub + 1), 2);
-  const int64_t ymid = floor_div_ll((int64_t)C * t.vb + (int64_t)C * (t.vb + 1), 2);
-  t.ru = __dadd_rn(u, -__ddiv_rn((double)xmid, theta));
-  t.rv = __dadd_rn(v, -__ddiv_rn((double)ymid, theta));
-  t.rw = __dadd_rn(w, -__dmul_rn(fw, winc));
-  return true;
+// floor(t / C) as numpy evaluates it (IEEE quotient, then floor), filtered as
+// in w_bin_fast: F = round(t * (1/C) * 2^20) from one FMA decides unless the
+// quotient lies within FIX_MARGIN units of an integer, where the exact
+// quotient is formed.  |t / C| < 2^30 on the fast path.
+__device__ __forceinline__ double floor_div_fast(double t, double C, double invC) {
+  const double e = fma(t, invC, FIX_MAGIC);
+  const long long F = (long long)((unsigned long long)__double_as_longlong(e) - FIX_MAGIC_BITS);
+  if (F > -(1ll << 50) && F < (1ll << 50)) {
+    const long long fr = F & (FIX_ONE - 1);
+    if (fr > FIX_MARGIN && fr < FIX_ONE - FIX_MARGIN) return (double)(F >> FIX_BITS);
+  }
+  return floor(__ddiv_rn(t, C));
 }
 
+// Pass 1: bins (ub, vb, wp) of every visibility, their ranges, and the bins
+// stored as three int32 at the start of the visibility's rel row (pass 2
+// reads them back before overwriting the row).
 __global__ void k_tower_bounds(const double *__restrict__ uvw, int64_t stride, int64_t n,
-                               double theta, int C, double winc, int32_t *mm,
-                               int32_t *status) {
+                               double theta, int C, double invC, double winc, double inv_winc,
+                               int32_t *mm, double *__restrict__ rel, int32_t *status) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  TowerBins t;
-  if (!tower_bins(uvw + i * stride, theta, C, winc, t)) {
+  const double *row = uvw + i * stride;
+  const double fu = floor_div_fast(__dmul_rn(row[0], theta), (double)C, invC);
+  const double fv = floor_div_fast(__dmul_rn(row[1], theta), (double)C, invC);
+  const double fw = w_bin_fast(row[2], winc, inv_winc);
+  int32_t *bins = (int32_t *)(rel + 3 * i);
+  if (!(fabs(fu) < 1e9 && fabs(fv) < 1e9 && fabs(fw) < 1e9)) {  // NaN too
     atomicAdd(&status[ST_RANGE], 1);
+    bins[0] = bins[1] = bins[2] = INT32_MIN;
     return;
   }
-  atomicMin(&mm[0], (int)t.ub);
-  atomicMax(&mm[1], (int)t.ub);
-  atomicMin(&mm[2], (int)t.vb);
-  atomicMax(&mm[3], (int)t.vb);
-  atomicMin(&mm[4], (int)t.wp);
-  atomicMax(&mm[5], (int)t.wp);
+  const int ub = (int)fu, vb = (int)fv, wp = (int)fw;
+  bins[0] = ub;
+  bins[1] = vb;
+  bins[2] = wp;
+  atomicMin(&mm[0], ub);
+  atomicMax(&mm[1], ub);
+  atomicMin(&mm[2], vb);
+  atomicMax(&mm[3], vb);
+  atomicMin(&mm[4], wp);
+  atomicMax(&mm[5], wp);
 }
 
 __global__ void k_tower_mm_init(int32_t *mm) {
   if (threadIdx.x < 6) mm[threadIdx.x] = (threadIdx.x & 1) ? INT32_MIN : INT32_MAX;
 }
 
-// key = ((vb - vbmin) * nub + (ub - ubmin)) * nwp + (wp - wpmin): sorted keys
-// group a chunk's planes together, in increasing w.
+// Pass 2: key = ((vb - vbmin) * nub + (ub - ubmin)) * nwp + (wp - wpmin) (sorted
+// keys group a chunk's planes together, in increasing w) and the coordinates
+// relative to the chunk centre xmid / theta (IEEE quotient, as numpy) and the
+// plane wp * wincrement.
 __global__ void k_tower_keys(const double *__restrict__ uvw, int64_t stride, int64_t n,
                              double theta, int C, double winc, int ubmin, int vbmin, int wpmin,
                              int nub, int nwp, int32_t *__restrict__ key,
                              double *__restrict__ rel) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  TowerBins t;
-  if (!tower_bins(uvw + i * stride, theta, C, winc, t)) {
-    key[i] = 0;  // counted as a range error by the bounds pass
+  const int32_t *bins = (const int32_t *)(rel + 3 * i);
+  const int ub = bins[0], vb = bins[1], wp = bins[2];
+  const double *row = uvw + i * stride;
+  if (ub == INT32_MIN) {  // counted as a range error by pass 1
+    key[i] = 0;
     rel[3 * i] = rel[3 * i + 1] = rel[3 * i + 2] = 0.0;
     return;
   }
-  key[i] = (int32_t)((((int)t.vb - vbmin) * nub + ((int)t.ub - ubmin)) * nwp +
-                     ((int)t.wp - wpmin));
-  rel[3 * i] = t.ru;
-  rel[3 * i + 1] = t.rv;
-  rel[3 * i + 2] = t.rw;
+  const int64_t xmid = floor_div_ll((int64_t)C * ub + (int64_t)C * (ub + 1), 2);
+  const int64_t ymid = floor_div_ll((int64_t)C * vb + (int64_t)C * (vb + 1), 2);
+  const double ru = __dadd_rn(row[0], -__ddiv_rn((double)xmid, theta));
+  const double rv = __dadd_rn(row[1], -__ddiv_rn((double)ymid, theta));
+  const double rw = __dadd_rn(row[2], -__dmul_rn((double)wp, winc));
+  key[i] = (int32_t)(((vb - vbmin) * nub + (ub - ubmin)) * nwp + (wp - wpmin));
+  rel[3 * i] = ru;
+  rel[3 * i + 1] = rv;
+  rel[3 * i + 2] = rw;
 }
 
 // out[c] = sum over the layers L of chunk c of image_L / exp(2 pi i w_L ph),
@@ -284,7 +295,8 @@ int cg_tower_keys(const double *uvw, int64_t stride, int64_t n, double theta, in
   cudaStream_t s = (cudaStream_t)stream;
   const unsigned blocks = (unsigned)((n + 255) / 256);
   k_tower_mm_init<<<1, 32, 0, s>>>(d_minmax);
-  k_tower_bounds<<<blocks, 256, 0, s>>>(uvw, stride, n, theta, chunk, wincrement, d_minmax,
+  k_tower_bounds<<<blocks, 256, 0, s>>>(uvw, stride, n, theta, chunk, 1.0 / (double)chunk,
+                                        wincrement, 1.0 / wincrement, d_minmax, rel_out,
                                         d_status);
   CG_LAUNCH("tower bounds");
   CG_CUDA(cudaMemcpyAsync(h_bounds, d_minmax, 6 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
