@@ -106,7 +106,7 @@ SIGNATURES = {
     "cg_w_kernels_workspace_bytes": (c_size_t, [c_int, c_int, c_int]),
     "cg_w_kernels": (c_int, [c_double, P, c_int, c_int, c_int, c_int, c_int, c_double, c_double,
                              P, P, c_int, P, c_size_t, P, P]),
-    "cg_aw_kernels_workspace_bytes": (c_size_t, [c_int, c_int]),
+    "cg_aw_kernels_workspace_bytes": (c_size_t, [c_int, c_int, c_int, c_int, c_int]),
     "cg_aw_kernels": (c_int, [P, c_int, c_int, P, c_int, c_int, c_int, P, P, P, c_int, P, c_int,
                               P, c_size_t, P, P]),
     "cg_w_bins": (c_int, [P, c_int64, c_int64, c_double, P, P, P, P, P]),

@@ -185,7 +185,7 @@ static int oversample_run(FarField F, int batch, int s, void *out, bool out_c64,
 //   same[i, j] = sum_{p, q} a[p, q] * b[i + o - p, j + o - q],  o = (nb - 1) / 2.
 __global__ void k_aw_akern(const double2 *__restrict__ A, int SA,
                            const int32_t *__restrict__ a1, const int32_t *__restrict__ a2,
-                           int nA, double2 *__restrict__ akern, int32_t *status) {
+                           int nA, float2 *__restrict__ akern, int32_t *status) {
   const int k = blockIdx.x;
   const int i1 = a1[k], i2 = a2[k];
   if (i1 < 0 || i1 >= nA || i2 < 0 || i2 >= nA) {
@@ -208,13 +208,13 @@ __global__ void k_aw_akern(const double2 *__restrict__ A, int SA,
         acc.y += u.x * v.y + u.y * v.x;
       }
     }
-    akern[(size_t)k * SA * SA + t] = acc;
+    akern[(size_t)k * SA * SA + t] = make_float2((float)acc.x, (float)acc.y);  // FP32 from here on
   }
 }
 
 template <typename C>
-__global__ void k_aw_conv(const double2 *__restrict__ akern, int SA,
-                          const double2 *__restrict__ Wk, int nW, int Q, int S,
+__global__ void k_aw_conv(const float2 *__restrict__ akern, int SA,
+                          const float2 *__restrict__ Wk, int nW, int Q, int S,
                           const int32_t *__restrict__ wi, C *__restrict__ out,
                           int32_t *status) {
   extern __shared__ float2 sh[];
@@ -226,12 +226,10 @@ __global__ void k_aw_conv(const double2 *__restrict__ akern, int SA,
     return;
   }
   if ((status[ST_RANGE] | status[ST_INDEX]) != 0) return;
-  const double2 *ak = akern + (size_t)k * SA * SA;
-  const double2 *wk = Wk + ((size_t)w * Q * Q + f) * S * S;
-  for (int t = threadIdx.x; t < SA * SA; t += blockDim.x)
-    sa[t] = make_float2((float)ak[t].x, (float)ak[t].y);
-  for (int t = threadIdx.x; t < S * S; t += blockDim.x)
-    sw[t] = make_float2((float)wk[t].x, (float)wk[t].y);
+  const float2 *ak = akern + (size_t)k * SA * SA;
+  const float2 *wk = Wk + ((size_t)w * Q * Q + f) * S * S;
+  for (int t = threadIdx.x; t < SA * SA; t += blockDim.x) sa[t] = ak[t];
+  for (int t = threadIdx.x; t < S * S; t += blockDim.x) sw[t] = wk[t];
   __syncthreads();
   const int o = (S - 1) / 2;
   C *dst = out + ((size_t)k * Q * Q + f) * SA * SA;
@@ -254,6 +252,76 @@ __global__ void k_aw_conv(const double2 *__restrict__ akern, int SA,
     r.x = ax;
     r.y = ay;
     dst[t] = r;
+  }
+}
+
+// The same convolution for SA x SA = SAC x SAC outputs with register blocking:
+// a thread computes JB neighbouring outputs (i, j0 .. j0+JB-1) of one row, and
+// for each A row p holds the SAC + JB - 1 w values that row needs in
+// registers, so a loaded A tap feeds JB complex multiply-adds (the
+// one-output-per-thread form is bound by shared-memory loads).
+template <typename C, int SAC, int JB>
+__global__ void __launch_bounds__(SAC *(SAC / JB)) k_aw_conv_blocked(
+    const float2 *__restrict__ akern, const float2 *__restrict__ Wk, int nW, int Q, int S,
+    const int32_t *__restrict__ wi, C *__restrict__ out, int32_t *status) {
+  extern __shared__ float2 sh[];
+  float2 *sa = sh, *sw = sh + SAC * SAC;
+  const int k = blockIdx.y, f = blockIdx.x;  // f = yf*Q + xf
+  const int w = wi[k];
+  if (w < 0 || w >= nW) {
+    if (threadIdx.x == 0 && f == 0) atomicAdd(&status[ST_INDEX], 1);
+    return;
+  }
+  if ((status[ST_RANGE] | status[ST_INDEX]) != 0) return;
+  const float2 *ak = akern + (size_t)k * SAC * SAC;
+  const float2 *wk = Wk + ((size_t)w * Q * Q + f) * S * S;
+  for (int t = threadIdx.x; t < SAC * SAC; t += blockDim.x) sa[t] = ak[t];
+  // w rows at an odd pitch (S + 1): a warp's lanes read 8 different rows, and a
+  // 16-element row is 128 B, so an even pitch would put them all on one bank set
+  const int SP = S + 1;
+  for (int t = threadIdx.x; t < S * S; t += blockDim.x) {
+    const int r = t / S, c = t - (t / S) * S;
+    sw[r * SP + c] = wk[t];
+  }
+  __syncthreads();
+  const int o = (S - 1) / 2;
+  const int i = threadIdx.x / (SAC / JB), j0 = (threadIdx.x % (SAC / JB)) * JB;
+  // (re, im) accumulators as pairs for the paired FP32 FMA: acc += (u.x, u.x) *
+  // (v.x, v.y), then acc += (-u.y, u.y) * (v.y, v.x) -- per component the same
+  // FMA sequence as the scalar form
+  float2 acc[JB];
+#pragma unroll
+  for (int d = 0; d < JB; ++d) acc[d] = make_float2(0.f, 0.f);
+  const int p_lo = max(0, i + o - (S - 1)), p_hi = min(SAC - 1, i + o);
+  const int c0 = j0 + o - (SAC - 1);  // w column of register m = c0 + m
+  for (int p = p_lo; p <= p_hi; ++p) {
+    const float2 *wrow = sw + (i + o - p) * SP;
+    float2 wv[SAC + JB - 1], ws[SAC + JB - 1];
+#pragma unroll
+    for (int m = 0; m < SAC + JB - 1; ++m) {
+      const int c = c0 + m;
+      wv[m] = (c >= 0 && c < S) ? wrow[c] : make_float2(0.f, 0.f);
+      ws[m] = make_float2(wv[m].y, wv[m].x);
+    }
+    const float2 *arow = sa + p * SAC;
+#pragma unroll
+    for (int q = 0; q < SAC; ++q) {
+      const float2 u = arow[q];
+      const float2 ux = make_float2(u.x, u.x), uy = make_float2(-u.y, u.y);
+#pragma unroll
+      for (int d = 0; d < JB; ++d) {  // w column j0 + d + o - q is register d + SAC - 1 - q
+        acc[d] = __ffma2_rn(ux, wv[d + SAC - 1 - q], acc[d]);
+        acc[d] = __ffma2_rn(uy, ws[d + SAC - 1 - q], acc[d]);
+      }
+    }
+  }
+  C *dst = out + ((size_t)k * Q * Q + f) * SAC * SAC + i * SAC + j0;
+#pragma unroll
+  for (int d = 0; d < JB; ++d) {
+    C r;
+    r.x = acc[d].x;
+    r.y = acc[d].y;
+    dst[d] = r;
   }
 }
 
@@ -326,8 +394,21 @@ int cg_w_kernels(double theta, const double *w_host, int nw, int NpixFF, int S, 
                         d_status, st);
 }
 
-size_t cg_aw_kernels_workspace_bytes(int nk, int SA) {
-  return (size_t)std::max(nk, 1) * SA * SA * sizeof(double2);
+__global__ void k_c128_to_c64(const double2 *__restrict__ in, int64_t n, float2 *__restrict__ out) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    out[t] = make_float2((float)in[t].x, (float)in[t].y);
+}
+
+// Workspace: the FP32 A1 (*) A2 kernels [nk, SA, SA], then the w sub-kernels
+// converted once to FP32 [nW, Q, Q, S, S] (the convolution blocks read both
+// many times; converting per block would load the narrow FP64 pipe).
+static size_t aw_ws_akern_bytes(int nk, int SA) {
+  return ((size_t)std::max(nk, 1) * SA * SA * sizeof(float2) + 255) & ~(size_t)255;
+}
+
+size_t cg_aw_kernels_workspace_bytes(int nk, int SA, int nW, int Q, int S) {
+  return aw_ws_akern_bytes(nk, SA) + (size_t)std::max(nW, 1) * Q * Q * S * S * sizeof(float2);
 }
 
 int cg_aw_kernels(const void *A, int nA, int SA, const void *Wk, int nW, int Q, int S,
@@ -339,20 +420,36 @@ int cg_aw_kernels(const void *A, int nA, int SA, const void *Wk, int nW, int Q, 
              "bad aw_kernels arguments");
   CG_REQUIRE(SA <= 64 && S <= 64, "AW kernel sizes above 64 are not supported");
   if (nk == 0) return CG_OK;
-  if (!ws || ws_bytes < cg_aw_kernels_workspace_bytes(nk, SA))
-    return set_error(CG_ERR_WORKSPACE, "aw_kernels needs %zu workspace bytes",
-                     cg_aw_kernels_workspace_bytes(nk, SA));
+  const size_t need = cg_aw_kernels_workspace_bytes(nk, SA, nW, Q, S);
+  if (!ws || ws_bytes < need)
+    return set_error(CG_ERR_WORKSPACE, "aw_kernels needs %zu workspace bytes", need);
   cudaStream_t st = (cudaStream_t)stream;
-  double2 *akern = (double2 *)ws;
+  float2 *akern = (float2 *)ws;
+  float2 *wk32 = (float2 *)((char *)ws + aw_ws_akern_bytes(nk, SA));
   k_aw_akern<<<nk, 256, 0, st>>>((const double2 *)A, SA, a1, a2, nA, akern, d_status);
   CG_LAUNCH("aw akern");
+  const int64_t nwk = (int64_t)nW * Q * Q * S * S;
+  k_c128_to_c64<<<(unsigned)std::min<int64_t>((nwk + 255) / 256, (int64_t)num_sms() * 16), 256, 0,
+                  st>>>((const double2 *)Wk, nwk, wk32);
+  CG_LAUNCH("aw w kernels to FP32");
   const size_t smem = (size_t)(SA * SA + S * S) * sizeof(float2);
   dim3 grid(Q * Q, nk);
+  if (SA == 16) {  // the AW kernels' size: register-blocked form, 4 outputs per thread
+    const size_t smem_b = (size_t)(SA * SA + S * (S + 1)) * sizeof(float2);
+    if (out_c64)
+      k_aw_conv_blocked<float2, 16, 4><<<grid, 64, smem_b, st>>>(
+          akern, wk32, nW, Q, S, wi, (float2 *)out, d_status);
+    else
+      k_aw_conv_blocked<double2, 16, 4><<<grid, 64, smem_b, st>>>(
+          akern, wk32, nW, Q, S, wi, (double2 *)out, d_status);
+    CG_LAUNCH("aw conv");
+    return CG_OK;
+  }
   if (out_c64)
-    k_aw_conv<float2><<<grid, 256, smem, st>>>(akern, SA, (const double2 *)Wk, nW, Q, S, wi,
+    k_aw_conv<float2><<<grid, 256, smem, st>>>(akern, SA, wk32, nW, Q, S, wi,
                                                (float2 *)out, d_status);
   else
-    k_aw_conv<double2><<<grid, 256, smem, st>>>(akern, SA, (const double2 *)Wk, nW, Q, S, wi,
+    k_aw_conv<double2><<<grid, 256, smem, st>>>(akern, SA, wk32, nW, Q, S, wi,
                                                 (double2 *)out, d_status);
   CG_LAUNCH("aw conv");
   return CG_OK;

@@ -445,7 +445,7 @@ def aw_kernels(A, Wk, a1, a2, wi, dtype=CF, status=None):
     st = status or Status()
     if status is None:
         st.reset()
-    nbytes = L.lib().cg_aw_kernels_workspace_bytes(nk, SA)
+    nbytes = L.lib().cg_aw_kernels_workspace_bytes(nk, SA, nW, Q, S)
     ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
     out = torch.empty((nk, Q, Q, SA, SA), dtype=dtype, device="cuda")
     L.call("cg_aw_kernels", _p(A), nA, SA, _p(Wk), nW, Q, S, _p(a1), _p(a2), _p(wi), nk,

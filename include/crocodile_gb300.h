@@ -399,8 +399,10 @@ int cg_w_kernels(double theta, const double *w_host, int nw, int NpixFF,
  *   out[k, yf, xf] = convolve2d(akern, W[wi[k], yf, xf], 'same')
  * A: [nA, SA, SA] c128, W: [nW, Q, Q, S, S] c128, out: [nk, Q, Q, SA, SA]
  * c64 or c128.  a1, a2, wi: int32 device arrays.  A kernels are combined
- * in FP64; the Q*Q sub-kernel convolutions use FP32 products and sums. */
-size_t cg_aw_kernels_workspace_bytes(int nk, int SA);
+ * in FP64 and rounded once to FP32; W is rounded once to FP32 into the
+ * workspace; the Q*Q sub-kernel convolutions use FP32 products and sums.
+ * Workspace: cg_aw_kernels_workspace_bytes(nk, SA, nW, Q, S) bytes. */
+size_t cg_aw_kernels_workspace_bytes(int nk, int SA, int nW, int Q, int S);
 int cg_aw_kernels(const void *A_c128, int nA, int SA, const void *W_c128,
                   int nW, int Q, int S, const int32_t *a1, const int32_t *a2,
                   const int32_t *wi, int nk, void *out, int out_c64,
