@@ -539,3 +539,32 @@ def towers_expand(images, theta, layer_w, chunk_first, status):
     L.call("cg_towers_expand", _p(images), S, float(theta), _p(lw), _p(cf),
            int(cf.shape[0]) - 1, _p(out), _p(status.t), stream())
     return out
+
+
+# --------------------------------------------------------------------------
+# Sze-Tan optimal gridding functions
+
+def szetan_gridding(h_ext, x0, R, kinv, nu):
+    """calc_gridding_fine on the device: C [2R, M] (float64) at offsets nu."""
+    h = cuda_tensor(h_ext, torch.float64)
+    k = cuda_tensor(kinv, torch.float64)
+    n = cuda_tensor(nu, torch.float64)
+    M = int(n.shape[0])
+    C = torch.empty((2 * R, M), dtype=torch.float64, device="cuda")
+    L.call("cg_szetan_gridding", _p(h), int(h.shape[0]), float(x0), int(R), _p(k), _p(n), M,
+           _p(C), stream())
+    return C
+
+
+def szetan_correction(C, R, x):
+    """calc_gridding_correction_fine's c / d on the device for coordinates x, from C
+    [2R, M] evaluated at nu_m = (m + 0.5) / (2M)."""
+    Ct = cuda_tensor(C, torch.float64)
+    xt = cuda_tensor(x, torch.float64)
+    nx = int(xt.numel())
+    out = torch.empty(nx, dtype=torch.float64, device="cuda")
+    nbytes = L.lib().cg_szetan_correction_workspace_bytes(int(R))
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    L.call("cg_szetan_correction", _p(Ct), int(R), int(Ct.shape[1]), _p(xt), nx, _p(out), _p(ws),
+           nbytes, stream())
+    return out

@@ -409,6 +409,26 @@ int cg_aw_kernels(const void *A_c128, int nA, int SA, const void *W_c128,
                   void *workspace, size_t workspace_bytes, int32_t *d_status,
                   cg_stream_t stream);
 
+/* ---------------------------------------------------------------- Sze-Tan
+ * Optimal gridding functions (crocodile/antialias.py).  All arrays are FP64
+ * device arrays; R is the half support (2R <= 32).
+ *
+ * calc_gridding_fine (antialias.py:189-213): C [2R, M] (row-major) of the
+ * gridding function at offsets nu [M], from h_ext = [1, h...] ([N+1],
+ * sampled at x0 * k / N) and kinv, the inverse of the 2R x 2R Gram matrix
+ * K[rp, r] = trap(h_ext^2 cos(2 pi (rp - r) x), x0 / N) (row-major). */
+int cg_szetan_gridding(const double *h_ext, int nh1, double x0, int R,
+                       const double *kinv, const double *nu, int M, double *C,
+                       cg_stream_t stream);
+
+/* calc_gridding_correction_fine (antialias.py:229-246): hfine[n] = c(x_n) /
+ * d(x_n) for nx coordinates x, from C [2R, M] evaluated at nu_m = (m + 0.5)
+ * / (2M).  Workspace: cg_szetan_correction_workspace_bytes(R) bytes. */
+size_t cg_szetan_correction_workspace_bytes(int R);
+int cg_szetan_correction(const double *C, int R, int M, const double *x,
+                         int nx, double *hfine, void *workspace,
+                         size_t workspace_bytes, cg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

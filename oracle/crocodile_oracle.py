@@ -635,3 +635,167 @@ def simulate_point(dist_uvw, l, m):
     """exp(-2 pi i (u l + v m + w (sqrt(1 - l^2 - m^2) - 1))) (simulate.py:210-230)."""
     s = numpy.array([l, m, numpy.sqrt(1 - l ** 2 - m ** 2) - 1.0])
     return numpy.exp(-2j * numpy.pi * numpy.dot(dist_uvw, s))
+
+
+# --------------------------------------------------------------------------
+# Sze-Tan optimal gridding functions (crocodile/antialias.py), loop for loop.
+# The reference reads its optimised h vectors from a json cache; these
+# functions take h explicitly.
+
+def sze_trap(vec, dx):
+    """antialias.py:22-24."""
+    return dx * (numpy.sum(vec) - 0.5 * (vec[0] + vec[-1]))
+
+
+def sze_gridder_as_C(h, x0, nu, R):
+    """calc_gridder_as_C (antialias.py:139-164): per offset, lstsq against the
+    Gram matrix with rcond 1e-14."""
+    M = len(nu)
+    C = numpy.zeros((2 * R, M))
+    K = numpy.zeros((2 * R, 2 * R))
+    N = len(h)
+    x = x0 * numpy.arange(0, N + 1, dtype=float) / N
+    dx = x0 / N
+    h_ext = numpy.concatenate(([1.0], h))
+    for rp in range(2 * R):
+        lp = rp - R + 1
+        for r in range(2 * R):
+            l = r - R + 1
+            K[rp, r] = sze_trap((h_ext ** 2) * numpy.cos(2 * numpy.pi * (lp - l) * x), dx)
+    rhs = numpy.zeros(2 * R)
+    for m, nu_val in enumerate(nu):
+        for rp in range(2 * R):
+            lp = rp - R + 1
+            rhs[rp] = sze_trap(h_ext * numpy.cos(2 * numpy.pi * (lp - nu_val) * x), dx)
+        C[:, m] = numpy.linalg.lstsq(K, rhs, 1e-14)[0]
+    return C
+
+
+def sze_func_to_min(h, x0, M, R):
+    """func_to_min (antialias.py:26-44)."""
+    N = len(h)
+    nu = (numpy.arange(M, dtype=float) + 0.5) / (2 * M)
+    x = x0 * numpy.arange(N + 1, dtype=float) / N
+    C = sze_gridder_as_C(h, x0, nu, R)
+    h_ext = numpy.concatenate(([1.0], h))
+    loss = numpy.zeros((len(h_ext), 2, M))
+    for n, x_val in enumerate(x):
+        one_app = 0
+        for r in range(2 * R):
+            l = r - R + 1
+            one_app += h_ext[n] * C[r, :] * numpy.exp(2j * numpy.pi * (l - nu) * x_val)
+        loss[n, 0, :] = 1.0 - numpy.real(one_app)
+        loss[n, 1, :] = numpy.imag(one_app)
+        if n in [0, N]:
+            loss[n, :, :] /= numpy.sqrt(2)
+    return loss.reshape(2 * M * (N + 1))
+
+
+def sze_gridding_fine(h, x0, nu, R):
+    """calc_gridding_fine (antialias.py:189-213): inverse Gram matrix."""
+    M = len(nu)
+    C = numpy.zeros((2 * R, M))
+    K = numpy.zeros((2 * R, 2 * R))
+    N = len(h)
+    x = x0 * numpy.arange(0, N + 1, dtype=float) / N
+    dx = x0 / N
+    h_ext = numpy.concatenate(([1.0], h))
+    for rp in range(2 * R):
+        lp = rp - R + 1
+        for r in range(2 * R):
+            l = r - R + 1
+            K[rp, r] = sze_trap((h_ext ** 2) * numpy.cos(2 * numpy.pi * (lp - l) * x), dx)
+    Kinv = numpy.linalg.inv(K)
+    rhs = numpy.zeros(2 * R)
+    for m, nu_val in enumerate(nu):
+        for rp in range(2 * R):
+            lp = rp - R + 1
+            rhs[rp] = sze_trap(h_ext * numpy.cos(2 * numpy.pi * (lp - nu_val) * x), dx)
+        C[:, m] = numpy.dot(Kinv, rhs)
+    return C
+
+
+def sze_gridding_correction_fine(x, h, x0, M, R):
+    """calc_gridding_correction_fine (antialias.py:229-246)."""
+    nu = (numpy.arange(M, dtype=float) + 0.5) / (2 * M)
+    C = sze_gridding_fine(h, x0, nu, R)
+    dnu = 1.0 / (2 * M)
+    c = numpy.zeros(numpy.shape(x))
+    d = numpy.zeros(numpy.shape(x))
+    for n, x_val in enumerate(x):
+        for rp in range(2 * R):
+            lp = rp - R + 1
+            for r in range(2 * R):
+                l = r - R + 1
+                d[n] += numpy.sum(C[rp, :] * C[r, :] * numpy.cos(2 * numpy.pi * (lp - l) * x_val)) \
+                    * dnu
+            c[n] += numpy.sum(C[rp, :] * numpy.cos(2 * numpy.pi * (lp - nu) * x_val)) * dnu
+    return c / d
+
+
+def sze_gridder(h, x0, nu, M, R):
+    """calc_gridder (antialias.py:176-187)."""
+    C = sze_gridder_as_C(h, x0, nu, R)
+    gridder = numpy.zeros(2 * M * R)
+    for m in range(M):
+        for rp in range(2 * R):
+            lp = rp - R + 1
+            indx = m - 2 * lp * M
+            if indx >= 0:
+                gridder[indx] = C[rp, m]
+            else:
+                gridder[-indx - 1] = C[rp, m]
+    return gridder
+
+
+def sze_gridder_to_C(gridder, R):
+    """gridder_to_C (antialias.py:215-227)."""
+    M = len(gridder) // (2 * R)
+    C = numpy.zeros((2 * R, M))
+    for r in range(2 * R):
+        l = r - R + 1
+        indx = numpy.arange(M) - 2 * M * l
+        indx[indx < 0] = -indx[indx < 0] - 1
+        C[r, :] = gridder[indx]
+    return C
+
+
+def sze_map_error(gridder, grid_correction, nu, x, R):
+    """calc_map_error (antialias.py:248-263)."""
+    M = len(nu) // (2 * R)
+    dnu = nu[1] - nu[0]
+    C = sze_gridder_to_C(gridder, R)
+    loss = numpy.zeros((len(x), 2, M))
+    for n, x_val in enumerate(x):
+        one_app = 0
+        for r in range(2 * R):
+            l = r - R + 1
+            one_app += grid_correction[n] * C[r, :] * numpy.exp(2j * numpy.pi * (l - nu[:M]) * x_val)
+        loss[n, 0, :] = 1.0 - numpy.real(one_app)
+        loss[n, 1, :] = numpy.imag(one_app)
+    map_error = numpy.zeros(len(x))
+    for i in range(len(x)):
+        map_error[i] = 2 * numpy.sum((loss[i, :, :].flatten()) ** 2) * dnu
+    return map_error
+
+
+def sze_mean_map_error(x0, N, M, R, h):
+    """calc_mean_map_error (antialias.py:265-271)."""
+    nu = (numpy.arange(2 * R * M, dtype=float) + 0.5) / (2 * M)
+    x = numpy.arange(N + 1, dtype=float) / (2 * N)
+    gridder = sze_gridder(h, x0, nu, M, R)
+    grid_correction = sze_gridding_correction_fine(x, h, x0, M, R)
+    map_err = sze_map_error(gridder, grid_correction, nu, x, R)
+    which = numpy.digitize(x0, x)
+    return numpy.sqrt(sze_trap(map_err[:which], 1.0 / (2 * N)) / x[which])
+
+
+def sze_tan_gridder(h, x0, R, over):
+    """sze_tan_gridder (antialias.py:299-306) for the cached (h, x0)."""
+    nu = numpy.arange(over, dtype=float) / over
+    return numpy.transpose(sze_gridding_fine(h, x0, nu, R)[::-1])
+
+
+def sze_tan_grid_correction_gen(h, x0, R, x):
+    """sze_tan_grid_correction_gen (antialias.py:285-297) for the cached (h, x0)."""
+    return 1 / sze_gridding_correction_fine(numpy.array(x), h, x0, len(x), R)
