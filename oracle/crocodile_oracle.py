@@ -799,3 +799,238 @@ def sze_tan_gridder(h, x0, R, over):
 def sze_tan_grid_correction_gen(h, x0, R, x):
     """sze_tan_grid_correction_gen (antialias.py:285-297) for the cached (h, x0)."""
     return 1 / sze_gridding_correction_fine(numpy.array(x), h, x0, len(x), R)
+
+
+# --------------------------------------------------------------------------
+# Facet <-> subgrid recombination (examples/notebooks/facet-subgrid-impl.ipynb,
+# examples/grid/recombine.c).  Two conventions:
+#   * centred (the notebook): arrays with their centre at n//2, transforms
+#     fft/ifft of this module;
+#   * raw (the C prototype): centre at index 0 (numpy.fft.ifftshift of the
+#     centred array), unnormalised FFTW transforms.
+
+def _pad_mid_axis(a, n, axis):
+    n0 = a.shape[axis]
+    if n == n0:
+        return a
+    pad = [(0, 0)] * a.ndim
+    pad[axis] = (n // 2 - n0 // 2, (n + 1) // 2 - (n0 + 1) // 2)
+    return numpy.pad(a, pad, mode='constant', constant_values=0.0)
+
+
+def _extract_mid_axis(a, n, axis):
+    c = a.shape[axis] // 2
+    idx = [slice(None)] * a.ndim
+    idx[axis] = slice(c - n // 2, c - n // 2 + n)
+    return a[tuple(idx)]
+
+
+def _fft_axis(a, axis, inverse=False):
+    f = numpy.fft.ifft if inverse else numpy.fft.fft
+    return numpy.fft.fftshift(f(numpy.fft.ifftshift(a, axis), axis=axis), axis)
+
+
+def _along(v, ndim, axis):
+    shape = [1] * ndim
+    shape[axis] = len(v)
+    return numpy.reshape(v, shape)
+
+
+class RecombineConfig:
+    """Sizes and the three PSWF-derived windows of the recombination
+    (facet-subgrid-impl.ipynb cells 11 and 14): Fb = 1 / the facet's PSWF,
+    Fn = the PSWF sampled at the xM rate, m0 = the truncated mask."""
+
+    def __init__(self, N, yB, yN, yP, xA, xM, xMxN_yP, pswf):
+        self.N, self.yB, self.yN, self.yP, self.xA, self.xM = N, yB, yN, yP, xA, xM
+        self.xMxN_yP = xMxN_yP
+        self.xM_yP = xM * yP // N
+        self.xM_yN = xM * yN // N
+        self.xM_step = N // xM
+        self.pswf = numpy.asarray(pswf, dtype=float)
+        self.Fb = 1 / extract_mid(self.pswf, yB)
+        self.Fn = self.pswf[(yN // 2) % self.xM_step::self.xM_step]
+        m0 = self.pswf * numpy.sinc(coordinates(yN) * xM / N * yN)
+        self.m0 = xM * yP / N * extract_mid(ifft(pad_mid(m0, yP)), xMxN_yP).real
+
+
+def rc_prepare_facet(cfg, facet, axis):
+    """b * F along one axis: multiply by Fb, pad to yP, inverse FFT (cell 24)."""
+    bf = _pad_mid_axis(facet * _along(cfg.Fb, facet.ndim, axis), cfg.yP, axis)
+    return _fft_axis(bf, axis, inverse=True)
+
+
+def rc_extract_subgrid(cfg, bf, subgrid_off, axis):
+    """n * m(b * F) along one axis for the subgrid at subgrid_off (grid cells):
+    window of xMxN_yP around the subgrid in the yP image, times m0, margins
+    folded onto xM_yP, FFT, middle xM_yN times Fn (cell 24)."""
+    xN_yP = cfg.xMxN_yP - cfg.xM_yP
+    mid = _extract_mid_axis(numpy.roll(bf, -subgrid_off * cfg.yP // cfg.N, axis), cfg.xMxN_yP,
+                            axis)
+    mbf = _along(cfg.m0, bf.ndim, axis) * mid
+    s = numpy.array(_extract_mid_axis(mbf, cfg.xM_yP, axis))
+    lo = [slice(None)] * bf.ndim
+    hi = [slice(None)] * bf.ndim
+    lo[axis] = slice(xN_yP // 2)
+    hi[axis] = slice(-xN_yP // 2, None)   # Python floor division, as the notebook writes it
+    s[tuple(lo)] += mbf[tuple(hi)]
+    s[tuple(hi)] += mbf[tuple(lo)]
+    return _along(cfg.Fn, bf.ndim, axis) * _extract_mid_axis(_fft_axis(s, axis), cfg.xM_yN, axis)
+
+
+def rc_facet_to_subgrids(cfg, facet, offs0, offs1):
+    """NMBF_NMBF[i0, i1] of one 2-D facet for subgrid offsets offs0 x offs1
+    (cell 29: axis 1 first, then axis 0)."""
+    out = numpy.empty((len(offs0), len(offs1), cfg.xM_yN, cfg.xM_yN), dtype=complex)
+    f_bf = rc_prepare_facet(cfg, facet, 1)
+    for i1, o1 in enumerate(offs1):
+        bf_nmbf = rc_prepare_facet(cfg, rc_extract_subgrid(cfg, f_bf, o1, 1), 0)
+        for i0, o0 in enumerate(offs0):
+            out[i0, i1] = rc_extract_subgrid(cfg, bf_nmbf, o0, 0)
+    return out
+
+
+def rc_add_facet(cfg, approx, nmbf, facet_off0, facet_off1):
+    """approx += nmbf padded to xM and rolled to the facet (cell 30)."""
+    approx += numpy.roll(pad_mid(nmbf, cfg.xM), (facet_off0 * cfg.xM // cfg.N,
+                                                 facet_off1 * cfg.xM // cfg.N), (0, 1))
+    return approx
+
+
+def rc_finish_subgrid(cfg, approx):
+    """The subgrid from its summed facet contributions: ifft, middle xA (cell 30)."""
+    return extract_mid(ifft(approx), cfg.xA)
+
+
+def rc_facet_to_subgrid_1d(cfg, facet, subgrid_off):
+    """1-D facet -> subgrid contribution RNjMiBjFj (cell 16)."""
+    return rc_extract_subgrid(cfg, rc_prepare_facet(cfg, facet, 0), subgrid_off, 0)
+
+
+def rc_split_subgrid(cfg, subgrid, facet_offs):
+    """FNjSi: the subgrid's FFT cut at each facet (cell 18, 1-D or 2-D)."""
+    fs = numpy.fft.fftshift(numpy.fft.fftn(numpy.fft.ifftshift(pad_mid(subgrid, cfg.xM))))
+    out = []
+    for fo in facet_offs:
+        shift = tuple(-f * cfg.xM // cfg.N for f in numpy.atleast_1d(fo))
+        out.append(extract_mid(numpy.roll(fs, shift, tuple(range(fs.ndim))), cfg.xM_yN))
+    return numpy.array(out)
+
+
+def rc_subgrid_to_facet_axis(cfg, fn, subgrid_off, axis):
+    """One subgrid's contribution to a facet along one axis (cell 18): Fn,
+    pad to xM_yP, inverse FFT, wrap onto xMxN_yP, m0, pad to yP, roll to the
+    subgrid, FFT, middle yB (Fb and the facet mask are applied by the caller
+    after the sum over subgrids)."""
+    xN_yP = cfg.xMxN_yP - cfg.xM_yP
+    nd = fn.ndim
+    mid = _fft_axis(_pad_mid_axis(_along(cfg.Fn, nd, axis) * fn, cfg.xM_yP, axis), axis,
+                    inverse=True)
+    shape = list(fn.shape)
+    shape[axis] = cfg.xMxN_yP
+    nj = numpy.zeros(shape, dtype=complex)
+    c = cfg.xMxN_yP // 2
+    idx = [slice(None)] * nd
+    idx[axis] = slice(c - cfg.xM_yP // 2, c - cfg.xM_yP // 2 + cfg.xM_yP)
+    nj[tuple(idx)] = mid
+    lo = [slice(None)] * nd
+    hi = [slice(None)] * nd
+    lo[axis] = slice(xN_yP // 2)
+    hi[axis] = slice(-xN_yP // 2, None)
+    # the margins wrap: NjSi[-xN//2:] = mid[:xN//2], NjSi[:xN//2] = mid[-xN//2:]
+    nj[tuple(hi)] = mid[tuple(lo)]
+    nj[tuple(lo)] = mid[tuple(hi)]
+    p = _pad_mid_axis(_along(cfg.m0, nd, axis) * nj, cfg.yP, axis)
+    p = numpy.roll(p, subgrid_off * cfg.yP // cfg.N, axis)
+    return _extract_mid_axis(_fft_axis(p, axis), cfg.yB, axis)
+
+
+def rc_subgrids_to_facet(cfg, fnjsi, offs0, offs1):
+    """Facet approximation (before Fb and the facet mask) from the FNjSi of
+    subgrids at offs0 x offs1 for one facet: axis 1 per subgrid, summed over
+    i1, then axis 0 per row of subgrids, summed over i0 (the 2-D form of cell
+    18 by separability).  fnjsi: [n0, n1, xM_yN, xM_yN]."""
+    acc = numpy.zeros((cfg.yB, cfg.yB), dtype=complex)
+    for i0, o0 in enumerate(offs0):
+        row = numpy.zeros((cfg.xM_yN, cfg.yB), dtype=complex)
+        for i1, o1 in enumerate(offs1):
+            row += rc_subgrid_to_facet_axis(cfg, fnjsi[i0, i1], o1, 1)
+        acc += rc_subgrid_to_facet_axis(cfg, row, o0, 0)
+    return acc
+
+
+# raw convention: the C prototype's primitives (examples/grid/recombine.c)
+
+def rc_generate_Fb(yB, pswf_raw):
+    """generate_Fb (recombine.c:12-22)."""
+    Fb = numpy.empty(yB)
+    for i in range(yB // 2 + 1):
+        Fb[i] = 1 / pswf_raw[i]
+    for i in range(yB // 2 + 1, yB):
+        Fb[i] = Fb[yB - i]
+    return Fb
+
+
+def rc_generate_Fn(yN, xM_yN, pswf_raw):
+    """generate_Fn (recombine.c:24-33)."""
+    assert yN % xM_yN == 0
+    step = yN // xM_yN
+    return numpy.array([pswf_raw[i * step] for i in range(xM_yN)])
+
+
+def rc_generate_m(image_size, yP, yN, xM, xMxN_yP, pswf_raw):
+    """generate_m (recombine.c:35-67): the sinc-truncated PSWF, DCT-I of
+    length yP/2+1 (FFTW REDFT00: Y_k = X_0 + (-1)^k X_{n-1} + 2 sum X_j
+    cos(pi j k / (n-1))), mirrored to xMxN_yP."""
+    n = yP // 2 + 1
+    m = numpy.zeros(n)
+    m[0] = pswf_raw[0] * xM / image_size
+    for i in range(1, yN // 2):
+        x = i * xM / image_size
+        m[i] = pswf_raw[i] * (numpy.sin(x * numpy.pi) / x / numpy.pi) * xM / image_size
+    j = numpy.arange(1, n - 1)
+    y = numpy.array([m[0] + (-1) ** k * m[n - 1] + 2 * numpy.sum(m[1:n - 1] *
+                     numpy.cos(numpy.pi * j * k / (n - 1))) for k in range(n)])
+    out = numpy.empty(xMxN_yP)
+    for i in range(xMxN_yP // 2 + 1):
+        out[i] = y[i]
+    for i in range(xMxN_yP // 2 + 1, xMxN_yP):
+        out[i] = y[xMxN_yP - i]
+    return out
+
+
+def rc_prepare_facet_raw(yB, yP, Fb, facet):
+    """prepare_facet (recombine.c:69-85) then FFTW_BACKWARD of length yP."""
+    bf = numpy.zeros(yP, dtype=complex)
+    for i in range(yB // 2):
+        bf[i] = Fb[i] * facet[i] / yP
+    for i in range(yP - yB // 2, yP):
+        bf[i] = Fb[yB - yP + i] * facet[yB - yP + i] / yP
+    return numpy.fft.ifft(bf) * yP
+
+
+def rc_extract_subgrid_raw(yP, xM_yP, xMxN_yP, xM_yN, subgrid_offset, m_trunc, Fn, bf):
+    """extract_subgrid (recombine.c:87-119); subgrid_offset in yP samples."""
+    xN_yP = xMxN_yP - xM_yP
+    off = subgrid_offset + 2 * yP
+    mbf = numpy.zeros(xM_yP, dtype=complex)
+    for i in range(xM_yP):
+        if i < (xMxN_yP + 1) // 2:
+            mbf[i] += m_trunc[i] * bf[(i + off) % yP]
+        if i >= xM_yP - xMxN_yP // 2:
+            mbf[i] += m_trunc[xN_yP + i] * bf[(i + off - xM_yP) % yP]
+    mbf = numpy.fft.fft(mbf)
+    nmbf = numpy.empty(xM_yN, dtype=complex)
+    for i in range(xM_yN // 2):
+        nmbf[i] = mbf[i] * Fn[i]
+    for i in range(xM_yN // 2, xM_yN):
+        nmbf[i] = mbf[xM_yP - xM_yN + i] * Fn[i]
+    return nmbf
+
+
+def rc_add_facet_raw(xM, xM_yN, facet_offset, nmbf, out):
+    """add_facet (recombine.c:122-133); facet_offset in xM samples."""
+    off = facet_offset + 2 * xM
+    for i in range(xM_yN):
+        out[(i - xM_yN // 2 + off) % xM] += nmbf[(i + xM_yN // 2) % xM_yN] / xM
+    return out
