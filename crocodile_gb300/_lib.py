@@ -80,6 +80,15 @@ SIGNATURES = {
     "cg_szetan_gridding": (c_int, [P, c_int, c_double, c_int, P, P, c_int, P, P]),
     "cg_szetan_correction_workspace_bytes": (c_size_t, [c_int]),
     "cg_szetan_correction": (c_int, [P, c_int, c_int, P, c_int, P, P, c_size_t, P]),
+    "cg_recombine_create": (c_int, [c_int, c_int, P, c_int, c_int, c_int, c_int, c_int, c_int,
+                                    P]),
+    "cg_recombine_destroy": (c_int, [P]),
+    "cg_recombine_sizes": (c_int, [P, P]),
+    "cg_recombine_windows": (c_int, [P, P, P, P]),
+    "cg_recombine_workspace_bytes": (c_size_t, [P, c_int, c_int]),
+    "cg_recombine_facet_to_subgrids": (c_int, [P, P, c_int, P, c_int, P, c_int, P, c_int, P,
+                                               c_size_t, P, P]),
+    "cg_recombine_add_facet": (c_int, [P, P, c_int, c_int, c_int, c_int, P, P]),
     "cg_plan_destroy": (c_int, [P]),
     "cg_set_tuning": (c_int, [ctypes.POINTER(Tuning)]),
     "cg_get_tuning": (c_int, [ctypes.POINTER(Tuning)]),

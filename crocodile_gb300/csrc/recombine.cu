@@ -1,0 +1,518 @@
+// Facet -> subgrid recombination (examples/grid/recombine.c, the 2-D
+// algorithm of examples/notebooks/facet-subgrid-impl.ipynb cells 24-30).
+//
+// One facet [yB, yB] becomes the contributions NMBF_NMBF[i0][i1]
+// [xM_yN, xM_yN] to every requested subgrid in one call:
+//   1. k_rc_prep_rows   : BF[r][k] = Fb[t] F[r][t] / yP, zero-padded to yP
+//                         (prepare_facet along axis 1; rows leave in raw order)
+//      inverse FFT of yB rows of length yP
+//   2. k_rc_window      : per subgrid column offset, the xMxN_yP samples around
+//                         it times m, margins folded onto xM_yP (extract_subgrid)
+//      forward FFT of n1 * yB rows of length xM_yP
+//   3. k_rc_crop_prep_T : crop to xM_yN times Fn, transpose, prepare_facet along
+//                         axis 0 (times Fb, zero-pad to yP), via a 32x32 tile
+//      inverse FFT of n1 * xM_yN rows of length yP
+//   4. k_rc_window      : per subgrid row offset, as 2.
+//      forward FFT of n0 * n1 * xM_yN rows of length xM_yP
+//   5. k_rc_crop_T      : crop times Fn, transpose to [i0][i1][axis 0][axis 1]
+// Every FFT runs over contiguous rows, complex128 as the reference.  Arrays
+// are in the C prototype's raw
+// layout (centre at index 0, FFTW sign conventions: backward = e^{+2 pi i},
+// unnormalised) except where a `centred` flag maps the facet in or the
+// result out in numpy's fftshift layout (the notebook's).
+//
+// k_rc_add_facet is recombine2d_af0_af1 (recombine.c:504-544): the facet's
+// contribution rolled to the facet offset and added into the subgrid,
+// divided by xM^2 in the raw form (an unnormalised backward FFT follows);
+// the centred form is the notebook's `approx += roll(pad_mid(...))`
+// (a normalised centred ifft follows).
+
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "cg_internal.cuh"
+
+namespace cg {
+int fft_plan(int batch, int H, int W, cufftType type, cufftHandle *out);
+}
+
+struct cg_recombine {
+  int N, subgrid_spacing, facet_spacing;
+  int yB, yN, yP, xA, xM, xMxN_yP;
+  int xM_yP, xM_yN, yP_spacing, xM_spacing;
+  double *d_Fb, *d_Fn, *d_m;
+};
+
+namespace {
+
+using namespace cg;
+
+__host__ __device__ inline int pmod(long long a, int n) {
+  long long r = a % n;
+  return (int)(r < 0 ? r + n : r);
+}
+
+template <typename C>
+struct RT;
+template <>
+struct RT<double2> {
+  typedef double R;
+};
+
+template <typename C>
+__device__ __forceinline__ C cscale(C a, typename RT<C>::R s) {
+  a.x *= s;
+  a.y *= s;
+  return a;
+}
+
+template <typename C>
+__device__ __forceinline__ C czero() {
+  C z;
+  z.x = 0;
+  z.y = 0;
+  return z;
+}
+
+// prepare_facet along the rows: out[r][k], k < yP.  With `centred`, the input
+// facet is in fftshift layout on both axes and row r of the output is raw row r.
+template <typename C>
+__global__ void k_rc_prep_rows(const C *__restrict__ in, int rows, int yB, int yP,
+                               const typename RT<C>::R *__restrict__ Fb, int centred,
+                               C *__restrict__ out) {
+  typedef typename RT<C>::R R;
+  const int h = yB / 2;
+  const size_t total = (size_t)rows * yP;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e / yP), k = (int)(e % yP);
+    int t = -1;
+    if (k < h)
+      t = k;
+    else if (k >= yP - h)
+      t = k - yP + yB;
+    C v = czero<C>();
+    if (t >= 0) {
+      const int rs = centred ? (r + h) % yB : r;
+      const int ts = centred ? (t + h) % yB : t;
+      v = cscale(in[(size_t)rs * yB + ts], Fb[t] / (R)yP);
+    }
+    out[e] = v;
+  }
+}
+
+// Subgrid offsets in grid cells -> yP samples; an offset that is not a
+// multiple of the subgrid spacing is counted as an index error and taken as 0.
+__global__ void k_rc_offsets(const int32_t *__restrict__ off0, int n0,
+                             const int32_t *__restrict__ off1, int n1, int spacing,
+                             int yP_spacing, int yP, int32_t *__restrict__ out,
+                             int32_t *status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n0 + n1) return;
+  const int o = i < n0 ? off0[i] : off1[i - n0];
+  if (pmod(o, spacing) != 0) {
+    atomicAdd(&status[ST_INDEX], 1);
+    out[i] = 0;
+    return;
+  }
+  out[i] = pmod((long long)(o - pmod(o, spacing)) / spacing * yP_spacing, yP);
+}
+
+// extract_subgrid's window: out[o][r][i] from row r of bf at offset offs[o]
+// (in yP samples).
+template <typename C>
+__global__ void k_rc_window(const C *__restrict__ bf, int rows, int yP,
+                            const int32_t *__restrict__ offs, int noff, int xM_yP, int xMxN_yP,
+                            const typename RT<C>::R *__restrict__ m, C *__restrict__ out) {
+  const int xN_yP = xMxN_yP - xM_yP;
+  const size_t total = (size_t)noff * rows * xM_yP;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % xM_yP);
+    const size_t orow = e / xM_yP;
+    const int r = (int)(orow % rows);
+    const int off = offs[orow / rows];
+    const C *row = bf + (size_t)r * yP;
+    C v = czero<C>();
+    if (i < (xMxN_yP + 1) / 2) {
+      const C b = row[pmod((long long)i + off, yP)];
+      const typename RT<C>::R w = m[i];
+      v.x += w * b.x;
+      v.y += w * b.y;
+    }
+    if (i >= xM_yP - xMxN_yP / 2) {
+      const C b = row[pmod((long long)i + off - xM_yP, yP)];
+      const typename RT<C>::R w = m[xN_yP + i];
+      v.x += w * b.x;
+      v.y += w * b.y;
+    }
+    out[e] = v;
+  }
+}
+
+__device__ __forceinline__ int crop_src(int c, int xM_yN, int xM_yP) {
+  return c < xM_yN / 2 ? c : xM_yP - xM_yN + c;
+}
+
+// Crop (times Fn) along the rows of mbf [n1][yB][xM_yP], transpose and
+// prepare along the former row axis: out[i1][c][k], k < yP.
+// Block: 32 x 8 threads; tile of 32 columns c by 32 output positions k.
+template <typename C>
+__global__ void k_rc_crop_prep_T(const C *__restrict__ mbf, int yB, int xM_yP, int xM_yN,
+                                 const typename RT<C>::R *__restrict__ Fn,
+                                 const typename RT<C>::R *__restrict__ Fb, int yP,
+                                 C *__restrict__ out) {
+  typedef typename RT<C>::R R;
+  __shared__ C tile[32][33];
+  const int i1 = blockIdx.z;
+  const int c0 = blockIdx.y * 32;
+  const int k0 = blockIdx.x * 32;
+  const int h = yB / 2;
+  const C *src = mbf + (size_t)i1 * yB * xM_yP;
+  // load: tile[kk][cc] = Fb[t] Fn[c] mbf[t][crop(c)] / yP for k = k0 + kk
+  for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
+    const int k = k0 + kk;
+    const int c = c0 + threadIdx.x;
+    int t = -1;
+    if (k < yP) {
+      if (k < h)
+        t = k;
+      else if (k >= yP - h)
+        t = k - yP + yB;
+    }
+    C v = czero<C>();
+    if (t >= 0 && c < xM_yN)
+      v = cscale(src[(size_t)t * xM_yP + crop_src(c, xM_yN, xM_yP)], Fn[c] * Fb[t] / (R)yP);
+    tile[kk][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int cc = threadIdx.y; cc < 32; cc += blockDim.y) {
+    const int c = c0 + cc;
+    const int k = k0 + threadIdx.x;
+    if (c < xM_yN && k < yP) out[((size_t)i1 * xM_yN + c) * yP + k] = tile[threadIdx.x][cc];
+  }
+}
+
+// Final crop (times Fn) along the rows of mbf2 [n0][n1][xM_yN (axis 1)][xM_yP]
+// and transpose: out[i0][i1][a0][a1].  With `centred`, both output axes in
+// fftshift layout.
+template <typename C>
+__global__ void k_rc_crop_T(const C *__restrict__ mbf2, int n1, int xM_yP, int xM_yN,
+                            const typename RT<C>::R *__restrict__ Fn, int centred,
+                            C *__restrict__ out) {
+  __shared__ C tile[32][33];
+  const int pair = blockIdx.z;  // i0 * n1 + i1
+  const int a10 = blockIdx.y * 32;
+  const int a00 = blockIdx.x * 32;
+  const C *src = mbf2 + (size_t)pair * xM_yN * xM_yP;
+  for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+    const int a1 = a10 + yy;
+    const int a0 = a00 + threadIdx.x;
+    C v = czero<C>();
+    if (a1 < xM_yN && a0 < xM_yN)
+      v = cscale(src[(size_t)a1 * xM_yP + crop_src(a0, xM_yN, xM_yP)], Fn[a0]);
+    tile[yy][threadIdx.x] = v;
+  }
+  __syncthreads();
+  const int h = xM_yN / 2;
+  C *dst = out + (size_t)pair * xM_yN * xM_yN;
+  for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+    const int a0 = a00 + yy;
+    const int a1 = a10 + threadIdx.x;
+    if (a0 < xM_yN && a1 < xM_yN) {
+      const int d0 = centred ? (a0 + h) % xM_yN : a0;
+      const int d1 = centred ? (a1 + h) % xM_yN : a1;
+      dst[(size_t)d0 * xM_yN + d1] = tile[threadIdx.x][yy];
+    }
+  }
+}
+
+// subgrids[s] += nmbf[s] rolled to (fo0, fo1) (in xM samples).  Raw: both in
+// raw layout, divided by xM^2; centred: both in fftshift layout, unscaled.
+template <typename C>
+__global__ void k_rc_add_facet(const C *__restrict__ nmbf, int xM_yN, int xM, int fo0, int fo1,
+                               int centred, C *__restrict__ sub) {
+  typedef typename RT<C>::R R;
+  const int j1 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j0 = blockIdx.y;
+  const int s = blockIdx.z;
+  if (j1 >= xM_yN || j0 >= xM_yN) return;
+  const int h = xM_yN / 2;
+  // j is the frequency index offset by h: signed frequency f = j - h
+  int src0, src1, dst0, dst1;
+  if (centred) {
+    src0 = j0;
+    src1 = j1;
+    // pad_mid puts centred index j at xM/2 - h + j; roll adds the facet offset
+    dst0 = pmod((long long)xM / 2 - h + j0 + fo0, xM);
+    dst1 = pmod((long long)xM / 2 - h + j1 + fo1, xM);
+  } else {
+    src0 = (j0 + h) % xM_yN;
+    src1 = (j1 + h) % xM_yN;
+    dst0 = pmod((long long)j0 - h + fo0, xM);
+    dst1 = pmod((long long)j1 - h + fo1, xM);
+  }
+  C v = nmbf[((size_t)s * xM_yN + src0) * xM_yN + src1];
+  if (!centred) v = cscale(v, (R)1 / ((R)xM * (R)xM));
+  C *d = sub + ((size_t)s * xM + dst0) * xM + dst1;
+  C a = *d;
+  a.x += v.x;
+  a.y += v.y;
+  *d = a;
+}
+
+// ------------------------------------------------------------------ host side
+
+template <typename C>
+struct Prec;
+template <>
+struct Prec<double2> {
+  static constexpr cufftType type = CUFFT_Z2Z;
+  static cufftResult exec(cufftHandle p, double2 *d, int dir) {
+    return cufftExecZ2Z(p, (cufftDoubleComplex *)d, (cufftDoubleComplex *)d, dir);
+  }
+  static const double *Fb(const cg_recombine *h) { return h->d_Fb; }
+  static const double *Fn(const cg_recombine *h) { return h->d_Fn; }
+  static const double *m(const cg_recombine *h) { return h->d_m; }
+  // complex128 only: Fb = 1 / PSWF spans many decades at the facet edge
+  // (6.4e6 for the 512 / 128 / 140 test set), and the contributions come out
+  // of intermediates 1e3 times larger than their peak, so single-precision
+  // FFTs lose 1e-3 of the result (measured) where the method delivers 1e-7.
+};
+
+template <typename C>
+int rows_fft(C *data, int batch, int len, int dir, cudaStream_t st) {
+  cufftHandle plan;
+  int rc = fft_plan(batch, 1, len, Prec<C>::type, &plan);
+  if (rc) return rc;
+  if (cufftSetStream(plan, st) != CUFFT_SUCCESS)
+    return set_error(CG_ERR_CUDA, "cufftSetStream failed");
+  const cufftResult r = Prec<C>::exec(plan, data, dir);
+  return r == CUFFT_SUCCESS ? CG_OK : set_error(CG_ERR_CUDA, "cufftExec failed: %d", (int)r);
+}
+
+inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// grid-stride launches: enough 256-thread blocks to fill the GPU a few times
+inline unsigned grid_for(size_t n) {
+  const size_t want = (n + 255) / 256;
+  return (unsigned)std::max<size_t>(1, std::min<size_t>(want, (size_t)num_sms() * 16));
+}
+
+struct WsLayout {
+  size_t bf, mbf, bf2, mbf2, offs, total;
+};
+
+WsLayout ws_layout(const cg_recombine *h, int n0, int n1) {
+  const size_t e = sizeof(double2);
+  WsLayout L;
+  L.bf = 0;
+  L.mbf = L.bf + align256((size_t)h->yB * h->yP * e);
+  L.bf2 = L.mbf + align256((size_t)n1 * h->yB * h->xM_yP * e);
+  L.mbf2 = L.bf2 + align256((size_t)n1 * h->xM_yN * h->yP * e);
+  L.offs = L.mbf2 + align256((size_t)n0 * n1 * h->xM_yN * h->xM_yP * e);
+  L.total = L.offs + align256((size_t)(n0 + n1) * sizeof(int32_t));
+  return L;
+}
+
+template <typename C>
+int facet_to_subgrids(cg_recombine *h, const void *facet, int centred, int n0, int n1,
+                      void *nmbf, int out_centred, char *ws, const WsLayout &L,
+                      cudaStream_t st) {
+  C *bf = (C *)(ws + L.bf);
+  C *mbf = (C *)(ws + L.mbf);
+  C *bf2 = (C *)(ws + L.bf2);
+  C *mbf2 = (C *)(ws + L.mbf2);
+  const int32_t *offs0 = (const int32_t *)(ws + L.offs);
+  const int32_t *offs1 = offs0 + n0;
+  const int yB = h->yB, yP = h->yP, xM_yP = h->xM_yP, xM_yN = h->xM_yN;
+  int rc;
+  const unsigned g1 = grid_for((size_t)yB * yP);
+  k_rc_prep_rows<C><<<g1, 256, 0, st>>>((const C *)facet, yB, yB, yP, Prec<C>::Fb(h), centred,
+                                         bf);
+  CG_LAUNCH("recombine prepare facet (axis 1)");
+  if ((rc = rows_fft<C>(bf, yB, yP, CUFFT_INVERSE, st))) return rc;
+  k_rc_window<C><<<grid_for((size_t)n1 * yB * xM_yP), 256, 0, st>>>(
+      bf, yB, yP, offs1, n1, xM_yP, h->xMxN_yP, Prec<C>::m(h), mbf);
+  CG_LAUNCH("recombine extract subgrid (axis 1)");
+  if ((rc = rows_fft<C>(mbf, n1 * yB, xM_yP, CUFFT_FORWARD, st))) return rc;
+  k_rc_crop_prep_T<C><<<dim3((yP + 31) / 32, (xM_yN + 31) / 32, n1), dim3(32, 8), 0, st>>>(
+      mbf, yB, xM_yP, xM_yN, Prec<C>::Fn(h), Prec<C>::Fb(h), yP, bf2);
+  CG_LAUNCH("recombine prepare facet (axis 0)");
+  if ((rc = rows_fft<C>(bf2, n1 * xM_yN, yP, CUFFT_INVERSE, st))) return rc;
+  k_rc_window<C><<<grid_for((size_t)n0 * n1 * xM_yN * xM_yP), 256, 0, st>>>(
+      bf2, n1 * xM_yN, yP, offs0, n0, xM_yP, h->xMxN_yP, Prec<C>::m(h), mbf2);
+  CG_LAUNCH("recombine extract subgrid (axis 0)");
+  if ((rc = rows_fft<C>(mbf2, n0 * n1 * xM_yN, xM_yP, CUFFT_FORWARD, st))) return rc;
+  k_rc_crop_T<C><<<dim3((xM_yN + 31) / 32, (xM_yN + 31) / 32, n0 * n1), dim3(32, 8), 0, st>>>(
+      mbf2, n1, xM_yP, xM_yN, Prec<C>::Fn(h), out_centred, (C *)nmbf);
+  CG_LAUNCH("recombine crop");
+  return CG_OK;
+}
+
+// generate_m (recombine.c:35-67): the PSWF times the sinc of the xM box, then
+// the DCT-I of length yP/2 + 1 (X_j = 0 from yN/2 on), mirrored to xMxN_yP.
+std::vector<double> generate_m(int N, int yP, int yN, int xM, int xMxN_yP, const double *pswf) {
+  const int n = yP / 2 + 1;
+  std::vector<double> X(n, 0.0);
+  X[0] = pswf[0] * xM / N;
+  for (int i = 1; i < yN / 2 && i < n; ++i) {
+    const double x = (double)i * xM / N;
+    X[i] = pswf[i] * (std::sin(x * M_PI) / x / M_PI) * xM / N;
+  }
+  const int half = xMxN_yP / 2;
+  std::vector<double> Y(half + 1);
+  for (int k = 0; k <= half; ++k) {
+    double s = X[0] + ((k & 1) ? -X[n - 1] : X[n - 1]);
+    for (int j = 1; j < n - 1; ++j)
+      if (X[j] != 0.0) s += 2 * X[j] * std::cos(M_PI * (double)j * k / (double)(n - 1));
+    Y[k] = s;
+  }
+  std::vector<double> m(xMxN_yP);
+  for (int i = 0; i <= half; ++i) m[i] = Y[i];
+  for (int i = half + 1; i < xMxN_yP; ++i) m[i] = Y[xMxN_yP - i];
+  return m;
+}
+
+int upload(const std::vector<double> &v, double **d) {
+  CG_CUDA(cudaMalloc(d, v.size() * sizeof(double)));
+  CG_CUDA(cudaMemcpy(*d, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return CG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cg_recombine_create(int image_size, int subgrid_spacing, const double *pswf, int yB, int yN,
+                        int yP, int xA, int xM, int xMxN_yP, cg_recombine **out) {
+  CG_REQUIRE(out && pswf, "bad recombine_create arguments");
+  *out = nullptr;
+  CG_REQUIRE(image_size > 0 && subgrid_spacing > 0 && yB > 0 && yN > 0 && yP > 0 && xA > 0 &&
+                 xM > 0 && xMxN_yP > 0,
+             "recombine sizes must be positive");
+  // the side conditions of recombine2d_set_config (recombine.c:139-172)
+  CG_REQUIRE(image_size % subgrid_spacing == 0, "image_size %% subgrid_spacing != 0");
+  const int facet_spacing = image_size / subgrid_spacing;
+  CG_REQUIRE(image_size % xM == 0, "image_size %% xM_size != 0");
+  const int xM_step = image_size / xM;
+  CG_REQUIRE(facet_spacing % xM_step == 0, "facet spacing not a multiple of image/xM");
+  CG_REQUIRE(((long long)subgrid_spacing * yP) % image_size == 0,
+             "subgrid_spacing * yP_size not a multiple of image_size");
+  CG_REQUIRE(yB % facet_spacing == 0, "yB_size not a multiple of the facet spacing");
+  CG_REQUIRE(xA % subgrid_spacing == 0, "xA_size not a multiple of subgrid_spacing");
+  CG_REQUIRE(((long long)xM * yP) % image_size == 0, "xM_size * yP_size not a multiple of image");
+  CG_REQUIRE(((long long)xM * yN) % image_size == 0, "xM_size * yN_size not a multiple of image");
+  const int xM_yP = (int)((long long)xM * yP / image_size);
+  const int xM_yN = (int)((long long)xM * yN / image_size);
+  CG_REQUIRE(yN % xM_yN == 0, "yN_size not a multiple of xM_yN_size");  // generate_Fn
+  CG_REQUIRE((xMxN_yP - xM_yP) % 2 == 0 && xMxN_yP >= xM_yP && xMxN_yP <= 2 * xM_yP,
+             "xMxN_yP_size - xM_yP_size must be even, xM_yP <= xMxN_yP <= 2 xM_yP");
+  CG_REQUIRE(yB % 2 == 0 && xM_yN % 2 == 0 && yB <= yP && yB <= yN && xM_yN <= xM_yP &&
+                 xM_yN <= xM,
+             "need even yB, xM_yN and yB <= yP, yN; xM_yN <= xM_yP, xM");
+  cg_recombine *h = new cg_recombine();
+  h->N = image_size;
+  h->subgrid_spacing = subgrid_spacing;
+  h->facet_spacing = facet_spacing;
+  h->yB = yB;
+  h->yN = yN;
+  h->yP = yP;
+  h->xA = xA;
+  h->xM = xM;
+  h->xMxN_yP = xMxN_yP;
+  h->xM_yP = xM_yP;
+  h->xM_yN = xM_yN;
+  h->yP_spacing = (int)((long long)subgrid_spacing * yP / image_size);
+  h->xM_spacing = (int)((long long)facet_spacing * xM / image_size);
+  // generate_Fb / generate_Fn (recombine.c:12-33) from the raw PSWF [yN]
+  std::vector<double> Fb(yB), Fn(xM_yN);
+  for (int i = 0; i <= yB / 2; ++i) Fb[i] = 1 / pswf[i];
+  for (int i = yB / 2 + 1; i < yB; ++i) Fb[i] = Fb[yB - i];
+  for (int i = 0; i < xM_yN; ++i) Fn[i] = pswf[(size_t)i * (yN / xM_yN)];
+  const std::vector<double> m = generate_m(image_size, yP, yN, xM, xMxN_yP, pswf);
+  int rc;
+  if ((rc = upload(Fb, &h->d_Fb)) || (rc = upload(Fn, &h->d_Fn)) || (rc = upload(m, &h->d_m))) {
+    cg_recombine_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return CG_OK;
+}
+
+int cg_recombine_destroy(cg_recombine *h) {
+  if (!h) return CG_OK;
+  cudaFree(h->d_Fb);
+  cudaFree(h->d_Fn);
+  cudaFree(h->d_m);
+  delete h;
+  return CG_OK;
+}
+
+int cg_recombine_sizes(const cg_recombine *h, int32_t *sizes) {
+  CG_REQUIRE(h && sizes, "bad recombine_sizes arguments");
+  sizes[0] = h->xM_yP;
+  sizes[1] = h->xM_yN;
+  sizes[2] = h->facet_spacing;
+  sizes[3] = h->yP_spacing;
+  sizes[4] = h->xM_spacing;
+  return CG_OK;
+}
+
+int cg_recombine_windows(const cg_recombine *h, double *Fb, double *Fn, double *m) {
+  CG_REQUIRE(h, "bad recombine_windows arguments");
+  if (Fb) CG_CUDA(cudaMemcpy(Fb, h->d_Fb, h->yB * sizeof(double), cudaMemcpyDeviceToHost));
+  if (Fn) CG_CUDA(cudaMemcpy(Fn, h->d_Fn, h->xM_yN * sizeof(double), cudaMemcpyDeviceToHost));
+  if (m) CG_CUDA(cudaMemcpy(m, h->d_m, h->xMxN_yP * sizeof(double), cudaMemcpyDeviceToHost));
+  return CG_OK;
+}
+
+size_t cg_recombine_workspace_bytes(const cg_recombine *h, int n0, int n1) {
+  if (!h || n0 < 0 || n1 < 0) return 0;
+  return ws_layout(h, n0, n1).total;
+}
+
+int cg_recombine_facet_to_subgrids(cg_recombine *h, const void *facet, int centred,
+                                   const int32_t *subgrid_off0, int n0,
+                                   const int32_t *subgrid_off1, int n1, void *nmbf,
+                                   int out_centred, void *ws, size_t ws_bytes, int32_t *d_status,
+                                   cg_stream_t stream) {
+  CG_REQUIRE(h && facet && d_status && n0 >= 0 && n1 >= 0,
+             "bad recombine_facet_to_subgrids arguments");
+  if (n0 == 0 || n1 == 0) return CG_OK;
+  CG_REQUIRE(nmbf && subgrid_off0 && subgrid_off1, "bad recombine_facet_to_subgrids arguments");
+  CG_REQUIRE(n1 <= 65535 && (long long)n0 * n1 <= 65535,
+             "at most 65535 subgrids (n0 * n1) per call; split the offsets");
+  const WsLayout L = ws_layout(h, n0, n1);
+  if (!ws || ws_bytes < L.total)
+    return set_error(CG_ERR_WORKSPACE, "recombine needs %zu workspace bytes", L.total);
+  cudaStream_t st = (cudaStream_t)stream;
+  char *w = (char *)ws;
+  k_rc_offsets<<<(n0 + n1 + 255) / 256, 256, 0, st>>>(subgrid_off0, n0, subgrid_off1, n1,
+                                                      h->subgrid_spacing, h->yP_spacing, h->yP,
+                                                      (int32_t *)(w + L.offs), d_status);
+  CG_LAUNCH("recombine offsets");
+  return facet_to_subgrids<double2>(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
+}
+
+int cg_recombine_add_facet(const cg_recombine *h, const void *nmbf, int n, int facet_off0,
+                           int facet_off1, int centred, void *subgrids, cg_stream_t stream) {
+  CG_REQUIRE(h && n >= 0 && (n == 0 || (nmbf && subgrids)), "bad recombine_add_facet arguments");
+  if (n == 0) return CG_OK;
+  CG_REQUIRE(pmod(facet_off0, h->facet_spacing) == 0 && pmod(facet_off1, h->facet_spacing) == 0,
+             "facet offsets must be multiples of the facet spacing %d", h->facet_spacing);
+  CG_REQUIRE(n <= 65535, "too many subgrids for one call");
+  const int fo0 = facet_off0 / h->facet_spacing * h->xM_spacing;
+  const int fo1 = facet_off1 / h->facet_spacing * h->xM_spacing;
+  const dim3 grid((h->xM_yN + 127) / 128, h->xM_yN, n);
+  cudaStream_t st = (cudaStream_t)stream;
+  k_rc_add_facet<double2><<<grid, 128, 0, st>>>((const double2 *)nmbf, h->xM_yN, h->xM, fo0, fo1,
+                                                centred, (double2 *)subgrids);
+  CG_LAUNCH("recombine add facet");
+  return CG_OK;
+}
+
+}  // extern "C"

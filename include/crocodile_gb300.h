@@ -429,6 +429,46 @@ int cg_szetan_correction(const double *C, int R, int M, const double *x,
                          int nx, double *hfine, void *workspace,
                          size_t workspace_bytes, cg_stream_t stream);
 
+/* ---------------------------------------------------------------- facets
+ * Facet -> subgrid recombination (examples/grid/recombine.h/.c; the 2-D
+ * algorithm of examples/notebooks/facet-subgrid-impl.ipynb cells 24-30).
+ * Layout: the C prototype's raw layout (centre at index 0, as numpy's
+ * ifftshift) unless a `centred` flag selects numpy's fftshift layout.
+ *
+ * recombine2d_set_config (recombine.c:135-196): sizes as there, pswf [yN]
+ * the PSWF in raw layout (host array; the reference reads it from a file).
+ * Fb, Fn and m are generated as generate_Fb/Fn/m (recombine.c:12-67) and kept
+ * on the device.  Arrays and FFTs are complex128, as the reference's.
+ * Returns CG_ERR_ARG when a side condition of the reference does not hold. */
+typedef struct cg_recombine cg_recombine;
+int cg_recombine_create(int image_size, int subgrid_spacing, const double *pswf_host,
+                        int yB_size, int yN_size, int yP_size, int xA_size,
+                        int xM_size, int xMxN_yP_size, cg_recombine **out);
+int cg_recombine_destroy(cg_recombine *h);
+/* sizes[0..4] = xM_yP_size, xM_yN_size, facet_spacing, yP_spacing, xM_spacing */
+int cg_recombine_sizes(const cg_recombine *h, int32_t *sizes);
+/* host copies of Fb [yB], Fn [xM_yN], m [xMxN_yP] (raw layout; NULL skips) */
+int cg_recombine_windows(const cg_recombine *h, double *Fb, double *Fn, double *m);
+size_t cg_recombine_workspace_bytes(const cg_recombine *h, int n0, int n1);
+/* recombine2d_pf1_ft1_es1 + pf0_ft0 + es0 (recombine.c:242-459) for one facet
+ * [yB, yB] and every pair of n0 x n1 subgrid offsets (device arrays, grid
+ * cells, multiples of subgrid_spacing; others count CG_ERR_INDEX in d_status):
+ * nmbf [n0][n1][xM_yN][xM_yN].  centred / out_centred: facet / nmbf layout. */
+int cg_recombine_facet_to_subgrids(cg_recombine *h, const void *facet, int centred,
+                                   const int32_t *subgrid_off0, int n0,
+                                   const int32_t *subgrid_off1, int n1, void *nmbf,
+                                   int out_centred, void *workspace,
+                                   size_t workspace_bytes, int32_t *d_status,
+                                   cg_stream_t stream);
+/* recombine2d_af0_af1 (recombine.c:504-544) for n subgrids: subgrids[s]
+ * [xM, xM] += nmbf[s] rolled to the facet offsets (grid pixels, multiples of
+ * the facet spacing).  Raw: divided by xM^2 (an unnormalised backward FFT
+ * of the subgrid follows, cg_fft_raw); centred: the notebook's sum, unscaled
+ * (a centred ifft follows, cg_fft). */
+int cg_recombine_add_facet(const cg_recombine *h, const void *nmbf, int n,
+                           int facet_off0, int facet_off1, int centred,
+                           void *subgrids, cg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
