@@ -110,6 +110,44 @@ def _cpu_shard(job):
     return len(v)
 
 
+def recombine_cpu_facet_s():
+    """Seconds of the numpy oracle's facet -> subgrid recombination per facet of
+    the 'tiny' set (8192^2, facets 1280^2, 22 x 22 subgrids), 1 core: one facet
+    with 1 and with 4 subgrid columns (all 22 rows each), per facet =
+    t1 + 21 (t4 - t1) / 3 (the per-facet preparation once, then linear in columns)."""
+    from oracle import crocodile_oracle as O
+    from crocodile_gb300 import bench_configs as BC
+    from crocodile_gb300.recombine import default_pswf
+    N, sp, yB, yN, yP, xA, xM, xMxN = BC.RECOMBINE_TINY
+    cfg = O.RecombineConfig(N, yB, yN, yP, xA, xM, xMxN, default_pswf(N, yN, xA, xM))
+    fo, so = BC.recombine_layout(N, sp, yB, xA)
+    rng = numpy.random.default_rng(11)
+    facet = rng.standard_normal((yB, yB)) + 1j * rng.standard_normal((yB, yB))
+    t = []
+    for n1 in (1, 4):
+        t0 = time.perf_counter()
+        O.rc_facet_to_subgrids(cfg, facet, so, so[:n1])
+        t.append(time.perf_counter() - t0)
+    return t[0] + (len(so) - 1) * (t[1] - t[0]) / 3, "one 1280^2 facet with 1 and 4 of 22 " \
+        "subgrid columns (%.2f s, %.2f s), extrapolated to 22 columns" % tuple(t)
+
+
+def szetan_cpu_correction_s(h):
+    """Seconds of the oracle's calc_gridding_correction_fine over 8192 pixels
+    (gridder at 8192 offsets, R 3, x0 0.3), 1 core: 32 and 64 pixels timed,
+    extrapolated linearly in pixels."""
+    from oracle import crocodile_oracle as O
+    x = (numpy.arange(8192) - 4096) / 8192
+    t = []
+    for k in (32, 64):
+        t0 = time.perf_counter()
+        O.sze_gridding_correction_fine(x[:k], numpy.asarray(h), 0.3, 8192, 3)
+        t.append(time.perf_counter() - t0)
+    per = (t[1] - t[0]) / 32
+    return t[0] + (8192 - 32) * per, "32 and 64 of 8192 pixels (%.2f s, %.2f s), " \
+        "extrapolated" % tuple(t)
+
+
 def oracle_sample(name, w, sample):
     """(uvw, vis, rows, kernel table) of a bounded sample, kernels from the oracle.
 
@@ -657,6 +695,19 @@ def run_ours(args):
         skip = {"aw"} if args.workload == "aw" else {"wproj"}
         cfg_results = bench_configs.run([k for k in bench_configs.MEASURES if k not in skip])
         autotune.set_tuning(**tuned)
+        if not args.no_cpu_baseline:
+            r = cfg_results.get("recombine")
+            if r:
+                sec, how = recombine_cpu_facet_s()
+                r["cpu_oracle"] = {"s_per_facet": sec, "s_whole_image": sec * r["facets"],
+                                   "cores": 1, "kind": "port", "sample": how}
+                r["speedup_vs_cpu_oracle"] = sec * r["facets"] / (r["ms"] * 1e-3)
+            z = cfg_results.get("szetan")
+            if z:
+                sec, how = szetan_cpu_correction_s(z["h"])
+                z["cpu_oracle_correction_s"] = sec
+                z["cpu_oracle_sample"] = how
+                z["speedup_vs_cpu_oracle"] = sec / (z["ms_correction"] * 1e-3)
 
     # kernels of ours per step: coords, scan (1 or 3), scatter, work items, grid, degrid
     per_step = 1 + (3 if info_plan["buckets"] > 4096 else 1) + 1 + 1 + 2

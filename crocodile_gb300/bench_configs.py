@@ -1,6 +1,7 @@
 """Throughput and accuracy of every benchmark configuration on the current GPU.
 
-    python -m crocodile_gb300.bench_configs [--only plain,wproj,diff,wstack,aw] [--steps K]
+    python -m crocodile_gb300.bench_configs [--only plain,wproj,...,recombine,szetan]
+                                            [--steps K]
 
 For each configuration (see configs.py) it times, with CUDA events on the
 current stream after warm-up, the FP32 batched form and the plain FP64 form
@@ -282,8 +283,105 @@ def measure_wtowers(steps=5, variants=True):
                     "tests/test_gpu_towers.py"}
 
 
+# "tiny" parameter set of examples/grid/bench_recombine.c ("8k-2k-512"): image,
+# subgrid spacing, yB, yN, yP, xA, xM, xMxN_yP
+RECOMBINE_TINY = (8192, 128, 1280, 1536, 2048, 384, 512, 144)
+
+
+def recombine_layout(image_size, subgrid_spacing, yB, xA):
+    """Facet and subgrid offsets covering the image: ceil(N / yB) facets and
+    ceil(N / xA) subgrids per axis, centres rounded to the allowed spacings."""
+    facet_spacing = image_size // subgrid_spacing
+    nf = -(-image_size // yB)
+    ns = -(-image_size // xA)
+    fo = [facet_spacing * int(round(j * image_size / nf / facet_spacing)) for j in range(nf)]
+    so = [subgrid_spacing * int(round(i * image_size / ns / subgrid_spacing)) for i in range(ns)]
+    return fo, so
+
+
+def recombine_flops_bytes(rc, n0, n1):
+    """FP64 FFT flops (5 n log2 n per transform) and stage bytes (each array
+    written once and read once) of one facet_to_subgrids call."""
+    import math
+    yB, yP, xM_yP, xM_yN = rc.yB_size, rc.yP_size, rc.xM_yP_size, rc.xM_yN_size
+    ffts = [(yP, yB), (xM_yP, n1 * yB), (yP, n1 * xM_yN), (xM_yP, n0 * n1 * xM_yN)]
+    flops = sum(5 * n * math.log2(n) * b for n, b in ffts)
+    elems = yB * yB + 3 * yB * yP + 3 * n1 * yB * xM_yP + 3 * n1 * xM_yN * yP \
+        + 3 * n0 * n1 * xM_yN * xM_yP + n0 * n1 * xM_yN ** 2
+    return flops, elems * 16
+
+
+def measure_recombine(steps=3, nfacets=None):
+    """Facet -> subgrid recombination of a whole image, the "tiny" (8k-2k-512)
+    set of examples/grid/bench_recombine.c: 8192^2 image as 7 x 7 facets of
+    1280^2, 22 x 22 subgrids of 384^2 (xM 512), complex128 throughout.  A step
+    is every facet's contributions to every subgrid, their sum, and the
+    subgrids' inverse FFTs."""
+    from .recombine import Recombine
+    N, sp, yB, yN, yP, xA, xM, xMxN = RECOMBINE_TINY
+    rc = Recombine(N, sp, yB, yN, yP, xA, xM, xMxN)
+    fo, so = recombine_layout(N, sp, yB, xA)
+    nf = len(fo) if nfacets is None else nfacets
+    g = torch.Generator(device="cuda").manual_seed(11)
+    facets = torch.randn((nf, len(fo), yB, yB), dtype=E.CD, device="cuda", generator=g)
+    o = E.cuda_tensor(numpy.asarray(so), torch.int32)
+    ns = len(so)
+    approx = torch.zeros((ns, ns, xM, xM), dtype=E.CD, device="cuda")
+    nm = torch.empty((ns, ns, rc.xM_yN_size, rc.xM_yN_size), dtype=E.CD, device="cuda")
+
+    def per_facet(j0, j1):
+        rc.facet_to_subgrids(facets[j0, j1], o, o, out=nm, check=False)
+        rc.add_facet(approx, nm, fo[j0], fo[j1])
+
+    def step():
+        approx.zero_()
+        rc.status.reset()
+        for j0 in range(nf):
+            for j1 in range(len(fo)):
+                per_facet(j0, j1)
+        rc.finish_subgrids(approx, crop=False)
+
+    ms = _time(step, steps, warmup=1)
+    rc.status.check()
+    ms_facet = _time(lambda: per_facet(0, 0), max(steps, 5))
+    flops, nbytes = recombine_flops_bytes(rc, ns, ns)
+    nfac = nf * len(fo)
+    return {"workload": "facet->subgrid recombination, bench_recombine.c 'tiny' (8k-2k-512): "
+                        "8192^2 image, %d x %d facets of %d^2, %d x %d subgrids (xA %d, xM %d), "
+                        "complex128" % (nf, len(fo), yB, ns, ns, xA, xM),
+            "facets": nfac, "subgrids": ns * ns, "ms": ms,
+            "contributions_per_s": nfac * ns * ns / (ms * 1e-3),
+            "ms_per_facet": ms_facet,
+            "fft_gflop_per_facet": flops / 1e9, "fp64_fft_tflop_s": flops / (ms_facet * 1e-3) / 1e12,
+            "stage_gb_per_facet": nbytes / 1e9,
+            "stage_gb_s": nbytes / (ms_facet * 1e-3) / 1e9,
+            "note": "per facet: 2 row-FFT passes per axis (cuFFT Z2Z) and 5 fused window / "
+                    "crop / transpose kernels; parity with the reference notebook in "
+                    "tests/test_gpu_recombine.py"}
+
+
+def measure_szetan(steps=5):
+    """Sze-Tan gridder evaluation (crocodile/antialias.py): the grid correction
+    of an 8192-pixel axis (the gridder sampled at 8192 offsets, as
+    sze_tan_grid_correction does) and a kernel table oversampled 16384 times,
+    for R = 3 with h fitted here at N = 16, M = 16 points (host least squares)."""
+    from . import antialias as A
+    t0 = time.perf_counter()
+    h = A.optimal_grid(3, 0.3, 16, 16)[0]
+    fit_s = time.perf_counter() - t0
+    x = (numpy.arange(8192) - 4096) / 8192
+    ms_corr = _time(lambda: A.calc_gridding_correction_fine(x, h, 0.3, 8192, 3), steps)
+    nu = numpy.arange(16384) / 16384
+    ms_table = _time(lambda: A.calc_gridding_fine(h, 0.3, nu, 3), steps)
+    return {"workload": "Sze-Tan R 3 x0 0.3: grid correction of 8192 pixels (M 8192), "
+                        "gridder table at 16384 offsets", "ms_correction": ms_corr,
+            "ms_table": ms_table, "host_fit_s": fit_s, "h": [float(v) for v in h],
+            "note": "host round trip included (numpy in and out); FP64"}
+
+
 MEASURES = {"plain": measure_plain, "wproj": measure_wproj, "diff": measure_diff,
-            "wstack": measure_wstack, "aw": measure_aw, "wtowers": measure_wtowers}
+            "wstack": measure_wstack, "aw": measure_aw, "wtowers": measure_wtowers,
+            "recombine": measure_recombine, "szetan": measure_szetan}
 
 
 def run(only=None, steps=None):
@@ -306,7 +404,12 @@ def main():
                     help="w-towers only: time the measured shape alone (profiling runs)")
     ap.add_argument("--aw-nvis", type=int, default=0,
                     help="AW only: the first N visibilities, FP32 only (profiling runs)")
+    ap.add_argument("--recombine-facets", type=int, default=0,
+                    help="recombination only: the first N rows of facets (profiling runs)")
     a = ap.parse_args()
+    if a.recombine_facets:
+        print(json.dumps(measure_recombine(a.steps or 2, nfacets=a.recombine_facets)))
+        return
     if a.no_variants:
         print(json.dumps(measure_wtowers(a.steps or 5, variants=False)))
         return
