@@ -89,6 +89,8 @@ SIGNATURES = {
     "cg_recombine_facet_to_subgrids": (c_int, [P, P, c_int, P, c_int, P, c_int, P, c_int, P,
                                                c_size_t, P, P]),
     "cg_recombine_add_facet": (c_int, [P, P, c_int, c_int, c_int, c_int, P, P]),
+    "cg_recombine_subgrids_to_facet": (c_int, [P, P, c_int, P, c_int, P, c_int, c_int, c_int, P,
+                                               c_int, c_int, P, c_size_t, P, P]),
     "cg_plan_destroy": (c_int, [P]),
     "cg_set_tuning": (c_int, [ctypes.POINTER(Tuning)]),
     "cg_get_tuning": (c_int, [ctypes.POINTER(Tuning)]),

@@ -346,6 +346,17 @@ def measure_recombine(steps=3, nfacets=None):
     ms_facet = _time(lambda: per_facet(0, 0), max(steps, 5))
     flops, nbytes = recombine_flops_bytes(rc, ns, ns)
     nfac = nf * len(fo)
+    # the other direction: every facet from the 484 subgrids (their spectra
+    # once, then one subgrids_to_facet call per facet)
+    step()
+    del facets
+    fo_rows = fo[:nf]
+    ms_split = _time(lambda: rc.split(approx, so, so, fo_rows, fo), steps, warmup=1)
+    fs = rc.subgrid_spectra(approx)
+    fout = torch.empty((yB, yB), dtype=E.CD, device="cuda")
+    ms_split_facet = _time(lambda: rc.subgrids_to_facet(fs, o, o, fo[0], fo[0], out=fout,
+                                                        check=False), max(steps, 5))
+    rc.status.check()
     return {"workload": "facet->subgrid recombination, bench_recombine.c 'tiny' (8k-2k-512): "
                         "8192^2 image, %d x %d facets of %d^2, %d x %d subgrids (xA %d, xM %d), "
                         "complex128" % (nf, len(fo), yB, ns, ns, xA, xM),
@@ -355,9 +366,12 @@ def measure_recombine(steps=3, nfacets=None):
             "fft_gflop_per_facet": flops / 1e9, "fp64_fft_tflop_s": flops / (ms_facet * 1e-3) / 1e12,
             "stage_gb_per_facet": nbytes / 1e9,
             "stage_gb_s": nbytes / (ms_facet * 1e-3) / 1e9,
-            "note": "per facet: 2 row-FFT passes per axis (cuFFT Z2Z) and 5 fused window / "
-                    "crop / transpose kernels; parity with the reference notebook in "
-                    "tests/test_gpu_recombine.py"}
+            "subgrids_to_facets_ms": ms_split, "subgrids_to_facet_ms_per_facet": ms_split_facet,
+            "note": "ms: facets -> subgrids (per facet: 2 row-FFT passes per axis, cuFFT Z2Z, "
+                    "and 5 fused window / crop / transpose kernels; then the subgrid sums' "
+                    "512^2 inverse FFTs); subgrids_to_facets_ms: the other direction for the "
+                    "whole image (the subgrids' spectra, then every facet); parity with the "
+                    "reference notebook in tests/test_gpu_recombine.py"}
 
 
 def measure_szetan(steps=5):

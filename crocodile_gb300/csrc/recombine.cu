@@ -55,6 +55,9 @@ __host__ __device__ inline int pmod(long long a, int n) {
   return (int)(r < 0 ? r + n : r);
 }
 
+// a mod n for a in [-n, 2n) (one conditional add or subtract, 32-bit)
+__device__ __forceinline__ int wrap1(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
 template <typename C>
 struct RT;
 template <>
@@ -137,14 +140,15 @@ __global__ void k_rc_window(const C *__restrict__ bf, int rows, int yP,
     const int off = offs[orow / rows];
     const C *row = bf + (size_t)r * yP;
     C v = czero<C>();
+    // off < yP and i < xM_yP <= yP, so both sums lie within one period
     if (i < (xMxN_yP + 1) / 2) {
-      const C b = row[pmod((long long)i + off, yP)];
+      const C b = row[wrap1(i + off, yP)];
       const typename RT<C>::R w = m[i];
       v.x += w * b.x;
       v.y += w * b.y;
     }
     if (i >= xM_yP - xMxN_yP / 2) {
-      const C b = row[pmod((long long)i + off - xM_yP, yP)];
+      const C b = row[wrap1(i + off - xM_yP, yP)];
       const typename RT<C>::R w = m[xN_yP + i];
       v.x += w * b.x;
       v.y += w * b.y;
@@ -247,13 +251,13 @@ __global__ void k_rc_add_facet(const C *__restrict__ nmbf, int xM_yN, int xM, in
     src0 = j0;
     src1 = j1;
     // pad_mid puts centred index j at xM/2 - h + j; roll adds the facet offset
-    dst0 = pmod((long long)xM / 2 - h + j0 + fo0, xM);
-    dst1 = pmod((long long)xM / 2 - h + j1 + fo1, xM);
+    dst0 = wrap1(xM / 2 - h + j0 + fo0, xM);
+    dst1 = wrap1(xM / 2 - h + j1 + fo1, xM);
   } else {
-    src0 = (j0 + h) % xM_yN;
-    src1 = (j1 + h) % xM_yN;
-    dst0 = pmod((long long)j0 - h + fo0, xM);
-    dst1 = pmod((long long)j1 - h + fo1, xM);
+    src0 = wrap1(j0 + h, xM_yN);
+    src1 = wrap1(j1 + h, xM_yN);
+    dst0 = wrap1(j0 - h + fo0, xM);
+    dst1 = wrap1(j1 - h + fo1, xM);
   }
   C v = nmbf[((size_t)s * xM_yN + src0) * xM_yN + src1];
   if (!centred) v = cscale(v, (R)1 / ((R)xM * (R)xM));
@@ -262,6 +266,156 @@ __global__ void k_rc_add_facet(const C *__restrict__ nmbf, int xM_yN, int xM, in
   a.x += v.x;
   a.y += v.y;
   *d = a;
+}
+
+// ---------------------------------------------------- subgrid -> facet
+// The adjoint direction (notebook cell 18, 2-D by separability): for one
+// facet and n0 x n1 subgrids whose spectra FS [n0][n1][xM][xM] are given.
+
+__device__ __forceinline__ int signed_freq(int c, int n) { return c < n / 2 ? c : c - n; }
+
+// inverse of the crop: padded index k (length np) -> cropped index, or -1
+__device__ __forceinline__ int uncrop(int k, int n, int np) {
+  if (k < n / 2) return k;
+  if (k >= np - n / 2) return k - np + n;
+  return -1;
+}
+
+// A[(i0 n1 + i1) xM_yN + a0][k]: the facet's xM_yN^2 block of each subgrid
+// spectrum (rolled by the facet offset), times Fn on both axes, padded to
+// xM_yP along axis 1 and divided by xM_yP (the inverse FFT that follows is
+// unnormalised).  `centred`: FS in fftshift layout.
+template <typename C>
+__global__ void k_rcT_split(const C *__restrict__ fs, int npair, int xM, int xM_yN, int xM_yP,
+                            int fo0, int fo1, const typename RT<C>::R *__restrict__ Fn,
+                            int centred, C *__restrict__ out) {
+  typedef typename RT<C>::R R;
+  const size_t total = (size_t)npair * xM_yN * xM_yP;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(e % xM_yP);
+    const size_t row = e / xM_yP;
+    const int a0 = (int)(row % xM_yN);
+    const size_t pair = row / xM_yN;
+    const int c1 = uncrop(k, xM_yN, xM_yP);
+    C v = czero<C>();
+    if (c1 >= 0) {
+      // |signed frequency| <= xM_yN / 2 <= xM and 0 <= fo < xM
+      int s0 = wrap1(signed_freq(a0, xM_yN) + fo0, xM);
+      int s1 = wrap1(signed_freq(c1, xM_yN) + fo1, xM);
+      if (centred) {
+        s0 = (s0 + xM / 2) % xM;
+        s1 = (s1 + xM / 2) % xM;
+      }
+      v = cscale(fs[(pair * xM + s0) * xM + s1], Fn[a0] * Fn[c1] / (R)xM_yP);
+    }
+    out[e] = v;
+  }
+}
+
+// out[o][r][k] (k < yP) = sum over j < noff of the window of in[o][j][r][.]
+// placed at offset offs[j]: position p (|p| within xMxN_yP / 2) of the
+// periodic extension of the xM_yP samples, times m, lands at (p + off) mod yP.
+template <typename C>
+__global__ void k_rcT_scatter(const C *__restrict__ in, int outer, int noff, int inner,
+                              int xM_yP, int xMxN_yP, int yP, const int32_t *__restrict__ offs,
+                              const typename RT<C>::R *__restrict__ m, C *__restrict__ out) {
+  const size_t total = (size_t)outer * inner * yP;
+  const int half = xMxN_yP / 2;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(e % yP);
+    const size_t orow = e / yP;
+    const int r = (int)(orow % inner);
+    const size_t o = orow / inner;
+    C v = czero<C>();
+    for (int j = 0; j < noff; ++j) {
+      // k, offs[j] in [0, yP): the signed distance in [-yP/2, yP/2)
+      int p = k - offs[j];
+      if (p >= yP / 2) p -= yP;
+      if (p < -(yP / 2)) p += yP;
+      if (p < -half || p >= xMxN_yP - half) continue;
+      // |p| <= xMxN_yP / 2 <= xM_yP: one wrap each
+      const typename RT<C>::R w = m[p < 0 ? p + xMxN_yP : p];
+      const C b = in[((o * noff + j) * inner + r) * xM_yP + (p < 0 ? p + xM_yP : p)];
+      v.x += w * b.x;
+      v.y += w * b.y;
+    }
+    out[e] = v;
+  }
+}
+
+// B[t][i0][k0]: rows (i0, a0) of acc [n0][xM_yN][yP] cropped to the yB facet
+// positions t, transposed so that a0 runs along the rows, padded to xM_yP
+// and divided by xM_yP.  Block 32 x 8: a tile of 32 positions t by 32 k0.
+template <typename C>
+__global__ void k_rcT_crop_T_pad(const C *__restrict__ acc, int n0, int xM_yN, int yP, int yB,
+                                 int xM_yP, C *__restrict__ out) {
+  typedef typename RT<C>::R R;
+  __shared__ C tile[32][33];
+  const int i0 = blockIdx.z;
+  const int t0 = blockIdx.y * 32;
+  const int k00 = blockIdx.x * 32;
+  // load tile[kk][tt] = acc[i0][a0(k0)][crop(t)]
+  for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
+    const int k0 = k00 + kk;
+    const int t = t0 + threadIdx.x;
+    C v = czero<C>();
+    const int a0 = k0 < xM_yP ? uncrop(k0, xM_yN, xM_yP) : -1;
+    if (a0 >= 0 && t < yB) {
+      const int kt = t < yB / 2 ? t : yP - yB + t;
+      v = cscale(acc[((size_t)i0 * xM_yN + a0) * yP + kt], (R)1 / (R)xM_yP);
+    }
+    tile[kk][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int tt = threadIdx.y; tt < 32; tt += blockDim.y) {
+    const int t = t0 + tt;
+    const int k0 = k00 + threadIdx.x;
+    if (t < yB && k0 < xM_yP)
+      out[((size_t)t * n0 + i0) * xM_yP + k0] = tile[threadIdx.x][tt];
+  }
+}
+
+// facet[s][t] (+)= acc2[t][crop(s)] Fb[s] Fb[t], transposed; `centred`:
+// facet in fftshift layout.  Block 32 x 8: a tile of 32 t by 32 s.
+template <typename C>
+__global__ void k_rcT_final(const C *__restrict__ acc2, int yP, int yB,
+                            const typename RT<C>::R *__restrict__ Fb, int centred, int accumulate,
+                            C *__restrict__ facet) {
+  __shared__ C tile[32][33];
+  const int t0 = blockIdx.y * 32;
+  const int s0 = blockIdx.x * 32;
+  for (int tt = threadIdx.y; tt < 32; tt += blockDim.y) {
+    const int t = t0 + tt;
+    const int s = s0 + threadIdx.x;
+    C v = czero<C>();
+    if (t < yB && s < yB) {
+      const int ks = s < yB / 2 ? s : yP - yB + s;
+      v = cscale(acc2[(size_t)t * yP + ks], Fb[s] * Fb[t]);
+    }
+    tile[tt][threadIdx.x] = v;
+  }
+  __syncthreads();
+  const int h = yB / 2;
+  for (int ss = threadIdx.y; ss < 32; ss += blockDim.y) {
+    const int s = s0 + ss;
+    const int t = t0 + threadIdx.x;
+    if (s < yB && t < yB) {
+      const int d0 = centred ? (s + h) % yB : s;
+      const int d1 = centred ? (t + h) % yB : t;
+      C *d = facet + (size_t)d0 * yB + d1;
+      const C v = tile[threadIdx.x][ss];
+      if (accumulate) {
+        C a = *d;
+        a.x += v.x;
+        a.y += v.y;
+        *d = a;
+      } else {
+        *d = v;
+      }
+    }
+  }
 }
 
 // ------------------------------------------------------------------ host side
@@ -305,6 +459,58 @@ inline unsigned grid_for(size_t n) {
 struct WsLayout {
   size_t bf, mbf, bf2, mbf2, offs, total;
 };
+
+// subgrid -> facet: A [n0 n1 xM_yN][xM_yP], acc [n0 xM_yN][yP], B [yB n0][xM_yP],
+// acc2 [yB][yP], the offsets
+struct WsLayoutT {
+  size_t a, acc, b, acc2, offs, total;
+};
+
+WsLayoutT ws_layout_t(const cg_recombine *h, int n0, int n1) {
+  const size_t e = sizeof(double2);
+  WsLayoutT L;
+  L.a = 0;
+  L.acc = L.a + align256((size_t)n0 * n1 * h->xM_yN * h->xM_yP * e);
+  L.b = L.acc + align256((size_t)n0 * h->xM_yN * h->yP * e);
+  L.acc2 = L.b + align256((size_t)h->yB * n0 * h->xM_yP * e);
+  L.offs = L.acc2 + align256((size_t)h->yB * h->yP * e);
+  L.total = L.offs + align256((size_t)(n0 + n1) * sizeof(int32_t));
+  return L;
+}
+
+template <typename C>
+int subgrids_to_facet(cg_recombine *h, const void *fs, int centred, int n0, int n1, int fo0,
+                      int fo1, void *facet, int out_centred, int accumulate, char *ws,
+                      const WsLayoutT &L, cudaStream_t st) {
+  C *A = (C *)(ws + L.a);
+  C *acc = (C *)(ws + L.acc);
+  C *B = (C *)(ws + L.b);
+  C *acc2 = (C *)(ws + L.acc2);
+  const int32_t *offs0 = (const int32_t *)(ws + L.offs);
+  const int32_t *offs1 = offs0 + n0;
+  const int yB = h->yB, yP = h->yP, xM = h->xM, xM_yP = h->xM_yP, xM_yN = h->xM_yN;
+  int rc;
+  k_rcT_split<C><<<grid_for((size_t)n0 * n1 * xM_yN * xM_yP), 256, 0, st>>>(
+      (const C *)fs, n0 * n1, xM, xM_yN, xM_yP, fo0, fo1, Prec<C>::Fn(h), centred, A);
+  CG_LAUNCH("recombine split subgrids");
+  if ((rc = rows_fft<C>(A, n0 * n1 * xM_yN, xM_yP, CUFFT_INVERSE, st))) return rc;
+  k_rcT_scatter<C><<<grid_for((size_t)n0 * xM_yN * yP), 256, 0, st>>>(
+      A, n0, n1, xM_yN, xM_yP, h->xMxN_yP, yP, offs1, Prec<C>::m(h), acc);
+  CG_LAUNCH("recombine subgrid windows (axis 1)");
+  if ((rc = rows_fft<C>(acc, n0 * xM_yN, yP, CUFFT_FORWARD, st))) return rc;
+  k_rcT_crop_T_pad<C><<<dim3((xM_yP + 31) / 32, (yB + 31) / 32, n0), dim3(32, 8), 0, st>>>(
+      acc, n0, xM_yN, yP, yB, xM_yP, B);
+  CG_LAUNCH("recombine crop to the facet (axis 1)");
+  if ((rc = rows_fft<C>(B, yB * n0, xM_yP, CUFFT_INVERSE, st))) return rc;
+  k_rcT_scatter<C><<<grid_for((size_t)yB * yP), 256, 0, st>>>(
+      B, yB, n0, 1, xM_yP, h->xMxN_yP, yP, offs0, Prec<C>::m(h), acc2);
+  CG_LAUNCH("recombine subgrid windows (axis 0)");
+  if ((rc = rows_fft<C>(acc2, yB, yP, CUFFT_FORWARD, st))) return rc;
+  k_rcT_final<C><<<dim3((yB + 31) / 32, (yB + 31) / 32), dim3(32, 8), 0, st>>>(
+      acc2, yP, yB, Prec<C>::Fb(h), out_centred, accumulate, (C *)facet);
+  CG_LAUNCH("recombine facet");
+  return CG_OK;
+}
 
 WsLayout ws_layout(const cg_recombine *h, int n0, int n1) {
   const size_t e = sizeof(double2);
@@ -472,7 +678,7 @@ int cg_recombine_windows(const cg_recombine *h, double *Fb, double *Fn, double *
 
 size_t cg_recombine_workspace_bytes(const cg_recombine *h, int n0, int n1) {
   if (!h || n0 < 0 || n1 < 0) return 0;
-  return ws_layout(h, n0, n1).total;
+  return std::max(ws_layout(h, n0, n1).total, ws_layout_t(h, n0, n1).total);
 }
 
 int cg_recombine_facet_to_subgrids(cg_recombine *h, const void *facet, int centred,
@@ -498,6 +704,40 @@ int cg_recombine_facet_to_subgrids(cg_recombine *h, const void *facet, int centr
   return facet_to_subgrids<double2>(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
 }
 
+int cg_recombine_subgrids_to_facet(cg_recombine *h, const void *fs, int centred,
+                                   const int32_t *subgrid_off0, int n0,
+                                   const int32_t *subgrid_off1, int n1, int facet_off0,
+                                   int facet_off1, void *facet, int out_centred, int accumulate,
+                                   void *ws, size_t ws_bytes, int32_t *d_status,
+                                   cg_stream_t stream) {
+  CG_REQUIRE(h && facet && d_status && n0 >= 0 && n1 >= 0,
+             "bad recombine_subgrids_to_facet arguments");
+  CG_REQUIRE(pmod(facet_off0, h->facet_spacing) == 0 && pmod(facet_off1, h->facet_spacing) == 0,
+             "facet offsets must be multiples of the facet spacing %d", h->facet_spacing);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n0 == 0 || n1 == 0) {
+    if (!accumulate)
+      CG_CUDA(cudaMemsetAsync(facet, 0, (size_t)h->yB * h->yB * sizeof(double2), st));
+    return CG_OK;
+  }
+  CG_REQUIRE(fs && subgrid_off0 && subgrid_off1, "bad recombine_subgrids_to_facet arguments");
+  CG_REQUIRE(n0 <= 65535 && (long long)n0 * n1 * h->xM_yN <= (1ll << 31) - 1,
+             "too many subgrids for one call; split the offsets");
+  const WsLayoutT L = ws_layout_t(h, n0, n1);
+  if (!ws || ws_bytes < L.total)
+    return set_error(CG_ERR_WORKSPACE, "recombine needs %zu workspace bytes", L.total);
+  char *w = (char *)ws;
+  k_rc_offsets<<<(n0 + n1 + 255) / 256, 256, 0, st>>>(subgrid_off0, n0, subgrid_off1, n1,
+                                                      h->subgrid_spacing, h->yP_spacing, h->yP,
+                                                      (int32_t *)(w + L.offs), d_status);
+  CG_LAUNCH("recombine offsets");
+  // facet offsets in xM samples, reduced to [0, xM) (the kernels wrap once)
+  const int fo0 = pmod((long long)facet_off0 / h->facet_spacing * h->xM_spacing, h->xM);
+  const int fo1 = pmod((long long)facet_off1 / h->facet_spacing * h->xM_spacing, h->xM);
+  return subgrids_to_facet<double2>(h, fs, centred, n0, n1, fo0, fo1, facet, out_centred,
+                                    accumulate, w, L, st);
+}
+
 int cg_recombine_add_facet(const cg_recombine *h, const void *nmbf, int n, int facet_off0,
                            int facet_off1, int centred, void *subgrids, cg_stream_t stream) {
   CG_REQUIRE(h && n >= 0 && (n == 0 || (nmbf && subgrids)), "bad recombine_add_facet arguments");
@@ -505,8 +745,9 @@ int cg_recombine_add_facet(const cg_recombine *h, const void *nmbf, int n, int f
   CG_REQUIRE(pmod(facet_off0, h->facet_spacing) == 0 && pmod(facet_off1, h->facet_spacing) == 0,
              "facet offsets must be multiples of the facet spacing %d", h->facet_spacing);
   CG_REQUIRE(n <= 65535, "too many subgrids for one call");
-  const int fo0 = facet_off0 / h->facet_spacing * h->xM_spacing;
-  const int fo1 = facet_off1 / h->facet_spacing * h->xM_spacing;
+  // facet offsets in xM samples, reduced to [0, xM) (the kernel wraps once)
+  const int fo0 = pmod((long long)facet_off0 / h->facet_spacing * h->xM_spacing, h->xM);
+  const int fo1 = pmod((long long)facet_off1 / h->facet_spacing * h->xM_spacing, h->xM);
   const dim3 grid((h->xM_yN + 127) / 128, h->xM_yN, n);
   cudaStream_t st = (cudaStream_t)stream;
   k_rc_add_facet<double2><<<grid, 128, 0, st>>>((const double2 *)nmbf, h->xM_yN, h->xM, fo0, fo1,

@@ -22,6 +22,13 @@ the notebook, and return CUDA tensors:
 * ``finish_subgrids(approx)``: ifft and the middle xA_size (cell 30);
 * ``recombine(facets, facet_offs0, facet_offs1, offs0, offs1)``: all of it.
 
+and the other direction (notebook cell 18, in 2-D by separability):
+
+* ``subgrid_spectra(subgrids)``: FFT of each subgrid padded to xM_size;
+* ``subgrids_to_facet(fs, offs0, offs1, facet_off0, facet_off1)``: the facet
+  approximation Fb x Fb x the sum of every subgrid's contribution;
+* ``split(subgrids, offs0, offs1, facet_offs0, facet_offs1)``: all facets.
+
 Arrays and FFTs are complex128, as in the reference: Fb = 1 / PSWF spans
 many decades towards the facet edge, and the contributions come out of
 intermediates a thousand times larger than their peak, which single
@@ -163,3 +170,58 @@ class Recombine:
                 self.add_facet(approx, nm, fo0, fo1)
         self.status.check()
         return self.finish_subgrids(approx, crop=crop)
+
+    # ------------------------------------------------------ subgrid -> facet
+
+    def subgrid_spectra(self, subgrids):
+        """FS [..., xM, xM]: centred FFT of each centred subgrid [..., xA, xA]
+        (or already [..., xM, xM]) zero-padded to xM_size."""
+        s = E.cuda_tensor(subgrids, self.dtype)
+        xA = s.shape[-1]
+        if xA != self.xM_size:
+            lo = self.xM_size // 2 - xA // 2
+            fs = torch.zeros(tuple(s.shape[:-2]) + (self.xM_size, self.xM_size),
+                             dtype=self.dtype, device="cuda")
+            fs[..., lo:lo + xA, lo:lo + xA] = s
+        else:
+            fs = s.clone()
+        return E.fft_(fs, inverse=False)
+
+    def subgrids_to_facet(self, fs, offs0, offs1, facet_off0, facet_off1, out=None,
+                          accumulate=False, check=True):
+        """The facet [yB, yB] (centred) from the spectra fs [n0, n1, xM, xM] of
+        the subgrids at offs0 x offs1: Fb x Fb times the sum of their
+        contributions (notebook cell 18; the facet mask is left to the caller)."""
+        fs = E.cuda_tensor(fs, self.dtype)
+        o0 = E.cuda_tensor(numpy.atleast_1d(offs0) if not isinstance(offs0, torch.Tensor)
+                           else offs0, torch.int32)
+        o1 = E.cuda_tensor(numpy.atleast_1d(offs1) if not isinstance(offs1, torch.Tensor)
+                           else offs1, torch.int32)
+        n0, n1 = int(o0.numel()), int(o1.numel())
+        if fs.numel() != n0 * n1 * self.xM_size ** 2:
+            raise ValueError("fs must hold %d x %d subgrid spectra of %d^2" % (n0, n1, self.xM_size))
+        if out is None:
+            out = torch.zeros((self.yB_size, self.yB_size), dtype=self.dtype, device="cuda")
+        ws = self._workspace(n0, n1)
+        if check:
+            self.status.reset()
+        L.call("cg_recombine_subgrids_to_facet", self._h, E._p(fs), 1, E._p(o0), n0, E._p(o1),
+               n1, int(facet_off0), int(facet_off1), E._p(out), 1, int(bool(accumulate)),
+               E._p(ws), ws.numel(), E._p(self.status.t), E.stream())
+        if check:
+            self.status.check()
+        return out
+
+    def split(self, subgrids, offs0, offs1, facet_offs0, facet_offs1):
+        """All facets [nf0, nf1, yB, yB] from the subgrids [n0, n1, xA, xA]."""
+        fs = self.subgrid_spectra(subgrids)
+        o0 = E.cuda_tensor(numpy.asarray(offs0), torch.int32)
+        o1 = E.cuda_tensor(numpy.asarray(offs1), torch.int32)
+        out = torch.empty((len(facet_offs0), len(facet_offs1), self.yB_size, self.yB_size),
+                          dtype=self.dtype, device="cuda")
+        self.status.reset()
+        for j0, fo0 in enumerate(facet_offs0):
+            for j1, fo1 in enumerate(facet_offs1):
+                self.subgrids_to_facet(fs, o0, o1, fo0, fo1, out=out[j0, j1], check=False)
+        self.status.check()
+        return out

@@ -460,6 +460,21 @@ int cg_recombine_facet_to_subgrids(cg_recombine *h, const void *facet, int centr
                                    int out_centred, void *workspace,
                                    size_t workspace_bytes, int32_t *d_status,
                                    cg_stream_t stream);
+/* Subgrid -> facet (the notebook's cell 18 in 2-D, by separability; the
+ * adjoint of the above): facet [yB, yB] (+)= Fb x Fb times the sum over
+ * n0 x n1 subgrids of their contributions, from the subgrids' spectra fs
+ * [n0][n1][xM][xM] (the centred or raw FFT of each subgrid padded to xM),
+ * subgrid offsets as above, the facet's offsets in grid pixels.  The facet
+ * mask of the notebook is left to the caller.  accumulate: add into facet
+ * instead of overwriting it (to split the subgrids over several calls).
+ * Workspace: cg_recombine_workspace_bytes(h, n0, n1). */
+int cg_recombine_subgrids_to_facet(cg_recombine *h, const void *fs, int centred,
+                                   const int32_t *subgrid_off0, int n0,
+                                   const int32_t *subgrid_off1, int n1,
+                                   int facet_off0, int facet_off1, void *facet,
+                                   int out_centred, int accumulate, void *workspace,
+                                   size_t workspace_bytes, int32_t *d_status,
+                                   cg_stream_t stream);
 /* recombine2d_af0_af1 (recombine.c:504-544) for n subgrids: subgrids[s]
  * [xM, xM] += nmbf[s] rolled to the facet offsets (grid pixels, multiples of
  * the facet spacing).  Raw: divided by xM^2 (an unnormalised backward FFT

@@ -213,3 +213,93 @@ def test_errors(env):
 
 def cfg_xM(rg):
     return int(rg["xM_size"])
+
+
+# ------------------------------------------------------------ subgrid -> facet
+
+def _subgrids(O, rg, G2, cfg):
+    so, sa = rg["subgrid_off"], rg["subgrid_A"]
+    return numpy.array([[O.extract_mid(numpy.roll(G2, (-so[i0], -so[i1]), (0, 1)), cfg.xA) *
+                         numpy.outer(sa[i0], sa[i1]) for i1 in range(len(so))]
+                        for i0 in range(len(so))])
+
+
+def test_subgrids_to_facet_vs_oracle(env):
+    torch, R, S, E, L, O, rg = env
+    cfg = ocfg(O, rg)
+    rc = R.Recombine(pswf=rg["pswf"], **sizes(rg))
+    rng = numpy.random.default_rng(5)
+    subs = rng.standard_normal((4, 4, cfg.xA, cfg.xA)) + 1j * rng.standard_normal(
+        (4, 4, cfg.xA, cfg.xA))
+    so, fo = rg["subgrid_off"], rg["facet_off"]
+    fs = rc.subgrid_spectra(subs)
+    fs_ref = numpy.array([[O.rc_split_subgrid(cfg, subs[i0, i1], [(0, 0)])[0] for i1 in range(4)]
+                          for i0 in range(4)])
+    # rc_split_subgrid crops to xM_yN; compare the full spectrum's middle
+    c = cfg.xM // 2 - cfg.xM_yN // 2
+    assert_allclose(fs.cpu().numpy()[:, :, c:c + cfg.xM_yN, c:c + cfg.xM_yN], fs_ref, rtol=0,
+                    atol=1e-12 * numpy.abs(fs_ref).max())
+    Fbb = numpy.outer(cfg.Fb, cfg.Fb)
+    for (j0, j1) in ((0, 0), (2, 1), (3, 3)):
+        got = rc.subgrids_to_facet(fs, so, so, fo[j0], fo[j1]).cpu().numpy() / Fbb
+        fn = numpy.array([[O.rc_split_subgrid(cfg, subs[i0, i1], [(fo[j0], fo[j1])])[0]
+                           for i1 in range(4)] for i0 in range(4)])
+        want = O.rc_subgrids_to_facet(cfg, fn, so, so)
+        assert_allclose(got, want, rtol=0, atol=1e-12 * numpy.abs(want).max())
+    # split over two calls with accumulate = one call (compared before the
+    # Fb x Fb weighting, which reaches 4e13 at the facet corners)
+    fo0, fo1 = fo[1], fo[2]
+    one = rc.subgrids_to_facet(fs, so, so, fo0, fo1).cpu().numpy() / Fbb
+    two = rc.subgrids_to_facet(fs[:2], so[:2], so, fo0, fo1)
+    rc.subgrids_to_facet(fs[2:].contiguous(), so[2:], so, fo0, fo1, out=two, accumulate=True)
+    assert_allclose(two.cpu().numpy() / Fbb, one, rtol=0, atol=1e-12 * numpy.abs(one).max())
+
+
+def test_split_accuracy(env):
+    # the notebook's subgrid -> facet check (cell 18) in 2-D on its test image:
+    # the device's error against the true facets equals the oracle's
+    torch, R, S, E, L, O, rg = env
+    cfg = ocfg(O, rg)
+    G2 = _test_image(O, rg)
+    FG2 = O.fft(G2)
+    subs = _subgrids(O, rg, G2, cfg)
+    facets = _facets(O, rg, FG2, cfg)
+    so, fo, fb = rg["subgrid_off"], rg["facet_off"], rg["facet_B"]
+    rc = R.Recombine(pswf=rg["pswf"], **sizes(rg))
+    got = rc.split(subs, so, so, fo, fo).cpu().numpy()
+    err = err_ref = 0
+    for j0 in (0, 2):
+        for j1 in (1, 3):
+            mask = numpy.outer(fb[j0], fb[j1])
+            fn = numpy.array([[O.rc_split_subgrid(cfg, subs[i0, i1], [(fo[j0], fo[j1])])[0]
+                               for i1 in range(4)] for i0 in range(4)])
+            ref = O.rc_subgrids_to_facet(cfg, fn, so, so) * numpy.outer(cfg.Fb, cfg.Fb) * mask
+            err += numpy.abs(got[j0, j1] * mask - facets[j0][j1]) ** 2
+            err_ref += numpy.abs(ref - facets[j0][j1]) ** 2
+    rmse, rmse_ref = numpy.sqrt(numpy.mean(err)), numpy.sqrt(numpy.mean(err_ref))
+    assert rmse_ref < 1e-4 * numpy.sqrt(numpy.mean(numpy.abs(facets[0][1]) ** 2))
+    assert_allclose(rmse, rmse_ref, rtol=1e-3)
+
+
+def test_subgrids_to_facet_raw_layout(env):
+    torch, R, S, E, L, O, rg = env
+    cfg = ocfg(O, rg)
+    rc = R.Recombine(pswf=rg["pswf"], **sizes(rg))
+    rng = numpy.random.default_rng(6)
+    subs = rng.standard_normal((2, 3, cfg.xA, cfg.xA)) + 0j
+    so = rg["subgrid_off"]
+    fs = rc.subgrid_spectra(subs)
+    want = rc.subgrids_to_facet(fs, so[:2], so[1:], 128, 256).cpu().numpy()
+    sh = numpy.fft.ifftshift
+    fs_raw = E.cuda_tensor(sh(fs.cpu().numpy(), axes=(2, 3)), E.CD)
+    o0 = E.cuda_tensor(so[:2], torch.int32)
+    o1 = E.cuda_tensor(so[1:], torch.int32)
+    out = torch.zeros((cfg.yB, cfg.yB), dtype=E.CD, device="cuda")
+    ws = torch.empty(L.lib().cg_recombine_workspace_bytes(rc._h, 2, 3), dtype=torch.uint8,
+                     device="cuda")
+    st = E.Status()
+    st.reset()
+    L.call("cg_recombine_subgrids_to_facet", rc._h, E._p(fs_raw), 0, E._p(o0), 2, E._p(o1), 3,
+           128, 256, E._p(out), 0, 0, E._p(ws), ws.numel(), E._p(st.t), E.stream())
+    st.check()
+    assert_allclose(out.cpu().numpy(), sh(want), rtol=0, atol=1e-13 * numpy.abs(want).max())
