@@ -702,6 +702,17 @@ def run_ours(args):
                 r["cpu_oracle"] = {"s_per_facet": sec, "s_whole_image": sec * r["facets"],
                                    "cores": 1, "kind": "port", "sample": how}
                 r["speedup_vs_cpu_oracle"] = sec * r["facets"] / (r["ms"] * 1e-3)
+            g = cfg_results.get("ingest")
+            if g:
+                from oracle import crocodile_oracle as O
+                blocks = bench_configs.ingest_blocks()[:200]
+                t0 = time.perf_counter()
+                O.collect_blocks(blocks)
+                dt = time.perf_counter() - t0
+                nb = sum(b.nrow * b.nchan for b in blocks)
+                g["cpu_oracle"] = {"mvis_s": nb / dt / 1e6, "cores": 1, "kind": "port",
+                                   "sample": "the first 200 of 2016 blocks (%d visibilities), "
+                                             "numpy collect_blocks, %.2f s" % (nb, dt)}
             z = cfg_results.get("szetan")
             if z:
                 sec, how = szetan_cpu_correction_s(z["h"])

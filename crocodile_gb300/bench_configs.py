@@ -393,9 +393,79 @@ def measure_szetan(steps=5):
             "note": "host round trip included (numpy in and out); FP64"}
 
 
+def ingest_blocks(seed=5, nant=64, ntime=125, nchan=64, npol=1):
+    """Synthetic per-baseline blocks of the AW workload's shape: 2016 baselines
+    x 125 times x 64 channels (16,128,000 visibilities), uvw in metres."""
+    from .ingest import VisibilityBlock
+    rng = numpy.random.default_rng(seed)
+    freq = 1.0e8 * (1 + 0.3 * numpy.arange(nchan) / max(nchan - 1, 1))
+    time = 58000.0 + numpy.arange(ntime) / 1440.0
+    blocks = []
+    for a1 in range(nant):
+        for a2 in range(a1 + 1, nant):
+            uvw = rng.normal(0, 1500.0, (ntime, 3))
+            vis = (rng.standard_normal((ntime, nchan, npol), dtype=numpy.float32) + 1j *
+                   rng.standard_normal((ntime, nchan, npol), dtype=numpy.float32))
+            blocks.append(VisibilityBlock(freq, time, uvw, numpy.full(ntime, a1),
+                                          numpy.full(ntime, a2), vis.astype(numpy.complex128)))
+    return blocks
+
+
+def measure_ingest(steps=3, blocks=None):
+    """Visibility ingest of the AW workload's shape (2016 baseline blocks, 125
+    times, 64 channels, 1 polarisation; 16.1M visibilities, 258 MB of
+    complex128 vis): host blocks -> device uvw (wavelengths), complex64 vis
+    and int32 antennas, through the pinned double buffer (host packing, copy
+    and conversion overlapped), and the conversion kernel alone on resident
+    inputs."""
+    from .ingest import Ingest
+    blocks = blocks or ingest_blocks()
+    n = sum(b.nrow * b.nchan for b in blocks)
+    ing = Ingest()
+    for _ in range(2):
+        ing.run(blocks, dtype=E.CF, want_src=False, want_antennas=True)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        ing.run(blocks, dtype=E.CF, want_src=False, want_antennas=True)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    s_e2e = statistics.median(ts)
+    # the kernel alone: one chunk holding everything, inputs already on the device
+    big = Ingest(chunk_bytes=1 << 40)
+    big.run(blocks, dtype=E.CF, want_src=False, want_antennas=True)
+    out = {"uvw": torch.empty((n, 3), dtype=torch.float64, device="cuda"),
+           "vis": torch.empty(n, dtype=E.CF, device="cuda"),
+           "a1": torch.empty(n, dtype=torch.int32, device="cuda"),
+           "a2": torch.empty(n, dtype=torch.int32, device="cuda")}
+    rows, nfreq, nvis, off, pos = big._layout(blocks)
+    d = big._dev[0].data_ptr()
+    import ctypes
+    cp = ctypes.c_void_p
+
+    def kernel():
+        L.call("cg_ingest_blocks", cp(d + off["blocks"]), len(blocks), cp(d + off["uvw"]),
+               cp(d + off["time"]), cp(d + off["a1"]), cp(d + off["a2"]), cp(d + off["freq"]),
+               cp(d + off["vis"]), 0, E._p(out["uvw"]), None, E._p(out["a1"]), E._p(out["a2"]),
+               E._p(out["vis"]), 1, E._p(big.status.t), E.stream())
+
+    ms_k = _time(kernel, max(steps, 5))
+    big.status.check()
+    nbytes = nvis * 16 + rows * 32 + n * (24 + 8 + 8)
+    return {"workload": "ingest of 2016 baseline blocks x 125 times x 64 channels x 1 "
+                        "polarisation (16,128,000 visibilities)", "n_vis": n,
+            "e2e_ms": s_e2e * 1e3, "e2e_mvis_s": n / s_e2e / 1e6,
+            "kernel_ms": ms_k, "kernel_mvis_s": n / ms_k / 1e3,
+            "kernel_gb_s": nbytes / (ms_k * 1e-3) / 1e9,
+            "note": "e2e: host blocks (numpy) to device arrays, host packing into pinned "
+                    "buffers included; kernel: uvw metres -> wavelengths (bit-exact), vis "
+                    "complex128 -> complex64, antennas, inputs resident"}
+
+
 MEASURES = {"plain": measure_plain, "wproj": measure_wproj, "diff": measure_diff,
             "wstack": measure_wstack, "aw": measure_aw, "wtowers": measure_wtowers,
-            "recombine": measure_recombine, "szetan": measure_szetan}
+            "recombine": measure_recombine, "szetan": measure_szetan, "ingest": measure_ingest}
 
 
 def run(only=None, steps=None):

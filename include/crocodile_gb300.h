@@ -409,6 +409,35 @@ int cg_aw_kernels(const void *A_c128, int nA, int SA, const void *W_c128,
                   void *workspace, size_t workspace_bytes, int32_t *d_status,
                   cg_stream_t stream);
 
+/* ---------------------------------------------------------------- ingest
+ * Visibility blocks as the reference's HDF5 files hold them (a vis/[a1]/[a2]
+ * group per baseline: frequency [nchan] Hz, time [nrow], uvw [nrow, 3]
+ * metres, vis [nrow, nchan, npol] complex128) and the arl Visibility table
+ * (antenna1, antenna2 per row), flattened into the gridder's rows in the
+ * order of collect_blocks (scripts/image_dataset.py:75-87): block by block,
+ * row by row, channel by channel.  Per output row o:
+ *   uvw_lambda[o] = uvw[r] * frequency[c] / 299792458  (data_models.py:198-202;
+ *                   IEEE-rounded, bit-identical to numpy)
+ *   src[o]        = (antenna1[r], antenna2[r], time[r], frequency[c])  (FP64)
+ *   vis_out[o]    = vis[r, c, pol]  (complex64 or complex128)
+ * blocks: device array; the inputs are the blocks' columns concatenated
+ * (row_start, freq_start, vis_start index them).  Any output may be NULL.  A
+ * block with pol >= npol, nchan <= 0 or nrow * nchan >= 2^31 counts an
+ * index error in d_status and is skipped. */
+typedef struct {
+  int64_t row_start;  /* first row of the block in uvw_m / time / a1 / a2 */
+  int64_t freq_start; /* first channel of the block in freq */
+  int64_t vis_start;  /* first element of the block's vis [nrow][nchan][npol] */
+  int64_t out_start;  /* first output row of the block */
+  int32_t nrow, nchan, npol, pad;
+} cg_vis_block;
+int cg_ingest_blocks(const cg_vis_block *blocks, int nblocks, const double *uvw_m,
+                     const double *time, const int32_t *a1, const int32_t *a2,
+                     const double *freq, const void *vis_c128, int pol,
+                     double *uvw_lambda, double *src, int32_t *a1_out,
+                     int32_t *a2_out, void *vis_out, int vis_c64, int32_t *d_status,
+                     cg_stream_t stream);
+
 /* ---------------------------------------------------------------- Sze-Tan
  * Optimal gridding functions (crocodile/antialias.py).  All arrays are FP64
  * device arrays; R is the half support (2R <= 32).

@@ -16,6 +16,15 @@ reference functions are broken as shipped (NameError) and are restated with
 the minimal fix, documented at each one: ``w_slice_imaging``,
 ``w_slice_predict``, ``w_cache_predict``.
 
+Sections beyond synthesis.py, each pinned the same way: the Sze-Tan
+gridder (crocodile/antialias.py; tests/golden/make_szetan.py), facet <->
+subgrid recombination (examples/notebooks/facet-subgrid-impl.ipynb executed
+by tests/golden/make_recombine.py; the raw-layout primitives of
+examples/grid/recombine.c are tied to it by tests/test_recombine_cpu.py),
+visibility ingest (scripts/image_dataset.py's collect_blocks run with arl's
+Visibility by tests/golden/make_ingest.py), and w-towers (pinned by
+reduction to w_cache_imaging).
+
 Vectorisation note: ``convgrid`` here adds the S x S footprints with
 ``numpy.add.at`` in visibility order, which performs exactly the same
 sequence of complex128 additions per grid cell as the reference's per-row
@@ -1034,3 +1043,41 @@ def rc_add_facet_raw(xM, xM_yN, facet_offset, nmbf, out):
     for i in range(xM_yN):
         out[(i - xM_yN // 2 + off) % xM] += nmbf[(i + xM_yN // 2) % xM_yN] / xM
     return out
+
+
+# --------------------------------------------------------------------------
+# visibility ingest: collect_blocks (scripts/image_dataset.py:75-87) over
+# per-baseline blocks, uvw_lambda as arl/data_models.py:198-202 (c = the SI
+# value astropy's const.c holds).  Each block: dict or object with
+# frequency [nchan], time [nrow], uvw [nrow, 3], antenna1, antenna2 [nrow],
+# vis [nrow, nchan, npol].
+
+C_LIGHT = 299792458.0
+
+
+def _col(b, name):
+    return numpy.asarray(b[name] if isinstance(b, dict) else getattr(b, name))
+
+
+def collect_blocks(blocks, pol=0):
+    """(uvw_lambda [n, 3], src [n, 4], vis [n]) in block, row, channel order,
+    whole blocks at a time as the reference's numpy code (the same
+    elementwise operations: (uvw * f) / c)."""
+    uvw, src, vis = [], [], []
+    for b in blocks:
+        freq, time = _col(b, "frequency"), _col(b, "time")
+        u, v = _col(b, "uvw"), _col(b, "vis")
+        a1, a2 = _col(b, "antenna1"), _col(b, "antenna2")
+        nrow, nchan = len(time), len(freq)
+        uvw.append((u[:, None, :] * freq[None, :, None] / C_LIGHT).reshape(-1, 3))
+        s = numpy.empty((nrow, nchan, 4))
+        s[:, :, 0] = a1[:, None]
+        s[:, :, 1] = a2[:, None]
+        s[:, :, 2] = time[:, None]
+        s[:, :, 3] = freq[None, :]
+        src.append(s.reshape(-1, 4))
+        vis.append(v[:, :, pol].reshape(-1))
+    if not uvw:
+        return numpy.zeros((0, 3)), numpy.zeros((0, 4)), numpy.zeros(0, dtype=complex)
+    return (numpy.concatenate(uvw), numpy.concatenate(src),
+            numpy.concatenate(vis).astype(complex))
