@@ -21,6 +21,7 @@ from . import _lib as L
 from . import autotune
 from . import configs
 from . import engine as E
+from . import synthesis
 
 
 def _time(fn, steps, warmup=2):
@@ -60,6 +61,39 @@ def _aa_kernel(N, Q=8, S=8, c=8):
     return synthesis.kernel_oversample(synthesis.anti_aliasing_function(N, 0, c), Q, S)
 
 
+def _drivers(theta, lam, uvw, vis, imgfn, predfn, steps=3, **kw):
+    """do_imaging and do_predict (synthesis.py:883-927) end to end from numpy,
+    the FP32 form against the FP64 form: rel-L2 of the dirty image, the PSF
+    and the predicted visibilities (of the FP64 dirty image as the model), and
+    the FP32 drivers' times (host arrays in and out)."""
+    from . import synthesis as S
+    d, p, _ = S.do_imaging(theta, lam, uvw, None, vis, imgfn, precision="fp32", **kw)
+    d64, p64, _ = S.do_imaging(theta, lam, uvw, None, vis, imgfn, precision="fp64", **kw)
+    v = S.do_predict(theta, lam, uvw, None, d64, predfn, precision="fp32", **kw)
+    v64 = S.do_predict(theta, lam, uvw, None, d64, predfn, precision="fp64", **kw)
+
+    def rel(a, b):
+        return float(numpy.linalg.norm(numpy.asarray(a) - b) / numpy.linalg.norm(b))
+
+    def host_ms(fn):
+        fn()
+        ts = []
+        for _ in range(steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(1e3 * (time.perf_counter() - t0))
+        return statistics.median(ts)
+
+    return {"rel_err_dirty_image": rel(d, d64), "rel_err_psf": rel(p, p64),
+            "rel_err_predict": rel(v, v64),
+            "do_imaging_ms": host_ms(lambda: S.do_imaging(theta, lam, uvw, None, vis, imgfn,
+                                                          precision="fp32", **kw)),
+            "do_predict_ms": host_ms(lambda: S.do_predict(theta, lam, uvw, None, d64, predfn,
+                                                          precision="fp32", **kw))}
+
+
 def measure_plain(steps=20):
     """conv_imaging + conv_predict, 1024^2, 200k visibilities, separable AA kernel S 8 Q 8."""
     w = configs.plain()
@@ -91,7 +125,9 @@ def measure_plain(steps=20):
     return {"workload": w.name, "n_vis": n, "ms": ms, "mvis_s": n / ms / 1e3, "launch": launch,
             "ms_eager": ms_eager,
             "plain_fp64_ms": ms64, "plain_fp64_mvis_s": n / ms64 / 1e3, "speedup": ms64 / ms,
-            "rel_err_grid": _rel(g, g64), "rel_err_degrid": _rel(out["v"], out["v64"])}
+            "rel_err_grid": _rel(g, g64), "rel_err_degrid": _rel(out["v"], out["v64"]),
+            "drivers": _drivers(w.theta, w.lam, w.uvw, w.vis, synthesis.conv_imaging,
+                                synthesis.conv_predict, kv=kv)}
 
 
 def measure_wproj(steps=20):
@@ -132,7 +168,10 @@ def measure_wproj(steps=20):
     return {"workload": w.name, "n_vis": n, "ms": ms, "mvis_s": n / ms / 1e3, "tuning": tuned,
             "launch": launch, "ms_eager": ms_eager,
             "plain_fp64_ms": ms64, "plain_fp64_mvis_s": n / ms64 / 1e3, "speedup": ms64 / ms,
-            "rel_err_grid": _rel(g, g64)}
+            "rel_err_grid": _rel(g, g64),
+            "drivers": _drivers(w.theta, w.lam, w.uvw, w.vis, synthesis.w_cache_imaging,
+                                synthesis.w_cache_predict, wstep=w.params["wstep"],
+                                NpixFF=w.params["NpixFF"], NpixKern=w.S, Qpx=w.Q)}
 
 
 def measure_diff(steps=20):
