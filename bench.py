@@ -713,6 +713,18 @@ def run_ours(args):
                 g["cpu_oracle"] = {"mvis_s": nb / dt / 1e6, "cores": 1, "kind": "port",
                                    "sample": "the first 200 of 2016 blocks (%d visibilities), "
                                              "numpy collect_blocks, %.2f s" % (nb, dt)}
+            a = cfg_results.get("awtowers")
+            if a:
+                from oracle import crocodile_oracle as O
+                w, src, aimage = bench_configs.awtowers_workload()
+                sel = numpy.isin(src[:, 0] * 16 + src[:, 1], [1, 2, 17])[:len(w.uvw)]
+                t0 = time.perf_counter()
+                O.aw_towers_imaging(w.theta, w.lam, w.uvw[sel], src[sel], w.vis[sel], 64, 16,
+                                    w.params["wstep"], aimage)
+                dt = time.perf_counter() - t0
+                a["cpu_oracle"] = {"mvis_s": int(sel.sum()) / dt / 1e6, "cores": 1, "kind": "port",
+                                   "sample": "3 of 120 baselines (%d visibilities), %.2f s"
+                                             % (int(sel.sum()), dt)}
             z = cfg_results.get("szetan")
             if z:
                 sec, how = szetan_cpu_correction_s(z["h"])

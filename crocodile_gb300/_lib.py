@@ -77,6 +77,10 @@ SIGNATURES = {
     "cg_towers_add": (c_int, [P, c_int, c_int, P, c_int, P, P]),
     "cg_towers_cut": (c_int, [P, c_int, P, c_int, c_int, P, P]),
     "cg_towers_expand": (c_int, [P, c_int, c_double, P, P, c_int, P, P, P]),
+    "cg_awtower_keys": (c_int, [P, c_int64, c_int64, c_double, c_int, c_double, P, P, c_int, P,
+                                P, P, P, P, P]),
+    "cg_awtowers_combine": (c_int, [P, c_int, c_int, c_double, P, P, c_int, P, P, P, P, c_int, P,
+                                    P, P]),
     "cg_ingest_blocks": (c_int, [P, c_int, P, P, P, P, P, P, c_int, P, P, P, P, P, c_int, P, P]),
     "cg_szetan_gridding": (c_int, [P, c_int, c_double, c_int, P, P, c_int, P, P]),
     "cg_szetan_correction_workspace_bytes": (c_size_t, [c_int]),

@@ -432,6 +432,49 @@ def measure_szetan(steps=5):
             "note": "host round trip included (numpy in and out); FP64"}
 
 
+def awtowers_workload(nant=16, ntime=125, nchan=16, s=64, seed=8):
+    """AW-towers input of the AW workload's kind: Earth-rotation tracks of 16
+    antennas (120 baselines x 125 hour angles x 16 channels, 240,000
+    visibilities) on the 8192^2 grid, 64^2 sub-grids, per-antenna A-images
+    (smooth random phase screens)."""
+    w = configs.aw(nant=nant, ntime=ntime, nchan=nchan)
+    rng = numpy.random.default_rng(seed)
+    c = (numpy.arange(s) - s // 2) / s
+    m, l = numpy.meshgrid(c, c, indexing="ij")
+    aimage = numpy.array([(1 + 0.1 * rng.random()) * numpy.exp(
+        2j * numpy.pi * 0.2 * (rng.normal() * l + rng.normal() * m + rng.normal() * l * m))
+        for _ in range(nant)])
+    src = numpy.column_stack([w.params["a1"], w.params["a2"]])
+    return w, src, aimage
+
+
+def measure_awtowers(steps=3):
+    """AW-towers imaging (awtowers.ipynb cells 17-22) of awtowers_workload(): 64^2
+    sub-grids with a 16-cell margin, w-planes of the workload's w step, the
+    anti-aliasing kernel (support 6, oversampled 4096 times) on 128^2 layer
+    grids.  Timed end to end (binning, key compaction, plan, one gridder
+    launch over every (chunk, plane, baseline) layer, batched FFTs, combine
+    with the antenna ratios and Fresnel factors, sub-grid add)."""
+    w, src, aimage = awtowers_workload()
+    n = len(w.uvw)
+    uvw = E.cuda_tensor(w.uvw, torch.float64)
+    vis = E.cuda_tensor(w.vis, E.CF)
+    s, margin, wstep = 64, 16, w.params["wstep"]
+    run = lambda: synthesis.aw_towers_imaging(w.theta, w.lam, uvw, src, vis, s, margin, wstep,
+                                              aimage)
+    ms = _time(run, steps, warmup=1)
+    st = E.Status()
+    key, _, b = E.awtower_keys(uvw, w.theta, s - margin, wstep, src[:, 0], src[:, 1],
+                               len(aimage), st)
+    nk = (b[1] - b[0] + 1) * (b[3] - b[2] + 1) * (b[5] - b[4] + 1) * len(aimage) ** 2
+    _, used = E.compact_keys(key, nk, st)
+    return {"workload": "AW-towers, %d visibilities (16 antennas, 125 hour angles x 16 "
+                        "channels), 8192^2, 64^2 sub-grids margin 16, w step %.0f" % (n, wstep),
+            "n_vis": n, "ms": ms, "mvis_s": n / ms / 1e3, "layers": int(used.shape[0]),
+            "note": "end to end from device-resident uvw / vis; parity with the reference "
+                    "notebook and the oracle in tests/test_gpu_awtowers.py"}
+
+
 def ingest_blocks(seed=5, nant=64, ntime=125, nchan=64, npol=1):
     """Synthetic per-baseline blocks of the AW workload's shape: 2016 baselines
     x 125 times x 64 channels (16,128,000 visibilities), uvw in metres."""
@@ -504,7 +547,8 @@ def measure_ingest(steps=3, blocks=None):
 
 MEASURES = {"plain": measure_plain, "wproj": measure_wproj, "diff": measure_diff,
             "wstack": measure_wstack, "aw": measure_aw, "wtowers": measure_wtowers,
-            "recombine": measure_recombine, "szetan": measure_szetan, "ingest": measure_ingest}
+            "recombine": measure_recombine, "szetan": measure_szetan, "ingest": measure_ingest,
+            "awtowers": measure_awtowers}
 
 
 def run(only=None, steps=None):

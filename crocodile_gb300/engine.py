@@ -542,6 +542,43 @@ def towers_expand(images, theta, layer_w, chunk_first, status):
 
 
 # --------------------------------------------------------------------------
+# AW-towers (examples/notebooks/awtowers.ipynb cells 17-22)
+
+def awtower_keys(uvw, theta, chunk, wstep, a1, a2, nant, status):
+    """(key int32 [n], chunk/plane-relative uvw [n, 3], (ubmin, ubmax, vbmin, vbmax,
+    wpmin, wpmax)) of cg_awtower_keys."""
+    uvw = cuda_tensor(uvw, torch.float64)
+    a1 = cuda_tensor(a1, torch.int32)
+    a2 = cuda_tensor(a2, torch.int32)
+    n = uvw.shape[0]
+    key = torch.empty(n, dtype=torch.int32, device="cuda")
+    rel = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    dmm = torch.empty(6, dtype=torch.int32, device="cuda")
+    hb = (ctypes.c_int32 * 6)()
+    L.call("cg_awtower_keys", _p(uvw), uvw.stride(0), n, float(theta), int(chunk), float(wstep),
+           _p(a1), _p(a2), int(nant), _p(key), _p(rel), _p(dmm), hb, _p(status.t), stream())
+    return key, rel, tuple(int(x) for x in hb)
+
+
+def awtowers_combine(stack, s, theta, corr, aimage, layer_a1, layer_a2, layer_w, chunk_first,
+                     status):
+    """Per chunk, the sum of its layers' cut images times corr, the antenna ratio and
+    the inverse Fresnel factor (rolled, for fft_raw and towers_add)."""
+    co = cuda_tensor(corr, torch.float32)
+    ai = cuda_tensor(aimage, CF)
+    a1 = cuda_tensor(layer_a1, torch.int32)
+    a2 = cuda_tensor(layer_a2, torch.int32)
+    lw = cuda_tensor(layer_w, torch.float64)
+    cf = cuda_tensor(chunk_first, torch.int32)
+    nchunks = int(cf.shape[0]) - 1
+    out = torch.empty((nchunks, s, s), dtype=CF, device="cuda")
+    L.call("cg_awtowers_combine", _p(stack), int(stack.shape[0]), int(s), float(theta), _p(co),
+           _p(ai), int(ai.shape[0]), _p(a1), _p(a2), _p(lw), _p(cf), nchunks, _p(out),
+           _p(status.t), stream())
+    return out
+
+
+# --------------------------------------------------------------------------
 # Sze-Tan optimal gridding functions
 
 def szetan_gridding(h_ext, x0, R, kinv, nu):

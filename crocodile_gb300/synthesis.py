@@ -863,6 +863,91 @@ def w_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wincrement
     return _host(grid, like=uvw)
 
 
+@functools.lru_cache(maxsize=8)
+def _aw_towers_tables(N, s, aa_support, aa_over):
+    """The anti-aliasing kernel table (kernel_oversample of the grid's PSWF, as the
+    notebook's aa_gcf) and the correction of a cut layer image, aa_s x aa_s /
+    aa_2s x aa_2s on the cut: built once per (grid, sub-grid, support, oversampling)."""
+    aa = anti_aliasing_function(N, 0, aa_support)
+    aa_s = anti_aliasing_function(s, 0, aa_support)
+    aa_2s = anti_aliasing_function(2 * s, 0, aa_support)
+    cut = aa_2s[s // 2:s // 2 + s]
+    corr = E.cuda_tensor((numpy.outer(aa_s, aa_s) / numpy.outer(cut, cut)).astype(numpy.float32),
+                         torch.float32)
+    ktab = E.KernelTable.from_gcf(kernel_oversample(numpy.real(aa), aa_over, aa_support), 0,
+                                  E.CF)
+    return ktab, corr
+
+
+def aw_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wstep, aimage,
+                      aa_support=6, aa_over=4096, precision=None, tile=32, gridder="auto"):
+    """AW-towers imaging (examples/notebooks/awtowers.ipynb cells 17-22, without a
+    phase-centre shift): visibilities binned into centred uv chunks of ``subgrid_size
+    - margin`` cells (floor(u theta / C + 1/2)), w-planes of width ``wstep`` and
+    baselines ``src[:, 0:2]`` (antenna indices into ``aimage``); each (chunk, plane,
+    baseline) gridded with the anti-aliasing kernel (``aa_support``, oversampled
+    ``aa_over`` times) relative to the chunk centre and the plane's w on a 2s x 2s grid
+    at 2 theta; its image cut to s x s and corrected for the kernel, times
+    aimage[a2] / aimage[a1]; each plane moved to w = 0 (divided by
+    w_kernel_function(l, m, w_plane)); each chunk's FFT added into the grid.  Returns
+    the grid; real(ifft(grid)) / aa x aa / sum(weights) is the notebook's image.  All
+    layers grid in one launch and transform in batched FFTs.  FP32 only; needs even
+    subgrid_size and margin, margin >= aa_support."""
+    if _prec(precision) != "fp32":
+        raise ValueError("aw_towers_imaging runs the FP32 path only")
+    N = int(numpy.ceil(theta * lam))
+    s, C = int(subgrid_size), int(subgrid_size) - int(margin)
+    if C < 1 or margin < aa_support or s % 2 or margin % 2:
+        raise ValueError("need even subgrid_size and margin, aa_support <= margin < subgrid_size")
+    grid = torch.zeros((N, N), dtype=E.CF, device="cuda")
+    n = _nrows(uvw)
+    if n == 0:
+        return _host(grid, like=uvw)
+    ai = numpy.asarray(aimage) if not _is_dev(aimage) else aimage
+    nant = int(ai.shape[0])
+    if tuple(ai.shape[1:]) != (s, s):
+        raise ValueError("aimage must be [antennas, subgrid_size, subgrid_size]")
+    uvw_t = E.cuda_tensor(uvw, torch.float64)
+    srcn = src if _is_dev(src) else numpy.asarray(src)
+    a1 = E.cuda_tensor(srcn[:, 0], torch.int32)
+    a2 = E.cuda_tensor(srcn[:, 1], torch.int32)
+    vis_t = E.cuda_tensor(vis, E.CF)
+    st = E.Status()
+    key, rel, (ubmin, ubmax, vbmin, vbmax, wpmin, wpmax) = E.awtower_keys(
+        uvw_t, theta, C, wstep, a1, a2, nant, st)
+    st.check()
+    nub, nvb, nwp = ubmax - ubmin + 1, vbmax - vbmin + 1, wpmax - wpmin + 1
+    row, used = E.compact_keys(key, nub * nvb * nwp * nant * nant, st)
+    used = used.cpu().numpy().astype(numpy.int64)
+    bl, rest = used % (nant * nant), used // (nant * nant)
+    plane = rest % nwp + wpmin
+    chunk, first = numpy.unique(rest // nwp, return_index=True)
+    chunk_first = numpy.append(first, len(used)).astype(numpy.int32)
+    ub, vb = chunk % nub + ubmin, chunk // nub + vbmin
+    # the notebook's sub-grid corner: xy_min = C (ub - 1/2) - (margin + 1) // 2
+    xy = numpy.column_stack([C * (ub - 0.5), C * (vb - 0.5)]) - (margin + 1) // 2
+    origin = (N // 2 + xy.astype(int)).astype(numpy.int32)
+    ktab, corr = _aw_towers_tables(N, s, int(aa_support), int(aa_over))
+    stack = torch.zeros((len(used), 2 * s, 2 * s), dtype=E.CF, device="cuda")
+    plan = E.Plan(rel, s / theta, (2 * s, 2 * s), ktab, None, status=st,
+                  layers=(len(used), row), tile=tile)
+    tiles = len(used) * (-(-2 * s // plan.info()["tile"])) ** 2
+    if gridder == "sparse" or (gridder == "auto" and n < 16 * tiles):
+        plan.grid_sparse(ktab, vis_t, stack)
+    elif gridder in ("auto", "tiled"):
+        plan.grid(ktab, vis_t, stack)
+    else:
+        raise ValueError("gridder must be 'auto', 'tiled' or 'sparse'")
+    E.fft_raw(stack, True)
+    sub = E.awtowers_combine(stack, s, theta, corr, ai, bl // nant, bl % nant,
+                             plane * float(wstep), chunk_first, st)
+    del stack
+    E.fft_raw(sub, False)
+    E.towers_add(sub, origin, grid)
+    st.check()
+    return _host(grid, like=uvw)
+
+
 def w_towers_predict(theta, lam, uvw, src, guv, subgrid_size, margin, wincrement, wstep=2000,
                      kernel_cache=None, kernel_fn=w_kernel, precision=None, tile=32, **kwargs):
     """w-towers predict (examples/notebooks/wtowers-predict.ipynb), the reverse of

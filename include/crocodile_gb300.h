@@ -409,6 +409,32 @@ int cg_aw_kernels(const void *A_c128, int nA, int SA, const void *W_c128,
                   void *workspace, size_t workspace_bytes, int32_t *d_status,
                   cg_stream_t stream);
 
+/* AW-towers (examples/notebooks/awtowers.ipynb cells 17-22): w-towers with
+ * per-baseline antenna terms applied in each sub-grid's image space.
+ * cg_awtower_keys bins visibilities into centred uv chunks, w-planes and
+ * baselines, as the notebook (IEEE double, bit-identical to numpy):
+ *   ub = floor(u*theta/chunk + 1/2), vb likewise, wp = rint(w / wstep),
+ *   key = (((vb-vbmin)*nub + (ub-ubmin))*nwp + (wp-wpmin))*nant^2 + a1*nant + a2,
+ *   rel = (u - chunk*ub/theta, v - chunk*vb/theta, w - wp*wstep);
+ * h_bounds (host) = {ubmin, ubmax, vbmin, vbmax, wpmin, wpmax}; synchronises
+ * the stream.  The (chunk, plane, baseline) layers are then gridded with the
+ * anti-aliasing kernel on 2s x 2s grids (a layered plan on rel with lam =
+ * s / theta) and inverse-transformed by an unshifted cg_fft_raw.
+ * cg_awtowers_combine: out[c] = sum over layers L in [chunk_first[c],
+ * chunk_first[c+1]) of the centred image of layer L cut to its middle s x s,
+ * times corr [s, s], times aimage[layer_a2[L]] / aimage[layer_a1[L]]
+ * ([nant, s, s] complex64), divided by w_kernel_function(l, m, layer_w[L]);
+ * written rolled for a forward cg_fft_raw and cg_towers_add. */
+int cg_awtower_keys(const double *uvw, int64_t stride, int64_t n, double theta, int chunk,
+                    double wstep, const int32_t *a1, const int32_t *a2, int nant,
+                    int32_t *key_out, double *rel_out, int32_t *d_minmax, int32_t *h_bounds,
+                    int32_t *d_status, cg_stream_t stream);
+int cg_awtowers_combine(const void *stack_c64, int layers, int s, double theta,
+                        const float *corr, const void *aimage_c64, int nant,
+                        const int32_t *layer_a1, const int32_t *layer_a2,
+                        const double *layer_w, const int32_t *chunk_first, int nchunks,
+                        void *out_c64, int32_t *d_status, cg_stream_t stream);
+
 /* ---------------------------------------------------------------- ingest
  * Visibility blocks as the reference's HDF5 files hold them (a vis/[a1]/[a2]
  * group per baseline: frequency [nchan] Hz, time [nrow], uvw [nrow, 3]

@@ -1081,3 +1081,66 @@ def collect_blocks(blocks, pol=0):
         return numpy.zeros((0, 3)), numpy.zeros((0, 4)), numpy.zeros(0, dtype=complex)
     return (numpy.concatenate(uvw), numpy.concatenate(src),
             numpy.concatenate(vis).astype(complex))
+
+
+# --------------------------------------------------------------------------
+# AW-towers imaging (examples/notebooks/awtowers.ipynb cells 17-22) with no
+# phase-centre shift (dl = dm = 0, T = identity).  Per uv chunk (centred
+# bins floor(u theta / C + 1/2), C = subgrid - margin), per w-plane
+# (around(w / wstep)) and per baseline, the visibilities are gridded with the
+# anti-aliasing kernel relative to the chunk centre on a 2s x 2s grid at 2
+# theta (pregrid_tower_plane), transformed, corrected for the kernel, cut to
+# s x s and multiplied by aimage[a2] / aimage[a1] (grid_tower_plane); each
+# plane is moved to w = 0 by dividing by w_kernel_function(l, m, wp wstep)
+# (the closed form of the notebook's wkern ** (wp - last_wp) chain; the
+# notebook skips one step of that chain after a chunk's first plane when it
+# is the data set's lowest, which the golden data avoids); the chunk's FFT
+# is added into the grid (grid_tower, grid_towers).
+
+def aw_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wstep, aimage,
+                      aa_support=6, aa_over=4096):
+    """(grid_sum, image): the uv grid and real(ifft(grid_sum)) / aa x aa."""
+    s, C = int(subgrid_size), int(subgrid_size) - int(margin)
+    N = int(numpy.ceil(theta * lam))
+    aa = anti_aliasing_function(N, 0, aa_support)
+    aa_sub = anti_aliasing_function(s, 0, aa_support)
+    aa_sub2 = anti_aliasing_function(2 * s, 0, aa_support)
+    aa_gcf = kernel_oversample(aa, aa_over, aa_support)
+    l, m = kernel_coordinates(s, theta)
+    uvw = numpy.asarray(uvw, dtype=float)
+    src = numpy.asarray(src)
+    vis = numpy.asarray(vis)
+    ubin = numpy.floor(uvw[:, 0] * theta / C + 0.5).astype(int)
+    vbin = numpy.floor(uvw[:, 1] * theta / C + 0.5).astype(int)
+    wplane = numpy.around(uvw[:, 2] / wstep).astype(int)
+    grid = numpy.zeros((N, N), dtype=complex)
+    uvw_size = s / theta
+    for ub in range(ubin.min(), ubin.max() + 1):
+        for vb in range(vbin.min(), vbin.max() + 1):
+            sel = (ubin == ub) & (vbin == vb)
+            if not numpy.any(sel):
+                continue
+            xy_min = C * numpy.array([ub - 0.5, vb - 0.5])
+            xy_max = C * numpy.array([ub + 0.5, vb + 0.5])
+            uv_mid = (xy_max + xy_min) // 2 / theta
+            xy_min -= (margin + 1) // 2
+            img = numpy.zeros((s, s), dtype=complex)
+            for wp in numpy.unique(wplane[sel]):
+                slc = sel & (wplane == wp)
+                uvw_mid = numpy.hstack([uv_mid, [wp * wstep]])
+                plane = numpy.zeros((s, s), dtype=complex)
+                for a1, a2 in numpy.unique(src[slc], axis=0):
+                    b = slc & (src[:, 0] == a1) & (src[:, 1] == a2)
+                    pg = conv_imaging(2 * theta, uvw_size, uvw[b] - uvw_mid,
+                                      numpy.empty((int(b.sum()), 0)), vis[b], aa_gcf)
+                    pim = ifft(pg) / numpy.outer(aa_sub2, aa_sub2)
+                    pim = extract_mid(pim, s) * numpy.outer(aa_sub, aa_sub)
+                    plane += pim * aimage[a2] / aimage[a1]
+                img += plane / w_kernel_function(l, m, wp * wstep)
+            sub = fft(img)
+            x0, y0 = N // 2 + xy_min.astype(int)
+            x1, y1 = x0 + s, y0 + s
+            x0b, y0b, x1b, y1b = max(x0, 0), max(y0, 0), min(x1, N), min(y1, N)
+            grid[y0b:y1b, x0b:x1b] += sub[y0b - y0:y1b - y0, x0b - x0:x1b - x0]
+    image = numpy.real(ifft(grid)) / numpy.outer(aa, aa)
+    return grid, image
