@@ -9,7 +9,9 @@
 // in FP64, with every product and sum explicitly rounded so the phase is
 // the one numpy evaluates.  aw_kernel_fn (:701-734) convolves two A kernels
 // and then the result with every oversampled w sub-kernel ('same' crops as
-// scipy.signal.convolve2d), on CUDA cores.
+// scipy.signal.convolve2d), on CUDA cores: complex64 tables of 16 x 16
+// kernels by 32 x 32 FFTs (aw_fft.cu), other sizes and complex128 output by
+// the direct sums below.
 #include <cufft.h>
 
 #include <algorithm>
@@ -19,6 +21,11 @@
 namespace cg {
 
 int fft_plan(int batch, int H, int W, cufftType type, cufftHandle *out);
+bool aw_fft_supported(int SA, int S);
+size_t aw_fft_workspace_bytes(int nk, int nW, int Q);
+int aw_fft_launch(const float2 *akern, int nk, const void *W, int nW, int Q, int S,
+                  const int32_t *wi, void *out, int out_c64, void *ws, size_t ws_bytes,
+                  int32_t *d_status, cudaStream_t st);
 
 struct FarField {
   int kind;  // 0: from ff array, 1: w-kernel phase
@@ -183,6 +190,10 @@ static int oversample_run(FarField F, int batch, int s, void *out, bool out_c64,
 // sub-kernels f, FP32 products with FP32 accumulation, one CTA per (k, f).
 // 'same' keeps the size of the first operand, centred on the full output:
 //   same[i, j] = sum_{p, q} a[p, q] * b[i + o - p, j + o - q],  o = (nb - 1) / 2.
+// R: the accumulation type.  double for complex128 output (the reference's
+// FP64); float for the complex64 tables, whose convolutions that follow run
+// in FP32 anyway.
+template <typename R>
 __global__ void k_aw_akern(const double2 *__restrict__ A, int SA,
                            const int32_t *__restrict__ a1, const int32_t *__restrict__ a2,
                            int nA, float2 *__restrict__ akern, int32_t *status) {
@@ -192,23 +203,34 @@ __global__ void k_aw_akern(const double2 *__restrict__ A, int SA,
     if (threadIdx.x == 0) atomicAdd(&status[ST_INDEX], 1);
     return;
   }
-  const double2 *P = A + (size_t)i1 * SA * SA, *R = A + (size_t)i2 * SA * SA;
+  // both A kernels staged in shared memory in the accumulation type
+  extern __shared__ unsigned char aw_sh[];
+  R *sp = (R *)aw_sh, *sr = sp + 2 * SA * SA;
+  for (int t = threadIdx.x; t < SA * SA; t += blockDim.x) {
+    const double2 u = A[(size_t)i1 * SA * SA + t], v = A[(size_t)i2 * SA * SA + t];
+    sp[2 * t] = (R)u.x;
+    sp[2 * t + 1] = (R)u.y;
+    sr[2 * t] = (R)v.x;
+    sr[2 * t + 1] = (R)v.y;
+  }
+  __syncthreads();
   const int o = (SA - 1) / 2;
   for (int t = threadIdx.x; t < SA * SA; t += blockDim.x) {
     const int i = t / SA, j = t - (t / SA) * SA;
-    double2 acc = make_double2(0.0, 0.0);
+    R ax = 0, ay = 0;
     for (int p = 0; p < SA; ++p) {
       const int y = i + o - p;
       if (y < 0 || y >= SA) continue;
       for (int q = 0; q < SA; ++q) {
         const int x = j + o - q;
         if (x < 0 || x >= SA) continue;
-        const double2 u = P[p * SA + q], v = R[y * SA + x];
-        acc.x += u.x * v.x - u.y * v.y;
-        acc.y += u.x * v.y + u.y * v.x;
+        const R ux = sp[2 * (p * SA + q)], uy = sp[2 * (p * SA + q) + 1];
+        const R vx = sr[2 * (y * SA + x)], vy = sr[2 * (y * SA + x) + 1];
+        ax += ux * vx - uy * vy;
+        ay += ux * vy + uy * vx;
       }
     }
-    akern[(size_t)k * SA * SA + t] = make_float2((float)acc.x, (float)acc.y);  // FP32 from here on
+    akern[(size_t)k * SA * SA + t] = make_float2((float)ax, (float)ay);  // FP32 from here on
   }
 }
 
@@ -408,7 +430,9 @@ static size_t aw_ws_akern_bytes(int nk, int SA) {
 }
 
 size_t cg_aw_kernels_workspace_bytes(int nk, int SA, int nW, int Q, int S) {
-  return aw_ws_akern_bytes(nk, SA) + (size_t)std::max(nW, 1) * Q * Q * S * S * sizeof(float2);
+  size_t rest = (size_t)std::max(nW, 1) * Q * Q * S * S * sizeof(float2);
+  if (aw_fft_supported(SA, S)) rest = std::max(rest, aw_fft_workspace_bytes(nk, nW, Q));
+  return aw_ws_akern_bytes(nk, SA) + rest;
 }
 
 int cg_aw_kernels(const void *A, int nA, int SA, const void *Wk, int nW, int Q, int S,
@@ -426,8 +450,28 @@ int cg_aw_kernels(const void *A, int nA, int SA, const void *Wk, int nW, int Q, 
   cudaStream_t st = (cudaStream_t)stream;
   float2 *akern = (float2 *)ws;
   float2 *wk32 = (float2 *)((char *)ws + aw_ws_akern_bytes(nk, SA));
-  k_aw_akern<<<nk, 256, 0, st>>>((const double2 *)A, SA, a1, a2, nA, akern, d_status);
+  const bool fft_form = out_c64 && aw_fft_supported(SA, S);
+  // shared staging of the two A kernels: up to 128 KB at SA = 64 in FP64
+  const size_t sh_a = 4 * (size_t)SA * SA * (fft_form ? sizeof(float) : sizeof(double));
+  if (sh_a > 48 * 1024) {
+    if (fft_form)
+      CG_CUDA(cudaFuncSetAttribute(k_aw_akern<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sh_a));
+    else
+      CG_CUDA(cudaFuncSetAttribute(k_aw_akern<double>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh_a));
+  }
+  if (fft_form)
+    k_aw_akern<float><<<nk, 256, sh_a, st>>>((const double2 *)A, SA, a1, a2, nA, akern,
+                                             d_status);
+  else
+    k_aw_akern<double><<<nk, 256, sh_a, st>>>((const double2 *)A, SA, a1, a2, nA, akern,
+                                              d_status);
   CG_LAUNCH("aw akern");
+  if (fft_form)  // complex64 tables: the FFT form
+    return aw_fft_launch(akern, nk, Wk, nW, Q, S, wi, out, 1,
+                         (char *)ws + aw_ws_akern_bytes(nk, SA),
+                         ws_bytes - aw_ws_akern_bytes(nk, SA), d_status, st);
   const int64_t nwk = (int64_t)nW * Q * Q * S * S;
   k_c128_to_c64<<<(unsigned)std::min<int64_t>((nwk + 255) / 256, (int64_t)num_sms() * 16), 256, 0,
                   st>>>((const double2 *)Wk, nwk, wk32);

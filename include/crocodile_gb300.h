@@ -400,7 +400,9 @@ int cg_w_kernels(double theta, const double *w_host, int nw, int NpixFF,
  * A: [nA, SA, SA] c128, W: [nW, Q, Q, S, S] c128, out: [nk, Q, Q, SA, SA]
  * c64 or c128.  a1, a2, wi: int32 device arrays.  A kernels are combined
  * in FP64 and rounded once to FP32; W is rounded once to FP32 into the
- * workspace; the Q*Q sub-kernel convolutions use FP32 products and sums.
+ * workspace; the Q*Q sub-kernel convolutions use FP32 arithmetic: direct
+ * sums, or for complex64 output of 16 x 16 kernels with S <= 16 the exact
+ * circular convolution of the zero-padded kernels by 32 x 32 FFTs.
  * Workspace: cg_aw_kernels_workspace_bytes(nk, SA, nW, Q, S) bytes. */
 size_t cg_aw_kernels_workspace_bytes(int nk, int SA, int nW, int Q, int S);
 int cg_aw_kernels(const void *A_c128, int nA, int SA, const void *W_c128,
