@@ -648,6 +648,14 @@ def run_ours(args):
     ms_plain, err_grid, err_degrid = G.plain(args.plain_steps)
     plain_value = n / (ms_plain * 1e-3) / 1e6
 
+    # ---- kernel generation again in the running process (libraries loaded,
+    # FFT plans cached): what a new data set's kernel table costs after the first
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    G._prepare()
+    torch.cuda.synchronize()
+    kgen_warm_ms = 1e3 * (time.perf_counter() - t0)
+
     # ---- roofline of the dominant kernel: algorithmic bytes per launch
     kbytes = G.kernel_bytes_per_vis()
     table_bytes = 0 if kbytes else G.kt.table.numel() * 8
@@ -753,7 +761,8 @@ def run_ours(args):
         "launch": launch, "ms_per_step_eager": ms_eager,
         "kernel_ms": {"grid": ms_grid, "degrid": ms_degrid,
                       "plan_and_grid_zeroing": ms_eager - ms_grid - ms_degrid,
-                      "kernel_generation_once": G.kgen_ms},
+                      "kernel_generation_once": G.kgen_ms,
+                      "kernel_generation_warm": kgen_warm_ms},
         "updates_per_s": 2 * n * S * S / (ms * 1e-3),
         "plain_fp64": {"value": plain_value, "unit": "Mvis/s", "ms_per_step": ms_plain,
                        "form": "complex128, FP64 atomics, " + G.groups_desc},
