@@ -37,12 +37,15 @@
 
 namespace cg {
 int fft_plan(int batch, int H, int W, cufftType type, cufftHandle *out);
+bool dfft_supported(int n);
+int dfft_rows(double2 *data, int64_t batch, int n, int inverse, cudaStream_t st);
 }
 
 struct cg_recombine {
   int N, subgrid_spacing, facet_spacing;
   int yB, yN, yP, xA, xM, xMxN_yP;
   int xM_yP, xM_yN, yP_spacing, xM_spacing;
+  int fft_mode;  // 0: double-float FFTs for power-of-two rows, cuFFT Z2Z otherwise; 1: cuFFT Z2Z
   double *d_Fb, *d_Fn, *d_m;
 };
 
@@ -438,7 +441,11 @@ struct Prec<double2> {
 };
 
 template <typename C>
-int rows_fft(C *data, int batch, int len, int dir, cudaStream_t st) {
+int rows_fft(const cg_recombine *h, C *data, int batch, int len, int dir, cudaStream_t st) {
+  // power-of-two rows in double-float arithmetic on the FP32 units: the FP64
+  // transforms are bound by GB300's FP64 rate
+  if (h->fft_mode == 0 && dfft_supported(len))
+    return dfft_rows((double2 *)data, batch, len, dir == CUFFT_INVERSE, st);
   cufftHandle plan;
   int rc = fft_plan(batch, 1, len, Prec<C>::type, &plan);
   if (rc) return rc;
@@ -493,19 +500,19 @@ int subgrids_to_facet(cg_recombine *h, const void *fs, int centred, int n0, int 
   k_rcT_split<C><<<grid_for((size_t)n0 * n1 * xM_yN * xM_yP), 256, 0, st>>>(
       (const C *)fs, n0 * n1, xM, xM_yN, xM_yP, fo0, fo1, Prec<C>::Fn(h), centred, A);
   CG_LAUNCH("recombine split subgrids");
-  if ((rc = rows_fft<C>(A, n0 * n1 * xM_yN, xM_yP, CUFFT_INVERSE, st))) return rc;
+  if ((rc = rows_fft<C>(h, A, n0 * n1 * xM_yN, xM_yP, CUFFT_INVERSE, st))) return rc;
   k_rcT_scatter<C><<<grid_for((size_t)n0 * xM_yN * yP), 256, 0, st>>>(
       A, n0, n1, xM_yN, xM_yP, h->xMxN_yP, yP, offs1, Prec<C>::m(h), acc);
   CG_LAUNCH("recombine subgrid windows (axis 1)");
-  if ((rc = rows_fft<C>(acc, n0 * xM_yN, yP, CUFFT_FORWARD, st))) return rc;
+  if ((rc = rows_fft<C>(h, acc, n0 * xM_yN, yP, CUFFT_FORWARD, st))) return rc;
   k_rcT_crop_T_pad<C><<<dim3((xM_yP + 31) / 32, (yB + 31) / 32, n0), dim3(32, 8), 0, st>>>(
       acc, n0, xM_yN, yP, yB, xM_yP, B);
   CG_LAUNCH("recombine crop to the facet (axis 1)");
-  if ((rc = rows_fft<C>(B, yB * n0, xM_yP, CUFFT_INVERSE, st))) return rc;
+  if ((rc = rows_fft<C>(h, B, yB * n0, xM_yP, CUFFT_INVERSE, st))) return rc;
   k_rcT_scatter<C><<<grid_for((size_t)yB * yP), 256, 0, st>>>(
       B, yB, n0, 1, xM_yP, h->xMxN_yP, yP, offs0, Prec<C>::m(h), acc2);
   CG_LAUNCH("recombine subgrid windows (axis 0)");
-  if ((rc = rows_fft<C>(acc2, yB, yP, CUFFT_FORWARD, st))) return rc;
+  if ((rc = rows_fft<C>(h, acc2, yB, yP, CUFFT_FORWARD, st))) return rc;
   k_rcT_final<C><<<dim3((yB + 31) / 32, (yB + 31) / 32), dim3(32, 8), 0, st>>>(
       acc2, yP, yB, Prec<C>::Fb(h), out_centred, accumulate, (C *)facet);
   CG_LAUNCH("recombine facet");
@@ -540,19 +547,19 @@ int facet_to_subgrids(cg_recombine *h, const void *facet, int centred, int n0, i
   k_rc_prep_rows<C><<<g1, 256, 0, st>>>((const C *)facet, yB, yB, yP, Prec<C>::Fb(h), centred,
                                          bf);
   CG_LAUNCH("recombine prepare facet (axis 1)");
-  if ((rc = rows_fft<C>(bf, yB, yP, CUFFT_INVERSE, st))) return rc;
+  if ((rc = rows_fft<C>(h, bf, yB, yP, CUFFT_INVERSE, st))) return rc;
   k_rc_window<C><<<grid_for((size_t)n1 * yB * xM_yP), 256, 0, st>>>(
       bf, yB, yP, offs1, n1, xM_yP, h->xMxN_yP, Prec<C>::m(h), mbf);
   CG_LAUNCH("recombine extract subgrid (axis 1)");
-  if ((rc = rows_fft<C>(mbf, n1 * yB, xM_yP, CUFFT_FORWARD, st))) return rc;
+  if ((rc = rows_fft<C>(h, mbf, n1 * yB, xM_yP, CUFFT_FORWARD, st))) return rc;
   k_rc_crop_prep_T<C><<<dim3((yP + 31) / 32, (xM_yN + 31) / 32, n1), dim3(32, 8), 0, st>>>(
       mbf, yB, xM_yP, xM_yN, Prec<C>::Fn(h), Prec<C>::Fb(h), yP, bf2);
   CG_LAUNCH("recombine prepare facet (axis 0)");
-  if ((rc = rows_fft<C>(bf2, n1 * xM_yN, yP, CUFFT_INVERSE, st))) return rc;
+  if ((rc = rows_fft<C>(h, bf2, n1 * xM_yN, yP, CUFFT_INVERSE, st))) return rc;
   k_rc_window<C><<<grid_for((size_t)n0 * n1 * xM_yN * xM_yP), 256, 0, st>>>(
       bf2, n1 * xM_yN, yP, offs0, n0, xM_yP, h->xMxN_yP, Prec<C>::m(h), mbf2);
   CG_LAUNCH("recombine extract subgrid (axis 0)");
-  if ((rc = rows_fft<C>(mbf2, n0 * n1 * xM_yN, xM_yP, CUFFT_FORWARD, st))) return rc;
+  if ((rc = rows_fft<C>(h, mbf2, n0 * n1 * xM_yN, xM_yP, CUFFT_FORWARD, st))) return rc;
   k_rc_crop_T<C><<<dim3((xM_yN + 31) / 32, (xM_yN + 31) / 32, n0 * n1), dim3(32, 8), 0, st>>>(
       mbf2, n1, xM_yP, xM_yN, Prec<C>::Fn(h), out_centred, (C *)nmbf);
   CG_LAUNCH("recombine crop");
@@ -632,6 +639,7 @@ int cg_recombine_create(int image_size, int subgrid_spacing, const double *pswf,
   h->xMxN_yP = xMxN_yP;
   h->xM_yP = xM_yP;
   h->xM_yN = xM_yN;
+  h->fft_mode = 0;
   h->yP_spacing = (int)((long long)subgrid_spacing * yP / image_size);
   h->xM_spacing = (int)((long long)facet_spacing * xM / image_size);
   // generate_Fb / generate_Fn (recombine.c:12-33) from the raw PSWF [yN]
@@ -655,6 +663,12 @@ int cg_recombine_destroy(cg_recombine *h) {
   cudaFree(h->d_Fn);
   cudaFree(h->d_m);
   delete h;
+  return CG_OK;
+}
+
+int cg_recombine_set_fft(cg_recombine *h, int mode) {
+  CG_REQUIRE(h && (mode == 0 || mode == 1), "fft mode 0 (double-float) or 1 (FP64 cuFFT)");
+  h->fft_mode = mode;
   return CG_OK;
 }
 

@@ -29,7 +29,10 @@ and the other direction (notebook cell 18, in 2-D by separability):
   approximation Fb x Fb x the sum of every subgrid's contribution;
 * ``split(subgrids, offs0, offs1, facet_offs0, facet_offs1)``: all facets.
 
-Arrays and FFTs are complex128, as in the reference: Fb = 1 / PSWF spans
+Row transforms of power-of-two length run in double-float arithmetic on the
+FP32 units (``fft="auto"``, about 48 significant bits; GB300's FP64 rate
+bounds an FP64 FFT), other lengths and ``fft="fp64"`` in FP64 (cuFFT Z2Z).
+Arrays are complex128, as in the reference: Fb = 1 / PSWF spans
 many decades towards the facet edge, and the contributions come out of
 intermediates a thousand times larger than their peak, which single
 precision cannot carry (measured: 6e-4 relative error per facet, the
@@ -59,7 +62,7 @@ class Recombine:
     notebook's centred layout (default: ``default_pswf``)."""
 
     def __init__(self, image_size, subgrid_spacing, yB_size, yN_size, yP_size, xA_size, xM_size,
-                 xMxN_yP_size, pswf=None):
+                 xMxN_yP_size, pswf=None, fft="auto"):
         E.require_cuda()
         if pswf is None:
             pswf = default_pswf(image_size, yN_size, xA_size, xM_size)
@@ -77,6 +80,9 @@ class Recombine:
                raw.ctypes.data_as(ctypes.c_void_p), self.yB_size, self.yN_size, self.yP_size,
                self.xA_size, self.xM_size, self.xMxN_yP_size, ctypes.byref(h))
         self._h = h
+        if fft not in ("auto", "fp64"):
+            raise ValueError("fft must be 'auto' (double-float for power-of-two rows) or 'fp64'")
+        L.call("cg_recombine_set_fft", h, 0 if fft == "auto" else 1)
         sizes = (ctypes.c_int32 * 5)()
         L.call("cg_recombine_sizes", h, sizes)
         (self.xM_yP_size, self.xM_yN_size, self.facet_spacing, self.yP_spacing,

@@ -289,6 +289,11 @@ int cg_fft(void *data, int batch, int H, int W, int is_c64, int inverse,
 /* The same transforms unshifted and unnormalised (cuFFT's own convention):
  * for callers that fold the centring shifts and the 1/(H W) of the inverse
  * into neighbouring passes (the w-towers pipeline). */
+/* batch contiguous complex128 rows of length n (a power of two, 64..2048)
+ * transformed in place, unshifted and unnormalised (inverse: exp(+2 pi i)),
+ * in double-float arithmetic (hi + lo pairs of floats, about 48 significant
+ * bits) on the FP32 units: GB300's FP64 rate bounds an FP64 FFT. */
+int cg_fft_rows_df(void *data_c128, int64_t batch, int n, int inverse, cg_stream_t stream);
 int cg_fft_raw(void *data, int batch, int H, int W, int is_c64, int inverse,
                cg_stream_t stream);
 
@@ -502,6 +507,10 @@ int cg_recombine_create(int image_size, int subgrid_spacing, const double *pswf_
                         int yB_size, int yN_size, int yP_size, int xA_size,
                         int xM_size, int xMxN_yP_size, cg_recombine **out);
 int cg_recombine_destroy(cg_recombine *h);
+/* FFTs of the recombination: mode 0 (default) transforms power-of-two rows
+ * (64..2048) in double-float arithmetic on the FP32 units (cg_fft_rows_df)
+ * and other lengths with cuFFT Z2Z; mode 1 uses cuFFT Z2Z throughout. */
+int cg_recombine_set_fft(cg_recombine *h, int mode);
 /* sizes[0..4] = xM_yP_size, xM_yN_size, facet_spacing, yP_spacing, xM_spacing */
 int cg_recombine_sizes(const cg_recombine *h, int32_t *sizes);
 /* host copies of Fb [yB], Fn [xM_yN], m [xMxN_yP] (raw layout; NULL skips) */
