@@ -118,6 +118,7 @@ SIGNATURES = {
     "cg_fft": (c_int, [P, c_int, c_int, c_int, c_int, c_int, P, P]),
     "cg_fft_raw": (c_int, [P, c_int, c_int, c_int, c_int, c_int, P]),
     "cg_fft_rows_df": (c_int, [P, c_int64, c_int, c_int, P]),
+    "cg_fft2_centred_df": (c_int, [P, c_int64, c_int, c_int, c_int, P]),
     "cg_recombine_set_fft": (c_int, [P, c_int]),
     "cg_image_from_grid": (c_int, [P, c_int, c_int, P, P, P]),
     "cg_scale_image": (c_int, [P, c_int64, P, P]),

@@ -1,19 +1,27 @@
-// Batched complex FFTs of FP64 rows computed in double-float arithmetic.
+// Batched complex FFTs computed in double-float arithmetic.
 //
 // GB300 runs FP64 at a small fraction of its FP32 rate, and a batched FP64
-// FFT is bound by that rate, not by memory.  Here each complex128 element is
+// FFT is bound by that rate, not by memory.  Here each complex value is
 // carried as two unevaluated float sums (hi + lo, about 48 significant bits)
-// and every butterfly uses error-free transformations on the FP32 units:
-//   two_sum (Knuth), two_prod by FMA, the double-float sum with both
-//   components' errors (the accurate pair sum of Joldes, Muller and Popescu,
-//   "Tight and rigorous error bounds for basic building blocks of
-//   double-word arithmetic", 2017) and the double-float product with FMA.
-// Rows are power-of-two lengths 64 .. 2048, contiguous in memory, one or more
-// rows per CTA, transformed in shared memory by the radix-2 Stockham
-// (self-sorting) algorithm: stage s reads x[q + s p], x[q + s (p + m)] and
-// writes y[q + s 2p] = a + b, y[q + s (2p + 1)] = (a - b) w^(p s), m = n/(2s),
-// so the output is in natural order.  Twiddles w^k = exp(-+2 pi i k / n) come
-// from an FP64 host table split into hi + lo.  Unnormalised, as cuFFT.
+// and every butterfly uses error-free transformations on the FP32 units
+// (df.cuh; sloppy pair sums in the butterflies, normwise error about 2u^2
+// per stage, u = 2^-24).  Transforms are power-of-two lengths 64 .. 2048 in
+// shared memory by the Stockham (self-sorting) algorithm in radix 4, with one
+// radix-2 stage first when log2 n is odd: the stage with stride s reads
+// x[q + s (p + k m)] (m = n/(4s), k < 4, t = p s + q) and writes
+// y[q + s (4p + k)] = (the 4-point DFT of those four)_k w^(k p s), so the
+// output is in natural order; half the shared-memory passes and a quarter
+// fewer twiddle products than radix 2.  Twiddles w^k = exp(-+2 pi i k / n),
+// k < 3n/4, come from an FP64 host table split into hi + lo.
+// Unnormalised, as cuFFT.
+//
+// Elements reach the kernels through an I/O policy, so one transform serves
+//   - complex128 rows in place (converted on load and store),
+//   - double-float rows (float4 = re.hi, re.lo, im.hi, im.lo) in place,
+//   - the two passes of a centred 2-D transform of complex128 planes: rows
+//     with the (-1)^(i+j) pre-modulation, complex128 in and double-float out;
+//     then columns, double-float in and complex128 out with the post-
+//     modulation and the 1 / (H W) of an inverse.
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -21,120 +29,212 @@
 #include <vector>
 
 #include "cg_internal.cuh"
+#include "df.cuh"
 
 namespace cg {
 
+bool dfft_supported(int n);
+
 namespace {
 
-struct df {
-  float hi, lo;
+// ---------------------------------------------------------------- I/O policies
+// ld(row, i) / st(row, i, v): element i of transform row `row`
+
+struct IoC128 {
+  double2 *d;
+  int n;
+  __device__ cdf ld(int64_t row, int i) const { return cdf_from(d[row * n + i]); }
+  __device__ void st(int64_t row, int i, const cdf &v) const { d[row * n + i] = cdf_to(v); }
 };
 
-__device__ __forceinline__ df two_sum(float a, float b) {
-  const float s = a + b;
-  const float bb = s - a;
-  const float e = (a - (s - bb)) + (b - bb);
-  return {s, e};
-}
-
-__device__ __forceinline__ df fast_two_sum(float a, float b) {  // |a| >= |b|
-  const float s = a + b;
-  return {s, b - (s - a)};
-}
-
-__device__ __forceinline__ df df_add(df x, df y) {
-  const df s = two_sum(x.hi, y.hi);
-  const df t = two_sum(x.lo, y.lo);
-  df v = fast_two_sum(s.hi, s.lo + t.hi);
-  return fast_two_sum(v.hi, t.lo + v.lo);
-}
-
-__device__ __forceinline__ df df_neg(df x) { return {-x.hi, -x.lo}; }
-
-__device__ __forceinline__ df df_mul(df x, df y) {
-  const float p = x.hi * y.hi;
-  float e = fmaf(x.hi, y.hi, -p);
-  e = fmaf(x.hi, y.lo, e);
-  e = fmaf(x.lo, y.hi, e);
-  return fast_two_sum(p, e);
-}
-
-struct cdf {
-  df re, im;
+struct IoDF {
+  float4 *d;
+  int n;
+  __device__ cdf ld(int64_t row, int i) const { return cdf_load(d[row * n + i]); }
+  __device__ void st(int64_t row, int i, const cdf &v) const { d[row * n + i] = cdf_store(v); }
 };
 
-__device__ __forceinline__ cdf cdf_add(const cdf &a, const cdf &b) {
-  return {df_add(a.re, b.re), df_add(a.im, b.im)};
-}
-__device__ __forceinline__ cdf cdf_sub(const cdf &a, const cdf &b) {
-  return {df_add(a.re, df_neg(b.re)), df_add(a.im, df_neg(b.im))};
-}
-__device__ __forceinline__ cdf cdf_mul(const cdf &a, const cdf &w) {
-  return {df_add(df_mul(a.re, w.re), df_neg(df_mul(a.im, w.im))),
-          df_add(df_mul(a.re, w.im), df_mul(a.im, w.re))};
+__device__ __forceinline__ cdf cdf_neg(const cdf &v) { return {df_neg(v.re), df_neg(v.im)}; }
+
+// centred 2-D, pass over rows: complex128 plane rows in, the sign (-1)^(i+j)
+// of the pre-modulation (i = row within its plane of H rows), double-float out
+// in place (same 16 bytes per element)
+struct IoRowsCentred {
+  double2 *d;
+  int n, H;
+  __device__ cdf ld(int64_t row, int i) const {
+    const cdf v = cdf_from(d[row * n + i]);
+    return (((int)(row % H) + i) & 1) ? cdf_neg(v) : v;
+  }
+  __device__ void st(int64_t row, int i, const cdf &v) const {
+    ((float4 *)d)[row * n + i] = cdf_store(v);
+  }
+};
+
+// ---------------------------------------------------------------- butterflies
+// One radix-2 butterfly of the first stage (stride 1, m = N/2) on element t2
+// and one radix-4 butterfly of the stage with stride s (m = N/(4s)) for
+// t = p s + q: inputs x[t + k N/4], outputs y[q + s (4p + k)], twiddles
+// w^(k p s) from the table (k p s < 3N/4).  x[.] indexes through `at`, so the
+// same code serves rows (at(i) = i) and column tiles (at(i) = i C + c).
+
+__device__ __forceinline__ cdf cdf_mul_j(const cdf &v, bool inverse) {  // times -i (+i)
+  return inverse ? cdf{df_neg(v.im), v.re} : cdf{v.im, df_neg(v.re)};
 }
 
-__device__ __forceinline__ df split(double v) {
-  const float hi = (float)v;
-  return {hi, (float)(v - (double)hi)};
+template <int N, class AT>
+__device__ __forceinline__ void radix2_first(const cdf *x, cdf *y, const cdf *stw, int t2,
+                                             AT at) {
+  const cdf a = x[at(t2)], b = x[at(t2 + N / 2)];
+  y[at(2 * t2)] = cdf_add_f(a, b);
+  const cdf d = cdf_sub_f(a, b);
+  y[at(2 * t2 + 1)] = t2 == 0 ? d : cdf_mul_f(d, stw[t2]);
 }
 
-__device__ __forceinline__ cdf to_cdf(double2 v) { return {split(v.x), split(v.y)}; }
-
-__device__ __forceinline__ double2 from_cdf(const cdf &v) {
-  return make_double2((double)v.re.hi + (double)v.re.lo, (double)v.im.hi + (double)v.im.lo);
+template <int N, class AT>
+__device__ __forceinline__ void radix4(const cdf *x, cdf *y, const cdf *stw, int t, int s,
+                                       bool inverse, AT at) {
+  constexpr int Q = N / 4;
+  const int q = t & (s - 1), ps = t - q;  // p s
+  const cdf x0 = x[at(t)], x1 = x[at(t + Q)], x2 = x[at(t + 2 * Q)], x3 = x[at(t + 3 * Q)];
+  const cdf a0 = cdf_add_f(x0, x2), a1 = cdf_sub_f(x0, x2);
+  const cdf b0 = cdf_add_f(x1, x3), b1 = cdf_mul_j(cdf_sub_f(x1, x3), inverse);
+  const int o = q + 4 * ps;
+  y[at(o)] = cdf_add_f(a0, b0);
+  if (ps == 0) {
+    y[at(o + s)] = cdf_add_f(a1, b1);
+    y[at(o + 2 * s)] = cdf_sub_f(a0, b0);
+    y[at(o + 3 * s)] = cdf_sub_f(a1, b1);
+  } else {
+    y[at(o + s)] = cdf_mul_f(cdf_add_f(a1, b1), stw[ps]);
+    y[at(o + 2 * s)] = cdf_mul_f(cdf_sub_f(a0, b0), stw[2 * ps]);
+    y[at(o + 3 * s)] = cdf_mul_f(cdf_sub_f(a1, b1), stw[3 * ps]);
+  }
 }
 
-// ROWS rows of length N per CTA, N/2 threads per row; two cdf buffers
-template <int LOGN, int ROWS>
-__global__ void __launch_bounds__((1 << LOGN) / 2 * ROWS)
-    k_dfft_rows(double2 *__restrict__ data, int64_t batch, const double2 *__restrict__ tw) {
+struct AtRow {
+  __device__ int operator()(int i) const { return i; }
+};
+template <int C>
+struct AtCol {
+  int c;
+  __device__ int operator()(int i) const { return i * C + c; }
+};
+
+// ---------------------------------------------------------------- row transforms
+// ROWS rows of length N per CTA, N/4 threads per row; two cdf buffers and
+// the 3N/4 twiddles in shared memory.  Odd log2 N: one radix-2 stage first.
+template <int LOGN, int ROWS, class IO>
+__global__ void __launch_bounds__((1 << LOGN) / 4 * ROWS)
+    k_dfft_rows(IO io, int64_t batch, const float4 *__restrict__ tw, int inverse) {
   constexpr int N = 1 << LOGN;
-  constexpr int H = N / 2;
+  constexpr int Q = N / 4;
   extern __shared__ float dsm[];
-  cdf *buf0 = (cdf *)dsm;                 // [ROWS][N]
-  cdf *buf1 = buf0 + ROWS * N;            // [ROWS][N]
-  cdf *stw = buf1 + ROWS * N;             // [N/2] twiddles, as double-float
-  const int r = threadIdx.x / H, t = threadIdx.x - (threadIdx.x / H) * H;
-  for (int k = threadIdx.x; k < H; k += blockDim.x) stw[k] = to_cdf(tw[k]);
+  cdf *buf0 = (cdf *)dsm;       // [ROWS][N]
+  cdf *buf1 = buf0 + ROWS * N;  // [ROWS][N]
+  cdf *stw = buf1 + ROWS * N;   // [3N/4] twiddles
+  const int r = threadIdx.x / Q, t = threadIdx.x - (threadIdx.x / Q) * Q;
+  for (int k = threadIdx.x; k < 3 * Q; k += blockDim.x) stw[k] = cdf_load(tw[k]);
+  const bool inv = inverse != 0;
   for (int64_t row0 = (int64_t)blockIdx.x * ROWS; row0 < batch;
        row0 += (int64_t)gridDim.x * ROWS) {
     const int64_t row = row0 + r;
     const bool live = row < batch;
-    double2 *src = data + row * N;
     cdf *x = buf0 + r * N, *y = buf1 + r * N;
     if (live) {
-      x[t] = to_cdf(src[t]);
-      x[t + H] = to_cdf(src[t + H]);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) x[t + k * Q] = io.ld(row, t + k * Q);
     }
     __syncthreads();
-#pragma unroll
-    for (int ls = 0; ls < LOGN; ++ls) {
-      const int s = 1 << ls;                  // stride
-      const int p = t >> ls, q = t & (s - 1);  // t = p s + q, p < m = N / (2s)
+    if (LOGN & 1) {
       if (live) {
-        const cdf a = x[q + s * p], b = x[q + s * p + H];
-        y[q + s * 2 * p] = cdf_add(a, b);
-        const cdf d = cdf_sub(a, b);
-        y[q + s * (2 * p + 1)] = (p == 0) ? d : cdf_mul(d, stw[p * s]);
+        radix2_first<N>(x, y, stw, t, AtRow());
+        radix2_first<N>(x, y, stw, t + Q, AtRow());
       }
       __syncthreads();
       cdf *tmp = x;
       x = y;
       y = tmp;
     }
+#pragma unroll
+    for (int ls = (LOGN & 1); ls < LOGN; ls += 2) {
+      if (live) radix4<N>(x, y, stw, t, 1 << ls, inv, AtRow());
+      __syncthreads();
+      cdf *tmp = x;
+      x = y;
+      y = tmp;
+    }
     if (live) {
-      src[t] = from_cdf(x[t]);
-      src[t + H] = from_cdf(x[t + H]);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) io.st(row, t + k * Q, x[t + k * Q]);
     }
     __syncthreads();
   }
 }
 
-std::mutex g_tw_mu;
-std::map<std::pair<int, int>, double2 *> g_tw;  // (device, n * sign) -> table
+// ---------------------------------------------------------------- column transforms
+// Planes [nplanes][N][W] of double-float, transformed along N (the columns);
+// each CTA takes C adjacent columns of one plane (C * 16 bytes per row read),
+// T threads; then the centred post-modulation (-1)^(l + k + phase) * scale and
+// complex128 out in place.
+template <int LOGN, int C, int T>
+__global__ void __launch_bounds__(T)
+    k_dfft_cols_centred(double2 *d, int64_t nplanes, int W, int phase, float scale,
+                        const float4 *__restrict__ tw, int inverse) {
+  constexpr int N = 1 << LOGN;
+  constexpr int Q = N / 4;
+  extern __shared__ float dsm[];
+  cdf *buf0 = (cdf *)dsm;    // [N][C]
+  cdf *buf1 = buf0 + N * C;  // [N][C]
+  cdf *stw = buf1 + N * C;   // [3N/4]
+  for (int k = threadIdx.x; k < 3 * Q; k += T) stw[k] = cdf_load(tw[k]);
+  const bool inv = inverse != 0;
+  const int groups = W / C;
+  const int64_t jobs = nplanes * groups;
+  for (int64_t job = blockIdx.x; job < jobs; job += gridDim.x) {
+    const int64_t plane = job / groups;
+    const int c0 = (int)(job - plane * groups) * C;
+    const float4 *src = (const float4 *)(d + plane * N * W) + c0;
+    for (int e = threadIdx.x; e < N * C; e += T) {
+      const int i = e / C, c = e - (e / C) * C;
+      buf0[e] = cdf_load(src[(int64_t)i * W + c]);
+    }
+    __syncthreads();
+    cdf *x = buf0, *y = buf1;
+    if (LOGN & 1) {
+      for (int b = threadIdx.x; b < N / 2 * C; b += T)
+        radix2_first<N>(x, y, stw, b / C, AtCol<C>{b % C});
+      __syncthreads();
+      cdf *tmp = x;
+      x = y;
+      y = tmp;
+    }
+#pragma unroll
+    for (int ls = (LOGN & 1); ls < LOGN; ls += 2) {
+      for (int b = threadIdx.x; b < Q * C; b += T)
+        radix4<N>(x, y, stw, b / C, 1 << ls, inv, AtCol<C>{b % C});
+      __syncthreads();
+      cdf *tmp = x;
+      x = y;
+      y = tmp;
+    }
+    double2 *dst = d + plane * N * W + c0;
+    for (int e = threadIdx.x; e < N * C; e += T) {
+      const int l = e / C, c = e - (e / C) * C;
+      const float sg = ((l + c0 + c + phase) & 1) ? -scale : scale;  // a power of two
+      const cdf v = x[e];
+      const cdf w = {{v.re.hi * sg, v.re.lo * sg}, {v.im.hi * sg, v.im.lo * sg}};
+      dst[(int64_t)l * W + c] = cdf_to(w);
+    }
+    __syncthreads();
+  }
+}
 
-int twiddles(int n, int sign, const double2 **out) {
+// ---------------------------------------------------------------- twiddles
+std::mutex g_tw_mu;
+std::map<std::pair<int, int>, float4 *> g_tw;  // (device, n * sign) -> table
+
+int twiddles(int n, int sign, const float4 **out) {
   int dev = 0;
   cudaGetDevice(&dev);
   std::lock_guard<std::mutex> lock(g_tw_mu);
@@ -144,30 +244,67 @@ int twiddles(int n, int sign, const double2 **out) {
     *out = it->second;
     return CG_OK;
   }
-  std::vector<double2> h(n / 2);
-  for (int k = 0; k < n / 2; ++k) {
+  std::vector<float4> h(3 * n / 4);
+  for (int k = 0; k < 3 * n / 4; ++k) {
     const double a = 2.0 * M_PI * (double)k / (double)n;
-    h[k] = make_double2(std::cos(a), sign * std::sin(a));
+    const double c = std::cos(a), s = sign * std::sin(a);
+    const float ch = (float)c, sh = (float)s;
+    h[k] = make_float4(ch, (float)(c - (double)ch), sh, (float)(s - (double)sh));
   }
-  double2 *d = nullptr;
-  CG_CUDA(cudaMalloc(&d, h.size() * sizeof(double2)));
-  CG_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  float4 *d = nullptr;
+  CG_CUDA(cudaMalloc(&d, h.size() * sizeof(float4)));
+  CG_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice));
   g_tw[key] = d;
   *out = d;
   return CG_OK;
 }
 
-template <int LOGN, int ROWS>
-int launch(double2 *data, int64_t batch, const double2 *tw, cudaStream_t st) {
+template <int LOGN, int ROWS, class IO>
+int launch_rows(IO io, int64_t batch, const float4 *tw, int inverse, cudaStream_t st) {
   constexpr int N = 1 << LOGN;
-  const size_t smem = (size_t)(2 * ROWS * N + N / 2) * sizeof(cdf);
+  const size_t smem = (size_t)(2 * ROWS * N + 3 * N / 4) * sizeof(cdf);
   if (smem > 48 * 1024)  // set on every launch: the attribute is per device
-    CG_CUDA(cudaFuncSetAttribute(k_dfft_rows<LOGN, ROWS>,
+    CG_CUDA(cudaFuncSetAttribute(k_dfft_rows<LOGN, ROWS, IO>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t ctas = (batch + ROWS - 1) / ROWS;
   const unsigned grid = (unsigned)std::min<int64_t>(ctas, (int64_t)num_sms() * 8);
-  k_dfft_rows<LOGN, ROWS><<<grid, N / 2 * ROWS, smem, st>>>(data, batch, tw);
+  k_dfft_rows<LOGN, ROWS, IO><<<grid, N / 4 * ROWS, smem, st>>>(io, batch, tw, inverse);
   CG_LAUNCH("double-float FFT");
+  return CG_OK;
+}
+
+template <class IO>
+int rows_any(IO io, int64_t batch, int n, int inverse, cudaStream_t st) {
+  CG_REQUIRE(dfft_supported(n), "double-float FFT lengths are powers of two 64..2048");
+  if (batch <= 0) return CG_OK;
+  const float4 *tw;
+  int rc = twiddles(n, inverse ? 1 : -1, &tw);
+  if (rc) return rc;
+  switch (n) {  // N/4 threads per row, 256 threads per CTA up to 1024
+    case 64: return launch_rows<6, 16>(io, batch, tw, inverse, st);
+    case 128: return launch_rows<7, 8>(io, batch, tw, inverse, st);
+    case 256: return launch_rows<8, 4>(io, batch, tw, inverse, st);
+    case 512: return launch_rows<9, 2>(io, batch, tw, inverse, st);
+    case 1024: return launch_rows<10, 1>(io, batch, tw, inverse, st);
+    case 2048: return launch_rows<11, 1>(io, batch, tw, inverse, st);
+  }
+  return set_error(CG_ERR_ARG, "unsupported double-float FFT length %d", n);
+}
+
+template <int LOGN, int C>
+int launch_cols(double2 *d, int64_t nplanes, int W, int phase, float scale, const float4 *tw,
+                int inverse, cudaStream_t st) {
+  constexpr int N = 1 << LOGN;
+  constexpr int T = 256;
+  const size_t smem = (size_t)(2 * N * C + 3 * N / 4) * sizeof(cdf);
+  if (smem > 48 * 1024)
+    CG_CUDA(cudaFuncSetAttribute(k_dfft_cols_centred<LOGN, C, T>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t jobs = nplanes * (W / C);
+  const unsigned grid = (unsigned)std::min<int64_t>(jobs, (int64_t)num_sms() * 8);
+  k_dfft_cols_centred<LOGN, C, T><<<grid, T, smem, st>>>(d, nplanes, W, phase, scale, tw,
+                                                         inverse);
+  CG_LAUNCH("double-float column FFT");
   return CG_OK;
 }
 
@@ -178,20 +315,37 @@ bool dfft_supported(int n) { return n >= 64 && n <= 2048 && (n & (n - 1)) == 0; 
 // In-place batched FFT of `batch` contiguous complex128 rows of length n
 // (a power of two, 64..2048); inverse: exp(+2 pi i), unnormalised.
 int dfft_rows(double2 *data, int64_t batch, int n, int inverse, cudaStream_t st) {
-  CG_REQUIRE(dfft_supported(n), "double-float FFT lengths are powers of two 64..2048");
+  return rows_any(IoC128{data, n}, batch, n, inverse, st);
+}
+
+// The same on rows stored as double-float (float4 per element).
+int dfft_rows_df(float4 *data, int64_t batch, int n, int inverse, cudaStream_t st) {
+  return rows_any(IoDF{data, n}, batch, n, inverse, st);
+}
+
+// In-place centred 2-D FFT of `batch` complex128 planes [H][W] (numpy's
+// fftshift(fft2(ifftshift(x))), or the normalised ifft2 for inverse), H and W
+// powers of two 64..2048.  The fftshifts are the checkerboard modulations
+// (-1)^(i+j) before and (-1)^(k+l+H/2+W/2) after the transform.
+int dfft2_centred(double2 *data, int64_t batch, int H, int W, int inverse, cudaStream_t st) {
+  CG_REQUIRE(dfft_supported(H) && dfft_supported(W),
+             "double-float 2-D FFT sides are powers of two 64..2048");
   if (batch <= 0) return CG_OK;
-  const double2 *tw;
-  int rc = twiddles(n, inverse ? 1 : -1, &tw);
+  int rc = rows_any(IoRowsCentred{data, W, H}, batch * H, W, inverse, st);
   if (rc) return rc;
-  switch (n) {
-    case 64: return launch<6, 8>(data, batch, tw, st);
-    case 128: return launch<7, 4>(data, batch, tw, st);
-    case 256: return launch<8, 2>(data, batch, tw, st);
-    case 512: return launch<9, 1>(data, batch, tw, st);
-    case 1024: return launch<10, 1>(data, batch, tw, st);
-    case 2048: return launch<11, 1>(data, batch, tw, st);
+  const float4 *tw;
+  if ((rc = twiddles(H, inverse ? 1 : -1, &tw))) return rc;
+  const int phase = (H / 2 + W / 2) & 1;
+  const float scale = inverse ? 1.0f / ((float)H * (float)W) : 1.0f;  // a power of two
+  switch (H) {  // columns per CTA: 64 KB of buffers (3 CTAs per SM) up to 512; C >= 2
+    case 64: return launch_cols<6, 16>(data, batch, W, phase, scale, tw, inverse, st);
+    case 128: return launch_cols<7, 16>(data, batch, W, phase, scale, tw, inverse, st);
+    case 256: return launch_cols<8, 8>(data, batch, W, phase, scale, tw, inverse, st);
+    case 512: return launch_cols<9, 4>(data, batch, W, phase, scale, tw, inverse, st);
+    case 1024: return launch_cols<10, 4>(data, batch, W, phase, scale, tw, inverse, st);
+    case 2048: return launch_cols<11, 2>(data, batch, W, phase, scale, tw, inverse, st);
   }
-  return set_error(CG_ERR_ARG, "unsupported double-float FFT length %d", n);
+  return set_error(CG_ERR_ARG, "unsupported double-float FFT length %d", H);
 }
 
 }  // namespace cg
@@ -200,4 +354,10 @@ extern "C" int cg_fft_rows_df(void *data_c128, int64_t batch, int n, int inverse
                               cg_stream_t stream) {
   CG_REQUIRE(data_c128 && batch >= 0, "bad double-float FFT arguments");
   return cg::dfft_rows((double2 *)data_c128, batch, n, inverse, (cudaStream_t)stream);
+}
+
+extern "C" int cg_fft2_centred_df(void *data_c128, int64_t batch, int H, int W, int inverse,
+                                  cg_stream_t stream) {
+  CG_REQUIRE(data_c128 && batch >= 0, "bad double-float 2-D FFT arguments");
+  return cg::dfft2_centred((double2 *)data_c128, batch, H, W, inverse, (cudaStream_t)stream);
 }

@@ -15,7 +15,11 @@
 //   4. k_rc_window      : per subgrid row offset, as 2.
 //      forward FFT of n0 * n1 * xM_yN rows of length xM_yP
 //   5. k_rc_crop_T      : crop times Fn, transpose to [i0][i1][axis 0][axis 1]
-// Every FFT runs over contiguous rows, complex128 as the reference.  Arrays
+// Every FFT runs over contiguous rows.  The caller's arrays are complex128 as
+// the reference; when both transform lengths are powers of two 64..2048 the
+// stage arrays between the kernels hold double-float pairs (about 48
+// significant bits, arithmetic on the FP32 units, df.cuh) and the transforms
+// are the double-float FFTs, else complex128 with FP64 cuFFT.  Arrays
 // are in the C prototype's raw
 // layout (centre at index 0, FFTW sign conventions: backward = e^{+2 pi i},
 // unnormalised) except where a `centred` flag maps the facet in or the
@@ -34,11 +38,13 @@
 #include <vector>
 
 #include "cg_internal.cuh"
+#include "df.cuh"
 
 namespace cg {
 int fft_plan(int batch, int H, int W, cufftType type, cufftHandle *out);
 bool dfft_supported(int n);
 int dfft_rows(double2 *data, int64_t batch, int n, int inverse, cudaStream_t st);
+int dfft_rows_df(float4 *data, int64_t batch, int n, int inverse, cudaStream_t st);
 }
 
 struct cg_recombine {
@@ -47,6 +53,7 @@ struct cg_recombine {
   int xM_yP, xM_yN, yP_spacing, xM_spacing;
   int fft_mode;  // 0: double-float FFTs for power-of-two rows, cuFFT Z2Z otherwise; 1: cuFFT Z2Z
   double *d_Fb, *d_Fn, *d_m;
+  float2 *d_Fb2, *d_Fn2, *d_m2;  // the same split into double-float (hi, lo)
 };
 
 namespace {
@@ -61,35 +68,68 @@ __host__ __device__ inline int pmod(long long a, int n) {
 // a mod n for a in [-n, 2n) (one conditional add or subtract, 32-bit)
 __device__ __forceinline__ int wrap1(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
-template <typename C>
-struct RT;
-template <>
-struct RT<double2> {
-  typedef double R;
+// Element policies of the stage arrays.  P64: complex128 with FP64
+// arithmetic.  PDF: double-float pairs (float4 = re.hi, re.lo, im.hi, im.lo,
+// the same 16 bytes) with arithmetic on the FP32 units, window weights as
+// float2 (hi, lo); conversions from and to complex128 only where the
+// pipeline reads the caller's arrays or writes its results.  The divisors
+// passed to wdiv are transform lengths, powers of two in the PDF pipeline.
+struct P64 {
+  typedef double2 S;  // stored element
+  typedef double2 V;  // element in registers
+  typedef double W;   // weight in registers
+  typedef double WS;  // weight as stored
+  __device__ static V in(double2 a) { return a; }
+  __device__ static double2 out(V a) { return a; }
+  __device__ static V ld(const S &s) { return s; }
+  __device__ static S st(const V &v) { return v; }
+  __device__ static V zero() { return make_double2(0.0, 0.0); }
+  __device__ static W w(const WS *a, int i) { return a[i]; }
+  __device__ static W one() { return 1.0; }
+  __device__ static W wmul(W a, W b) { return a * b; }
+  __device__ static W wdiv(W a, int n) { return a / (double)n; }
+  __device__ static V scale(V a, W s) {
+    a.x *= s;
+    a.y *= s;
+    return a;
+  }
+  __device__ static V madd(V acc, W w, const V &b) {  // acc + w b
+    acc.x += w * b.x;
+    acc.y += w * b.y;
+    return acc;
+  }
 };
 
-template <typename C>
-__device__ __forceinline__ C cscale(C a, typename RT<C>::R s) {
-  a.x *= s;
-  a.y *= s;
-  return a;
-}
-
-template <typename C>
-__device__ __forceinline__ C czero() {
-  C z;
-  z.x = 0;
-  z.y = 0;
-  return z;
-}
+struct PDF {
+  typedef float4 S;
+  typedef cdf V;
+  typedef df W;
+  typedef float2 WS;
+  __device__ static V in(double2 a) { return cdf_from(a); }
+  __device__ static double2 out(const V &a) { return cdf_to(a); }
+  __device__ static V ld(const S &s) { return cdf_load(s); }
+  __device__ static S st(const V &v) { return cdf_store(v); }
+  __device__ static V zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
+  __device__ static W w(const WS *a, int i) {
+    const float2 t = a[i];
+    return {t.x, t.y};
+  }
+  __device__ static W one() { return {1.f, 0.f}; }
+  __device__ static W wmul(W a, W b) { return df_mul(a, b); }
+  __device__ static W wdiv(W a, int n) {  // n a power of two: exact
+    const float r = 1.0f / (float)n;
+    return {a.hi * r, a.lo * r};
+  }
+  __device__ static V scale(const V &a, W s) { return cdf_scale(a, s); }
+  __device__ static V madd(const V &acc, W w, const V &b) { return cdf_add(acc, cdf_scale(b, w)); }
+};
 
 // prepare_facet along the rows: out[r][k], k < yP.  With `centred`, the input
 // facet is in fftshift layout on both axes and row r of the output is raw row r.
-template <typename C>
-__global__ void k_rc_prep_rows(const C *__restrict__ in, int rows, int yB, int yP,
-                               const typename RT<C>::R *__restrict__ Fb, int centred,
-                               C *__restrict__ out) {
-  typedef typename RT<C>::R R;
+template <class P>
+__global__ void k_rc_prep_rows(const double2 *__restrict__ in, int rows, int yB, int yP,
+                               const typename P::WS *__restrict__ Fb, int centred,
+                               typename P::S *__restrict__ out) {
   const int h = yB / 2;
   const size_t total = (size_t)rows * yP;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
@@ -100,13 +140,13 @@ __global__ void k_rc_prep_rows(const C *__restrict__ in, int rows, int yB, int y
       t = k;
     else if (k >= yP - h)
       t = k - yP + yB;
-    C v = czero<C>();
+    typename P::V v = P::zero();
     if (t >= 0) {
       const int rs = centred ? (r + h) % yB : r;
       const int ts = centred ? (t + h) % yB : t;
-      v = cscale(in[(size_t)rs * yB + ts], Fb[t] / (R)yP);
+      v = P::scale(P::in(in[(size_t)rs * yB + ts]), P::wdiv(P::w(Fb, t), yP));
     }
-    out[e] = v;
+    out[e] = P::st(v);
   }
 }
 
@@ -129,10 +169,11 @@ __global__ void k_rc_offsets(const int32_t *__restrict__ off0, int n0,
 
 // extract_subgrid's window: out[o][r][i] from row r of bf at offset offs[o]
 // (in yP samples).
-template <typename C>
-__global__ void k_rc_window(const C *__restrict__ bf, int rows, int yP,
+template <class P>
+__global__ void k_rc_window(const typename P::S *__restrict__ bf, int rows, int yP,
                             const int32_t *__restrict__ offs, int noff, int xM_yP, int xMxN_yP,
-                            const typename RT<C>::R *__restrict__ m, C *__restrict__ out) {
+                            const typename P::WS *__restrict__ m,
+                            typename P::S *__restrict__ out) {
   const int xN_yP = xMxN_yP - xM_yP;
   const size_t total = (size_t)noff * rows * xM_yP;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
@@ -141,22 +182,13 @@ __global__ void k_rc_window(const C *__restrict__ bf, int rows, int yP,
     const size_t orow = e / xM_yP;
     const int r = (int)(orow % rows);
     const int off = offs[orow / rows];
-    const C *row = bf + (size_t)r * yP;
-    C v = czero<C>();
+    const typename P::S *row = bf + (size_t)r * yP;
+    typename P::V v = P::zero();
     // off < yP and i < xM_yP <= yP, so both sums lie within one period
-    if (i < (xMxN_yP + 1) / 2) {
-      const C b = row[wrap1(i + off, yP)];
-      const typename RT<C>::R w = m[i];
-      v.x += w * b.x;
-      v.y += w * b.y;
-    }
-    if (i >= xM_yP - xMxN_yP / 2) {
-      const C b = row[wrap1(i + off - xM_yP, yP)];
-      const typename RT<C>::R w = m[xN_yP + i];
-      v.x += w * b.x;
-      v.y += w * b.y;
-    }
-    out[e] = v;
+    if (i < (xMxN_yP + 1) / 2) v = P::madd(v, P::w(m, i), P::ld(row[wrap1(i + off, yP)]));
+    if (i >= xM_yP - xMxN_yP / 2)
+      v = P::madd(v, P::w(m, xN_yP + i), P::ld(row[wrap1(i + off - xM_yP, yP)]));
+    out[e] = P::st(v);
   }
 }
 
@@ -167,18 +199,17 @@ __device__ __forceinline__ int crop_src(int c, int xM_yN, int xM_yP) {
 // Crop (times Fn) along the rows of mbf [n1][yB][xM_yP], transpose and
 // prepare along the former row axis: out[i1][c][k], k < yP.
 // Block: 32 x 8 threads; tile of 32 columns c by 32 output positions k.
-template <typename C>
-__global__ void k_rc_crop_prep_T(const C *__restrict__ mbf, int yB, int xM_yP, int xM_yN,
-                                 const typename RT<C>::R *__restrict__ Fn,
-                                 const typename RT<C>::R *__restrict__ Fb, int yP,
-                                 C *__restrict__ out) {
-  typedef typename RT<C>::R R;
-  __shared__ C tile[32][33];
+template <class P>
+__global__ void k_rc_crop_prep_T(const typename P::S *__restrict__ mbf, int yB, int xM_yP,
+                                 int xM_yN, const typename P::WS *__restrict__ Fn,
+                                 const typename P::WS *__restrict__ Fb, int yP,
+                                 typename P::S *__restrict__ out) {
+  __shared__ typename P::S tile[32][33];
   const int i1 = blockIdx.z;
   const int c0 = blockIdx.y * 32;
   const int k0 = blockIdx.x * 32;
   const int h = yB / 2;
-  const C *src = mbf + (size_t)i1 * yB * xM_yP;
+  const typename P::S *src = mbf + (size_t)i1 * yB * xM_yP;
   // load: tile[kk][cc] = Fb[t] Fn[c] mbf[t][crop(c)] / yP for k = k0 + kk
   for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
     const int k = k0 + kk;
@@ -190,10 +221,11 @@ __global__ void k_rc_crop_prep_T(const C *__restrict__ mbf, int yB, int xM_yP, i
       else if (k >= yP - h)
         t = k - yP + yB;
     }
-    C v = czero<C>();
+    typename P::V v = P::zero();
     if (t >= 0 && c < xM_yN)
-      v = cscale(src[(size_t)t * xM_yP + crop_src(c, xM_yN, xM_yP)], Fn[c] * Fb[t] / (R)yP);
-    tile[kk][threadIdx.x] = v;
+      v = P::scale(P::ld(src[(size_t)t * xM_yP + crop_src(c, xM_yN, xM_yP)]),
+                   P::wdiv(P::wmul(P::w(Fn, c), P::w(Fb, t)), yP));
+    tile[kk][threadIdx.x] = P::st(v);
   }
   __syncthreads();
   for (int cc = threadIdx.y; cc < 32; cc += blockDim.y) {
@@ -206,43 +238,41 @@ __global__ void k_rc_crop_prep_T(const C *__restrict__ mbf, int yB, int xM_yP, i
 // Final crop (times Fn) along the rows of mbf2 [n0][n1][xM_yN (axis 1)][xM_yP]
 // and transpose: out[i0][i1][a0][a1].  With `centred`, both output axes in
 // fftshift layout.
-template <typename C>
-__global__ void k_rc_crop_T(const C *__restrict__ mbf2, int n1, int xM_yP, int xM_yN,
-                            const typename RT<C>::R *__restrict__ Fn, int centred,
-                            C *__restrict__ out) {
-  __shared__ C tile[32][33];
+template <class P>
+__global__ void k_rc_crop_T(const typename P::S *__restrict__ mbf2, int n1, int xM_yP, int xM_yN,
+                            const typename P::WS *__restrict__ Fn, int centred,
+                            double2 *__restrict__ out) {
+  __shared__ typename P::S tile[32][33];
   const int pair = blockIdx.z;  // i0 * n1 + i1
   const int a10 = blockIdx.y * 32;
   const int a00 = blockIdx.x * 32;
-  const C *src = mbf2 + (size_t)pair * xM_yN * xM_yP;
+  const typename P::S *src = mbf2 + (size_t)pair * xM_yN * xM_yP;
   for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
     const int a1 = a10 + yy;
     const int a0 = a00 + threadIdx.x;
-    C v = czero<C>();
+    typename P::V v = P::zero();
     if (a1 < xM_yN && a0 < xM_yN)
-      v = cscale(src[(size_t)a1 * xM_yP + crop_src(a0, xM_yN, xM_yP)], Fn[a0]);
-    tile[yy][threadIdx.x] = v;
+      v = P::scale(P::ld(src[(size_t)a1 * xM_yP + crop_src(a0, xM_yN, xM_yP)]), P::w(Fn, a0));
+    tile[yy][threadIdx.x] = P::st(v);
   }
   __syncthreads();
   const int h = xM_yN / 2;
-  C *dst = out + (size_t)pair * xM_yN * xM_yN;
+  double2 *dst = out + (size_t)pair * xM_yN * xM_yN;
   for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
     const int a0 = a00 + yy;
     const int a1 = a10 + threadIdx.x;
     if (a0 < xM_yN && a1 < xM_yN) {
       const int d0 = centred ? (a0 + h) % xM_yN : a0;
       const int d1 = centred ? (a1 + h) % xM_yN : a1;
-      dst[(size_t)d0 * xM_yN + d1] = tile[threadIdx.x][yy];
+      dst[(size_t)d0 * xM_yN + d1] = P::out(P::ld(tile[threadIdx.x][yy]));
     }
   }
 }
 
 // subgrids[s] += nmbf[s] rolled to (fo0, fo1) (in xM samples).  Raw: both in
 // raw layout, divided by xM^2; centred: both in fftshift layout, unscaled.
-template <typename C>
-__global__ void k_rc_add_facet(const C *__restrict__ nmbf, int xM_yN, int xM, int fo0, int fo1,
-                               int centred, C *__restrict__ sub) {
-  typedef typename RT<C>::R R;
+__global__ void k_rc_add_facet(const double2 *__restrict__ nmbf, int xM_yN, int xM, int fo0,
+                               int fo1, int centred, double2 *__restrict__ sub) {
   const int j1 = blockIdx.x * blockDim.x + threadIdx.x;
   const int j0 = blockIdx.y;
   const int s = blockIdx.z;
@@ -262,10 +292,14 @@ __global__ void k_rc_add_facet(const C *__restrict__ nmbf, int xM_yN, int xM, in
     dst0 = wrap1(j0 - h + fo0, xM);
     dst1 = wrap1(j1 - h + fo1, xM);
   }
-  C v = nmbf[((size_t)s * xM_yN + src0) * xM_yN + src1];
-  if (!centred) v = cscale(v, (R)1 / ((R)xM * (R)xM));
-  C *d = sub + ((size_t)s * xM + dst0) * xM + dst1;
-  C a = *d;
+  double2 v = nmbf[((size_t)s * xM_yN + src0) * xM_yN + src1];
+  if (!centred) {
+    const double sc = 1.0 / ((double)xM * (double)xM);
+    v.x *= sc;
+    v.y *= sc;
+  }
+  double2 *d = sub + ((size_t)s * xM + dst0) * xM + dst1;
+  double2 a = *d;
   a.x += v.x;
   a.y += v.y;
   *d = a;
@@ -288,11 +322,10 @@ __device__ __forceinline__ int uncrop(int k, int n, int np) {
 // spectrum (rolled by the facet offset), times Fn on both axes, padded to
 // xM_yP along axis 1 and divided by xM_yP (the inverse FFT that follows is
 // unnormalised).  `centred`: FS in fftshift layout.
-template <typename C>
-__global__ void k_rcT_split(const C *__restrict__ fs, int npair, int xM, int xM_yN, int xM_yP,
-                            int fo0, int fo1, const typename RT<C>::R *__restrict__ Fn,
-                            int centred, C *__restrict__ out) {
-  typedef typename RT<C>::R R;
+template <class P>
+__global__ void k_rcT_split(const double2 *__restrict__ fs, int npair, int xM, int xM_yN,
+                            int xM_yP, int fo0, int fo1, const typename P::WS *__restrict__ Fn,
+                            int centred, typename P::S *__restrict__ out) {
   const size_t total = (size_t)npair * xM_yN * xM_yP;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (size_t)gridDim.x * blockDim.x) {
@@ -301,7 +334,7 @@ __global__ void k_rcT_split(const C *__restrict__ fs, int npair, int xM, int xM_
     const int a0 = (int)(row % xM_yN);
     const size_t pair = row / xM_yN;
     const int c1 = uncrop(k, xM_yN, xM_yP);
-    C v = czero<C>();
+    typename P::V v = P::zero();
     if (c1 >= 0) {
       // |signed frequency| <= xM_yN / 2 <= xM and 0 <= fo < xM
       int s0 = wrap1(signed_freq(a0, xM_yN) + fo0, xM);
@@ -310,19 +343,22 @@ __global__ void k_rcT_split(const C *__restrict__ fs, int npair, int xM, int xM_
         s0 = (s0 + xM / 2) % xM;
         s1 = (s1 + xM / 2) % xM;
       }
-      v = cscale(fs[(pair * xM + s0) * xM + s1], Fn[a0] * Fn[c1] / (R)xM_yP);
+      v = P::scale(P::in(fs[(pair * xM + s0) * xM + s1]),
+                   P::wdiv(P::wmul(P::w(Fn, a0), P::w(Fn, c1)), xM_yP));
     }
-    out[e] = v;
+    out[e] = P::st(v);
   }
 }
 
 // out[o][r][k] (k < yP) = sum over j < noff of the window of in[o][j][r][.]
 // placed at offset offs[j]: position p (|p| within xMxN_yP / 2) of the
 // periodic extension of the xM_yP samples, times m, lands at (p + off) mod yP.
-template <typename C>
-__global__ void k_rcT_scatter(const C *__restrict__ in, int outer, int noff, int inner,
-                              int xM_yP, int xMxN_yP, int yP, const int32_t *__restrict__ offs,
-                              const typename RT<C>::R *__restrict__ m, C *__restrict__ out) {
+template <class P>
+__global__ void k_rcT_scatter(const typename P::S *__restrict__ in, int outer, int noff,
+                              int inner, int xM_yP, int xMxN_yP, int yP,
+                              const int32_t *__restrict__ offs,
+                              const typename P::WS *__restrict__ m,
+                              typename P::S *__restrict__ out) {
   const size_t total = (size_t)outer * inner * yP;
   const int half = xMxN_yP / 2;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
@@ -331,7 +367,7 @@ __global__ void k_rcT_scatter(const C *__restrict__ in, int outer, int noff, int
     const size_t orow = e / yP;
     const int r = (int)(orow % inner);
     const size_t o = orow / inner;
-    C v = czero<C>();
+    typename P::V v = P::zero();
     for (int j = 0; j < noff; ++j) {
       // k, offs[j] in [0, yP): the signed distance in [-yP/2, yP/2)
       int p = k - offs[j];
@@ -339,23 +375,20 @@ __global__ void k_rcT_scatter(const C *__restrict__ in, int outer, int noff, int
       if (p < -(yP / 2)) p += yP;
       if (p < -half || p >= xMxN_yP - half) continue;
       // |p| <= xMxN_yP / 2 <= xM_yP: one wrap each
-      const typename RT<C>::R w = m[p < 0 ? p + xMxN_yP : p];
-      const C b = in[((o * noff + j) * inner + r) * xM_yP + (p < 0 ? p + xM_yP : p)];
-      v.x += w * b.x;
-      v.y += w * b.y;
+      v = P::madd(v, P::w(m, p < 0 ? p + xMxN_yP : p),
+                  P::ld(in[((o * noff + j) * inner + r) * xM_yP + (p < 0 ? p + xM_yP : p)]));
     }
-    out[e] = v;
+    out[e] = P::st(v);
   }
 }
 
 // B[t][i0][k0]: rows (i0, a0) of acc [n0][xM_yN][yP] cropped to the yB facet
 // positions t, transposed so that a0 runs along the rows, padded to xM_yP
 // and divided by xM_yP.  Block 32 x 8: a tile of 32 positions t by 32 k0.
-template <typename C>
-__global__ void k_rcT_crop_T_pad(const C *__restrict__ acc, int n0, int xM_yN, int yP, int yB,
-                                 int xM_yP, C *__restrict__ out) {
-  typedef typename RT<C>::R R;
-  __shared__ C tile[32][33];
+template <class P>
+__global__ void k_rcT_crop_T_pad(const typename P::S *__restrict__ acc, int n0, int xM_yN,
+                                 int yP, int yB, int xM_yP, typename P::S *__restrict__ out) {
+  __shared__ typename P::S tile[32][33];
   const int i0 = blockIdx.z;
   const int t0 = blockIdx.y * 32;
   const int k00 = blockIdx.x * 32;
@@ -363,13 +396,13 @@ __global__ void k_rcT_crop_T_pad(const C *__restrict__ acc, int n0, int xM_yN, i
   for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
     const int k0 = k00 + kk;
     const int t = t0 + threadIdx.x;
-    C v = czero<C>();
+    typename P::V v = P::zero();
     const int a0 = k0 < xM_yP ? uncrop(k0, xM_yN, xM_yP) : -1;
     if (a0 >= 0 && t < yB) {
       const int kt = t < yB / 2 ? t : yP - yB + t;
-      v = cscale(acc[((size_t)i0 * xM_yN + a0) * yP + kt], (R)1 / (R)xM_yP);
+      v = P::scale(P::ld(acc[((size_t)i0 * xM_yN + a0) * yP + kt]), P::wdiv(P::one(), xM_yP));
     }
-    tile[kk][threadIdx.x] = v;
+    tile[kk][threadIdx.x] = P::st(v);
   }
   __syncthreads();
   for (int tt = threadIdx.y; tt < 32; tt += blockDim.y) {
@@ -382,22 +415,22 @@ __global__ void k_rcT_crop_T_pad(const C *__restrict__ acc, int n0, int xM_yN, i
 
 // facet[s][t] (+)= acc2[t][crop(s)] Fb[s] Fb[t], transposed; `centred`:
 // facet in fftshift layout.  Block 32 x 8: a tile of 32 t by 32 s.
-template <typename C>
-__global__ void k_rcT_final(const C *__restrict__ acc2, int yP, int yB,
-                            const typename RT<C>::R *__restrict__ Fb, int centred, int accumulate,
-                            C *__restrict__ facet) {
-  __shared__ C tile[32][33];
+template <class P>
+__global__ void k_rcT_final(const typename P::S *__restrict__ acc2, int yP, int yB,
+                            const typename P::WS *__restrict__ Fb, int centred, int accumulate,
+                            double2 *__restrict__ facet) {
+  __shared__ typename P::S tile[32][33];
   const int t0 = blockIdx.y * 32;
   const int s0 = blockIdx.x * 32;
   for (int tt = threadIdx.y; tt < 32; tt += blockDim.y) {
     const int t = t0 + tt;
     const int s = s0 + threadIdx.x;
-    C v = czero<C>();
+    typename P::V v = P::zero();
     if (t < yB && s < yB) {
       const int ks = s < yB / 2 ? s : yP - yB + s;
-      v = cscale(acc2[(size_t)t * yP + ks], Fb[s] * Fb[t]);
+      v = P::scale(P::ld(acc2[(size_t)t * yP + ks]), P::wmul(P::w(Fb, s), P::w(Fb, t)));
     }
-    tile[tt][threadIdx.x] = v;
+    tile[tt][threadIdx.x] = P::st(v);
   }
   __syncthreads();
   const int h = yB / 2;
@@ -407,10 +440,10 @@ __global__ void k_rcT_final(const C *__restrict__ acc2, int yP, int yB,
     if (s < yB && t < yB) {
       const int d0 = centred ? (s + h) % yB : s;
       const int d1 = centred ? (t + h) % yB : t;
-      C *d = facet + (size_t)d0 * yB + d1;
-      const C v = tile[threadIdx.x][ss];
+      double2 *d = facet + (size_t)d0 * yB + d1;
+      const double2 v = P::out(P::ld(tile[threadIdx.x][ss]));
       if (accumulate) {
-        C a = *d;
+        double2 a = *d;
         a.x += v.x;
         a.y += v.y;
         *d = a;
@@ -423,36 +456,49 @@ __global__ void k_rcT_final(const C *__restrict__ acc2, int yP, int yB,
 
 // ------------------------------------------------------------------ host side
 
-template <typename C>
-struct Prec;
+// the window tables of a policy
+template <class P>
+struct Tab;
 template <>
-struct Prec<double2> {
-  static constexpr cufftType type = CUFFT_Z2Z;
-  static cufftResult exec(cufftHandle p, double2 *d, int dir) {
-    return cufftExecZ2Z(p, (cufftDoubleComplex *)d, (cufftDoubleComplex *)d, dir);
-  }
+struct Tab<P64> {
   static const double *Fb(const cg_recombine *h) { return h->d_Fb; }
   static const double *Fn(const cg_recombine *h) { return h->d_Fn; }
   static const double *m(const cg_recombine *h) { return h->d_m; }
-  // complex128 only: Fb = 1 / PSWF spans many decades at the facet edge
-  // (6.4e6 for the 512 / 128 / 140 test set), and the contributions come out
-  // of intermediates 1e3 times larger than their peak, so single-precision
-  // FFTs lose 1e-3 of the result (measured) where the method delivers 1e-7.
+};
+template <>
+struct Tab<PDF> {
+  static const float2 *Fb(const cg_recombine *h) { return h->d_Fb2; }
+  static const float2 *Fn(const cg_recombine *h) { return h->d_Fn2; }
+  static const float2 *m(const cg_recombine *h) { return h->d_m2; }
 };
 
-template <typename C>
-int rows_fft(const cg_recombine *h, C *data, int batch, int len, int dir, cudaStream_t st) {
+// complex128 only: Fb = 1 / PSWF spans many decades at the facet edge (6.4e6
+// for the 512 / 128 / 140 test set), and the contributions come out of
+// intermediates 1e3 times larger than their peak, so single-precision FFTs
+// lose 1e-3 of the result (measured) where the method delivers 1e-7.
+int rows_fft(const cg_recombine *h, double2 *data, int batch, int len, int dir, cudaStream_t st) {
   // power-of-two rows in double-float arithmetic on the FP32 units: the FP64
   // transforms are bound by GB300's FP64 rate
   if (h->fft_mode == 0 && dfft_supported(len))
-    return dfft_rows((double2 *)data, batch, len, dir == CUFFT_INVERSE, st);
+    return dfft_rows(data, batch, len, dir == CUFFT_INVERSE, st);
   cufftHandle plan;
-  int rc = fft_plan(batch, 1, len, Prec<C>::type, &plan);
+  int rc = fft_plan(batch, 1, len, CUFFT_Z2Z, &plan);
   if (rc) return rc;
   if (cufftSetStream(plan, st) != CUFFT_SUCCESS)
     return set_error(CG_ERR_CUDA, "cufftSetStream failed");
-  const cufftResult r = Prec<C>::exec(plan, data, dir);
+  const cufftResult r =
+      cufftExecZ2Z(plan, (cufftDoubleComplex *)data, (cufftDoubleComplex *)data, dir);
   return r == CUFFT_SUCCESS ? CG_OK : set_error(CG_ERR_CUDA, "cufftExec failed: %d", (int)r);
+}
+
+int rows_fft(const cg_recombine *, float4 *data, int batch, int len, int dir, cudaStream_t st) {
+  return dfft_rows_df(data, batch, len, dir == CUFFT_INVERSE, st);
+}
+
+// the double-float pipeline: both transform lengths in reach of the
+// double-float FFT, unless FP64 cuFFT was asked for
+bool use_df(const cg_recombine *h) {
+  return h->fft_mode == 0 && dfft_supported(h->yP) && dfft_supported(h->xM_yP);
 }
 
 inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -485,36 +531,37 @@ WsLayoutT ws_layout_t(const cg_recombine *h, int n0, int n1) {
   return L;
 }
 
-template <typename C>
+template <class P>
 int subgrids_to_facet(cg_recombine *h, const void *fs, int centred, int n0, int n1, int fo0,
                       int fo1, void *facet, int out_centred, int accumulate, char *ws,
                       const WsLayoutT &L, cudaStream_t st) {
-  C *A = (C *)(ws + L.a);
-  C *acc = (C *)(ws + L.acc);
-  C *B = (C *)(ws + L.b);
-  C *acc2 = (C *)(ws + L.acc2);
+  typedef typename P::S S;
+  S *A = (S *)(ws + L.a);
+  S *acc = (S *)(ws + L.acc);
+  S *B = (S *)(ws + L.b);
+  S *acc2 = (S *)(ws + L.acc2);
   const int32_t *offs0 = (const int32_t *)(ws + L.offs);
   const int32_t *offs1 = offs0 + n0;
   const int yB = h->yB, yP = h->yP, xM = h->xM, xM_yP = h->xM_yP, xM_yN = h->xM_yN;
   int rc;
-  k_rcT_split<C><<<grid_for((size_t)n0 * n1 * xM_yN * xM_yP), 256, 0, st>>>(
-      (const C *)fs, n0 * n1, xM, xM_yN, xM_yP, fo0, fo1, Prec<C>::Fn(h), centred, A);
+  k_rcT_split<P><<<grid_for((size_t)n0 * n1 * xM_yN * xM_yP), 256, 0, st>>>(
+      (const double2 *)fs, n0 * n1, xM, xM_yN, xM_yP, fo0, fo1, Tab<P>::Fn(h), centred, A);
   CG_LAUNCH("recombine split subgrids");
-  if ((rc = rows_fft<C>(h, A, n0 * n1 * xM_yN, xM_yP, CUFFT_INVERSE, st))) return rc;
-  k_rcT_scatter<C><<<grid_for((size_t)n0 * xM_yN * yP), 256, 0, st>>>(
-      A, n0, n1, xM_yN, xM_yP, h->xMxN_yP, yP, offs1, Prec<C>::m(h), acc);
+  if ((rc = rows_fft(h, A, n0 * n1 * xM_yN, xM_yP, CUFFT_INVERSE, st))) return rc;
+  k_rcT_scatter<P><<<grid_for((size_t)n0 * xM_yN * yP), 256, 0, st>>>(
+      A, n0, n1, xM_yN, xM_yP, h->xMxN_yP, yP, offs1, Tab<P>::m(h), acc);
   CG_LAUNCH("recombine subgrid windows (axis 1)");
-  if ((rc = rows_fft<C>(h, acc, n0 * xM_yN, yP, CUFFT_FORWARD, st))) return rc;
-  k_rcT_crop_T_pad<C><<<dim3((xM_yP + 31) / 32, (yB + 31) / 32, n0), dim3(32, 8), 0, st>>>(
+  if ((rc = rows_fft(h, acc, n0 * xM_yN, yP, CUFFT_FORWARD, st))) return rc;
+  k_rcT_crop_T_pad<P><<<dim3((xM_yP + 31) / 32, (yB + 31) / 32, n0), dim3(32, 8), 0, st>>>(
       acc, n0, xM_yN, yP, yB, xM_yP, B);
   CG_LAUNCH("recombine crop to the facet (axis 1)");
-  if ((rc = rows_fft<C>(h, B, yB * n0, xM_yP, CUFFT_INVERSE, st))) return rc;
-  k_rcT_scatter<C><<<grid_for((size_t)yB * yP), 256, 0, st>>>(
-      B, yB, n0, 1, xM_yP, h->xMxN_yP, yP, offs0, Prec<C>::m(h), acc2);
+  if ((rc = rows_fft(h, B, yB * n0, xM_yP, CUFFT_INVERSE, st))) return rc;
+  k_rcT_scatter<P><<<grid_for((size_t)yB * yP), 256, 0, st>>>(
+      B, yB, n0, 1, xM_yP, h->xMxN_yP, yP, offs0, Tab<P>::m(h), acc2);
   CG_LAUNCH("recombine subgrid windows (axis 0)");
-  if ((rc = rows_fft<C>(h, acc2, yB, yP, CUFFT_FORWARD, st))) return rc;
-  k_rcT_final<C><<<dim3((yB + 31) / 32, (yB + 31) / 32), dim3(32, 8), 0, st>>>(
-      acc2, yP, yB, Prec<C>::Fb(h), out_centred, accumulate, (C *)facet);
+  if ((rc = rows_fft(h, acc2, yB, yP, CUFFT_FORWARD, st))) return rc;
+  k_rcT_final<P><<<dim3((yB + 31) / 32, (yB + 31) / 32), dim3(32, 8), 0, st>>>(
+      acc2, yP, yB, Tab<P>::Fb(h), out_centred, accumulate, (double2 *)facet);
   CG_LAUNCH("recombine facet");
   return CG_OK;
 }
@@ -531,37 +578,38 @@ WsLayout ws_layout(const cg_recombine *h, int n0, int n1) {
   return L;
 }
 
-template <typename C>
+template <class P>
 int facet_to_subgrids(cg_recombine *h, const void *facet, int centred, int n0, int n1,
                       void *nmbf, int out_centred, char *ws, const WsLayout &L,
                       cudaStream_t st) {
-  C *bf = (C *)(ws + L.bf);
-  C *mbf = (C *)(ws + L.mbf);
-  C *bf2 = (C *)(ws + L.bf2);
-  C *mbf2 = (C *)(ws + L.mbf2);
+  typedef typename P::S S;
+  S *bf = (S *)(ws + L.bf);
+  S *mbf = (S *)(ws + L.mbf);
+  S *bf2 = (S *)(ws + L.bf2);
+  S *mbf2 = (S *)(ws + L.mbf2);
   const int32_t *offs0 = (const int32_t *)(ws + L.offs);
   const int32_t *offs1 = offs0 + n0;
   const int yB = h->yB, yP = h->yP, xM_yP = h->xM_yP, xM_yN = h->xM_yN;
   int rc;
   const unsigned g1 = grid_for((size_t)yB * yP);
-  k_rc_prep_rows<C><<<g1, 256, 0, st>>>((const C *)facet, yB, yB, yP, Prec<C>::Fb(h), centred,
-                                         bf);
+  k_rc_prep_rows<P><<<g1, 256, 0, st>>>((const double2 *)facet, yB, yB, yP, Tab<P>::Fb(h),
+                                         centred, bf);
   CG_LAUNCH("recombine prepare facet (axis 1)");
-  if ((rc = rows_fft<C>(h, bf, yB, yP, CUFFT_INVERSE, st))) return rc;
-  k_rc_window<C><<<grid_for((size_t)n1 * yB * xM_yP), 256, 0, st>>>(
-      bf, yB, yP, offs1, n1, xM_yP, h->xMxN_yP, Prec<C>::m(h), mbf);
+  if ((rc = rows_fft(h, bf, yB, yP, CUFFT_INVERSE, st))) return rc;
+  k_rc_window<P><<<grid_for((size_t)n1 * yB * xM_yP), 256, 0, st>>>(
+      bf, yB, yP, offs1, n1, xM_yP, h->xMxN_yP, Tab<P>::m(h), mbf);
   CG_LAUNCH("recombine extract subgrid (axis 1)");
-  if ((rc = rows_fft<C>(h, mbf, n1 * yB, xM_yP, CUFFT_FORWARD, st))) return rc;
-  k_rc_crop_prep_T<C><<<dim3((yP + 31) / 32, (xM_yN + 31) / 32, n1), dim3(32, 8), 0, st>>>(
-      mbf, yB, xM_yP, xM_yN, Prec<C>::Fn(h), Prec<C>::Fb(h), yP, bf2);
+  if ((rc = rows_fft(h, mbf, n1 * yB, xM_yP, CUFFT_FORWARD, st))) return rc;
+  k_rc_crop_prep_T<P><<<dim3((yP + 31) / 32, (xM_yN + 31) / 32, n1), dim3(32, 8), 0, st>>>(
+      mbf, yB, xM_yP, xM_yN, Tab<P>::Fn(h), Tab<P>::Fb(h), yP, bf2);
   CG_LAUNCH("recombine prepare facet (axis 0)");
-  if ((rc = rows_fft<C>(h, bf2, n1 * xM_yN, yP, CUFFT_INVERSE, st))) return rc;
-  k_rc_window<C><<<grid_for((size_t)n0 * n1 * xM_yN * xM_yP), 256, 0, st>>>(
-      bf2, n1 * xM_yN, yP, offs0, n0, xM_yP, h->xMxN_yP, Prec<C>::m(h), mbf2);
+  if ((rc = rows_fft(h, bf2, n1 * xM_yN, yP, CUFFT_INVERSE, st))) return rc;
+  k_rc_window<P><<<grid_for((size_t)n0 * n1 * xM_yN * xM_yP), 256, 0, st>>>(
+      bf2, n1 * xM_yN, yP, offs0, n0, xM_yP, h->xMxN_yP, Tab<P>::m(h), mbf2);
   CG_LAUNCH("recombine extract subgrid (axis 0)");
-  if ((rc = rows_fft<C>(h, mbf2, n0 * n1 * xM_yN, xM_yP, CUFFT_FORWARD, st))) return rc;
-  k_rc_crop_T<C><<<dim3((xM_yN + 31) / 32, (xM_yN + 31) / 32, n0 * n1), dim3(32, 8), 0, st>>>(
-      mbf2, n1, xM_yP, xM_yN, Prec<C>::Fn(h), out_centred, (C *)nmbf);
+  if ((rc = rows_fft(h, mbf2, n0 * n1 * xM_yN, xM_yP, CUFFT_FORWARD, st))) return rc;
+  k_rc_crop_T<P><<<dim3((xM_yN + 31) / 32, (xM_yN + 31) / 32, n0 * n1), dim3(32, 8), 0, st>>>(
+      mbf2, n1, xM_yP, xM_yN, Tab<P>::Fn(h), out_centred, (double2 *)nmbf);
   CG_LAUNCH("recombine crop");
   return CG_OK;
 }
@@ -593,6 +641,17 @@ std::vector<double> generate_m(int N, int yP, int yN, int xM, int xMxN_yP, const
 int upload(const std::vector<double> &v, double **d) {
   CG_CUDA(cudaMalloc(d, v.size() * sizeof(double)));
   CG_CUDA(cudaMemcpy(*d, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return CG_OK;
+}
+
+int upload_df(const std::vector<double> &v, float2 **d) {
+  std::vector<float2> s(v.size());
+  for (size_t i = 0; i < v.size(); ++i) {
+    const float hi = (float)v[i];
+    s[i] = make_float2(hi, (float)(v[i] - (double)hi));
+  }
+  CG_CUDA(cudaMalloc(d, s.size() * sizeof(float2)));
+  CG_CUDA(cudaMemcpy(*d, s.data(), s.size() * sizeof(float2), cudaMemcpyHostToDevice));
   return CG_OK;
 }
 
@@ -649,7 +708,9 @@ int cg_recombine_create(int image_size, int subgrid_spacing, const double *pswf,
   for (int i = 0; i < xM_yN; ++i) Fn[i] = pswf[(size_t)i * (yN / xM_yN)];
   const std::vector<double> m = generate_m(image_size, yP, yN, xM, xMxN_yP, pswf);
   int rc;
-  if ((rc = upload(Fb, &h->d_Fb)) || (rc = upload(Fn, &h->d_Fn)) || (rc = upload(m, &h->d_m))) {
+  if ((rc = upload(Fb, &h->d_Fb)) || (rc = upload(Fn, &h->d_Fn)) || (rc = upload(m, &h->d_m)) ||
+      (rc = upload_df(Fb, &h->d_Fb2)) || (rc = upload_df(Fn, &h->d_Fn2)) ||
+      (rc = upload_df(m, &h->d_m2))) {
     cg_recombine_destroy(h);
     return rc;
   }
@@ -662,6 +723,9 @@ int cg_recombine_destroy(cg_recombine *h) {
   cudaFree(h->d_Fb);
   cudaFree(h->d_Fn);
   cudaFree(h->d_m);
+  cudaFree(h->d_Fb2);
+  cudaFree(h->d_Fn2);
+  cudaFree(h->d_m2);
   delete h;
   return CG_OK;
 }
@@ -715,7 +779,9 @@ int cg_recombine_facet_to_subgrids(cg_recombine *h, const void *facet, int centr
                                                       h->subgrid_spacing, h->yP_spacing, h->yP,
                                                       (int32_t *)(w + L.offs), d_status);
   CG_LAUNCH("recombine offsets");
-  return facet_to_subgrids<double2>(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
+  if (use_df(h))
+    return facet_to_subgrids<PDF>(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
+  return facet_to_subgrids<P64>(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
 }
 
 int cg_recombine_subgrids_to_facet(cg_recombine *h, const void *fs, int centred,
@@ -748,8 +814,11 @@ int cg_recombine_subgrids_to_facet(cg_recombine *h, const void *fs, int centred,
   // facet offsets in xM samples, reduced to [0, xM) (the kernels wrap once)
   const int fo0 = pmod((long long)facet_off0 / h->facet_spacing * h->xM_spacing, h->xM);
   const int fo1 = pmod((long long)facet_off1 / h->facet_spacing * h->xM_spacing, h->xM);
-  return subgrids_to_facet<double2>(h, fs, centred, n0, n1, fo0, fo1, facet, out_centred,
-                                    accumulate, w, L, st);
+  if (use_df(h))
+    return subgrids_to_facet<PDF>(h, fs, centred, n0, n1, fo0, fo1, facet, out_centred,
+                                  accumulate, w, L, st);
+  return subgrids_to_facet<P64>(h, fs, centred, n0, n1, fo0, fo1, facet, out_centred,
+                                accumulate, w, L, st);
 }
 
 int cg_recombine_add_facet(const cg_recombine *h, const void *nmbf, int n, int facet_off0,
@@ -764,7 +833,7 @@ int cg_recombine_add_facet(const cg_recombine *h, const void *nmbf, int n, int f
   const int fo1 = pmod((long long)facet_off1 / h->facet_spacing * h->xM_spacing, h->xM);
   const dim3 grid((h->xM_yN + 127) / 128, h->xM_yN, n);
   cudaStream_t st = (cudaStream_t)stream;
-  k_rc_add_facet<double2><<<grid, 128, 0, st>>>((const double2 *)nmbf, h->xM_yN, h->xM, fo0, fo1,
+  k_rc_add_facet<<<grid, 128, 0, st>>>((const double2 *)nmbf, h->xM_yN, h->xM, fo0, fo1,
                                                 centred, (double2 *)subgrids);
   CG_LAUNCH("recombine add facet");
   return CG_OK;

@@ -360,6 +360,22 @@ def fft_(t, inverse):
     return t
 
 
+def dfft2_supported(H, W):
+    """Sides the double-float 2-D transform takes: powers of two 64..2048."""
+    return all(64 <= n <= 2048 and n & (n - 1) == 0 for n in (H, W))
+
+
+def fft_df_(t, inverse):
+    """Centred (i)fft of the last two dims of a complex128 t, in place, in
+    double-float arithmetic on the FP32 units (about 48 significant bits)."""
+    H, W = t.shape[-2], t.shape[-1]
+    if t.dtype != CD or not t.is_contiguous() or not dfft2_supported(H, W):
+        raise ValueError("fft_df_ takes contiguous complex128 planes with power-of-two "
+                         "sides 64..2048")
+    L.call("cg_fft2_centred_df", _p(t), t.numel() // (H * W), H, W, int(inverse), stream())
+    return t
+
+
 def fft_raw(t, inverse):
     """Unshifted, unnormalised (i)fft of the last two dims of t, in place."""
     H, W = t.shape[-2], t.shape[-1]

@@ -83,6 +83,7 @@ class Recombine:
         if fft not in ("auto", "fp64"):
             raise ValueError("fft must be 'auto' (double-float for power-of-two rows) or 'fp64'")
         L.call("cg_recombine_set_fft", h, 0 if fft == "auto" else 1)
+        self.fft = fft
         sizes = (ctypes.c_int32 * 5)()
         L.call("cg_recombine_sizes", h, sizes)
         (self.xM_yP_size, self.xM_yN_size, self.facet_spacing, self.yP_spacing,
@@ -150,10 +151,18 @@ class Recombine:
                int(facet_off1), 1, E._p(approx), E.stream())
         return approx
 
+    def _fft2_(self, t, inverse):
+        # the double-float 2-D transform where its sizes allow ("auto"), else
+        # FP64 cuFFT
+        if self.fft == "auto" and E.dfft2_supported(self.xM_size, self.xM_size) \
+                and t.is_contiguous():
+            return E.fft_df_(t, inverse)
+        return E.fft_(t, inverse)
+
     def finish_subgrids(self, approx, crop=True):
         """The subgrids from their summed contributions: centred ifft (in place)
         and, with crop, the middle xA_size (a view)."""
-        E.fft_(approx, inverse=True)
+        self._fft2_(approx, inverse=True)
         if not crop:
             return approx
         c = self.xM_size // 2 - self.xA_size // 2
@@ -191,7 +200,7 @@ class Recombine:
             fs[..., lo:lo + xA, lo:lo + xA] = s
         else:
             fs = s.clone()
-        return E.fft_(fs, inverse=False)
+        return self._fft2_(fs, inverse=False)
 
     def subgrids_to_facet(self, fs, offs0, offs1, facet_off0, facet_off1, out=None,
                           accumulate=False, check=True):

@@ -289,13 +289,20 @@ int cg_fft(void *data, int batch, int H, int W, int is_c64, int inverse,
 /* The same transforms unshifted and unnormalised (cuFFT's own convention):
  * for callers that fold the centring shifts and the 1/(H W) of the inverse
  * into neighbouring passes (the w-towers pipeline). */
+int cg_fft_raw(void *data, int batch, int H, int W, int is_c64, int inverse,
+               cg_stream_t stream);
 /* batch contiguous complex128 rows of length n (a power of two, 64..2048)
  * transformed in place, unshifted and unnormalised (inverse: exp(+2 pi i)),
  * in double-float arithmetic (hi + lo pairs of floats, about 48 significant
  * bits) on the FP32 units: GB300's FP64 rate bounds an FP64 FFT. */
 int cg_fft_rows_df(void *data_c128, int64_t batch, int n, int inverse, cg_stream_t stream);
-int cg_fft_raw(void *data, int batch, int H, int W, int is_c64, int inverse,
-               cg_stream_t stream);
+/* cg_fft's centred 2-D transform (fft / ifft of synthesis.py) of batch
+ * complex128 planes H x W in place, H and W powers of two 64..2048, in the
+ * same double-float arithmetic: a row pass with the (-1)^(i+j) modulation
+ * that stands for ifftshift, then a column pass with the fftshift modulation
+ * and the 1/(H W) of the inverse. */
+int cg_fft2_centred_df(void *data_c128, int64_t batch, int H, int W, int inverse,
+                       cg_stream_t stream);
 
 /* Dirty image / PSF of a grid (synthesis.py:904-907): image = Re(ifft(
  * make_grid_hermitian(grid))), written as float32 H x W; the grid is
@@ -509,7 +516,9 @@ int cg_recombine_create(int image_size, int subgrid_spacing, const double *pswf_
 int cg_recombine_destroy(cg_recombine *h);
 /* FFTs of the recombination: mode 0 (default) transforms power-of-two rows
  * (64..2048) in double-float arithmetic on the FP32 units (cg_fft_rows_df)
- * and other lengths with cuFFT Z2Z; mode 1 uses cuFFT Z2Z throughout. */
+ * and other lengths with cuFFT Z2Z; when yP_size and xM_yP_size both qualify
+ * the stage arrays between the passes are double-float too (complex128 only
+ * in the caller's arrays).  Mode 1 uses complex128 and cuFFT Z2Z throughout. */
 int cg_recombine_set_fft(cg_recombine *h, int mode);
 /* sizes[0..4] = xM_yP_size, xM_yN_size, facet_spacing, yP_spacing, xM_spacing */
 int cg_recombine_sizes(const cg_recombine *h, int32_t *sizes);

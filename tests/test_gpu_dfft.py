@@ -1,6 +1,7 @@
-"""Double-float FFTs of complex128 rows (cg_fft_rows_df) against numpy's FP64
-FFT, and the recombination with power-of-two rows (double-float transforms)
-against the FP64 cuFFT form and the oracle."""
+"""Double-float FFTs of complex128 rows (cg_fft_rows_df) and centred 2-D
+planes (cg_fft2_centred_df) against numpy's FP64 FFT, and the recombination
+with power-of-two rows (double-float stage arrays and transforms) against the
+FP64 cuFFT form and the oracle."""
 
 import ctypes
 
@@ -72,3 +73,69 @@ def test_recombination_double_float_vs_fp64_and_oracle(env):
     fa = rc.subgrids_to_facet(fs, offs, offs, 128, 256).cpu().numpy() / Fbb
     fb = rc64.subgrids_to_facet(fs, offs, offs, 128, 256).cpu().numpy() / Fbb
     assert numpy.abs(fa - fb).max() / numpy.abs(fb).max() < 1e-10
+
+
+def centred(x, inverse):
+    ax = (-2, -1)
+    f = numpy.fft.ifft2 if inverse else numpy.fft.fft2
+    return numpy.fft.fftshift(f(numpy.fft.ifftshift(x, axes=ax), axes=ax), axes=ax)
+
+
+@pytest.mark.parametrize("H,W", [(64, 64), (512, 512), (64, 2048), (2048, 128), (256, 1024),
+                                 (1024, 64), (128, 256)])
+def test_fft2_centred_matches_numpy(env, H, W):
+    torch, E, L, R, O = env
+    rng = numpy.random.default_rng(H * 7 + W)
+    for batch in (1, 3):
+        x = rng.normal(size=(batch, H, W)) + 1j * rng.normal(size=(batch, H, W))
+        for inverse in (False, True):
+            t = E.cuda_tensor(x, E.CD)
+            E.fft_df_(t, inverse)
+            want = centred(x, inverse)
+            err = numpy.abs(t.cpu().numpy() - want).max() / numpy.abs(want).max()
+            # log2(H W) <= 22 double-float stages, ~1e-15 each
+            assert err < 5e-14, (H, W, batch, inverse, err)
+
+
+def test_fft2_centred_bad_sizes(env):
+    torch, E, L, R, O = env
+    t = torch.zeros((96, 128), dtype=E.CD, device="cuda")
+    with pytest.raises(ValueError):
+        E.fft_df_(t, True)
+    with pytest.raises(ValueError):
+        L.call("cg_fft2_centred_df", E._p(t), 1, 96, 128, 1, E.stream())
+
+
+def test_recombination_tiny_double_float_vs_fp64(env):
+    """The 8192 / 1280 / 512 configuration (every transform a power of two:
+    double-float stage arrays and FFTs) against complex128 with FP64 cuFFT,
+    both directions and the subgrids' finishing transforms."""
+    torch, E, L, R, O = env
+    from crocodile_gb300.bench_configs import RECOMBINE_TINY, recombine_layout
+    N, sp, yB, yN, yP, xA, xM, xMxN = RECOMBINE_TINY
+    rc = R.Recombine(N, sp, yB, yN, yP, xA, xM, xMxN)
+    rc64 = R.Recombine(N, sp, yB, yN, yP, xA, xM, xMxN, fft="fp64")
+    fo, so = recombine_layout(N, sp, yB, xA)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    facet = torch.randn((yB, yB), dtype=E.CD, device="cuda", generator=g)
+    a = rc.facet_to_subgrids(facet, so, so)
+    b = rc64.facet_to_subgrids(facet, so, so)
+    peak = b.abs().max().item()
+    # observed on the 256 / 128 set: double-float 1.4e-11 of the peak
+    assert (a - b).abs().max().item() / peak < 1e-10
+    ns = len(so)
+    approx = torch.zeros((ns, 2, xM, xM), dtype=E.CD, device="cuda")
+    rc.add_facet(approx, b[:, :2].contiguous(), fo[1], fo[2])
+    approx64 = approx.clone()
+    fa = rc.finish_subgrids(approx, crop=False)
+    fb = rc64.finish_subgrids(approx64, crop=False)
+    assert (fa - fb).abs().max().item() / fb.abs().max().item() < 5e-14
+    # the other direction, compared before the Fb x Fb weighting
+    spec = rc.subgrid_spectra(fb)
+    spec64 = rc64.subgrid_spectra(fb)
+    assert (spec - spec64).abs().max().item() / spec64.abs().max().item() < 5e-14
+    Fb = rc.windows()[0]
+    Fbb = torch.as_tensor(numpy.fft.fftshift(numpy.outer(Fb, Fb)), device="cuda")
+    x = rc.subgrids_to_facet(spec64, so, so[:2], fo[1], fo[2]) / Fbb
+    y = rc64.subgrids_to_facet(spec64, so, so[:2], fo[1], fo[2]) / Fbb
+    assert (x - y).abs().max().item() / y.abs().max().item() < 1e-10
