@@ -30,12 +30,15 @@
 
 #include "cg_internal.cuh"
 #include "df.cuh"
+#include "dfft.cuh"
 
 namespace cg {
 
-bool dfft_supported(int n);
-
 namespace {
+
+using dfk::AtCol;
+using dfk::radix2_first;
+using dfk::radix4;
 
 // ---------------------------------------------------------------- I/O policies
 // ld(row, i) / st(row, i, v): element i of transform row `row`
@@ -70,107 +73,6 @@ struct IoRowsCentred {
     ((float4 *)d)[row * n + i] = cdf_store(v);
   }
 };
-
-// ---------------------------------------------------------------- butterflies
-// One radix-2 butterfly of the first stage (stride 1, m = N/2) on element t2
-// and one radix-4 butterfly of the stage with stride s (m = N/(4s)) for
-// t = p s + q: inputs x[t + k N/4], outputs y[q + s (4p + k)], twiddles
-// w^(k p s) from the table (k p s < 3N/4).  x[.] indexes through `at`, so the
-// same code serves rows (at(i) = i) and column tiles (at(i) = i C + c).
-
-__device__ __forceinline__ cdf cdf_mul_j(const cdf &v, bool inverse) {  // times -i (+i)
-  return inverse ? cdf{df_neg(v.im), v.re} : cdf{v.im, df_neg(v.re)};
-}
-
-template <int N, class AT>
-__device__ __forceinline__ void radix2_first(const cdf *x, cdf *y, const cdf *stw, int t2,
-                                             AT at) {
-  const cdf a = x[at(t2)], b = x[at(t2 + N / 2)];
-  y[at(2 * t2)] = cdf_add_f(a, b);
-  const cdf d = cdf_sub_f(a, b);
-  y[at(2 * t2 + 1)] = t2 == 0 ? d : cdf_mul_f(d, stw[t2]);
-}
-
-template <int N, class AT>
-__device__ __forceinline__ void radix4(const cdf *x, cdf *y, const cdf *stw, int t, int s,
-                                       bool inverse, AT at) {
-  constexpr int Q = N / 4;
-  const int q = t & (s - 1), ps = t - q;  // p s
-  const cdf x0 = x[at(t)], x1 = x[at(t + Q)], x2 = x[at(t + 2 * Q)], x3 = x[at(t + 3 * Q)];
-  const cdf a0 = cdf_add_f(x0, x2), a1 = cdf_sub_f(x0, x2);
-  const cdf b0 = cdf_add_f(x1, x3), b1 = cdf_mul_j(cdf_sub_f(x1, x3), inverse);
-  const int o = q + 4 * ps;
-  y[at(o)] = cdf_add_f(a0, b0);
-  if (ps == 0) {
-    y[at(o + s)] = cdf_add_f(a1, b1);
-    y[at(o + 2 * s)] = cdf_sub_f(a0, b0);
-    y[at(o + 3 * s)] = cdf_sub_f(a1, b1);
-  } else {
-    y[at(o + s)] = cdf_mul_f(cdf_add_f(a1, b1), stw[ps]);
-    y[at(o + 2 * s)] = cdf_mul_f(cdf_sub_f(a0, b0), stw[2 * ps]);
-    y[at(o + 3 * s)] = cdf_mul_f(cdf_sub_f(a1, b1), stw[3 * ps]);
-  }
-}
-
-struct AtRow {
-  __device__ int operator()(int i) const { return i; }
-};
-template <int C>
-struct AtCol {
-  int c;
-  __device__ int operator()(int i) const { return i * C + c; }
-};
-
-// ---------------------------------------------------------------- row transforms
-// ROWS rows of length N per CTA, N/4 threads per row; two cdf buffers and
-// the 3N/4 twiddles in shared memory.  Odd log2 N: one radix-2 stage first.
-template <int LOGN, int ROWS, class IO>
-__global__ void __launch_bounds__((1 << LOGN) / 4 * ROWS)
-    k_dfft_rows(IO io, int64_t batch, const float4 *__restrict__ tw, int inverse) {
-  constexpr int N = 1 << LOGN;
-  constexpr int Q = N / 4;
-  extern __shared__ float dsm[];
-  cdf *buf0 = (cdf *)dsm;       // [ROWS][N]
-  cdf *buf1 = buf0 + ROWS * N;  // [ROWS][N]
-  cdf *stw = buf1 + ROWS * N;   // [3N/4] twiddles
-  const int r = threadIdx.x / Q, t = threadIdx.x - (threadIdx.x / Q) * Q;
-  for (int k = threadIdx.x; k < 3 * Q; k += blockDim.x) stw[k] = cdf_load(tw[k]);
-  const bool inv = inverse != 0;
-  for (int64_t row0 = (int64_t)blockIdx.x * ROWS; row0 < batch;
-       row0 += (int64_t)gridDim.x * ROWS) {
-    const int64_t row = row0 + r;
-    const bool live = row < batch;
-    cdf *x = buf0 + r * N, *y = buf1 + r * N;
-    if (live) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) x[t + k * Q] = io.ld(row, t + k * Q);
-    }
-    __syncthreads();
-    if (LOGN & 1) {
-      if (live) {
-        radix2_first<N>(x, y, stw, t, AtRow());
-        radix2_first<N>(x, y, stw, t + Q, AtRow());
-      }
-      __syncthreads();
-      cdf *tmp = x;
-      x = y;
-      y = tmp;
-    }
-#pragma unroll
-    for (int ls = (LOGN & 1); ls < LOGN; ls += 2) {
-      if (live) radix4<N>(x, y, stw, t, 1 << ls, inv, AtRow());
-      __syncthreads();
-      cdf *tmp = x;
-      x = y;
-      y = tmp;
-    }
-    if (live) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) io.st(row, t + k * Q, x[t + k * Q]);
-    }
-    __syncthreads();
-  }
-}
 
 // ---------------------------------------------------------------- column transforms
 // Planes [nplanes][N][W] of double-float, transformed along N (the columns);
@@ -231,10 +133,12 @@ __global__ void __launch_bounds__(T)
 }
 
 // ---------------------------------------------------------------- twiddles
+}  // namespace
+
 std::mutex g_tw_mu;
 std::map<std::pair<int, int>, float4 *> g_tw;  // (device, n * sign) -> table
 
-int twiddles(int n, int sign, const float4 **out) {
+int dfft_twiddles(int n, int sign, const float4 **out) {
   int dev = 0;
   cudaGetDevice(&dev);
   std::lock_guard<std::mutex> lock(g_tw_mu);
@@ -259,37 +163,7 @@ int twiddles(int n, int sign, const float4 **out) {
   return CG_OK;
 }
 
-template <int LOGN, int ROWS, class IO>
-int launch_rows(IO io, int64_t batch, const float4 *tw, int inverse, cudaStream_t st) {
-  constexpr int N = 1 << LOGN;
-  const size_t smem = (size_t)(2 * ROWS * N + 3 * N / 4) * sizeof(cdf);
-  if (smem > 48 * 1024)  // set on every launch: the attribute is per device
-    CG_CUDA(cudaFuncSetAttribute(k_dfft_rows<LOGN, ROWS, IO>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int64_t ctas = (batch + ROWS - 1) / ROWS;
-  const unsigned grid = (unsigned)std::min<int64_t>(ctas, (int64_t)num_sms() * 8);
-  k_dfft_rows<LOGN, ROWS, IO><<<grid, N / 4 * ROWS, smem, st>>>(io, batch, tw, inverse);
-  CG_LAUNCH("double-float FFT");
-  return CG_OK;
-}
-
-template <class IO>
-int rows_any(IO io, int64_t batch, int n, int inverse, cudaStream_t st) {
-  CG_REQUIRE(dfft_supported(n), "double-float FFT lengths are powers of two 64..2048");
-  if (batch <= 0) return CG_OK;
-  const float4 *tw;
-  int rc = twiddles(n, inverse ? 1 : -1, &tw);
-  if (rc) return rc;
-  switch (n) {  // N/4 threads per row, 256 threads per CTA up to 1024
-    case 64: return launch_rows<6, 16>(io, batch, tw, inverse, st);
-    case 128: return launch_rows<7, 8>(io, batch, tw, inverse, st);
-    case 256: return launch_rows<8, 4>(io, batch, tw, inverse, st);
-    case 512: return launch_rows<9, 2>(io, batch, tw, inverse, st);
-    case 1024: return launch_rows<10, 1>(io, batch, tw, inverse, st);
-    case 2048: return launch_rows<11, 1>(io, batch, tw, inverse, st);
-  }
-  return set_error(CG_ERR_ARG, "unsupported double-float FFT length %d", n);
-}
+namespace {
 
 template <int LOGN, int C>
 int launch_cols(double2 *d, int64_t nplanes, int W, int phase, float scale, const float4 *tw,
@@ -315,12 +189,12 @@ bool dfft_supported(int n) { return n >= 64 && n <= 2048 && (n & (n - 1)) == 0; 
 // In-place batched FFT of `batch` contiguous complex128 rows of length n
 // (a power of two, 64..2048); inverse: exp(+2 pi i), unnormalised.
 int dfft_rows(double2 *data, int64_t batch, int n, int inverse, cudaStream_t st) {
-  return rows_any(IoC128{data, n}, batch, n, inverse, st);
+  return dfft_rows_io(IoC128{data, n}, batch, n, inverse, st);
 }
 
 // The same on rows stored as double-float (float4 per element).
 int dfft_rows_df(float4 *data, int64_t batch, int n, int inverse, cudaStream_t st) {
-  return rows_any(IoDF{data, n}, batch, n, inverse, st);
+  return dfft_rows_io(IoDF{data, n}, batch, n, inverse, st);
 }
 
 // In-place centred 2-D FFT of `batch` complex128 planes [H][W] (numpy's
@@ -331,10 +205,10 @@ int dfft2_centred(double2 *data, int64_t batch, int H, int W, int inverse, cudaS
   CG_REQUIRE(dfft_supported(H) && dfft_supported(W),
              "double-float 2-D FFT sides are powers of two 64..2048");
   if (batch <= 0) return CG_OK;
-  int rc = rows_any(IoRowsCentred{data, W, H}, batch * H, W, inverse, st);
+  int rc = dfft_rows_io(IoRowsCentred{data, W, H}, batch * H, W, inverse, st);
   if (rc) return rc;
   const float4 *tw;
-  if ((rc = twiddles(H, inverse ? 1 : -1, &tw))) return rc;
+  if ((rc = dfft_twiddles(H, inverse ? 1 : -1, &tw))) return rc;
   const int phase = (H / 2 + W / 2) & 1;
   const float scale = inverse ? 1.0f / ((float)H * (float)W) : 1.0f;  // a power of two
   switch (H) {  // columns per CTA: 64 KB of buffers (3 CTAs per SM) up to 512; C >= 2

@@ -16,11 +16,16 @@
 //      forward FFT of n0 * n1 * xM_yN rows of length xM_yP
 //   5. k_rc_crop_T      : crop times Fn, transpose to [i0][i1][axis 0][axis 1]
 // Every FFT runs over contiguous rows.  The caller's arrays are complex128 as
-// the reference; when both transform lengths are powers of two 64..2048 the
-// stage arrays between the kernels hold double-float pairs (about 48
-// significant bits, arithmetic on the FP32 units, df.cuh) and the transforms
-// are the double-float FFTs, else complex128 with FP64 cuFFT.  Arrays
-// are in the C prototype's raw
+// the reference.  When both transform lengths are powers of two 64..2048 the
+// double-float pipeline runs (facet_to_subgrids_df / subgrids_to_facet_df):
+// stage arrays of double-float pairs (about 48 significant bits, arithmetic
+// on the FP32 units, df.cuh), double-float FFTs (dfft.cuh), and steps 1, 2,
+// 4 and 5 done inside the loads and stores of the neighbouring transforms
+// (prepare in the loads of the first, the windows in the loads of the
+// xM_yP transforms, the final crop in the stores of the last), so that per
+// facet four transform launches and the transpose of step 3 remain.
+// Otherwise complex128 with FP64 cuFFT and the separate stage kernels.
+// Arrays are in the C prototype's raw
 // layout (centre at index 0, FFTW sign conventions: backward = e^{+2 pi i},
 // unnormalised) except where a `centred` flag maps the facet in or the
 // result out in numpy's fftshift layout (the notebook's).
@@ -39,6 +44,7 @@
 
 #include "cg_internal.cuh"
 #include "df.cuh"
+#include "dfft.cuh"
 
 namespace cg {
 int fft_plan(int batch, int H, int W, cufftType type, cufftHandle *out);
@@ -353,20 +359,19 @@ __global__ void k_rcT_split(const double2 *__restrict__ fs, int npair, int xM, i
 // out[o][r][k] (k < yP) = sum over j < noff of the window of in[o][j][r][.]
 // placed at offset offs[j]: position p (|p| within xMxN_yP / 2) of the
 // periodic extension of the xM_yP samples, times m, lands at (p + off) mod yP.
+// Grid: x over k, y striding over the rows o * inner + r.
 template <class P>
 __global__ void k_rcT_scatter(const typename P::S *__restrict__ in, int outer, int noff,
                               int inner, int xM_yP, int xMxN_yP, int yP,
                               const int32_t *__restrict__ offs,
                               const typename P::WS *__restrict__ m,
                               typename P::S *__restrict__ out) {
-  const size_t total = (size_t)outer * inner * yP;
   const int half = xMxN_yP / 2;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (size_t)gridDim.x * blockDim.x) {
-    const int k = (int)(e % yP);
-    const size_t orow = e / yP;
-    const int r = (int)(orow % inner);
-    const size_t o = orow / inner;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= yP) return;
+  const int nrow = outer * inner;
+  for (int row = blockIdx.y; row < nrow; row += gridDim.y) {
+    const int o = row / inner, r = row - (row / inner) * inner;
     typename P::V v = P::zero();
     for (int j = 0; j < noff; ++j) {
       // k, offs[j] in [0, yP): the signed distance in [-yP/2, yP/2)
@@ -376,10 +381,16 @@ __global__ void k_rcT_scatter(const typename P::S *__restrict__ in, int outer, i
       if (p < -half || p >= xMxN_yP - half) continue;
       // |p| <= xMxN_yP / 2 <= xM_yP: one wrap each
       v = P::madd(v, P::w(m, p < 0 ? p + xMxN_yP : p),
-                  P::ld(in[((o * noff + j) * inner + r) * xM_yP + (p < 0 ? p + xM_yP : p)]));
+                  P::ld(in[(((size_t)o * noff + j) * inner + r) * xM_yP +
+                           (p < 0 ? p + xM_yP : p)]));
     }
-    out[e] = P::st(v);
+    out[(size_t)row * yP + k] = P::st(v);
   }
+}
+
+// launch shape of k_rcT_scatter
+inline dim3 scatter_grid(int nrow, int yP) {
+  return dim3((yP + 255) / 256, std::min(std::max(nrow, 1), 65535));
 }
 
 // B[t][i0][k0]: rows (i0, a0) of acc [n0][xM_yN][yP] cropped to the yB facet
@@ -454,9 +465,161 @@ __global__ void k_rcT_final(const typename P::S *__restrict__ acc2, int yP, int 
   }
 }
 
+// ------------------------------------------------ fused double-float passes
+// I/O policies of the double-float row transforms (dfft.cuh) that take over
+// the stage kernels above in the double-float pipeline: each window, prepare
+// or crop step runs inside the loads or the stores of the transform next to
+// it, with the same arithmetic as the stage kernel it replaces, so that stage
+// array is neither written nor read.
+
+// prepare_facet along the rows (k_rc_prep_rows) as the load of the yP inverse
+// transforms; rows r < yB
+struct IoPrep {
+  const double2 *facet;
+  const float2 *Fb;
+  float4 *out;
+  int yB, yP, centred;
+  __device__ cdf ld(int64_t row, int k) const {
+    const int t = uncrop(k, yB, yP);
+    if (t < 0) return PDF::zero();
+    const int r = (int)row, h = yB / 2;
+    const int rs = centred ? (r + h) % yB : r;
+    const int ts = centred ? (t + h) % yB : t;
+    return PDF::scale(PDF::in(facet[(size_t)rs * yB + ts]), PDF::wdiv(PDF::w(Fb, t), yP));
+  }
+  __device__ void st(int64_t row, int k, const cdf &v) const {
+    out[row * yP + k] = PDF::st(v);
+  }
+};
+
+// extract_subgrid's window (k_rc_window): element i of transform row
+// o * rows + r is the window of bf row r at offset offs[o]
+struct WindowSrc {
+  const float4 *bf;
+  const int32_t *offs;
+  const float2 *m;
+  int rows, yP, xM_yP, xMxN_yP;
+  __device__ cdf ld(int64_t row, int i) const {
+    const int o = (int)row / rows, r = (int)row - ((int)row / rows) * rows;
+    const int off = offs[o];
+    const float4 *src = bf + (size_t)r * yP;
+    cdf v = PDF::zero();
+    if (i < (xMxN_yP + 1) / 2) v = PDF::madd(v, PDF::w(m, i), PDF::ld(src[wrap1(i + off, yP)]));
+    if (i >= xM_yP - xMxN_yP / 2)
+      v = PDF::madd(v, PDF::w(m, xMxN_yP - xM_yP + i),
+                    PDF::ld(src[wrap1(i + off - xM_yP, yP)]));
+    return v;
+  }
+};
+
+struct IoWindowDF {  // the window in, double-float rows out
+  WindowSrc w;
+  float4 *out;
+  __device__ cdf ld(int64_t row, int i) const { return w.ld(row, i); }
+  __device__ void st(int64_t row, int i, const cdf &v) const {
+    out[row * w.xM_yP + i] = PDF::st(v);
+  }
+};
+
+// the window in; the final crop times Fn and transpose (k_rc_crop_T) out:
+// transform row pair * xM_yN + a1, element crop_src(a0) -> out[pair][a0][a1]
+struct IoWindowCrop {
+  WindowSrc w;
+  const float2 *Fn;
+  double2 *out;
+  int xM_yN, centred;
+  __device__ cdf ld(int64_t row, int i) const { return w.ld(row, i); }
+  __device__ void st(int64_t row, int i, const cdf &v) const {
+    const int a0 = uncrop(i, xM_yN, w.xM_yP);
+    if (a0 < 0) return;
+    const int pair = (int)row / xM_yN, a1 = (int)row - ((int)row / xM_yN) * xM_yN;
+    const int h = xM_yN / 2;
+    const int d0 = centred ? (a0 + h) % xM_yN : a0;
+    const int d1 = centred ? (a1 + h) % xM_yN : a1;
+    out[((size_t)pair * xM_yN + d0) * xM_yN + d1] = PDF::out(PDF::scale(v, PDF::w(Fn, a0)));
+  }
+};
+
+// subgrid -> facet: the split of each subgrid spectrum (k_rcT_split) as the
+// load of the xM_yP inverse transforms; rows pair * xM_yN + a0
+struct IoSplit {
+  const double2 *fs;
+  const float2 *Fn;
+  float4 *out;
+  int xM, xM_yN, xM_yP, fo0, fo1, centred;
+  __device__ cdf ld(int64_t row, int k) const {
+    const int c1 = uncrop(k, xM_yN, xM_yP);
+    if (c1 < 0) return PDF::zero();
+    const int pair = (int)row / xM_yN, a0 = (int)row - ((int)row / xM_yN) * xM_yN;
+    int s0 = wrap1(signed_freq(a0, xM_yN) + fo0, xM);
+    int s1 = wrap1(signed_freq(c1, xM_yN) + fo1, xM);
+    if (centred) {
+      s0 = (s0 + xM / 2) % xM;
+      s1 = (s1 + xM / 2) % xM;
+    }
+    return PDF::scale(PDF::in(fs[((size_t)pair * xM + s0) * xM + s1]),
+                      PDF::wdiv(PDF::wmul(PDF::w(Fn, a0), PDF::w(Fn, c1)), xM_yP));
+  }
+  __device__ void st(int64_t row, int k, const cdf &v) const {
+    out[row * xM_yP + k] = PDF::st(v);
+  }
+};
+
+// the windows of every subgrid summed into place (k_rcT_scatter): element k
+// of transform row o * inner + r
+struct ScatterSrc {
+  const float4 *in;
+  const int32_t *offs;
+  const float2 *m;
+  int noff, inner, xM_yP, xMxN_yP, yP;
+  __device__ cdf ld(int64_t row, int k) const {
+    const int o = (int)row / inner, r = (int)row - ((int)row / inner) * inner;
+    const int half = xMxN_yP / 2;
+    cdf v = PDF::zero();
+    for (int j = 0; j < noff; ++j) {
+      int p = k - offs[j];
+      if (p >= yP / 2) p -= yP;
+      if (p < -(yP / 2)) p += yP;
+      if (p < -half || p >= xMxN_yP - half) continue;
+      v = PDF::madd(v, PDF::w(m, p < 0 ? p + xMxN_yP : p),
+                    PDF::ld(in[(((size_t)o * noff + j) * inner + r) * xM_yP +
+                               (p < 0 ? p + xM_yP : p)]));
+    }
+    return v;
+  }
+};
+
+// the scatter in; the facet crop times Fb x Fb and transpose (k_rcT_final)
+// out: transform row t, element ks -> facet[s][t]
+struct IoScatterFinal {
+  ScatterSrc s;
+  const float2 *Fb;
+  double2 *facet;
+  int yB, centred, accumulate;
+  __device__ cdf ld(int64_t row, int k) const { return s.ld(row, k); }
+  __device__ void st(int64_t row, int k, const cdf &v) const {
+    const int sx = uncrop(k, yB, s.yP);
+    if (sx < 0) return;
+    const int t = (int)row, h = yB / 2;
+    const int d0 = centred ? (sx + h) % yB : sx;
+    const int d1 = centred ? (t + h) % yB : t;
+    const double2 o = PDF::out(PDF::scale(v, PDF::wmul(PDF::w(Fb, sx), PDF::w(Fb, t))));
+    double2 *d = facet + (size_t)d0 * yB + d1;
+    if (accumulate) {
+      double2 a = *d;
+      a.x += o.x;
+      a.y += o.y;
+      *d = a;
+    } else {
+      *d = o;
+    }
+  }
+};
+
 // ------------------------------------------------------------------ host side
 
-// the window tables of a policy
+// the window tables of the complex128 pipeline (the double-float one reads
+// the split copies d_Fb2, d_Fn2, d_m2)
 template <class P>
 struct Tab;
 template <>
@@ -464,12 +627,6 @@ struct Tab<P64> {
   static const double *Fb(const cg_recombine *h) { return h->d_Fb; }
   static const double *Fn(const cg_recombine *h) { return h->d_Fn; }
   static const double *m(const cg_recombine *h) { return h->d_m; }
-};
-template <>
-struct Tab<PDF> {
-  static const float2 *Fb(const cg_recombine *h) { return h->d_Fb2; }
-  static const float2 *Fn(const cg_recombine *h) { return h->d_Fn2; }
-  static const float2 *m(const cg_recombine *h) { return h->d_m2; }
 };
 
 // complex128 only: Fb = 1 / PSWF spans many decades at the facet edge (6.4e6
@@ -489,10 +646,6 @@ int rows_fft(const cg_recombine *h, double2 *data, int batch, int len, int dir, 
   const cufftResult r =
       cufftExecZ2Z(plan, (cufftDoubleComplex *)data, (cufftDoubleComplex *)data, dir);
   return r == CUFFT_SUCCESS ? CG_OK : set_error(CG_ERR_CUDA, "cufftExec failed: %d", (int)r);
-}
-
-int rows_fft(const cg_recombine *, float4 *data, int batch, int len, int dir, cudaStream_t st) {
-  return dfft_rows_df(data, batch, len, dir == CUFFT_INVERSE, st);
 }
 
 // the double-float pipeline: both transform lengths in reach of the
@@ -548,7 +701,7 @@ int subgrids_to_facet(cg_recombine *h, const void *fs, int centred, int n0, int 
       (const double2 *)fs, n0 * n1, xM, xM_yN, xM_yP, fo0, fo1, Tab<P>::Fn(h), centred, A);
   CG_LAUNCH("recombine split subgrids");
   if ((rc = rows_fft(h, A, n0 * n1 * xM_yN, xM_yP, CUFFT_INVERSE, st))) return rc;
-  k_rcT_scatter<P><<<grid_for((size_t)n0 * xM_yN * yP), 256, 0, st>>>(
+  k_rcT_scatter<P><<<scatter_grid(n0 * xM_yN, yP), 256, 0, st>>>(
       A, n0, n1, xM_yN, xM_yP, h->xMxN_yP, yP, offs1, Tab<P>::m(h), acc);
   CG_LAUNCH("recombine subgrid windows (axis 1)");
   if ((rc = rows_fft(h, acc, n0 * xM_yN, yP, CUFFT_FORWARD, st))) return rc;
@@ -556,7 +709,7 @@ int subgrids_to_facet(cg_recombine *h, const void *fs, int centred, int n0, int 
       acc, n0, xM_yN, yP, yB, xM_yP, B);
   CG_LAUNCH("recombine crop to the facet (axis 1)");
   if ((rc = rows_fft(h, B, yB * n0, xM_yP, CUFFT_INVERSE, st))) return rc;
-  k_rcT_scatter<P><<<grid_for((size_t)yB * yP), 256, 0, st>>>(
+  k_rcT_scatter<P><<<scatter_grid(yB, yP), 256, 0, st>>>(
       B, yB, n0, 1, xM_yP, h->xMxN_yP, yP, offs0, Tab<P>::m(h), acc2);
   CG_LAUNCH("recombine subgrid windows (axis 0)");
   if ((rc = rows_fft(h, acc2, yB, yP, CUFFT_FORWARD, st))) return rc;
@@ -612,6 +765,73 @@ int facet_to_subgrids(cg_recombine *h, const void *facet, int centred, int n0, i
       mbf2, n1, xM_yP, xM_yN, Tab<P>::Fn(h), out_centred, (double2 *)nmbf);
   CG_LAUNCH("recombine crop");
   return CG_OK;
+}
+
+// The double-float pipelines with the fused passes: per facet, four
+// transform launches and one transpose kernel each way (and the scatter
+// kernel of the first axis on the way back).
+int facet_to_subgrids_df(cg_recombine *h, const void *facet, int centred, int n0, int n1,
+                         void *nmbf, int out_centred, char *ws, const WsLayout &L,
+                         cudaStream_t st) {
+  float4 *bf = (float4 *)(ws + L.bf);
+  float4 *mbf = (float4 *)(ws + L.mbf);
+  float4 *bf2 = (float4 *)(ws + L.bf2);
+  const int32_t *offs0 = (const int32_t *)(ws + L.offs);
+  const int32_t *offs1 = offs0 + n0;
+  const int yB = h->yB, yP = h->yP, xM_yP = h->xM_yP, xM_yN = h->xM_yN, xMxN = h->xMxN_yP;
+  int rc;
+  // prepare along axis 1 in the loads of the yP inverse transforms
+  if ((rc = dfft_rows_io(IoPrep{(const double2 *)facet, h->d_Fb2, bf, yB, yP, centred}, yB, yP,
+                         1, st)))
+    return rc;
+  // each subgrid column offset's window in the loads of the xM_yP transforms
+  if ((rc = dfft_rows_io(IoWindowDF{WindowSrc{bf, offs1, h->d_m2, yB, yP, xM_yP, xMxN}, mbf},
+                         (int64_t)n1 * yB, xM_yP, 0, st)))
+    return rc;
+  k_rc_crop_prep_T<PDF><<<dim3((yP + 31) / 32, (xM_yN + 31) / 32, n1), dim3(32, 8), 0, st>>>(
+      mbf, yB, xM_yP, xM_yN, h->d_Fn2, h->d_Fb2, yP, bf2);
+  CG_LAUNCH("recombine prepare facet (axis 0)");
+  if ((rc = dfft_rows_df(bf2, (int64_t)n1 * xM_yN, yP, 1, st))) return rc;
+  // each subgrid row offset's window in the loads, the crop in the stores
+  return dfft_rows_io(
+      IoWindowCrop{WindowSrc{bf2, offs0, h->d_m2, n1 * xM_yN, yP, xM_yP, xMxN}, h->d_Fn2,
+                   (double2 *)nmbf, xM_yN, out_centred},
+      (int64_t)n0 * n1 * xM_yN, xM_yP, 0, st);
+}
+
+int subgrids_to_facet_df(cg_recombine *h, const void *fs, int centred, int n0, int n1, int fo0,
+                         int fo1, void *facet, int out_centred, int accumulate, char *ws,
+                         const WsLayoutT &L, cudaStream_t st) {
+  float4 *A = (float4 *)(ws + L.a);
+  float4 *acc = (float4 *)(ws + L.acc);
+  float4 *B = (float4 *)(ws + L.b);
+  const int32_t *offs0 = (const int32_t *)(ws + L.offs);
+  const int32_t *offs1 = offs0 + n0;
+  const int yB = h->yB, yP = h->yP, xM = h->xM, xM_yP = h->xM_yP, xM_yN = h->xM_yN;
+  const int xMxN = h->xMxN_yP;
+  int rc;
+  // each subgrid spectrum's share of the facet in the loads of the xM_yP inverse transforms
+  if ((rc = dfft_rows_io(IoSplit{(const double2 *)fs, h->d_Fn2, A, xM, xM_yN, xM_yP, fo0, fo1,
+                                 centred},
+                         (int64_t)n0 * n1 * xM_yN, xM_yP, 1, st)))
+    return rc;
+  // the subgrid column windows summed by a separate kernel: in the loads of
+  // the yP transforms (ScatterSrc) the 2048-point kernel's occupancy leaves
+  // the offset loop's dependent loads exposed (measured 193 us against 158
+  // for the pair on the 8192 / 1280 / 512 set)
+  k_rcT_scatter<PDF><<<scatter_grid(n0 * xM_yN, yP), 256, 0, st>>>(
+      A, n0, n1, xM_yN, xM_yP, xMxN, yP, offs1, h->d_m2, acc);
+  CG_LAUNCH("recombine subgrid windows (axis 1)");
+  if ((rc = dfft_rows_df(acc, (int64_t)n0 * xM_yN, yP, 0, st))) return rc;
+  k_rcT_crop_T_pad<PDF><<<dim3((xM_yP + 31) / 32, (yB + 31) / 32, n0), dim3(32, 8), 0, st>>>(
+      acc, n0, xM_yN, yP, yB, xM_yP, B);
+  CG_LAUNCH("recombine crop to the facet (axis 1)");
+  if ((rc = dfft_rows_df(B, (int64_t)yB * n0, xM_yP, 1, st))) return rc;
+  // the subgrid row windows summed in the loads, the facet crop in the stores
+  return dfft_rows_io(
+      IoScatterFinal{ScatterSrc{B, offs0, h->d_m2, n0, 1, xM_yP, xMxN, yP}, h->d_Fb2,
+                     (double2 *)facet, yB, out_centred, accumulate},
+      yB, yP, 0, st);
 }
 
 // generate_m (recombine.c:35-67): the PSWF times the sinc of the xM box, then
@@ -780,7 +1000,7 @@ int cg_recombine_facet_to_subgrids(cg_recombine *h, const void *facet, int centr
                                                       (int32_t *)(w + L.offs), d_status);
   CG_LAUNCH("recombine offsets");
   if (use_df(h))
-    return facet_to_subgrids<PDF>(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
+    return facet_to_subgrids_df(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
   return facet_to_subgrids<P64>(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
 }
 
@@ -815,8 +1035,8 @@ int cg_recombine_subgrids_to_facet(cg_recombine *h, const void *fs, int centred,
   const int fo0 = pmod((long long)facet_off0 / h->facet_spacing * h->xM_spacing, h->xM);
   const int fo1 = pmod((long long)facet_off1 / h->facet_spacing * h->xM_spacing, h->xM);
   if (use_df(h))
-    return subgrids_to_facet<PDF>(h, fs, centred, n0, n1, fo0, fo1, facet, out_centred,
-                                  accumulate, w, L, st);
+    return subgrids_to_facet_df(h, fs, centred, n0, n1, fo0, fo1, facet, out_centred,
+                                accumulate, w, L, st);
   return subgrids_to_facet<P64>(h, fs, centred, n0, n1, fo0, fo1, facet, out_centred,
                                 accumulate, w, L, st);
 }
