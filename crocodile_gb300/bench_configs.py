@@ -406,8 +406,9 @@ def measure_recombine(steps=3, nfacets=None):
             "stage_gb_per_facet": nbytes / 1e9,
             "stage_gb_s": nbytes / (ms_facet * 1e-3) / 1e9,
             "subgrids_to_facets_ms": ms_split, "subgrids_to_facet_ms_per_facet": ms_split_facet,
-            "note": "ms: facets -> subgrids (per facet: 2 row-FFT passes per axis and 5 "
-                    "fused window / crop / transpose kernels, stage arrays and FFTs in "
+            "note": "ms: facets -> subgrids (per facet: 4 row-transform launches with the "
+                    "prepare, window and crop steps in their loads and stores, 1 transpose "
+                    "kernel and the sum into the subgrids; stage arrays and FFTs in "
                     "double-float arithmetic on the FP32 units, complex128 in and out; then "
                     "the subgrid sums' 512^2 inverse FFTs, double-float too); "
                     "fp64_fft_tflop_s counts 5 n log2 n per transform; "

@@ -77,9 +77,23 @@ __device__ __forceinline__ cdf cdf_add_f(const cdf &a, const cdf &b) {
 __device__ __forceinline__ cdf cdf_sub_f(const cdf &a, const cdf &b) {
   return {df_add_fast(a.re, df_neg(b.re)), df_add_fast(a.im, df_neg(b.im))};
 }
+// x.hi y.hi + sg z.hi t.hi as an exact two_sum of the two rounded products,
+// their rounding errors (FMA) and the four cross terms accumulated in one
+// float, then one renormalisation: 19 operations against 25 for two df_mul
+// and a sloppy sum, with the same kind of normwise bound
+__device__ __forceinline__ df df_dot2(df x, df y, df z, df t, float sg) {
+  const float p1 = x.hi * y.hi, p2 = sg * z.hi * t.hi;
+  const float e1 = fmaf(x.hi, y.hi, -p1), e2 = fmaf(sg * z.hi, t.hi, -p2);
+  const df s = two_sum(p1, p2);
+  float c = s.lo + (e1 + e2);
+  c = fmaf(x.hi, y.lo, c);
+  c = fmaf(x.lo, y.hi, c);
+  c = fmaf(sg * z.hi, t.lo, c);
+  c = fmaf(sg * z.lo, t.hi, c);
+  return fast_two_sum(s.hi, c);
+}
 __device__ __forceinline__ cdf cdf_mul_f(const cdf &a, const cdf &w) {
-  return {df_add_fast(df_mul(a.re, w.re), df_neg(df_mul(a.im, w.im))),
-          df_add_fast(df_mul(a.re, w.im), df_mul(a.im, w.re))};
+  return {df_dot2(a.re, w.re, a.im, w.im, -1.f), df_dot2(a.re, w.im, a.im, w.re, 1.f)};
 }
 // a times a real double-float
 __device__ __forceinline__ cdf cdf_scale(const cdf &a, df w) {
