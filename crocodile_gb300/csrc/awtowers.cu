@@ -19,8 +19,11 @@
 // order numpy evaluates the notebook's expressions, so they are bit-identical.
 
 #include <algorithm>
+#include <cmath>
+#include <vector>
 
 #include "cg_internal.cuh"
+#include "tiled.cuh"
 
 namespace {
 
@@ -165,6 +168,141 @@ __global__ void k_awtowers_combine(const float2 *__restrict__ stack, int s, doub
   if (bad && status) atomicAdd(&status[ST_RANGE], 1);
 }
 
+// ------------------------------------------------ direct layer images
+// The layers' values at the cut without the 2s x 2s grids and their FFTs.
+// The anti-aliasing kernel is separable, so the unshifted inverse transform
+// of a layer's grid at (Ar, Br) is the sum over its visibilities of
+//   vis * Av(Ar) * Au(Br),  Av(Ar) = sum_a ky[a] w^((y0 + a) Ar),
+//                           Au(Br) = sum_b kx[b] w^((x0 + b) Br),
+// w = exp(+2 pi i / 2s), with (x0, y0, ky, kx) the plan's footprint and tap
+// rows of that visibility (the values cuFFT would produce there, summed in
+// another order).  Only the s x s cut is formed: Ar = (i + 3s/2) mod 2s,
+// Br = (j + 3s/2) mod 2s.  A layer of a few visibilities costs a few
+// thousand complex products instead of a 2s x 2s grid, its zeroing and its
+// transform.  Each CTA takes chunks in turn; per layer the visibilities'
+// A-vectors go through shared memory in batches of AWT_NB, each thread
+// accumulates its pixels (column j = tid mod s, rows i = tid / s + k 256/s),
+// then multiplies by the combine's factor (antenna ratio, conjugate Fresnel
+// factor) into its chunk sums, which leave times corr x sign / (2s)^2 rolled
+// as k_awtowers_combine writes them.
+
+constexpr int AWT_NB = 32;  // visibilities per shared-memory batch
+
+bool awtowers_direct_supported(int s) { return s == 16 || s == 32 || s == 64; }
+
+// per cut pixel: the Fresnel phase 1 - sqrt(1 - l^2 - m^2) as hi + lo floats
+// and corr x (-1)^(A+B) / (2s)^2
+__global__ void k_awt_pixels(int s, double theta, const float *__restrict__ corr,
+                             float4 *__restrict__ pix, int32_t *status) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= s * s) return;
+  const int i = k / s, j = k - (k / s) * s, half = s / 2;
+  const double l = __dmul_rn(theta, __ddiv_rn((double)(j - half), (double)s));
+  const double m = __dmul_rn(theta, __ddiv_rn((double)(i - half), (double)s));
+  const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
+  if (!(r2 < 1.0) && status) atomicAdd(&status[ST_RANGE], 1);
+  const double ph = 1.0 - sqrt(1.0 - r2);
+  const float ph_h = (float)ph, ph_l = (float)(ph - (double)ph_h);
+  const float scale = 1.0f / ((float)(2 * s) * (float)(2 * s));
+  const float sg = ((((i + half) + (j + half)) & 1) ? -scale : scale) * corr[k];
+  pix[k] = make_float4(ph_h, ph_l, sg, 0.f);
+}
+
+template <int SUB>
+__global__ void __launch_bounds__(256)
+    k_awtowers_direct(TiledArgs A, int bpl, int nbuckets, int layers,
+                      const int32_t *__restrict__ offsets, const int32_t *__restrict__ counts,
+                      const float2 *__restrict__ ktab, const float2 *__restrict__ vis,
+                      const float4 *__restrict__ pix, const float2 *__restrict__ tw,
+                      const float2 *__restrict__ aimage, const int32_t *__restrict__ la1,
+                      const int32_t *__restrict__ la2, const double *__restrict__ layer_w,
+                      const int32_t *__restrict__ chunk_first, int nchunks,
+                      float2 *__restrict__ out) {
+  constexpr int s2 = 2 * SUB, cells = SUB * SUB;
+  constexpr int PPT = cells / 256;  // pixels per thread
+  constexpr int RSTEP = 256 / SUB;  // rows between a thread's pixels
+  __shared__ float2 sAv[AWT_NB][SUB];
+  __shared__ float2 sAu[AWT_NB][SUB];
+  __shared__ float2 stw[s2];
+  if (status_failed(A.status)) return;
+  for (int t = threadIdx.x; t < s2; t += blockDim.x) stw[t] = tw[t];
+  const int j = threadIdx.x % SUB, i0 = threadIdx.x / SUB;
+  const int S = A.S;
+  __syncthreads();
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    float2 acc[PPT];
+#pragma unroll
+    for (int t = 0; t < PPT; ++t) acc[t] = make_float2(0.f, 0.f);
+    for (int L = chunk_first[c]; L < chunk_first[c + 1]; ++L) {
+      const int rb = offsets[(int64_t)L * bpl];
+      const int re = L + 1 < layers ? offsets[(int64_t)(L + 1) * bpl]
+                                    : offsets[nbuckets - 1] + counts[nbuckets - 1];
+      float2 lac[PPT];
+#pragma unroll
+      for (int t = 0; t < PPT; ++t) lac[t] = make_float2(0.f, 0.f);
+      for (int b = rb; b < re; b += AWT_NB) {
+        const int nb = min(AWT_NB, re - b);
+        // the A-vectors of this batch: Av (times the visibility) over the cut
+        // rows, Au over the cut columns
+        for (int e = threadIdx.x; e < 2 * nb * SUB; e += blockDim.x) {
+          const int r = e / s2, rem = e - (e / s2) * s2;
+          const int axis = rem / SUB, idx = rem - (rem / SUB) * SUB;
+          const VisRec rec = A.recs[b + r];
+          const int rot = (idx + 3 * SUB / 2) & (s2 - 1);  // Ar or Br
+          const int o = axis ? rec.x0 : rec.y0;
+          const float2 *kk = ktab + (int64_t)(axis ? rec.k1 : rec.k0) * S;
+          float2 a = make_float2(0.f, 0.f);
+          for (int q = 0; q < S; ++q) cfma(a, __ldg(&kk[q]), stw[((o + q) * rot) & (s2 - 1)]);
+          if (axis) {
+            sAu[r][idx] = a;
+          } else {
+            sAv[r][idx] = cmul(a, vis[A.perm[b + r]]);
+          }
+        }
+        __syncthreads();
+        for (int r = 0; r < nb; ++r) {
+          const float2 au = sAu[r][j];
+#pragma unroll
+          for (int t = 0; t < PPT; ++t) cfma(lac[t], sAv[r][i0 + RSTEP * t], au);
+        }
+        __syncthreads();
+      }
+      // the combine's factor: aimage[a2] / aimage[a1] and the conjugate
+      // Fresnel factor of the layer's w, per pixel
+      const float2 *p2b = aimage + (int64_t)la2[L] * cells;
+      const float2 *p1b = aimage + (int64_t)la1[L] * cells;
+      const float2 w2 = awt_split(layer_w[L]);
+#pragma unroll
+      for (int t = 0; t < PPT; ++t) {
+        const int k = (i0 + RSTEP * t) * SUB + j;
+        const float2 p2 = __ldg(&p2b[k]), p1 = __ldg(&p1b[k]);
+        const float inv = 1.0f / (p1.x * p1.x + p1.y * p1.y);
+        const float rx = (p2.x * p1.x + p2.y * p1.y) * inv;
+        const float ry = (p2.y * p1.x - p2.x * p1.y) * inv;
+        const float2 g = lac[t];
+        const float gx = g.x * rx - g.y * ry, gy = g.x * ry + g.y * rx;
+        const float4 px = __ldg(&pix[k]);
+        const float hi = w2.x * px.x;
+        const float lo = fmaf(w2.x, px.x, -hi) + fmaf(w2.x, px.y, w2.y * px.x);
+        const float f = (hi - rintf(hi)) + lo;
+        float sn, cs;
+        sincospif(2.0f * f, &sn, &cs);
+        acc[t].x += gx * cs + gy * sn;
+        acc[t].y += gy * cs - gx * sn;
+      }
+    }
+    // out[c] rolled by s/2 (for an unshifted forward FFT and cg_towers_add)
+#pragma unroll
+    for (int t = 0; t < PPT; ++t) {
+      const int i = i0 + RSTEP * t;
+      const int k = i * SUB + j;
+      const float sg = __ldg(&pix[k]).z;
+      const int ir = (i + SUB / 2) & (SUB - 1), jr = (j + SUB / 2) & (SUB - 1);
+      out[(int64_t)c * cells + ir * SUB + jr] = make_float2(acc[t].x * sg, acc[t].y * sg);
+    }
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -215,6 +353,60 @@ int cg_awtowers_combine(const void *stack_c64, int layers, int s, double theta, 
       (const float2 *)stack_c64, s, theta, corr, (const float2 *)aimage_c64, nant, layer_a1,
       layer_a2, layer_w, chunk_first, nchunks, (float2 *)out_c64, d_status);
   CG_LAUNCH("AW-towers combine");
+  return CG_OK;
+}
+
+
+size_t cg_awtowers_direct_workspace_bytes(int s) {
+  if (s < 2) return 0;
+  return (((size_t)s * s * sizeof(float4) + 255) & ~(size_t)255) + 2 * (size_t)s * sizeof(float2);
+}
+
+int cg_awtowers_direct(const cg_plan *plan, const void *ktab_c64, const void *vis_c64, int s,
+                       double theta, const float *corr, const void *aimage_c64, int nant,
+                       const int32_t *layer_a1, const int32_t *layer_a2, const double *layer_w,
+                       const int32_t *chunk_first, int nchunks, void *out_c64, void *ws,
+                       size_t ws_bytes, int32_t *d_status, cg_stream_t stream) {
+  CG_REQUIRE(plan && ktab_c64 && vis_c64 && corr && aimage_c64 && layer_a1 && layer_a2 &&
+                 layer_w && chunk_first && out_c64 && d_status && nchunks >= 1 && nant >= 1,
+             "bad AW-towers direct arguments");
+  CG_REQUIRE(awtowers_direct_supported(s), "the direct AW-towers layers need s of 16, 32 or 64");
+  CG_REQUIRE(plan->mode == CG_PLAN_TILED && plan->kd.sep && plan->H == 2 * s &&
+                 plan->W == 2 * s && plan->layers >= 1,
+             "the direct AW-towers layers need a tiled plan of a separable kernel on 2s x 2s "
+             "layers");
+  if (!ws || ws_bytes < cg_awtowers_direct_workspace_bytes(s))
+    return set_error(CG_ERR_WORKSPACE, "AW-towers direct workspace too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  float4 *pix = (float4 *)ws;
+  float2 *tw = (float2 *)((char *)ws + (((size_t)s * s * sizeof(float4) + 255) & ~(size_t)255));
+  std::vector<float2> h_tw(2 * s);
+  for (int t = 0; t < 2 * s; ++t) {
+    const double a = 2.0 * M_PI * (double)t / (2.0 * s);
+    h_tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  CG_CUDA(cudaMemcpyAsync(tw, h_tw.data(), h_tw.size() * sizeof(float2), cudaMemcpyHostToDevice,
+                          st));
+  k_awt_pixels<<<(s * s + 255) / 256, 256, 0, st>>>(s, theta, corr, pix, d_status);
+  CG_LAUNCH("AW-towers pixel table");
+  if (plan->n == 0) {
+    CG_CUDA(cudaMemsetAsync(out_c64, 0, (size_t)nchunks * s * s * sizeof(float2), st));
+    return CG_OK;
+  }
+  const int bpl = plan->tpl << (2 * plan->sublog);
+  CG_REQUIRE((int64_t)bpl * plan->layers == plan->nbuckets, "unexpected plan bucket layout");
+  const TiledArgs A = tiled_args(plan);
+  const unsigned grid = (unsigned)std::min<int64_t>(nchunks, (int64_t)num_sms() * 8);
+#define CG_AWT_DIRECT(SS)                                                                      \
+  k_awtowers_direct<SS><<<grid, 256, 0, st>>>(                                                 \
+      A, bpl, plan->nbuckets, plan->layers, plan->offsets, plan->counts,                       \
+      (const float2 *)ktab_c64, (const float2 *)vis_c64, pix, tw, (const float2 *)aimage_c64,  \
+      layer_a1, layer_a2, layer_w, chunk_first, nchunks, (float2 *)out_c64)
+  if (s == 16) CG_AWT_DIRECT(16);
+  else if (s == 32) CG_AWT_DIRECT(32);
+  else CG_AWT_DIRECT(64);
+#undef CG_AWT_DIRECT
+  CG_LAUNCH("AW-towers direct layers");
   return CG_OK;
 }
 

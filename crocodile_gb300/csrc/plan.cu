@@ -342,8 +342,13 @@ __global__ void k_minmax_init(int32_t *mm) {
 }
 
 // ---------------------------------------------------------------- key compaction
-__global__ void k_key_flags(const int32_t *__restrict__ key, int64_t n, int nkeys,
-                            int32_t *__restrict__ flags, int32_t *status) {
+// The keys in use as a bitmap (one bit per possible key), the rank of a key
+// = the prefix of the words' popcounts + the bits below it in its word: the
+// key space of the tower schemes (chunks x planes x antenna pairs) runs to
+// hundreds of millions of keys for a few hundred thousand visibilities, and
+// a bit per key keeps the passes over it 32 times smaller than a flag word.
+__global__ void k_key_bits(const int32_t *__restrict__ key, int64_t n, int nkeys,
+                           uint32_t *__restrict__ bits, int32_t *status) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int k = key[i];
@@ -351,21 +356,39 @@ __global__ void k_key_flags(const int32_t *__restrict__ key, int64_t n, int nkey
     atomicAdd(&status[ST_INDEX], 1);
     return;
   }
-  flags[k] = 1;  // benign race: every writer stores 1
+  atomicOr(&bits[k >> 5], 1u << (k & 31));
+}
+
+__global__ void k_key_popc(const uint32_t *__restrict__ bits, int nw, int32_t *__restrict__ cnt) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w < nw) cnt[w] = __popc(bits[w]);
 }
 
 __global__ void k_key_rows(const int32_t *__restrict__ key, int64_t n, int nkeys,
-                           const int32_t *__restrict__ rank, int32_t *__restrict__ row) {
+                           const uint32_t *__restrict__ bits, const int32_t *__restrict__ wpre,
+                           int32_t *__restrict__ row) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int k = key[i];
-  row[i] = (k >= 0 && k < nkeys) ? rank[k] : 0;
+  if (k < 0 || k >= nkeys) {
+    row[i] = 0;
+    return;
+  }
+  const uint32_t below = (1u << (k & 31)) - 1u;
+  row[i] = wpre[k >> 5] + __popc(bits[k >> 5] & below);
 }
 
-__global__ void k_key_of_row(int nkeys, const int32_t *__restrict__ flags,
-                             const int32_t *__restrict__ rank, int32_t *__restrict__ key_of_row) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < nkeys && flags[k]) key_of_row[rank[k]] = k;
+__global__ void k_key_of_row(int nw, const uint32_t *__restrict__ bits,
+                             const int32_t *__restrict__ wpre, int32_t *__restrict__ key_of_row) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nw) return;
+  uint32_t b = bits[w];
+  int r = wpre[w];
+  while (b) {
+    const int t = __ffs(b) - 1;
+    key_of_row[r++] = (w << 5) + t;
+    b &= b - 1u;
+  }
 }
 
 // AW kernel key of every visibility: (a1 * nant + a2) * nbins + w bin - kmin, the
@@ -774,7 +797,8 @@ int cg_w_bins_fixed(const double *uvw, int64_t stride, int64_t n, double wstep, 
 }
 
 size_t cg_compact_keys_workspace_bytes(int nkeys) {
-  return (2 * (size_t)std::max(nkeys, 1) + scan_scratch_words(std::max(nkeys, 1)) + 64) * 4;
+  const int nw = (std::max(nkeys, 1) + 31) / 32;
+  return (3 * (size_t)nw + scan_scratch_words(nw) + 64) * 4;
 }
 
 int cg_compact_keys(const int32_t *key, int64_t n, int nkeys, int32_t *row, int32_t *key_of_row,
@@ -786,19 +810,22 @@ int cg_compact_keys(const int32_t *key, int64_t n, int nkeys, int32_t *row, int3
     return set_error(CG_ERR_WORKSPACE, "compact_keys needs %zu workspace bytes",
                      cg_compact_keys_workspace_bytes(nkeys));
   cudaStream_t s = (cudaStream_t)stream;
-  int32_t *flags = (int32_t *)ws, *rank = flags + nkeys, *scratch = rank + nkeys;
-  CG_CUDA(cudaMemsetAsync(flags, 0, (size_t)nkeys * 4, s));
+  const int nw = (nkeys + 31) / 32;
+  uint32_t *bits = (uint32_t *)ws;
+  int32_t *cnt = (int32_t *)(bits + nw), *wpre = cnt + nw, *scratch = wpre + nw;
+  CG_CUDA(cudaMemsetAsync(bits, 0, (size_t)nw * 4, s));
   const unsigned blocks = (unsigned)((n + 255) / 256);
-  if (n > 0) k_key_flags<<<blocks, 256, 0, s>>>(key, n, nkeys, flags, d_status);
-  CG_LAUNCH("key flags");
-  int rc = launch_scan(flags, rank, nkeys, scratch, s);
+  if (n > 0) k_key_bits<<<blocks, 256, 0, s>>>(key, n, nkeys, bits, d_status);
+  k_key_popc<<<(nw + 255) / 256, 256, 0, s>>>(bits, nw, cnt);
+  CG_LAUNCH("key bits");
+  int rc = launch_scan(cnt, wpre, nw, scratch, s);
   if (rc) return rc;
-  if (n > 0) k_key_rows<<<blocks, 256, 0, s>>>(key, n, nkeys, rank, row);
-  k_key_of_row<<<(nkeys + 255) / 256, 256, 0, s>>>(nkeys, flags, rank, key_of_row);
+  if (n > 0) k_key_rows<<<blocks, 256, 0, s>>>(key, n, nkeys, bits, wpre, row);
+  k_key_of_row<<<(nw + 255) / 256, 256, 0, s>>>(nw, bits, wpre, key_of_row);
   CG_LAUNCH("key rows");
   int32_t last[2];
-  CG_CUDA(cudaMemcpyAsync(&last[0], rank + nkeys - 1, 4, cudaMemcpyDeviceToHost, s));
-  CG_CUDA(cudaMemcpyAsync(&last[1], flags + nkeys - 1, 4, cudaMemcpyDeviceToHost, s));
+  CG_CUDA(cudaMemcpyAsync(&last[0], wpre + nw - 1, 4, cudaMemcpyDeviceToHost, s));
+  CG_CUDA(cudaMemcpyAsync(&last[1], cnt + nw - 1, 4, cudaMemcpyDeviceToHost, s));
   CG_CUDA(cudaStreamSynchronize(s));
   *h_nrows = last[0] + last[1];
   return CG_OK;

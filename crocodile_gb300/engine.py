@@ -281,7 +281,7 @@ def compact_keys(key, nkeys, status):
     key = cuda_tensor(key, torch.int32)
     n = key.shape[0]
     row = torch.empty(n, dtype=torch.int32, device="cuda")
-    kor = torch.empty(nkeys, dtype=torch.int32, device="cuda")
+    kor = torch.empty(max(1, min(n, int(nkeys))), dtype=torch.int32, device="cuda")
     nbytes = L.lib().cg_compact_keys_workspace_bytes(int(nkeys))
     ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
     nrows = ctypes.c_int32()
@@ -591,6 +591,27 @@ def awtowers_combine(stack, s, theta, corr, aimage, layer_a1, layer_a2, layer_w,
     L.call("cg_awtowers_combine", _p(stack), int(stack.shape[0]), int(s), float(theta), _p(co),
            _p(ai), int(ai.shape[0]), _p(a1), _p(a2), _p(lw), _p(cf), nchunks, _p(out),
            _p(status.t), stream())
+    return out
+
+
+def awtowers_direct(plan, ktab, vis, s, theta, corr, aimage, layer_a1, layer_a2, layer_w,
+                    chunk_first, status):
+    """awtowers_combine's output formed directly from the plan's sorted visibilities
+    (cg_awtowers_direct; s = 16, 32 or 64): no layer grids, no layer transforms."""
+    co = cuda_tensor(corr, torch.float32)
+    ai = cuda_tensor(aimage, CF)
+    a1 = cuda_tensor(layer_a1, torch.int32)
+    a2 = cuda_tensor(layer_a2, torch.int32)
+    lw = cuda_tensor(layer_w, torch.float64)
+    cf = cuda_tensor(chunk_first, torch.int32)
+    nchunks = int(cf.shape[0]) - 1
+    out = torch.empty((nchunks, s, s), dtype=CF, device="cuda")
+    ws = torch.empty(L.lib().cg_awtowers_direct_workspace_bytes(int(s)), dtype=torch.uint8,
+                     device="cuda")
+    t = plan._table(ktab, CF)
+    L.call("cg_awtowers_direct", plan.handle, _p(t), _p(vis), int(s), float(theta), _p(co),
+           _p(ai), int(ai.shape[0]), _p(a1), _p(a2), _p(lw), _p(cf), nchunks, _p(out), _p(ws),
+           ws.numel(), _p(status.t), stream())
     return out
 
 

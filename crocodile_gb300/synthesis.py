@@ -880,7 +880,8 @@ def _aw_towers_tables(N, s, aa_support, aa_over):
 
 
 def aw_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wstep, aimage,
-                      aa_support=6, aa_over=4096, precision=None, tile=32, gridder="auto"):
+                      aa_support=6, aa_over=4096, precision=None, tile=32, gridder="auto",
+                      method="auto"):
     """AW-towers imaging (examples/notebooks/awtowers.ipynb cells 17-22, without a
     phase-centre shift): visibilities binned into centred uv chunks of ``subgrid_size
     - margin`` cells (floor(u theta / C + 1/2)), w-planes of width ``wstep`` and
@@ -892,7 +893,12 @@ def aw_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wstep, ai
     w_kernel_function(l, m, w_plane)); each chunk's FFT added into the grid.  Returns
     the grid; real(ifft(grid)) / aa x aa / sum(weights) is the notebook's image.  All
     layers grid in one launch and transform in batched FFTs.  FP32 only; needs even
-    subgrid_size and margin, margin >= aa_support."""
+    subgrid_size and margin, margin >= aa_support.
+
+    method "direct" (the default for subgrid_size 16, 32 or 64) forms each layer's
+    cut image straight from its visibilities (cg_awtowers_direct: the kernel is
+    separable, so per visibility two s-point sums of its taps and an outer product)
+    instead of gridding 2s x 2s layers and transforming them ("fft")."""
     if _prec(precision) != "fp32":
         raise ValueError("aw_towers_imaging runs the FP32 path only")
     N = int(numpy.ceil(theta * lam))
@@ -928,9 +934,21 @@ def aw_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wstep, ai
     xy = numpy.column_stack([C * (ub - 0.5), C * (vb - 0.5)]) - (margin + 1) // 2
     origin = (N // 2 + xy.astype(int)).astype(numpy.int32)
     ktab, corr = _aw_towers_tables(N, s, int(aa_support), int(aa_over))
-    stack = torch.zeros((len(used), 2 * s, 2 * s), dtype=E.CF, device="cuda")
+    if method not in ("auto", "direct", "fft"):
+        raise ValueError("method must be 'auto', 'direct' or 'fft'")
+    direct = method == "direct" or (method == "auto" and s in (16, 32, 64))
+    if direct and s not in (16, 32, 64):
+        raise ValueError("the direct AW-towers layers need subgrid_size 16, 32 or 64")
     plan = E.Plan(rel, s / theta, (2 * s, 2 * s), ktab, None, status=st,
                   layers=(len(used), row), tile=tile)
+    if direct:
+        sub = E.awtowers_direct(plan, ktab, vis_t, s, theta, corr, ai, bl // nant, bl % nant,
+                                plane * float(wstep), chunk_first, st)
+        E.fft_raw(sub, False)
+        E.towers_add(sub, origin, grid)
+        st.check()
+        return _host(grid, like=uvw)
+    stack = torch.zeros((len(used), 2 * s, 2 * s), dtype=E.CF, device="cuda")
     tiles = len(used) * (-(-2 * s // plan.info()["tile"])) ** 2
     if gridder == "sparse" or (gridder == "auto" and n < 16 * tiles):
         plan.grid_sparse(ktab, vis_t, stack)

@@ -315,10 +315,11 @@ int cg_scale_image(float *image, int64_t count, const float *d_scale,
                    cg_stream_t stream);
 
 /* Distinct keys: for keys in [0, nkeys), row[i] = rank of key[i] among the
- * distinct keys present (ascending), key_of_row[r] = the r-th distinct key,
- * *h_nrows (host) = their number; synchronises the stream.  Replaces the
- * kernel cache lookup of w_cache_imaging (synthesis.py:788, 794) with one
- * table row per distinct cache key. */
+ * distinct keys present (ascending), key_of_row[r] = the r-th distinct key
+ * (room for min(n, nkeys) entries), *h_nrows (host) = their number;
+ * synchronises the stream.  The keys in use are a bitmap (nkeys / 8 bytes
+ * of the workspace).  Replaces the kernel cache lookup of w_cache_imaging
+ * (synthesis.py:788, 794) with one table row per distinct cache key. */
 size_t cg_compact_keys_workspace_bytes(int nkeys);
 int cg_compact_keys(const int32_t *key, int64_t n, int nkeys, int32_t *row,
                     int32_t *key_of_row, int32_t *h_nrows, void *workspace,
@@ -448,6 +449,20 @@ int cg_awtowers_combine(const void *stack_c64, int layers, int s, double theta,
                         const int32_t *layer_a1, const int32_t *layer_a2,
                         const double *layer_w, const int32_t *chunk_first, int nchunks,
                         void *out_c64, int32_t *d_status, cg_stream_t stream);
+/* The same out[] without the 2s x 2s layer grids and their transforms, for
+ * s = 16, 32 or 64: the anti-aliasing kernel being separable, the unshifted
+ * inverse transform of a layer at the cut pixel (Ar, Br) is the sum over its
+ * visibilities of vis * Av(Ar) * Au(Br), Av / Au the visibility's taps times
+ * exp(+2 pi i (origin + tap) Ar / 2s) summed; plan is the layered tiled plan
+ * of the gridding (lam = s / theta, 2s x 2s layers, separable ktab) whose
+ * sorted records give each layer's visibilities.  ws: at least
+ * cg_awtowers_direct_workspace_bytes(s) bytes of device memory. */
+size_t cg_awtowers_direct_workspace_bytes(int s);
+int cg_awtowers_direct(const cg_plan *plan, const void *ktab_c64, const void *vis_c64, int s,
+                       double theta, const float *corr, const void *aimage_c64, int nant,
+                       const int32_t *layer_a1, const int32_t *layer_a2, const double *layer_w,
+                       const int32_t *chunk_first, int nchunks, void *out_c64, void *ws,
+                       size_t ws_bytes, int32_t *d_status, cg_stream_t stream);
 
 /* ---------------------------------------------------------------- ingest
  * Visibility blocks as the reference's HDF5 files hold them (a vis/[a1]/[a2]
