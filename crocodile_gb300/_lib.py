@@ -81,9 +81,9 @@ SIGNATURES = {
                                 P, P, P, P, P]),
     "cg_awtowers_combine": (c_int, [P, c_int, c_int, c_double, P, P, c_int, P, P, P, P, c_int, P,
                                     P, P]),
-    "cg_awtowers_direct_workspace_bytes": (c_size_t, [c_int]),
-    "cg_awtowers_direct": (c_int, [P, P, P, c_int, c_double, P, P, c_int, P, P, P, P, c_int, P, P,
-                                   c_size_t, P, P]),
+    "cg_awtowers_direct_workspace_bytes": (c_size_t, [c_int, c_int, c_int]),
+    "cg_awtowers_direct": (c_int, [P, P, P, c_int, c_double, P, P, c_int, P, P, P, P, c_int, P,
+                                   c_int, P, P, c_size_t, P, P]),
     "cg_ingest_blocks": (c_int, [P, c_int, P, P, P, P, P, P, c_int, P, P, P, P, P, c_int, P, P]),
     "cg_szetan_gridding": (c_int, [P, c_int, c_double, c_int, P, P, c_int, P, P]),
     "cg_szetan_correction_workspace_bytes": (c_size_t, [c_int]),

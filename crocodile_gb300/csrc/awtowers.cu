@@ -186,7 +186,8 @@ __global__ void k_awtowers_combine(const float2 *__restrict__ stack, int s, doub
 // factor) into its chunk sums, which leave times corr x sign / (2s)^2 rolled
 // as k_awtowers_combine writes them.
 
-constexpr int AWT_NB = 32;  // visibilities per shared-memory batch
+constexpr int AWT_NB = 32;    // visibilities per shared-memory batch
+constexpr int AWT_MAXS = 16;  // largest kernel support of the direct form
 
 bool awtowers_direct_supported(int s) { return s == 16 || s == 32 || s == 64; }
 
@@ -208,14 +209,42 @@ __global__ void k_awt_pixels(int s, double theta, const float *__restrict__ corr
   pix[k] = make_float4(ph_h, ph_l, sg, 0.f);
 }
 
+// per w-plane and cut pixel the conjugate Fresnel factor exp(-2 pi i w ph)
+// (the phase formed as k_awtowers_combine forms it), and per antenna and
+// pixel conj(aimage) / |aimage|^2: the per-layer factor becomes two products
+__global__ void k_awt_tables(int cells, const float4 *__restrict__ pix,
+                             const double *__restrict__ plane_w, int nplanes,
+                             const float2 *__restrict__ aimage, int nant,
+                             float2 *__restrict__ fres, float2 *__restrict__ ainv) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nf = (int64_t)nplanes * cells;
+  if (e < nf) {
+    const int pl = (int)(e / cells), k = (int)(e - (int64_t)pl * cells);
+    const float4 px = pix[k];
+    const float2 w2 = awt_split(plane_w[pl]);
+    const float hi = w2.x * px.x;
+    const float lo = fmaf(w2.x, px.x, -hi) + fmaf(w2.x, px.y, w2.y * px.x);
+    const float f = (hi - rintf(hi)) + lo;
+    float sn, cs;
+    sincospif(2.0f * f, &sn, &cs);
+    fres[e] = make_float2(cs, -sn);
+  } else if (e < nf + (int64_t)nant * cells) {
+    const int64_t a = e - nf;
+    const float2 p = aimage[a];
+    const float inv = 1.0f / (p.x * p.x + p.y * p.y);
+    ainv[a] = make_float2(p.x * inv, -p.y * inv);
+  }
+}
+
 template <int SUB>
 __global__ void __launch_bounds__(256)
     k_awtowers_direct(TiledArgs A, int bpl, int nbuckets, int layers,
                       const int32_t *__restrict__ offsets, const int32_t *__restrict__ counts,
                       const float2 *__restrict__ ktab, const float2 *__restrict__ vis,
                       const float4 *__restrict__ pix, const float2 *__restrict__ tw,
-                      const float2 *__restrict__ aimage, const int32_t *__restrict__ la1,
-                      const int32_t *__restrict__ la2, const double *__restrict__ layer_w,
+                      const float2 *__restrict__ aimage, const float2 *__restrict__ ainv,
+                      const float2 *__restrict__ fres, const int32_t *__restrict__ la1,
+                      const int32_t *__restrict__ la2, const int32_t *__restrict__ lplane,
                       const int32_t *__restrict__ chunk_first, int nchunks,
                       float2 *__restrict__ out) {
   constexpr int s2 = 2 * SUB, cells = SUB * SUB;
@@ -224,6 +253,9 @@ __global__ void __launch_bounds__(256)
   __shared__ float2 sAv[AWT_NB][SUB];
   __shared__ float2 sAu[AWT_NB][SUB];
   __shared__ float2 stw[s2];
+  __shared__ float2 sTap[AWT_NB][2][AWT_MAXS];
+  __shared__ float2 sVis[AWT_NB];
+  __shared__ int2 sOrg[AWT_NB];
   if (status_failed(A.status)) return;
   for (int t = threadIdx.x; t < s2; t += blockDim.x) stw[t] = tw[t];
   const int j = threadIdx.x % SUB, i0 = threadIdx.x / SUB;
@@ -237,26 +269,44 @@ __global__ void __launch_bounds__(256)
       const int rb = offsets[(int64_t)L * bpl];
       const int re = L + 1 < layers ? offsets[(int64_t)(L + 1) * bpl]
                                     : offsets[nbuckets - 1] + counts[nbuckets - 1];
+      // the layer's antennas and plane, loaded before its batches
+      const int pa1 = la1[L], pa2 = la2[L], pl = lplane[L];
       float2 lac[PPT];
 #pragma unroll
       for (int t = 0; t < PPT; ++t) lac[t] = make_float2(0.f, 0.f);
       for (int b = rb; b < re; b += AWT_NB) {
         const int nb = min(AWT_NB, re - b);
+        // stage the batch: footprints, visibilities and both tap rows, one
+        // round of independent loads
+        for (int e = threadIdx.x; e < nb * (2 + 2 * AWT_MAXS); e += blockDim.x) {
+          const int r = e / (2 + 2 * AWT_MAXS), q = e - r * (2 + 2 * AWT_MAXS);
+          if (q == 0) {
+            const VisRec rec = A.recs[b + r];
+            sOrg[r] = make_int2(rec.x0, rec.y0);
+          } else if (q == 1) {
+            sVis[r] = vis[A.perm[b + r]];
+          } else {
+            const int t = q - 2, axis = t / AWT_MAXS, tap = t - axis * AWT_MAXS;
+            if (tap < S) {
+              const VisRec rec = A.recs[b + r];
+              sTap[r][axis][tap] = __ldg(&ktab[(int64_t)(axis ? rec.k1 : rec.k0) * S + tap]);
+            }
+          }
+        }
+        __syncthreads();
         // the A-vectors of this batch: Av (times the visibility) over the cut
         // rows, Au over the cut columns
         for (int e = threadIdx.x; e < 2 * nb * SUB; e += blockDim.x) {
           const int r = e / s2, rem = e - (e / s2) * s2;
           const int axis = rem / SUB, idx = rem - (rem / SUB) * SUB;
-          const VisRec rec = A.recs[b + r];
           const int rot = (idx + 3 * SUB / 2) & (s2 - 1);  // Ar or Br
-          const int o = axis ? rec.x0 : rec.y0;
-          const float2 *kk = ktab + (int64_t)(axis ? rec.k1 : rec.k0) * S;
+          const int o = axis ? sOrg[r].x : sOrg[r].y;
           float2 a = make_float2(0.f, 0.f);
-          for (int q = 0; q < S; ++q) cfma(a, __ldg(&kk[q]), stw[((o + q) * rot) & (s2 - 1)]);
+          for (int q = 0; q < S; ++q) cfma(a, sTap[r][axis][q], stw[((o + q) * rot) & (s2 - 1)]);
           if (axis) {
             sAu[r][idx] = a;
           } else {
-            sAv[r][idx] = cmul(a, vis[A.perm[b + r]]);
+            sAv[r][idx] = cmul(a, sVis[r]);
           }
         }
         __syncthreads();
@@ -267,28 +317,16 @@ __global__ void __launch_bounds__(256)
         }
         __syncthreads();
       }
-      // the combine's factor: aimage[a2] / aimage[a1] and the conjugate
-      // Fresnel factor of the layer's w, per pixel
-      const float2 *p2b = aimage + (int64_t)la2[L] * cells;
-      const float2 *p1b = aimage + (int64_t)la1[L] * cells;
-      const float2 w2 = awt_split(layer_w[L]);
+      // the combine's factor: aimage[a2] / aimage[a1] times the conjugate
+      // Fresnel factor of the layer's plane (tables)
+      const float2 *p2b = aimage + (int64_t)pa2 * cells;
+      const float2 *i1b = ainv + (int64_t)pa1 * cells;
+      const float2 *fb = fres + (int64_t)pl * cells;
 #pragma unroll
       for (int t = 0; t < PPT; ++t) {
         const int k = (i0 + RSTEP * t) * SUB + j;
-        const float2 p2 = __ldg(&p2b[k]), p1 = __ldg(&p1b[k]);
-        const float inv = 1.0f / (p1.x * p1.x + p1.y * p1.y);
-        const float rx = (p2.x * p1.x + p2.y * p1.y) * inv;
-        const float ry = (p2.y * p1.x - p2.x * p1.y) * inv;
-        const float2 g = lac[t];
-        const float gx = g.x * rx - g.y * ry, gy = g.x * ry + g.y * rx;
-        const float4 px = __ldg(&pix[k]);
-        const float hi = w2.x * px.x;
-        const float lo = fmaf(w2.x, px.x, -hi) + fmaf(w2.x, px.y, w2.y * px.x);
-        const float f = (hi - rintf(hi)) + lo;
-        float sn, cs;
-        sincospif(2.0f * f, &sn, &cs);
-        acc[t].x += gx * cs + gy * sn;
-        acc[t].y += gy * cs - gx * sn;
+        const float2 r = cmul(__ldg(&p2b[k]), __ldg(&i1b[k]));
+        cfma(acc[t], cmul(lac[t], r), __ldg(&fb[k]));
       }
     }
     // out[c] rolled by s/2 (for an unshifted forward FFT and cg_towers_add)
@@ -357,29 +395,46 @@ int cg_awtowers_combine(const void *stack_c64, int layers, int s, double theta, 
 }
 
 
-size_t cg_awtowers_direct_workspace_bytes(int s) {
-  if (s < 2) return 0;
-  return (((size_t)s * s * sizeof(float4) + 255) & ~(size_t)255) + 2 * (size_t)s * sizeof(float2);
+// workspace: the pixel table, the twiddles, the Fresnel table, the A-image reciprocals
+static size_t awt_ws_part(size_t b) { return (b + 255) & ~(size_t)255; }
+
+size_t cg_awtowers_direct_workspace_bytes(int s, int nant, int nplanes) {
+  if (s < 2 || nant < 1 || nplanes < 1) return 0;
+  const size_t cells = (size_t)s * s;
+  return awt_ws_part(cells * sizeof(float4)) + awt_ws_part(2 * (size_t)s * sizeof(float2)) +
+         awt_ws_part((size_t)nplanes * cells * sizeof(float2)) +
+         awt_ws_part((size_t)nant * cells * sizeof(float2));
 }
 
 int cg_awtowers_direct(const cg_plan *plan, const void *ktab_c64, const void *vis_c64, int s,
                        double theta, const float *corr, const void *aimage_c64, int nant,
-                       const int32_t *layer_a1, const int32_t *layer_a2, const double *layer_w,
+                       const int32_t *layer_a1, const int32_t *layer_a2,
+                       const int32_t *layer_plane, const double *plane_w, int nplanes,
                        const int32_t *chunk_first, int nchunks, void *out_c64, void *ws,
                        size_t ws_bytes, int32_t *d_status, cg_stream_t stream) {
   CG_REQUIRE(plan && ktab_c64 && vis_c64 && corr && aimage_c64 && layer_a1 && layer_a2 &&
-                 layer_w && chunk_first && out_c64 && d_status && nchunks >= 1 && nant >= 1,
+                 layer_plane && plane_w && chunk_first && out_c64 && d_status && nchunks >= 1 &&
+                 nant >= 1 && nplanes >= 1,
              "bad AW-towers direct arguments");
   CG_REQUIRE(awtowers_direct_supported(s), "the direct AW-towers layers need s of 16, 32 or 64");
+  CG_REQUIRE(plan->kd.S >= 1 && plan->kd.S <= AWT_MAXS,
+             "the direct AW-towers layers take kernel supports up to %d", AWT_MAXS);
   CG_REQUIRE(plan->mode == CG_PLAN_TILED && plan->kd.sep && plan->H == 2 * s &&
                  plan->W == 2 * s && plan->layers >= 1,
              "the direct AW-towers layers need a tiled plan of a separable kernel on 2s x 2s "
              "layers");
-  if (!ws || ws_bytes < cg_awtowers_direct_workspace_bytes(s))
+  if (!ws || ws_bytes < cg_awtowers_direct_workspace_bytes(s, nant, nplanes))
     return set_error(CG_ERR_WORKSPACE, "AW-towers direct workspace too small");
   cudaStream_t st = (cudaStream_t)stream;
-  float4 *pix = (float4 *)ws;
-  float2 *tw = (float2 *)((char *)ws + (((size_t)s * s * sizeof(float4) + 255) & ~(size_t)255));
+  const size_t cells = (size_t)s * s;
+  char *w = (char *)ws;
+  float4 *pix = (float4 *)w;
+  w += awt_ws_part(cells * sizeof(float4));
+  float2 *tw = (float2 *)w;
+  w += awt_ws_part(2 * (size_t)s * sizeof(float2));
+  float2 *fres = (float2 *)w;
+  w += awt_ws_part((size_t)nplanes * cells * sizeof(float2));
+  float2 *ainv = (float2 *)w;
   std::vector<float2> h_tw(2 * s);
   for (int t = 0; t < 2 * s; ++t) {
     const double a = 2.0 * M_PI * (double)t / (2.0 * s);
@@ -387,10 +442,13 @@ int cg_awtowers_direct(const cg_plan *plan, const void *ktab_c64, const void *vi
   }
   CG_CUDA(cudaMemcpyAsync(tw, h_tw.data(), h_tw.size() * sizeof(float2), cudaMemcpyHostToDevice,
                           st));
-  k_awt_pixels<<<(s * s + 255) / 256, 256, 0, st>>>(s, theta, corr, pix, d_status);
-  CG_LAUNCH("AW-towers pixel table");
+  k_awt_pixels<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(s, theta, corr, pix, d_status);
+  const int64_t nt = (int64_t)(nplanes + nant) * (int64_t)cells;
+  k_awt_tables<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(
+      (int)cells, pix, plane_w, nplanes, (const float2 *)aimage_c64, nant, fres, ainv);
+  CG_LAUNCH("AW-towers pixel, Fresnel and A-image tables");
   if (plan->n == 0) {
-    CG_CUDA(cudaMemsetAsync(out_c64, 0, (size_t)nchunks * s * s * sizeof(float2), st));
+    CG_CUDA(cudaMemsetAsync(out_c64, 0, (size_t)nchunks * cells * sizeof(float2), st));
     return CG_OK;
   }
   const int bpl = plan->tpl << (2 * plan->sublog);
@@ -401,7 +459,7 @@ int cg_awtowers_direct(const cg_plan *plan, const void *ktab_c64, const void *vi
   k_awtowers_direct<SS><<<grid, 256, 0, st>>>(                                                 \
       A, bpl, plan->nbuckets, plan->layers, plan->offsets, plan->counts,                       \
       (const float2 *)ktab_c64, (const float2 *)vis_c64, pix, tw, (const float2 *)aimage_c64,  \
-      layer_a1, layer_a2, layer_w, chunk_first, nchunks, (float2 *)out_c64)
+      ainv, fres, layer_a1, layer_a2, layer_plane, chunk_first, nchunks, (float2 *)out_c64)
   if (s == 16) CG_AWT_DIRECT(16);
   else if (s == 32) CG_AWT_DIRECT(32);
   else CG_AWT_DIRECT(64);

@@ -359,19 +359,22 @@ __global__ void k_rcT_split(const double2 *__restrict__ fs, int npair, int xM, i
 // out[o][r][k] (k < yP) = sum over j < noff of the window of in[o][j][r][.]
 // placed at offset offs[j]: position p (|p| within xMxN_yP / 2) of the
 // periodic extension of the xM_yP samples, times m, lands at (p + off) mod yP.
-// Grid: x over k, y striding over the rows o * inner + r.
-template <class P>
+// Grid-stride over the outputs; I is the index type (32-bit while the
+// outputs fit, its divisions being a fraction of the 64-bit ones).
+template <class P, typename I>
 __global__ void k_rcT_scatter(const typename P::S *__restrict__ in, int outer, int noff,
                               int inner, int xM_yP, int xMxN_yP, int yP,
                               const int32_t *__restrict__ offs,
                               const typename P::WS *__restrict__ m,
                               typename P::S *__restrict__ out) {
+  const I total = (I)outer * (I)inner * (I)yP;
   const int half = xMxN_yP / 2;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= yP) return;
-  const int nrow = outer * inner;
-  for (int row = blockIdx.y; row < nrow; row += gridDim.y) {
-    const int o = row / inner, r = row - (row / inner) * inner;
+  for (I e = (I)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (I)gridDim.x * blockDim.x) {
+    const int k = (int)(e % (I)yP);
+    const I orow = e / (I)yP;
+    const int r = (int)(orow % (I)inner);
+    const I o = orow / (I)inner;
     typename P::V v = P::zero();
     for (int j = 0; j < noff; ++j) {
       // k, offs[j] in [0, yP): the signed distance in [-yP/2, yP/2)
@@ -384,13 +387,8 @@ __global__ void k_rcT_scatter(const typename P::S *__restrict__ in, int outer, i
                   P::ld(in[(((size_t)o * noff + j) * inner + r) * xM_yP +
                            (p < 0 ? p + xM_yP : p)]));
     }
-    out[(size_t)row * yP + k] = P::st(v);
+    out[e] = P::st(v);
   }
-}
-
-// launch shape of k_rcT_scatter
-inline dim3 scatter_grid(int nrow, int yP) {
-  return dim3((yP + 255) / 256, std::min(std::max(nrow, 1), 65535));
 }
 
 // B[t][i0][k0]: rows (i0, a0) of acc [n0][xM_yN][yP] cropped to the yB facet
@@ -656,6 +654,21 @@ bool use_df(const cg_recombine *h) {
 
 inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+inline unsigned grid_for(size_t n);
+
+template <class P>
+void launch_scatter(const typename P::S *in, int outer, int noff, int inner, int xM_yP,
+                    int xMxN_yP, int yP, const int32_t *offs, const typename P::WS *m,
+                    typename P::S *out, cudaStream_t st) {
+  const size_t total = (size_t)outer * inner * yP;
+  if (total < ((size_t)1 << 31))
+    k_rcT_scatter<P, uint32_t><<<grid_for(total), 256, 0, st>>>(in, outer, noff, inner, xM_yP,
+                                                                xMxN_yP, yP, offs, m, out);
+  else
+    k_rcT_scatter<P, size_t><<<grid_for(total), 256, 0, st>>>(in, outer, noff, inner, xM_yP,
+                                                              xMxN_yP, yP, offs, m, out);
+}
+
 // grid-stride launches: enough 256-thread blocks to fill the GPU a few times
 inline unsigned grid_for(size_t n) {
   const size_t want = (n + 255) / 256;
@@ -701,16 +714,14 @@ int subgrids_to_facet(cg_recombine *h, const void *fs, int centred, int n0, int 
       (const double2 *)fs, n0 * n1, xM, xM_yN, xM_yP, fo0, fo1, Tab<P>::Fn(h), centred, A);
   CG_LAUNCH("recombine split subgrids");
   if ((rc = rows_fft(h, A, n0 * n1 * xM_yN, xM_yP, CUFFT_INVERSE, st))) return rc;
-  k_rcT_scatter<P><<<scatter_grid(n0 * xM_yN, yP), 256, 0, st>>>(
-      A, n0, n1, xM_yN, xM_yP, h->xMxN_yP, yP, offs1, Tab<P>::m(h), acc);
+  launch_scatter<P>(A, n0, n1, xM_yN, xM_yP, h->xMxN_yP, yP, offs1, Tab<P>::m(h), acc, st);
   CG_LAUNCH("recombine subgrid windows (axis 1)");
   if ((rc = rows_fft(h, acc, n0 * xM_yN, yP, CUFFT_FORWARD, st))) return rc;
   k_rcT_crop_T_pad<P><<<dim3((xM_yP + 31) / 32, (yB + 31) / 32, n0), dim3(32, 8), 0, st>>>(
       acc, n0, xM_yN, yP, yB, xM_yP, B);
   CG_LAUNCH("recombine crop to the facet (axis 1)");
   if ((rc = rows_fft(h, B, yB * n0, xM_yP, CUFFT_INVERSE, st))) return rc;
-  k_rcT_scatter<P><<<scatter_grid(yB, yP), 256, 0, st>>>(
-      B, yB, n0, 1, xM_yP, h->xMxN_yP, yP, offs0, Tab<P>::m(h), acc2);
+  launch_scatter<P>(B, yB, n0, 1, xM_yP, h->xMxN_yP, yP, offs0, Tab<P>::m(h), acc2, st);
   CG_LAUNCH("recombine subgrid windows (axis 0)");
   if ((rc = rows_fft(h, acc2, yB, yP, CUFFT_FORWARD, st))) return rc;
   k_rcT_final<P><<<dim3((yB + 31) / 32, (yB + 31) / 32), dim3(32, 8), 0, st>>>(
@@ -819,8 +830,7 @@ int subgrids_to_facet_df(cg_recombine *h, const void *fs, int centred, int n0, i
   // the yP transforms (ScatterSrc) the 2048-point kernel's occupancy leaves
   // the offset loop's dependent loads exposed (measured 193 us against 158
   // for the pair on the 8192 / 1280 / 512 set)
-  k_rcT_scatter<PDF><<<scatter_grid(n0 * xM_yN, yP), 256, 0, st>>>(
-      A, n0, n1, xM_yN, xM_yP, xMxN, yP, offs1, h->d_m2, acc);
+  launch_scatter<PDF>(A, n0, n1, xM_yN, xM_yP, xMxN, yP, offs1, h->d_m2, acc, st);
   CG_LAUNCH("recombine subgrid windows (axis 1)");
   if ((rc = dfft_rows_df(acc, (int64_t)n0 * xM_yN, yP, 0, st))) return rc;
   k_rcT_crop_T_pad<PDF><<<dim3((xM_yP + 31) / 32, (yB + 31) / 32, n0), dim3(32, 8), 0, st>>>(

@@ -594,24 +594,27 @@ def awtowers_combine(stack, s, theta, corr, aimage, layer_a1, layer_a2, layer_w,
     return out
 
 
-def awtowers_direct(plan, ktab, vis, s, theta, corr, aimage, layer_a1, layer_a2, layer_w,
-                    chunk_first, status):
+def awtowers_direct(plan, ktab, vis, s, theta, corr, aimage, layer_a1, layer_a2, layer_plane,
+                    plane_w, chunk_first, status):
     """awtowers_combine's output formed directly from the plan's sorted visibilities
-    (cg_awtowers_direct; s = 16, 32 or 64): no layer grids, no layer transforms."""
+    (cg_awtowers_direct; s = 16, 32 or 64): no layer grids, no layer transforms.
+    layer_plane: each layer's index into plane_w, the w of each plane."""
     co = cuda_tensor(corr, torch.float32)
     ai = cuda_tensor(aimage, CF)
     a1 = cuda_tensor(layer_a1, torch.int32)
     a2 = cuda_tensor(layer_a2, torch.int32)
-    lw = cuda_tensor(layer_w, torch.float64)
+    lp = cuda_tensor(layer_plane, torch.int32)
+    pw = cuda_tensor(plane_w, torch.float64)
     cf = cuda_tensor(chunk_first, torch.int32)
     nchunks = int(cf.shape[0]) - 1
+    nant, nplanes = int(ai.shape[0]), int(pw.shape[0])
     out = torch.empty((nchunks, s, s), dtype=CF, device="cuda")
-    ws = torch.empty(L.lib().cg_awtowers_direct_workspace_bytes(int(s)), dtype=torch.uint8,
-                     device="cuda")
+    ws = torch.empty(L.lib().cg_awtowers_direct_workspace_bytes(int(s), nant, nplanes),
+                     dtype=torch.uint8, device="cuda")
     t = plan._table(ktab, CF)
     L.call("cg_awtowers_direct", plan.handle, _p(t), _p(vis), int(s), float(theta), _p(co),
-           _p(ai), int(ai.shape[0]), _p(a1), _p(a2), _p(lw), _p(cf), nchunks, _p(out), _p(ws),
-           ws.numel(), _p(status.t), stream())
+           _p(ai), nant, _p(a1), _p(a2), _p(lp), _p(pw), nplanes, _p(cf), nchunks, _p(out),
+           _p(ws), ws.numel(), _p(status.t), stream())
     return out
 
 

@@ -905,6 +905,11 @@ def aw_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wstep, ai
     s, C = int(subgrid_size), int(subgrid_size) - int(margin)
     if C < 1 or margin < aa_support or s % 2 or margin % 2:
         raise ValueError("need even subgrid_size and margin, aa_support <= margin < subgrid_size")
+    if method not in ("auto", "direct", "fft"):
+        raise ValueError("method must be 'auto', 'direct' or 'fft'")
+    direct = method == "direct" or (method == "auto" and s in (16, 32, 64))
+    if direct and s not in (16, 32, 64):
+        raise ValueError("the direct AW-towers layers need subgrid_size 16, 32 or 64")
     grid = torch.zeros((N, N), dtype=E.CF, device="cuda")
     n = _nrows(uvw)
     if n == 0:
@@ -927,23 +932,23 @@ def aw_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wstep, ai
     used = used.cpu().numpy().astype(numpy.int64)
     bl, rest = used % (nant * nant), used // (nant * nant)
     plane = rest % nwp + wpmin
-    chunk, first = numpy.unique(rest // nwp, return_index=True)
+    # used is ascending, so each chunk's layers are one run
+    ch = rest // nwp
+    first = numpy.flatnonzero(numpy.r_[True, ch[1:] != ch[:-1]])
+    chunk = ch[first]
     chunk_first = numpy.append(first, len(used)).astype(numpy.int32)
     ub, vb = chunk % nub + ubmin, chunk // nub + vbmin
     # the notebook's sub-grid corner: xy_min = C (ub - 1/2) - (margin + 1) // 2
     xy = numpy.column_stack([C * (ub - 0.5), C * (vb - 0.5)]) - (margin + 1) // 2
     origin = (N // 2 + xy.astype(int)).astype(numpy.int32)
     ktab, corr = _aw_towers_tables(N, s, int(aa_support), int(aa_over))
-    if method not in ("auto", "direct", "fft"):
-        raise ValueError("method must be 'auto', 'direct' or 'fft'")
-    direct = method == "direct" or (method == "auto" and s in (16, 32, 64))
-    if direct and s not in (16, 32, 64):
-        raise ValueError("the direct AW-towers layers need subgrid_size 16, 32 or 64")
     plan = E.Plan(rel, s / theta, (2 * s, 2 * s), ktab, None, status=st,
                   layers=(len(used), row), tile=tile)
     if direct:
+        # plane index rest % nwp into the planes wpmin .. wpmax
         sub = E.awtowers_direct(plan, ktab, vis_t, s, theta, corr, ai, bl // nant, bl % nant,
-                                plane * float(wstep), chunk_first, st)
+                                (rest % nwp).astype(numpy.int32),
+                                (numpy.arange(nwp) + wpmin) * float(wstep), chunk_first, st)
         E.fft_raw(sub, False)
         E.towers_add(sub, origin, grid)
         st.check()

@@ -454,13 +454,17 @@ int cg_awtowers_combine(const void *stack_c64, int layers, int s, double theta,
  * inverse transform of a layer at the cut pixel (Ar, Br) is the sum over its
  * visibilities of vis * Av(Ar) * Au(Br), Av / Au the visibility's taps times
  * exp(+2 pi i (origin + tap) Ar / 2s) summed; plan is the layered tiled plan
- * of the gridding (lam = s / theta, 2s x 2s layers, separable ktab) whose
- * sorted records give each layer's visibilities.  ws: at least
- * cg_awtowers_direct_workspace_bytes(s) bytes of device memory. */
-size_t cg_awtowers_direct_workspace_bytes(int s);
+ * of the gridding (lam = s / theta, 2s x 2s layers, separable ktab, support
+ * <= 16) whose sorted records give each layer's visibilities.  Layer L lies
+ * in w-plane layer_plane[L] of nplanes, whose w is plane_w[plane] (the
+ * Fresnel factor is tabulated per plane, aimage's reciprocal per antenna).
+ * ws: at least cg_awtowers_direct_workspace_bytes(s, nant, nplanes) bytes of
+ * device memory. */
+size_t cg_awtowers_direct_workspace_bytes(int s, int nant, int nplanes);
 int cg_awtowers_direct(const cg_plan *plan, const void *ktab_c64, const void *vis_c64, int s,
                        double theta, const float *corr, const void *aimage_c64, int nant,
-                       const int32_t *layer_a1, const int32_t *layer_a2, const double *layer_w,
+                       const int32_t *layer_a1, const int32_t *layer_a2,
+                       const int32_t *layer_plane, const double *plane_w, int nplanes,
                        const int32_t *chunk_first, int nchunks, void *out_c64, void *ws,
                        size_t ws_bytes, int32_t *d_status, cg_stream_t stream);
 
