@@ -94,6 +94,8 @@ SIGNATURES = {
     "cg_recombine_sizes": (c_int, [P, P]),
     "cg_recombine_windows": (c_int, [P, P, P, P]),
     "cg_recombine_workspace_bytes": (c_size_t, [P, c_int, c_int]),
+    "cg_recombine_facet_add": (c_int, [P, P, c_int, P, c_int, P, c_int, c_int, c_int, P, c_int,
+                                       P, c_size_t, P, P]),
     "cg_recombine_facet_to_subgrids": (c_int, [P, P, c_int, P, c_int, P, c_int, P, c_int, P,
                                                c_size_t, P, P]),
     "cg_recombine_add_facet": (c_int, [P, P, c_int, c_int, c_int, c_int, P, P]),

@@ -366,11 +366,9 @@ def measure_recombine(steps=3, nfacets=None):
     o = E.cuda_tensor(numpy.asarray(so), torch.int32)
     ns = len(so)
     approx = torch.zeros((ns, ns, xM, xM), dtype=E.CD, device="cuda")
-    nm = torch.empty((ns, ns, rc.xM_yN_size, rc.xM_yN_size), dtype=E.CD, device="cuda")
 
     def per_facet(j0, j1):
-        rc.facet_to_subgrids(facets[j0, j1], o, o, out=nm, check=False)
-        rc.add_facet(approx, nm, fo[j0], fo[j1])
+        rc.facet_add(approx, facets[j0, j1], o, o, fo[j0], fo[j1], check=False)
 
     def step():
         approx.zero_()
@@ -406,9 +404,10 @@ def measure_recombine(steps=3, nfacets=None):
             "stage_gb_per_facet": nbytes / 1e9,
             "stage_gb_s": nbytes / (ms_facet * 1e-3) / 1e9,
             "subgrids_to_facets_ms": ms_split, "subgrids_to_facet_ms_per_facet": ms_split_facet,
-            "note": "ms: facets -> subgrids (per facet: 4 row-transform launches with the "
-                    "prepare, window and crop steps in their loads and stores, 1 transpose "
-                    "kernel and the sum into the subgrids; stage arrays and FFTs in "
+            "note": "ms: facets -> subgrids (per facet, cg_recombine_facet_add: 4 "
+                    "row-transform launches with the prepare, window, crop and sum-into-the-"
+                    "subgrids steps in their loads and stores, 1 transpose kernel; "
+                    "stage arrays and FFTs in "
                     "double-float arithmetic on the FP32 units, complex128 in and out; then "
                     "the subgrid sums' 512^2 inverse FFTs, double-float too); "
                     "fp64_fft_tflop_s counts 5 n log2 n per transform; "

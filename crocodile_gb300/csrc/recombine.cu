@@ -538,6 +538,39 @@ struct IoWindowCrop {
   }
 };
 
+// the window in; the crop times Fn (k_rc_crop_T) and the sum into the
+// subgrids (k_rc_add_facet) out: element (a0, a1) of subgrid pair's
+// contribution lands at (off + f0 + fo0, off + f1 + fo1) mod xM, f the signed
+// frequency of the raw index and off = xM/2 for centred subgrids (0 raw,
+// where the contribution is also divided by xM^2) -- the same FP64 values
+// and additions as k_rc_crop_T followed by k_rc_add_facet
+struct IoWindowCropAdd {
+  WindowSrc w;
+  const float2 *Fn;
+  double2 *sub;
+  int xM_yN, xM, fo0, fo1, centred;
+  __device__ cdf ld(int64_t row, int i) const { return w.ld(row, i); }
+  __device__ void st(int64_t row, int i, const cdf &v) const {
+    const int a0 = uncrop(i, xM_yN, w.xM_yP);
+    if (a0 < 0) return;
+    const int pair = (int)row / xM_yN, a1 = (int)row - ((int)row / xM_yN) * xM_yN;
+    const int base = centred ? xM / 2 : 0;
+    const int d0 = wrap1(base + signed_freq(a0, xM_yN) + fo0, xM);
+    const int d1 = wrap1(base + signed_freq(a1, xM_yN) + fo1, xM);
+    double2 o = PDF::out(PDF::scale(v, PDF::w(Fn, a0)));
+    if (!centred) {
+      const double sc = 1.0 / ((double)xM * (double)xM);
+      o.x *= sc;
+      o.y *= sc;
+    }
+    double2 *d = sub + ((size_t)pair * xM + d0) * xM + d1;
+    double2 a = *d;
+    a.x += o.x;
+    a.y += o.y;
+    *d = a;
+  }
+};
+
 // subgrid -> facet: the split of each subgrid spectrum (k_rcT_split) as the
 // load of the xM_yP inverse transforms; rows pair * xM_yN + a0
 struct IoSplit {
@@ -676,7 +709,7 @@ inline unsigned grid_for(size_t n) {
 }
 
 struct WsLayout {
-  size_t bf, mbf, bf2, mbf2, offs, total;
+  size_t bf, mbf, bf2, mbf2, offs, nm, total;
 };
 
 // subgrid -> facet: A [n0 n1 xM_yN][xM_yP], acc [n0 xM_yN][yP], B [yB n0][xM_yP],
@@ -738,7 +771,9 @@ WsLayout ws_layout(const cg_recombine *h, int n0, int n1) {
   L.bf2 = L.mbf + align256((size_t)n1 * h->yB * h->xM_yP * e);
   L.mbf2 = L.bf2 + align256((size_t)n1 * h->xM_yN * h->yP * e);
   L.offs = L.mbf2 + align256((size_t)n0 * n1 * h->xM_yN * h->xM_yP * e);
-  L.total = L.offs + align256((size_t)(n0 + n1) * sizeof(int32_t));
+  // the contributions, for cg_recombine_facet_add on the complex128 pipeline
+  L.nm = L.offs + align256((size_t)(n0 + n1) * sizeof(int32_t));
+  L.total = L.nm + align256((size_t)n0 * n1 * h->xM_yN * h->xM_yN * e);
   return L;
 }
 
@@ -781,9 +816,38 @@ int facet_to_subgrids(cg_recombine *h, const void *facet, int centred, int n0, i
 // The double-float pipelines with the fused passes: per facet, four
 // transform launches and one transpose kernel each way (and the scatter
 // kernel of the first axis on the way back).
+// the last transforms' stores: the contributions (IoWindowCrop) or their sum
+// into the subgrids (IoWindowCropAdd)
+template <class LastIO>
+int facet_df_passes(cg_recombine *h, const void *facet, int centred, int n0, int n1,
+                    LastIO last, char *ws, const WsLayout &L, cudaStream_t st);
+
 int facet_to_subgrids_df(cg_recombine *h, const void *facet, int centred, int n0, int n1,
                          void *nmbf, int out_centred, char *ws, const WsLayout &L,
                          cudaStream_t st) {
+  const int32_t *offs0 = (const int32_t *)(ws + L.offs);
+  const WindowSrc w2{(const float4 *)(ws + L.bf2), offs0, h->d_m2, n1 * h->xM_yN, h->yP,
+                     h->xM_yP, h->xMxN_yP};
+  return facet_df_passes(h, facet, centred, n0, n1,
+                         IoWindowCrop{w2, h->d_Fn2, (double2 *)nmbf, h->xM_yN, out_centred}, ws,
+                         L, st);
+}
+
+int facet_add_df(cg_recombine *h, const void *facet, int centred, int n0, int n1, int fo0,
+                 int fo1, void *sub, int sub_centred, char *ws, const WsLayout &L,
+                 cudaStream_t st) {
+  const int32_t *offs0 = (const int32_t *)(ws + L.offs);
+  const WindowSrc w2{(const float4 *)(ws + L.bf2), offs0, h->d_m2, n1 * h->xM_yN, h->yP,
+                     h->xM_yP, h->xMxN_yP};
+  return facet_df_passes(h, facet, centred, n0, n1,
+                         IoWindowCropAdd{w2, h->d_Fn2, (double2 *)sub, h->xM_yN, h->xM, fo0,
+                                         fo1, sub_centred},
+                         ws, L, st);
+}
+
+template <class LastIO>
+int facet_df_passes(cg_recombine *h, const void *facet, int centred, int n0, int n1,
+                    LastIO last, char *ws, const WsLayout &L, cudaStream_t st) {
   float4 *bf = (float4 *)(ws + L.bf);
   float4 *mbf = (float4 *)(ws + L.mbf);
   float4 *bf2 = (float4 *)(ws + L.bf2);
@@ -804,10 +868,7 @@ int facet_to_subgrids_df(cg_recombine *h, const void *facet, int centred, int n0
   CG_LAUNCH("recombine prepare facet (axis 0)");
   if ((rc = dfft_rows_df(bf2, (int64_t)n1 * xM_yN, yP, 1, st))) return rc;
   // each subgrid row offset's window in the loads, the crop in the stores
-  return dfft_rows_io(
-      IoWindowCrop{WindowSrc{bf2, offs0, h->d_m2, n1 * xM_yN, yP, xM_yP, xMxN}, h->d_Fn2,
-                   (double2 *)nmbf, xM_yN, out_centred},
-      (int64_t)n0 * n1 * xM_yN, xM_yP, 0, st);
+  return dfft_rows_io(last, (int64_t)n0 * n1 * xM_yN, xM_yP, 0, st);
 }
 
 int subgrids_to_facet_df(cg_recombine *h, const void *fs, int centred, int n0, int n1, int fo0,
@@ -1012,6 +1073,42 @@ int cg_recombine_facet_to_subgrids(cg_recombine *h, const void *facet, int centr
   if (use_df(h))
     return facet_to_subgrids_df(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
   return facet_to_subgrids<P64>(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
+}
+
+int cg_recombine_facet_add(cg_recombine *h, const void *facet, int centred,
+                           const int32_t *subgrid_off0, int n0, const int32_t *subgrid_off1,
+                           int n1, int facet_off0, int facet_off1, void *subgrids,
+                           int sub_centred, void *ws, size_t ws_bytes, int32_t *d_status,
+                           cg_stream_t stream) {
+  CG_REQUIRE(h && facet && d_status && n0 >= 0 && n1 >= 0, "bad recombine_facet_add arguments");
+  if (n0 == 0 || n1 == 0) return CG_OK;
+  CG_REQUIRE(subgrids && subgrid_off0 && subgrid_off1, "bad recombine_facet_add arguments");
+  CG_REQUIRE(n1 <= 65535 && (long long)n0 * n1 <= 65535,
+             "at most 65535 subgrids (n0 * n1) per call; split the offsets");
+  CG_REQUIRE(pmod(facet_off0, h->facet_spacing) == 0 && pmod(facet_off1, h->facet_spacing) == 0,
+             "facet offsets must be multiples of the facet spacing %d", h->facet_spacing);
+  const WsLayout L = ws_layout(h, n0, n1);
+  if (!ws || ws_bytes < L.total)
+    return set_error(CG_ERR_WORKSPACE, "recombine needs %zu workspace bytes", L.total);
+  cudaStream_t st = (cudaStream_t)stream;
+  char *w = (char *)ws;
+  k_rc_offsets<<<(n0 + n1 + 255) / 256, 256, 0, st>>>(subgrid_off0, n0, subgrid_off1, n1,
+                                                      h->subgrid_spacing, h->yP_spacing, h->yP,
+                                                      (int32_t *)(w + L.offs), d_status);
+  CG_LAUNCH("recombine offsets");
+  // facet offsets in xM samples, reduced to [0, xM) (the kernels wrap once)
+  const int fo0 = pmod((long long)facet_off0 / h->facet_spacing * h->xM_spacing, h->xM);
+  const int fo1 = pmod((long long)facet_off1 / h->facet_spacing * h->xM_spacing, h->xM);
+  if (use_df(h))
+    return facet_add_df(h, facet, centred, n0, n1, fo0, fo1, subgrids, sub_centred, w, L, st);
+  double2 *nm = (double2 *)(w + L.nm);
+  int rc = facet_to_subgrids<P64>(h, facet, centred, n0, n1, nm, sub_centred, w, L, st);
+  if (rc) return rc;
+  const dim3 grid((h->xM_yN + 127) / 128, h->xM_yN, n0 * n1);
+  k_rc_add_facet<<<grid, 128, 0, st>>>(nm, h->xM_yN, h->xM, fo0, fo1, sub_centred,
+                                       (double2 *)subgrids);
+  CG_LAUNCH("recombine add facet");
+  return CG_OK;
 }
 
 int cg_recombine_subgrids_to_facet(cg_recombine *h, const void *fs, int centred,

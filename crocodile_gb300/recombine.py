@@ -19,6 +19,8 @@ the notebook, and return CUDA tensors:
   pf1_ft1_es1 + pf0_ft0 + es0): two batched FFT passes per axis on the device;
 * ``add_facet(approx, nmbf, facet_off0, facet_off1)``: approx += the
   contributions rolled to the facet (cell 30; recombine2d_af0_af1);
+* ``facet_add(approx, facet, offs0, offs1, facet_off0, facet_off1)``: the two
+  above in one call;
 * ``finish_subgrids(approx)``: ifft and the middle xA_size (cell 30);
 * ``recombine(facets, facet_offs0, facet_offs1, offs0, offs1)``: all of it.
 
@@ -159,6 +161,34 @@ class Recombine:
             return E.fft_df_(t, inverse)
         return E.fft_(t, inverse)
 
+    def facet_add(self, approx, facet, offs0, offs1, facet_off0, facet_off1, check=True):
+        """approx [n0, n1, xM, xM] (centred) += the contributions of one centred
+        facet at (facet_off0, facet_off1) to the subgrids at offs0 x offs1:
+        facet_to_subgrids and add_facet in one call (cg_recombine_facet_add), the
+        same values, without the contributions array on the double-float
+        pipeline."""
+        f = E.cuda_tensor(facet, self.dtype)
+        if tuple(f.shape) != (self.yB_size, self.yB_size):
+            raise ValueError("facet must be %d x %d" % (self.yB_size, self.yB_size))
+        o0 = E.cuda_tensor(numpy.atleast_1d(offs0) if not isinstance(offs0, torch.Tensor)
+                           else offs0, torch.int32)
+        o1 = E.cuda_tensor(numpy.atleast_1d(offs1) if not isinstance(offs1, torch.Tensor)
+                           else offs1, torch.int32)
+        n0, n1 = int(o0.numel()), int(o1.numel())
+        if approx.numel() != n0 * n1 * self.xM_size ** 2 or approx.dtype != self.dtype \
+                or not approx.is_contiguous():
+            raise ValueError("approx must be contiguous %d x %d subgrids of %d^2 %s"
+                             % (n0, n1, self.xM_size, self.dtype))
+        ws = self._workspace(n0, n1)
+        if check:
+            self.status.reset()
+        L.call("cg_recombine_facet_add", self._h, E._p(f), 1, E._p(o0), n0, E._p(o1), n1,
+               int(facet_off0), int(facet_off1), E._p(approx), 1, E._p(ws), ws.numel(),
+               E._p(self.status.t), E.stream())
+        if check:
+            self.status.check()
+        return approx
+
     def finish_subgrids(self, approx, crop=True):
         """The subgrids from their summed contributions: centred ifft (in place)
         and, with crop, the middle xA_size (a view)."""
@@ -174,15 +204,12 @@ class Recombine:
         n0, n1 = len(offs0), len(offs1)
         approx = torch.zeros((n0, n1, self.xM_size, self.xM_size), dtype=self.dtype,
                              device="cuda")
-        nm = torch.empty((n0, n1, self.xM_yN_size, self.xM_yN_size), dtype=self.dtype,
-                         device="cuda")
         o0 = E.cuda_tensor(numpy.asarray(offs0), torch.int32)
         o1 = E.cuda_tensor(numpy.asarray(offs1), torch.int32)
         self.status.reset()
         for j0, fo0 in enumerate(facet_offs0):
             for j1, fo1 in enumerate(facet_offs1):
-                self.facet_to_subgrids(facets[j0][j1], o0, o1, out=nm, check=False)
-                self.add_facet(approx, nm, fo0, fo1)
+                self.facet_add(approx, facets[j0][j1], o0, o1, fo0, fo1, check=False)
         self.status.check()
         return self.finish_subgrids(approx, crop=crop)
 

@@ -554,6 +554,17 @@ int cg_recombine_facet_to_subgrids(cg_recombine *h, const void *facet, int centr
                                    int out_centred, void *workspace,
                                    size_t workspace_bytes, int32_t *d_status,
                                    cg_stream_t stream);
+/* cg_recombine_facet_to_subgrids and cg_recombine_add_facet in one call: the
+ * facet's contributions to the n0 x n1 subgrids summed straight into
+ * subgrids [n0][n1][xM][xM] at the facet offsets (sub_centred: both layouts
+ * as cg_recombine_add_facet's centred flag), the same values and additions,
+ * without the intermediate contributions array on the double-float pipeline.
+ * Workspace: cg_recombine_workspace_bytes(h, n0, n1). */
+int cg_recombine_facet_add(cg_recombine *h, const void *facet, int centred,
+                           const int32_t *subgrid_off0, int n0, const int32_t *subgrid_off1,
+                           int n1, int facet_off0, int facet_off1, void *subgrids,
+                           int sub_centred, void *ws, size_t ws_bytes, int32_t *d_status,
+                           cg_stream_t stream);
 /* Subgrid -> facet (the notebook's cell 18 in 2-D, by separability; the
  * adjoint of the above): facet [yB, yB] (+)= Fb x Fb times the sum over
  * n0 x n1 subgrids of their contributions, from the subgrids' spectra fs

@@ -303,3 +303,61 @@ def test_subgrids_to_facet_raw_layout(env):
            128, 256, E._p(out), 0, 0, E._p(ws), ws.numel(), E._p(st.t), E.stream())
     st.check()
     assert_allclose(out.cpu().numpy(), sh(want), rtol=0, atol=1e-13 * numpy.abs(want).max())
+
+
+@pytest.mark.parametrize("pow2", [False, True])
+@pytest.mark.parametrize("centred", [1, 0])
+def test_facet_add_equals_two_calls(env, pow2, centred):
+    """cg_recombine_facet_add (the contributions summed into the subgrids by
+    the last transforms' stores on the double-float pipeline, the two calls
+    inside on the complex128 one) equals facet_to_subgrids + add_facet bit for
+    bit, on the T05 set (yP 216: complex128 pipeline) and on a power-of-two set
+    (double-float pipeline), in both layouts, at facet offsets that wrap."""
+    torch, R, S, E, L, O, rg = env
+    if pow2:
+        kw = dict(image_size=512, subgrid_spacing=128, yB_size=128, yN_size=160, yP_size=256,
+                  xA_size=128, xM_size=256, xMxN_yP_size=160)
+        rc = R.Recombine(**kw)
+    else:
+        kw = sizes(rg)
+        rc = R.Recombine(pswf=rg["pswf"], **kw)
+    xM, n = rc.xM_size, rc.xM_yN_size
+    yB = rc.yB_size
+    rng = numpy.random.default_rng(11)
+    so = numpy.array([0, 128, 256, 384], dtype=numpy.int32)
+    o = E.cuda_tensor(so, torch.int32)
+    ws = torch.empty(L.lib().cg_recombine_workspace_bytes(rc._h, 4, 4), dtype=torch.uint8,
+                     device="cuda")
+    st = E.Status()
+    for fo0, fo1 in ((256, 128), (-128, 384)):
+        f = E.cuda_tensor(rng.normal(size=(yB, yB)) + 1j * rng.normal(size=(yB, yB)), E.CD)
+        base = E.cuda_tensor(rng.normal(size=(16, xM, xM)) + 0j, E.CD)
+        two = base.clone()
+        nm = torch.empty((4, 4, n, n), dtype=E.CD, device="cuda")
+        st.reset()
+        L.call("cg_recombine_facet_to_subgrids", rc._h, E._p(f), centred, E._p(o), 4, E._p(o),
+               4, E._p(nm), centred, E._p(ws), ws.numel(), E._p(st.t), E.stream())
+        L.call("cg_recombine_add_facet", rc._h, E._p(nm), 16, fo0, fo1, centred, E._p(two),
+               E.stream())
+        one = base.clone()
+        L.call("cg_recombine_facet_add", rc._h, E._p(f), centred, E._p(o), 4, E._p(o), 4, fo0,
+               fo1, E._p(one), centred, E._p(ws), ws.numel(), E._p(st.t), E.stream())
+        st.check()
+        assert torch.equal(one, two), (pow2, centred, fo0, fo1)
+
+
+def test_recombine_uses_facet_add(env):
+    # Recombine.recombine sums through facet_add: the same subgrids as the
+    # two-call form
+    torch, R, S, E, L, O, rg = env
+    rc = R.Recombine(pswf=rg["pswf"], **sizes(rg))
+    rng = numpy.random.default_rng(5)
+    yB = rc.yB_size
+    facets = [[rng.normal(size=(yB, yB)) + 0j for _ in range(2)] for _ in range(2)]
+    fo, so = [0, 128], [0, 128, 256]
+    got = rc.recombine(facets, fo, fo, so, so, crop=False)
+    approx = torch.zeros_like(got)
+    for j0 in range(2):
+        for j1 in range(2):
+            rc.add_facet(approx, rc.facet_to_subgrids(facets[j0][j1], so, so), fo[j0], fo[j1])
+    assert torch.equal(got, rc.finish_subgrids(approx, crop=False))
