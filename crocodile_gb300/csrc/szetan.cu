@@ -13,14 +13,16 @@
 //   c(x) = sum_rp sum_m C[rp, m] cos(2 pi (lp - nu_m) x) dnu
 //   hfine = c / d
 // d only needs the Gram sums G[rp, r] = sum_m C[rp, m] C[r, m], formed once
-// (one block per pair); c is one block per coordinate reducing over m.  The
-// image-sized sweep is nx * M * 2R FP64 cosines (8192^2 image: 6.7e8).
+// (one block per pair); c is one block per coordinate reducing over m, with
+// the cosine split by angle subtraction: nx * M FP64 sincos and nx * M * 2R
+// products (8192-pixel axis, M 8192: 6.7e7 sincos).
 
 #include "cg_internal.cuh"
 
 namespace {
 
 constexpr double TWO_PI = 6.283185307179586;  // 2 * numpy.pi, as the reference forms it
+constexpr int SZT_MAXR = 16;                   // largest R of the correction sweep
 
 // Block-wide FP64 sum; every thread gets the total.
 __device__ double block_sum(double v, double *red) {
@@ -79,23 +81,31 @@ __global__ void k_szetan_gram(const double *__restrict__ C, int R2, int M, doubl
   if (threadIdx.x == 0) G[blockIdx.x] = s;
 }
 
-// One block per image coordinate.
+// One block per image coordinate.  cos(2 pi (lp - nu) x) is evaluated as
+// cos(2 pi lp x) cos(2 pi nu x) + sin(2 pi lp x) sin(2 pi nu x): one sincos
+// per offset instead of 2R cosines (GB300's FP64 rate bounds this sweep), the
+// 2R values of the first factors once per block.
 __global__ void k_szetan_correction(const double *__restrict__ C, const double *__restrict__ G,
                                     int R, int M, const double *__restrict__ x, int nx,
                                     double *__restrict__ hfine) {
   __shared__ double red[32];
+  __shared__ double cl[2 * SZT_MAXR], sl[2 * SZT_MAXR];
   const int n = blockIdx.x;
   if (n >= nx) return;
   const int R2 = 2 * R;
   const double xv = x[n];
   const double dnu = 1.0 / (2.0 * M);
+  if (threadIdx.x < R2) {
+    const double lp = (double)((int)threadIdx.x - R + 1);
+    sincos(TWO_PI * lp * xv, &sl[threadIdx.x], &cl[threadIdx.x]);
+  }
+  __syncthreads();
   double s = 0;
   for (int m = threadIdx.x; m < M; m += blockDim.x) {
     const double nv = ((double)m + 0.5) / (2.0 * M);
-    for (int rp = 0; rp < R2; ++rp) {
-      const double lp = (double)(rp - R + 1);
-      s += C[(size_t)rp * M + m] * cos(TWO_PI * (lp - nv) * xv);
-    }
+    double sn, cs;
+    sincos(TWO_PI * nv * xv, &sn, &cs);
+    for (int rp = 0; rp < R2; ++rp) s += C[(size_t)rp * M + m] * (cl[rp] * cs + sl[rp] * sn);
   }
   const double c = block_sum(s, red) * dnu;
   if (threadIdx.x == 0) {
