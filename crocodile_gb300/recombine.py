@@ -31,10 +31,14 @@ and the other direction (notebook cell 18, in 2-D by separability):
   approximation Fb x Fb x the sum of every subgrid's contribution;
 * ``split(subgrids, offs0, offs1, facet_offs0, facet_offs1)``: all facets.
 
-Row transforms of power-of-two length run in double-float arithmetic on the
-FP32 units (``fft="auto"``, about 48 significant bits; GB300's FP64 rate
-bounds an FP64 FFT), other lengths and ``fft="fp64"`` in FP64 (cuFFT Z2Z).
-Arrays are complex128, as in the reference: Fb = 1 / PSWF spans
+With ``fft="auto"`` and power-of-two transform lengths (yP and xM_yP in
+64..2048) the whole pipeline runs in double-float arithmetic on the FP32
+units (hi + lo float pairs, about 48 significant bits; GB300's FP64 rate
+bounds FP64 work): the stage arrays, the row FFTs with the prepare, window
+and crop steps in their loads and stores, and the subgrids' centred xM^2
+transforms (``finish_subgrids``, ``subgrid_spectra``).  Other lengths and
+``fft="fp64"`` keep complex128 stage arrays and FP64 cuFFT.  The arrays the
+caller sees are complex128, as in the reference: Fb = 1 / PSWF spans
 many decades towards the facet edge, and the contributions come out of
 intermediates a thousand times larger than their peak, which single
 precision cannot carry (measured: 6e-4 relative error per facet, the
