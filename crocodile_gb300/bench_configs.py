@@ -416,6 +416,43 @@ def measure_recombine(steps=3, nfacets=None):
                     "reference notebook in tests/test_gpu_recombine.py"}
 
 
+RECOMBINE_SMALL = (16384, 32, 5120, 5632, 8192, 416, 512, 280)
+
+
+def measure_recombine_small(steps=3):
+    """One facet of bench_recombine.c's "small" set (16k-8k-512: 16384^2 image,
+    4 x 4 facets of 5120^2, 40 x 40 subgrids of xM 512) summed into all 1600
+    subgrids (cg_recombine_facet_add): yP 8192 runs the double-float stage
+    kernels with the four-step rows, against complex128 with FP64 cuFFT."""
+    from .recombine import Recombine
+    N, sp, yB, yN, yP, xA, xM, xMxN = RECOMBINE_SMALL
+    fo, so = recombine_layout(N, sp, yB, xA)
+    g = torch.Generator(device="cuda").manual_seed(13)
+    facet = torch.randn((yB, yB), dtype=E.CD, device="cuda", generator=g)
+    o = E.cuda_tensor(numpy.asarray(so), torch.int32)
+    ns = len(so)
+    approx = torch.zeros((ns, ns, xM, xM), dtype=E.CD, device="cuda")
+    out = {}
+    for mode in ("auto", "fp64"):
+        rc = Recombine(N, sp, yB, yN, yP, xA, xM, xMxN, fft=mode)
+        rc.status.reset()
+        out[mode] = _time(lambda: rc.facet_add(approx, facet, o, o, fo[0], fo[0], check=False),
+                          steps, warmup=1)
+        rc.status.check()
+        del rc
+        torch.cuda.empty_cache()
+    nf = len(fo) ** 2
+    return {"workload": "facet->subgrid recombination, bench_recombine.c 'small' (16k-8k-512): "
+                        "16384^2 image, %d facets of %d^2, %d x %d subgrids (xA %d, xM %d), "
+                        "complex128" % (nf, yB, ns, ns, xA, xM),
+            "facets": nf, "subgrids": ns * ns, "ms_per_facet": out["auto"],
+            "ms_per_facet_fp64_cufft": out["fp64"], "speedup": out["fp64"] / out["auto"],
+            "note": "one facet's contributions summed into every subgrid; yP 8192: "
+                    "double-float stage arrays and four-step double-float rows (auto) "
+                    "against complex128 stage arrays and FP64 cuFFT; parity of the two in "
+                    "tests/test_gpu_dfft.py"}
+
+
 def measure_szetan(steps=5):
     """Sze-Tan gridder evaluation (crocodile/antialias.py): the grid correction
     of an 8192-pixel axis (the gridder sampled at 8192 offsets, as
@@ -550,7 +587,8 @@ def measure_ingest(steps=3, blocks=None):
 
 MEASURES = {"plain": measure_plain, "wproj": measure_wproj, "diff": measure_diff,
             "wstack": measure_wstack, "aw": measure_aw, "wtowers": measure_wtowers,
-            "recombine": measure_recombine, "szetan": measure_szetan, "ingest": measure_ingest,
+            "recombine": measure_recombine, "recombine_small": measure_recombine_small,
+            "szetan": measure_szetan, "ingest": measure_ingest,
             "awtowers": measure_awtowers}
 
 

@@ -132,6 +132,74 @@ __global__ void __launch_bounds__(T)
   }
 }
 
+// ---------------------------------------------------------------- long rows
+// n = N1 * 2048 (N1 = 2, 4) in three passes, the four-step factorisation
+//   X[k1 + N1 k2] = sum_n2 w_n^(n2 k1) [sum_n1 x[n2 + 2048 n1] w_N1^(n1 k1)] w_2048^(n2 k2):
+// k_dfft_long_pre forms the bracket times w_n^(n2 k1) in place (row position
+// k1 * 2048 + n2), the 2048-point kernel transforms the N1 sub-rows, and
+// k_dfft_long_T puts X back in natural order through shared memory.
+constexpr int DF_LONG_N2 = 2048;
+
+template <int N1>
+__global__ void k_dfft_long_pre(float4 *d, int64_t batch, const float4 *__restrict__ tw,
+                                int inverse) {
+  constexpr int N2 = DF_LONG_N2, N = N1 * N2;
+  const int64_t total = batch * N2;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / N2;
+    const int n2 = (int)(e - b * N2);
+    float4 *row = d + b * N;
+    cdf x[N1], y[N1];
+#pragma unroll
+    for (int j = 0; j < N1; ++j) x[j] = cdf_load(row[n2 + N2 * j]);
+    if (N1 == 2) {
+      y[0] = cdf_add_f(x[0], x[1]);
+      y[1] = cdf_sub_f(x[0], x[1]);
+    } else {
+      const cdf a0 = cdf_add_f(x[0], x[N1 > 2 ? 2 : 0]), a1 = cdf_sub_f(x[0], x[N1 > 2 ? 2 : 0]);
+      const cdf b0 = cdf_add_f(x[1], x[N1 > 3 ? 3 : 1]);
+      const cdf b1 = dfk::cdf_mul_j(cdf_sub_f(x[1], x[N1 > 3 ? 3 : 1]), inverse != 0);
+      y[0] = cdf_add_f(a0, b0);
+      y[1] = cdf_add_f(a1, b1);
+      y[N1 > 2 ? 2 : 0] = cdf_sub_f(a0, b0);
+      y[N1 > 3 ? 3 : 1] = cdf_sub_f(a1, b1);
+    }
+    row[n2] = cdf_store(y[0]);
+#pragma unroll
+    for (int k1 = 1; k1 < N1; ++k1)
+      row[k1 * N2 + n2] = cdf_store(n2 == 0 ? y[k1] : cdf_mul_f(y[k1], cdf_load(tw[n2 * k1])));
+  }
+}
+
+// X[k1 + N1 k2] = Z[k1][k2] for each row, in place; one CTA per row, the sub-
+// rows padded by one element in shared memory
+template <int N1>
+__global__ void __launch_bounds__(1024) k_dfft_long_T(float4 *d, int64_t batch) {
+  constexpr int N2 = DF_LONG_N2, N = N1 * N2, P = N2 + 1;
+  extern __shared__ float dsm[];
+  float4 *buf = (float4 *)dsm;  // [N1][P]
+  for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+    float4 *row = d + b * N;
+    for (int e = threadIdx.x; e < N; e += blockDim.x) buf[(e / N2) * P + (e % N2)] = row[e];
+    __syncthreads();
+    for (int k = threadIdx.x; k < N; k += blockDim.x) row[k] = buf[(k % N1) * P + k / N1];
+    __syncthreads();
+  }
+}
+
+// complex128 <-> double-float in place (the same 16 bytes per element)
+__global__ void k_c128_to_df(double2 *d, int64_t count) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x)
+    ((float4 *)d)[e] = cdf_store(cdf_from(d[e]));
+}
+__global__ void k_df_to_c128(double2 *d, int64_t count) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x)
+    d[e] = cdf_to(cdf_load(((float4 *)d)[e]));
+}
+
 // ---------------------------------------------------------------- twiddles
 }  // namespace
 
@@ -192,8 +260,37 @@ int dfft_rows(double2 *data, int64_t batch, int n, int inverse, cudaStream_t st)
   return dfft_rows_io(IoC128{data, n}, batch, n, inverse, st);
 }
 
-// The same on rows stored as double-float (float4 per element).
+bool dfft_long_supported(int n) { return dfft_supported(n) || n == 4096 || n == 8192; }
+
+namespace {
+template <int N1>
+int dfft_long(float4 *data, int64_t batch, int inverse, cudaStream_t st) {
+  const int n = N1 * DF_LONG_N2;
+  const float4 *tw;
+  int rc = dfft_twiddles(n, inverse ? 1 : -1, &tw);
+  if (rc) return rc;
+  const int64_t total = batch * DF_LONG_N2;
+  const unsigned g = (unsigned)std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16);
+  k_dfft_long_pre<N1><<<g, 256, 0, st>>>(data, batch, tw, inverse);
+  CG_LAUNCH("double-float long FFT (first pass)");
+  if ((rc = dfft_rows_io(IoDF{data, DF_LONG_N2}, batch * N1, DF_LONG_N2, inverse, st)))
+    return rc;
+  const size_t smem = (size_t)N1 * (DF_LONG_N2 + 1) * sizeof(float4);
+  CG_CUDA(cudaFuncSetAttribute(k_dfft_long_T<N1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem));
+  const unsigned gt = (unsigned)std::min<int64_t>(batch, (int64_t)num_sms() * 4);
+  k_dfft_long_T<N1><<<gt, 1024, smem, st>>>(data, batch);
+  CG_LAUNCH("double-float long FFT (transpose)");
+  return CG_OK;
+}
+}  // namespace
+
+// The same on rows stored as double-float (float4 per element); lengths up to
+// 8192 (4096 and 8192 by the four-step passes).
 int dfft_rows_df(float4 *data, int64_t batch, int n, int inverse, cudaStream_t st) {
+  if (batch <= 0) return CG_OK;
+  if (n == 4096) return dfft_long<2>(data, batch, inverse, st);
+  if (n == 8192) return dfft_long<4>(data, batch, inverse, st);
   return dfft_rows_io(IoDF{data, n}, batch, n, inverse, st);
 }
 
@@ -227,6 +324,20 @@ int dfft2_centred(double2 *data, int64_t batch, int H, int W, int inverse, cudaS
 extern "C" int cg_fft_rows_df(void *data_c128, int64_t batch, int n, int inverse,
                               cg_stream_t stream) {
   CG_REQUIRE(data_c128 && batch >= 0, "bad double-float FFT arguments");
+  if (n == 4096 || n == 8192) {  // converted in place around the double-float passes
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t count = batch * n;
+    if (count == 0) return CG_OK;
+    const unsigned g =
+        (unsigned)std::min<int64_t>((count + 255) / 256, (int64_t)cg::num_sms() * 16);
+    cg::k_c128_to_df<<<g, 256, 0, st>>>((double2 *)data_c128, count);
+    CG_LAUNCH("complex128 to double-float");
+    const int rc = cg::dfft_rows_df((float4 *)data_c128, batch, n, inverse, st);
+    if (rc) return rc;
+    cg::k_df_to_c128<<<g, 256, 0, st>>>((double2 *)data_c128, count);
+    CG_LAUNCH("double-float to complex128");
+    return CG_OK;
+  }
   return cg::dfft_rows((double2 *)data_c128, batch, n, inverse, (cudaStream_t)stream);
 }
 

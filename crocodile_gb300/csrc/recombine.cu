@@ -49,6 +49,7 @@
 namespace cg {
 int fft_plan(int batch, int H, int W, cufftType type, cufftHandle *out);
 bool dfft_supported(int n);
+bool dfft_long_supported(int n);
 int dfft_rows(double2 *data, int64_t batch, int n, int inverse, cudaStream_t st);
 int dfft_rows_df(float4 *data, int64_t batch, int n, int inverse, cudaStream_t st);
 }
@@ -659,6 +660,12 @@ struct Tab<P64> {
   static const double *Fn(const cg_recombine *h) { return h->d_Fn; }
   static const double *m(const cg_recombine *h) { return h->d_m; }
 };
+template <>
+struct Tab<PDF> {
+  static const float2 *Fb(const cg_recombine *h) { return h->d_Fb2; }
+  static const float2 *Fn(const cg_recombine *h) { return h->d_Fn2; }
+  static const float2 *m(const cg_recombine *h) { return h->d_m2; }
+};
 
 // complex128 only: Fb = 1 / PSWF spans many decades at the facet edge (6.4e6
 // for the 512 / 128 / 140 test set), and the contributions come out of
@@ -679,10 +686,20 @@ int rows_fft(const cg_recombine *h, double2 *data, int batch, int len, int dir, 
   return r == CUFFT_SUCCESS ? CG_OK : set_error(CG_ERR_CUDA, "cufftExec failed: %d", (int)r);
 }
 
-// the double-float pipeline: both transform lengths in reach of the
-// double-float FFT, unless FP64 cuFFT was asked for
-bool use_df(const cg_recombine *h) {
-  return h->fft_mode == 0 && dfft_supported(h->yP) && dfft_supported(h->xM_yP);
+int rows_fft(const cg_recombine *, float4 *data, int batch, int len, int dir, cudaStream_t st) {
+  return dfft_rows_df(data, batch, len, dir == CUFFT_INVERSE, st);
+}
+
+// The pipeline of a configuration (unless FP64 cuFFT was asked for): both
+// transform lengths within one CTA's double-float FFT (64..2048): the fused
+// double-float passes; yP up to 8192 (the four-step double-float rows): the
+// double-float stage kernels; otherwise complex128 and FP64 cuFFT.
+enum { PIPE_C128 = 0, PIPE_DF_FUSED = 1, PIPE_DF = 2 };
+int pipeline(const cg_recombine *h) {
+  if (h->fft_mode != 0) return PIPE_C128;
+  if (dfft_supported(h->yP) && dfft_supported(h->xM_yP)) return PIPE_DF_FUSED;
+  if (dfft_long_supported(h->yP) && dfft_long_supported(h->xM_yP)) return PIPE_DF;
+  return PIPE_C128;
 }
 
 inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -1070,8 +1087,12 @@ int cg_recombine_facet_to_subgrids(cg_recombine *h, const void *facet, int centr
                                                       h->subgrid_spacing, h->yP_spacing, h->yP,
                                                       (int32_t *)(w + L.offs), d_status);
   CG_LAUNCH("recombine offsets");
-  if (use_df(h))
-    return facet_to_subgrids_df(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
+  switch (pipeline(h)) {
+    case PIPE_DF_FUSED:
+      return facet_to_subgrids_df(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
+    case PIPE_DF:
+      return facet_to_subgrids<PDF>(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
+  }
   return facet_to_subgrids<P64>(h, facet, centred, n0, n1, nmbf, out_centred, w, L, st);
 }
 
@@ -1099,10 +1120,13 @@ int cg_recombine_facet_add(cg_recombine *h, const void *facet, int centred,
   // facet offsets in xM samples, reduced to [0, xM) (the kernels wrap once)
   const int fo0 = pmod((long long)facet_off0 / h->facet_spacing * h->xM_spacing, h->xM);
   const int fo1 = pmod((long long)facet_off1 / h->facet_spacing * h->xM_spacing, h->xM);
-  if (use_df(h))
+  const int pipe = pipeline(h);
+  if (pipe == PIPE_DF_FUSED)
     return facet_add_df(h, facet, centred, n0, n1, fo0, fo1, subgrids, sub_centred, w, L, st);
   double2 *nm = (double2 *)(w + L.nm);
-  int rc = facet_to_subgrids<P64>(h, facet, centred, n0, n1, nm, sub_centred, w, L, st);
+  int rc = pipe == PIPE_DF
+               ? facet_to_subgrids<PDF>(h, facet, centred, n0, n1, nm, sub_centred, w, L, st)
+               : facet_to_subgrids<P64>(h, facet, centred, n0, n1, nm, sub_centred, w, L, st);
   if (rc) return rc;
   const dim3 grid((h->xM_yN + 127) / 128, h->xM_yN, n0 * n1);
   k_rc_add_facet<<<grid, 128, 0, st>>>(nm, h->xM_yN, h->xM, fo0, fo1, sub_centred,
@@ -1141,9 +1165,14 @@ int cg_recombine_subgrids_to_facet(cg_recombine *h, const void *fs, int centred,
   // facet offsets in xM samples, reduced to [0, xM) (the kernels wrap once)
   const int fo0 = pmod((long long)facet_off0 / h->facet_spacing * h->xM_spacing, h->xM);
   const int fo1 = pmod((long long)facet_off1 / h->facet_spacing * h->xM_spacing, h->xM);
-  if (use_df(h))
-    return subgrids_to_facet_df(h, fs, centred, n0, n1, fo0, fo1, facet, out_centred,
-                                accumulate, w, L, st);
+  switch (pipeline(h)) {
+    case PIPE_DF_FUSED:
+      return subgrids_to_facet_df(h, fs, centred, n0, n1, fo0, fo1, facet, out_centred,
+                                  accumulate, w, L, st);
+    case PIPE_DF:
+      return subgrids_to_facet<PDF>(h, fs, centred, n0, n1, fo0, fo1, facet, out_centred,
+                                    accumulate, w, L, st);
+  }
   return subgrids_to_facet<P64>(h, fs, centred, n0, n1, fo0, fo1, facet, out_centred,
                                 accumulate, w, L, st);
 }

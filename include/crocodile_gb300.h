@@ -291,7 +291,8 @@ int cg_fft(void *data, int batch, int H, int W, int is_c64, int inverse,
  * into neighbouring passes (the w-towers pipeline). */
 int cg_fft_raw(void *data, int batch, int H, int W, int is_c64, int inverse,
                cg_stream_t stream);
-/* batch contiguous complex128 rows of length n (a power of two, 64..2048)
+/* batch contiguous complex128 rows of length n (a power of two, 64..8192;
+ * 4096 and 8192 by a four-step factorisation over the 2048-point transform)
  * transformed in place, unshifted and unnormalised (inverse: exp(+2 pi i)),
  * in double-float arithmetic (hi + lo pairs of floats, about 48 significant
  * bits) on the FP32 units: GB300's FP64 rate bounds an FP64 FFT. */
@@ -533,11 +534,13 @@ int cg_recombine_create(int image_size, int subgrid_spacing, const double *pswf_
                         int yB_size, int yN_size, int yP_size, int xA_size,
                         int xM_size, int xMxN_yP_size, cg_recombine **out);
 int cg_recombine_destroy(cg_recombine *h);
-/* FFTs of the recombination: mode 0 (default) transforms power-of-two rows
- * (64..2048) in double-float arithmetic on the FP32 units (cg_fft_rows_df)
- * and other lengths with cuFFT Z2Z; when yP_size and xM_yP_size both qualify
- * the stage arrays between the passes are double-float too (complex128 only
- * in the caller's arrays).  Mode 1 uses complex128 and cuFFT Z2Z throughout. */
+/* FFTs of the recombination: mode 0 (default) runs double-float arithmetic
+ * on the FP32 units (complex128 only in the caller's arrays) when the
+ * transform lengths allow: yP_size and xM_yP_size powers of two 64..2048, the
+ * fused pipeline (prepare / window / crop steps inside the transforms); yP up
+ * to 8192 (four-step rows), the double-float stage kernels; otherwise power-
+ * of-two rows up to 2048 in double-float on complex128 stage arrays and other
+ * lengths with cuFFT Z2Z.  Mode 1 uses complex128 and cuFFT Z2Z throughout. */
 int cg_recombine_set_fft(cg_recombine *h, int mode);
 /* sizes[0..4] = xM_yP_size, xM_yN_size, facet_spacing, yP_spacing, xM_spacing */
 int cg_recombine_sizes(const cg_recombine *h, int32_t *sizes);

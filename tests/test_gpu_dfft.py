@@ -21,7 +21,7 @@ def env():
     return torch, engine, _lib, recombine, crocodile_oracle
 
 
-@pytest.mark.parametrize("n", [64, 128, 256, 512, 1024, 2048])
+@pytest.mark.parametrize("n", [64, 128, 256, 512, 1024, 2048, 4096, 8192])
 def test_rows_match_numpy(env, n):
     torch, E, L, R, O = env
     rng = numpy.random.default_rng(n)
@@ -33,8 +33,9 @@ def test_rows_match_numpy(env, n):
             want = numpy.fft.ifft(x, axis=1) * n if inverse else numpy.fft.fft(x, axis=1)
             got = t.cpu().numpy()
             # double-float carries about 48 bits: rounding ~1e-15 per stage
+            # (4096 and 8192: the four-step passes, 12 and 13 stages)
             err = numpy.abs(got - want).max() / numpy.abs(want).max()
-            assert err < 2e-14, (n, batch, inverse, err)
+            assert err < (2e-14 if n <= 2048 else 4e-14), (n, batch, inverse, err)
 
 
 def test_bad_lengths(env):
@@ -138,4 +139,40 @@ def test_recombination_tiny_double_float_vs_fp64(env):
     Fbb = torch.as_tensor(numpy.fft.fftshift(numpy.outer(Fb, Fb)), device="cuda")
     x = rc.subgrids_to_facet(spec64, so, so[:2], fo[1], fo[2]) / Fbb
     y = rc64.subgrids_to_facet(spec64, so, so[:2], fo[1], fo[2]) / Fbb
+    assert (x - y).abs().max().item() / y.abs().max().item() < 1e-10
+
+
+LONG_SETS = {
+    # bench_recombine.c's "small" (16k-8k-512) and the same at half scale: yP
+    # of 8192 and 4096, the four-step double-float rows
+    "small": (16384, 32, 5120, 5632, 8192, 416, 512, 280),
+    "half-small": (8192, 16, 2560, 2816, 4096, 208, 256, 140),
+}
+
+
+@pytest.mark.parametrize("name", ["half-small", "small"])
+def test_recombination_long_rows_vs_fp64(env, name):
+    """Sets whose yP is beyond one CTA's transform (4096, 8192): the
+    double-float stage kernels with the four-step rows against complex128
+    with FP64 cuFFT, both directions, and facet_add against the two calls."""
+    torch, E, L, R, O = env
+    N, sp, yB, yN, yP, xA, xM, xMxN = LONG_SETS[name]
+    rc = R.Recombine(N, sp, yB, yN, yP, xA, xM, xMxN)
+    rc64 = R.Recombine(N, sp, yB, yN, yP, xA, xM, xMxN, fft="fp64")
+    offs = [0, xA, N - xA]
+    g = torch.Generator(device="cuda").manual_seed(7)
+    facet = torch.randn((yB, yB), dtype=E.CD, device="cuda", generator=g)
+    a = rc.facet_to_subgrids(facet, offs, offs)
+    b = rc64.facet_to_subgrids(facet, offs, offs)
+    assert (a - b).abs().max().item() / b.abs().max().item() < 1e-10
+    approx = torch.zeros((3, 3, xM, xM), dtype=E.CD, device="cuda")
+    two = rc.add_facet(approx.clone(), a, sp * (N // sp // 4), 0)
+    one = rc.facet_add(approx.clone(), facet, offs, offs, sp * (N // sp // 4), 0)
+    assert torch.equal(one, two)
+    subs = torch.randn((3, 3, xM, xM), dtype=E.CD, device="cuda", generator=g)
+    spec = rc64.subgrid_spectra(subs)
+    Fb = rc.windows()[0]
+    Fbb = torch.as_tensor(numpy.fft.fftshift(numpy.outer(Fb, Fb)), device="cuda")
+    x = rc.subgrids_to_facet(spec, offs, offs, 0, 0) / Fbb
+    y = rc64.subgrids_to_facet(spec, offs, offs, 0, 0) / Fbb
     assert (x - y).abs().max().item() / y.abs().max().item() < 1e-10
