@@ -81,6 +81,9 @@ SIGNATURES = {
                                 P, P, P, P, P]),
     "cg_awtowers_combine": (c_int, [P, c_int, c_int, c_double, P, P, c_int, P, P, P, P, c_int, P,
                                     P, P]),
+    "cg_awtower_layers_workspace_bytes": (c_size_t, [c_int]),
+    "cg_awtower_layers": (c_int, [P, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
+                                  c_int, P, P, P, P, P, P, P, c_size_t, P]),
     "cg_awtowers_direct_workspace_bytes": (c_size_t, [c_int, c_int, c_int]),
     "cg_awtowers_direct": (c_int, [P, P, P, c_int, c_double, P, P, c_int, P, P, P, P, c_int, P,
                                    c_int, P, P, c_size_t, P, P]),

@@ -495,10 +495,12 @@ def measure_awtowers(steps=3):
     grids.  Timed end to end (binning, key compaction, plan, one gridder
     launch over every (chunk, plane, baseline) layer, batched FFTs, combine
     with the antenna ratios and Fresnel factors, sub-grid add)."""
-    w, src, aimage = awtowers_workload()
+    w, src_h, aimage_h = awtowers_workload()
     n = len(w.uvw)
     uvw = E.cuda_tensor(w.uvw, torch.float64)
     vis = E.cuda_tensor(w.vis, E.CF)
+    src = E.cuda_tensor(src_h, torch.int32)
+    aimage = E.cuda_tensor(aimage_h, E.CF)
     s, margin, wstep = 64, 16, w.params["wstep"]
     run = lambda: synthesis.aw_towers_imaging(w.theta, w.lam, uvw, src, vis, s, margin, wstep,
                                               aimage)
@@ -511,8 +513,9 @@ def measure_awtowers(steps=3):
     return {"workload": "AW-towers, %d visibilities (16 antennas, 125 hour angles x 16 "
                         "channels), 8192^2, 64^2 sub-grids margin 16, w step %.0f" % (n, wstep),
             "n_vis": n, "ms": ms, "mvis_s": n / ms / 1e3, "layers": int(used.shape[0]),
-            "note": "end to end from device-resident uvw / vis; parity with the reference "
-                    "notebook and the oracle in tests/test_gpu_awtowers.py"}
+            "note": "end to end from device-resident uvw, vis, antenna pairs and A-images; "
+                    "parity with the reference notebook and the oracle in "
+                    "tests/test_gpu_awtowers.py"}
 
 
 def ingest_blocks(seed=5, nant=64, ntime=125, nchan=64, npol=1):

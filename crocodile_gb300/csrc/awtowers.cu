@@ -168,6 +168,43 @@ __global__ void k_awtowers_combine(const float2 *__restrict__ stack, int s, doub
   if (bad && status) atomicAdd(&status[ST_RANGE], 1);
 }
 
+// ------------------------------------------------ layer bookkeeping
+// From the ascending distinct keys of the layers: each layer's antennas and
+// plane index, and a flag where a new chunk starts; then, from the flags'
+// exclusive scan, each chunk's first layer and its sub-grid origin
+//   (N/2 + C ub - C/2 - (margin + 1)/2, N/2 + C vb - C/2 - (margin + 1)/2),
+// the notebook's xy_min = C (ub - 1/2) - (margin + 1) // 2 (C even).
+__global__ void k_awt_layers(const int32_t *__restrict__ used, int nl, int nant, int nwp,
+                             int32_t *__restrict__ la1, int32_t *__restrict__ la2,
+                             int32_t *__restrict__ lplane, int32_t *__restrict__ flag) {
+  const int L = blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= nl) return;
+  const int nn = nant * nant;
+  const int k = used[L];
+  const int bl = k % nn, rest = k / nn;
+  la1[L] = bl / nant;
+  la2[L] = bl % nant;
+  lplane[L] = rest % nwp;
+  flag[L] = (L == 0 || rest / nwp != (used[L - 1] / nn) / nwp) ? 1 : 0;
+}
+
+__global__ void k_awt_chunks(const int32_t *__restrict__ used, int nl, int nant, int nwp,
+                             const int32_t *__restrict__ flag, const int32_t *__restrict__ scan,
+                             int nub, int ubmin, int vbmin, int C, int margin, int N,
+                             int32_t *__restrict__ chunk_first, int32_t *__restrict__ origin) {
+  const int L = blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= nl) return;
+  if (L == nl - 1) chunk_first[scan[L] + flag[L]] = nl;
+  if (!flag[L]) return;
+  const int c = scan[L];
+  const int ch = (used[L] / (nant * nant)) / nwp;
+  const int ub = ch % nub + ubmin, vb = ch / nub + vbmin;
+  const int corner = C / 2 + (margin + 1) / 2;
+  chunk_first[c] = L;
+  origin[2 * c] = N / 2 + C * ub - corner;
+  origin[2 * c + 1] = N / 2 + C * vb - corner;
+}
+
 // ------------------------------------------------ direct layer images
 // The layers' values at the cut without the 2s x 2s grids and their FFTs.
 // The anti-aliasing kernel is separable, so the unshifted inverse transform
@@ -465,6 +502,42 @@ int cg_awtowers_direct(const cg_plan *plan, const void *ktab_c64, const void *vi
   else CG_AWT_DIRECT(64);
 #undef CG_AWT_DIRECT
   CG_LAUNCH("AW-towers direct layers");
+  return CG_OK;
+}
+
+
+size_t cg_awtower_layers_workspace_bytes(int nlayers) {
+  const int n = std::max(nlayers, 1);
+  return (2 * (size_t)n + scan_scratch_words(n) + 64) * sizeof(int32_t);
+}
+
+int cg_awtower_layers(const int32_t *used, int nlayers, int nant, int nwp, int nub, int ubmin,
+                      int vbmin, int chunk, int margin, int N, int32_t *layer_a1,
+                      int32_t *layer_a2, int32_t *layer_plane, int32_t *chunk_first,
+                      int32_t *origin, int32_t *h_nchunks, void *ws, size_t ws_bytes,
+                      cg_stream_t stream) {
+  CG_REQUIRE(used && nlayers >= 1 && nant >= 1 && nwp >= 1 && nub >= 1 && chunk >= 2 &&
+                 chunk % 2 == 0 && margin >= 0 && layer_a1 && layer_a2 && layer_plane &&
+                 chunk_first && origin && h_nchunks,
+             "bad AW-tower layer arguments");
+  if (!ws || ws_bytes < cg_awtower_layers_workspace_bytes(nlayers))
+    return set_error(CG_ERR_WORKSPACE, "AW-tower layer workspace too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  int32_t *flag = (int32_t *)ws, *scan = flag + nlayers, *scratch = scan + nlayers;
+  const unsigned g = (unsigned)((nlayers + 255) / 256);
+  k_awt_layers<<<g, 256, 0, st>>>(used, nlayers, nant, nwp, layer_a1, layer_a2, layer_plane,
+                                  flag);
+  CG_LAUNCH("AW-tower layers");
+  int rc = launch_scan(flag, scan, nlayers, scratch, st);
+  if (rc) return rc;
+  k_awt_chunks<<<g, 256, 0, st>>>(used, nlayers, nant, nwp, flag, scan, nub, ubmin, vbmin, chunk,
+                                  margin, N, chunk_first, origin);
+  CG_LAUNCH("AW-tower chunks");
+  int32_t last[2];
+  CG_CUDA(cudaMemcpyAsync(&last[0], scan + nlayers - 1, 4, cudaMemcpyDeviceToHost, st));
+  CG_CUDA(cudaMemcpyAsync(&last[1], flag + nlayers - 1, 4, cudaMemcpyDeviceToHost, st));
+  CG_CUDA(cudaStreamSynchronize(st));
+  *h_nchunks = last[0] + last[1];
   return CG_OK;
 }
 

@@ -594,6 +594,25 @@ def awtowers_combine(stack, s, theta, corr, aimage, layer_a1, layer_a2, layer_w,
     return out
 
 
+def awtower_layers(used, nant, nwp, nub, ubmin, vbmin, chunk, margin, N):
+    """(layer_a1, layer_a2, layer_plane [nlayers], chunk_first [nchunks + 1], origin
+    [nchunks, 2]) as int32 CUDA tensors from the layers' ascending keys
+    (cg_awtower_layers)."""
+    used = cuda_tensor(used, torch.int32)
+    nl = int(used.shape[0])
+    a1, a2, lp = (torch.empty(nl, dtype=torch.int32, device="cuda") for _ in range(3))
+    cf = torch.empty(nl + 1, dtype=torch.int32, device="cuda")
+    org = torch.empty((nl, 2), dtype=torch.int32, device="cuda")
+    ws = torch.empty(L.lib().cg_awtower_layers_workspace_bytes(nl), dtype=torch.uint8,
+                     device="cuda")
+    nc = ctypes.c_int32()
+    L.call("cg_awtower_layers", _p(used), nl, int(nant), int(nwp), int(nub), int(ubmin),
+           int(vbmin), int(chunk), int(margin), int(N), _p(a1), _p(a2), _p(lp), _p(cf), _p(org),
+           ctypes.byref(nc), _p(ws), ws.numel(), stream())
+    n = nc.value
+    return a1, a2, lp, cf[:n + 1], org[:n]
+
+
 def awtowers_direct(plan, ktab, vis, s, theta, corr, aimage, layer_a1, layer_a2, layer_plane,
                     plane_w, chunk_first, status):
     """awtowers_combine's output formed directly from the plan's sorted visibilities

@@ -929,26 +929,18 @@ def aw_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wstep, ai
     st.check()
     nub, nvb, nwp = ubmax - ubmin + 1, vbmax - vbmin + 1, wpmax - wpmin + 1
     row, used = E.compact_keys(key, nub * nvb * nwp * nant * nant, st)
-    used = used.cpu().numpy().astype(numpy.int64)
-    bl, rest = used % (nant * nant), used // (nant * nant)
-    plane = rest % nwp + wpmin
-    # used is ascending, so each chunk's layers are one run
-    ch = rest // nwp
-    first = numpy.flatnonzero(numpy.r_[True, ch[1:] != ch[:-1]])
-    chunk = ch[first]
-    chunk_first = numpy.append(first, len(used)).astype(numpy.int32)
-    ub, vb = chunk % nub + ubmin, chunk // nub + vbmin
-    # the notebook's sub-grid corner: xy_min = C (ub - 1/2) - (margin + 1) // 2
-    xy = numpy.column_stack([C * (ub - 0.5), C * (vb - 0.5)]) - (margin + 1) // 2
-    origin = (N // 2 + xy.astype(int)).astype(numpy.int32)
+    # per layer its antennas and plane index, per chunk (a run of layers: used
+    # ascends) its first layer and the notebook's sub-grid corner
+    # xy_min = C (ub - 1/2) - (margin + 1) // 2, on the device
+    la1, la2, lplane, chunk_first, origin = E.awtower_layers(used, nant, nwp, nub, ubmin,
+                                                             vbmin, C, margin, N)
+    plane_w = (numpy.arange(nwp) + wpmin) * float(wstep)
     ktab, corr = _aw_towers_tables(N, s, int(aa_support), int(aa_over))
     plan = E.Plan(rel, s / theta, (2 * s, 2 * s), ktab, None, status=st,
                   layers=(len(used), row), tile=tile)
     if direct:
-        # plane index rest % nwp into the planes wpmin .. wpmax
-        sub = E.awtowers_direct(plan, ktab, vis_t, s, theta, corr, ai, bl // nant, bl % nant,
-                                (rest % nwp).astype(numpy.int32),
-                                (numpy.arange(nwp) + wpmin) * float(wstep), chunk_first, st)
+        sub = E.awtowers_direct(plan, ktab, vis_t, s, theta, corr, ai, la1, la2, lplane,
+                                plane_w, chunk_first, st)
         E.fft_raw(sub, False)
         E.towers_add(sub, origin, grid)
         st.check()
@@ -962,8 +954,8 @@ def aw_towers_imaging(theta, lam, uvw, src, vis, subgrid_size, margin, wstep, ai
     else:
         raise ValueError("gridder must be 'auto', 'tiled' or 'sparse'")
     E.fft_raw(stack, True)
-    sub = E.awtowers_combine(stack, s, theta, corr, ai, bl // nant, bl % nant,
-                             plane * float(wstep), chunk_first, st)
+    layer_w = E.cuda_tensor(plane_w, torch.float64)[lplane.long()]
+    sub = E.awtowers_combine(stack, s, theta, corr, ai, la1, la2, layer_w, chunk_first, st)
     del stack
     E.fft_raw(sub, False)
     E.towers_add(sub, origin, grid)

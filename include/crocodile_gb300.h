@@ -450,6 +450,18 @@ int cg_awtowers_combine(const void *stack_c64, int layers, int s, double theta,
                         const int32_t *layer_a1, const int32_t *layer_a2,
                         const double *layer_w, const int32_t *chunk_first, int nchunks,
                         void *out_c64, int32_t *d_status, cg_stream_t stream);
+/* The layer bookkeeping on the device, from used [nlayers], the ascending
+ * distinct keys of cg_awtower_keys (cg_compact_keys): each layer's antennas
+ * (layer_a1, layer_a2) and plane index key / nant^2 mod nwp (layer_plane),
+ * chunk_first [nchunks + 1] (room for nlayers + 1) and each chunk's sub-grid
+ * origin [nchunks][2] = N/2 + chunk*(ub, vb) - chunk/2 - (margin+1)/2 (room for
+ * 2 nlayers), *h_nchunks (host); synchronises the stream. */
+size_t cg_awtower_layers_workspace_bytes(int nlayers);
+int cg_awtower_layers(const int32_t *used, int nlayers, int nant, int nwp, int nub, int ubmin,
+                      int vbmin, int chunk, int margin, int N, int32_t *layer_a1,
+                      int32_t *layer_a2, int32_t *layer_plane, int32_t *chunk_first,
+                      int32_t *origin, int32_t *h_nchunks, void *ws, size_t ws_bytes,
+                      cg_stream_t stream);
 /* The same out[] without the 2s x 2s layer grids and their transforms, for
  * s = 16, 32 or 64: the anti-aliasing kernel being separable, the unshifted
  * inverse transform of a layer at the cut pixel (Ar, Br) is the sum over its
