@@ -229,20 +229,24 @@ def run_reference(args):
     probe.measure()
     rate, _ = probe.measure()
     probe.close()
-    sample = int(min(n, max(2000 * procs, rate * 1e6 * 90.0 / max(min(args.steps, 20), 1))))
+    steps, warm = min(args.steps, 20), max(args.warmup, 3)
+    sample = int(min(n, max(2000 * procs, rate * 1e6 * 90.0 / max(steps + warm, 1))))
     arm = CpuArm(args.workload, w, sample, procs)
     rates, secs = [], []
-    for i in range(min(args.steps, 20) + 1):
+    for i in range(steps + warm):
         r, dt = arm.measure()
-        if i:  # the first pass is a warm-up
+        if i >= warm:
             rates.append(r)
             secs.append(dt)
     arm.close()
     value = statistics.median(rates)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mvis/s",
-        "n_gpus": args.gpus, "steps": len(rates), "warmup": 1,
-        "ms_per_step": 1e3 * statistics.median(secs) * n / arm.sample,
+        "n_gpus": args.gpus, "steps": len(rates), "warmup": warm,
+        # one step is one bounded sample of the workload (its time as measured);
+        # the whole set's time at the same rate is given beside it
+        "ms_per_step": 1e3 * statistics.median(secs),
+        "ms_full_set_at_this_rate": 1e3 * statistics.median(secs) * n / arm.sample,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
         "data": "synthetic (seeded)",
         "config": {"workload": w.name, "n_vis": n, "N": w.N, "S": w.S, "Q": w.Q},
@@ -384,6 +388,18 @@ class GpuWorkload:
     def kernel_bytes_per_vis(self):
         return 0
 
+    def kernel_input_bytes(self):
+        """Bytes of the kernel inputs the step starts from, as complex64."""
+        return self.kt.table.numel() * 8
+
+    def algorithmic_bytes_step(self):
+        """Algorithmic bytes of one grid + degrid step, from the configuration's
+        parameters rather than this implementation's traffic: per visibility its
+        uvw (24 B), value in (8 B), kernel index (4 B) and predicted value out
+        (8 B); the N^2 complex64 grid written once and read once; the kernel
+        inputs."""
+        return self.n * (24 + 8 + 4 + 8) + 2 * self.N * self.N * 8 + self.kernel_input_bytes()
+
 
 class WProjGpu(GpuWorkload):
     def _prepare(self):
@@ -456,11 +472,20 @@ class AWGpu(GpuWorkload):
     def kernel_bytes_per_vis(self):
         return self.S * self.S * 8  # each visibility's AW kernel slice
 
+    def kernel_input_bytes(self):
+        """The A-kernels and the w sub-kernels the AW kernels are made from, as
+        complex64 (the AW table itself is derived data)."""
+        return (self.op.A.numel() + self.op.Wk.numel()) * 8
+
     def plain(self, steps):
         """(ms per plain FP64 step, FP32-vs-FP64 errors): the same AW kernels held as
         complex128, FP64 atomics, one launch per w-plane."""
         E, torch, op, w = self.E, self.torch, self.op, self.w
-        op.enable_fp64()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        op.enable_fp64()  # complex128 AW kernels, FP64 throughout, and the groups plan
+        torch.cuda.synchronize()
+        self.kgen64_ms = 1e3 * (time.perf_counter() - t0)
         vis64 = torch.from_numpy(w.vis).to(self.dev)
         g64 = torch.zeros((self.N, self.N), dtype=torch.complex128, device=self.dev)
         ms = []
@@ -483,6 +508,29 @@ class AWGpu(GpuWorkload):
         op.disable_fp64()
         torch.cuda.empty_cache()
         return (statistics.mean(ms),) + errs
+
+
+def update_peaks(G):
+    """Measured grid-point update peaks (updates/s): shared-memory float2
+    read-modify-write in the lane gridder's form, and float2 atomics into L2."""
+    torch, L = G.torch, G.L
+    buf = torch.empty(32 << 20, dtype=torch.uint8, device=G.dev)
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = {}
+    for name, kind, work in (("smem", 0, 4096), ("red", 1, 4096)):
+        u = ctypes.c_double()
+        L.call("cg_update_peak", kind, work, G.P(buf), buf.numel(), ctypes.byref(u), sp)
+        best = float("inf")
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            L.call("cg_update_peak", kind, work, G.P(buf), buf.numel(), ctypes.byref(u), sp)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        out[name] = u.value / (best * 1e-3)
+    del buf
+    return out
 
 
 def _rel(a, b):
@@ -656,10 +704,16 @@ def run_ours(args):
     torch.cuda.synchronize()
     kgen_warm_ms = 1e3 * (time.perf_counter() - t0)
 
-    # ---- roofline of the dominant kernel: algorithmic bytes per launch
+    # ---- roofline of the dominant kernel: the step's algorithmic bytes (inputs
+    # and outputs of grid + degrid from the configuration's parameters), half of
+    # them per direction; the bytes this implementation streams per launch (the
+    # kernel slice of every visibility) and the DRAM traffic ncu measured are
+    # reported beside them
+    alg_step = G.algorithmic_bytes_step()
+    alg = alg_step / 2
     kbytes = G.kernel_bytes_per_vis()
-    table_bytes = 0 if kbytes else G.kt.table.numel() * 8
-    alg = n * (16 + 4 + 8 + kbytes) + N * N * 8 + table_bytes
+    stream_bytes = n * (16 + 4 + 8 + kbytes) + N * N * 8 + (0 if kbytes
+                                                            else G.kt.table.numel() * 8)
     dom = "grid" if ms_grid >= ms_degrid else "degrid"
     dom_ms = max(ms_grid, ms_degrid)
     tuned = G.tuned
@@ -681,6 +735,11 @@ def run_ours(args):
         entry = json.load(open(tf)).get(args.workload, {}).get(kname)
         if entry:
             traffic = entry["bytes_per_launch"]
+
+    # ---- update rate: 2 n S^2 grid-point updates per step against the measured
+    # shared-memory update and L2 atomic peaks (microbenchmarks of cg_update_peak)
+    upeaks = update_peaks(G)
+    urate = 2 * n * S * S / (ms * 1e-3)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -724,11 +783,11 @@ def run_ours(args):
             a = cfg_results.get("awtowers")
             if a:
                 from oracle import crocodile_oracle as O
-                w, src, aimage = bench_configs.awtowers_workload()
-                sel = numpy.isin(src[:, 0] * 16 + src[:, 1], [1, 2, 17])[:len(w.uvw)]
+                wt, src, aimage = bench_configs.awtowers_workload()
+                sel = numpy.isin(src[:, 0] * 16 + src[:, 1], [1, 2, 17])[:len(wt.uvw)]
                 t0 = time.perf_counter()
-                O.aw_towers_imaging(w.theta, w.lam, w.uvw[sel], src[sel], w.vis[sel], 64, 16,
-                                    w.params["wstep"], aimage)
+                O.aw_towers_imaging(wt.theta, wt.lam, wt.uvw[sel], src[sel], wt.vis[sel], 64, 16,
+                                    wt.params["wstep"], aimage)
                 dt = time.perf_counter() - t0
                 a["cpu_oracle"] = {"mvis_s": int(sel.sum()) / dt / 1e6, "cores": 1, "kind": "port",
                                    "sample": "3 of 120 baselines (%d visibilities), %.2f s"
@@ -756,18 +815,39 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "kernel": kname,
                      "algorithmic_bytes": alg, "ms": dom_ms,
+                     "algorithmic_bytes_def": "half of one grid+degrid step's n*(24 uvw + 8 vis "
+                                              "+ 4 kernel index + 8 vis out) + 2*N^2*8 grid + "
+                                              "kernel inputs (complex64)",
+                     "step": {"algorithmic_bytes": alg_step, "ms": ms,
+                              "achieved": alg_step / (ms * 1e-3) / 1e9,
+                              "frac": alg_step / (ms * 1e-3) / 1e9 / peak},
+                     "streamed_bytes_per_launch": stream_bytes,
+                     "streamed_bytes_def": "n*(16 record + 4 index + 8 value + %d kernel slice) + "
+                                           "N^2*8: what this gridder reads per launch" % kbytes,
+                     "traffic_over_algorithmic": traffic / alg if traffic else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks
                      else "fallback 6800 GB/s"},
+        "update_roofline": {"updates_per_s": urate, "updates_per_step": 2 * n * S * S,
+                            "peak_smem_updates_per_s": upeaks["smem"],
+                            "frac_of_smem_peak": urate / upeaks["smem"],
+                            "peak_l2_atomic_updates_per_s": upeaks["red"],
+                            "frac_of_l2_atomic_peak": urate / upeaks["red"],
+                            "peak_source": "cg_update_peak microbenchmarks run in this process "
+                                           "(shared-memory float2 read-modify-write in the lane "
+                                           "gridder's form; float2 red.global.add into a 32 MiB "
+                                           "L2-resident buffer), best of 5 CUDA-event timings"},
         "launch": launch, "ms_per_step_eager": ms_eager,
         "kernel_ms": {"grid": ms_grid, "degrid": ms_degrid,
                       "plan_and_grid_zeroing": ms_eager - ms_grid - ms_degrid,
                       "kernel_generation_once": G.kgen_ms,
-                      "kernel_generation_warm": kgen_warm_ms},
-        "updates_per_s": 2 * n * S * S / (ms * 1e-3),
+                      "kernel_generation_warm": kgen_warm_ms,
+                      "kernel_generation_fp64": getattr(G, "kgen64_ms", None)},
         "plain_fp64": {"value": plain_value, "unit": "Mvis/s", "ms_per_step": ms_plain,
                        "form": "complex128, FP64 atomics, " + G.groups_desc},
         "speedup_vs_plain": value / plain_value,
-        "rel_err_vs_fp64": {"grid": err_grid, "degrid": err_degrid},
+        "rel_err_vs_fp64": {"grid": err_grid, "degrid": err_degrid,
+                            "against": "the plain FP64 form with complex128 kernels generated "
+                                       "in FP64 throughout (kernel generation error included)"},
         "fused": {"value": n / (ms_fused * 1e-3) / 1e6, "unit": "Mvis/s", "ms_per_step": ms_fused,
                   "form": "plan + one degrid+grid pass (cg_degrid_grid), each kernel tap read "
                           "once", "speedup_vs_plain": ms_plain / ms_fused},

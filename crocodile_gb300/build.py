@@ -34,7 +34,8 @@ def sources():
 
 
 def _deps():
-    files = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    files = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC)
+                         if f.endswith(".cuh") or f.endswith(".h")]
     files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     return files
 

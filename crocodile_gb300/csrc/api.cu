@@ -2,6 +2,7 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "cg_internal.cuh"
@@ -42,6 +43,12 @@ cg_tuning tuning() {
   return g_tuning;
 }
 
+// Clock-cycle limit of the gridders' bounded waits on bulk copies (about two
+// seconds at 2 GHz); lowered only by tests that make a wait run out.
+static std::atomic<long long> g_wait_cycles{4000000000ll};
+
+long long wait_cycles() { return g_wait_cycles.load(std::memory_order_relaxed); }
+
 // The tuned layout, or automatically the lane layout for tables whose S x S
 // slices stream by bulk copies (non-separable, even S <= 16) and the warp
 // layout otherwise.  The lane layout needs S <= 16.
@@ -70,6 +77,14 @@ int cg_set_tuning(const cg_tuning *t) {
   cg::g_tuning = *t;
   return CG_OK;
 }
+
+int cg_set_wait_limit(long long cycles) {
+  CG_REQUIRE(cycles >= 0, "wait limit %lld must be >= 0", cycles);
+  cg::g_wait_cycles.store(cycles, std::memory_order_relaxed);
+  return CG_OK;
+}
+
+long long cg_get_wait_limit(void) { return cg::wait_cycles(); }
 
 int cg_get_tuning(cg_tuning *out) {
   CG_REQUIRE(out, "output is NULL");

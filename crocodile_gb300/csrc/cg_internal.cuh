@@ -6,6 +6,7 @@
 #include <stdio.h>
 
 #include "../../include/crocodile_gb300.h"
+#include "tile_order.h"
 
 namespace cg {
 
@@ -32,6 +33,7 @@ enum { ST_RANGE = 0, ST_BOUNDS = 1, ST_INDEX = 2, ST_TIMEOUT = 3 };
 
 int num_sms();
 cg_tuning tuning();  // current process-wide launch-shape tuning
+long long wait_cycles();  // clock limit of the bounded waits on bulk copies
 int layout_for(const cg_kernel_desc &kd);  // gridder layout used for this kernel table
 
 // ---------------------------------------------------------------- device helpers
@@ -207,7 +209,9 @@ struct cg_plan {
   int nbuckets;
   int layers;   // stacked grids (w-stacking planes); a grid of H*W cells each
   int gper;     // groups mode: buckets per layer (launch groups, or kernel groups)
-  int tpl;      // tiles per layer (ntx * nty)
+  int tblog;    // tiles are numbered in Morton order inside blocks of 2^tblog x 2^tblog tiles
+  int nbx;      // tile blocks per row
+  int tpl;      // tile numbers per layer (whole blocks: nbx * nby * 4^tblog >= ntx * nty)
   int ntiles;   // tiled mode: tiles of all layers; each holds 4^sublog sub-tile buckets
   int sublog;   // 2^sublog sub-tiles per tile edge, ordered along a Morton curve
   int subshift; // sub-tile edge = 1 << subshift cells (4, or more for huge grid stacks)

@@ -43,6 +43,7 @@ struct LaneArgs {
   const float2 *grid_in;  // fused: grid to degrid
   float2 *vis_out;        // fused: degridded visibilities (may be NULL)
   int mode;               // gridding: 0 vis, 1 vis * weight, 2 weight; fused: 0 plain, 1 residual
+  long long wait_cycles;  // limit of a consumer's wait for a slice (the drain keeps LANE_WAIT_CYCLES)
   int warp_bytes;         // shared memory per warp
   int stage_off, meta_off, val_off, bar_off;  // byte offsets inside a warp's region
 };
@@ -237,7 +238,7 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
         bool ok = mbar_try(&bar[cst], cpar);
         if (!__all_sync(FULL_MASK, ok)) {  // warp-uniform slow path, bounded
           const long long t0 = clock64();
-          while (!ok && clock64() - t0 <= LANE_WAIT_CYCLES) ok = mbar_try(&bar[cst], cpar);
+          while (!ok && clock64() - t0 <= P.wait_cycles) ok = mbar_try(&bar[cst], cpar);
           if (__any_sync(FULL_MASK, !ok)) return false;
         }
         const float2 *kp = stages + (size_t)cst * SS + lane;
@@ -396,6 +397,7 @@ int lane_launch(const cg_plan *p, const float2 *ktab, const float2 *vis, const f
   P.grid_in = grid_in;
   P.vis_out = vis_out;
   P.mode = fused ? (residual ? 1 : 0) : gmode;
+  P.wait_cycles = wait_cycles();
   auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
   size_t off = up16((size_t)p->pitch * p->win * sizeof(float2));
   P.stage_off = (int)off;

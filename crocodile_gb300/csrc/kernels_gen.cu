@@ -190,13 +190,13 @@ static int oversample_run(FarField F, int batch, int s, void *out, bool out_c64,
 // sub-kernels f, FP32 products with FP32 accumulation, one CTA per (k, f).
 // 'same' keeps the size of the first operand, centred on the full output:
 //   same[i, j] = sum_{p, q} a[p, q] * b[i + o - p, j + o - q],  o = (nb - 1) / 2.
-// R: the accumulation type.  double for complex128 output (the reference's
-// FP64); float for the complex64 tables, whose convolutions that follow run
-// in FP32 anyway.
-template <typename R>
+// R: the accumulation type, C: the stored type.  double / double2 for
+// complex128 output (the reference's FP64 throughout); float / float2 for the
+// complex64 tables, whose convolutions that follow run in FP32 anyway.
+template <typename R, typename C>
 __global__ void k_aw_akern(const double2 *__restrict__ A, int SA,
                            const int32_t *__restrict__ a1, const int32_t *__restrict__ a2,
-                           int nA, float2 *__restrict__ akern, int32_t *status) {
+                           int nA, C *__restrict__ akern, int32_t *status) {
   const int k = blockIdx.x;
   const int i1 = a1[k], i2 = a2[k];
   if (i1 < 0 || i1 >= nA || i2 < 0 || i2 >= nA) {
@@ -230,7 +230,10 @@ __global__ void k_aw_akern(const double2 *__restrict__ A, int SA,
         ay += ux * vy + uy * vx;
       }
     }
-    akern[(size_t)k * SA * SA + t] = make_float2((float)ax, (float)ay);  // FP32 from here on
+    C r;
+    r.x = ax;
+    r.y = ay;
+    akern[(size_t)k * SA * SA + t] = r;
   }
 }
 
@@ -347,6 +350,108 @@ __global__ void __launch_bounds__(SAC *(SAC / JB)) k_aw_conv_blocked(
   }
 }
 
+// The complex128 AW kernels in FP64 throughout: A1 (*) A2 and the w
+// sub-kernels as double2, products and sums in FP64 (the reference's
+// scipy.signal.convolve2d of complex128 arrays).  A thread computes JB
+// neighbouring outputs of one row; for each A row p it holds the S + JB - 1
+// w values that row needs in registers (columns outside [0, S) read as
+// zero), so one A tap feeds JB complex multiply-adds.  SA = SAC, S <= SAC.
+template <int SAC, int JB>
+__global__ void __launch_bounds__(SAC *(SAC / JB)) k_aw_conv64(
+    const double2 *__restrict__ akern, const double2 *__restrict__ Wk, int nW, int Q, int S,
+    const int32_t *__restrict__ wi, double2 *__restrict__ out, int32_t *status) {
+  extern __shared__ double2 sh64[];
+  double2 *sa = sh64, *sw = sh64 + SAC * SAC;
+  const int k = blockIdx.y, f = blockIdx.x;  // f = yf*Q + xf
+  const int w = wi[k];
+  if (w < 0 || w >= nW) {
+    if (threadIdx.x == 0 && f == 0) atomicAdd(&status[ST_INDEX], 1);
+    return;
+  }
+  if ((status[ST_RANGE] | status[ST_INDEX]) != 0) return;
+  const double2 *ak = akern + (size_t)k * SAC * SAC;
+  const double2 *wk = Wk + ((size_t)w * Q * Q + f) * S * S;
+  for (int t = threadIdx.x; t < SAC * SAC; t += blockDim.x) sa[t] = ak[t];
+  const int SP = S + 1;  // odd pitch against bank conflicts
+  for (int t = threadIdx.x; t < S * S; t += blockDim.x) {
+    const int r = t / S, c = t - (t / S) * S;
+    sw[r * SP + c] = wk[t];
+  }
+  __syncthreads();
+  const int o = (S - 1) / 2;
+  const int i = threadIdx.x / (SAC / JB), j0 = (threadIdx.x % (SAC / JB)) * JB;
+  double ax[JB], ay[JB];
+#pragma unroll
+  for (int d = 0; d < JB; ++d) ax[d] = ay[d] = 0.0;
+  const int p_lo = max(0, i + o - (S - 1)), p_hi = min(SAC - 1, i + o);
+  const int c0 = j0 + o - (SAC - 1);  // w column of register m = c0 + m
+  for (int p = p_lo; p <= p_hi; ++p) {
+    const double2 *wrow = sw + (i + o - p) * SP;
+    double2 wv[SAC + JB - 1];
+#pragma unroll
+    for (int m = 0; m < SAC + JB - 1; ++m) {
+      const int c = c0 + m;
+      wv[m] = (c >= 0 && c < S) ? wrow[c] : make_double2(0.0, 0.0);
+    }
+    const double2 *arow = sa + p * SAC;
+#pragma unroll
+    for (int q = 0; q < SAC; ++q) {
+      const double2 u = arow[q];
+#pragma unroll
+      for (int d = 0; d < JB; ++d) {  // w column j0 + d + o - q is register d + SAC - 1 - q
+        const double2 v = wv[d + SAC - 1 - q];
+        ax[d] = fma(u.x, v.x, ax[d]);
+        ax[d] = fma(-u.y, v.y, ax[d]);
+        ay[d] = fma(u.x, v.y, ay[d]);
+        ay[d] = fma(u.y, v.x, ay[d]);
+      }
+    }
+  }
+  double2 *dst = out + ((size_t)k * Q * Q + f) * SAC * SAC + i * SAC + j0;
+#pragma unroll
+  for (int d = 0; d < JB; ++d) dst[d] = make_double2(ax[d], ay[d]);
+}
+
+// Any SA: one output per thread, FP64 sums over the 'same' support.
+__global__ void k_aw_conv64_any(const double2 *__restrict__ akern, int SA,
+                                const double2 *__restrict__ Wk, int nW, int Q, int S,
+                                const int32_t *__restrict__ wi, double2 *__restrict__ out,
+                                int32_t *status) {
+  extern __shared__ double2 sh64[];
+  double2 *sa = sh64, *sw = sh64 + SA * SA;
+  const int k = blockIdx.y, f = blockIdx.x;
+  const int w = wi[k];
+  if (w < 0 || w >= nW) {
+    if (threadIdx.x == 0 && f == 0) atomicAdd(&status[ST_INDEX], 1);
+    return;
+  }
+  if ((status[ST_RANGE] | status[ST_INDEX]) != 0) return;
+  const double2 *ak = akern + (size_t)k * SA * SA;
+  const double2 *wk = Wk + ((size_t)w * Q * Q + f) * S * S;
+  for (int t = threadIdx.x; t < SA * SA; t += blockDim.x) sa[t] = ak[t];
+  for (int t = threadIdx.x; t < S * S; t += blockDim.x) sw[t] = wk[t];
+  __syncthreads();
+  const int o = (S - 1) / 2;
+  double2 *dst = out + ((size_t)k * Q * Q + f) * SA * SA;
+  for (int t = threadIdx.x; t < SA * SA; t += blockDim.x) {
+    const int i = t / SA, j = t - (t / SA) * SA;
+    double ax = 0.0, ay = 0.0;
+    const int p_lo = max(0, i + o - (S - 1)), p_hi = min(SA - 1, i + o);
+    const int q_lo = max(0, j + o - (S - 1)), q_hi = min(SA - 1, j + o);
+    for (int p = p_lo; p <= p_hi; ++p) {
+      const double2 *wrow = sw + (i + o - p) * S;
+      for (int q = q_lo; q <= q_hi; ++q) {
+        const double2 u = sa[p * SA + q], v = wrow[j + o - q];
+        ax = fma(u.x, v.x, ax);
+        ax = fma(-u.y, v.y, ax);
+        ay = fma(u.x, v.y, ay);
+        ay = fma(u.y, v.x, ay);
+      }
+    }
+    dst[t] = make_double2(ax, ay);
+  }
+}
+
 }  // namespace cg
 
 using namespace cg;
@@ -422,11 +527,13 @@ __global__ void k_c128_to_c64(const double2 *__restrict__ in, int64_t n, float2 
     out[t] = make_float2((float)in[t].x, (float)in[t].y);
 }
 
-// Workspace: the FP32 A1 (*) A2 kernels [nk, SA, SA], then the w sub-kernels
-// converted once to FP32 [nW, Q, Q, S, S] (the convolution blocks read both
-// many times; converting per block would load the narrow FP64 pipe).
+// Workspace: the A1 (*) A2 kernels [nk, SA, SA] (FP32 for complex64 tables,
+// FP64 for complex128 ones; room for FP64), then for complex64 tables the w
+// sub-kernels converted once to FP32 [nW, Q, Q, S, S] (the convolution blocks
+// read both many times; converting per block would load the narrow FP64 pipe)
+// or the FFT form's spectra.
 static size_t aw_ws_akern_bytes(int nk, int SA) {
-  return ((size_t)std::max(nk, 1) * SA * SA * sizeof(float2) + 255) & ~(size_t)255;
+  return ((size_t)std::max(nk, 1) * SA * SA * sizeof(double2) + 255) & ~(size_t)255;
 }
 
 size_t cg_aw_kernels_workspace_bytes(int nk, int SA, int nW, int Q, int S) {
@@ -448,25 +555,41 @@ int cg_aw_kernels(const void *A, int nA, int SA, const void *Wk, int nW, int Q, 
   if (!ws || ws_bytes < need)
     return set_error(CG_ERR_WORKSPACE, "aw_kernels needs %zu workspace bytes", need);
   cudaStream_t st = (cudaStream_t)stream;
+  if (!out_c64) {  // complex128 tables: FP64 throughout
+    double2 *akern64 = (double2 *)ws;
+    const size_t sh_a = 4 * (size_t)SA * SA * sizeof(double);
+    if (sh_a > 48 * 1024)
+      CG_CUDA(cudaFuncSetAttribute(k_aw_akern<double, double2>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh_a));
+    k_aw_akern<double, double2><<<nk, 256, sh_a, st>>>((const double2 *)A, SA, a1, a2, nA,
+                                                       akern64, d_status);
+    CG_LAUNCH("aw akern (FP64)");
+    dim3 grid(Q * Q, nk);
+    if (SA == 16 && S <= 16) {
+      const size_t smem = (size_t)(SA * SA + S * (S + 1)) * sizeof(double2);
+      k_aw_conv64<16, 4><<<grid, 64, smem, st>>>(akern64, (const double2 *)Wk, nW, Q, S, wi,
+                                                 (double2 *)out, d_status);
+    } else {
+      const size_t smem = (size_t)(SA * SA + S * S) * sizeof(double2);
+      if (smem > 48 * 1024)
+        CG_CUDA(cudaFuncSetAttribute(k_aw_conv64_any, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+      k_aw_conv64_any<<<grid, 256, smem, st>>>(akern64, SA, (const double2 *)Wk, nW, Q, S, wi,
+                                               (double2 *)out, d_status);
+    }
+    CG_LAUNCH("aw conv (FP64)");
+    return CG_OK;
+  }
   float2 *akern = (float2 *)ws;
   float2 *wk32 = (float2 *)((char *)ws + aw_ws_akern_bytes(nk, SA));
-  const bool fft_form = out_c64 && aw_fft_supported(SA, S);
-  // shared staging of the two A kernels: up to 128 KB at SA = 64 in FP64
-  const size_t sh_a = 4 * (size_t)SA * SA * (fft_form ? sizeof(float) : sizeof(double));
-  if (sh_a > 48 * 1024) {
-    if (fft_form)
-      CG_CUDA(cudaFuncSetAttribute(k_aw_akern<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)sh_a));
-    else
-      CG_CUDA(cudaFuncSetAttribute(k_aw_akern<double>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh_a));
-  }
-  if (fft_form)
-    k_aw_akern<float><<<nk, 256, sh_a, st>>>((const double2 *)A, SA, a1, a2, nA, akern,
-                                             d_status);
-  else
-    k_aw_akern<double><<<nk, 256, sh_a, st>>>((const double2 *)A, SA, a1, a2, nA, akern,
-                                              d_status);
+  const bool fft_form = aw_fft_supported(SA, S);
+  // shared staging of the two A kernels in FP32: up to 64 KB at SA = 64
+  const size_t sh_a = 4 * (size_t)SA * SA * sizeof(float);
+  if (sh_a > 48 * 1024)
+    CG_CUDA(cudaFuncSetAttribute(k_aw_akern<float, float2>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh_a));
+  k_aw_akern<float, float2><<<nk, 256, sh_a, st>>>((const double2 *)A, SA, a1, a2, nA, akern,
+                                                   d_status);
   CG_LAUNCH("aw akern");
   if (fft_form)  // complex64 tables: the FFT form
     return aw_fft_launch(akern, nk, Wk, nW, Q, S, wi, out, 1,
@@ -480,21 +603,13 @@ int cg_aw_kernels(const void *A, int nA, int SA, const void *Wk, int nW, int Q, 
   dim3 grid(Q * Q, nk);
   if (SA == 16) {  // the AW kernels' size: register-blocked form, 4 outputs per thread
     const size_t smem_b = (size_t)(SA * SA + S * (S + 1)) * sizeof(float2);
-    if (out_c64)
-      k_aw_conv_blocked<float2, 16, 4><<<grid, 64, smem_b, st>>>(
-          akern, wk32, nW, Q, S, wi, (float2 *)out, d_status);
-    else
-      k_aw_conv_blocked<double2, 16, 4><<<grid, 64, smem_b, st>>>(
-          akern, wk32, nW, Q, S, wi, (double2 *)out, d_status);
+    k_aw_conv_blocked<float2, 16, 4><<<grid, 64, smem_b, st>>>(akern, wk32, nW, Q, S, wi,
+                                                               (float2 *)out, d_status);
     CG_LAUNCH("aw conv");
     return CG_OK;
   }
-  if (out_c64)
-    k_aw_conv<float2><<<grid, 256, smem, st>>>(akern, SA, wk32, nW, Q, S, wi,
-                                               (float2 *)out, d_status);
-  else
-    k_aw_conv<double2><<<grid, 256, smem, st>>>(akern, SA, wk32, nW, Q, S, wi,
-                                                (double2 *)out, d_status);
+  k_aw_conv<float2><<<grid, 256, smem, st>>>(akern, SA, wk32, nW, Q, S, wi, (float2 *)out,
+                                             d_status);
   CG_LAUNCH("aw conv");
   return CG_OK;
 }

@@ -16,7 +16,9 @@
 // it keeps what the last call left there: each call re-zeroes the counters and
 // histograms it accumulates into before using them, and calls that overlap on
 // the GPU (different streams, or different host threads on one device) race
-// on it and must be serialised by the caller.
+// on it and must be serialised by the caller.  The device address of the
+// array is looked up once per device and cached; cudaDeviceReset in the same
+// process invalidates it, so calls after a device reset are not supported.
 #include <string.h>
 
 #include <mutex>
@@ -69,8 +71,11 @@ extern "C" int cg_grid_noalloc(const cg_kernel_desc *kd, int H, int W, const dou
   int rc = scratch_address(&ws);
   if (rc) return rc;
   cg_plan plan;
-  rc = cg::plan_build_tiled_into(&plan, kd, H, W, uvw, stride, lam, kidx, n, ws, need,
-                                 d_status, (cudaStream_t)stream);
+  // the whole array as the workspace: the build re-derives the layout from the
+  // current tuning and checks its own need against this size
+  rc = cg::plan_build_tiled_into(&plan, kd, H, W, uvw, stride, lam, kidx, n, ws,
+                                 (size_t)CG_NOALLOC_SCRATCH_BYTES, d_status,
+                                 (cudaStream_t)stream);
   if (rc) return rc;
   return cg_grid(&plan, ktab_c64, vis_c64, grid_c64, stream);
 }

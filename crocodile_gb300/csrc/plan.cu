@@ -121,7 +121,7 @@ struct CoordParams {
   int64_t n;
   int H, W, Q, S, G, sep;
   const int32_t *kidx;
-  int mode, T, ntx, nbuckets, sublog, subshift;
+  int mode, T, tblog, nbx, nbuckets, sublog, subshift;
   const int32_t *layer;  // per-visibility layer (grid of the stack), or NULL
   int layers, tpl;
   const int32_t *group;  // groups mode: per-visibility launch group, or NULL (= kernel group)
@@ -151,23 +151,16 @@ __device__ __forceinline__ int aggregated_slot(int32_t *hist, int key,
 
 // Interleave the low 8 bits of x and y (Morton / Z order).
 __device__ __forceinline__ int morton2(int x, int y) {
-  unsigned a = (unsigned)x & 0xffu, b = (unsigned)y & 0xffu;
-  a = (a | (a << 4)) & 0x0f0fu;
-  a = (a | (a << 2)) & 0x3333u;
-  a = (a | (a << 1)) & 0x5555u;
-  b = (b | (b << 4)) & 0x0f0fu;
-  b = (b | (b << 2)) & 0x3333u;
-  b = (b | (b << 1)) & 0x5555u;
-  return (int)(a | (b << 1));
+  return (int)(spread_bits((unsigned)x) | (spread_bits((unsigned)y) << 1));
 }
 
-// Tiled-mode bucket: tile, then the 4x4-cell sub-tile of the footprint
-// origin along a Morton curve, so that consecutive visibilities of a work
-// item are spatial neighbours.
+// Tiled-mode bucket: tile (numbered along the blocked Morton curve), then the
+// 4x4-cell sub-tile of the footprint origin along a Morton curve, so that
+// consecutive visibilities of a work item are spatial neighbours.
 __device__ __forceinline__ int tile_bucket(const CoordParams &P, int lyr, int x0, int y0) {
   const int ty = y0 / P.T, tx = x0 / P.T;
   const int ly = y0 - ty * P.T, lx = x0 - tx * P.T;
-  return ((lyr * P.tpl + ty * P.ntx + tx) << (2 * P.sublog)) |
+  return ((lyr * P.tpl + tile_index(tx, ty, P.tblog, P.nbx)) << (2 * P.sublog)) |
          morton2(lx >> P.subshift, ly >> P.subshift);
 }
 
@@ -431,7 +424,11 @@ static void plan_geometry(cg_plan &p) {
     p.T = tile_edge(p.kd, p.tile_req);
     p.ntx = (p.W + p.T - 1) / p.T;
     p.nty = (p.H + p.T - 1) / p.T;
-    p.tpl = p.ntx * p.nty;
+    // Morton blocks of up to 32 x 32 tiles (no larger than the grid needs)
+    p.tblog = tile_block_log(p.ntx, p.nty);
+    p.nbx = (p.ntx + (1 << p.tblog) - 1) >> p.tblog;
+    const int nby = (p.nty + (1 << p.tblog) - 1) >> p.tblog;
+    p.tpl = (p.nbx * nby) << (2 * p.tblog);
     p.ntiles = p.tpl * p.layers;
     const cg_tuning t = tuning();
     // 4x4-cell sub-tiles, 2^sublog per tile edge (4 << full >= T), except for the
@@ -464,6 +461,8 @@ static void plan_geometry(cg_plan &p) {
   } else {
     p.T = 0;
     p.ntx = p.nty = 0;
+    p.tblog = 0;
+    p.nbx = 1;
     p.tpl = 1;
     p.nbuckets = p.gper * p.layers;
     p.win = p.pitch = 0;
@@ -567,7 +566,8 @@ int plan_build_into(cg_plan *p, int mode, const cg_kernel_desc *kd, int H, int W
   P.kidx = kidx;
   P.mode = mode;
   P.T = p->T;
-  P.ntx = p->ntx;
+  P.tblog = p->tblog;
+  P.nbx = p->nbx;
   P.nbuckets = p->nbuckets;
   P.sublog = p->sublog;
   P.subshift = p->subshift;

@@ -13,7 +13,7 @@ struct TiledArgs {
   const int32_t *nitems;
   int32_t *ticket;
   const int32_t *status;
-  int H, W, S, Q, T, ntx, tpl, win, pitch;
+  int H, W, S, Q, T, tblog, nbx, tpl, win, pitch;
 };
 
 // Window origin of a work item's tile and the offset of its layer's grid.
@@ -23,9 +23,11 @@ struct TileOrigin {
 };
 __device__ __forceinline__ TileOrigin tile_origin(const TiledArgs &A, int tile) {
   const int lyr = tile / A.tpl, t = tile - lyr * A.tpl;
+  int tx, ty;
+  tile_xy(t, A.tblog, A.nbx, tx, ty);
   TileOrigin o;
-  o.wx0 = (t % A.ntx) * A.T;
-  o.wy0 = (t / A.ntx) * A.T;
+  o.wx0 = tx * A.T;
+  o.wy0 = ty * A.T;
   o.layer_off = (size_t)lyr * A.H * A.W;
   return o;
 }
@@ -66,7 +68,8 @@ inline TiledArgs tiled_args(const cg_plan *p) {
   A.S = p->kd.S;
   A.Q = p->kd.Q;
   A.T = p->T;
-  A.ntx = p->ntx;
+  A.tblog = p->tblog;
+  A.nbx = p->nbx;
   A.tpl = p->tpl;
   A.win = p->win;
   A.pitch = p->pitch;

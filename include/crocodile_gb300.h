@@ -119,6 +119,16 @@ typedef struct {
 int cg_set_tuning(const cg_tuning *t);
 int cg_get_tuning(cg_tuning *out);
 
+/* The lane gridders wait for each kernel slice's bulk copy for at most this
+ * many SM clock cycles (default 4e9, about two seconds); a wait that runs out
+ * counts CG_ERR_TIMEOUT in the status block, the warp lets its copies in
+ * flight land (waiting at most the default limit) and stops, and the call
+ * returns.  No counterpart in the reference: a test hook that makes a wait
+ * run out on purpose (a limit of 0 fails every copy not yet landed when it
+ * is first polled).  Process-wide. */
+int cg_set_wait_limit(long long cycles);
+long long cg_get_wait_limit(void);
+
 /* A plan holds the visibilities' bit-exact cell assignment, their order
  * (sorted into grid tiles, or into kernel groups for the plain FP64 form)
  * and the work list of the gridding kernels.  It lives in a caller-owned
@@ -221,6 +231,20 @@ int cg_degrid_grid(const cg_plan *plan, const void *ktab_c64,
                    const void *grid_in_c64, const void *vis_in_c64, int residual,
                    void *vis_out_c64, void *grid_out_c64, cg_stream_t stream);
 
+/* cg_update_peak: no counterpart in the reference (a measurement utility).
+ * One launch of an update-rate microbenchmark, the peaks that the gridders'
+ * grid-point update rate is compared with.  kind 0: shared-memory
+ * read-modify-write updates of float2 cells, the lane gridder's inner loop
+ * without its HBM traffic (per warp a private 31 x 32 window and a 16 x 16
+ * tap slice in shared memory; `work` synthetic visibilities of 256 updates
+ * per warp; buf receives one value per warp, >= 8 * 16 * SMs bytes).
+ * kind 1: float2 atomic additions into an L2-resident buffer (red.global.add
+ * of 32 consecutive cells per warp instruction; `work` instructions per warp;
+ * buf >= 256 KiB, at most 32 MiB of it used).  *updates receives the cell
+ * updates the launch performs; time it with events on `stream`. */
+int cg_update_peak(int kind, int work, void *buf, size_t buf_bytes, double *updates,
+                   cg_stream_t stream);
+
 /* cg_grid_noalloc: no counterpart in the reference.  For callers that
  * cannot allocate device memory (a pipeline that owns all GPU memory in its
  * own pool and may not call cudaMalloc/cudaFree while it runs, or an FFI
@@ -231,12 +255,20 @@ int cg_degrid_grid(const cg_plan *plan, const void *ktab_c64,
  * Allocates nothing, on the host or the device.  Inputs and outputs are the
  * caller's device buffers, as for cg_grid; d_status is the caller's status
  * block.  Returns CG_ERR_WORKSPACE, writing nothing, when n visibilities on
- * an H x W grid need more scratch than that (cg_plan_workspace_bytes gives
- * the need; about 16 MiB / 44 B = 380 000 visibilities).
+ * an H x W grid need more scratch than that.  The need depends on n, the grid
+ * and the gridder layout; cg_plan_workspace_bytes(CG_PLAN_TILED, ...) gives
+ * it.  It is about 44 B per visibility plus the bucket tables and work
+ * list: about H * W / 10 bytes for the lane layout (non-separable tables,
+ * even S <= 16), but H * W / 2 bytes for the warp and owner layouts (4 x
+ * 4-cell sub-tile buckets), which alone exceed the array above about
+ * 5800 x 5800.  So a 512 x 512 grid takes up to about 380 000 visibilities,
+ * a 4096 x 4096 grid about 345 000 with the lane layout but only about
+ * 190 000 with the others.
  * The first call on a device looks up the array's device address, once per
  * device, with that device current; make that first call before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race
- * and must be serialised by the caller. */
+ * capture.  The address stays cached, so calls after cudaDeviceReset in the
+ * same process are not supported.  All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. */
 #define CG_NOALLOC_SCRATCH_BYTES (16u << 20)
 int cg_grid_noalloc(const cg_kernel_desc *kd, int H, int W, const double *uvw,
                     int64_t stride, double lam, const int32_t *kidx, int64_t n,

@@ -17,7 +17,7 @@ def declared_symbols():
     for name in os.listdir(os.path.join(ROOT, "include")):
         if name.endswith(".h"):
             text = open(os.path.join(ROOT, "include", name)).read()
-            syms |= set(re.findall(r"^\s*(?:const\s+char\s*\*|int|size_t)\s*\**\s*(cg_\w+)\s*\(",
+            syms |= set(re.findall(r"^\s*(?:const\s+char\s*\*|int|size_t|long\s+long)\s*\**\s*(cg_\w+)\s*\(",
                                    text, re.M))
     return syms
 

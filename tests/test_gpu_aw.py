@@ -1,7 +1,9 @@
 """AW-projection at scale (8192^2, theta 0.05, 64 antennas, 16.1M visibilities,
 AW kernels S 16 / Q 16): the device AW path against the oracle's w-cache loop
-with aw_kernel_fn on all visibilities of a few baselines, and at full size the
-FP32 tiled form against the plain FP64 form (one launch per w-plane)."""
+with aw_kernel_fn on all visibilities of 16 baselines, and at full size the
+FP32 tiled form (complex64 kernels) against the plain FP64 form (complex128
+kernels generated in FP64 throughout, one launch per w-plane), so that the
+full-size error includes kernel generation."""
 
 import numpy
 import pytest
@@ -28,7 +30,9 @@ def test_aw_subset_matches_oracle(aw_workload):
     from oracle import crocodile_oracle as O
     w = aw_workload
     a1, a2 = w.params["a1"], w.params["a2"]
-    pairs = [(0, 1), (3, 17), (10, 40), (25, 63), (5, 6), (31, 32)]
+    # all visibilities of 16 baselines (about 128k), short and long ones
+    pairs = [(0, 1), (3, 17), (10, 40), (25, 63), (5, 6), (31, 32), (2, 50), (7, 44),
+             (12, 13), (15, 60), (20, 21), (33, 48), (38, 39), (45, 58), (50, 51), (61, 62)]
     sel = numpy.zeros(len(a1), bool)
     for p, q in pairs:
         sel |= (a1 == p) & (a2 == q)
@@ -43,7 +47,16 @@ def test_aw_subset_matches_oracle(aw_workload):
 
     akern = lambda theta, a: O.kernel_oversample(beams[a], 1, 16)[0, 0]
     wkern = lambda theta, ww: O.w_kernel(theta, ww, npff, 16, 16)
-    fn = O.aw_kernel_fn(akern, wkern)
+    memo = {}
+    gen = O.aw_kernel_fn(akern, wkern)
+
+    def fn(theta, ww, p, q):  # the reference's kernel cache: one generation per key
+        key = (theta, float(ww), int(p), int(q))
+        if key not in memo:
+            memo[key] = gen(theta, ww, p, q)
+        return memo[key]
+
+    assert len(uvw) == 16 * 125 * 64
     ref = O.w_cache_imaging(w.theta, w.lam, uvw, src, vis, wstep=wstep, kernel_cache=fn)
     assert rel(g_host, ref) < 1e-5
     vref = O.w_cache_predict(w.theta, w.lam, uvw, src, ref, wstep=wstep, kernel_cache=fn)

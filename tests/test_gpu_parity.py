@@ -103,7 +103,30 @@ def test_aw_kernels(S, golden):
     ak = golden["aw_akerns"]
     fn = S.aw_kernel_fn(lambda theta, a: ak[a], lambda theta, w: S.w_kernel(theta, w, 16, 6, 2))
     for args, key in (((0.1, 25.0, 0, 1), "aw_k01"), ((0.1, -40.0, 1, 2), "aw_k12")):
-        assert rel(fn(*args), golden[key]) < 1e-6
+        assert rel(fn(*args), golden[key]) < FP64_TOL  # complex128: FP64 throughout
+
+
+def test_aw_kernels_headline_shape(S, O):
+    """16 x 16 A kernels, w sub-kernels of support 16 at oversampling 16 (the AW
+    configuration's shape): the complex128 table (FP64 throughout) and the
+    complex64 table (32 x 32 FFT form) against the oracle's aw_kernel_fn."""
+    from crocodile_gb300 import configs, engine as E
+    rng = numpy.random.default_rng(17)
+    theta = 0.05
+    beams = configs.a_beams(rng, 3, 32, theta)
+    A = numpy.array([O.kernel_oversample(b, 1, 16)[0, 0] for b in beams])
+    ws = [37.0, -118.0]
+    Wk = numpy.array([O.w_kernel(theta, w, 32, 16, 16) for w in ws])
+    a1 = numpy.array([0, 1, 0], dtype=numpy.int32)
+    a2 = numpy.array([1, 2, 2], dtype=numpy.int32)
+    wi = numpy.array([0, 1, 1], dtype=numpy.int32)
+    k64 = E.aw_kernels(A, Wk, a1, a2, wi, dtype=E.CD).cpu().numpy()
+    k32 = E.aw_kernels(A, Wk, a1, a2, wi, dtype=E.CF).cpu().numpy()
+    for k in range(3):
+        fn = O.aw_kernel_fn(lambda t, a: A[a], lambda t, w: Wk[wi[k]])
+        ref = fn(theta, 0.0, a1[k], a2[k])
+        assert rel(k64[k], ref) < FP64_TOL, k
+        assert rel(k32[k], ref) < 1e-6, k
 
 
 # ---------------------------------------------------------------- gridding

@@ -7,6 +7,8 @@ the plain form's kernel groups."""
 
 import numpy
 import pytest
+
+from test_tile_order_cpu import tile_index, tiles_per_layer  # the plans' tile numbering
 from numpy.testing import assert_array_equal
 
 pytestmark = pytest.mark.gpu
@@ -88,10 +90,10 @@ def test_tiled_plan_sort(env, layout, S_, sep):
         full += 1
     sublog = 0 if eff == L.CG_LAYOUT_LANE else full
     subshift = 2 + full - sublog
-    assert info["buckets"] == ntx * ntx << (2 * sublog)
+    assert info["buckets"] == tiles_per_layer(ntx, ntx) << (2 * sublog)
 
     def key_of(r):
-        tile = (r[:, 1] // T) * ntx + r[:, 0] // T
+        tile = tile_index(r[:, 0] // T, r[:, 1] // T, ntx, ntx)
         lx, ly = r[:, 0] - (r[:, 0] // T) * T, r[:, 1] - (r[:, 1] // T) * T
         return (tile << (2 * sublog)) | _morton(lx >> subshift, ly >> subshift)
 
@@ -111,7 +113,7 @@ def test_wbin_plan_sort(env):
     T = plan.info()["tile"]
     ntx = (N + T - 1) // T
     _check(plan, _expected(O, uvw, lam, N, Q, S_, False, k - kmin),
-           lambda r: (r[:, 1] // T) * ntx + r[:, 0] // T)
+           lambda r: tile_index(r[:, 0] // T, r[:, 1] // T, ntx, ntx))
 
 
 def test_group_plan_sort(env):

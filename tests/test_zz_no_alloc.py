@@ -49,11 +49,22 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
-def test_noalloc_matches_workspace_path_twice(env):
+# (S, Q, G, n): odd S runs the warp/owner gridders with 4 x 4-cell sub-tile
+# buckets; even S <= 16 with a 4-D table runs the lane gridder (tile buckets,
+# bulk-copy ring of kernel slices) with its scratch in the static array too
+CASES = [(7, 4, 3, 100_000), (16, 4, 2, 60_000)]
+
+
+@pytest.mark.parametrize("S,Q,G,n", CASES, ids=["warp-S7", "lane-S16"])
+def test_noalloc_matches_workspace_path_twice(env, S, Q, G, n):
     torch, L = env
     lib = L.lib()
-    N, S, Q, G, n = 512, 7, 4, 3, 100_000
+    N = 512
     kd = L.KernelDesc(0, Q, S, G)
+    from types import SimpleNamespace
+    from crocodile_gb300 import autotune
+    lane = autotune.effective_layout(SimpleNamespace(S=S, sep=False)) == L.CG_LAYOUT_LANE
+    assert lane == (S == 16)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     for call, seed in enumerate((11, 12)):
         uvw, vis, ktab, kidx = _inputs(torch, seed, n, N, S, Q, G)
