@@ -646,6 +646,20 @@ def simulate_point(dist_uvw, l, m):
     return numpy.exp(-2j * numpy.pi * numpy.dot(dist_uvw, s))
 
 
+def visibility_shift(uvw, vis, dl, dm):
+    """vis * exp(-2 pi i (u dl + v dm)): the image shifted by (dl, dm)
+    (simulate.py:259-274)."""
+    s = numpy.array([dl, dm])
+    return vis * numpy.exp(-2j * numpy.pi * numpy.dot(uvw[:, 0:2], s))
+
+
+def uvw_transform(uvw, T):
+    """uv multiplied by inv(T^T), w kept: the image transformed by the 2x2 matrix T
+    (simulate.py:278-298, after Sault, Staveley-Smith and Brouw 1996)."""
+    Tt = numpy.linalg.inv(numpy.transpose(T))
+    return numpy.hstack([numpy.dot(uvw[:, 0:2], Tt), uvw[:, 2:3]])
+
+
 # --------------------------------------------------------------------------
 # Sze-Tan optimal gridding functions (crocodile/antialias.py), loop for loop.
 # The reference reads its optimised h vectors from a json cache; these

@@ -130,3 +130,149 @@ def test_w_kernel_function_recentre(S):
                                                      dm * lam / N / w))
                     assert_allclose(numpy.roll(numpy.roll(kern, dl, axis=1), dm, axis=0), kerns,
                                     atol=1e-15)
+
+
+@pytest.fixture(scope="module")
+def O():
+    from oracle import crocodile_oracle
+    return crocodile_oracle
+
+
+TRANSFORMS = [numpy.array([[1, 0], [0, 1]]), numpy.array([[-1, 0], [0, 1]]),
+              numpy.array([[1 / numpy.sqrt(2), -1 / numpy.sqrt(2)],
+                           [1 / numpy.sqrt(2), 1 / numpy.sqrt(2)]]),
+              numpy.array([[2, 0], [0, 3]]), numpy.array([[1, 2], [2, 1]]),
+              numpy.array([[1e5, -5e3], [6e4, -1e6]]), numpy.array([[0, .05], [-.05, 0]])]
+PLACES7 = 5e-8  # unittest's assertAlmostEqual (7 decimal places)
+
+
+def test_grid_shift(S, O):
+    # tests/test_synthesis.py:140-157: boxcar grid of shifted point sources, device FFT
+    lam = 100
+    for N in range(3, 7):
+        for dl, dm in [(1 / lam, 1 / lam), (-1 / lam, 2 / lam), (5 / lam, 0)]:
+            uvw = _uvw(S, N) * lam
+            xys = range(-(N // 2), (N + 1) // 2)
+            for x, y in itertools.product(xys, xys):
+                vis = O.simulate_point(uvw, x / lam - dl, y / lam - dm)
+                vis = O.visibility_shift(uvw, vis, dl, dm)
+                a = numpy.zeros((N, N), dtype=complex)
+                S.grid(a, uvw / lam, vis)
+                img = numpy.real(S.ifft(a))
+                assert abs(img[N // 2 + y, N // 2 + x] - 1) < PLACES7
+
+
+@pytest.mark.parametrize("shifts", [[(0, 0)], [(1, 1), (-1, 2), (5, 0)]],
+                         ids=["transform", "transform_shift"])
+def test_grid_transform(S, O, shifts):
+    # tests/test_synthesis.py:159-196 (test_grid_transform) and :198-233
+    # (test_grid_transform_shift): grid on uvw transformed so that the sources land
+    # on grid points
+    lam = 100
+    for T in TRANSFORMS:
+        Ti = numpy.linalg.inv(T)
+        for sx, sy in shifts:
+            dl, dm = sx / lam, sy / lam
+            for N in range(3, 7):
+                uvwt = _uvw(S, N) * lam
+                uvw = O.uvw_transform(uvwt, Ti)
+                assert_allclose(O.uvw_transform(uvw, T), uvwt, atol=1e-13)
+                xys = range(-(N // 2), (N + 1) // 2)
+                for xt, yt in itertools.product(xys, xys):
+                    x, y = numpy.dot([xt, yt], Ti)
+                    assert_allclose(numpy.dot([x, y], T), [xt, yt], atol=1e-13)
+                    vis = O.simulate_point(uvw, x / lam - dl, y / lam - dm)
+                    vis = O.visibility_shift(uvw, vis, dl, dm)
+                    a = numpy.zeros((N, N), dtype=complex)
+                    S.grid(a, uvwt / lam, vis)
+                    img = numpy.real(S.ifft(a))
+                    assert abs(img[N // 2 + yt, N // 2 + xt] - 1) < PLACES7
+
+
+@pytest.mark.parametrize("precision,rtol", [("fp64", 1e-7), ("fp32", 1e-5)])
+def test_grid_shift_w(S, O, precision, rtol):
+    # tests/test_synthesis.py:283-311: w-kernels re-centred by (-dl, -dm), device
+    # kernel generation and convgrid
+    lam = 10
+    for uw, vw in [(.5, 0), (0, .5), (-1, 0), (0, -1)]:
+        for N in range(1, 6):
+            for dl, dm in [(1 / lam, 1 / lam), (-1 / lam, 2 / lam), (5 / lam, 0)]:
+                theta = N / lam
+                uvw_all = _uvw(S, N, uw, vw) * lam
+                slices = S.slice_vis(N, S.sort_vis_w(uvw_all))
+                gcfs = [S.w_kernel(theta, numpy.mean(u[:, 2]), N, N, 1, dl=-dl, dm=-dm) / N ** 2
+                        for u in slices]
+                xys = range(-(N // 2), (N + 1) // 2)
+                for x, y in itertools.product(xys, xys):
+                    a = numpy.zeros((2 * N, 2 * N), dtype=complex)
+                    for u, gcf in zip(slices, gcfs):
+                        vis = O.simulate_point(u, x / lam - dl, y / lam - dm)
+                        viss = O.visibility_shift(u, vis, dl, dm)
+                        assert_allclose(O.visibility_shift(u, viss, -dl, -dm), vis)
+                        S.convgrid(gcf, a, u / lam / 2, None, viss, precision=precision)
+                    a2 = numpy.fft.fftshift(a[:N, :N] + a[:N, N:] + a[N:, :N] + a[N:, N:])
+                    img = numpy.real(S.ifft(a2))
+                    assert_allclose(img[N // 2 + y, N // 2 + x], 1, rtol=rtol)
+
+
+W_TRANSFORMS = [numpy.array([[1, 0], [0, 1]]), numpy.array([[2, 0], [0, 3]]),
+                numpy.array([[0, 1], [-1, 0]]),
+                numpy.array([[1 / numpy.sqrt(2), 1 / numpy.sqrt(2)],
+                             [-1 / numpy.sqrt(2), 1 / numpy.sqrt(2)]]),
+                numpy.array([[1e5, -5e3], [6e4, -1e6]]), numpy.array([[0, .5], [-.5, 0]])]
+
+
+@pytest.mark.parametrize("precision,rtol", [("fp64", 1e-7), ("fp32", 1e-5)])
+def test_grid_transform_shift_w(S, O, precision, rtol):
+    # tests/test_synthesis.py:313-356: transformed and shifted w-kernels (T, dl, dm)
+    # generated on the device
+    lam = 10
+    for T in W_TRANSFORMS:
+        Ti = numpy.linalg.inv(T)
+        for uw, vw in [(.5, 0), (0, .5), (0, -1)]:
+            for dl, dm in [(0, 0), (1 / lam, 1 / lam), (-1 / lam, 4 / lam)]:
+                for N in range(1, 6):
+                    uvwt_all = _uvw(S, N, uw, vw) * lam
+                    uvw_all = O.uvw_transform(uvwt_all, Ti)
+                    slices = S.slice_vis(N, *S.sort_vis_w(uvwt_all, uvw_all))
+                    gcfs = [S.w_kernel(N / lam, numpy.mean(ut[:, 2]), N, N, 1, T=Ti, dl=-dl,
+                                       dm=-dm) / N ** 2 for ut, _ in slices]
+                    xys = range(-(N // 2), (N + 1) // 2)
+                    for xt, yt in itertools.product(xys, xys):
+                        x, y = numpy.dot([xt, yt], Ti)
+                        assert_allclose(numpy.dot([x, y], T), [xt, yt], atol=1e-14)
+                        a = numpy.zeros((2 * N, 2 * N), dtype=complex)
+                        for (ut, u), gcf in zip(slices, gcfs):
+                            vis = O.simulate_point(u, x / lam - dl, y / lam - dm)
+                            vis = O.visibility_shift(u, vis, dl, dm)
+                            S.convgrid(gcf, a, ut / lam / 2, None, vis, precision=precision)
+                        a = numpy.fft.fftshift(a[:N, :N] + a[:N, N:] + a[N:, :N] + a[N:, N:])
+                        img = numpy.real(S.ifft(a))
+                        assert_allclose(img[N // 2 + yt, N // 2 + xt], 1, rtol=rtol)
+
+
+def test_kernel_oversampled_subgrid(S):
+    # tests/test_synthesis.py:77-91: oversampled kernels agree where sub-grids overlap
+    for N in range(3, 30):
+        pat = S.coordinates2(N)[1] + S.coordinates2(N)[0] * 1j
+        kern = S.kernel_oversample(pat, 1, N - 2)
+        kern2 = S.kernel_oversample(pat, 2, N - 2)
+        assert_allclose(kern[0, 0], kern2[0, 0], atol=1e-13)
+        kern3 = S.kernel_oversample(pat, 3, N - 2)
+        assert_allclose(kern[0, 0], kern3[0, 0], atol=1e-13)
+        kern4 = S.kernel_oversample(pat, 4, N - 2)
+        for ux, uy in itertools.product(range(2), range(2)):
+            assert_allclose(kern2[uy, ux], kern4[2 * uy, 2 * ux], atol=1e-13)
+        kern8 = S.kernel_oversample(pat, 8, N - 2)
+        for ux, uy in itertools.product(range(3), range(3)):
+            assert_allclose(kern4[uy, ux], kern8[2 * uy, 2 * ux], atol=1e-13)
+
+
+def test_frac_coord(S):
+    # tests/test_synthesis.py:393-409: offsets exactly between oversampling values
+    for Qpx in range(1, 6):
+        p = numpy.arange(-2 * Qpx, 2 * Qpx) / 4 / Qpx
+        flx, fracx = S.frac_coord(2, Qpx, p)
+        assert (fracx >= 0).all()
+        assert (fracx < Qpx).all()
+        assert_allclose(flx - fracx / Qpx, numpy.around(numpy.arange(0, 4 * Qpx) / 2) / Qpx)

@@ -185,3 +185,15 @@ def test_w_towers_predict_single_plane_is_the_reference_predict(golden):
         got = O.w_towers_predict(theta, lam, uvw, None, guv, s, margin, winc, 10.0,
                                  NpixFF=16, NpixKern=7, Qpx=4)
         assert numpy.linalg.norm(got - ref) <= 1e-12 * numpy.linalg.norm(ref)
+
+
+def test_simulate_helpers_match_reference():
+    """simulate_point, visibility_shift and uvw_transform against the reference's
+    own outputs (tests/golden/make_simulate.py)."""
+    import os
+    g = numpy.load(os.path.join(os.path.dirname(__file__), "golden", "simulate_golden.npz"))
+    uvw, vis = g["uvw"], g["vis"]
+    assert_array_equal(O.simulate_point(uvw, 0.013, -0.021), g["point"])
+    assert_array_equal(O.visibility_shift(uvw, vis, 0.01, -0.03), g["shift"])
+    for T, ref in zip(g["Ts"], g["transformed"]):
+        assert_array_equal(O.uvw_transform(uvw, T), ref)
