@@ -276,7 +276,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -799,8 +799,12 @@ def run_ours(args):
                 z["cpu_oracle_sample"] = how
                 z["speedup_vs_cpu_oracle"] = sec / (z["ms_correction"] * 1e-3)
 
-    # kernels of ours per step: coords, scan (1 or 3), scatter, work items, grid, degrid
-    per_step = 1 + (3 if info_plan["buckets"] > 4096 else 1) + 1 + 1 + 2
+    # kernels of ours per step: coords, bucket scan (1 or 3), scatter, items per tile,
+    # their scan (1 or 3), work items, (slice padding,) grid, degrid
+    ntiles = (N // info_plan["tile"] + 1) ** 2 if info_plan["tile"] else 1
+    per_step = 1 + (3 if info_plan["buckets"] > 4096 else 1) + 1 + 1 + \
+        (3 if ntiles > 4096 else 1) + 1 + (1 if S * S % 2 and
+                                           tuned.get("layout") == L.CG_LAYOUT_LANE else 0) + 2
     line = {
         "metric": METRIC, "value": value, "unit": "Mvis/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,

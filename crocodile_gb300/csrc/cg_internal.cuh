@@ -217,12 +217,15 @@ struct cg_plan {
   int subshift; // sub-tile edge = 1 << subshift cells (4, or more for huge grid stacks)
   int64_t max_items;
   int chunk;    // visibilities per work item
+  int slice_stride;  // lane layout: elements between S x S slices of the table it reads
+  int64_t kpad_slices;  // lane layout, slices padded to a 16-byte multiple: slices to copy
   // device arrays inside the caller's workspace
   cg::VisRec *recs;   // sorted records [n]
   int32_t *perm;      // sorted position -> original index [n]
   int32_t *counts;    // [nbuckets]
   int32_t *offsets;   // [nbuckets]
   cg::WorkItem *items;
+  float2 *kpad;       // lane layout, odd S * S: the table with padded slices (workspace)
   int32_t *nitems;    // device counter
   int32_t *ticket;    // device counter for the persistent kernels (2 words)
   int32_t *status;    // caller's status block

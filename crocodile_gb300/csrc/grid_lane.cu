@@ -44,6 +44,7 @@ struct LaneArgs {
   float2 *vis_out;        // fused: degridded visibilities (may be NULL)
   int mode;               // gridding: 0 vis, 1 vis * weight, 2 weight; fused: 0 plain, 1 residual
   long long wait_cycles;  // limit of a consumer's wait for a slice (the drain keeps LANE_WAIT_CYCLES)
+  int kstride;            // elements between slices in ktab and in the stage ring (4-D tables)
   int warp_bytes;         // shared memory per warp
   int stage_off, meta_off, val_off, bar_off;  // byte offsets inside a warp's region
 };
@@ -77,6 +78,19 @@ __device__ __forceinline__ void bulk_load_if(bool p, void *dst, const void *src,
       "\n\t}" ::"r"(smem_u32(dst)),
       "l"(src), "r"(bytes), "r"(smem_u32(bar)), "r"((int)p)
       : "memory");
+}
+
+// Non-blocking poll of a phase (test_wait returns at once; try_wait may
+// suspend the thread for a while until the phase completes).
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
 }
 
 __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
@@ -116,7 +130,8 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
   uint64_t *bar = (uint64_t *)(region + P.bar_off);
   const int QQ = A.Q * A.Q;
   const float2 zero = make_float2(0.f, 0.f);
-  const uint32_t slice_bytes = (uint32_t)SS * 8u;
+  const int KS = P.kstride;  // S * S, or S * S + 1 for padded odd slices
+  const uint32_t slice_bytes = (uint32_t)KS * 8u;
 
   // lane l owns taps t = l + 32 i: footprint cell (dy, dx) = (t / S, t % S)
   int soff[MAXT], goff[MAXT], tdy[MAXT], tdx[MAXT];
@@ -196,7 +211,7 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
       int ist = cst;
       for (; issued < min(n, LANE_DEPTH - 1); ++issued) {
         const int4 m = meta[issued];
-        bulk_load_if(lane == 0, stages + (size_t)ist * SS, P.ktab + (size_t)m.y * SS,
+        bulk_load_if(lane == 0, stages + (size_t)ist * KS, P.ktab + (size_t)m.y * KS,
                      slice_bytes, &bar[ist]);
         ist = ist + 1 == LANE_DEPTH ? 0 : ist + 1;
       }
@@ -210,7 +225,7 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
     auto load_global = [&](int j) {
       const int4 m = meta[j & (LANE_RING - 1)];
       const int lx0 = m.x & 0xffff, ly0 = m.x >> 16;
-      const float2 *kk = SEP ? P.ktab + (size_t)m.y * S : P.ktab + (size_t)m.y * SS;
+      const float2 *kk = SEP ? P.ktab + (size_t)m.y * S : P.ktab + (size_t)m.y * KS;
       const float2 *kx = P.ktab + (size_t)m.z * S;
 #pragma unroll
       for (int i = 0; i < MAXT; ++i)
@@ -231,17 +246,18 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
         if (issued < n) {
           const int4 mi = meta[issued & (LANE_RING - 1)];
           const int ist = cst == 0 ? LANE_DEPTH - 1 : cst - 1;
-          bulk_load_if(lane == 0, stages + (size_t)ist * SS, P.ktab + (size_t)mi.y * SS,
+          bulk_load_if(lane == 0, stages + (size_t)ist * KS, P.ktab + (size_t)mi.y * KS,
                        slice_bytes, &bar[ist]);
           ++issued;
         }
-        bool ok = mbar_try(&bar[cst], cpar);
+        // a limit of 0 (a test of the timeout path) polls without blocking
+        bool ok = P.wait_cycles ? mbar_try(&bar[cst], cpar) : mbar_test(&bar[cst], cpar);
         if (!__all_sync(FULL_MASK, ok)) {  // warp-uniform slow path, bounded
           const long long t0 = clock64();
           while (!ok && clock64() - t0 <= P.wait_cycles) ok = mbar_try(&bar[cst], cpar);
           if (__any_sync(FULL_MASK, !ok)) return false;
         }
-        const float2 *kp = stages + (size_t)cst * SS + lane;
+        const float2 *kp = stages + (size_t)cst * KS + lane;
 #pragma unroll
         for (int i = 0; i < MAXT; ++i) kc[i] = own[i] ? kp[32 * i] : zero;
         if (++cst == LANE_DEPTH) {
@@ -362,6 +378,18 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
   }
 }
 
+// dst[s][t] = src[s][t] for t < SS, 0 for SS <= t < KS: slices padded to KS elements
+__global__ void k_pad_slices(const float2 *__restrict__ src, int64_t nslices, int SS, int KS,
+                             float2 *__restrict__ dst) {
+  const int64_t total = nslices * KS;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t sl = e / KS;
+    const int t = (int)(e - sl * KS);
+    dst[e] = t < SS ? src[sl * SS + t] : make_float2(0.f, 0.f);
+  }
+}
+
 template <bool SEP, bool BULK, bool FUSED>
 static void *lane_kernel_for(int maxt, int SS, int pitch) {
   if (maxt == 8 && SS == 256 && pitch == 32) return (void *)k_lane<SEP, BULK, FUSED, 8, true, 16, 32>;
@@ -387,7 +415,19 @@ int lane_launch(const cg_plan *p, const float2 *ktab, const float2 *vis, const f
   const int need = (SS + 31) / 32;
   int maxt = 1;
   while (maxt < need) maxt *= 2;
-  const bool bulk = !p->kd.sep && (SS * 8) % 16 == 0 && ((uintptr_t)ktab & 15) == 0;
+  // odd S * S: the table with slices padded to an even element count (a
+  // 16-byte multiple), copied into the plan's workspace
+  const int KS = p->kd.sep ? S : p->slice_stride;
+  if (!p->kd.sep && KS != SS) {
+    CG_REQUIRE(p->kpad && KS == SS + 1, "plan has no padded kernel table");
+    const int64_t total = p->kpad_slices * KS;
+    const unsigned blocks = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16));
+    k_pad_slices<<<blocks, 256, 0, s>>>(ktab, p->kpad_slices, SS, KS, p->kpad);
+    CG_LAUNCH("kernel slice padding");
+    ktab = p->kpad;
+  }
+  const bool bulk = !p->kd.sep && (KS * 8) % 16 == 0 && ((uintptr_t)ktab & 15) == 0;
 
   LaneArgs P;
   P.ktab = ktab;
@@ -398,10 +438,11 @@ int lane_launch(const cg_plan *p, const float2 *ktab, const float2 *vis, const f
   P.vis_out = vis_out;
   P.mode = fused ? (residual ? 1 : 0) : gmode;
   P.wait_cycles = wait_cycles();
+  P.kstride = KS;
   auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
   size_t off = up16((size_t)p->pitch * p->win * sizeof(float2));
   P.stage_off = (int)off;
-  if (bulk) off += (size_t)LANE_DEPTH * SS * sizeof(float2);
+  if (bulk) off += (size_t)LANE_DEPTH * KS * sizeof(float2);
   P.meta_off = (int)off;
   off += LANE_RING * sizeof(int4);
   P.val_off = (int)off;

@@ -249,20 +249,35 @@ __global__ void k_plan_scatter(int64_t n, const VisRec *__restrict__ rec,
 }
 
 // Work items: each tile's sorted range (its 4^sublog sub-tile buckets are
-// contiguous) cut into pieces of at most `chunk` visibilities.
+// contiguous) cut into pieces of at most `chunk` visibilities.  First the
+// number of pieces per tile, then (after an exclusive scan of those numbers)
+// the items at their scanned positions, so that the work list follows the
+// tile numbering exactly and the persistent kernels, which take items in list
+// order, visit the tiles in that order.
+__global__ void k_plan_item_counts(int ntiles, int sublog, const int32_t *__restrict__ counts,
+                                   const int32_t *__restrict__ offsets, int chunk,
+                                   int32_t *__restrict__ nch) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const int b0 = t << (2 * sublog), b1 = b0 + (1 << (2 * sublog)) - 1;
+  const int c = offsets[b1] + counts[b1] - offsets[b0];
+  nch[t] = (c + chunk - 1) / chunk;
+}
+
 __global__ void k_plan_items(int ntiles, int sublog, const int32_t *__restrict__ counts,
                              const int32_t *__restrict__ offsets, int chunk,
-                             WorkItem *__restrict__ items,
-                             int32_t *__restrict__ nitems) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+                             const int32_t *__restrict__ nch, const int32_t *__restrict__ ioff,
+                             WorkItem *__restrict__ items, int32_t *__restrict__ nitems) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntiles) return;
+  if (t == ntiles - 1) *nitems = ioff[t] + nch[t];
+  const int m = nch[t];
+  if (m == 0) return;
   const int b0 = t << (2 * sublog), b1 = b0 + (1 << (2 * sublog)) - 1;
   const int off = offsets[b0];
   const int c = offsets[b1] + counts[b1] - off;
-  if (c == 0) return;
-  int nch = (c + chunk - 1) / chunk;
-  int base = atomicAdd(nitems, nch);
-  for (int j = 0; j < nch; ++j) {
+  const int base = ioff[t];
+  for (int j = 0; j < m; ++j) {
     WorkItem w;
     w.tile = t;
     w.start = off + j * chunk;
@@ -405,7 +420,8 @@ __global__ void k_aw_keys(const double *__restrict__ uvw, int64_t stride,
 
 // ---------------------------------------------------------------- sizing
 struct Layout {
-  size_t rec_tmp, key, rank, recs, perm, counts, offsets, scan, items, ctr, total;
+  size_t rec_tmp, key, rank, recs, perm, counts, offsets, scan, items, tnch, tioff, ctr, kpad,
+      total;
 };
 
 static int tile_edge(const cg_kernel_desc &kd, int req) {
@@ -458,6 +474,17 @@ static void plan_geometry(cg_plan &p) {
                                                    : (int)std::min<int64_t>(
                                                          2048, std::max<int64_t>(256, want));
     p.max_items = (p.n + p.chunk - 1) / p.chunk + p.ntiles;
+    // The lane gridder streams each visibility's S x S slice with one bulk copy,
+    // which needs a multiple of 16 bytes: for odd S * S it reads a copy of the
+    // table whose slices are padded by one element (made in the workspace by
+    // every gridding call).
+    const int SS = p.kd.S * p.kd.S;
+    p.slice_stride = SS;
+    p.kpad_slices = 0;
+    if (layout_for(p.kd) == CG_LAYOUT_LANE && !p.kd.sep && (SS & 1)) {
+      p.slice_stride = SS + 1;
+      p.kpad_slices = (int64_t)p.kd.G * p.kd.Q * p.kd.Q;
+    }
   } else {
     p.T = 0;
     p.ntx = p.nty = 0;
@@ -468,6 +495,8 @@ static void plan_geometry(cg_plan &p) {
     p.win = p.pitch = 0;
     p.chunk = 0;
     p.max_items = 0;
+    p.slice_stride = p.kd.sep ? p.kd.S : p.kd.S * p.kd.S;
+    p.kpad_slices = 0;
   }
 }
 
@@ -484,7 +513,11 @@ static Layout layout_of(const cg_plan &p) {
   L.offsets = o; o = align256(o + (size_t)p.nbuckets * 4);
   L.scan = o;    o = align256(o + scan_scratch_words(p.nbuckets) * 4);
   L.items = o;   o = align256(o + (size_t)std::max<int64_t>(p.max_items, 1) * sizeof(WorkItem));
+  const size_t nt = p.mode == CG_PLAN_TILED ? (size_t)p.ntiles : 0;  // items per tile, scanned
+  L.tnch = o;    o = align256(o + nt * 4);
+  L.tioff = o;   o = align256(o + nt * 4);
   L.ctr = o;     o = align256(o + 4 * 4);
+  L.kpad = o;    o = align256(o + (size_t)p.kpad_slices * p.slice_stride * sizeof(float2));
   L.total = o;
   return L;
 }
@@ -544,6 +577,7 @@ int plan_build_into(cg_plan *p, int mode, const cg_kernel_desc *kd, int H, int W
   p->counts = (int32_t *)(ws + L.counts);
   p->offsets = (int32_t *)(ws + L.offsets);
   p->items = (WorkItem *)(ws + L.items);
+  p->kpad = p->kpad_slices ? (float2 *)(ws + L.kpad) : nullptr;
   int32_t *ctr = (int32_t *)(ws + L.ctr);
   p->nitems = ctr;
   p->ticket = ctr + 1;
@@ -593,10 +627,19 @@ int plan_build_into(cg_plan *p, int mode, const cg_kernel_desc *kd, int H, int W
   rc = launch_scan(p->counts, p->offsets, p->nbuckets, (int32_t *)(ws + L.scan), s);
   if (rc) return rc;
   k_plan_scatter<<<blocks, 256, 0, s>>>(n, rec_tmp, key, rank, p->offsets, p->recs, p->perm);
-  if (mode == CG_PLAN_TILED)
-    k_plan_items<<<(p->ntiles + 255) / 256, 256, 0, s>>>(p->ntiles, p->sublog, p->counts,
-                                                          p->offsets, p->chunk, p->items,
-                                                          p->nitems);
+  CG_LAUNCH("plan sort");
+  if (mode == CG_PLAN_TILED) {
+    int32_t *tnch = (int32_t *)(ws + L.tnch), *tioff = (int32_t *)(ws + L.tioff);
+    const unsigned tb = (unsigned)((p->ntiles + 255) / 256);
+    k_plan_item_counts<<<tb, 256, 0, s>>>(p->ntiles, p->sublog, p->counts, p->offsets, p->chunk,
+                                          tnch);
+    CG_LAUNCH("plan item counts");
+    // the bucket scan's scratch is free again (ntiles <= nbuckets)
+    rc = launch_scan(tnch, tioff, p->ntiles, (int32_t *)(ws + L.scan), s);
+    if (rc) return rc;
+    k_plan_items<<<tb, 256, 0, s>>>(p->ntiles, p->sublog, p->counts, p->offsets, p->chunk, tnch,
+                                    tioff, p->items, p->nitems);
+  }
   CG_LAUNCH("plan sort");
   return CG_OK;
 }

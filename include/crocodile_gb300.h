@@ -258,11 +258,11 @@ int cg_update_peak(int kind, int work, void *buf, size_t buf_bytes, double *upda
  * an H x W grid need more scratch than that.  The need depends on n, the grid
  * and the gridder layout; cg_plan_workspace_bytes(CG_PLAN_TILED, ...) gives
  * it.  It is about 44 B per visibility plus the bucket tables and work
- * list: about H * W / 10 bytes for the lane layout (non-separable tables,
+ * list: about H * W / 8 bytes for the lane layout (non-separable tables,
  * even S <= 16), but H * W / 2 bytes for the warp and owner layouts (4 x
  * 4-cell sub-tile buckets), which alone exceed the array above about
  * 5800 x 5800.  So a 512 x 512 grid takes up to about 380 000 visibilities,
- * a 4096 x 4096 grid about 345 000 with the lane layout but only about
+ * a 4096 x 4096 grid about 330 000 with the lane layout but only about
  * 190 000 with the others.
  * The first call on a device looks up the array's device address, once per
  * device, with that device current; make that first call before any stream

@@ -1,7 +1,8 @@
 """Batched w-stacking (all planes in one gridding launch and one batched FFT)
 against the oracle's per-plane loop (examples/notebooks/wstacking.ipynb cell 10
-with conv_imaging), and at the full 4096^2 / 32-plane / 4M-visibility size
-against the one-plane-per-launch form."""
+with conv_imaging), at a small size and at the full 4096^2 / 32-plane /
+4M-visibility size of the w-stacking configuration, and at full size against
+the one-plane-per-launch form."""
 
 import numpy
 import pytest
@@ -67,3 +68,19 @@ def test_wstack_full_size_batched_vs_per_plane(env):
     err = float(torch.linalg.vector_norm((a - b).to(torch.complex128)) /
                 torch.linalg.vector_norm(b.to(torch.complex128)))
     assert err < 1e-6, err
+
+
+def test_wstack_full_size_matches_oracle(env):
+    """The w-stacking configuration in full (4096^2, 32 planes, 4,000,000
+    visibilities, S 8, Q 8 anti-aliasing kernel) against the oracle's complex128
+    per-plane loop (examples/notebooks/wstacking.ipynb:190-226): about two minutes
+    of host time for the oracle."""
+    torch, configs, S, O = env
+    w = configs.wstack()
+    assert len(w.uvw) == 4_000_000 and w.N == 4096
+    kv = O.kernel_oversample(O.anti_aliasing_function(w.N, 0, 8), 8, 8)
+    plane = w.params["plane"]
+    assert len(numpy.unique(plane)) == 32
+    got = S.w_stack_imaging(w.theta, w.lam, w.uvw, None, w.vis, kv, plane)
+    ref = O.w_stack_imaging(w.theta, w.lam, w.uvw, None, w.vis, kv, plane)
+    assert rel(got, ref) < 1e-5
