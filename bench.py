@@ -510,6 +510,44 @@ class AWGpu(GpuWorkload):
         return (statistics.mean(ms),) + errs
 
 
+def reference_api_imaging(G):
+    """Seconds of do_imaging through the drop-in's reference API on the whole AW
+    set: host numpy uvw, src = [a1, a2] and vis in, host dirty image and PSF out,
+    kernel_cache = aw_kernel_fn(host A kernels, w_kernel) keyed on the device and
+    generated in one batched pass; cold (kernel generation included) and warm
+    (the AW table cached on the callable, as the reference's kernel cache)."""
+    import torch
+    from crocodile_gb300 import synthesis as S
+    w = G.w
+    beams, npff = w.params["beams"], w.params["NpixFF"]
+    akern = {}
+
+    def a_fn(theta, a):
+        if a not in akern:
+            akern[a] = S.kernel_oversample(beams[int(a)], 1, 16)[0, 0]
+        return akern[a]
+
+    fn = S.aw_kernel_fn(a_fn, lambda theta, ww: S.w_kernel(theta, ww, npff, 16, 16))
+    src = numpy.column_stack([w.params["a1"], w.params["a2"]])
+    out = {}
+    for leg in ("cold", "warm"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d, p, pm = S.do_imaging(w.theta, w.lam, w.uvw, src, w.vis, S.w_cache_imaging,
+                                wstep=w.params["wstep"], kernel_cache=fn)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[leg] = {"s": dt, "mvis_s": len(w.uvw) / dt / 1e6}
+    del d, p, fn
+    torch.cuda.empty_cache()
+    out["form"] = ("synthesis.do_imaging(theta, lam, uvw, src=[a1, a2], vis, w_cache_imaging, "
+                   "wstep, kernel_cache=aw_kernel_fn(a_kernel_fn, w_kernel_fn)) on all %d "
+                   "visibilities, host numpy in and out (mirror, weights, image and PSF "
+                   "gridding, hermitian FFTs, two 8192^2 float64 images back); host clock"
+                   % len(w.uvw))
+    return out
+
+
 def update_peaks(G):
     """Measured grid-point update peaks (updates/s): shared-memory float2
     read-modify-write in the lane gridder's form, and float2 atomics into L2."""
@@ -696,6 +734,13 @@ def run_ours(args):
     ms_plain, err_grid, err_degrid = G.plain(args.plain_steps)
     plain_value = n / (ms_plain * 1e-3) / 1e6
 
+    # ---- the reference's own AW call through the drop-in: do_imaging(theta, lam,
+    # uvw, src=[a1, a2], vis, w_cache_imaging, wstep, kernel_cache=aw_kernel_fn(...))
+    # from host numpy arrays to host images (scripts/image_dataset.py:162-187)
+    ref_api = None
+    if args.workload == "aw" and world == 1:
+        ref_api = reference_api_imaging(G)
+
     # ---- kernel generation again in the running process (libraries loaded,
     # FFT plans cached): what a new data set's kernel table costs after the first
     torch.cuda.synchronize()
@@ -856,6 +901,7 @@ def run_ours(args):
                   "form": "plan + one degrid+grid pass (cg_degrid_grid), each kernel tap read "
                           "once", "speedup_vs_plain": ms_plain / ms_fused},
         "e2e": e2e,
+        "reference_api": ref_api,
         "cold_start": {"value": n / ((ms_e2e + G.kgen_ms) * 1e-3) / 1e6, "unit": "Mvis/s",
                        "ms": ms_e2e + G.kgen_ms,
                        "form": "one end-to-end step plus the one-off generation of the step's "

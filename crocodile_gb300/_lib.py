@@ -70,6 +70,8 @@ SIGNATURES = {
     "cg_plan_layer_mean_w": (c_int, [P, P, c_int64, P, P, P]),
     "cg_compact_keys_workspace_bytes": (c_size_t, [c_int]),
     "cg_compact_keys": (c_int, [P, c_int64, c_int, P, P, P, P, c_size_t, P, P]),
+    "cg_row_keys": (c_int, [P, c_int64, c_int64, c_double, c_int, c_int, P, c_int, P, P, P, P,
+                            P]),
     "cg_aw_keys": (c_int, [P, c_int64, P, P, c_int64, c_int, c_double, c_int, c_int, P, P, P]),
     "cg_wstack_combine": (c_int, [P, c_int, c_int, c_double, P, P, P, P, P]),
     "cg_tower_keys": (c_int, [P, c_int64, c_int64, c_double, c_int, c_double, P, P, P, P, P, P]),

@@ -399,6 +399,37 @@ __global__ void k_key_of_row(int nw, const uint32_t *__restrict__ bits,
   }
 }
 
+// Kernel-cache key of every visibility for w_cache_imaging with src columns
+// (synthesis.py:793-794: kernel_cache(theta, wbin, *src[i])): the w bin and
+// the integer src columns of the row packed in mixed radix,
+//   key = ((wbin - kmin) * r0 + (c0 - m0)) * r1 + (c1 - m1) ...
+// A column value outside [m, m + r) is an index error (key 0).
+struct RowKeyCols {
+  int ncols;
+  int32_t mins[8], ranges[8];
+};
+
+__global__ void k_row_keys(const double *__restrict__ uvw, int64_t stride, int64_t n,
+                           double wstep, double inv_wstep, int kmin, int nbins,
+                           const int32_t *__restrict__ cols, RowKeyCols C,
+                           int32_t *__restrict__ key, int32_t *status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double j = w_bin_fast(uvw[i * stride + 2], wstep, inv_wstep) - (double)kmin;
+  bool ok = j >= 0.0 && j < (double)nbins;
+  int64_t k = ok ? (int64_t)j : 0;
+  for (int c = 0; c < C.ncols; ++c) {
+    const int v = cols[i * C.ncols + c] - C.mins[c];
+    ok = ok && v >= 0 && v < C.ranges[c];
+    k = k * C.ranges[c] + (ok ? v : 0);
+  }
+  if (!ok) {
+    atomicAdd(&status[ST_INDEX], 1);
+    k = 0;
+  }
+  key[i] = (int32_t)k;
+}
+
 // AW kernel key of every visibility: (a1 * nant + a2) * nbins + w bin - kmin, the
 // (wbin, a1, a2) key of the AW kernel cache (scripts/image_dataset.py:153-171,
 // synthesis.py:793).
@@ -885,6 +916,31 @@ int cg_aw_keys(const double *uvw, int64_t stride, const int32_t *a1, const int32
   k_aw_keys<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
       uvw, stride, a1, a2, n, nant, wstep, 1.0 / wstep, kmin, nbins, key, d_status);
   CG_LAUNCH("aw keys");
+  return CG_OK;
+}
+
+int cg_row_keys(const double *uvw, int64_t stride, int64_t n, double wstep, int kmin, int nbins,
+                const int32_t *cols, int ncols, const int32_t *col_min, const int32_t *col_range,
+                int32_t *key, int32_t *d_status, cg_stream_t stream) {
+  CG_REQUIRE(nbins >= 1 && wstep != 0.0 && d_status && ncols >= 0 && ncols <= 8 &&
+                 (ncols == 0 || (col_min && col_range)) &&
+                 (n == 0 || (uvw && stride >= 3 && key && (ncols == 0 || cols))),
+             "bad row_keys arguments");
+  RowKeyCols C;
+  C.ncols = ncols;
+  int64_t space = nbins;
+  for (int c = 0; c < ncols; ++c) {
+    CG_REQUIRE(col_range[c] >= 1, "column %d has an empty range", c);
+    C.mins[c] = col_min[c];
+    C.ranges[c] = col_range[c];
+    space *= col_range[c];
+    CG_REQUIRE(space < (int64_t)INT32_MAX, "key space of %lld keys or more is too large",
+               (long long)space);
+  }
+  if (n == 0) return CG_OK;
+  k_row_keys<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      uvw, stride, n, wstep, 1.0 / wstep, kmin, nbins, cols, C, key, d_status);
+  CG_LAUNCH("row keys");
   return CG_OK;
 }
 

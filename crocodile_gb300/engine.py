@@ -290,6 +290,21 @@ def compact_keys(key, nkeys, status):
     return row, kor[:nrows.value]
 
 
+def row_keys(uvw, wstep, kmin, nbins, cols, mins, ranges, status):
+    """int32 kernel-cache key per row: (w bin - kmin, integer src columns) packed in
+    mixed radix (cg_row_keys); cols is an int32 [n, k] tensor, mins / ranges host ints."""
+    uvw = cuda_tensor(uvw, torch.float64)
+    n = uvw.shape[0]
+    k = len(mins)
+    cols = None if k == 0 else cuda_tensor(cols, torch.int32).reshape(n, k).contiguous()
+    key = torch.empty(n, dtype=torch.int32, device="cuda")
+    cm = (ctypes.c_int32 * max(k, 1))(*[int(m) for m in mins])
+    cr = (ctypes.c_int32 * max(k, 1))(*[int(r) for r in ranges])
+    L.call("cg_row_keys", _p(uvw), uvw.stride(0), n, float(wstep), int(kmin), int(nbins),
+           _p(cols), k, cm, cr, _p(key), _p(status.t), stream())
+    return key
+
+
 def aw_keys(uvw, a1, a2, nant, wstep, kmin, nbins, status):
     uvw = cuda_tensor(uvw, torch.float64)
     a1, a2 = cuda_tensor(a1, torch.int32), cuda_tensor(a2, torch.int32)

@@ -251,15 +251,64 @@ def w_conj_kernel_fn(kernel_fn):
     return fn
 
 
-def aw_kernel_fn(a_kernel_fn, w_kernel_fn=w_kernel):
-    """AW kernel function: (A1 conv A2) conv W[yf, xf] on the device (synthesis.py:701-734)."""
-    def fn(theta, w, a1, a2, *src):
-        A = numpy.array([a_kernel_fn(theta, a1, *src), a_kernel_fn(theta, a2, *src)])
-        Wk = numpy.asarray(w_kernel_fn(theta, w))[None]
+class AWKernelFn:
+    """The AW kernel function of aw_kernel_fn (synthesis.py:701-734): called with
+    (theta, w, a1, a2, *src) it returns (A1 conv A2) conv W[yf, xf] for one key,
+    computed on the device in FP64 as the reference does in complex128.
+
+    w_cache_imaging / w_cache_predict / do_imaging / do_predict recognise it as
+    their kernel_cache and, instead of one call per key, generate the kernels of
+    every distinct key in one batched device pass (cg_aw_kernels): the A kernels
+    once per distinct (antenna, *src) and the w kernels once per w bin, from the
+    two callables given here.  Batched tables stay cached on the object (keyed by
+    theta, the keys and the precision), as the reference's kernel cache keeps its
+    kernels between calls."""
+
+    def __init__(self, a_kernel_fn, w_kernel_fn, cache_size=2):
+        self.a_kernel_fn, self.w_kernel_fn = a_kernel_fn, w_kernel_fn
+        self.cache_size = cache_size
+        self._tables = {}
+
+    def __call__(self, theta, w, a1, a2, *src):
+        A = numpy.array([self.a_kernel_fn(theta, a1, *src), self.a_kernel_fn(theta, a2, *src)])
+        Wk = numpy.asarray(self.w_kernel_fn(theta, w))[None]
         one = numpy.zeros(1, dtype=numpy.int32)
         out = E.aw_kernels(A, Wk, one, one + 1, one, dtype=E.CD)
         return _host(out[0])
-    return fn
+
+    def batch(self, theta, wbins, src_rows, dtype):
+        """Device table [nk, Q, Q, SA, SA] of the kernels of keys (wbins[k],
+        *src_rows[k]) with src_rows[k] = (a1, a2, *rest)."""
+        key = (float(theta), numpy.asarray(wbins, numpy.float64).tobytes(),
+               numpy.asarray(src_rows).tobytes(), dtype)
+        if key in self._tables:
+            t = self._tables.pop(key)
+            self._tables[key] = t
+            return t
+        src_rows = numpy.asarray(src_rows)
+        rest = [tuple(r[2:]) for r in src_rows]
+        ants = {}
+        ia = numpy.empty((len(src_rows), 2), dtype=numpy.int32)
+        for k, r in enumerate(src_rows):
+            for j in (0, 1):
+                a = (r[j],) + rest[k]
+                if a not in ants:
+                    ants[a] = len(ants)
+                ia[k, j] = ants[a]
+        A = numpy.array([numpy.asarray(self.a_kernel_fn(theta, a[0], *a[1:]))
+                         for a in ants])
+        wu, wi = numpy.unique(numpy.asarray(wbins, numpy.float64), return_inverse=True)
+        Wk = numpy.array([numpy.asarray(self.w_kernel_fn(theta, w)) for w in wu])
+        t = E.aw_kernels(A, Wk, ia[:, 0], ia[:, 1], wi.astype(numpy.int32).ravel(), dtype=dtype)
+        self._tables[key] = t
+        while len(self._tables) > self.cache_size:
+            self._tables.pop(next(iter(self._tables)))
+        return t
+
+
+def aw_kernel_fn(a_kernel_fn, w_kernel_fn=w_kernel):
+    """AW kernel function: (A1 conv A2) conv W[yf, xf] on the device (synthesis.py:701-734)."""
+    return AWKernelFn(a_kernel_fn, w_kernel_fn)
 
 
 # --------------------------------------------------------------------------
@@ -497,9 +546,12 @@ def _spec_w_cache(theta, uvw_t, uvw_host, src, wstep, kernel_cache, kernel_fn, k
         t = W_KERNEL_TABLES.get(theta, wstep, kmin, kmax, NpixFF, NpixKern, Qpx, invert, dl,
                                 dm, T, dtype)
         return E.KernelTable(t.reshape(-1), False, Qpx, NpixKern), kidx
+    fn = kernel_cache if kernel_cache is not None else kernel_fn
+    dev = _device_keys(theta, uvw_t, src, nsrc, wstep, fn, kwargs, dtype)
+    if dev is not None:
+        return dev
     # Generic kernel callables are host functions: call each once per distinct
     # (wbin, *src_row) key, in first-use order, and upload the table.
-    fn = kernel_cache if kernel_cache is not None else kernel_fn
     uh = uvw_host if uvw_host is not None else uvw_t.cpu().numpy()
     wbin = wstep * numpy.round(uh[:, 2] / wstep)
     s = numpy.zeros((n, 0)) if nsrc == 0 else numpy.asarray(
@@ -514,6 +566,67 @@ def _spec_w_cache(theta, uvw_t, uvw_host, src, wstep, kernel_cache, kernel_fn, k
     Q, S = table.shape[1], table.shape[-1]
     return (E.KernelTable(E.cuda_tensor(table, dtype).reshape(-1), False, Q, S),
             rank[inv.ravel()].astype(numpy.int32))
+
+
+def _int_columns(src, n, nsrc):
+    """The src columns as an int32 [n, nsrc] host array with per-column minima and
+    ranges, or None when a column is not integer-valued or the ranges are too wide
+    for packed keys."""
+    s = src.cpu().numpy() if isinstance(src, torch.Tensor) else numpy.asarray(src)
+    s = s.reshape(n, nsrc)
+    if s.dtype.kind in "iu":
+        si = s
+    elif s.dtype.kind == "f":
+        if not numpy.all(numpy.isfinite(s)) or not numpy.array_equal(numpy.floor(s), s):
+            return None
+        si = s
+    else:
+        return None
+    lo, hi = si.min(axis=0), si.max(axis=0)
+    if numpy.any(lo < -2 ** 31) or numpy.any(hi >= 2 ** 31):
+        return None
+    return si.astype(numpy.int32), lo.astype(numpy.int64), (hi - lo + 1).astype(numpy.int64)
+
+
+def _device_keys(theta, uvw_t, src, nsrc, wstep, fn, kwargs, dtype):
+    """(ktab, kidx) with the distinct (wbin, *src_row) keys found on the device: the
+    w bins and integer src columns packed into one key per visibility
+    (cg_row_keys), compacted to the keys in use (cg_compact_keys); then one call
+    of the kernel callable per distinct key, or, for an AWKernelFn, one batched
+    generation of all of them.  None when the src columns are not integers or
+    the key space is too large (the host path then handles the call)."""
+    n = uvw_t.shape[0]
+    if nsrc == 0 or n == 0:
+        return None
+    cols = _int_columns(src, n, nsrc)
+    if cols is None:
+        return None
+    si, lo, rng = cols
+    st = E.Status()
+    _, kmin, kmax = E.w_bins(uvw_t, wstep, st)
+    st.check()
+    nb = kmax - kmin + 1
+    space = int(nb) * int(numpy.prod(rng))
+    if space >= 2 ** 31 - 1 or space > 64 * n + (1 << 24):
+        return None
+    key = E.row_keys(uvw_t, wstep, kmin, nb, torch.from_numpy(si), lo, rng, st)
+    rows, kor = E.compact_keys(key, space, st)
+    st.check()
+    kor = kor.cpu().numpy().astype(numpy.int64)
+    digits = []
+    r = kor
+    for c in range(nsrc - 1, -1, -1):
+        digits.append(r % rng[c] + lo[c])
+        r = r // rng[c]
+    wbins = wstep * (r + kmin).astype(numpy.float64)
+    srow = numpy.column_stack(digits[::-1])
+    if isinstance(fn, AWKernelFn) and nsrc >= 2 and not kwargs:
+        t = fn.batch(theta, wbins, srow, dtype)
+    else:
+        t = E.cuda_tensor(numpy.array([numpy.asarray(fn(theta, wbins[k], *srow[k], **kwargs))
+                                       for k in range(len(kor))]), dtype)
+    Q, S = t.shape[1], t.shape[-1]
+    return E.KernelTable(t.reshape(-1), False, Q, S), rows
 
 
 def _spec_w_slice(theta, uvw_t, uvw_host, wstep, kernel_fn, kwargs, dtype):
@@ -675,8 +788,8 @@ def do_imaging(theta, lam, uvw, src, vis, imgfn, **kwargs):
     st.check()
     spec = None
     if imgfn is not simple_imaging:
-        spec = _device_spec(imgfn, theta, uvw_t, None if _is_dev(uvw) else uvw_t.cpu().numpy(),
-                            src, kwargs, cplx)
+        # (the host copy of the mirrored uvw is fetched only by the paths that need it)
+        spec = _device_spec(imgfn, theta, uvw_t, None, src, kwargs, cplx)
     if spec is None and imgfn is not simple_imaging:
         # a caller-supplied imaging function: run it as the reference does
         uh = uvw_t.cpu().numpy()

@@ -358,6 +358,16 @@ int cg_compact_keys(const int32_t *key, int64_t n, int nkeys, int32_t *row,
                     int32_t *key_of_row, int32_t *h_nrows, void *workspace,
                     size_t workspace_bytes, int32_t *d_status,
                     cg_stream_t stream);
+/* Kernel-cache keys of w_cache_imaging with integer src columns (the
+ * kernel_cache(theta, wbin, *src[i]) lookup of synthesis.py:793-794):
+ * key[i] = ((round(w_i / wstep) - kmin) * r0 + (c0 - m0)) * r1 + (c1 - m1) ...
+ * over the ncols (<= 8) int32 columns cols[i * ncols + c], with the minima
+ * m and ranges r given on the host; the key space nbins * r0 * r1 ... must
+ * stay below 2^31.  Values outside [m, m + r) count CG_ERR_INDEX.  The keys
+ * feed cg_compact_keys. */
+int cg_row_keys(const double *uvw, int64_t stride, int64_t n, double wstep, int kmin, int nbins,
+                const int32_t *cols, int ncols, const int32_t *col_min, const int32_t *col_range,
+                int32_t *key, int32_t *d_status, cg_stream_t stream);
 /* AW cache keys (the (wbin, a1, a2) arguments of aw_kernel_fn through
  * w_cache_imaging, synthesis.py:719, 793-794; scripts/image_dataset.py:153-171):
  * key[i] = (a1[i] * nant + a2[i]) * nbins + round(w_i / wstep) - kmin. */

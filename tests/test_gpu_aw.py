@@ -91,3 +91,60 @@ def test_aw_full_size_fp32_vs_fp64(aw_workload):
                 torch.linalg.vector_norm(v64))
     assert err < 1e-5, err
     op.status.check()
+
+
+def _aw_reference_case(w, pairs):
+    from oracle import crocodile_oracle as O
+    a1, a2 = w.params["a1"], w.params["a2"]
+    sel = numpy.zeros(len(a1), bool)
+    for p, q in pairs:
+        sel |= (a1 == p) & (a2 == q)
+    beams, wstep, npff = w.params["beams"], w.params["wstep"], w.params["NpixFF"]
+    akern = {}
+
+    def a_fn(theta, a):  # host A kernels, as the reference reads them from its file
+        if a not in akern:
+            akern[a] = O.kernel_oversample(beams[a], 1, 16)[0, 0]
+        return akern[a]
+
+    memo = {}
+    gen = O.aw_kernel_fn(a_fn, lambda theta, ww: O.w_kernel(theta, ww, npff, 16, 16))
+
+    def oracle_fn(theta, ww, p, q):
+        key = (theta, float(ww), int(p), int(q))
+        if key not in memo:
+            memo[key] = gen(theta, ww, p, q)
+        return memo[key]
+
+    src = numpy.column_stack([a1[sel], a2[sel]])
+    return w.uvw[sel], w.vis[sel], src, wstep, npff, a_fn, oracle_fn
+
+
+def test_reference_api_aw_matches_oracle(aw_workload):
+    """The reference's own AW call (scripts/image_dataset.py:162-187):
+    w_cache_imaging / w_cache_predict / do_imaging with src = [a1, a2] and
+    kernel_cache = aw_kernel_fn(a_kernel_fn, w_kernel_fn).  The drop-in keys the
+    visibilities on the device (cg_row_keys + cg_compact_keys) and generates every
+    key's AW kernel in one batched pass; a plain callable as kernel_cache is called
+    once per distinct device key.  Both against the oracle's complex128 loop."""
+    from crocodile_gb300 import synthesis as S
+    from oracle import crocodile_oracle as O
+    w = aw_workload
+    uvw, vis, src, wstep, npff, a_fn, oracle_fn = _aw_reference_case(
+        w, [(0, 1), (3, 17), (10, 40), (25, 63)])
+    fn = S.aw_kernel_fn(a_fn, lambda theta, ww: S.w_kernel(theta, ww, npff, 16, 16))
+    ref = O.w_cache_imaging(w.theta, w.lam, uvw, src, vis, wstep=wstep, kernel_cache=oracle_fn)
+    got = S.w_cache_imaging(w.theta, w.lam, uvw, src, vis, wstep=wstep, kernel_cache=fn)
+    assert rel(got, ref) < 1e-5
+    assert len(fn._tables) == 1  # one batched table, cached on the callable
+    got2 = S.w_cache_imaging(w.theta, w.lam, uvw, src, vis, wstep=wstep, kernel_cache=oracle_fn)
+    assert rel(got2, ref) < 1e-5  # generic callable, device-keyed
+    vref = O.w_cache_predict(w.theta, w.lam, uvw, src, ref, wstep=wstep, kernel_cache=oracle_fn)
+    vgot = S.w_cache_predict(w.theta, w.lam, uvw, src, ref, wstep=wstep, kernel_cache=fn)
+    assert rel(vgot, vref) < 1e-5
+    assert len(fn._tables) == 1  # predict reused the cached table
+    d, p, pm = S.do_imaging(w.theta, w.lam, uvw, src, vis, S.w_cache_imaging, wstep=wstep,
+                            kernel_cache=fn)
+    dr, pr, pmr = O.do_imaging(w.theta, w.lam, uvw, src, vis, O.w_cache_imaging, wstep=wstep,
+                               kernel_cache=oracle_fn)
+    assert rel(d, dr) < 1e-5 and rel(p, pr) < 1e-5 and abs(pm / pmr - 1) < 1e-5
