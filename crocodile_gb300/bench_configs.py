@@ -588,11 +588,45 @@ def measure_ingest(steps=3, blocks=None):
                     "complex128 -> complex64, antennas, inputs resident"}
 
 
+def measure_fft(steps=10):
+    """The hand-written FP32 FFTs of the imaging path against cuFFT (torch.fft) on the
+    same complex64 planes: the centred inverse transform (ifft of synthesis.py,
+    checkerboard and 1/N^2 folded into the two passes), the unshifted unscaled
+    inverse (cuFFT's own operation, out of place), and the dirty image of a grid
+    (hermitian + transform + real part + maximum)."""
+    out = {}
+    for N in (4096, 8192):
+        rng = numpy.random.default_rng(N)
+        g = torch.from_numpy((rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N)))
+                             .astype(numpy.complex64)).cuda()
+        t = g.clone()
+        y = torch.empty_like(g)
+        ms_c = _time(lambda: E.fft_(t, True), steps)
+        ms_r = _time(lambda: E.fft_raw(t, True), steps)
+        ms_cu = _time(lambda: torch.fft.ifft2(t, norm="forward", out=y), steps)
+
+        def image():
+            t.copy_(g)
+            E.image_from_grid(t, want_max=True)
+
+        ms_img = _time(image, steps) - _time(lambda: t.copy_(g), steps)
+        nbytes = N * N * 8
+        out["%d" % N] = {"centred_ifft_ms": ms_c, "raw_ifft_ms": ms_r, "cufft_ifft2_ms": ms_cu,
+                         "raw_vs_cufft": ms_cu / ms_r, "dirty_image_ms": ms_img,
+                         "gb_s_two_passes": 4 * nbytes / (ms_r * 1e-3) / 1e9}
+        del g, t, y
+        torch.cuda.empty_cache()
+    out["note"] = ("complex64 N^2 planes; ours: two in-place passes over HBM (rows, column "
+                   "tiles), radix-4 DIT in shared memory; cuFFT: torch.fft.ifft2 out of place, "
+                   "no normalisation; gb_s counts 2 reads + 2 writes of the plane")
+    return out
+
+
 MEASURES = {"plain": measure_plain, "wproj": measure_wproj, "diff": measure_diff,
             "wstack": measure_wstack, "aw": measure_aw, "wtowers": measure_wtowers,
             "recombine": measure_recombine, "recombine_small": measure_recombine_small,
             "szetan": measure_szetan, "ingest": measure_ingest,
-            "awtowers": measure_awtowers}
+            "awtowers": measure_awtowers, "fft": measure_fft}
 
 
 def run(only=None, steps=None):

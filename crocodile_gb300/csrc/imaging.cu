@@ -22,6 +22,14 @@ namespace cg {
 static std::mutex g_fft_mu;
 static std::map<std::tuple<int, int, int, int, int>, cufftHandle> g_fft_plans;
 
+bool fft32_supported(int H, int W);
+int fft32_planes(float2 *data, int64_t batch, int H, int W, bool inverse, bool centred,
+                 cudaStream_t st);
+int fft32_image(const float2 *grid_premod, int H, int W, float *image, float *max_out,
+                cudaStream_t st);
+bool dfft_supported(int n);
+int dfft2_centred(double2 *data, int64_t batch, int H, int W, int inverse, cudaStream_t st);
+
 int fft_plan(int batch, int H, int W, cufftType type, cufftHandle *out) {
   int dev = 0;
   cudaGetDevice(&dev);
@@ -200,6 +208,13 @@ int centred_fft(void *data, int batch, int H, int W, bool c64, bool inverse,
                 void *workspace, cudaStream_t s) {
   CG_REQUIRE(data && batch >= 1 && H >= 1 && W >= 1, "bad fft arguments");
   if (H == 1 && W == 1) return CG_OK;  // the 1 x 1 transform is the identity (scale 1)
+  // the hand-written transforms: FP32 for complex64 planes with power-of-two
+  // sides 64..8192, double-float (about 48 significant bits) for complex128
+  // planes with sides 64..2048; cuFFT for the other shapes
+  if (c64 && fft32_supported(H, W))
+    return fft32_planes((float2 *)data, batch, H, W, inverse, true, s);
+  if (!c64 && H > 1 && dfft_supported(H) && dfft_supported(W))
+    return dfft2_centred((double2 *)data, batch, H, W, inverse ? 1 : 0, s);
   cufftHandle plan;
   int rc = fft_plan(batch, H, W, c64 ? CUFFT_C2C : CUFFT_Z2Z, &plan);
   if (rc) return rc;
@@ -335,6 +350,8 @@ int cg_fft_raw(void *data, int batch, int H, int W, int is_c64, int inverse,
                cg_stream_t stream) {
   CG_REQUIRE(data && batch >= 1 && H >= 1 && W >= 1, "bad fft arguments");
   cudaStream_t s = (cudaStream_t)stream;
+  if (is_c64 && fft32_supported(H, W))
+    return fft32_planes((float2 *)data, batch, H, W, inverse != 0, false, s);
   cufftHandle plan;
   int rc = fft_plan(batch, H, W, is_c64 ? CUFFT_C2C : CUFFT_Z2Z, &plan);
   if (rc) return rc;
@@ -355,6 +372,8 @@ int cg_image_from_grid(void *grid, int H, int W, float *image, float *max_out,
   const unsigned g = grid_for((int64_t)H * W);
   k_hermitian<float2, true><<<g, 256, 0, s>>>((float2 *)grid, H, W);
   CG_LAUNCH("image hermitian");
+  if (fft32_supported(H, W))  // rows, then columns storing the demodulated real part
+    return fft32_image((const float2 *)grid, H, W, image, max_out, s);
   cufftHandle plan;
   int rc = fft_plan(1, H, W, CUFFT_C2C, &plan);
   if (rc) return rc;

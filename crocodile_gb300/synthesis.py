@@ -842,7 +842,10 @@ def do_predict(theta, lam, uvw, src, modelimage, predfn, **kwargs):
     """Predict visibilities of a model image (synthesis.py:914-927)."""
     prec = _prec(kwargs.pop("precision", None))
     img = modelimage if _is_dev(modelimage) else numpy.asarray(modelimage)
-    ximage = E.cuda_tensor(img, E.CD)
+    # the FP32 path transforms the model in complex64 (its degridding is FP32);
+    # the boxcar and FP64 paths in complex128
+    fp32_fft = prec == "fp32" and predfn in (conv_predict, w_cache_predict, w_slice_predict)
+    ximage = E.cuda_tensor(img, E.CF if fp32_fft else E.CD)
     E.fft_(ximage, False)
     uvw_t = E.cuda_tensor(uvw, torch.float64)
     if predfn is simple_predict:
