@@ -27,28 +27,44 @@ namespace cg {
 
 int fft_plan(int batch, int H, int W, cufftType type, cufftHandle *out);
 
-__constant__ float2 c_tw32[32];  // exp(+2 pi i t / 32)
+__constant__ float2 c_tw32[32];    // exp(+2 pi i t / 32)
+__constant__ double2 c_tw32d[32];  // the same in FP64 (complex128 tables)
 
 namespace {
+
+// the complex type of each precision
+template <typename R> struct Cx;
+template <> struct Cx<float> {
+  typedef float2 T;
+  static __device__ __forceinline__ T tw(int i) { return c_tw32[i]; }
+};
+template <> struct Cx<double> {
+  typedef double2 T;
+  static __device__ __forceinline__ T tw(int i) { return c_tw32d[i]; }
+};
 
 __host__ __device__ constexpr int bitrev5(int i) {
   return ((i & 1) << 4) | ((i & 2) << 2) | (i & 4) | ((i & 8) >> 2) | ((i & 16) >> 4);
 }
 
-template <int H>
-__device__ __forceinline__ void dif_stage(float2 (&x)[32]) {
+template <int H, typename T>
+__device__ __forceinline__ void dif_stage(T (&x)[32]) {
 #pragma unroll
   for (int b = 0; b < 32; b += 2 * H) {
 #pragma unroll
     for (int j = 0; j < H; ++j) {
-      const float2 a = x[b + j], c = x[b + j + H];
-      x[b + j] = make_float2(a.x + c.x, a.y + c.y);
-      const float2 d = make_float2(a.x - c.x, a.y - c.y);
+      const T a = x[b + j], c = x[b + j + H];
+      x[b + j].x = a.x + c.x;
+      x[b + j].y = a.y + c.y;
+      T d;
+      d.x = a.x - c.x;
+      d.y = a.y - c.y;
       if (j == 0) {
         x[b + j + H] = d;
       } else {
-        const float2 w = c_tw32[j * (16 / H)];
-        x[b + j + H] = make_float2(d.x * w.x - d.y * w.y, d.x * w.y + d.y * w.x);
+        const T w = Cx<decltype(d.x)>::tw(j * (16 / H));
+        x[b + j + H].x = d.x * w.x - d.y * w.y;
+        x[b + j + H].y = d.x * w.y + d.y * w.x;
       }
     }
   }
@@ -56,7 +72,8 @@ __device__ __forceinline__ void dif_stage(float2 (&x)[32]) {
 
 // 32-point inverse DFT (exp(+2 pi i), unnormalised): natural order in,
 // bit-reversed order out (x[i] holds output bitrev5(i))
-__device__ __forceinline__ void idft32_dif(float2 (&x)[32]) {
+template <typename T>
+__device__ __forceinline__ void idft32_dif(T (&x)[32]) {
   dif_stage<16>(x);
   dif_stage<8>(x);
   dif_stage<4>(x);
@@ -64,45 +81,49 @@ __device__ __forceinline__ void idft32_dif(float2 (&x)[32]) {
   dif_stage<1>(x);
 }
 
-// FA: akern [nk][16][16] (FP32) zero-padded to [nk][32][32] and scaled by 1/1024
-__global__ void k_pad_akern(const float2 *__restrict__ akern, int nk, float2 *__restrict__ fa) {
+// FA: akern [nk][16][16] zero-padded to [nk][32][32] and scaled by 1/1024
+template <typename T>
+__global__ void k_pad_akern(const T *__restrict__ akern, int nk, T *__restrict__ fa) {
   const int64_t total = (int64_t)nk * 1024;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int k = (int)(e >> 10), r = (int)((e >> 5) & 31), c = (int)(e & 31);
-    float2 v = make_float2(0.f, 0.f);
+    T v;
+    v.x = v.y = 0;
     if (r < 16 && c < 16) {
       v = akern[((int64_t)k * 16 + r) * 16 + c];
-      v.x *= 1.0f / 1024.0f;
-      v.y *= 1.0f / 1024.0f;
+      v.x *= (decltype(v.x))(1.0 / 1024.0);
+      v.y *= (decltype(v.x))(1.0 / 1024.0);
     }
     fa[e] = v;
   }
 }
 
-// FW: W [nWQ][S][S] (FP64) zero-padded to [nWQ][32][32], rounded to FP32
-__global__ void k_pad_w(const double2 *__restrict__ W, int64_t nwq, int S,
-                        float2 *__restrict__ fw) {
+// FW: W [nWQ][S][S] (FP64) zero-padded to [nWQ][32][32] (rounded to FP32 for
+// complex64 tables)
+template <typename T>
+__global__ void k_pad_w(const double2 *__restrict__ W, int64_t nwq, int S, T *__restrict__ fw) {
   const int64_t total = nwq * 1024;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t g = e >> 10;
     const int r = (int)((e >> 5) & 31), c = (int)(e & 31);
-    float2 v = make_float2(0.f, 0.f);
+    T v;
+    v.x = v.y = 0;
     if (r < S && c < S) {
       const double2 d = W[(g * S + r) * S + c];
-      v = make_float2((float)d.x, (float)d.y);
+      v.x = (decltype(v.x))d.x;
+      v.y = (decltype(v.x))d.y;
     }
     fw[e] = v;
   }
 }
 
-template <typename C, int S>
-__global__ void __launch_bounds__(256, 2) k_aw_fftconv(const float2 *__restrict__ fa,
-                                                    const float2 *__restrict__ fw, int nW,
-                                                    int QQ, const int32_t *__restrict__ wi,
-                                                    C *__restrict__ out, int32_t *status) {
-  __shared__ float2 sfa[32][33];
+template <typename T, int S>
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 1) k_aw_fftconv(
+    const T *__restrict__ fa, const T *__restrict__ fw, int nW, int QQ,
+    const int32_t *__restrict__ wi, T *__restrict__ out, int32_t *status) {
+  __shared__ T sfa[32][33];
   constexpr int o = (S - 1) / 2;
   const int k = blockIdx.x;
   const int w = wi[k];
@@ -115,48 +136,49 @@ __global__ void __launch_bounds__(256, 2) k_aw_fftconv(const float2 *__restrict_
     sfa[t >> 5][t & 31] = fa[(int64_t)k * 1024 + t];
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  typedef decltype(sfa[0][0].x) R;
   // this lane's twiddle in each across-lane stage (distance d = 16 .. 1)
-  float2 tw[5];
+  T tw[5];
 #pragma unroll
   for (int st = 0; st < 5; ++st) {
     const int d = 16 >> st;
-    tw[st] = c_tw32[(lane & (d - 1)) * (16 / d)];
+    tw[st] = Cx<R>::tw((lane & (d - 1)) * (16 / d));
   }
   const int n2 = bitrev5(lane);
   const bool keep = n2 >= o && n2 < o + 16;
   for (int f = warp; f < QQ; f += 8) {
-    const float2 *src = fw + ((int64_t)w * QQ + f) * 1024;
-    float2 x[32];
+    const T *src = fw + ((int64_t)w * QQ + f) * 1024;
+    T x[32];
 #pragma unroll
     for (int k1 = 0; k1 < 32; ++k1) {
-      const float2 b = src[k1 * 32 + lane];
-      const float2 a = sfa[k1][lane];
-      x[k1] = make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+      const T b = src[k1 * 32 + lane];
+      const T a = sfa[k1][lane];
+      x[k1].x = a.x * b.x - a.y * b.y;
+      x[k1].y = a.x * b.y + a.y * b.x;
     }
     idft32_dif(x);  // over k1: x[i] = Y[bitrev5(i)][lane]
-    C *dst = out + ((int64_t)k * QQ + f) * 256;
+    T *dst = out + ((int64_t)k * QQ + f) * 256;
 #pragma unroll
     for (int r = 0; r < 16; ++r) {
-      float2 v = x[bitrev5(o + r)];  // row n1 = o + r
+      T v = x[bitrev5(o + r)];  // row n1 = o + r
 #pragma unroll
       for (int st = 0; st < 5; ++st) {
         const int d = 16 >> st;
-        float2 p;
+        T p;
         p.x = __shfl_xor_sync(0xffffffffu, v.x, d);
         p.y = __shfl_xor_sync(0xffffffffu, v.y, d);
         if (lane & d) {  // upper element: (partner - v) * twiddle
-          const float2 q = make_float2(p.x - v.x, p.y - v.y);
-          v = make_float2(q.x * tw[st].x - q.y * tw[st].y, q.x * tw[st].y + q.y * tw[st].x);
+          T q;
+          q.x = p.x - v.x;
+          q.y = p.y - v.y;
+          v.x = q.x * tw[st].x - q.y * tw[st].y;
+          v.y = q.x * tw[st].y + q.y * tw[st].x;
         } else {
-          v = make_float2(v.x + p.x, v.y + p.y);
+          v.x = v.x + p.x;
+          v.y = v.y + p.y;
         }
       }
-      if (keep) {
-        C o2;
-        o2.x = v.x;
-        o2.y = v.y;
-        dst[r * 16 + (n2 - o)] = o2;
-      }
+      if (keep) dst[r * 16 + (n2 - o)] = v;
     }
   }
 }
@@ -165,52 +187,63 @@ __global__ void __launch_bounds__(256, 2) k_aw_fftconv(const float2 *__restrict_
 
 bool aw_fft_supported(int SA, int S) { return SA == 16 && S >= 1 && S <= 16; }
 
+// room for either precision (complex128 spectra)
 size_t aw_fft_workspace_bytes(int nk, int nW, int Q) {
-  return ((size_t)std::max(nk, 1) + (size_t)std::max(nW, 1) * Q * Q) * 1024 * sizeof(float2);
+  return ((size_t)std::max(nk, 1) + (size_t)std::max(nW, 1) * Q * Q) * 1024 * sizeof(double2);
 }
 
-// akern: [nk][16][16] FP32 (the A1 (*) A2 kernels), W: [nW][Q][Q][S][S] FP64.
-int aw_fft_launch(const float2 *akern, int nk, const void *W, int nW, int Q, int S,
-                  const int32_t *wi, void *out, int out_c64, void *ws, size_t ws_bytes,
-                  int32_t *d_status, cudaStream_t st) {
+namespace {
+
+// akern: [nk][16][16] A1 (*) A2 kernels in precision R, W: [nW][Q][Q][S][S] FP64;
+// out: [nk][Q][Q][16][16] complex64 (R = float) or complex128 (R = double).
+template <typename R>
+int aw_fft_run(const typename Cx<R>::T *akern, int nk, const void *W, int nW, int Q, int S,
+               const int32_t *wi, void *out, void *ws, size_t ws_bytes, int32_t *d_status,
+               cudaStream_t st) {
+  typedef typename Cx<R>::T T;
   CG_REQUIRE(aw_fft_supported(16, S), "FFT AW convolution needs 16 x 16 kernels, S <= 16");
   if (ws_bytes < aw_fft_workspace_bytes(nk, nW, Q))
     return set_error(CG_ERR_WORKSPACE, "AW FFT convolution workspace too small");
-  float tw[64];
+  T tw[32];
   for (int t = 0; t < 32; ++t) {
-    tw[2 * t] = (float)std::cos(2.0 * M_PI * t / 32.0);
-    tw[2 * t + 1] = (float)std::sin(2.0 * M_PI * t / 32.0);
+    tw[t].x = (R)std::cos(2.0 * M_PI * t / 32.0);
+    tw[t].y = (R)std::sin(2.0 * M_PI * t / 32.0);
   }
-  CG_CUDA(cudaMemcpyToSymbolAsync(c_tw32, tw, sizeof(tw), 0, cudaMemcpyHostToDevice, st));
-  float2 *fa = (float2 *)ws;
-  float2 *fw = fa + (size_t)nk * 1024;
+  if (sizeof(R) == 4)
+    CG_CUDA(cudaMemcpyToSymbolAsync(c_tw32, tw, sizeof(tw), 0, cudaMemcpyHostToDevice, st));
+  else
+    CG_CUDA(cudaMemcpyToSymbolAsync(c_tw32d, tw, sizeof(tw), 0, cudaMemcpyHostToDevice, st));
+  T *fa = (T *)ws;
+  T *fw = fa + (size_t)nk * 1024;
   const int64_t nwq = (int64_t)nW * Q * Q;
   const unsigned gb = (unsigned)std::min<int64_t>(((int64_t)nk * 1024 + 255) / 256,
                                                   (int64_t)num_sms() * 16);
-  k_pad_akern<<<gb, 256, 0, st>>>(akern, nk, fa);
+  k_pad_akern<T><<<gb, 256, 0, st>>>(akern, nk, fa);
   CG_LAUNCH("AW FFT pad A");
   const unsigned gw = (unsigned)std::min<int64_t>((nwq * 1024 + 255) / 256,
                                                   (int64_t)num_sms() * 16);
-  k_pad_w<<<gw, 256, 0, st>>>((const double2 *)W, nwq, S, fw);
+  k_pad_w<T><<<gw, 256, 0, st>>>((const double2 *)W, nwq, S, fw);
   CG_LAUNCH("AW FFT pad W");
   cufftHandle plan;
   int rc;
   for (int pass = 0; pass < 2; ++pass) {
     const int batch = pass ? (int)nwq : nk;
-    float2 *data = pass ? fw : fa;
-    if ((rc = fft_plan(batch, 32, 32, CUFFT_C2C, &plan))) return rc;
+    T *data = pass ? fw : fa;
+    if ((rc = fft_plan(batch, 32, 32, sizeof(R) == 4 ? CUFFT_C2C : CUFFT_Z2Z, &plan))) return rc;
     if (cufftSetStream(plan, st) != CUFFT_SUCCESS)
       return set_error(CG_ERR_CUDA, "cufftSetStream failed");
-    if (cufftExecC2C(plan, (cufftComplex *)data, (cufftComplex *)data, CUFFT_FORWARD) !=
-        CUFFT_SUCCESS)
-      return set_error(CG_ERR_CUDA, "cufftExecC2C failed (AW FFT convolution)");
+    const cufftResult r =
+        sizeof(R) == 4
+            ? cufftExecC2C(plan, (cufftComplex *)data, (cufftComplex *)data, CUFFT_FORWARD)
+            : cufftExecZ2Z(plan, (cufftDoubleComplex *)data, (cufftDoubleComplex *)data,
+                           CUFFT_FORWARD);
+    if (r != CUFFT_SUCCESS)
+      return set_error(CG_ERR_CUDA, "cuFFT failed (AW FFT convolution)");
   }
   const int QQ = Q * Q;
-  CG_REQUIRE(out_c64, "the FFT AW convolution writes complex64 tables");
-#define CG_AW_FFT_CASE(SS)                                                            \
-  case SS:                                                                            \
-    k_aw_fftconv<float2, SS><<<nk, 256, 0, st>>>(fa, fw, nW, QQ, wi, (float2 *)out, \
-                                                 d_status);                           \
+#define CG_AW_FFT_CASE(SS)                                                               \
+  case SS:                                                                               \
+    k_aw_fftconv<T, SS><<<nk, 256, 0, st>>>(fa, fw, nW, QQ, wi, (T *)out, d_status);     \
     break;
   switch (S) {
     CG_AW_FFT_CASE(1) CG_AW_FFT_CASE(2) CG_AW_FFT_CASE(3) CG_AW_FFT_CASE(4)
@@ -221,6 +254,22 @@ int aw_fft_launch(const float2 *akern, int nk, const void *W, int nW, int Q, int
 #undef CG_AW_FFT_CASE
   CG_LAUNCH("AW FFT convolution");
   return CG_OK;
+}
+
+}  // namespace
+
+int aw_fft_launch(const float2 *akern, int nk, const void *W, int nW, int Q, int S,
+                  const int32_t *wi, void *out, int out_c64, void *ws, size_t ws_bytes,
+                  int32_t *d_status, cudaStream_t st) {
+  CG_REQUIRE(out_c64, "aw_fft_launch writes complex64 tables");
+  return aw_fft_run<float>(akern, nk, W, nW, Q, S, wi, out, ws, ws_bytes, d_status, st);
+}
+
+// complex128 tables in FP64 throughout: FP64 spectra, products and transforms
+int aw_fft_launch64(const double2 *akern, int nk, const void *W, int nW, int Q, int S,
+                    const int32_t *wi, void *out, void *ws, size_t ws_bytes, int32_t *d_status,
+                    cudaStream_t st) {
+  return aw_fft_run<double>(akern, nk, W, nW, Q, S, wi, out, ws, ws_bytes, d_status, st);
 }
 
 }  // namespace cg

@@ -26,6 +26,9 @@ size_t aw_fft_workspace_bytes(int nk, int nW, int Q);
 int aw_fft_launch(const float2 *akern, int nk, const void *W, int nW, int Q, int S,
                   const int32_t *wi, void *out, int out_c64, void *ws, size_t ws_bytes,
                   int32_t *d_status, cudaStream_t st);
+int aw_fft_launch64(const double2 *akern, int nk, const void *W, int nW, int Q, int S,
+                    const int32_t *wi, void *out, void *ws, size_t ws_bytes, int32_t *d_status,
+                    cudaStream_t st);
 
 struct FarField {
   int kind;  // 0: from ff array, 1: w-kernel phase
@@ -564,6 +567,10 @@ int cg_aw_kernels(const void *A, int nA, int SA, const void *Wk, int nW, int Q, 
     k_aw_akern<double, double2><<<nk, 256, sh_a, st>>>((const double2 *)A, SA, a1, a2, nA,
                                                        akern64, d_status);
     CG_LAUNCH("aw akern (FP64)");
+    if (aw_fft_supported(SA, S))  // the 32 x 32 FFT form in FP64
+      return aw_fft_launch64(akern64, nk, Wk, nW, Q, S, wi, out,
+                             (char *)ws + aw_ws_akern_bytes(nk, SA),
+                             ws_bytes - aw_ws_akern_bytes(nk, SA), d_status, st);
     dim3 grid(Q * Q, nk);
     if (SA == 16 && S <= 16) {
       const size_t smem = (size_t)(SA * SA + S * (S + 1)) * sizeof(double2);
