@@ -748,6 +748,22 @@ def run_ours(args):
     G._prepare()
     torch.cuda.synchronize()
     kgen_warm_ms = 1e3 * (time.perf_counter() - t0)
+    # the same again with the caching allocator holding the blocks of the last
+    # table (no fresh device allocation), and a bare allocation of the table's
+    # size after the cache is released: what separates the two warm figures
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    G._prepare()
+    torch.cuda.synchronize()
+    kgen_cached_ms = 1e3 * (time.perf_counter() - t0)
+    tbytes = G.kt.table.numel() * 8
+    torch.cuda.empty_cache()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    probe = torch.empty(tbytes, dtype=torch.uint8, device=G.dev)
+    torch.cuda.synchronize()
+    alloc_ms = 1e3 * (time.perf_counter() - t0)
+    del probe
 
     # ---- roofline of the dominant kernel: the step's algorithmic bytes (inputs
     # and outputs of grid + degrid from the configuration's parameters), half of
@@ -890,6 +906,8 @@ def run_ours(args):
                       "plan_and_grid_zeroing": ms_eager - ms_grid - ms_degrid,
                       "kernel_generation_once": G.kgen_ms,
                       "kernel_generation_warm": kgen_warm_ms,
+                      "kernel_generation_warm_cached_blocks": kgen_cached_ms,
+                      "fresh_allocation_of_table_size": alloc_ms,
                       "kernel_generation_fp64": getattr(G, "kgen64_ms", None)},
         "plain_fp64": {"value": plain_value, "unit": "Mvis/s", "ms_per_step": ms_plain,
                        "form": "complex128, FP64 atomics, " + G.groups_desc},
