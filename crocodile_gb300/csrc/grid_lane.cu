@@ -30,7 +30,7 @@
 
 namespace cg {
 
-static constexpr int LANE_DEPTH = 4;                          // bulk-copy stages per warp
+static constexpr int LANE_DEPTH = 4;                          // bulk-copy stages per warp (max)
 static constexpr int LANE_RING = 64;                          // staged visibility records per warp
 static constexpr long long LANE_WAIT_CYCLES = 4000000000ll;   // ~2 s at 2 GHz
 static constexpr unsigned FULL_MASK = 0xffffffffu;
@@ -45,6 +45,7 @@ struct LaneArgs {
   int mode;               // gridding: 0 vis, 1 vis * weight, 2 weight; fused: 0 plain, 1 residual
   long long wait_cycles;  // limit of a consumer's wait for a slice (the drain keeps LANE_WAIT_CYCLES)
   int kstride;            // elements between slices in ktab and in the stage ring (4-D tables)
+  int depth;              // bulk-copy stages per warp, 2..LANE_DEPTH
   int warp_bytes;         // shared memory per warp
   int stage_off, meta_off, val_off, bar_off;  // byte offsets inside a warp's region
 };
@@ -149,7 +150,7 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
 
   for (int c = lane; c < pitch * win; c += 32) wbuf[c] = zero;
   if (BULK && lane == 0) {
-    for (int d = 0; d < LANE_DEPTH; ++d) mbar_init(&bar[d], 1);
+    for (int d = 0; d < P.depth; ++d) mbar_init(&bar[d], 1);
     mbar_fence_init();
   }
   __syncwarp();
@@ -209,11 +210,11 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
     int issued = 0;
     if (BULK) {
       int ist = cst;
-      for (; issued < min(n, LANE_DEPTH - 1); ++issued) {
+      for (; issued < min(n, P.depth - 1); ++issued) {
         const int4 m = meta[issued];
         bulk_load_if(lane == 0, stages + (size_t)ist * KS, P.ktab + (size_t)m.y * KS,
                      slice_bytes, &bar[ist]);
-        ist = ist + 1 == LANE_DEPTH ? 0 : ist + 1;
+        ist = ist + 1 == P.depth ? 0 : ist + 1;
       }
     }
 
@@ -245,7 +246,7 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
       if (BULK) {
         if (issued < n) {
           const int4 mi = meta[issued & (LANE_RING - 1)];
-          const int ist = cst == 0 ? LANE_DEPTH - 1 : cst - 1;
+          const int ist = cst == 0 ? P.depth - 1 : cst - 1;
           bulk_load_if(lane == 0, stages + (size_t)ist * KS, P.ktab + (size_t)mi.y * KS,
                        slice_bytes, &bar[ist]);
           ++issued;
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
         const float2 *kp = stages + (size_t)cst * KS + lane;
 #pragma unroll
         for (int i = 0; i < MAXT; ++i) kc[i] = own[i] ? kp[32 * i] : zero;
-        if (++cst == LANE_DEPTH) {
+        if (++cst == P.depth) {
           cst = 0;
           cpar ^= 1u;
         }
@@ -352,7 +353,7 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
         uint32_t par = cpar;
         for (int jx = j; jx < issued; ++jx) {
           mbar_wait(&bar[st], par);
-          if (++st == LANE_DEPTH) {
+          if (++st == P.depth) {
             st = 0;
             par ^= 1u;
           }
@@ -429,6 +430,7 @@ int lane_launch(const cg_plan *p, const float2 *ktab, const float2 *vis, const f
   }
   const bool bulk = !p->kd.sep && (KS * 8) % 16 == 0 && ((uintptr_t)ktab & 15) == 0;
 
+  const cg_tuning t = tuning();
   LaneArgs P;
   P.ktab = ktab;
   P.vis = vis;
@@ -442,16 +444,18 @@ int lane_launch(const cg_plan *p, const float2 *ktab, const float2 *vis, const f
   auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
   size_t off = up16((size_t)p->pitch * p->win * sizeof(float2));
   P.stage_off = (int)off;
-  if (bulk) off += (size_t)LANE_DEPTH * KS * sizeof(float2);
+  // stages: the tuning's rows field (2..4) for the lane layout, 4 by default
+  const int depth = t.rows >= 2 && t.rows <= LANE_DEPTH ? t.rows : LANE_DEPTH;
+  P.depth = depth;
+  if (bulk) off += (size_t)depth * KS * sizeof(float2);
   P.meta_off = (int)off;
   off += LANE_RING * sizeof(int4);
   P.val_off = (int)off;
   off += LANE_RING * sizeof(float2);
   P.bar_off = (int)off;
-  off = up16(off + LANE_DEPTH * sizeof(uint64_t));
+  off = up16(off + depth * sizeof(uint64_t));
   P.warp_bytes = (int)off;
 
-  const cg_tuning t = tuning();
   // warps per CTA: as asked (or as many as fill ~220 KB), at most what fits in 227 KB
   const int fit = (int)std::min<size_t>(16, (227u << 10) / off);
   CG_REQUIRE(fit >= 1, "lane-layout window does not fit in shared memory (%zu bytes per warp)",

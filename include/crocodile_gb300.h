@@ -100,12 +100,14 @@ typedef struct {
  * cells by position mod S and keep running sums in registers) or
  * CG_LAYOUT_LANE (one warp per work item with a private window, lanes own
  * cells by position mod S, kernel slices streamed by bulk copies; S <= 16;
- * also selects the lane form of cg_degrid_grid); rows: row residues per
- * owner-layout thread (1..8); groups: owner-layout thread groups, or
- * warp-layout warps, per CTA (1..8), or lane-layout warps per CTA (1..16).
- * layout 0 picks CG_LAYOUT_LANE (with 16-cell tiles) for non-separable tables
- * with even S <= 16, whose slices stream by bulk copies, and CG_LAYOUT_WARP
- * otherwise.  Process-wide. */
+ * also selects the lane form of cg_degrid_grid; odd S * S slices stream
+ * from a padded copy of the table in the plan's workspace); rows: row
+ * residues per owner-layout thread (1..8), or bulk-copy stages per
+ * lane-layout warp (2..4; other values: 4); groups: owner-layout thread
+ * groups, or warp-layout warps, per CTA (1..8), or lane-layout warps per
+ * CTA (1..16).  layout 0 picks CG_LAYOUT_LANE (with 16-cell tiles) for
+ * non-separable tables with even S <= 16, whose slices stream by bulk
+ * copies as they are, and CG_LAYOUT_WARP otherwise.  Process-wide. */
 #define CG_LAYOUT_WARP 1
 #define CG_LAYOUT_OWNER 2
 #define CG_LAYOUT_LANE 3

@@ -94,6 +94,8 @@ def _wproj_case(O, n=20000, N=256, seed=5):
     {"layout": 3, "tile": 32},
     {"layout": 3, "groups": 3, "tile": 16, "chunk": 40},
     {"layout": 3, "groups": 16, "tile": 24},
+    {"layout": 3, "rows": 2, "tile": 16},            # two bulk-copy stages per warp
+    {"layout": 3, "rows": 3, "groups": 14, "tile": 16, "chunk": 64},
 ])
 def test_gridder_shapes_match_oracle(env, cfg):
     torch, E, S, A, O = env
@@ -161,9 +163,11 @@ def test_fused_wbin_plan(env):
     assert float(g2.abs().sum()) == 0.0
 
 
-@pytest.mark.parametrize("sep,S_,layout", [(False, 7, 1), (True, 7, 1), (False, 7, 3),
-                                           (True, 7, 3), (False, 8, 3), (False, 16, 3)])
-def test_fused_degrid_grid_matches_separate(env, sep, S_, layout):
+@pytest.mark.parametrize("sep,S_,layout,rows", [(False, 7, 1, 0), (True, 7, 1, 0),
+                                                (False, 7, 3, 0), (True, 7, 3, 0),
+                                                (False, 8, 3, 0), (False, 16, 3, 0),
+                                                (False, 16, 3, 2)])
+def test_fused_degrid_grid_matches_separate(env, sep, S_, layout, rows):
     torch, E, S, A, O = env
     theta, lam, uvw, vis = _wproj_case(O, n=30000, N=256, seed=13)
     N = int(round(theta * lam))
@@ -171,7 +175,7 @@ def test_fused_degrid_grid_matches_separate(env, sep, S_, layout):
     kv = O.kernel_oversample(aa, 4, S_) if sep else \
         O.kernel_oversample(numpy.outer(aa, aa), 4, S_)
     kt = E.KernelTable.from_gcf(kv, 0, E.CF)
-    A.set_tuning(layout=layout)
+    A.set_tuning(layout=layout, rows=rows)
     try:
         _fused_checks(torch, E, kt, uvw, lam, N, vis)
     finally:
