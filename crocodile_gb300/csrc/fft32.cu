@@ -5,14 +5,16 @@
 // for sides 64 .. 8192.
 //
 // Two passes over HBM per plane, both in place:
-//   rows:    each CTA loads whole rows (bit-reversed into shared memory),
-//            transforms them with the radix-4 DIT of fft32.h and stores them;
-//   columns: each CTA loads a tile of C adjacent columns (C x 8 bytes of every
-//            row, H x C <= 16384 elements), transforms every column of the
-//            tile and stores it.
-// Neither needs a second buffer (the DIT runs in place on the bit-reversed
-// line), so even 8192-long columns fit two to a CTA.  The centring of the
-// centred transform is the checkerboard identity for even sides,
+//   rows:    512 threads per CTA transform 512 / (N / 16) whole rows;
+//   columns: up to 512 threads per CTA transform a tile of C adjacent
+//            columns (C x 8 bytes of every row, H x C <= 8192 elements).
+// Each line runs the register-blocked Stockham stages of fft32.h (radix 16,
+// 16 values per thread): the first stage reads global memory and the last
+// writes it, coalesced; the stages between exchange through one padded
+// shared-memory buffer (every thread reads, barrier, every thread writes),
+// so a line makes one or two round trips through shared memory.  The
+// centring of the centred transform is the checkerboard identity for even
+// sides,
 //   fftshift(F(ifftshift x))[k] = (-1)^(k + H/2 + W/2) F((-1)^n x)[k],
 // folded into the row pass's loads and the column pass's stores together
 // with the 1 / (H W) of the inverse; the dirty image's real part, sign and
@@ -31,29 +33,11 @@ namespace cg {
 namespace f32 {
 
 constexpr int MIN_LOG = 6, MAX_LOG = 13;
-constexpr int ROW_THREADS = 512, COL_THREADS = 1024;
+constexpr int ROW_THREADS = 512, COL_THREADS = 512;
 
-__device__ __forceinline__ int pad(int i) { return i + (i >> 5); }  // bank spread
+__device__ __forceinline__ int pad(int e) { return e + (e >> 5); }  // bank spread
 
-// A line in shared memory: element p at base[pad(p) * C + c] (C lines interleaved).
-struct SmLine {
-  float2 *base;
-  int C, c;
-  __device__ cf get(int p) const {
-    const float2 v = base[pad(p) * C + c];
-    return {v.x, v.y};
-  }
-  __device__ void set(int p, cf v) const { base[pad(p) * C + c] = make_float2(v.x, v.y); }
-};
-struct SmTw {
-  const float2 *t;
-  __device__ cf get(int k) const {
-    const float2 v = t[k];
-    return {v.x, v.y};
-  }
-};
-
-// w_N^k = exp(sign 2 pi i k / N), k < N / 2, cached per device, log N and sign
+// w_N^j = exp(sign 2 pi i j / N), j < N, cached per device, log N and sign
 std::mutex g_mu;
 std::map<std::tuple<int, int, int>, float2 *> g_tw;
 
@@ -68,8 +52,8 @@ int twiddles(int logn, int sign, const float2 **out) {
     return CG_OK;
   }
   const int n = 1 << logn;
-  std::vector<float2> h(n / 2);
-  for (int k = 0; k < n / 2; ++k) {
+  std::vector<float2> h(n);
+  for (int k = 0; k < n; ++k) {
     const double a = 2.0 * M_PI * (double)k / (double)n;
     h[k] = make_float2((float)std::cos(a), (float)(sign * std::sin(a)));
   }
@@ -145,102 +129,98 @@ __device__ __forceinline__ void atomic_max_f(float *addr, float v) {
 }
 
 // ---------------------------------------------------------------- kernels
-// R = 2048 / N rows per CTA for short rows (at least 512 butterflies a stage).
+// T = N / 16 threads per line.  Rows: 512 / T lines per CTA.
 template <int LOGN>
 __global__ void __launch_bounds__(ROW_THREADS) k_fft32_rows(RowIO io, int64_t nrows,
                                                             const float2 *__restrict__ tw,
                                                             int sign) {
-  constexpr int N = 1 << LOGN;
-  constexpr int R = N >= 2048 ? 1 : 2048 / N;
-  constexpr int P = N + N / 32;  // padded row
+  constexpr int N = 1 << LOGN, T = N / 16, LPC = ROW_THREADS / T, P = N + N / 32;
+  constexpr int NS = (LOGN + 3) / 4;
   extern __shared__ float2 f32_sm[];
-  float2 *stw = f32_sm;
-  float2 *rows = f32_sm + N / 2;
-  const int tid = threadIdx.x;
-  for (int k = tid; k < N / 2; k += ROW_THREADS) stw[k] = tw[k];
-  const SmTw T{stw};
-  for (int64_t row0 = (int64_t)blockIdx.x * R; row0 < nrows; row0 += (int64_t)gridDim.x * R) {
-    __syncthreads();  // twiddles staged; the previous rows' stores have read smem
-    for (int e = tid; e < R * N; e += ROW_THREADS) {
-      const int r = e >> LOGN, i = e & (N - 1);
-      const int64_t row = row0 + r;
-      rows[r * P + pad((int)bitrev((unsigned)i, LOGN))] =
-          row < nrows ? io.ld(row, i) : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    int lh = 0;
-    if (LOGN & 1) {
-      for (int b = tid; b < R * N / 2; b += ROW_THREADS) {
-        SmLine x{rows + (b >> (LOGN - 1)) * P, 1, 0};
-        radix2_first(x, b & (N / 2 - 1));
+  const int line = threadIdx.x / T, t = threadIdx.x % T;
+  float2 *buf = f32_sm + line * P;
+  auto twf = [&](int j) {
+    const float2 w = __ldg(&tw[j]);
+    return cf{w.x, w.y};
+  };
+  auto lds = [&](int e) {
+    const float2 v = buf[pad(e)];
+    return cf{v.x, v.y};
+  };
+  auto sts = [&](int e, cf v) { buf[pad(e)] = make_float2(v.x, v.y); };
+  for (int64_t row0 = (int64_t)blockIdx.x * LPC; row0 < nrows; row0 += (int64_t)gridDim.x * LPC) {
+    const int64_t row = row0 + line;
+    const bool live = row < nrows;
+    cf v[16];
+    stage_load(LOGN, 0, t, [&](int e) {
+      const float2 x = live ? io.ld(row, e) : make_float2(0.f, 0.f);
+      return cf{x.x, x.y};
+    }, twf, v);
+    stage_dft(LOGN, 0, sign, v);
+    stage_store(LOGN, 0, t, sts, v);
+#pragma unroll
+    for (int s = 1; s < NS; ++s) {
+      __syncthreads();  // the previous stage's stores are visible
+      stage_load(LOGN, s, t, lds, twf, v);
+      __syncthreads();  // every read of this stage is done before any write
+      stage_dft(LOGN, s, sign, v);
+      if (s + 1 < NS) {
+        stage_store(LOGN, s, t, sts, v);
+      } else if (live) {
+        stage_store(LOGN, s, t, [&](int e, cf x) { io.st(row, e, make_float2(x.x, x.y)); }, v);
       }
-      __syncthreads();
-      lh = 1;
-    }
-#pragma unroll 1
-    for (; lh + 1 < LOGN; lh += 2) {
-      for (int b = tid; b < R * N / 4; b += ROW_THREADS) {
-        SmLine x{rows + (b >> (LOGN - 2)) * P, 1, 0};
-        radix4(x, T, LOGN, lh, b & (N / 4 - 1), sign);
-      }
-      __syncthreads();
-    }
-    for (int e = tid; e < R * N; e += ROW_THREADS) {
-      const int r = e >> LOGN, i = e & (N - 1);
-      const int64_t row = row0 + r;
-      if (row < nrows) io.st(row, i, rows[r * P + pad(i)]);
     }
   }
 }
 
-// Tiles of C columns of one plane; units = planes * (W / C).
+// Tiles of C columns of one plane (units = planes * W / C), T = H / 16
+// threads per column, thread (t, c) with c fastest for coalesced rows.
 template <int LOGH, int C, class IO>
 __global__ void __launch_bounds__(COL_THREADS) k_fft32_cols(IO io, int64_t nplanes, int W,
                                                             const float2 *__restrict__ tw,
                                                             int sign, float *max_out) {
-  constexpr int H = 1 << LOGH;
+  constexpr int H = 1 << LOGH, T = H / 16;
+  constexpr int NS = (LOGH + 3) / 4;
   extern __shared__ float2 f32_sm[];
-  float2 *stw = f32_sm;
-  float2 *cols = f32_sm + H / 2;
-  const int tid = threadIdx.x;
-  for (int k = tid; k < H / 2; k += COL_THREADS) stw[k] = tw[k];
-  const SmTw T{stw};
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  auto twf = [&](int j) {
+    const float2 w = __ldg(&tw[j]);
+    return cf{w.x, w.y};
+  };
+  auto lds = [&](int e) {
+    const float2 v = f32_sm[pad(e) * C + c];
+    return cf{v.x, v.y};
+  };
+  auto sts = [&](int e, cf v) { f32_sm[pad(e) * C + c] = make_float2(v.x, v.y); };
   const int per_plane = W / C;
   float mx = -FLT_MAX;
   for (int64_t unit = blockIdx.x; unit < nplanes * per_plane; unit += gridDim.x) {
     const int64_t plane = unit / per_plane;
-    const int c0 = (int)(unit - plane * per_plane) * C;
-    __syncthreads();
-    for (int e = tid; e < H * C; e += COL_THREADS) {
-      const int i = e / C, c = e - (e / C) * C;
-      cols[pad((int)bitrev((unsigned)i, LOGH)) * C + c] = io.ld(plane, i, c0 + c);
-    }
-    __syncthreads();
-    int lh = 0;
-    if (LOGH & 1) {
-      for (int b = tid; b < C * H / 2; b += COL_THREADS) {
-        SmLine x{cols, C, b % C};
-        radix2_first(x, b / C);
-      }
+    const int col = (int)(unit - plane * per_plane) * C + c;
+    cf v[16];
+    __syncthreads();  // the previous tile's last reads of shared memory are done
+    stage_load(LOGH, 0, t, [&](int e) {
+      const float2 x = io.ld(plane, e, col);
+      return cf{x.x, x.y};
+    }, twf, v);
+    stage_dft(LOGH, 0, sign, v);
+    stage_store(LOGH, 0, t, sts, v);
+#pragma unroll
+    for (int s = 1; s < NS; ++s) {
       __syncthreads();
-      lh = 1;
-    }
-#pragma unroll 1
-    for (; lh + 1 < LOGH; lh += 2) {
-      for (int b = tid; b < C * H / 4; b += COL_THREADS) {
-        SmLine x{cols, C, b % C};
-        radix4(x, T, LOGH, lh, b / C, sign);
-      }
+      stage_load(LOGH, s, t, lds, twf, v);
       __syncthreads();
-    }
-    for (int e = tid; e < H * C; e += COL_THREADS) {
-      const int i = e / C, c = e - (e / C) * C;
-      io.st(plane, i, c0 + c, cols[pad(i) * C + c], mx);
+      stage_dft(LOGH, s, sign, v);
+      if (s + 1 < NS)
+        stage_store(LOGH, s, t, sts, v);
+      else
+        stage_store(LOGH, s, t, [&](int e, cf x) { io.st(plane, e, col, make_float2(x.x, x.y), mx); },
+                    v);
     }
   }
   if (IO::kMax && max_out) {
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if ((tid & 31) == 0) atomic_max_f(max_out, mx);
+    if ((threadIdx.x & 31) == 0) atomic_max_f(max_out, mx);
   }
 }
 
@@ -254,37 +234,38 @@ int log2_exact(int n) {
 
 template <int LOGN>
 int launch_rows(const RowIO &io, int64_t nrows, int sign, cudaStream_t st) {
-  constexpr int N = 1 << LOGN;
-  constexpr int R = N >= 2048 ? 1 : 2048 / N;
+  constexpr int N = 1 << LOGN, T = N / 16, LPC = ROW_THREADS / T;
   const float2 *tw;
   int rc = twiddles(LOGN, sign, &tw);
   if (rc) return rc;
-  const size_t smem = (size_t)(N / 2 + R * (N + N / 32)) * sizeof(float2);
+  const size_t smem = (size_t)LPC * (N + N / 32) * sizeof(float2);
   CG_CUDA(cudaFuncSetAttribute(k_fft32_rows<LOGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem));
-  const int64_t ctas = (nrows + R - 1) / R;
-  const unsigned grid = (unsigned)std::min<int64_t>(ctas, (int64_t)num_sms() * 4);
+  const int64_t ctas = (nrows + LPC - 1) / LPC;
+  const unsigned grid = (unsigned)std::min<int64_t>(ctas, (int64_t)num_sms() * 3);
   k_fft32_rows<LOGN><<<grid, ROW_THREADS, smem, st>>>(io, nrows, tw, sign);
   CG_LAUNCH("FP32 FFT rows");
   return CG_OK;
 }
 
-// columns per tile: H * C <= 16384 elements (128 KB), at most 32
-constexpr int cols_for(int logh) { return logh >= 13 ? 2 : logh >= 9 ? (1 << (14 - logh)) : 32; }
+// columns per tile: 512 threads (T = H / 16 per column), at most 32 columns
+constexpr int cols_for(int logh) {
+  return (COL_THREADS >> (logh - 4)) < 32 ? (COL_THREADS >> (logh - 4)) : 32;
+}
 
 template <int LOGH, class IO>
 int launch_cols(const IO &io, int64_t nplanes, int W, int sign, float *max_out, cudaStream_t st) {
-  constexpr int H = 1 << LOGH, C = cols_for(LOGH);
+  constexpr int H = 1 << LOGH, C = cols_for(LOGH), T = H / 16;
   CG_REQUIRE(W % C == 0, "FP32 FFT: width %d is not a multiple of the column tile %d", W, C);
   const float2 *tw;
   int rc = twiddles(LOGH, sign, &tw);
   if (rc) return rc;
-  const size_t smem = (size_t)(H / 2 + (H + H / 32) * C) * sizeof(float2);
+  const size_t smem = (size_t)(H + H / 32) * C * sizeof(float2);
   CG_CUDA(cudaFuncSetAttribute(k_fft32_cols<LOGH, C, IO>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t units = nplanes * (W / C);
   const unsigned grid = (unsigned)std::min<int64_t>(units, (int64_t)num_sms() * 2);
-  k_fft32_cols<LOGH, C, IO><<<grid, COL_THREADS, smem, st>>>(io, nplanes, W, tw, sign, max_out);
+  k_fft32_cols<LOGH, C, IO><<<grid, C * T, smem, st>>>(io, nplanes, W, tw, sign, max_out);
   CG_LAUNCH("FP32 FFT columns");
   return CG_OK;
 }

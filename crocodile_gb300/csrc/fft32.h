@@ -1,20 +1,21 @@
-// In-place radix-4 decimation-in-time FFT of one line of N = 2^logn complex
-// values held in an indexable buffer (shared memory on the device; plain
-// arrays in tests/fft32_check.cpp, which checks it on the host against a
-// direct DFT).  Plain C++ apart from the qualifiers.
+// Register-blocked Stockham FFT of power-of-two lines (N = 2^logn, 64..8192)
+// in FP32: the arithmetic shared by the kernels of fft32.cu and the host
+// check tests/fft32_check.cpp.  Plain C++ apart from the qualifiers.
 //
-// The line is loaded in bit-reversed order (element i at position
-// bitrev(i)); the stages then leave X[k] at position k.  Radix-2 DIT stage
-// with half-span h (h = 1, 2, 4, ..., N/2): for groups of 2h and j < h,
-//   (x[a], x[a + h]) <- (x[a] + w^j x[a + h], x[a] - w^j x[a + h]),
-//   w = w_N^(N / 2h), w_N = exp(sign 2 pi i / N).
-// Two consecutive stages h, 2h form one radix-4 butterfly on a0 = g 4h + j,
-// a1 = a0 + h, a2 = a0 + 2h, a3 = a0 + 3h (j < h):
-//   stage h:  b0,1 = x0 +- w1 x1,  b2,3 = x2 +- w1 x3,   w1 = w_N^(j N / 2h)
-//   stage 2h: c0,2 = b0 +- w2 b2,  c1,3 = b1 +- w3 b3,   w2 = w_N^(j N / 4h),
-//             w3 = w2 w_N^(N/4) = w2 * (sign i)
-// With odd logn one radix-2 stage (h = 1, twiddle 1) comes first.  The
-// twiddle table holds w_N^k for k < N / 2.
+// Every stage is radix 16 except one first stage of radix 2^(logn mod 4)
+// when logn is not a multiple of 4.  A line is worked by T = N / 16
+// threads, each holding 16 values in registers per stage: 16 / R
+// butterflies of radix R.  Stage with span p (the length of the
+// subsequences already transformed: 1 at the first stage, then times R):
+// butterfly b (b < N / R), k = b mod p,
+//   inputs  x[b + r N/R]                (r < R), times the twiddle w_N^(r k N/(pR)),
+//   an R-point DFT (w_R = exp(sign 2 pi i / R)),
+//   outputs y[(b - k) R + k + r p].
+// The last stage has p = N / R, so its outputs y[b + r p] are in natural
+// order, and every stage's inputs x[b + r N/R] are contiguous across b:
+// the first stage reads and the last stage writes global memory directly,
+// coalesced across threads.  Between stages all threads read their inputs
+// before any thread writes, so one buffer holds the line throughout.
 #pragma once
 
 #ifdef __CUDACC__
@@ -39,58 +40,147 @@ CG_FHD cf cf_mul(cf a, cf b) {
   return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
 #endif
 }
-// times (sign i): sign > 0: i (a.x, a.y) = (-a.y, a.x); sign < 0: -i -> (a.y, -a.x)
+// times (sign i): sign > 0: i (x + iy) = -y + ix; sign < 0: -i (x + iy) = y - ix
 CG_FHD cf cf_mul_si(cf a, int sign) { return sign > 0 ? cf{-a.y, a.x} : cf{a.y, -a.x}; }
 
-CG_FHD unsigned bitrev(unsigned i, int logn) {
-#ifdef __CUDA_ARCH__
-  return __brev(i) >> (32 - logn);
-#else
-  unsigned r = 0;
-  for (int b = 0; b < logn; ++b) r |= ((i >> b) & 1u) << (logn - 1 - b);
-  return r;
-#endif
+// stages of a 2^logn transform: count, log2 radix and log2 span of stage s
+CG_FHD int stage_count(int logn) { return (logn + 3) / 4; }
+CG_FHD int stage_logr(int logn, int s) { return ((logn & 3) && s == 0) ? (logn & 3) : 4; }
+CG_FHD int stage_logp(int logn, int s) {
+  const int rem = logn & 3;
+  return s == 0 ? 0 : (rem ? rem + 4 * (s - 1) : 4 * s);
 }
 
-// Butterfly q of the odd-logn radix-2 first stage (q < N / 2): pair (2q, 2q + 1).
-template <class BUF>
-CG_FHD void radix2_first(BUF &x, int q) {
-  const cf u = x.get(2 * q), v = x.get(2 * q + 1);
-  x.set(2 * q, cf_add(u, v));
-  x.set(2 * q + 1, cf_sub(u, v));
+// R-point DFTs in place, X[k] = sum_n v[n] w_R^(n k)
+CG_FHD void dft2(cf *v) {
+  const cf a = v[0], b = v[1];
+  v[0] = cf_add(a, b);
+  v[1] = cf_sub(a, b);
 }
-
-// Radix-4 butterfly q (q < N / 4) of the stage pair (h, 2h), h = 2^lh.
-template <class BUF, class TW>
-CG_FHD void radix4(BUF &x, const TW &tw, int logn, int lh, int q, int sign) {
-  const int h = 1 << lh;
-  const int j = q & (h - 1), g = q >> lh;
-  const int a0 = (g << (lh + 2)) + j;
-  const cf x0 = x.get(a0), x1 = x.get(a0 + h), x2 = x.get(a0 + 2 * h), x3 = x.get(a0 + 3 * h);
-  // w1 = w_N^(j N / 2h), w2 = w_N^(j N / 4h)
-  const cf w1 = tw.get(j << (logn - 1 - lh)), w2 = tw.get(j << (logn - 2 - lh));
-  const cf t1 = cf_mul(w1, x1), t3 = cf_mul(w1, x3);
-  const cf b0 = cf_add(x0, t1), b1 = cf_sub(x0, t1), b2 = cf_add(x2, t3), b3 = cf_sub(x2, t3);
-  const cf u2 = cf_mul(w2, b2), u3 = cf_mul_si(cf_mul(w2, b3), sign);
-  x.set(a0, cf_add(b0, u2));
-  x.set(a0 + 2 * h, cf_sub(b0, u2));
-  x.set(a0 + h, cf_add(b1, u3));
-  x.set(a0 + 3 * h, cf_sub(b1, u3));
+CG_FHD void dft4(cf *v, int sign) {
+  const cf a0 = cf_add(v[0], v[2]), a1 = cf_sub(v[0], v[2]);
+  const cf b0 = cf_add(v[1], v[3]), b1 = cf_mul_si(cf_sub(v[1], v[3]), sign);
+  v[0] = cf_add(a0, b0);
+  v[2] = cf_sub(a0, b0);
+  v[1] = cf_add(a1, b1);
+  v[3] = cf_sub(a1, b1);
 }
-
-// The whole line in one thread (host reference of the stage sequence; the
-// kernels run the same butterflies spread over threads with a barrier
-// between stages).
-template <class BUF, class TW>
-CG_FHD void line_serial(BUF &x, const TW &tw, int logn, int sign) {
-  const int N = 1 << logn;
-  int lh = 0;
-  if (logn & 1) {
-    for (int q = 0; q < N / 2; ++q) radix2_first(x, q);
-    lh = 1;
+// w_8^j for the sign
+CG_FHD cf w8(int j, int sign) {
+  const float h = 0.70710678118654752f, s = (float)sign;
+  switch (j & 7) {
+    case 0: return {1.f, 0.f};
+    case 1: return {h, s * h};
+    case 2: return {0.f, s};
+    case 3: return {-h, s * h};
+    case 4: return {-1.f, 0.f};
+    case 5: return {-h, -s * h};
+    case 6: return {0.f, -s};
+    default: return {h, -s * h};
   }
-  for (; lh + 1 < logn; lh += 2)
-    for (int q = 0; q < N / 4; ++q) radix4(x, tw, logn, lh, q, sign);
+}
+// w_16^j for the sign
+CG_FHD cf w16(int j, int sign) {
+  const float c = 0.92387953251128676f, q = 0.38268343236508977f, s = (float)sign;
+  switch (j & 15) {
+    case 1: return {c, s * q};
+    case 3: return {q, s * c};
+    case 5: return {-q, s * c};
+    case 7: return {-c, s * q};
+    case 9: return {-c, -s * q};
+    case 11: return {-q, -s * c};
+    case 13: return {q, -s * c};
+    case 15: return {c, -s * q};
+    default: return w8((j & 15) >> 1, sign);
+  }
+}
+// Radix-8 and radix-16 DFTs in place with their outputs left permuted:
+// X[r] ends in v[out_slot(logr, r)] (the stage's store reads that slot), so
+// that no copy between register arrays is needed.
+// 8 = 2 x 4: n = b + 4a (b < 4, a < 2), k = k1 + 2 k2:
+//   X[k1 + 2 k2] = sum_b w_4^(b k2) [w_8^(b k1) sum_a v[b + 4a] w_2^(a k1)];
+//   after the pass over a, v[b + 4 k1] holds the bracket; X[k1 + 2 k2] in
+//   v[4 k1 + k2].
+CG_FHD void dft8(cf *v, int sign) {
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const cf x = v[b], y = v[b + 4];
+    v[b] = cf_add(x, y);
+    v[b + 4] = b ? cf_mul(cf_sub(x, y), w8(b, sign)) : cf_sub(x, y);
+  }
+  dft4(v, sign);
+  dft4(v + 4, sign);
+}
+// 16 = 4 x 4: n = a + 4b, k = c + 4d:
+//   X[c + 4d] = sum_a w_4^(a d) [w_16^(a c) sum_b v[a + 4b] w_4^(b c)];
+//   after the pass over b, v[a + 4c] holds the bracket; X[c + 4d] in v[4c + d].
+CG_FHD void dft16(cf *v, int sign) {
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    cf t[4] = {v[a], v[a + 4], v[a + 8], v[a + 12]};
+    dft4(t, sign);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) v[a + 4 * c] = (a && c) ? cf_mul(t[c], w16(a * c, sign)) : t[c];
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    cf t[4] = {v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]};
+    dft4(t, sign);
+#pragma unroll
+    for (int d = 0; d < 4; ++d) v[4 * c + d] = t[d];
+  }
+}
+CG_FHD void dft_r(cf *v, int logr, int sign) {
+  if (logr == 1) dft2(v);
+  else if (logr == 2) dft4(v, sign);
+  else if (logr == 3) dft8(v, sign);
+  else dft16(v, sign);
+}
+// register slot holding output r of a radix-2^logr DFT
+CG_FHD int out_slot(int logr, int r) {
+  if (logr == 3) return 4 * (r & 1) + (r >> 1);
+  if (logr == 4) return 4 * (r & 3) + (r >> 2);
+  return r;
+}
+
+// One thread's share of stage s: 16 / R butterflies b = t + m T (m < 16/R,
+// T = N / 16), in three steps so that a kernel can put a barrier between
+// every thread's reads and every thread's writes.  ld(e) / st(e, v) access
+// element e of the line; tw(j) gives w_N^j (j < N).
+template <class LD, class TW>
+CG_FHD void stage_load(int logn, int s, int t, const LD &ld, const TW &tw, cf *v) {
+  const int logr = stage_logr(logn, s), logp = stage_logp(logn, s);
+  const int R = 1 << logr, nb = 16 >> logr, T = 1 << (logn - 4);
+  const int NR = 1 << (logn - logr);  // N / R
+#pragma unroll
+  for (int m = 0; m < nb; ++m) {
+    const int b = t + m * T;
+    const int k = b & ((1 << logp) - 1);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      cf x = ld(b + r * NR);
+      if (r && k) x = cf_mul(x, tw((r * k) << (logn - logp - logr)));  // w_N^(r k N/(pR))
+      v[m * R + r] = x;
+    }
+  }
+}
+CG_FHD void stage_dft(int logn, int s, int sign, cf *v) {
+  const int logr = stage_logr(logn, s), nb = 16 >> logr;
+#pragma unroll
+  for (int m = 0; m < nb; ++m) dft_r(v + (m << logr), logr, sign);
+}
+template <class ST>
+CG_FHD void stage_store(int logn, int s, int t, const ST &st, const cf *v) {
+  const int logr = stage_logr(logn, s), logp = stage_logp(logn, s);
+  const int R = 1 << logr, nb = 16 >> logr, T = 1 << (logn - 4);
+#pragma unroll
+  for (int m = 0; m < nb; ++m) {
+    const int b = t + m * T;
+    const int k = b & ((1 << logp) - 1);
+    const int j = ((b - k) << logr) + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) st(j + (r << logp), v[m * R + out_slot(logr, r)]);
+  }
 }
 
 }  // namespace f32

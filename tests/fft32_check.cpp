@@ -1,7 +1,9 @@
-// Host check of crocodile_gb300/csrc/fft32.h: the in-place radix-4 DIT line
-// transform (bit-reversed load, odd and even log2 N, both signs) against a
-// direct DFT in double precision, for N = 2 .. 8192.  Prints the worst error
-// relative to the transform's norm; exit status 0 when it is below 1e-5.
+// Host check of crocodile_gb300/csrc/fft32.h: the register-blocked Stockham
+// stages (radix 16, one first stage of radix 2, 4 or 8), run thread by
+// thread as the kernels run them (all threads' loads of a stage before any
+// store, one buffer), against a direct DFT in double precision for
+// N = 64 .. 8192 and both signs.  Prints the worst error relative to the
+// transform's norm; exit status 0 when it is below 1e-6.
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -10,38 +12,35 @@
 
 using namespace cg::f32;
 
-struct Buf {
-  std::vector<cf> v;
-  cf get(int i) const { return v[i]; }
-  void set(int i, cf a) { v[i] = a; }
-};
-struct Tw {
-  std::vector<cf> v;
-  cf get(int k) const { return v[k]; }
-};
-
 int main() {
   double worst = 0;
-  unsigned s = 12345;
+  unsigned seed = 12345;
   auto rnd = [&]() {
-    s = s * 1664525u + 1013904223u;
-    return (float)((s >> 8) * (1.0 / 16777216.0) - 0.5);
+    seed = seed * 1664525u + 1013904223u;
+    return (float)((seed >> 8) * (1.0 / 16777216.0) - 0.5);
   };
-  for (int logn = 1; logn <= 13; ++logn) {
-    const int N = 1 << logn;
+  for (int logn = 6; logn <= 13; ++logn) {
+    const int N = 1 << logn, T = N / 16;
     for (int sign = -1; sign <= 1; sign += 2) {
-      std::vector<cf> in(N);
+      std::vector<cf> in(N), buf(N), tw(N);
       for (auto &c : in) c = {rnd(), rnd()};
-      Tw tw;
-      tw.v.resize(N / 2 > 0 ? N / 2 : 1);
-      for (int k = 0; k < N / 2; ++k) {
-        const double a = sign * 2.0 * M_PI * k / N;
-        tw.v[k] = {(float)std::cos(a), (float)std::sin(a)};
+      for (int j = 0; j < N; ++j) {
+        const double a = sign * 2.0 * M_PI * j / N;
+        tw[j] = {(float)std::cos(a), (float)std::sin(a)};
       }
-      Buf x;
-      x.v.resize(N);
-      for (int i = 0; i < N; ++i) x.v[bitrev(i, logn)] = in[i];
-      line_serial(x, tw, logn, sign);
+      auto twf = [&](int j) { return tw[j]; };
+      std::vector<std::vector<cf>> regs(T, std::vector<cf>(16));
+      const int ns = stage_count(logn);
+      for (int s = 0; s < ns; ++s) {
+        const std::vector<cf> &src = s == 0 ? in : buf;
+        auto ld = [&](int e) { return src[e]; };
+        for (int t = 0; t < T; ++t) stage_load(logn, s, t, ld, twf, regs[t].data());
+        auto st = [&](int e, cf v) { buf[e] = v; };
+        for (int t = 0; t < T; ++t) {
+          stage_dft(logn, s, sign, regs[t].data());
+          stage_store(logn, s, t, st, regs[t].data());
+        }
+      }
       double num = 0, den = 0;
       const int kstep = N > 512 ? N / 512 : 1;  // direct DFT on a sample of outputs
       for (int k = 0; k < N; k += kstep) {
@@ -51,7 +50,7 @@ int main() {
           re += in[n].x * std::cos(a) - in[n].y * std::sin(a);
           im += in[n].x * std::sin(a) + in[n].y * std::cos(a);
         }
-        num += (x.v[k].x - re) * (x.v[k].x - re) + (x.v[k].y - im) * (x.v[k].y - im);
+        num += (buf[k].x - re) * (buf[k].x - re) + (buf[k].y - im) * (buf[k].y - im);
         den += re * re + im * im;
       }
       const double e = std::sqrt(num / den);
@@ -60,5 +59,5 @@ int main() {
     }
   }
   printf("worst %.3g\n", worst);
-  return worst < 1e-5 ? 0 : 1;
+  return worst < 1e-6 ? 0 : 1;
 }
