@@ -44,7 +44,7 @@ class KernelDesc(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("tile", c_int), ("chunk", c_int), ("rows", c_int), ("groups", c_int),
-                ("layout", c_int)]
+                ("layout", c_int), ("dvis", c_int)]
 
 
 # name -> (restype, argtypes); the declarations of include/crocodile_gb300.h

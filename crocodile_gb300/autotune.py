@@ -25,8 +25,8 @@ CACHE = os.environ.get("CROCODILE_GB300_TUNING",
 _lock = threading.Lock()
 
 
-def set_tuning(tile=0, chunk=0, rows=0, groups=0, layout=0):
-    t = L.Tuning(int(tile), int(chunk), int(rows), int(groups), int(layout))
+def set_tuning(tile=0, chunk=0, rows=0, groups=0, layout=0, dvis=0):
+    t = L.Tuning(int(tile), int(chunk), int(rows), int(groups), int(layout), int(dvis))
     L.call("cg_set_tuning", ctypes.byref(t))
 
 
@@ -34,7 +34,7 @@ def get_tuning():
     t = L.Tuning()
     L.call("cg_get_tuning", ctypes.byref(t))
     return {"tile": t.tile, "chunk": t.chunk, "rows": t.rows, "groups": t.groups,
-            "layout": t.layout}
+            "layout": t.layout, "dvis": t.dvis}
 
 
 def effective_layout(ktab):

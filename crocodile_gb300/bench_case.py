@@ -121,13 +121,13 @@ def main():
     ap.add_argument("--fused", action="store_true",
                     help="one degrid+grid pass (cg_degrid_grid) instead of two calls")
     ap.add_argument("--tuning", default="",
-                    help="explicit launch shape tile,chunk,rows,groups,layout (no autotuning)")
+                    help="explicit launch shape tile,chunk,rows,groups,layout[,dvis] "
+                         "(no autotuning)")
     a = ap.parse_args()
     ctx = setup(a.workload, a.nvis)
     if a.tuning:
         from . import autotune
-        tile, chunk, rows, groups, layout = (int(x) for x in a.tuning.split(","))
-        autotune.set_tuning(tile, chunk, rows, groups, layout)
+        autotune.set_tuning(*(int(x) for x in a.tuning.split(",")))
     elif a.tune:
         from . import autotune
         w = ctx["w"]

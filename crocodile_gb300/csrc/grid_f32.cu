@@ -405,10 +405,10 @@ __global__ void __launch_bounds__(256) k_degrid_grid_warp(
 }
 
 // ---------------------------------------------------------------- degridder
-// Each warp sums the S*S taps of two visibilities at a time (taps fixed per
-// lane, interleaved so that both visibilities' kernel loads are in flight
-// together) and reduces both with shuffles.
-template <bool SEP, int MAXT>
+// Each warp sums the S*S taps of V visibilities at a time (taps fixed per
+// lane, interleaved so that all V visibilities' kernel loads are in flight
+// together) and reduces them with shuffles.
+template <bool SEP, int MAXT, int V>
 __global__ void __launch_bounds__(256) k_degrid_tiled(
     TiledArgs A, const float2 *__restrict__ ktab, const float2 *__restrict__ grid,
     float2 *__restrict__ out) {
@@ -444,41 +444,42 @@ __global__ void __launch_bounds__(256) k_degrid_tiled(
                                : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    for (int j = 2 * warp; j < w.count; j += 2 * nwarps) {
-      const bool two = j + 1 < w.count;
-      const VisRec r1 = A.recs[w.start + j];
-      const VisRec r2 = two ? A.recs[w.start + j + 1] : r1;
-      const int b1 = (r1.y0 - wy0) * pitch + (r1.x0 - wx0);
-      const int b2 = (r2.y0 - wy0) * pitch + (r2.x0 - wx0);
-      const float2 *k1 = ktab + (SEP ? 0 : (long long)r1.k0 * KSZ + (long long)r1.k1 * SS);
-      const float2 *k2 = ktab + (SEP ? 0 : (long long)r2.k0 * KSZ + (long long)r2.k1 * SS);
-      const float2 *ky1 = ktab + (long long)r1.k0 * S, *kx1 = ktab + (long long)r1.k1 * S;
-      const float2 *ky2 = ktab + (long long)r2.k0 * S, *kx2 = ktab + (long long)r2.k1 * S;
-      float2 s1 = make_float2(0.f, 0.f), s2 = make_float2(0.f, 0.f);
+    for (int j = V * warp; j < w.count; j += V * nwarps) {
+      int base[V];
+      const float2 *kk[V], *ky[V], *kx[V];
+      float2 sum[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        // past the item's end: repeat its first visibility (summed, not written)
+        const VisRec r = A.recs[w.start + (j + v < w.count ? j + v : j)];
+        base[v] = (r.y0 - wy0) * pitch + (r.x0 - wx0);
+        kk[v] = ktab + (SEP ? 0 : (long long)r.k0 * KSZ + (long long)r.k1 * SS);
+        ky[v] = ktab + (long long)r.k0 * S;
+        kx[v] = ktab + (long long)r.k1 * S;
+        sum[v] = make_float2(0.f, 0.f);
+      }
 #pragma unroll
       for (int i = 0; i < MAXT; ++i)
         if (soff[i] >= 0) {
-          float2 ka, kb;
-          if (SEP) {
-            ka = cmul(__ldg(&ky1[kdy[i]]), __ldg(&kx1[kdx[i]]));
-            kb = cmul(__ldg(&ky2[kdy[i]]), __ldg(&kx2[kdx[i]]));
-          } else {
-            ka = __ldg(&k1[lane + 32 * i]);
-            kb = __ldg(&k2[lane + 32 * i]);
-          }
-          cfma(s1, win[b1 + soff[i]], ka);
-          cfma(s2, win[b2 + soff[i]], kb);
+          float2 k[V];
+#pragma unroll
+          for (int v = 0; v < V; ++v)
+            k[v] = SEP ? cmul(__ldg(&ky[v][kdy[i]]), __ldg(&kx[v][kdx[i]]))
+                       : __ldg(&kk[v][lane + 32 * i]);
+#pragma unroll
+          for (int v = 0; v < V; ++v) cfma(sum[v], win[base[v] + soff[i]], k[v]);
         }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        s1.x += __shfl_xor_sync(0xffffffffu, s1.x, o);
-        s1.y += __shfl_xor_sync(0xffffffffu, s1.y, o);
-        s2.x += __shfl_xor_sync(0xffffffffu, s2.x, o);
-        s2.y += __shfl_xor_sync(0xffffffffu, s2.y, o);
-      }
+      for (int v = 0; v < V; ++v)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          sum[v].x += __shfl_xor_sync(0xffffffffu, sum[v].x, o);
+          sum[v].y += __shfl_xor_sync(0xffffffffu, sum[v].y, o);
+        }
       if (lane == 0) {
-        out[A.perm[w.start + j]] = s1;
-        if (two) out[A.perm[w.start + j + 1]] = s2;
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+          if (j + v < w.count) out[A.perm[w.start + j + v]] = sum[v];
       }
     }
   }
@@ -701,9 +702,12 @@ int cg_degrid(const cg_plan *p, const void *ktab, const void *grid, void *out,
   const int need = (SS + 31) / 32;
   const int threads = 256;
   const size_t smem = (size_t)p->pitch * p->win * sizeof(float2);
+  const bool four = tuning().dvis == 4;  // visibilities per warp step: 4, or 2
   void (*fn)(TiledArgs, const float2 *, const float2 *, float2 *) = nullptr;
 #define PICK(M)                                                                \
-  if (!fn && need <= M) fn = p->kd.sep ? k_degrid_tiled<true, M> : k_degrid_tiled<false, M>;
+  if (!fn && need <= M)                                                        \
+    fn = four ? (p->kd.sep ? k_degrid_tiled<true, M, 4> : k_degrid_tiled<false, M, 4>)  \
+              : (p->kd.sep ? k_degrid_tiled<true, M, 2> : k_degrid_tiled<false, M, 2>);
   PICK(1) PICK(2) PICK(4) PICK(8) PICK(16) PICK(32)
 #undef PICK
   CG_REQUIRE(fn, "support too large for the degridder");

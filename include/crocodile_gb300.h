@@ -105,7 +105,8 @@ typedef struct {
  * residues per owner-layout thread (1..8), or bulk-copy stages per
  * lane-layout warp (2..4; other values: 4); groups: owner-layout thread
  * groups, or warp-layout warps, per CTA (1..8), or lane-layout warps per
- * CTA (1..16).  layout 0 picks CG_LAYOUT_LANE (with 16-cell tiles) for
+ * CTA (1..16); dvis: visibilities each degridder warp sums at a time (2 or
+ * 4; 0: 2).  layout 0 picks CG_LAYOUT_LANE (with 16-cell tiles) for
  * non-separable tables with even S <= 16, whose slices stream by bulk
  * copies as they are, and CG_LAYOUT_WARP otherwise.  Process-wide. */
 #define CG_LAYOUT_WARP 1
@@ -117,6 +118,7 @@ typedef struct {
   int rows;
   int groups;
   int layout;
+  int dvis;
 } cg_tuning;
 int cg_set_tuning(const cg_tuning *t);
 int cg_get_tuning(cg_tuning *out);

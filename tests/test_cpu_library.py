@@ -102,16 +102,18 @@ def test_host_helpers_match_oracle():
 def test_tuning_roundtrip_and_validation(libpath):
     from crocodile_gb300 import _lib, autotune
     try:
-        autotune.set_tuning(tile=32, chunk=700, rows=3, groups=2, layout=_lib.CG_LAYOUT_OWNER)
+        autotune.set_tuning(tile=32, chunk=700, rows=3, groups=2, layout=_lib.CG_LAYOUT_OWNER,
+                            dvis=4)
         assert autotune.get_tuning() == {"tile": 32, "chunk": 700, "rows": 3, "groups": 2,
-                                         "layout": 2}
+                                         "layout": 2, "dvis": 4}
         for bad in ({"tile": 30}, {"tile": 68}, {"rows": 9}, {"groups": 9}, {"layout": 4},
-                    {"layout": 3, "groups": 17}):
+                    {"layout": 3, "groups": 17}, {"dvis": 3}):
             with pytest.raises(ValueError):
                 autotune.set_tuning(**bad)
     finally:
         autotune.set_tuning()
-    assert autotune.get_tuning() == {"tile": 0, "chunk": 0, "rows": 0, "groups": 0, "layout": 0}
+    assert autotune.get_tuning() == {"tile": 0, "chunk": 0, "rows": 0, "groups": 0, "layout": 0,
+                                     "dvis": 0}
     cands = autotune.candidates(15)
     assert any(c["layout"] == 1 for c in cands) and any(c["layout"] == 2 for c in cands)
     assert any(c["layout"] == 3 for c in cands)
