@@ -16,16 +16,22 @@
 
 namespace cg {
 
-// One block per layer: mean of w over the layer's visibilities, summed in the
-// plan's sorted order (deterministic).  Empty layers get mean 0 and count 0.
-__global__ void k_layer_mean_w(const double *__restrict__ uvw, int64_t stride,
-                               const int32_t *__restrict__ perm,
-                               const int32_t *__restrict__ counts,
-                               const int32_t *__restrict__ offsets, int buckets_per_layer,
-                               double *__restrict__ mean_out, int32_t *__restrict__ count_out) {
-  const int l = blockIdx.x;
+// Mean of w over each layer's visibilities (the plan's sorted order keeps a
+// layer's visibilities contiguous).  Grid (chunk, layer): every block sums up
+// to LMW_CHUNK of its layer's visibilities and adds its sum to the layer's
+// total (FP64 atomics, so the order of the partial sums varies between runs);
+// k_layer_mean_finish divides by the counts.  Empty layers get mean 0, count 0.
+constexpr int LMW_CHUNK = 8192;
+
+__global__ void k_layer_sum_w(const double *__restrict__ uvw, int64_t stride,
+                              const int32_t *__restrict__ perm, const int32_t *__restrict__ counts,
+                              const int32_t *__restrict__ offsets, int buckets_per_layer,
+                              double *__restrict__ sum_out) {
+  const int l = blockIdx.y;
   const int b0 = l * buckets_per_layer, b1 = b0 + buckets_per_layer - 1;
-  const int start = offsets[b0], end = offsets[b1] + counts[b1];
+  const int start = offsets[b0] + blockIdx.x * LMW_CHUNK;
+  const int end = min(offsets[b1] + counts[b1], start + LMW_CHUNK);
+  if (start >= end) return;
   double sum = 0.0;
   for (int j = start + threadIdx.x; j < end; j += blockDim.x) sum += uvw[(int64_t)perm[j] * stride + 2];
   __shared__ double s[32];
@@ -35,12 +41,19 @@ __global__ void k_layer_mean_w(const double *__restrict__ uvw, int64_t stride,
   if (threadIdx.x < 32) {
     double t = threadIdx.x < (blockDim.x >> 5) ? s[threadIdx.x] : 0.0;
     for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (threadIdx.x == 0) {
-      const int c = end - start;
-      mean_out[l] = c ? t / (double)c : 0.0;
-      if (count_out) count_out[l] = c;
-    }
+    if (threadIdx.x == 0) atomicAdd(&sum_out[l], t);
   }
+}
+
+__global__ void k_layer_mean_finish(int layers, const int32_t *__restrict__ counts,
+                                    const int32_t *__restrict__ offsets, int buckets_per_layer,
+                                    double *__restrict__ mean, int32_t *__restrict__ count_out) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= layers) return;
+  const int b0 = l * buckets_per_layer, b1 = b0 + buckets_per_layer - 1;
+  const int c = offsets[b1] + counts[b1] - offsets[b0];
+  mean[l] = c ? mean[l] / (double)c : 0.0;
+  if (count_out) count_out[l] = c;
 }
 
 // image[i, j] = sum_p planes[p, i, j] / exp(2 pi i midw_p ph(i, j)).
@@ -106,9 +119,14 @@ int cg_plan_layer_mean_w(const cg_plan *p, const double *uvw, int64_t stride, do
     return CG_OK;
   }
   const int bpl = p->tpl << (2 * p->sublog);
-  k_layer_mean_w<<<p->layers, 256, 0, (cudaStream_t)stream>>>(uvw, stride, p->perm, p->counts,
-                                                               p->offsets, bpl, mean_out,
-                                                               count_out);
+  cudaStream_t st = (cudaStream_t)stream;
+  CG_REQUIRE(p->layers <= 65535, "at most 65535 layers");
+  CG_CUDA(cudaMemsetAsync(mean_out, 0, sizeof(double) * p->layers, st));
+  const dim3 grid((unsigned)((p->n + LMW_CHUNK - 1) / LMW_CHUNK), (unsigned)p->layers);
+  k_layer_sum_w<<<grid, 256, 0, st>>>(uvw, stride, p->perm, p->counts, p->offsets, bpl, mean_out);
+  CG_LAUNCH("layer sum w");
+  k_layer_mean_finish<<<(p->layers + 255) / 256, 256, 0, st>>>(p->layers, p->counts, p->offsets,
+                                                                bpl, mean_out, count_out);
   CG_LAUNCH("layer mean w");
   return CG_OK;
 }

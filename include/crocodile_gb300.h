@@ -103,7 +103,7 @@ typedef struct {
  * also selects the lane form of cg_degrid_grid; odd S * S slices stream
  * from a padded copy of the table in the plan's workspace); rows: row
  * residues per owner-layout thread (1..8), or bulk-copy stages per
- * lane-layout warp (2..4; other values: 4); groups: owner-layout thread
+ * lane-layout warp (2..4; other values: 3); groups: owner-layout thread
  * groups, or warp-layout warps, per CTA (1..8), or lane-layout warps per
  * CTA (1..16); dvis: visibilities each degridder warp sums at a time (2 or
  * 4; 0: 2).  layout 0 picks CG_LAYOUT_LANE (with 16-cell tiles) for
@@ -385,8 +385,9 @@ int cg_aw_keys(const double *uvw, int64_t stride, const int32_t *a1,
  * layered plan (cg_plan_create_ex) and an inverse centred cg_fft of the
  * stack, image = sum_p plane_p / w_kernel_function(l, m, mean w of plane p)
  * (synthesis.py:273-293).  cg_plan_layer_mean_w writes the mean w (double)
- * and visibility count (int32, may be NULL) of each layer, summed in the
- * plan's order; cg_wstack_combine forms the complex64 N x N image (planes
+ * and visibility count (int32, may be NULL) of each layer (FP64 sums over
+ * chunks of the layer, the chunk sums added in an order that varies between
+ * runs); cg_wstack_combine forms the complex64 N x N image (planes
  * without visibilities are skipped, as in the notebook). */
 int cg_plan_layer_mean_w(const cg_plan *plan, const double *uvw, int64_t stride,
                          double *mean_out, int32_t *count_out,
