@@ -94,13 +94,13 @@ struct ColIO {
   int W, H;
   int centred, phase;
   float scale;
-  __device__ float2 ld(int64_t plane, int i, int c) const {
-    return d[(plane * H + i) * (int64_t)W + c];
-  }
-  __device__ void st(int64_t plane, int i, int c, float2 v, float &) const {
+  // column `c` of plane `plane`: element i at base[i * W]
+  __device__ const float2 *src(int64_t plane, int c) const { return d + plane * H * (int64_t)W + c; }
+  __device__ float2 *dst(int64_t plane, int c) const { return d + plane * H * (int64_t)W + c; }
+  __device__ void st(float2 *base, int i, int c, float2 v, float &) const {
     float s = scale;
     if (centred && ((i + c + phase) & 1)) s = -s;
-    d[(plane * H + i) * (int64_t)W + c] = make_float2(v.x * s, v.y * s);
+    base[i * W] = make_float2(v.x * s, v.y * s);
   }
   static constexpr bool kMax = false;
 };
@@ -112,10 +112,11 @@ struct ColImageIO {
   float *img;
   int W, H, phase;
   float scale;
-  __device__ float2 ld(int64_t, int i, int c) const { return d[(int64_t)i * W + c]; }
-  __device__ void st(int64_t, int i, int c, float2 v, float &mx) const {
+  __device__ const float2 *src(int64_t, int c) const { return d + c; }
+  __device__ float *dst(int64_t, int c) const { return img + c; }
+  __device__ void st(float *base, int i, int c, float2 v, float &mx) const {
     const float r = v.x * (((i + c + phase) & 1) ? -scale : scale);
-    img[(int64_t)i * W + c] = r;
+    base[i * W] = r;
     mx = fmaxf(mx, r);
   }
   static constexpr bool kMax = true;
@@ -131,7 +132,7 @@ __device__ __forceinline__ void atomic_max_f(float *addr, float v) {
 // ---------------------------------------------------------------- kernels
 // T = N / 16 threads per line.  Rows: 512 / T lines per CTA.
 template <int LOGN>
-__global__ void __launch_bounds__(ROW_THREADS) k_fft32_rows(RowIO io, int64_t nrows,
+__global__ void __launch_bounds__(ROW_THREADS, 2) k_fft32_rows(RowIO io, int64_t nrows,
                                                             const float2 *__restrict__ tw,
                                                             int sign) {
   constexpr int N = 1 << LOGN, T = N / 16, LPC = ROW_THREADS / T, P = N + N / 32;
@@ -197,10 +198,12 @@ __global__ void __launch_bounds__(COL_THREADS) k_fft32_cols(IO io, int64_t nplan
   for (int64_t unit = blockIdx.x; unit < nplanes * per_plane; unit += gridDim.x) {
     const int64_t plane = unit / per_plane;
     const int col = (int)(unit - plane * per_plane) * C + c;
+    const float2 *src = io.src(plane, col);
+    auto dst = io.dst(plane, col);
     cf v[16];
     __syncthreads();  // the previous tile's last reads of shared memory are done
     stage_load(LOGH, 0, t, [&](int e) {
-      const float2 x = io.ld(plane, e, col);
+      const float2 x = src[e * W];
       return cf{x.x, x.y};
     }, twf, v);
     stage_dft(LOGH, 0, sign, v);
@@ -214,7 +217,7 @@ __global__ void __launch_bounds__(COL_THREADS) k_fft32_cols(IO io, int64_t nplan
       if (s + 1 < NS)
         stage_store(LOGH, s, t, sts, v);
       else
-        stage_store(LOGH, s, t, [&](int e, cf x) { io.st(plane, e, col, make_float2(x.x, x.y), mx); },
+        stage_store(LOGH, s, t, [&](int e, cf x) { io.st(dst, e, col, make_float2(x.x, x.y), mx); },
                     v);
     }
   }

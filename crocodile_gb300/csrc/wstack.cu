@@ -73,12 +73,20 @@ __global__ void k_wstack_combine(const float2 *__restrict__ planes, int layers, 
   __syncthreads();
   const int64_t total = (int64_t)N * N;
   int bad = 0;
+  // (k - N/2) / N: a multiplication by the exact reciprocal for power-of-two N
+  // (the same bits as the division, without an FP64 division per pixel)
+  const bool pow2 = (N & (N - 1)) == 0;
+  const double invN = 1.0 / (double)N;
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total;
        L += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(L / N), j = (int)(L - (int64_t)i * N);
     // theta * coordinates2(N): l along columns (x), m along rows (y)
-    const double l = __dmul_rn(theta, __ddiv_rn((double)(j - N / 2), (double)N));
-    const double m = __dmul_rn(theta, __ddiv_rn((double)(i - N / 2), (double)N));
+    const double cj = pow2 ? __dmul_rn((double)(j - N / 2), invN)
+                           : __ddiv_rn((double)(j - N / 2), (double)N);
+    const double ci = pow2 ? __dmul_rn((double)(i - N / 2), invN)
+                           : __ddiv_rn((double)(i - N / 2), (double)N);
+    const double l = __dmul_rn(theta, cj);
+    const double m = __dmul_rn(theta, ci);
     const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
     if (!(r2 < 1.0)) bad = 1;
     const double ph = 1.0 - sqrt(1.0 - r2);
