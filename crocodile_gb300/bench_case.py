@@ -116,7 +116,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--nvis", type=int, default=500_000)
     ap.add_argument("--steps", type=int, default=2)
-    ap.add_argument("--workload", default="wproj", choices=["wproj", "plain", "aw"])
+    ap.add_argument("--workload", default="wproj", choices=["wproj", "plain", "aw", "fft"],
+                    help="fft: one --nvis x --nvis complex64 plane, centred inverse FFTs")
     ap.add_argument("--tune", action="store_true", help="autotune the launch shape first")
     ap.add_argument("--fused", action="store_true",
                     help="one degrid+grid pass (cg_degrid_grid) instead of two calls")
@@ -124,6 +125,19 @@ def main():
                     help="explicit launch shape tile,chunk,rows,groups,layout[,dvis] "
                          "(no autotuning)")
     a = ap.parse_args()
+    if a.workload == "fft":  # one N x N complex64 plane (N = --nvis), centred inverse FFTs
+        N = a.nvis
+        rng = numpy.random.default_rng(N)
+        g = torch.from_numpy((rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N)))
+                             .astype(numpy.complex64)).cuda()
+        E.fft_(g, True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            E.fft_(g, True)
+        torch.cuda.synchronize()
+        print("fft %d^2: %.3f ms per transform" % (N, 1e3 * (time.perf_counter() - t0) / a.steps))
+        return
     ctx = setup(a.workload, a.nvis)
     if a.tuning:
         from . import autotune
