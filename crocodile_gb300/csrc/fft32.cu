@@ -34,10 +34,22 @@ namespace f32 {
 
 constexpr int MIN_LOG = 6, MAX_LOG = 13;
 constexpr int ROW_THREADS = 512, COL_THREADS = 512;
+// square planes from this side on run their columns as rows between two
+// in-place transposes (the column tiles hold only 1 or 2 columns there)
+constexpr int TRANSPOSE_MIN = 4096;
 
 __device__ __forceinline__ int pad(int e) { return e + (e >> 5); }  // bank spread
 
-// w_N^j = exp(sign 2 pi i j / N), j < N, cached per device, log N and sign
+// Twiddles w_N^j = exp(sign 2 pi i j / N), j < N, as a two-level table:
+// w_N^j = A[j mod TWB] * C[j / TWB], A[a] = w_N^a (a < TWB), C[c] = w_N^(c TWB)
+// (c < N / TWB); TWB + N / TWB entries (192 for N = 8192), staged in shared
+// memory by every CTA.  Each twiddle costs one complex product more than a
+// full table (within about 1.5 units of FP32 rounding).  Cached per device,
+// log N and sign.
+constexpr int TWB_LOG = 6, TWB = 1 << TWB_LOG;
+constexpr int tw_entries(int logn) {
+  return logn > TWB_LOG ? TWB + (1 << (logn - TWB_LOG)) : (1 << logn) + 1;
+}
 std::mutex g_mu;
 std::map<std::tuple<int, int, int>, float2 *> g_tw;
 
@@ -52,11 +64,14 @@ int twiddles(int logn, int sign, const float2 **out) {
     return CG_OK;
   }
   const int n = 1 << logn;
-  std::vector<float2> h(n);
-  for (int k = 0; k < n; ++k) {
-    const double a = 2.0 * M_PI * (double)k / (double)n;
-    h[k] = make_float2((float)std::cos(a), (float)(sign * std::sin(a)));
-  }
+  const int nb = logn > TWB_LOG ? TWB : n, nc = logn > TWB_LOG ? n / TWB : 1;
+  std::vector<float2> h(tw_entries(logn));
+  auto w = [&](long j) {
+    const double a = 2.0 * M_PI * (double)j / (double)n;
+    return make_float2((float)std::cos(a), (float)(sign * std::sin(a)));
+  };
+  for (int a = 0; a < nb; ++a) h[a] = w(a);
+  for (int c = 0; c < nc; ++c) h[nb + c] = w((long)c * nb);
   float2 *d = nullptr;
   CG_CUDA(cudaMalloc(&d, h.size() * sizeof(float2)));
   CG_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice));
@@ -64,6 +79,20 @@ int twiddles(int logn, int sign, const float2 **out) {
   *out = d;
   return CG_OK;
 }
+
+// the two-level table in shared memory
+template <int LOGN>
+struct SmTw2 {
+  const float2 *t;
+  __device__ cf operator()(int j) const {
+    if (LOGN <= TWB_LOG) {
+      const float2 v = t[j];
+      return cf{v.x, v.y};
+    }
+    const float2 a = t[j & (TWB - 1)], c = t[TWB + (j >> TWB_LOG)];
+    return cf_mul(cf{a.x, a.y}, cf{c.x, c.y});
+  }
+};
 
 // ---------------------------------------------------------------- I/O policies
 // Row pass: rows of all planes, row index = plane * H + r.
@@ -140,10 +169,10 @@ __global__ void __launch_bounds__(ROW_THREADS, 2) k_fft32_rows(RowIO io, int64_t
   extern __shared__ float2 f32_sm[];
   const int line = threadIdx.x / T, t = threadIdx.x % T;
   float2 *buf = f32_sm + line * P;
-  auto twf = [&](int j) {
-    const float2 w = __ldg(&tw[j]);
-    return cf{w.x, w.y};
-  };
+  float2 *stw = f32_sm + LPC * P;
+  for (int k = threadIdx.x; k < tw_entries(LOGN); k += ROW_THREADS) stw[k] = tw[k];
+  __syncthreads();
+  const SmTw2<LOGN> twf{stw};
   auto lds = [&](int e) {
     const float2 v = buf[pad(e)];
     return cf{v.x, v.y};
@@ -184,10 +213,10 @@ __global__ void __launch_bounds__(COL_THREADS) k_fft32_cols(IO io, int64_t nplan
   constexpr int NS = (LOGH + 3) / 4;
   extern __shared__ float2 f32_sm[];
   const int c = threadIdx.x % C, t = threadIdx.x / C;
-  auto twf = [&](int j) {
-    const float2 w = __ldg(&tw[j]);
-    return cf{w.x, w.y};
-  };
+  float2 *stw = f32_sm + (H + H / 32) * C;
+  for (int k = threadIdx.x; k < tw_entries(LOGH); k += C * T) stw[k] = tw[k];
+  __syncthreads();
+  const SmTw2<LOGH> twf{stw};
   auto lds = [&](int e) {
     const float2 v = f32_sm[pad(e) * C + c];
     return cf{v.x, v.y};
@@ -227,6 +256,81 @@ __global__ void __launch_bounds__(COL_THREADS) k_fft32_cols(IO io, int64_t nplan
   }
 }
 
+// ---------------------------------------------------------------- square transposes
+// In place on nplanes N x N planes: the CTA of tile pair (I, J), I <= J, of
+// 32 x 32 tiles reads both tiles into shared memory and writes each to the
+// other's place (a diagonal tile to itself).  The store policy takes the
+// final position (r, c); the last transpose of a centred transform applies
+// (-1)^(r + c + phase) and the scale there, or writes the dirty image.
+struct TpPlain {
+  __device__ void st(float2 *d, int64_t off, int, int, float2 v, float &) const { d[off] = v; }
+  static constexpr bool kMax = false;
+};
+struct TpCentred {
+  int phase;
+  float scale;
+  __device__ void st(float2 *d, int64_t off, int r, int c, float2 v, float &) const {
+    const float s = ((r + c + phase) & 1) ? -scale : scale;
+    d[off] = make_float2(v.x * s, v.y * s);
+  }
+  static constexpr bool kMax = false;
+};
+struct TpImage {
+  float *img;
+  int phase;
+  float scale;
+  __device__ void st(float2 *, int64_t off, int r, int c, float2 v, float &mx) const {
+    const float x = v.x * (((r + c + phase) & 1) ? -scale : scale);
+    img[off] = x;
+    mx = fmaxf(mx, x);
+  }
+  static constexpr bool kMax = true;
+};
+
+template <class ST>
+__global__ void __launch_bounds__(256) k_fft32_transpose(float2 *d, int N, ST st, float *max_out) {
+  __shared__ float2 ta[32][33], tb[32][33];
+  const int nt = N / 32;
+  const int I = blockIdx.x / nt, J = blockIdx.x - (blockIdx.x / nt) * nt;
+  float mx = -FLT_MAX;
+  if (I <= J) {
+    float2 *p = d + (int64_t)blockIdx.y * N * N;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+#pragma unroll
+    for (int k = 0; k < 32; k += 8) {
+      ta[ty + k][tx] = p[(int64_t)(I * 32 + ty + k) * N + J * 32 + tx];
+      if (I != J) tb[ty + k][tx] = p[(int64_t)(J * 32 + ty + k) * N + I * 32 + tx];
+    }
+    __syncthreads();
+    const int64_t plane = (int64_t)blockIdx.y * N * N;
+#pragma unroll
+    for (int k = 0; k < 32; k += 8) {
+      // tile (J, I) receives ta transposed; tile (I, J) receives tb transposed
+      const int r1 = J * 32 + ty + k, c1 = I * 32 + tx;
+      st.st(d, plane + (int64_t)r1 * N + c1, r1, c1, ta[tx][ty + k], mx);
+      if (I != J) {
+        const int r2 = I * 32 + ty + k, c2 = J * 32 + tx;
+        st.st(d, plane + (int64_t)r2 * N + c2, r2, c2, tb[tx][ty + k], mx);
+      }
+    }
+  }
+  if (ST::kMax && max_out) {
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomic_max_f(max_out, mx);
+  }
+}
+
+template <class ST>
+int launch_transpose(float2 *d, int64_t nplanes, int N, const ST &st, float *max_out,
+                     cudaStream_t s) {
+  CG_REQUIRE(N % 32 == 0 && nplanes <= 65535, "transpose needs N a multiple of 32");
+  const int nt = N / 32;
+  k_fft32_transpose<ST><<<dim3((unsigned)(nt * nt), (unsigned)nplanes), 256, 0, s>>>(d, N, st,
+                                                                                      max_out);
+  CG_LAUNCH("FP32 FFT transpose");
+  return CG_OK;
+}
+
 __global__ void k_fft32_init_max(float *m) { *m = -FLT_MAX; }
 
 int log2_exact(int n) {
@@ -241,7 +345,7 @@ int launch_rows(const RowIO &io, int64_t nrows, int sign, cudaStream_t st) {
   const float2 *tw;
   int rc = twiddles(LOGN, sign, &tw);
   if (rc) return rc;
-  const size_t smem = (size_t)LPC * (N + N / 32) * sizeof(float2);
+  const size_t smem = (size_t)(LPC * (N + N / 32) + tw_entries(LOGN)) * sizeof(float2);
   CG_CUDA(cudaFuncSetAttribute(k_fft32_rows<LOGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem));
   const int64_t ctas = (nrows + LPC - 1) / LPC;
@@ -263,7 +367,7 @@ int launch_cols(const IO &io, int64_t nplanes, int W, int sign, float *max_out, 
   const float2 *tw;
   int rc = twiddles(LOGH, sign, &tw);
   if (rc) return rc;
-  const size_t smem = (size_t)(H + H / 32) * C * sizeof(float2);
+  const size_t smem = (size_t)((H + H / 32) * C + tw_entries(LOGH)) * sizeof(float2);
   CG_CUDA(cudaFuncSetAttribute(k_fft32_cols<LOGH, C, IO>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t units = nplanes * (W / C);
@@ -330,6 +434,16 @@ int fft32_planes(float2 *data, int64_t batch, int H, int W, bool inverse, bool c
   f32::RowIO rio{data, W, H, centred ? 1 : 0, 0, 0, 1.f};
   int rc = f32::dispatch_rows(lw, rio, batch * H, sign, st);
   if (rc) return rc;
+  if (H == W && H >= f32::TRANSPOSE_MIN && batch <= 65535) {
+    // long columns: transpose, transform rows, transpose back (all coalesced)
+    if ((rc = f32::launch_transpose(data, batch, H, f32::TpPlain{}, nullptr, st))) return rc;
+    f32::RowIO r2{data, W, H, 0, 0, 0, 1.f};
+    if ((rc = f32::dispatch_rows(lw, r2, batch * H, sign, st))) return rc;
+    if (centred)
+      return f32::launch_transpose(data, batch, H, f32::TpCentred{phase & 1, (float)scale},
+                                   nullptr, st);
+    return f32::launch_transpose(data, batch, H, f32::TpPlain{}, nullptr, st);
+  }
   f32::ColIO cio{data, W, H, centred ? 1 : 0, phase & 1, (float)scale};
   return f32::dispatch_cols(lh, cio, batch, W, sign, nullptr, st);
 }
@@ -347,6 +461,14 @@ int fft32_image(const float2 *grid_premod, int H, int W, float *image, float *ma
   if (max_out) {
     f32::k_fft32_init_max<<<1, 1, 0, st>>>(max_out);
     CG_LAUNCH("image max init");
+  }
+  if (H == W && H >= f32::TRANSPOSE_MIN) {
+    float2 *g = (float2 *)grid_premod;
+    if ((rc = f32::launch_transpose(g, 1, H, f32::TpPlain{}, nullptr, st))) return rc;
+    if ((rc = f32::dispatch_rows(lw, rio, H, 1, st))) return rc;
+    return f32::launch_transpose(g, 1, H, f32::TpImage{image, (H / 2 + W / 2) & 1,
+                                                       (float)(1.0 / ((double)H * W))},
+                                 max_out, st);
   }
   f32::ColImageIO io{grid_premod, image, W, H, (H / 2 + W / 2) & 1,
                      (float)(1.0 / ((double)H * W))};

@@ -697,12 +697,18 @@ int cg_degrid(const cg_plan *p, const void *ktab, const void *grid, void *out,
   if (p->n == 0) return CG_OK;
   CG_REQUIRE(ktab && grid && out, "NULL argument");
   cudaStream_t s = (cudaStream_t)stream;
+  const int dvis = tuning().dvis;
+  // lane-layout plans: the lane kernel's degridding traversal (slices by bulk
+  // copies, no output grid) unless the tuning asks for the tiled degridder
+  if (dvis == 0 && layout_for(p->kd) == CG_LAYOUT_LANE)
+    return lane_launch(p, (const float2 *)ktab, nullptr, nullptr, 0, nullptr,
+                       (const float2 *)grid, (float2 *)out, 0, true, s);
   TiledArgs A = tiled_args(p);
   const int SS = p->kd.S * p->kd.S;
   const int need = (SS + 31) / 32;
   const int threads = 256;
   const size_t smem = (size_t)p->pitch * p->win * sizeof(float2);
-  const bool four = tuning().dvis == 4;  // visibilities per warp step: 4, or 2
+  const bool four = dvis == 4;  // visibilities per warp step: 4, or 2
   void (*fn)(TiledArgs, const float2 *, const float2 *, float2 *) = nullptr;
 #define PICK(M)                                                                \
   if (!fn && need <= M)                                                        \

@@ -46,6 +46,7 @@ struct LaneArgs {
   long long wait_cycles;  // limit of a consumer's wait for a slice (the drain keeps LANE_WAIT_CYCLES)
   int kstride;            // elements between slices in ktab and in the stage ring (4-D tables)
   int depth;              // bulk-copy stages per warp, 2..LANE_DEPTH
+  int degrid_only;        // fused form without an output grid: the degridder alone
   int warp_bytes;         // shared memory per warp
   int stage_off, meta_off, val_off, bar_off;  // byte offsets inside a warp's region
 };
@@ -171,6 +172,7 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
     // window: staging and flushing the window would cost more than per-tap
     // global atomics (sparse tiles, e.g. the many small sub-grids of w-towers).
     const bool direct = (int64_t)n * SS * 2 < (int64_t)win * win;
+    const bool gout = !FUSED || !P.degrid_only;  // this traversal grids
     const float2 *gin = FUSED ? P.grid_in + org.layer_off + (size_t)org.wy0 * A.W + org.wx0
                               : nullptr;
 
@@ -291,7 +293,9 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
           u.y -= sum.y;
         }
       }
-      if (direct) {
+      if (!gout) {
+        // degridding only: nothing to add
+      } else if (direct) {
         // sparse item: the taps go straight to the grid (float2 atomics)
         float2 *gp = P.grid + org.layer_off + (size_t)(org.wy0 + (m.x >> 16)) * A.W +
                      org.wx0 + (m.x & 0xffff);
@@ -362,7 +366,7 @@ __global__ void __launch_bounds__(512) k_lane(TiledArgs A, LaneArgs P) {
       __syncwarp();
       return;
     }
-    for (int row = 0; row < (direct ? 0 : win); ++row) {
+    for (int row = 0; row < (direct || !gout ? 0 : win); ++row) {
       const int gy = org.wy0 + row;
       for (int q = lane; q < win; q += 32) {
         const int c = row * pitch + q;
@@ -441,6 +445,7 @@ int lane_launch(const cg_plan *p, const float2 *ktab, const float2 *vis, const f
   P.mode = fused ? (residual ? 1 : 0) : gmode;
   P.wait_cycles = wait_cycles();
   P.kstride = KS;
+  P.degrid_only = fused && grid == nullptr;
   auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
   size_t off = up16((size_t)p->pitch * p->win * sizeof(float2));
   P.stage_off = (int)off;

@@ -1,7 +1,8 @@
 // Host check of crocodile_gb300/csrc/fft32.h: the register-blocked Stockham
 // stages (radix 16, one first stage of radix 2, 4 or 8), run thread by
 // thread as the kernels run them (all threads' loads of a stage before any
-// store, one buffer), against a direct DFT in double precision for
+// store, one buffer, the two-level twiddle table), against a direct DFT in
+// double precision for
 // N = 64 .. 8192 and both signs.  Prints the worst error relative to the
 // transform's norm; exit status 0 when it is below 1e-6.
 #include <cmath>
@@ -28,7 +29,11 @@ int main() {
         const double a = sign * 2.0 * M_PI * j / N;
         tw[j] = {(float)std::cos(a), (float)std::sin(a)};
       }
-      auto twf = [&](int j) { return tw[j]; };
+      // the kernels' two-level table: w^j = A[j mod 64] * C[j / 64] for N > 64
+      std::vector<cf> A(64), Cc(N / 64 + 1);
+      for (int a = 0; a < 64; ++a) A[a] = tw[a % N];
+      for (int c = 0; c * 64 < N; ++c) Cc[c] = tw[c * 64];
+      auto twf = [&](int j) { return N > 64 ? cf_mul(A[j & 63], Cc[j >> 6]) : tw[j]; };
       std::vector<std::vector<cf>> regs(T, std::vector<cf>(16));
       const int ns = stage_count(logn);
       for (int s = 0; s < ns; ++s) {

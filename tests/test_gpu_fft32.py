@@ -43,10 +43,14 @@ def test_centred_fft32_matches_numpy(env, H, W):
         assert rel(t.cpu().numpy(), ref) < 2e-6, (H, W, inverse)
 
 
-def test_batched_and_raw_fft32(env):
+@pytest.mark.parametrize("shape", [(3, 256, 512), (2, 4096, 4096)])
+def test_batched_and_raw_fft32(env, shape):
+    """Column tiles (256 x 512) and, for square planes of 4096 and up, rows
+    between two in-place transposes."""
     torch, E, S, O = env
     rng = numpy.random.default_rng(3)
-    a = _rand(rng, (3, 256, 512))
+    a = _rand(rng, shape)
+    H, W = shape[1], shape[2]
     t = E.cuda_tensor(a, E.CF)
     E.fft_(t, True)
     ref = numpy.array([O.ifft(p) for p in a])
@@ -54,7 +58,7 @@ def test_batched_and_raw_fft32(env):
     for inverse in (False, True):
         t = E.cuda_tensor(a, E.CF)
         E.fft_raw(t, inverse)
-        ref = numpy.fft.ifft2(a) * 256 * 512 if inverse else numpy.fft.fft2(a)
+        ref = numpy.fft.ifft2(a) * H * W if inverse else numpy.fft.fft2(a)
         assert rel(t.cpu().numpy(), ref) < 2e-6
 
 
