@@ -190,9 +190,10 @@ __global__ void __launch_bounds__(ROW_THREADS, 2) k_fft32_rows(RowIO io, int64_t
     stage_store(LOGN, 0, t, sts, v);
 #pragma unroll
     for (int s = 1; s < NS; ++s) {
-      __syncthreads();  // the previous stage's stores are visible
+      // a row of N <= 512 is one warp's (T <= 32 threads): warp barriers suffice
+      if (T <= 32) __syncwarp(); else __syncthreads();  // previous stores visible
       stage_load(LOGN, s, t, lds, twf, v);
-      __syncthreads();  // every read of this stage is done before any write
+      if (T <= 32) __syncwarp(); else __syncthreads();  // all reads before any write
       stage_dft(LOGN, s, sign, v);
       if (s + 1 < NS) {
         stage_store(LOGN, s, t, sts, v);
