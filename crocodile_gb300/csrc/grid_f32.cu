@@ -698,9 +698,10 @@ int cg_degrid(const cg_plan *p, const void *ktab, const void *grid, void *out,
   CG_REQUIRE(ktab && grid && out, "NULL argument");
   cudaStream_t s = (cudaStream_t)stream;
   const int dvis = tuning().dvis;
-  // lane-layout plans: the lane kernel's degridding traversal (slices by bulk
-  // copies, no output grid) unless the tuning asks for the tiled degridder
-  if (dvis == 0 && layout_for(p->kd) == CG_LAYOUT_LANE)
+  // dvis 1: lane-layout plans through the lane kernel's degridding traversal
+  // (slices by bulk copies, no output grid); everything else through the
+  // tiled degridder, which is the faster of the two at S 16
+  if (dvis == 1 && layout_for(p->kd) == CG_LAYOUT_LANE)
     return lane_launch(p, (const float2 *)ktab, nullptr, nullptr, 0, nullptr,
                        (const float2 *)grid, (float2 *)out, 0, true, s);
   TiledArgs A = tiled_args(p);

@@ -105,10 +105,9 @@ typedef struct {
  * residues per owner-layout thread (1..8), or bulk-copy stages per
  * lane-layout warp (2..4; other values: 3); groups: owner-layout thread
  * groups, or warp-layout warps, per CTA (1..8), or lane-layout warps per
- * CTA (1..16); dvis: the degridder: 0 (automatic) runs lane-layout plans
- * through the lane kernel's degridding traversal and others through the
- * tiled degridder with 2 visibilities per warp step; 2 or 4 select the tiled
- * degridder with that many.  layout 0 picks CG_LAYOUT_LANE (with 16-cell tiles) for
+ * CTA (1..16); dvis: the degridder: 0 (automatic) or 2 runs the tiled
+ * degridder with 2 visibilities per warp step, 4 with 4; 1 runs lane-layout
+ * plans through the lane kernel's degridding traversal (others as 0).  layout 0 picks CG_LAYOUT_LANE (with 16-cell tiles) for
  * non-separable tables with even S <= 16, whose slices stream by bulk
  * copies as they are, and CG_LAYOUT_WARP otherwise.  Process-wide. */
 #define CG_LAYOUT_WARP 1

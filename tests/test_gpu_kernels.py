@@ -97,6 +97,7 @@ def _wproj_case(O, n=20000, N=256, seed=5):
     {"layout": 3, "rows": 2, "tile": 16},            # two bulk-copy stages per warp
     {"layout": 3, "rows": 3, "groups": 14, "tile": 16, "chunk": 64},
     {"layout": 3, "tile": 16, "dvis": 4},            # degridder: four visibilities a warp
+    {"layout": 3, "tile": 16, "dvis": 1},            # degridder: the lane kernel's traversal
     {"layout": 1, "groups": 8, "tile": 32, "chunk": 100, "dvis": 4},
 ])
 def test_gridder_shapes_match_oracle(env, cfg):
