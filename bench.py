@@ -705,9 +705,33 @@ def run_ours(args):
 
     pipeline(2)  # warm-up
     ms_e2e = pipeline(k_steps)
+
+    def copies_alone():
+        # one step's copy-in and copy-out, each alone on its stream (no kernels)
+        c = [ev() for _ in range(4)]
+        torch.cuda.synchronize()
+        c[0].record(s_in)
+        with torch.cuda.stream(s_in):
+            d_uvw[1].copy_(h_uvw, non_blocking=True)
+            d_vis[1].copy_(h_vis, non_blocking=True)
+        c[1].record(s_in)
+        torch.cuda.synchronize()
+        c[2].record(s_outs)
+        with torch.cuda.stream(s_outs):
+            h_grid[1].copy_(d_grid[1], non_blocking=True)
+            h_out[1].copy_(d_out[1], non_blocking=True)
+        c[3].record(s_outs)
+        torch.cuda.synchronize()
+        return c[0].elapsed_time(c[1]), c[2].elapsed_time(c[3])
+
+    ms_in, ms_out = copies_alone()
+    h2d = h_uvw.numel() * 8 + h_vis.numel() * 8
+    d2h = h_grid[0].numel() * 8 + h_out[0].numel() * 8
     e2e = {"value": world * n / (ms_e2e * 1e-3) / 1e6, "unit": "Mvis/s",
-           "h2d_bytes_per_step": h_uvw.numel() * 8 + h_vis.numel() * 8,
-           "d2h_bytes_per_step": h_grid[0].numel() * 8 + h_out[0].numel() * 8,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "ms_per_step": ms_e2e,
+           "copy_in_alone_ms": ms_in, "copy_in_gb_s": h2d / ms_in / 1e6,
+           "copy_out_alone_ms": ms_out, "copy_out_gb_s": d2h / ms_out / 1e6,
            "form": "pipelined over %d steps: copy-in, kernels and copy-out on three streams, "
                    "double-buffered device inputs and results" % k_steps}
     G.st.check()

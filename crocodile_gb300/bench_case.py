@@ -116,8 +116,11 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--nvis", type=int, default=500_000)
     ap.add_argument("--steps", type=int, default=2)
-    ap.add_argument("--workload", default="wproj", choices=["wproj", "plain", "aw", "fft"],
-                    help="fft: one --nvis x --nvis complex64 plane, centred inverse FFTs")
+    ap.add_argument("--workload", default="wproj",
+                    choices=["wproj", "plain", "aw", "fft", "wstack"],
+                    help="fft: one --nvis x --nvis complex64 plane, centred inverse FFTs; "
+                         "wstack: w-stacking imaging of 4096^2, 32 planes, 4M visibilities "
+                         "(--nvis ignored)")
     ap.add_argument("--tune", action="store_true", help="autotune the launch shape first")
     ap.add_argument("--fused", action="store_true",
                     help="one degrid+grid pass (cg_degrid_grid) instead of two calls")
@@ -137,6 +140,21 @@ def main():
             E.fft_(g, True)
         torch.cuda.synchronize()
         print("fft %d^2: %.3f ms per transform" % (N, 1e3 * (time.perf_counter() - t0) / a.steps))
+        return
+    if a.workload == "wstack":  # one batched w-stacking imaging call per step
+        w = configs.wstack()
+        aa = synthesis.anti_aliasing_function(w.N, 0, 8)
+        kv = numpy.asarray(synthesis.kernel_oversample(aa, 8, 8))
+        uvw = torch.from_numpy(w.uvw).cuda()
+        vis = torch.from_numpy(w.vis).cuda()
+        plane = w.params["plane"]
+        synthesis.w_stack_imaging(w.theta, w.lam, uvw, None, vis, kv, plane)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            synthesis.w_stack_imaging(w.theta, w.lam, uvw, None, vis, kv, plane)
+        torch.cuda.synchronize()
+        print("wstack %s: %.3f ms per call" % (w.name, 1e3 * (time.perf_counter() - t0) / a.steps))
         return
     ctx = setup(a.workload, a.nvis)
     if a.tuning:

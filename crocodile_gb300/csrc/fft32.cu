@@ -4,15 +4,18 @@
 // and the dirty image of do_imaging (real part of the centred ifft, :903-906),
 // for sides 64 .. 8192.
 //
-// Two passes over HBM per plane, both in place:
-//   rows:    512 threads per CTA transform 512 / (N / 16) whole rows;
-//   columns: up to 512 threads per CTA transform a tile of C adjacent
-//            columns (C x 8 bytes of every row, H x C <= 8192 elements).
+// Passes over HBM per plane:
+//   rows:    N / 16 threads per row, whole rows per CTA, in place;
+//   columns up to 2048: up to 512 threads per CTA transform a tile of C
+//            adjacent columns (C x 8 bytes of every row, H x C <= 8192
+//            elements), in place;
+//   columns from 4096: two four-step passes over tiles of 32 columns
+//            (H = H1 x H2, lines of H1 then H2 elements), the second out of
+//            place (through a scratch stack, or into the dirty image).
 // Each line runs the register-blocked Stockham stages of fft32.h (radix 16,
 // 16 values per thread): the first stage reads global memory and the last
 // writes it, coalesced; the stages between exchange through one padded
-// shared-memory buffer (every thread reads, barrier, every thread writes),
-// so a line makes one or two round trips through shared memory.  The
+// shared-memory buffer (every thread reads, barrier, every thread writes).  The
 // centring of the centred transform is the checkerboard identity for even
 // sides,
 //   fftshift(F(ifftshift x))[k] = (-1)^(k + H/2 + W/2) F((-1)^n x)[k],
@@ -33,23 +36,17 @@ namespace cg {
 namespace f32 {
 
 constexpr int MIN_LOG = 6, MAX_LOG = 13;
-constexpr int ROW_THREADS = 512, COL_THREADS = 512;
-// square planes from this side on run their columns as rows between two
-// in-place transposes (the column tiles hold only 1 or 2 columns there)
-constexpr int TRANSPOSE_MIN = 4096;
+constexpr int COL_THREADS = 512;
+// columns from this length on run as the four-step passes (both >= 64)
+constexpr int STEP_MIN = 4096;
 
 __device__ __forceinline__ int pad(int e) { return e + (e >> 5); }  // bank spread
 
-// Twiddles w_N^j = exp(sign 2 pi i j / N), j < N, as a two-level table:
-// w_N^j = A[j mod TWB] * C[j / TWB], A[a] = w_N^a (a < TWB), C[c] = w_N^(c TWB)
-// (c < N / TWB); TWB + N / TWB entries (192 for N = 8192), staged in shared
-// memory by every CTA.  Each twiddle costs one complex product more than a
-// full table (within about 1.5 units of FP32 rounding).  Cached per device,
-// log N and sign.
-constexpr int TWB_LOG = 6, TWB = 1 << TWB_LOG;
-constexpr int tw_entries(int logn) {
-  return logn > TWB_LOG ? TWB + (1 << (logn - TWB_LOG)) : (1 << logn) + 1;
-}
+// Twiddles: the per-stage tables of fft32.h (tw_table_fill / tw_lookup),
+// correctly rounded entries computed in double on the host, staged in
+// shared memory by every CTA (1312 entries for N = 8192).  Cached per
+// device, log N and sign.
+constexpr int tw_entries(int logn) { return tw_table_entries(logn) + 1; }
 std::mutex g_mu;
 std::map<std::tuple<int, int, int>, float2 *> g_tw;
 
@@ -64,14 +61,11 @@ int twiddles(int logn, int sign, const float2 **out) {
     return CG_OK;
   }
   const int n = 1 << logn;
-  const int nb = logn > TWB_LOG ? TWB : n, nc = logn > TWB_LOG ? n / TWB : 1;
-  std::vector<float2> h(tw_entries(logn));
-  auto w = [&](long j) {
+  std::vector<cf> h(tw_entries(logn));
+  tw_table_fill(logn, [&](long long j) {
     const double a = 2.0 * M_PI * (double)j / (double)n;
-    return make_float2((float)std::cos(a), (float)(sign * std::sin(a)));
-  };
-  for (int a = 0; a < nb; ++a) h[a] = w(a);
-  for (int c = 0; c < nc; ++c) h[nb + c] = w((long)c * nb);
+    return cf{(float)std::cos(a), (float)(sign * std::sin(a))};
+  }, h.data());
   float2 *d = nullptr;
   CG_CUDA(cudaMalloc(&d, h.size() * sizeof(float2)));
   CG_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice));
@@ -80,17 +74,15 @@ int twiddles(int logn, int sign, const float2 **out) {
   return CG_OK;
 }
 
-// the two-level table in shared memory
+// the table in shared memory
 template <int LOGN>
-struct SmTw2 {
+struct SmTw {
   const float2 *t;
-  __device__ cf operator()(int j) const {
-    if (LOGN <= TWB_LOG) {
-      const float2 v = t[j];
+  __device__ cf operator()(int s, int r, int k) const {
+    return tw_lookup(LOGN, s, r, k, [this](int i) {
+      const float2 v = t[i];
       return cf{v.x, v.y};
-    }
-    const float2 a = t[j & (TWB - 1)], c = t[TWB + (j >> TWB_LOG)];
-    return cf_mul(cf{a.x, a.y}, cf{c.x, c.y});
+    });
   }
 };
 
@@ -103,11 +95,7 @@ struct RowIO {
   int post;      // rows-only transforms: times scale (-1)^(k + phase) on the way out
   int phase;
   float scale;
-  __device__ float2 ld(int64_t row, int i) const {
-    float2 v = d[row * W + i];
-    if (modulate && (((int)(row % H) + i) & 1)) v = make_float2(-v.x, -v.y);
-    return v;
-  }
+  __device__ const float2 *src(int64_t row) const { return d + row * W; }
   __device__ void st(int64_t row, int i, float2 v) const {
     if (post) {
       const float s = ((i + phase) & 1) ? -scale : scale;
@@ -159,41 +147,60 @@ __device__ __forceinline__ void atomic_max_f(float *addr, float v) {
 }
 
 // ---------------------------------------------------------------- kernels
-// T = N / 16 threads per line.  Rows: 512 / T lines per CTA.
+// Rows: T = N / 16 threads per row, TPC = max(T, 256) threads and TPC / T
+// rows per CTA at a time (small CTAs: each barrier holds fewer warps); the
+// first stage loads global memory straight into registers and the last
+// stage writes it from registers.  (Copying the next row into a
+// second shared buffer by cp.async while a row is transformed, at the cost
+// of half the CTAs per SM, measured slower: 0.088 against 0.078 ms for the
+// rows of a 4096^2 plane, 0.350 against 0.300 ms at 8192^2.)
 template <int LOGN>
-__global__ void __launch_bounds__(ROW_THREADS, 2) k_fft32_rows(RowIO io, int64_t nrows,
-                                                            const float2 *__restrict__ tw,
-                                                            int sign) {
-  constexpr int N = 1 << LOGN, T = N / 16, LPC = ROW_THREADS / T, P = N + N / 32;
+struct RowShape {
+  static constexpr int N = 1 << LOGN, T = N / 16;
+  static constexpr int TPC = T > 256 ? T : 256, LPC = TPC / T, MINB = 1024 / TPC;
+  static constexpr int P = N + N / 32;  // padded row
+};
+
+template <int LOGN>
+__global__ void __launch_bounds__(RowShape<LOGN>::TPC, RowShape<LOGN>::MINB)
+    k_fft32_rows(RowIO io, int64_t nrows, const float2 *__restrict__ tw, int sign) {
+  using RS = RowShape<LOGN>;
+  constexpr int T = RS::T, LPC = RS::LPC, P = RS::P;
   constexpr int NS = (LOGN + 3) / 4;
   extern __shared__ float2 f32_sm[];
   const int line = threadIdx.x / T, t = threadIdx.x % T;
   float2 *buf = f32_sm + line * P;
   float2 *stw = f32_sm + LPC * P;
-  for (int k = threadIdx.x; k < tw_entries(LOGN); k += ROW_THREADS) stw[k] = tw[k];
+  for (int k = threadIdx.x; k < tw_entries(LOGN); k += RS::TPC) stw[k] = tw[k];
   __syncthreads();
-  const SmTw2<LOGN> twf{stw};
-  auto lds = [&](int e) {
-    const float2 v = buf[pad(e)];
-    return cf{v.x, v.y};
+  const SmTw<LOGN> twf{stw};
+  // a row of N <= 512 is one warp's (T <= 32 threads): warp barriers suffice
+  auto sync = [] {
+    if (T <= 32) __syncwarp(); else __syncthreads();
   };
-  auto sts = [&](int e, cf v) { buf[pad(e)] = make_float2(v.x, v.y); };
+  auto lds = [&](int e) {
+    const float2 x = buf[pad(e)];
+    return cf{x.x, x.y};
+  };
+  auto sts = [&](int e, cf x) { buf[pad(e)] = make_float2(x.x, x.y); };
   for (int64_t row0 = (int64_t)blockIdx.x * LPC; row0 < nrows; row0 += (int64_t)gridDim.x * LPC) {
     const int64_t row = row0 + line;
     const bool live = row < nrows;
+    const int rpar = io.modulate ? (int)(row % io.H) & 1 : 0;
+    const float2 *src = io.src(row);
     cf v[16];
     stage_load(LOGN, 0, t, [&](int e) {
-      const float2 x = live ? io.ld(row, e) : make_float2(0.f, 0.f);
-      return cf{x.x, x.y};
+      if (!live) return cf{0.f, 0.f};
+      const float2 x = src[e];
+      return (io.modulate && ((rpar + e) & 1)) ? cf{-x.x, -x.y} : cf{x.x, x.y};
     }, twf, v);
     stage_dft(LOGN, 0, sign, v);
     stage_store(LOGN, 0, t, sts, v);
 #pragma unroll
     for (int s = 1; s < NS; ++s) {
-      // a row of N <= 512 is one warp's (T <= 32 threads): warp barriers suffice
-      if (T <= 32) __syncwarp(); else __syncthreads();  // previous stores visible
+      sync();  // previous stores visible
       stage_load(LOGN, s, t, lds, twf, v);
-      if (T <= 32) __syncwarp(); else __syncthreads();  // all reads before any write
+      sync();  // all reads before any write
       stage_dft(LOGN, s, sign, v);
       if (s + 1 < NS) {
         stage_store(LOGN, s, t, sts, v);
@@ -217,7 +224,7 @@ __global__ void __launch_bounds__(COL_THREADS) k_fft32_cols(IO io, int64_t nplan
   float2 *stw = f32_sm + (H + H / 32) * C;
   for (int k = threadIdx.x; k < tw_entries(LOGH); k += C * T) stw[k] = tw[k];
   __syncthreads();
-  const SmTw2<LOGH> twf{stw};
+  const SmTw<LOGH> twf{stw};
   auto lds = [&](int e) {
     const float2 v = f32_sm[pad(e) * C + c];
     return cf{v.x, v.y};
@@ -257,79 +264,243 @@ __global__ void __launch_bounds__(COL_THREADS) k_fft32_cols(IO io, int64_t nplan
   }
 }
 
-// ---------------------------------------------------------------- square transposes
-// In place on nplanes N x N planes: the CTA of tile pair (I, J), I <= J, of
-// 32 x 32 tiles reads both tiles into shared memory and writes each to the
-// other's place (a diagonal tile to itself).  The store policy takes the
-// final position (r, c); the last transpose of a centred transform applies
-// (-1)^(r + c + phase) and the scale there, or writes the dirty image.
-struct TpPlain {
-  __device__ void st(float2 *d, int64_t off, int, int, float2 v, float &) const { d[off] = v; }
-  static constexpr bool kMax = false;
+// ---------------------------------------------------------------- four-step columns
+// Columns of length H = H1 x H2 (H1, H2 >= 64) in two passes over tiles of
+// 32 adjacent columns (256 contiguous bytes of every row touched), with
+// n = n1 H2 + n2 and k = k1 + H1 k2:
+//   A: for each n2, Y[k1, n2] = w_H^(n2 k1) sum_n1 x[n1 H2 + n2] w_H1^(n1 k1),
+//      stored at row k1 H2 + n2 (the rows it read: A may run in place);
+//   B: for each k1, X[k1 + H1 k2] = sum_n2 Y[k1, n2] w_H2^(n2 k2), reading the
+//      block of rows k1 H2 .. k1 H2 + H2 - 1 and writing row k1 + H1 k2 (out
+//      of place: the rows it writes belong to other blocks).
+// A unit is (plane, n2 or k1, tile), the tile fastest, so neighbouring CTAs
+// touch neighbouring 256-byte segments of the same rows.  The twiddles of A
+// come from a full table of w_H^j in global memory (the 32 lanes of a warp
+// share k1: one broadcast load).
+struct StepShape {
+  int W, H1, H2, tiles;  // tiles = W / 32
+  int nj;                // units per plane and tile: H2 (pass A) or H1 (pass B)
+  int64_t plane;         // elements per plane
+  __device__ void unit(int64_t u, int64_t &pl, int &j, int &col0) const {
+    const int64_t per = (int64_t)tiles * nj;
+    pl = u / per;
+    const int64_t r = u - pl * per;
+    j = (int)(r / tiles);
+    col0 = (int)(r - (int64_t)j * tiles) * 32;
+  }
 };
-struct TpCentred {
-  int phase;
-  float scale;
-  __device__ void st(float2 *d, int64_t off, int r, int c, float2 v, float &) const {
-    const float s = ((r + c + phase) & 1) ? -scale : scale;
-    d[off] = make_float2(v.x * s, v.y * s);
+
+// Per unit and column: ctx(u, c) gives the input column (element i at
+// src[i * stride]) and what the store needs; st(x, i, v, mx) stores output i.
+struct StepCtx {
+  const float2 *src;
+  int64_t stride;
+  float2 *dst;   // complex output column (pass A, B)
+  float *fdst;   // image column (pass B of the dirty image)
+  int j, col;
+};
+
+struct StepA {
+  StepShape sh;
+  const float2 *in;
+  float2 *out;
+  const float2 *twH;  // w_H^j, j < H
+  __device__ StepCtx ctx(int64_t u, int c) const {
+    int64_t pl;
+    int j, col0;
+    sh.unit(u, pl, j, col0);
+    const int64_t base = pl * sh.plane + (int64_t)j * sh.W + col0 + c;
+    return StepCtx{in + base, (int64_t)sh.H2 * sh.W, out + base, nullptr, j, col0 + c};
+  }
+  __device__ void st(const StepCtx &x, int k1, cf v, float &) const {
+    const float2 w = twH[x.j * k1];
+    x.dst[(int64_t)k1 * x.stride] = make_float2(fmaf(v.x, w.x, -v.y * w.y),
+                                                fmaf(v.x, w.y, v.y * w.x));
   }
   static constexpr bool kMax = false;
 };
-struct TpImage {
+
+// B into complex planes: times scale, and (-1)^(row + col + phase) if centred
+struct StepB {
+  StepShape sh;
+  const float2 *in;
+  float2 *out;
+  int centred, phase;
+  float scale;
+  __device__ StepCtx ctx(int64_t u, int c) const {
+    int64_t pl;
+    int j, col0;
+    sh.unit(u, pl, j, col0);
+    const int64_t pb = pl * sh.plane + col0 + c;
+    return StepCtx{in + pb + (int64_t)j * sh.H2 * sh.W, sh.W, out + pb + (int64_t)j * sh.W,
+                   nullptr, j, col0 + c};
+  }
+  __device__ void st(const StepCtx &x, int k2, cf v, float &) const {
+    float s = scale;
+    if (centred && ((x.j + sh.H1 * k2 + x.col + phase) & 1)) s = -s;
+    x.dst[(int64_t)k2 * sh.H1 * sh.W] = make_float2(v.x * s, v.y * s);
+  }
+  static constexpr bool kMax = false;
+};
+
+// B of the dirty image: the real part, demodulated and scaled, and its maximum
+struct StepBImage {
+  StepShape sh;
+  const float2 *in;
   float *img;
   int phase;
   float scale;
-  __device__ void st(float2 *, int64_t off, int r, int c, float2 v, float &mx) const {
-    const float x = v.x * (((r + c + phase) & 1) ? -scale : scale);
-    img[off] = x;
-    mx = fmaxf(mx, x);
+  __device__ StepCtx ctx(int64_t u, int c) const {
+    int64_t pl;
+    int j, col0;
+    sh.unit(u, pl, j, col0);
+    const int col = col0 + c;
+    return StepCtx{in + (int64_t)j * sh.H2 * sh.W + col, sh.W, nullptr,
+                   img + (int64_t)j * sh.W + col, j, col};
+  }
+  __device__ void st(const StepCtx &x, int k2, cf v, float &mx) const {
+    const float r = v.x * (((x.j + sh.H1 * k2 + x.col + phase) & 1) ? -scale : scale);
+    x.fdst[(int64_t)k2 * sh.H1 * sh.W] = r;
+    mx = fmaxf(mx, r);
   }
   static constexpr bool kMax = true;
 };
 
-template <class ST>
-__global__ void __launch_bounds__(256) k_fft32_transpose(float2 *d, int N, ST st, float *max_out) {
-  __shared__ float2 ta[32][33], tb[32][33];
-  const int nt = N / 32;
-  const int I = blockIdx.x / nt, J = blockIdx.x - (blockIdx.x / nt) * nt;
+// One pass of the four-step columns: lines of L = 2^LOGL, 32 columns per
+// tile, T = L / 16 threads per column (thread (t, c), c fastest).
+template <int LOGL, class IO>
+__global__ void __launch_bounds__(32 * (1 << (LOGL - 4)), 6 >> (LOGL - 6))
+    k_fft32_step(IO io, int64_t units, const float2 *__restrict__ tw, int sign,
+                 float *max_out) {
+  constexpr int L = 1 << LOGL, T = L / 16, C = 32, NS = (LOGL + 3) / 4;
+  extern __shared__ float2 f32_sm[];
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  float2 *stw = f32_sm + (L + L / 32) * C;
+  for (int k = threadIdx.x; k < tw_entries(LOGL); k += C * T) stw[k] = tw[k];
+  __syncthreads();
+  const SmTw<LOGL> twf{stw};
+  auto lds = [&](int e) {
+    const float2 v = f32_sm[pad(e) * C + c];
+    return cf{v.x, v.y};
+  };
+  auto sts = [&](int e, cf v) { f32_sm[pad(e) * C + c] = make_float2(v.x, v.y); };
   float mx = -FLT_MAX;
-  if (I <= J) {
-    float2 *p = d + (int64_t)blockIdx.y * N * N;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
+    const StepCtx x = io.ctx(u, c);
+    cf v[16];
+    __syncthreads();  // the previous unit's last reads of shared memory are done
+    stage_load(LOGL, 0, t, [&](int e) {
+      const float2 y = x.src[e * x.stride];
+      return cf{y.x, y.y};
+    }, twf, v);
+    stage_dft(LOGL, 0, sign, v);
+    stage_store(LOGL, 0, t, sts, v);
 #pragma unroll
-    for (int k = 0; k < 32; k += 8) {
-      ta[ty + k][tx] = p[(int64_t)(I * 32 + ty + k) * N + J * 32 + tx];
-      if (I != J) tb[ty + k][tx] = p[(int64_t)(J * 32 + ty + k) * N + I * 32 + tx];
-    }
-    __syncthreads();
-    const int64_t plane = (int64_t)blockIdx.y * N * N;
-#pragma unroll
-    for (int k = 0; k < 32; k += 8) {
-      // tile (J, I) receives ta transposed; tile (I, J) receives tb transposed
-      const int r1 = J * 32 + ty + k, c1 = I * 32 + tx;
-      st.st(d, plane + (int64_t)r1 * N + c1, r1, c1, ta[tx][ty + k], mx);
-      if (I != J) {
-        const int r2 = I * 32 + ty + k, c2 = J * 32 + tx;
-        st.st(d, plane + (int64_t)r2 * N + c2, r2, c2, tb[tx][ty + k], mx);
-      }
+    for (int s = 1; s < NS; ++s) {
+      __syncthreads();
+      stage_load(LOGL, s, t, lds, twf, v);
+      __syncthreads();
+      stage_dft(LOGL, s, sign, v);
+      if (s + 1 < NS)
+        stage_store(LOGL, s, t, sts, v);
+      else
+        stage_store(LOGL, s, t, [&](int e, cf y) { io.st(x, e, y, mx); }, v);
     }
   }
-  if (ST::kMax && max_out) {
+  if (IO::kMax && max_out) {
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) atomic_max_f(max_out, mx);
   }
 }
 
-template <class ST>
-int launch_transpose(float2 *d, int64_t nplanes, int N, const ST &st, float *max_out,
-                     cudaStream_t s) {
-  CG_REQUIRE(N % 32 == 0 && nplanes <= 65535, "transpose needs N a multiple of 32");
-  const int nt = N / 32;
-  k_fft32_transpose<ST><<<dim3((unsigned)(nt * nt), (unsigned)nplanes), 256, 0, s>>>(d, N, st,
-                                                                                      max_out);
-  CG_LAUNCH("FP32 FFT transpose");
+// w_H^j for j < H, correctly rounded, cached per device, log H and sign
+std::map<std::tuple<int, int, int>, float2 *> g_twfull;
+
+int twiddles_full(int logn, int sign, const float2 **out) {
+  int dev = 0;
+  CG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_mu);
+  const auto key = std::make_tuple(dev, logn, sign);
+  auto it = g_twfull.find(key);
+  if (it != g_twfull.end()) {
+    *out = it->second;
+    return CG_OK;
+  }
+  const int n = 1 << logn;
+  std::vector<float2> h(n);
+  for (int j = 0; j < n; ++j) {
+    const double a = 2.0 * M_PI * (double)j / (double)n;
+    h[j] = make_float2((float)std::cos(a), (float)(sign * std::sin(a)));
+  }
+  float2 *d = nullptr;
+  CG_CUDA(cudaMalloc(&d, h.size() * sizeof(float2)));
+  CG_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice));
+  g_twfull[key] = d;
+  *out = d;
   return CG_OK;
+}
+
+template <int LOGL, class IO>
+int launch_step_as(const IO &io, int64_t units, int sign, float *max_out, cudaStream_t st) {
+  constexpr int L = 1 << LOGL, threads = 32 * (L / 16);
+  const float2 *tw;
+  int rc = twiddles(LOGL, sign, &tw);
+  if (rc) return rc;
+  const size_t smem = (size_t)((L + L / 32) * 32 + tw_entries(LOGL)) * sizeof(float2);
+  CG_CUDA(cudaFuncSetAttribute(k_fft32_step<LOGL, IO>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft32_step<LOGL, IO>, threads,
+                                                        smem));
+  CG_REQUIRE(per_sm > 0, "FP32 FFT column step does not fit on an SM (smem %zu)", smem);
+  const unsigned grid = (unsigned)std::min<int64_t>(units, (int64_t)num_sms() * per_sm);
+  k_fft32_step<LOGL, IO><<<grid, threads, smem, st>>>(io, units, tw, sign, max_out);
+  CG_LAUNCH("FP32 FFT column step");
+  return CG_OK;
+}
+
+template <class IO>
+int launch_step(int logl, const IO &io, int64_t units, int sign, float *max_out,
+                cudaStream_t st) {
+  switch (logl) {
+    case 6: return launch_step_as<6>(io, units, sign, max_out, st);
+    case 7: return launch_step_as<7>(io, units, sign, max_out, st);
+  }
+  return set_error(CG_ERR_ARG, "FP32 FFT: unsupported column step length 2^%d", logl);
+}
+
+// The scratch stacks of pass B come from a memory pool of the library's own
+// per device, which keeps what it has mapped (release threshold: unlimited),
+// so that repeated transforms neither map nor touch fresh pages; stream
+// ordering keeps concurrent transforms on different streams apart.
+std::map<int, cudaMemPool_t> g_pools;
+
+int scratch_pool(cudaMemPool_t *out) {
+  int dev = 0;
+  CG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_mu);
+  auto it = g_pools.find(dev);
+  if (it != g_pools.end()) {
+    *out = it->second;
+    return CG_OK;
+  }
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool;
+  CG_CUDA(cudaMemPoolCreate(&pool, &props));
+  uint64_t keep = ~0ull;
+  CG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  g_pools[dev] = pool;
+  *out = pool;
+  return CG_OK;
+}
+
+// lengths of the two passes: H1 = 2^ceil(log H / 2) (A), H2 = H / H1 (B)
+void step_split(int logh, int &logh1, int &logh2) {
+  logh1 = (logh + 1) / 2;
+  logh2 = logh - logh1;
 }
 
 __global__ void k_fft32_init_max(float *m) { *m = -FLT_MAX; }
@@ -342,16 +513,20 @@ int log2_exact(int n) {
 
 template <int LOGN>
 int launch_rows(const RowIO &io, int64_t nrows, int sign, cudaStream_t st) {
-  constexpr int N = 1 << LOGN, T = N / 16, LPC = ROW_THREADS / T;
+  using RS = RowShape<LOGN>;
   const float2 *tw;
   int rc = twiddles(LOGN, sign, &tw);
   if (rc) return rc;
-  const size_t smem = (size_t)(LPC * (N + N / 32) + tw_entries(LOGN)) * sizeof(float2);
+  const size_t smem = (size_t)(RS::LPC * RS::P + tw_entries(LOGN)) * sizeof(float2);
   CG_CUDA(cudaFuncSetAttribute(k_fft32_rows<LOGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem));
-  const int64_t ctas = (nrows + LPC - 1) / LPC;
-  const unsigned grid = (unsigned)std::min<int64_t>(ctas, (int64_t)num_sms() * 3);
-  k_fft32_rows<LOGN><<<grid, ROW_THREADS, smem, st>>>(io, nrows, tw, sign);
+  int per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft32_rows<LOGN>, RS::TPC,
+                                                        smem));
+  CG_REQUIRE(per_sm > 0, "FP32 FFT rows do not fit on an SM (smem %zu)", smem);
+  const int64_t ctas = (nrows + RS::LPC - 1) / RS::LPC;
+  const unsigned grid = (unsigned)std::min<int64_t>(ctas, (int64_t)num_sms() * per_sm);
+  k_fft32_rows<LOGN><<<grid, RS::TPC, smem, st>>>(io, nrows, tw, sign);
   CG_LAUNCH("FP32 FFT rows");
   return CG_OK;
 }
@@ -435,15 +610,39 @@ int fft32_planes(float2 *data, int64_t batch, int H, int W, bool inverse, bool c
   f32::RowIO rio{data, W, H, centred ? 1 : 0, 0, 0, 1.f};
   int rc = f32::dispatch_rows(lw, rio, batch * H, sign, st);
   if (rc) return rc;
-  if (H == W && H >= f32::TRANSPOSE_MIN && batch <= 65535) {
-    // long columns: transpose, transform rows, transpose back (all coalesced)
-    if ((rc = f32::launch_transpose(data, batch, H, f32::TpPlain{}, nullptr, st))) return rc;
-    f32::RowIO r2{data, W, H, 0, 0, 0, 1.f};
-    if ((rc = f32::dispatch_rows(lw, r2, batch * H, sign, st))) return rc;
-    if (centred)
-      return f32::launch_transpose(data, batch, H, f32::TpCentred{phase & 1, (float)scale},
-                                   nullptr, st);
-    return f32::launch_transpose(data, batch, H, f32::TpPlain{}, nullptr, st);
+  if (H >= f32::STEP_MIN && W % 32 == 0) {
+    // long columns: the four-step passes A (into a scratch stack of at most
+    // 1 GiB, a few planes at a time) and B (back into the planes)
+    int l1, l2;
+    f32::step_split(lh, l1, l2);
+    const int64_t plane = (int64_t)H * W;
+    const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(batch, (1LL << 27) / plane));
+    float2 *scratch = nullptr;
+    cudaMemPool_t pool;
+    if ((rc = f32::scratch_pool(&pool))) return rc;
+    CG_CUDA(cudaMallocFromPoolAsync((void **)&scratch, (size_t)(chunk * plane) * sizeof(float2),
+                                    pool, st));
+    const float2 *twH;
+    if ((rc = f32::twiddles_full(lh, sign, &twH))) {
+      cudaFreeAsync(scratch, st);
+      return rc;
+    }
+    for (int64_t b0 = 0; b0 < batch && !rc; b0 += chunk) {
+      const int64_t nb = std::min(chunk, batch - b0);
+      float2 *d = data + b0 * plane;
+      f32::StepShape sa{W, 1 << l1, 1 << l2, W / 32, 1 << l2, plane};
+      f32::StepA A{sa, d, scratch, twH};
+      rc = f32::launch_step(l1, A, nb * sa.nj * sa.tiles, sign, nullptr, st);
+      if (rc) break;
+      f32::StepShape sb = sa;
+      sb.nj = 1 << l1;
+      f32::StepB B{sb, scratch, d, centred ? 1 : 0, phase & 1, (float)scale};
+      rc = f32::launch_step(l2, B, nb * sb.nj * sb.tiles, sign, nullptr, st);
+    }
+    const cudaError_t fe = cudaFreeAsync(scratch, st);
+    if (rc) return rc;
+    CG_CUDA(fe);
+    return CG_OK;
   }
   f32::ColIO cio{data, W, H, centred ? 1 : 0, phase & 1, (float)scale};
   return f32::dispatch_cols(lh, cio, batch, W, sign, nullptr, st);
@@ -463,13 +662,20 @@ int fft32_image(const float2 *grid_premod, int H, int W, float *image, float *ma
     f32::k_fft32_init_max<<<1, 1, 0, st>>>(max_out);
     CG_LAUNCH("image max init");
   }
-  if (H == W && H >= f32::TRANSPOSE_MIN) {
+  if (H >= f32::STEP_MIN && W % 32 == 0) {
+    // four-step columns: A in place on the grid, B into the image
+    int l1, l2;
+    f32::step_split(lh, l1, l2);
+    const float2 *twH;
+    if ((rc = f32::twiddles_full(lh, 1, &twH))) return rc;
     float2 *g = (float2 *)grid_premod;
-    if ((rc = f32::launch_transpose(g, 1, H, f32::TpPlain{}, nullptr, st))) return rc;
-    if ((rc = f32::dispatch_rows(lw, rio, H, 1, st))) return rc;
-    return f32::launch_transpose(g, 1, H, f32::TpImage{image, (H / 2 + W / 2) & 1,
-                                                       (float)(1.0 / ((double)H * W))},
-                                 max_out, st);
+    f32::StepShape sa{W, 1 << l1, 1 << l2, W / 32, 1 << l2, (int64_t)H * W};
+    f32::StepA A{sa, g, g, twH};
+    if ((rc = f32::launch_step(l1, A, (int64_t)sa.nj * sa.tiles, 1, nullptr, st))) return rc;
+    f32::StepShape sb = sa;
+    sb.nj = 1 << l1;
+    f32::StepBImage B{sb, g, image, (H / 2 + W / 2) & 1, (float)(1.0 / ((double)H * W))};
+    return f32::launch_step(l2, B, (int64_t)sb.nj * sb.tiles, 1, max_out, st);
   }
   f32::ColImageIO io{grid_premod, image, W, H, (H / 2 + W / 2) & 1,
                      (float)(1.0 / ((double)H * W))};

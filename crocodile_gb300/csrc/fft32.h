@@ -13,8 +13,8 @@
 //   outputs y[(b - k) R + k + r p].
 // The last stage has p = N / R, so its outputs y[b + r p] are in natural
 // order, and every stage's inputs x[b + r N/R] are contiguous across b:
-// the first stage reads and the last stage writes global memory directly,
-// coalesced across threads.  Between stages all threads read their inputs
+// the first stage can read global memory and the last stage write it
+// directly, coalesced across threads.  Between stages all threads read their inputs
 // before any thread writes, so one buffer holds the line throughout.
 #pragma once
 
@@ -44,9 +44,9 @@ CG_FHD cf cf_mul(cf a, cf b) {
 CG_FHD cf cf_mul_si(cf a, int sign) { return sign > 0 ? cf{-a.y, a.x} : cf{a.y, -a.x}; }
 
 // stages of a 2^logn transform: count, log2 radix and log2 span of stage s
-CG_FHD int stage_count(int logn) { return (logn + 3) / 4; }
-CG_FHD int stage_logr(int logn, int s) { return ((logn & 3) && s == 0) ? (logn & 3) : 4; }
-CG_FHD int stage_logp(int logn, int s) {
+CG_FHD constexpr int stage_count(int logn) { return (logn + 3) / 4; }
+CG_FHD constexpr int stage_logr(int logn, int s) { return ((logn & 3) && s == 0) ? (logn & 3) : 4; }
+CG_FHD constexpr int stage_logp(int logn, int s) {
   const int rem = logn & 3;
   return s == 0 ? 0 : (rem ? rem + 4 * (s - 1) : 4 * s);
 }
@@ -143,10 +143,57 @@ CG_FHD int out_slot(int logr, int r) {
   return r;
 }
 
+// Twiddles of stage s (s >= 1), w_N^(r k N / (p R)) for r < R, k < p, from a
+// table laid out per stage so that a warp's lookups do not conflict in
+// shared-memory banks: with k = k_lo + 32 k_hi (k_lo < 32),
+//   L_s[r][k_lo] = w^(r k_lo N / (p R))      (R x min(p, 32) entries)
+//   H_s[r][k_hi] = w^(r 32 k_hi N / (p R))   (R x p / 32 entries, p > 32)
+// and the twiddle is L_s[r][k] for p <= 32 (the correctly rounded value)
+// or L_s[r][k_lo] H_s[r][k_hi] (one complex product more).  The threads of
+// a warp share k_hi and hold consecutive k_lo (or few distinct k), so L
+// reads are contiguous or broadcast and H reads are broadcast.
+CG_FHD constexpr int tw_stage_entries(int logn, int s) {
+  const int logr = stage_logr(logn, s), logp = stage_logp(logn, s);
+  const int p = 1 << logp, lo = p < 32 ? p : 32, hi = p > 32 ? p >> 5 : 0;
+  return (1 << logr) * (lo + hi);
+}
+CG_FHD constexpr int tw_stage_offset(int logn, int s) {
+  int off = 0;
+  for (int q = 1; q < s; ++q) off += tw_stage_entries(logn, q);
+  return off;
+}
+CG_FHD constexpr int tw_table_entries(int logn) {
+  return tw_stage_offset(logn, stage_count(logn));
+}
+// fills the table; w(j) gives the exact w_N^j (j < N) rounded to FP32
+template <class W>
+inline void tw_table_fill(int logn, const W &w, cf *out) {
+  for (int s = 1; s < stage_count(logn); ++s) {
+    const int logr = stage_logr(logn, s), logp = stage_logp(logn, s);
+    const int R = 1 << logr, p = 1 << logp, lo = p < 32 ? p : 32;
+    const int sh = logn - logp - logr;  // N / (p R) = 2^sh
+    cf *L = out + tw_stage_offset(logn, s), *H = L + R * lo;
+    for (int r = 0; r < R; ++r) {
+      for (int k = 0; k < lo; ++k) L[r * lo + k] = w(((long long)r * k << sh) & ((1 << logn) - 1));
+      for (int kh = 0; kh < (p >> 5) && p > 32; ++kh)
+        H[r * (p >> 5) + kh] = w(((long long)r * 32 * kh << sh) & ((1 << logn) - 1));
+    }
+  }
+}
+// the twiddle of input r of a butterfly with k, at stage s; tb(i) reads entry i
+template <class TB>
+CG_FHD cf tw_lookup(int logn, int s, int r, int k, const TB &tb) {
+  const int logr = stage_logr(logn, s), logp = stage_logp(logn, s);
+  const int R = 1 << logr, p = 1 << logp;
+  const int base = tw_stage_offset(logn, s);
+  if (p <= 32) return tb(base + r * p + k);
+  return cf_mul(tb(base + r * 32 + (k & 31)), tb(base + R * 32 + r * (p >> 5) + (k >> 5)));
+}
+
 // One thread's share of stage s: 16 / R butterflies b = t + m T (m < 16/R,
 // T = N / 16), in three steps so that a kernel can put a barrier between
 // every thread's reads and every thread's writes.  ld(e) / st(e, v) access
-// element e of the line; tw(j) gives w_N^j (j < N).
+// element e of the line; tw(s, r, k) gives w_N^(r k N / (p R)) of stage s.
 template <class LD, class TW>
 CG_FHD void stage_load(int logn, int s, int t, const LD &ld, const TW &tw, cf *v) {
   const int logr = stage_logr(logn, s), logp = stage_logp(logn, s);
@@ -159,7 +206,7 @@ CG_FHD void stage_load(int logn, int s, int t, const LD &ld, const TW &tw, cf *v
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       cf x = ld(b + r * NR);
-      if (r && k) x = cf_mul(x, tw((r * k) << (logn - logp - logr)));  // w_N^(r k N/(pR))
+      if (r && k) x = cf_mul(x, tw(s, r, k));  // w_N^(r k N/(pR))
       v[m * R + r] = x;
     }
   }

@@ -6,8 +6,8 @@
 //       image += ifft(grid_p) / w_kernel_function(l, m, midw)
 //
 // The planes are gridded in one launch into a stack of grids (a layered
-// plan), transformed by one batched cuFFT, and combined here in one pass over
-// the stack.  w_kernel_function (crocodile/synthesis.py:273-293) is
+// plan), transformed as one batch of centred inverse FFTs, and combined here
+// in one pass over the stack.  w_kernel_function (crocodile/synthesis.py:273-293) is
 // exp(2 pi i w ph) with ph = 1 - sqrt(1 - l^2 - m^2); ph is computed in FP64
 // once per pixel, the turns w ph of each plane are formed in double-float
 // arithmetic and reduced to a fraction of a turn before the FP32 sincospi,
@@ -60,6 +60,12 @@ __global__ void k_layer_mean_finish(int layers, const int32_t *__restrict__ coun
 // The turns t = midw_p * ph are formed as a double-float product (midw and ph
 // split into FP32 hi + lo parts, exact FMA residual), so their fraction keeps
 // ~2^-44 relative precision for any w without 32 FP64 products per pixel.
+// ph depends on l^2 + m^2 only, and the coordinates (k - N/2) / N of column
+// k and of its mirror 2 (N/2) - k are negatives of each other, so the pixels
+// (i, j), (i', j), (i, j'), (i', j') share ph and every plane's factor: one
+// thread takes all four (those that exist), with one FP64 ph and one
+// sincospi per plane, and gives each the same result as alone.  Consecutive
+// threads take consecutive j, so the four row segments stay coalesced.
 __global__ void k_wstack_combine(const float2 *__restrict__ planes, int layers, int N,
                                  double theta, const double *__restrict__ midw,
                                  const int32_t *__restrict__ counts, float2 *__restrict__ out,
@@ -72,26 +78,35 @@ __global__ void k_wstack_combine(const float2 *__restrict__ planes, int layers, 
   }
   __syncthreads();
   const int64_t total = (int64_t)N * N;
+  const int half = N / 2, M = half + 1, mirror = 2 * half;  // representatives 0 .. N/2
+  const int64_t reps = (int64_t)M * M;
   int bad = 0;
   // (k - N/2) / N: a multiplication by the exact reciprocal for power-of-two N
   // (the same bits as the division, without an FP64 division per pixel)
   const bool pow2 = (N & (N - 1)) == 0;
   const double invN = 1.0 / (double)N;
-  for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total;
+  for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < reps;
        L += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(L / N), j = (int)(L - (int64_t)i * N);
+    const int i = (int)(L / M), j = (int)(L - (int64_t)i * M);
+    const int i2 = mirror - i, j2 = mirror - j;
+    const bool hasi = i2 < N && i2 != i, hasj = j2 < N && j2 != j;
+    int64_t off[4];
+    off[0] = (int64_t)i * N + j;
+    off[1] = hasj ? (int64_t)i * N + j2 : -1;
+    off[2] = hasi ? (int64_t)i2 * N + j : -1;
+    off[3] = hasi && hasj ? (int64_t)i2 * N + j2 : -1;
     // theta * coordinates2(N): l along columns (x), m along rows (y)
-    const double cj = pow2 ? __dmul_rn((double)(j - N / 2), invN)
-                           : __ddiv_rn((double)(j - N / 2), (double)N);
-    const double ci = pow2 ? __dmul_rn((double)(i - N / 2), invN)
-                           : __ddiv_rn((double)(i - N / 2), (double)N);
+    const double cj = pow2 ? __dmul_rn((double)(j - half), invN)
+                           : __ddiv_rn((double)(j - half), (double)N);
+    const double ci = pow2 ? __dmul_rn((double)(i - half), invN)
+                           : __ddiv_rn((double)(i - half), (double)N);
     const double l = __dmul_rn(theta, cj);
     const double m = __dmul_rn(theta, ci);
     const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
     if (!(r2 < 1.0)) bad = 1;
     const double ph = 1.0 - sqrt(1.0 - r2);
     const float ph_h = (float)ph, ph_l = (float)(ph - (double)ph_h);
-    float ax = 0.f, ay = 0.f;
+    float ax[4] = {0.f, 0.f, 0.f, 0.f}, ay[4] = {0.f, 0.f, 0.f, 0.f};
     for (int p = 0; p < layers; ++p) {
       const float2 w = s_w[p];
       if (w.y != w.y) continue;  // empty plane
@@ -100,12 +115,19 @@ __global__ void k_wstack_combine(const float2 *__restrict__ planes, int layers, 
       const float f = (hi - rintf(hi)) + lo;
       float sn, cs;
       sincospif(2.0f * f, &sn, &cs);
-      const float2 g = planes[(int64_t)p * total + L];
-      // g / (cs + i sn) = g * (cs - i sn) for |e| = 1
-      ax += g.x * cs + g.y * sn;
-      ay += g.y * cs - g.x * sn;
+      const float2 *plane = planes + (int64_t)p * total;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (off[q] < 0) continue;
+        const float2 g = plane[off[q]];
+        // g / (cs + i sn) = g * (cs - i sn) for |e| = 1
+        ax[q] += g.x * cs + g.y * sn;
+        ay[q] += g.y * cs - g.x * sn;
+      }
     }
-    out[L] = make_float2(ax, ay);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (off[q] >= 0) out[off[q]] = make_float2(ax[q], ay[q]);
   }
   if (bad && status) atomicAdd(&status[ST_RANGE], 1);
 }
@@ -144,8 +166,8 @@ int cg_wstack_combine(const void *planes_c64, int layers, int N, double theta,
                       int32_t *d_status, cg_stream_t stream) {
   CG_REQUIRE(planes_c64 && mean_w && counts && image_c64 && layers >= 1 && N >= 1,
              "bad w-stacking arguments");
-  const int64_t total = (int64_t)N * N;
-  int64_t blocks = (total + 255) / 256;
+  const int64_t reps = (int64_t)(N / 2 + 1) * (N / 2 + 1);  // mirror-symmetric pixel sets
+  int64_t blocks = (reps + 255) / 256;
   const int64_t cap = (int64_t)num_sms() * 8;
   if (blocks > cap) blocks = cap;
   CG_REQUIRE(layers <= 4096, "at most 4096 w-planes");

@@ -1,7 +1,7 @@
-"""The radix-4 decimation-in-time line transform of the FP32 FFTs
+"""The register-blocked Stockham line transform of the FP32 FFTs
 (crocodile_gb300/csrc/fft32.h, plain C++ compiled for the host) against a
-direct DFT in double precision for N = 2 .. 8192 and both signs
-(tests/fft32_check.cpp)."""
+direct DFT in double precision for N = 64 .. 8192 and both signs, and its
+per-stage twiddle tables against the exact values (tests/fft32_check.cpp)."""
 
 import os
 import shutil

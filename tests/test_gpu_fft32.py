@@ -32,7 +32,7 @@ def _rand(rng, shape):
 
 
 @pytest.mark.parametrize("H,W", [(64, 64), (128, 512), (1024, 1024), (2048, 256), (4096, 4096),
-                                 (8192, 8192), (1, 4096), (1, 64)])
+                                 (8192, 8192), (4096, 256), (8192, 64), (1, 4096), (1, 64)])
 def test_centred_fft32_matches_numpy(env, H, W):
     torch, E, S, O = env
     rng = numpy.random.default_rng(H + W)
@@ -43,10 +43,11 @@ def test_centred_fft32_matches_numpy(env, H, W):
         assert rel(t.cpu().numpy(), ref) < 2e-6, (H, W, inverse)
 
 
-@pytest.mark.parametrize("shape", [(3, 256, 512), (2, 4096, 4096)])
+@pytest.mark.parametrize("shape", [(3, 256, 512), (3, 4096, 512), (9, 4096, 4096)])
 def test_batched_and_raw_fft32(env, shape):
-    """Column tiles (256 x 512) and, for square planes of 4096 and up, rows
-    between two in-place transposes."""
+    """Column tiles (256 x 512) and, for columns of 4096 and up, the four-step
+    column passes (9 planes of 4096^2 go through the 1 GiB scratch stack in
+    two chunks)."""
     torch, E, S, O = env
     rng = numpy.random.default_rng(3)
     a = _rand(rng, shape)
@@ -62,7 +63,7 @@ def test_batched_and_raw_fft32(env, shape):
         assert rel(t.cpu().numpy(), ref) < 2e-6
 
 
-@pytest.mark.parametrize("N", [256, 4096])
+@pytest.mark.parametrize("N", [256, 4096, 8192])
 def test_image_from_grid_fft32(env, N):
     torch, E, S, O = env
     rng = numpy.random.default_rng(N)
