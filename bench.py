@@ -672,10 +672,13 @@ def run_ours(args):
     s_in, s_outs = torch.cuda.Stream(), torch.cuda.Stream()
     k_steps = min(args.steps, 20)
 
+    kernel_spans = []
+
     def pipeline(k):
         in_ready = [ev(), ev()]
         done = [None, None]
         copied = [None, None]
+        kernel_spans.clear()
         t0, t1 = ev(), ev()
         t0.record(s_in)
         for i in range(k):
@@ -690,9 +693,12 @@ def run_ours(args):
             stream.wait_event(in_ready[b])
             if copied[b] is not None:
                 stream.wait_event(copied[b])  # step i - 2's results are out
+            k0 = ev()
+            k0.record(stream)
             G.step(d_uvw[b], d_vis[b], grid=d_grid[b], out=d_out[b])
             done[b] = ev()
             done[b].record(stream)
+            kernel_spans.append((k0, done[b]))
             s_outs.wait_event(done[b])
             with torch.cuda.stream(s_outs):
                 h_grid[b].copy_(d_grid[b], non_blocking=True)
@@ -705,6 +711,8 @@ def run_ours(args):
 
     pipeline(2)  # warm-up
     ms_e2e = pipeline(k_steps)
+    # each step's kernels as they ran inside the pipeline (copies alongside)
+    ms_kernels_in_pipeline = statistics.mean(a.elapsed_time(b) for a, b in kernel_spans)
 
     def copies_alone():
         # one step's copy-in and copy-out, each alone on its stream (no kernels)
@@ -730,6 +738,7 @@ def run_ours(args):
     e2e = {"value": world * n / (ms_e2e * 1e-3) / 1e6, "unit": "Mvis/s",
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
            "ms_per_step": ms_e2e,
+           "kernels_ms_in_pipeline": ms_kernels_in_pipeline,
            "copy_in_alone_ms": ms_in, "copy_in_gb_s": h2d / ms_in / 1e6,
            "copy_out_alone_ms": ms_out, "copy_out_gb_s": d2h / ms_out / 1e6,
            "form": "pipelined over %d steps: copy-in, kernels and copy-out on three streams, "
@@ -767,19 +776,31 @@ def run_ours(args):
 
     # ---- kernel generation again in the running process (libraries loaded,
     # FFT plans cached): what a new data set's kernel table costs after the first
+    def allocator_counts():
+        m = torch.cuda.memory_stats(G.dev)
+        return {k: int(m.get(k, 0)) for k in ("num_device_alloc", "num_device_free",
+                                               "num_alloc_retries")}
+
+    def allocator_delta(a, b):
+        return {k: b[k] - a[k] for k in a}
+
     torch.cuda.synchronize()
+    c0 = allocator_counts()
     t0 = time.perf_counter()
     G._prepare()
     torch.cuda.synchronize()
     kgen_warm_ms = 1e3 * (time.perf_counter() - t0)
+    kgen_warm_alloc = allocator_delta(c0, allocator_counts())
     # the same again with the caching allocator holding the blocks of the last
     # table (no fresh device allocation), and a bare allocation of the table's
     # size after the cache is released: what separates the two warm figures
     torch.cuda.synchronize()
+    c0 = allocator_counts()
     t0 = time.perf_counter()
     G._prepare()
     torch.cuda.synchronize()
     kgen_cached_ms = 1e3 * (time.perf_counter() - t0)
+    kgen_cached_alloc = allocator_delta(c0, allocator_counts())
     tbytes = G.kt.table.numel() * 8
     torch.cuda.empty_cache()
     torch.cuda.synchronize()
@@ -931,6 +952,8 @@ def run_ours(args):
                       "kernel_generation_once": G.kgen_ms,
                       "kernel_generation_warm": kgen_warm_ms,
                       "kernel_generation_warm_cached_blocks": kgen_cached_ms,
+                      "kernel_generation_warm_allocator": kgen_warm_alloc,
+                      "kernel_generation_warm_cached_blocks_allocator": kgen_cached_alloc,
                       "fresh_allocation_of_table_size": alloc_ms,
                       "kernel_generation_fp64": getattr(G, "kgen64_ms", None)},
         "plain_fp64": {"value": plain_value, "unit": "Mvis/s", "ms_per_step": ms_plain,

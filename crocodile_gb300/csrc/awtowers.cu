@@ -58,22 +58,20 @@ __global__ void k_awt_bounds(const double *__restrict__ uvw, int64_t stride, int
                              const int32_t *__restrict__ a2, int nant, int32_t *mm,
                              int32_t *status) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int64_t ub, vb, wp;
-  if (!awt_bins(uvw + i * stride, theta, C, wstep, ub, vb, wp)) {
-    atomicAdd(&status[ST_RANGE], 1);
-    return;
+  int64_t ub = 0, vb = 0, wp = 0;
+  bool ok = false;
+  if (i < n) {
+    if (!awt_bins(uvw + i * stride, theta, C, wstep, ub, vb, wp))
+      atomicAdd(&status[ST_RANGE], 1);
+    else if ((unsigned)a1[i] >= (unsigned)nant || (unsigned)a2[i] >= (unsigned)nant)
+      atomicAdd(&status[ST_INDEX], 1);
+    else
+      ok = true;
   }
-  if ((unsigned)a1[i] >= (unsigned)nant || (unsigned)a2[i] >= (unsigned)nant) {
-    atomicAdd(&status[ST_INDEX], 1);
-    return;
-  }
-  atomicMin(&mm[0], (int)ub);
-  atomicMax(&mm[1], (int)ub);
-  atomicMin(&mm[2], (int)vb);
-  atomicMax(&mm[3], (int)vb);
-  atomicMin(&mm[4], (int)wp);
-  atomicMax(&mm[5], (int)wp);
+  // whole warps: blocks of 256
+  warp_atomic_min_max(&mm[0], &mm[1], ok ? (int)ub : INT32_MAX, ok ? (int)ub : INT32_MIN);
+  warp_atomic_min_max(&mm[2], &mm[3], ok ? (int)vb : INT32_MAX, ok ? (int)vb : INT32_MIN);
+  warp_atomic_min_max(&mm[4], &mm[5], ok ? (int)wp : INT32_MAX, ok ? (int)wp : INT32_MIN);
 }
 
 // key = (((vb - vbmin) nub + (ub - ubmin)) nwp + (wp - wpmin)) nant^2 + a1 nant + a2;
@@ -127,8 +125,8 @@ __global__ void k_awtowers_combine(const float2 *__restrict__ stack, int s, doub
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cells;
        k += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(k / s), j = (int)(k - (int64_t)i * s);
-    const double l = __dmul_rn(theta, __ddiv_rn((double)(j - half), (double)s));
-    const double m = __dmul_rn(theta, __ddiv_rn((double)(i - half), (double)s));
+    const double l = __dmul_rn(theta, centred_coord(j, half, s));
+    const double m = __dmul_rn(theta, centred_coord(i, half, s));
     const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
     if (!(r2 < 1.0)) bad = 1;
     const double ph = 1.0 - sqrt(1.0 - r2);
@@ -235,8 +233,8 @@ __global__ void k_awt_pixels(int s, double theta, const float *__restrict__ corr
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= s * s) return;
   const int i = k / s, j = k - (k / s) * s, half = s / 2;
-  const double l = __dmul_rn(theta, __ddiv_rn((double)(j - half), (double)s));
-  const double m = __dmul_rn(theta, __ddiv_rn((double)(i - half), (double)s));
+  const double l = __dmul_rn(theta, centred_coord(j, half, s));
+  const double m = __dmul_rn(theta, centred_coord(i, half, s));
   const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
   if (!(r2 < 1.0) && status) atomicAdd(&status[ST_RANGE], 1);
   const double ph = 1.0 - sqrt(1.0 - r2);

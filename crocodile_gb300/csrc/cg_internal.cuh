@@ -157,6 +157,29 @@ __device__ __forceinline__ double w_bin_fast(double w, double wstep, double inv_
   return rint(__ddiv_rn(w, wstep));
 }
 
+// (k - half) / S, the centred image coordinate of pixel k (coordinates2 of
+// synthesis.py): for power-of-two S a multiplication by the exact reciprocal
+// (the quotient is exact, so the bits are the division's) instead of an FP64
+// division per pixel.
+__device__ __forceinline__ double centred_coord(int k, int half, int S) {
+  return (S & (S - 1)) == 0 ? __dmul_rn((double)(k - half), 1.0 / (double)S)
+                            : __ddiv_rn((double)(k - half), (double)S);
+}
+
+// Running minimum and maximum of v over a grid in mn / mx: reduced over the
+// warp first, then one atomic each per warp (a pair per visibility on two
+// addresses serialises in L2).  Every lane of the warp must call it; a lane
+// without a value passes INT32_MAX and INT32_MIN.
+__device__ __forceinline__ void warp_atomic_min_max(int32_t *mn, int32_t *mx, int vmin,
+                                                    int vmax) {
+  vmin = __reduce_min_sync(0xffffffffu, vmin);
+  vmax = __reduce_max_sync(0xffffffffu, vmax);
+  if ((threadIdx.x & 31) == 0) {
+    if (vmin != INT32_MAX) atomicMin(mn, vmin);
+    if (vmax != INT32_MIN) atomicMax(mx, vmax);
+  }
+}
+
 inline AxisConst axis_const(int N, int Q, double lam) {
   AxisConst k;
   k.nq_over_lam = ((double)N * (double)Q) / lam;

@@ -309,18 +309,20 @@ __global__ void k_frac_coords(const double *uvw, int64_t stride, double lam,
 // half-to-even.  k = rint(w / wstep) is the bin number.
 __global__ void k_w_bins(const double *uvw, int64_t stride, int64_t n, double wstep,
                          double inv_wstep, int32_t *kidx, int32_t *minmax, int32_t *status) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double k = w_bin_fast(uvw[i * stride + 2], wstep, inv_wstep);
-  if (!(k > -1.0e9 && k < 1.0e9)) {
-    atomicAdd(&status[ST_RANGE], 1);
-    kidx[i] = 0;
-    return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int lo = INT32_MAX, hi = INT32_MIN;
+  if (i < n) {
+    const double k = w_bin_fast(uvw[i * stride + 2], wstep, inv_wstep);
+    if (!(k > -1.0e9 && k < 1.0e9)) {
+      atomicAdd(&status[ST_RANGE], 1);
+      kidx[i] = 0;
+    } else {
+      const int ki = (int)k;
+      kidx[i] = ki;
+      lo = hi = ki;
+    }
   }
-  const int ki = (int)k;
-  kidx[i] = ki;
-  atomicMin(&minmax[0], ki);
-  atomicMax(&minmax[1], ki);
+  warp_atomic_min_max(&minmax[0], &minmax[1], lo, hi);  // whole warps: blocks of 256
 }
 
 __global__ void k_w_bins_rebase(int32_t *kidx, int64_t n, const int32_t *minmax) {
@@ -355,16 +357,27 @@ __global__ void k_minmax_init(int32_t *mm) {
 // key space of the tower schemes (chunks x planes x antenna pairs) runs to
 // hundreds of millions of keys for a few hundred thousand visibilities, and
 // a bit per key keeps the passes over it 32 times smaller than a flag word.
+// Neighbouring visibilities mostly share a key (a baseline's run of times or
+// channels), so the lanes of a warp that set bits of one word merge them
+// first and one lane sets them: one atomic per distinct word per warp
+// instead of one per visibility on the same address.
 __global__ void k_key_bits(const int32_t *__restrict__ key, int64_t n, int nkeys,
                            uint32_t *__restrict__ bits, int32_t *status) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int k = key[i];
-  if (k < 0 || k >= nkeys) {
-    atomicAdd(&status[ST_INDEX], 1);
-    return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = i < n ? key[i] : -1;
+  const bool ok = k >= 0 && k < nkeys;
+  if (i < n && !ok) atomicAdd(&status[ST_INDEX], 1);
+  const int word = ok ? k >> 5 : -1;
+  const uint32_t bit = ok ? 1u << (k & 31) : 0u;
+  const uint32_t same = __match_any_sync(0xffffffffu, word);
+  uint32_t acc = 0;
+#pragma unroll
+  for (int l = 0; l < 32; ++l) {
+    const uint32_t b = __shfl_sync(0xffffffffu, bit, l);
+    if (same & (1u << l)) acc |= b;
   }
-  atomicOr(&bits[k >> 5], 1u << (k & 31));
+  const int lane = threadIdx.x & 31;
+  if (ok && lane == __ffs(same) - 1) atomicOr(&bits[word], acc);
 }
 
 __global__ void k_key_popc(const uint32_t *__restrict__ bits, int nw, int32_t *__restrict__ cnt) {

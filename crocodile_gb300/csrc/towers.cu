@@ -50,28 +50,32 @@ __device__ __forceinline__ double floor_div_fast(double t, double C, double invC
 __global__ void k_tower_bounds(const double *__restrict__ uvw, int64_t stride, int64_t n,
                                double theta, int C, double invC, double winc, double inv_winc,
                                int32_t *mm, double *__restrict__ rel, int32_t *status) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double *row = uvw + i * stride;
-  const double fu = floor_div_fast(__dmul_rn(row[0], theta), (double)C, invC);
-  const double fv = floor_div_fast(__dmul_rn(row[1], theta), (double)C, invC);
-  const double fw = w_bin_fast(row[2], winc, inv_winc);
-  int32_t *bins = (int32_t *)(rel + 3 * i);
-  if (!(fabs(fu) < 1e9 && fabs(fv) < 1e9 && fabs(fw) < 1e9)) {  // NaN too
-    atomicAdd(&status[ST_RANGE], 1);
-    bins[0] = bins[1] = bins[2] = INT32_MIN;
-    return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int ub = INT32_MAX, vb = INT32_MAX, wp = INT32_MAX;  // no value: out of range
+  bool ok = false;
+  if (i < n) {
+    const double *row = uvw + i * stride;
+    const double fu = floor_div_fast(__dmul_rn(row[0], theta), (double)C, invC);
+    const double fv = floor_div_fast(__dmul_rn(row[1], theta), (double)C, invC);
+    const double fw = w_bin_fast(row[2], winc, inv_winc);
+    int32_t *bins = (int32_t *)(rel + 3 * i);
+    if (!(fabs(fu) < 1e9 && fabs(fv) < 1e9 && fabs(fw) < 1e9)) {  // NaN too
+      atomicAdd(&status[ST_RANGE], 1);
+      bins[0] = bins[1] = bins[2] = INT32_MIN;
+    } else {
+      ub = (int)fu;
+      vb = (int)fv;
+      wp = (int)fw;
+      bins[0] = ub;
+      bins[1] = vb;
+      bins[2] = wp;
+      ok = true;
+    }
   }
-  const int ub = (int)fu, vb = (int)fv, wp = (int)fw;
-  bins[0] = ub;
-  bins[1] = vb;
-  bins[2] = wp;
-  atomicMin(&mm[0], ub);
-  atomicMax(&mm[1], ub);
-  atomicMin(&mm[2], vb);
-  atomicMax(&mm[3], vb);
-  atomicMin(&mm[4], wp);
-  atomicMax(&mm[5], wp);
+  // whole warps: blocks of 256
+  warp_atomic_min_max(&mm[0], &mm[1], ub, ok ? ub : INT32_MIN);
+  warp_atomic_min_max(&mm[2], &mm[3], vb, ok ? vb : INT32_MIN);
+  warp_atomic_min_max(&mm[4], &mm[5], wp, ok ? wp : INT32_MIN);
 }
 
 __global__ void k_tower_mm_init(int32_t *mm) {
@@ -144,8 +148,8 @@ __global__ void k_towers_combine(const float2 *__restrict__ stack, int S, double
        k += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(k / S), j = (int)(k - (int64_t)i * S);
     // the cell's phase, once for every chunk of the block (FP64 is slow here)
-    const double l = __dmul_rn(theta, __ddiv_rn((double)(j - half), (double)S));
-    const double m = __dmul_rn(theta, __ddiv_rn((double)(i - half), (double)S));
+    const double l = __dmul_rn(theta, centred_coord(j, half, S));
+    const double m = __dmul_rn(theta, centred_coord(i, half, S));
     const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
     if (!(r2 < 1.0)) bad = 1;
     const double ph = 1.0 - sqrt(1.0 - r2);
@@ -250,8 +254,8 @@ __global__ void k_towers_expand(const float2 *__restrict__ images, int S, double
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cells;
        k += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(k / S), j = (int)(k - (int64_t)i * S);
-    const double l = __dmul_rn(theta, __ddiv_rn((double)(j - half), (double)S));
-    const double m = __dmul_rn(theta, __ddiv_rn((double)(i - half), (double)S));
+    const double l = __dmul_rn(theta, centred_coord(j, half, S));
+    const double m = __dmul_rn(theta, centred_coord(i, half, S));
     const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
     if (!(r2 < 1.0)) bad = 1;
     const double ph = 1.0 - sqrt(1.0 - r2);

@@ -81,10 +81,6 @@ __global__ void k_wstack_combine(const float2 *__restrict__ planes, int layers, 
   const int half = N / 2, M = half + 1, mirror = 2 * half;  // representatives 0 .. N/2
   const int64_t reps = (int64_t)M * M;
   int bad = 0;
-  // (k - N/2) / N: a multiplication by the exact reciprocal for power-of-two N
-  // (the same bits as the division, without an FP64 division per pixel)
-  const bool pow2 = (N & (N - 1)) == 0;
-  const double invN = 1.0 / (double)N;
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < reps;
        L += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(L / M), j = (int)(L - (int64_t)i * M);
@@ -96,12 +92,8 @@ __global__ void k_wstack_combine(const float2 *__restrict__ planes, int layers, 
     off[2] = hasi ? (int64_t)i2 * N + j : -1;
     off[3] = hasi && hasj ? (int64_t)i2 * N + j2 : -1;
     // theta * coordinates2(N): l along columns (x), m along rows (y)
-    const double cj = pow2 ? __dmul_rn((double)(j - half), invN)
-                           : __ddiv_rn((double)(j - half), (double)N);
-    const double ci = pow2 ? __dmul_rn((double)(i - half), invN)
-                           : __ddiv_rn((double)(i - half), (double)N);
-    const double l = __dmul_rn(theta, cj);
-    const double m = __dmul_rn(theta, ci);
+    const double l = __dmul_rn(theta, centred_coord(j, half, N));
+    const double m = __dmul_rn(theta, centred_coord(i, half, N));
     const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
     if (!(r2 < 1.0)) bad = 1;
     const double ph = 1.0 - sqrt(1.0 - r2);
