@@ -57,21 +57,30 @@ __global__ void k_awt_bounds(const double *__restrict__ uvw, int64_t stride, int
                              double theta, int C, double wstep, const int32_t *__restrict__ a1,
                              const int32_t *__restrict__ a2, int nant, int32_t *mm,
                              int32_t *status) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int64_t ub = 0, vb = 0, wp = 0;
-  bool ok = false;
-  if (i < n) {
-    if (!awt_bins(uvw + i * stride, theta, C, wstep, ub, vb, wp))
-      atomicAdd(&status[ST_RANGE], 1);
-    else if ((unsigned)a1[i] >= (unsigned)nant || (unsigned)a2[i] >= (unsigned)nant)
-      atomicAdd(&status[ST_INDEX], 1);
-    else
-      ok = true;
+  int mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+  int bad_range = 0, bad_index = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t ub, vb, wp;
+    if (!awt_bins(uvw + i * stride, theta, C, wstep, ub, vb, wp)) {
+      ++bad_range;
+      continue;
+    }
+    if ((unsigned)a1[i] >= (unsigned)nant || (unsigned)a2[i] >= (unsigned)nant) {
+      ++bad_index;
+      continue;
+    }
+    const int b[3] = {(int)ub, (int)vb, (int)wp};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      mn[d] = min(mn[d], b[d]);
+      mx[d] = max(mx[d], b[d]);
+    }
   }
-  // whole warps: blocks of 256
-  warp_atomic_min_max(&mm[0], &mm[1], ok ? (int)ub : INT32_MAX, ok ? (int)ub : INT32_MIN);
-  warp_atomic_min_max(&mm[2], &mm[3], ok ? (int)vb : INT32_MAX, ok ? (int)vb : INT32_MIN);
-  warp_atomic_min_max(&mm[4], &mm[5], ok ? (int)wp : INT32_MAX, ok ? (int)wp : INT32_MIN);
+  if (bad_range) atomicAdd(&status[ST_RANGE], bad_range);
+  if (bad_index) atomicAdd(&status[ST_INDEX], bad_index);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) block_atomic_min_max(&mm[2 * d], &mm[2 * d + 1], mn[d], mx[d]);
 }
 
 // key = (((vb - vbmin) nub + (ub - ubmin)) nwp + (wp - wpmin)) nant^2 + a1 nant + a2;
@@ -392,8 +401,8 @@ int cg_awtower_keys(const double *uvw, int64_t stride, int64_t n, double theta, 
   cudaStream_t s = (cudaStream_t)stream;
   const unsigned blocks = (unsigned)((n + 255) / 256);
   k_awt_mm_init<<<1, 32, 0, s>>>(d_minmax);
-  k_awt_bounds<<<blocks, 256, 0, s>>>(uvw, stride, n, theta, chunk, wstep, a1, a2, nant,
-                                      d_minmax, d_status);
+  k_awt_bounds<<<stride_blocks(n, 256), 256, 0, s>>>(uvw, stride, n, theta, chunk, wstep, a1,
+                                                    a2, nant, d_minmax, d_status);
   CG_LAUNCH("AW-tower bounds");
   CG_CUDA(cudaMemcpyAsync(h_bounds, d_minmax, 6 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   CG_CUDA(cudaStreamSynchronize(s));

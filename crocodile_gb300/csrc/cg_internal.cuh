@@ -166,18 +166,41 @@ __device__ __forceinline__ double centred_coord(int k, int half, int S) {
                             : __ddiv_rn((double)(k - half), (double)S);
 }
 
-// Running minimum and maximum of v over a grid in mn / mx: reduced over the
-// warp first, then one atomic each per warp (a pair per visibility on two
-// addresses serialises in L2).  Every lane of the warp must call it; a lane
-// without a value passes INT32_MAX and INT32_MIN.
-__device__ __forceinline__ void warp_atomic_min_max(int32_t *mn, int32_t *mx, int vmin,
-                                                    int vmax) {
+// Running minimum and maximum over a grid in mn / mx: the block reduces its
+// threads' values (warp reductions, then one warp over the warps' results)
+// and one thread applies them, so each address takes one atomic per block
+// (atomics of every warp on one address serialise in L2: about 4 ns each).
+// Every thread of the block must call it (blockDim.x a multiple of 32); a
+// thread without a value passes INT32_MAX and INT32_MIN.
+__device__ __forceinline__ void block_atomic_min_max(int32_t *mn, int32_t *mx, int vmin,
+                                                     int vmax) {
+  __shared__ int s_mm[2][32];
   vmin = __reduce_min_sync(0xffffffffu, vmin);
   vmax = __reduce_max_sync(0xffffffffu, vmax);
+  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    if (vmin != INT32_MAX) atomicMin(mn, vmin);
-    if (vmax != INT32_MIN) atomicMax(mx, vmax);
+    s_mm[0][warp] = vmin;
+    s_mm[1][warp] = vmax;
   }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int a = threadIdx.x < nwarps ? s_mm[0][threadIdx.x] : INT32_MAX;
+    int b = threadIdx.x < nwarps ? s_mm[1][threadIdx.x] : INT32_MIN;
+    a = __reduce_min_sync(0xffffffffu, a);
+    b = __reduce_max_sync(0xffffffffu, b);
+    if (threadIdx.x == 0) {
+      if (a != INT32_MAX) atomicMin(mn, a);
+      if (b != INT32_MIN) atomicMax(mx, b);
+    }
+  }
+  __syncthreads();  // s_mm free for the next call
+}
+
+// blocks for a grid-stride pass over n items: enough to fill the GPU, few
+// enough that per-block atomics stay cheap
+inline unsigned stride_blocks(int64_t n, int threads) {
+  const int64_t need = (n + threads - 1) / threads, cap = (int64_t)num_sms() * 8;
+  return (unsigned)(need < cap ? (need > 0 ? need : 1) : cap);
 }
 
 inline AxisConst axis_const(int N, int Q, double lam) {

@@ -309,20 +309,22 @@ __global__ void k_frac_coords(const double *uvw, int64_t stride, double lam,
 // half-to-even.  k = rint(w / wstep) is the bin number.
 __global__ void k_w_bins(const double *uvw, int64_t stride, int64_t n, double wstep,
                          double inv_wstep, int32_t *kidx, int32_t *minmax, int32_t *status) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int lo = INT32_MAX, hi = INT32_MIN;
-  if (i < n) {
+  int lo = INT32_MAX, hi = INT32_MIN, bad = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
     const double k = w_bin_fast(uvw[i * stride + 2], wstep, inv_wstep);
     if (!(k > -1.0e9 && k < 1.0e9)) {
-      atomicAdd(&status[ST_RANGE], 1);
+      ++bad;
       kidx[i] = 0;
     } else {
       const int ki = (int)k;
       kidx[i] = ki;
-      lo = hi = ki;
+      lo = min(lo, ki);
+      hi = max(hi, ki);
     }
   }
-  warp_atomic_min_max(&minmax[0], &minmax[1], lo, hi);  // whole warps: blocks of 256
+  if (bad) atomicAdd(&status[ST_RANGE], bad);
+  block_atomic_min_max(&minmax[0], &minmax[1], lo, hi);
 }
 
 __global__ void k_w_bins_rebase(int32_t *kidx, int64_t n, const int32_t *minmax) {
@@ -357,27 +359,53 @@ __global__ void k_minmax_init(int32_t *mm) {
 // key space of the tower schemes (chunks x planes x antenna pairs) runs to
 // hundreds of millions of keys for a few hundred thousand visibilities, and
 // a bit per key keeps the passes over it 32 times smaller than a flag word.
-// Neighbouring visibilities mostly share a key (a baseline's run of times or
-// channels), so the lanes of a warp that set bits of one word merge them
-// first and one lane sets them: one atomic per distinct word per warp
-// instead of one per visibility on the same address.
+// Bits of the keys in use.  Small key spaces (at most KEY_SMEM_WORDS words:
+// the w-towers' chunk x plane keys) collect in a shared-memory copy of the
+// bitmap that each block ORs into the global one at the end, one atomic per
+// non-zero word per block: the keys of a few thousand words take atomics
+// from every warp of the grid otherwise, and atomics on one address
+// serialise.  Larger key spaces set their bits directly, the lanes of a warp
+// that set bits of one word merging them first.
+constexpr int KEY_SMEM_WORDS = 8192;
+
 __global__ void k_key_bits(const int32_t *__restrict__ key, int64_t n, int nkeys,
                            uint32_t *__restrict__ bits, int32_t *status) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int k = i < n ? key[i] : -1;
-  const bool ok = k >= 0 && k < nkeys;
-  if (i < n && !ok) atomicAdd(&status[ST_INDEX], 1);
-  const int word = ok ? k >> 5 : -1;
-  const uint32_t bit = ok ? 1u << (k & 31) : 0u;
-  const uint32_t same = __match_any_sync(0xffffffffu, word);
-  uint32_t acc = 0;
-#pragma unroll
-  for (int l = 0; l < 32; ++l) {
-    const uint32_t b = __shfl_sync(0xffffffffu, bit, l);
-    if (same & (1u << l)) acc |= b;
+  extern __shared__ uint32_t s_bits[];
+  const int nw = (nkeys + 31) >> 5;
+  const bool local = nw <= KEY_SMEM_WORDS;
+  if (local) {
+    for (int w = threadIdx.x; w < nw; w += blockDim.x) s_bits[w] = 0u;
+    __syncthreads();
   }
-  const int lane = threadIdx.x & 31;
-  if (ok && lane == __ffs(same) - 1) atomicOr(&bits[word], acc);
+  int bad = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // whole warps walk the range together (the merge below needs all 32 lanes)
+  const int64_t nround = (n + 31) & ~(int64_t)31;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nround; i += stride) {
+    const int k = i < n ? key[i] : -1;
+    const bool ok = k >= 0 && k < nkeys;
+    if (i < n && !ok) ++bad;
+    if (local) {
+      if (ok) atomicOr(&s_bits[k >> 5], 1u << (k & 31));
+      continue;
+    }
+    const int word = ok ? k >> 5 : -1;
+    const uint32_t bit = ok ? 1u << (k & 31) : 0u;
+    const uint32_t same = __match_any_sync(0xffffffffu, word);
+    uint32_t acc = 0;
+#pragma unroll
+    for (int l = 0; l < 32; ++l) {
+      const uint32_t b = __shfl_sync(0xffffffffu, bit, l);
+      if (same & (1u << l)) acc |= b;
+    }
+    if (ok && (threadIdx.x & 31) == __ffs(same) - 1) atomicOr(&bits[word], acc);
+  }
+  if (bad) atomicAdd(&status[ST_INDEX], bad);
+  if (local) {
+    __syncthreads();
+    for (int w = threadIdx.x; w < nw; w += blockDim.x)
+      if (s_bits[w]) atomicOr(&bits[w], s_bits[w]);
+  }
 }
 
 __global__ void k_key_popc(const uint32_t *__restrict__ bits, int nw, int32_t *__restrict__ cnt) {
@@ -863,7 +891,8 @@ int cg_w_bins(const double *uvw, int64_t stride, int64_t n, double wstep, int32_
   cudaStream_t s = (cudaStream_t)stream;
   const unsigned blocks = (unsigned)((n + 255) / 256);
   k_minmax_init<<<1, 1, 0, s>>>(d_minmax);
-  k_w_bins<<<blocks, 256, 0, s>>>(uvw, stride, n, wstep, 1.0 / wstep, kidx, d_minmax, d_status);
+  k_w_bins<<<stride_blocks(n, 256), 256, 0, s>>>(uvw, stride, n, wstep, 1.0 / wstep, kidx,
+                                                 d_minmax, d_status);
   k_w_bins_rebase<<<blocks, 256, 0, s>>>(kidx, n, d_minmax);
   CG_LAUNCH("w_bins");
   CG_CUDA(cudaMemcpyAsync(h_minmax, d_minmax, 8, cudaMemcpyDeviceToHost, s));
@@ -902,7 +931,9 @@ int cg_compact_keys(const int32_t *key, int64_t n, int nkeys, int32_t *row, int3
   int32_t *cnt = (int32_t *)(bits + nw), *wpre = cnt + nw, *scratch = wpre + nw;
   CG_CUDA(cudaMemsetAsync(bits, 0, (size_t)nw * 4, s));
   const unsigned blocks = (unsigned)((n + 255) / 256);
-  if (n > 0) k_key_bits<<<blocks, 256, 0, s>>>(key, n, nkeys, bits, d_status);
+  if (n > 0)
+    k_key_bits<<<stride_blocks(n, 256), 256, nw <= KEY_SMEM_WORDS ? (size_t)nw * 4 : 0, s>>>(
+        key, n, nkeys, bits, d_status);
   k_key_popc<<<(nw + 255) / 256, 256, 0, s>>>(bits, nw, cnt);
   CG_LAUNCH("key bits");
   int rc = launch_scan(cnt, wpre, nw, scratch, s);

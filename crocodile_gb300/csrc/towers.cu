@@ -50,32 +50,31 @@ __device__ __forceinline__ double floor_div_fast(double t, double C, double invC
 __global__ void k_tower_bounds(const double *__restrict__ uvw, int64_t stride, int64_t n,
                                double theta, int C, double invC, double winc, double inv_winc,
                                int32_t *mm, double *__restrict__ rel, int32_t *status) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int ub = INT32_MAX, vb = INT32_MAX, wp = INT32_MAX;  // no value: out of range
-  bool ok = false;
-  if (i < n) {
+  int mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+  int bad = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
     const double *row = uvw + i * stride;
     const double fu = floor_div_fast(__dmul_rn(row[0], theta), (double)C, invC);
     const double fv = floor_div_fast(__dmul_rn(row[1], theta), (double)C, invC);
     const double fw = w_bin_fast(row[2], winc, inv_winc);
     int32_t *bins = (int32_t *)(rel + 3 * i);
     if (!(fabs(fu) < 1e9 && fabs(fv) < 1e9 && fabs(fw) < 1e9)) {  // NaN too
-      atomicAdd(&status[ST_RANGE], 1);
+      ++bad;
       bins[0] = bins[1] = bins[2] = INT32_MIN;
-    } else {
-      ub = (int)fu;
-      vb = (int)fv;
-      wp = (int)fw;
-      bins[0] = ub;
-      bins[1] = vb;
-      bins[2] = wp;
-      ok = true;
+      continue;
+    }
+    const int b[3] = {(int)fu, (int)fv, (int)fw};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      bins[d] = b[d];
+      mn[d] = min(mn[d], b[d]);
+      mx[d] = max(mx[d], b[d]);
     }
   }
-  // whole warps: blocks of 256
-  warp_atomic_min_max(&mm[0], &mm[1], ub, ok ? ub : INT32_MIN);
-  warp_atomic_min_max(&mm[2], &mm[3], vb, ok ? vb : INT32_MIN);
-  warp_atomic_min_max(&mm[4], &mm[5], wp, ok ? wp : INT32_MIN);
+  if (bad) atomicAdd(&status[ST_RANGE], bad);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) block_atomic_min_max(&mm[2 * d], &mm[2 * d + 1], mn[d], mx[d]);
 }
 
 __global__ void k_tower_mm_init(int32_t *mm) {
@@ -128,6 +127,27 @@ __device__ __forceinline__ float2 split_w(double w) {
   return make_float2(hi, (float)(w - (double)hi));
 }
 
+// The four mirror cells (i, j), (S-i, j), (i, S-j), (S-i, S-j) have
+// coordinates of equal magnitude, hence the same ph, factors and sign: one
+// thread takes all four (those that exist), with one FP64 ph and one
+// sincospi per layer, and gives each the value it would get alone.
+struct MirrorCells {
+  int64_t kr[4];  // rolled index of each cell, -1 where the mirror does not exist
+  int i, j;       // the representative, 0 <= i, j <= S/2
+  __device__ MirrorCells(int64_t rep, int S) {
+    const int half = S / 2, M = half + 1;
+    i = (int)(rep / M);
+    j = (int)(rep - (int64_t)i * M);
+    const int i2 = S - i, j2 = S - j;
+    const bool hi = i2 < S && i2 != i, hj = j2 < S && j2 != j;
+    auto roll = [&](int x) { return x + half >= S ? x + half - S : x + half; };
+    kr[0] = (int64_t)roll(i) * S + roll(j);
+    kr[1] = hj ? (int64_t)roll(i) * S + roll(j2) : -1;
+    kr[2] = hi ? (int64_t)roll(i2) * S + roll(j) : -1;
+    kr[3] = hi && hj ? (int64_t)roll(i2) * S + roll(j2) : -1;
+  }
+};
+
 __global__ void k_towers_combine(const float2 *__restrict__ stack, int S, double theta,
                                  const double *__restrict__ layer_w,
                                  const int32_t *__restrict__ chunk_first, int nchunks,
@@ -142,46 +162,52 @@ __global__ void k_towers_combine(const float2 *__restrict__ stack, int S, double
   __syncthreads();
   const int64_t cells = (int64_t)S * S;
   const int half = S / 2;
+  const int64_t reps = (int64_t)(half + 1) * (half + 1);
   const float scale = 1.0f / (float)cells;
   int bad = 0;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cells;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < reps;
        k += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(k / S), j = (int)(k - (int64_t)i * S);
-    // the cell's phase, once for every chunk of the block (FP64 is slow here)
-    const double l = __dmul_rn(theta, centred_coord(j, half, S));
-    const double m = __dmul_rn(theta, centred_coord(i, half, S));
+    const MirrorCells mc(k, S);
+    // the cells' phase, once for every chunk of the block (FP64 is slow here)
+    const double l = __dmul_rn(theta, centred_coord(mc.j, half, S));
+    const double m = __dmul_rn(theta, centred_coord(mc.i, half, S));
     const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
     if (!(r2 < 1.0)) bad = 1;
     const double ph = 1.0 - sqrt(1.0 - r2);
     const float ph_h = (float)ph, ph_l = (float)(ph - (double)ph_h);
-    const int ir = i + half >= S ? i + half - S : i + half;
-    const int jr = j + half >= S ? j + half - S : j + half;
-    const int64_t kr = (int64_t)ir * S + jr;  // rolled index, read and write
-    const float sg = ((i + j) & 1) ? -scale : scale;
+    const float sg = ((mc.i + mc.j) & 1) ? -scale : scale;  // S even: mirrors alike
     for (int c = c0; c < c1; ++c) {
       const int L0 = chunk_first[c], L1 = chunk_first[c + 1];
-      float ax = 0.f, ay = 0.f;
-      for (int L = L0; L < L1; L += 4) {
-        float2 g[4], w2[4];
+      float ax[4] = {0.f, 0.f, 0.f, 0.f}, ay[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int L = L0; L < L1; L += 2) {
+        float2 g[2][4], w2[2];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {  // four layers' loads in flight
+        for (int q = 0; q < 2; ++q) {  // two layers' loads of four cells in flight
           const bool in = L + q < L1;
-          g[q] = in ? stack[(int64_t)(L + q) * cells + kr] : make_float2(0.f, 0.f);
+          const float2 *layer = stack + (int64_t)(L + q) * cells;
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            g[q][e] = in && mc.kr[e] >= 0 ? layer[mc.kr[e]] : make_float2(0.f, 0.f);
           w2[q] = !in ? make_float2(0.f, 0.f) : cached ? s_w[L + q - Lb0] : split_w(layer_w[L + q]);
         }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < 2; ++q) {
           const float wh = w2[q].x, wl = w2[q].y;
           const float hi = wh * ph_h;
           const float lo = fmaf(wh, ph_h, -hi) + fmaf(wh, ph_l, wl * ph_h);
           const float f = (hi - rintf(hi)) + lo;
           float sn, cs;
           sincospif(2.0f * f, &sn, &cs);
-          ax += g[q].x * cs + g[q].y * sn;
-          ay += g[q].y * cs - g[q].x * sn;
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            ax[e] += g[q][e].x * cs + g[q][e].y * sn;
+            ay[e] += g[q][e].y * cs - g[q][e].x * sn;
+          }
         }
       }
-      out[(int64_t)c * cells + kr] = make_float2(ax * sg, ay * sg);
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (mc.kr[e] >= 0) out[(int64_t)c * cells + mc.kr[e]] = make_float2(ax[e] * sg, ay[e] * sg);
     }
   }
   if (bad && status) atomicAdd(&status[ST_RANGE], 1);
@@ -249,25 +275,27 @@ __global__ void k_towers_expand(const float2 *__restrict__ images, int S, double
   __syncthreads();
   const int64_t cells = (int64_t)S * S;
   const int half = S / 2;
+  const int64_t reps = (int64_t)(half + 1) * (half + 1);
   const float scale = 1.0f / (float)cells;
   int bad = 0;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cells;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < reps;
        k += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(k / S), j = (int)(k - (int64_t)i * S);
-    const double l = __dmul_rn(theta, centred_coord(j, half, S));
-    const double m = __dmul_rn(theta, centred_coord(i, half, S));
+    const MirrorCells mc(k, S);
+    const double l = __dmul_rn(theta, centred_coord(mc.j, half, S));
+    const double m = __dmul_rn(theta, centred_coord(mc.i, half, S));
     const double r2 = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
     if (!(r2 < 1.0)) bad = 1;
     const double ph = 1.0 - sqrt(1.0 - r2);
     const float ph_h = (float)ph, ph_l = (float)(ph - (double)ph_h);
-    const int ir = i + half >= S ? i + half - S : i + half;
-    const int jr = j + half >= S ? j + half - S : j + half;
-    const int64_t kr = (int64_t)ir * S + jr;
-    const float sg = ((i + j) & 1) ? -scale : scale;
+    const float sg = ((mc.i + mc.j) & 1) ? -scale : scale;  // S even: mirrors alike
     for (int c = c0; c < c1; ++c) {
-      float2 a = images[(int64_t)c * cells + kr];
-      a.x *= sg;
-      a.y *= sg;
+      float2 a[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        a[e] = mc.kr[e] >= 0 ? images[(int64_t)c * cells + mc.kr[e]] : make_float2(0.f, 0.f);
+        a[e].x *= sg;
+        a[e].y *= sg;
+      }
       for (int L = chunk_first[c]; L < chunk_first[c + 1]; ++L) {
         const float2 w2 = cached ? s_w[L - Lb0] : split_w(layer_w[L]);
         const float hi = w2.x * ph_h;
@@ -275,8 +303,12 @@ __global__ void k_towers_expand(const float2 *__restrict__ images, int S, double
         const float f = (hi - rintf(hi)) + lo;
         float sn, cs;
         sincospif(2.0f * f, &sn, &cs);
+        float2 *layer = out + (int64_t)L * cells;
         // a / (cs + i sn) = a * (cs - i sn)
-        out[(int64_t)L * cells + kr] = make_float2(a.x * cs + a.y * sn, a.y * cs - a.x * sn);
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (mc.kr[e] >= 0)
+            layer[mc.kr[e]] = make_float2(a[e].x * cs + a[e].y * sn, a[e].y * cs - a[e].x * sn);
       }
     }
   }
@@ -299,7 +331,8 @@ int cg_tower_keys(const double *uvw, int64_t stride, int64_t n, double theta, in
   cudaStream_t s = (cudaStream_t)stream;
   const unsigned blocks = (unsigned)((n + 255) / 256);
   k_tower_mm_init<<<1, 32, 0, s>>>(d_minmax);
-  k_tower_bounds<<<blocks, 256, 0, s>>>(uvw, stride, n, theta, chunk, 1.0 / (double)chunk,
+  k_tower_bounds<<<stride_blocks(n, 256), 256, 0, s>>>(uvw, stride, n, theta, chunk,
+                                                      1.0 / (double)chunk,
                                         wincrement, 1.0 / wincrement, d_minmax, rel_out,
                                         d_status);
   CG_LAUNCH("tower bounds");
@@ -323,8 +356,8 @@ int cg_towers_combine(const void *stack_c64, int layers, int S, double theta,
   CG_REQUIRE(stack_c64 && layer_w && chunk_first && out_c64 && layers >= 1 && S >= 2 &&
                  S % 2 == 0 && nchunks >= 1,
              "bad w-towers combine arguments (even sub-grid size)");
-  const int64_t cells = (int64_t)S * S;
-  const unsigned bx = (unsigned)std::min<int64_t>((cells + 255) / 256, 1024);
+  const int64_t reps = (int64_t)(S / 2 + 1) * (S / 2 + 1);  // mirror-cell sets
+  const unsigned bx = (unsigned)std::min<int64_t>((reps + 255) / 256, 1024);
   const unsigned by = (unsigned)((nchunks + TOWER_CHUNKS_PER_BLOCK - 1) / TOWER_CHUNKS_PER_BLOCK);
   k_towers_combine<<<dim3(bx, by), 256, TOWER_SMEM_LAYERS * sizeof(float2),
                      (cudaStream_t)stream>>>(
@@ -366,8 +399,8 @@ int cg_towers_expand(const void *images_c64, int S, double theta, const double *
   CG_REQUIRE(images_c64 && layer_w && chunk_first && out_c64 && S >= 2 && S % 2 == 0 &&
                  nchunks >= 1,
              "bad w-towers expand arguments (even sub-grid size)");
-  const int64_t cells = (int64_t)S * S;
-  const unsigned bx = (unsigned)std::min<int64_t>((cells + 255) / 256, 1024);
+  const int64_t reps = (int64_t)(S / 2 + 1) * (S / 2 + 1);  // mirror-cell sets
+  const unsigned bx = (unsigned)std::min<int64_t>((reps + 255) / 256, 1024);
   const unsigned by = (unsigned)((nchunks + TOWER_CHUNKS_PER_BLOCK - 1) / TOWER_CHUNKS_PER_BLOCK);
   k_towers_expand<<<dim3(bx, by), 256, TOWER_SMEM_LAYERS * sizeof(float2),
                     (cudaStream_t)stream>>>((const float2 *)images_c64, S, theta, layer_w,

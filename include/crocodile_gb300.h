@@ -320,7 +320,10 @@ int cg_make_hermitian(void *grid, int H, int W, int is_c64,
 /* fft / ifft (synthesis.py:83-106): centred 2-D transform of `batch`
  * H x W arrays (H = 1: 1-D), in place; the inverse includes 1/(H*W).
  * Grids with H and W even need no workspace; otherwise workspace must hold
- * one array of the same size. */
+ * one array of the same size.  complex64 with power-of-two sides 64..8192
+ * run the library's own FP32 FFT; from H = 4096 its column passes go
+ * through a scratch stack of at most 1 GiB taken from a memory pool the
+ * library keeps per device (stream-ordered, retained after the first use). */
 int cg_fft(void *data, int batch, int H, int W, int is_c64, int inverse,
            void *workspace, cg_stream_t stream);
 /* The same transforms unshifted and unnormalised (cuFFT's own convention):
