@@ -85,11 +85,27 @@ __global__ void k_tower_mm_init(int32_t *mm) {
 // keys group a chunk's planes together, in increasing w) and the coordinates
 // relative to the chunk centre xmid / theta (IEEE quotient, as numpy) and the
 // plane wp * wincrement.
+constexpr int TOWER_MID_TABLE = 1024;  // chunk columns / rows whose centres a block tabulates
+
+__device__ __forceinline__ double tower_mid_over_theta(int b, int C, double theta) {
+  const int64_t mid = floor_div_ll((int64_t)C * b + (int64_t)C * (b + 1), 2);
+  return __ddiv_rn((double)mid, theta);
+}
+
 __global__ void k_tower_keys(const double *__restrict__ uvw, int64_t stride, int64_t n,
                              double theta, int C, double winc, int ubmin, int vbmin, int wpmin,
-                             int nub, int nwp, int32_t *__restrict__ key,
+                             int nub, int nvb, int nwp, int32_t *__restrict__ key,
                              double *__restrict__ rel) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // xmid / theta of every chunk column and row, once per block instead of two
+  // FP64 divisions per visibility (the same IEEE quotients)
+  __shared__ double s_mid[2][TOWER_MID_TABLE];
+  const bool tu = nub <= TOWER_MID_TABLE, tv = nvb <= TOWER_MID_TABLE;
+  for (int t = threadIdx.x; t < TOWER_MID_TABLE; t += blockDim.x) {
+    if (tu && t < nub) s_mid[0][t] = tower_mid_over_theta(ubmin + t, C, theta);
+    if (tv && t < nvb) s_mid[1][t] = tower_mid_over_theta(vbmin + t, C, theta);
+  }
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int32_t *bins = (const int32_t *)(rel + 3 * i);
   const int ub = bins[0], vb = bins[1], wp = bins[2];
@@ -99,10 +115,10 @@ __global__ void k_tower_keys(const double *__restrict__ uvw, int64_t stride, int
     rel[3 * i] = rel[3 * i + 1] = rel[3 * i + 2] = 0.0;
     return;
   }
-  const int64_t xmid = floor_div_ll((int64_t)C * ub + (int64_t)C * (ub + 1), 2);
-  const int64_t ymid = floor_div_ll((int64_t)C * vb + (int64_t)C * (vb + 1), 2);
-  const double ru = __dadd_rn(row[0], -__ddiv_rn((double)xmid, theta));
-  const double rv = __dadd_rn(row[1], -__ddiv_rn((double)ymid, theta));
+  const double mu = tu ? s_mid[0][ub - ubmin] : tower_mid_over_theta(ub, C, theta);
+  const double mv = tv ? s_mid[1][vb - vbmin] : tower_mid_over_theta(vb, C, theta);
+  const double ru = __dadd_rn(row[0], -mu);
+  const double rv = __dadd_rn(row[1], -mv);
   const double rw = __dadd_rn(row[2], -__dmul_rn((double)wp, winc));
   key[i] = (int32_t)(((vb - vbmin) * nub + (ub - ubmin)) * nwp + (wp - wpmin));
   rel[3 * i] = ru;
@@ -344,8 +360,8 @@ int cg_tower_keys(const double *uvw, int64_t stride, int64_t n, double theta, in
   const int64_t nwp = (int64_t)h_bounds[5] - h_bounds[4] + 1;
   CG_REQUIRE(nub * nvb * nwp < ((int64_t)1 << 31), "too many (chunk, plane) keys");
   k_tower_keys<<<blocks, 256, 0, s>>>(uvw, stride, n, theta, chunk, wincrement, h_bounds[0],
-                                      h_bounds[2], h_bounds[4], (int)nub, (int)nwp, key_out,
-                                      rel_out);
+                                      h_bounds[2], h_bounds[4], (int)nub, (int)nvb, (int)nwp,
+                                      key_out, rel_out);
   CG_LAUNCH("tower keys");
   return CG_OK;
 }

@@ -70,13 +70,24 @@ __global__ void k_wstack_combine(const float2 *__restrict__ planes, int layers, 
                                  double theta, const double *__restrict__ midw,
                                  const int32_t *__restrict__ counts, float2 *__restrict__ out,
                                  int32_t *status) {
-  extern __shared__ float2 s_w[];  // (hi, lo) of midw per layer; lo = NaN marks empty layers
-  for (int p = threadIdx.x; p < layers; p += blockDim.x) {
-    const double w = midw[p];
-    const float hi = (float)w;
-    s_w[p] = make_float2(hi, counts[p] ? (float)(w - (double)hi) : __int_as_float(0x7fc00000));
+  // (hi, lo) of midw for the layers with visibilities, in layer order, and
+  // their count
+  extern __shared__ float2 s_w[];
+  int *s_pl = (int *)(s_w + layers);  // their layer numbers
+  __shared__ int s_np;
+  if (threadIdx.x == 0) {
+    int np = 0;
+    for (int p = 0; p < layers; ++p)
+      if (counts[p]) {
+        const double w = midw[p];
+        const float hi = (float)w;
+        s_pl[np] = p;
+        s_w[np++] = make_float2(hi, (float)(w - (double)hi));
+      }
+    s_np = np;
   }
   __syncthreads();
+  const int np = s_np;
   const int64_t total = (int64_t)N * N;
   const int half = N / 2, M = half + 1, mirror = 2 * half;  // representatives 0 .. N/2
   const int64_t reps = (int64_t)M * M;
@@ -99,22 +110,32 @@ __global__ void k_wstack_combine(const float2 *__restrict__ planes, int layers, 
     const double ph = 1.0 - sqrt(1.0 - r2);
     const float ph_h = (float)ph, ph_l = (float)(ph - (double)ph_h);
     float ax[4] = {0.f, 0.f, 0.f, 0.f}, ay[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int p = 0; p < layers; ++p) {
-      const float2 w = s_w[p];
-      if (w.y != w.y) continue;  // empty plane
-      const float hi = w.x * ph_h;
-      const float lo = fmaf(w.x, ph_h, -hi) + fmaf(w.x, ph_l, w.y * ph_h);
-      const float f = (hi - rintf(hi)) + lo;
-      float sn, cs;
-      sincospif(2.0f * f, &sn, &cs);
-      const float2 *plane = planes + (int64_t)p * total;
+    // two planes per pass: eight loads in flight before the first use
+    for (int t = 0; t < np; t += 2) {
+      float2 g[2][4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        if (off[q] < 0) continue;
-        const float2 g = plane[off[q]];
-        // g / (cs + i sn) = g * (cs - i sn) for |e| = 1
-        ax[q] += g.x * cs + g.y * sn;
-        ay[q] += g.y * cs - g.x * sn;
+      for (int u = 0; u < 2; ++u) {
+        const bool in = t + u < np;
+        const float2 *plane = planes + (int64_t)(in ? s_pl[t + u] : 0) * total;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          g[u][q] = in && off[q] >= 0 ? plane[off[q]] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (t + u >= np) break;
+        const float2 w = s_w[t + u];
+        const float hi = w.x * ph_h;
+        const float lo = fmaf(w.x, ph_h, -hi) + fmaf(w.x, ph_l, w.y * ph_h);
+        const float f = (hi - rintf(hi)) + lo;
+        float sn, cs;
+        sincospif(2.0f * f, &sn, &cs);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          // g / (cs + i sn) = g * (cs - i sn) for |e| = 1
+          ax[q] += g[u][q].x * cs + g[u][q].y * sn;
+          ay[q] += g[u][q].y * cs - g[u][q].x * sn;
+        }
       }
     }
 #pragma unroll
@@ -163,7 +184,8 @@ int cg_wstack_combine(const void *planes_c64, int layers, int N, double theta,
   const int64_t cap = (int64_t)num_sms() * 8;
   if (blocks > cap) blocks = cap;
   CG_REQUIRE(layers <= 4096, "at most 4096 w-planes");
-  k_wstack_combine<<<(unsigned)blocks, 256, layers * sizeof(float2), (cudaStream_t)stream>>>(
+  k_wstack_combine<<<(unsigned)blocks, 256, layers * (sizeof(float2) + sizeof(int)),
+                     (cudaStream_t)stream>>>(
       (const float2 *)planes_c64, layers, N, theta, mean_w, counts, (float2 *)image_c64,
       d_status);
   CG_LAUNCH("w-stack combine");

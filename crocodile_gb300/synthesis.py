@@ -862,14 +862,18 @@ def do_predict(theta, lam, uvw, src, modelimage, predfn, **kwargs):
     return _host(_degrid_from(ktab, kidx, uvw_t, lam, ximage, prec), like=uvw)
 
 
-def w_stack_imaging(theta, lam, uvw, src, vis, kv, plane, precision=None, per_plane=False):
+def w_stack_imaging(theta, lam, uvw, src, vis, kv, plane, precision=None, per_plane=False,
+                    gridder="auto"):
     """w-stacking (examples/notebooks/wstacking.ipynb, code cell 10, with conv_imaging in
     place of the notebook's boxcar gridding): for each w-plane p holding visibilities,
     ifft(grid_p) / w_kernel_function(l, m, mean w of the plane), summed; returns the
     complex image (the notebook shows 2 Re of it).  ``plane`` is each visibility's plane
     index.  All planes grid in one launch into a stack of grids and transform in one
     batched FFT; ``per_plane=True`` grids and transforms one plane per launch instead
-    (the comparator).  FP32 only."""
+    (the comparator).  ``gridder``: "tiled" (cg_grid), "sparse" (cg_grid_sparse, per-tap
+    atomics) or "auto", sparse when the stack's tiles average fewer than 16 visibilities
+    (4M visibilities over 32 planes of 4096^2: 1.4 ms sparse against 2.4 ms tiled).
+    FP32 only."""
     if _prec(precision) != "fp32":
         raise ValueError("w_stack_imaging runs the FP32 tiled path only")
     N = _grid_size(theta, lam)
@@ -884,7 +888,13 @@ def w_stack_imaging(theta, lam, uvw, src, vis, kv, plane, precision=None, per_pl
     if not per_plane:
         plan = E.Plan(uvw_t, lam, (N, N), ktab, kidx, status=st,
                       layers=(layers, ptab.astype(numpy.int32)))
-        plan.grid(ktab, vis_t, planes)
+        tiles = layers * (-(-N // plan.info()["tile"])) ** 2
+        if gridder == "sparse" or (gridder == "auto" and n < 16 * tiles):
+            plan.grid_sparse(ktab, vis_t, planes)
+        elif gridder in ("auto", "tiled"):
+            plan.grid(ktab, vis_t, planes)
+        else:
+            raise ValueError("gridder must be 'auto', 'tiled' or 'sparse'")
         mean_w, counts = plan.layer_mean_w()
         E.fft_(planes, True)
     else:

@@ -39,6 +39,9 @@ def test_wstack_matches_oracle(env):
     ref = O.w_stack_imaging(theta, lam, uvw, None, w.vis, kv, plane)
     got = S.w_stack_imaging(theta, lam, uvw, None, w.vis, kv, plane)
     assert rel(got, ref) < 1e-5
+    for gridder in ("tiled", "sparse"):  # both gridders of the stack
+        got = S.w_stack_imaging(theta, lam, uvw, None, w.vis, kv, plane, gridder=gridder)
+        assert rel(got, ref) < 1e-5, gridder
     got1 = S.w_stack_imaging(theta, lam, uvw, None, w.vis, kv, plane, per_plane=True)
     assert rel(got1, ref) < 1e-5
 
