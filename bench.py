@@ -455,7 +455,8 @@ class AWGpu(GpuWorkload):
         from crocodile_gb300 import awproj
         w = self.w
         self.op = awproj.AWProjection(w.theta, w.lam, self.uvw, w.params["a1"], w.params["a2"],
-                                      w.params["beams"], w.params["wstep"], w.params["NpixFF"])
+                                      w.params["beams"], w.params["wstep"], w.params["NpixFF"],
+                                      phase_ms=getattr(self, "phase_ms", None))
         self.kt, self.rows = self.op.ktab, self.op.rows
         self._alloc_ws()
         self.groups_desc = "one launch per w-plane (%d)" % self.op.nbins
@@ -791,6 +792,13 @@ def run_ours(args):
     torch.cuda.synchronize()
     kgen_warm_ms = 1e3 * (time.perf_counter() - t0)
     kgen_warm_alloc = allocator_delta(c0, allocator_counts())
+    # once more with the device synchronised at each phase boundary: host time
+    # per phase (key binning and compaction with its readbacks, A-kernels,
+    # w-kernels, the AW table, the plan)
+    G.phase_ms = {}
+    G._prepare()
+    kgen_phases = {k: round(v, 3) for k, v in G.phase_ms.items()}
+    G.phase_ms = None
     # the same again with the caching allocator holding the blocks of the last
     # table (no fresh device allocation), and a bare allocation of the table's
     # size after the cache is released: what separates the two warm figures
@@ -954,6 +962,7 @@ def run_ours(args):
                       "kernel_generation_warm_cached_blocks": kgen_cached_ms,
                       "kernel_generation_warm_allocator": kgen_warm_alloc,
                       "kernel_generation_warm_cached_blocks_allocator": kgen_cached_alloc,
+                      "kernel_generation_warm_phases": kgen_phases,
                       "fresh_allocation_of_table_size": alloc_ms,
                       "kernel_generation_fp64": getattr(G, "kgen64_ms", None)},
         "plain_fp64": {"value": plain_value, "unit": "Mvis/s", "ms_per_step": ms_plain,

@@ -10,6 +10,8 @@ is generated in one batch (cg_aw_kernels) into a table resident in HBM, and
 all visibilities grid and degrid through one plan.
 """
 
+import time
+
 import numpy
 import torch
 
@@ -23,10 +25,21 @@ class AWProjection:
     uvw [n, 3] (wavelengths), a1, a2 [n] antenna indices, beams [nant, F, F]
     complex far fields of the antennas (A-kernel = kernel_oversample(beam, 1,
     SA)), wstep: w-bin width, w-kernels w_kernel(theta, wbin, NpixFF, S, Q).
-    fp64=True also prepares the plain FP64 form (one launch per w-plane)."""
+    fp64=True also prepares the plain FP64 form (one launch per w-plane).
+    phase_ms: a dict that receives the host time of each set-up phase (the
+    device synchronised at every phase boundary), for profiling."""
 
     def __init__(self, theta, lam, uvw, a1, a2, beams, wstep, NpixFF=32, Q=16, S=16, SA=16,
-                 N=None, fp64=False):
+                 N=None, fp64=False, phase_ms=None):
+        t_last = [time.perf_counter()]
+
+        def phase(name):
+            if phase_ms is not None:
+                torch.cuda.synchronize()
+                now = time.perf_counter()
+                phase_ms[name] = 1e3 * (now - t_last[0])
+                t_last[0] = now
+
         self.status = st = E.Status()
         self.theta, self.lam = float(theta), float(lam)
         self.N = int(round(theta * lam)) if N is None else int(N)
@@ -42,16 +55,21 @@ class AWProjection:
         wi, pair = kor % nb, kor // nb
         self.rows, self.wbin, self.nbins, self.kmin = rows, wbin, nb, kmin
         self.nkernels = len(kor)
+        phase("bins_and_keys")
         A = E.kernel_oversample(beams, 1, SA, dtype=E.CD, ndim=2).reshape(nant, SA, SA)
+        phase("a_kernels")
         Wk = E.w_kernels(theta, wstep * numpy.arange(kmin, kmax + 1).astype(numpy.float64),
                          NpixFF, S, Q, dtype=E.CD, status=st)
+        phase("w_kernels")
         self.A, self.Wk = A, Wk
         args = (A, Wk, (pair // nant).astype(numpy.int32), (pair % nant).astype(numpy.int32),
                 wi.astype(numpy.int32))
         self._aw_args = args
         self.ktab = E.KernelTable(E.aw_kernels(*args, dtype=E.CF, status=st).reshape(-1), False,
                                   Q, SA)
+        phase("aw_table")
         self.replan()
+        phase("plan")
         self.ktab64 = self.plan64 = None
         if fp64:
             self.enable_fp64()

@@ -216,17 +216,22 @@ CG_FHD void stage_dft(int logn, int s, int sign, cf *v) {
 #pragma unroll
   for (int m = 0; m < nb; ++m) dft_r(v + (m << logr), logr, sign);
 }
+// Output index of butterfly m's output r at stage s for thread t, and the
+// register slot holding it: slot q = m R + r is output out_index(q).
+CG_FHD int out_index(int logn, int s, int t, int m, int r) {
+  const int logr = stage_logr(logn, s), logp = stage_logp(logn, s);
+  const int b = t + m * (1 << (logn - 4));
+  const int k = b & ((1 << logp) - 1);
+  return ((b - k) << logr) + k + (r << logp);
+}
 template <class ST>
 CG_FHD void stage_store(int logn, int s, int t, const ST &st, const cf *v) {
-  const int logr = stage_logr(logn, s), logp = stage_logp(logn, s);
-  const int R = 1 << logr, nb = 16 >> logr, T = 1 << (logn - 4);
+  const int logr = stage_logr(logn, s);
+  const int R = 1 << logr, nb = 16 >> logr;
 #pragma unroll
   for (int m = 0; m < nb; ++m) {
-    const int b = t + m * T;
-    const int k = b & ((1 << logp) - 1);
-    const int j = ((b - k) << logr) + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) st(j + (r << logp), v[m * R + out_slot(logr, r)]);
+    for (int r = 0; r < R; ++r) st(out_index(logn, s, t, m, r), v[m * R + out_slot(logr, r)]);
   }
 }
 

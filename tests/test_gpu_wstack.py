@@ -87,3 +87,21 @@ def test_wstack_full_size_matches_oracle(env):
     got = S.w_stack_imaging(w.theta, w.lam, w.uvw, None, w.vis, kv, plane)
     ref = O.w_stack_imaging(w.theta, w.lam, w.uvw, None, w.vis, kv, plane)
     assert rel(got, ref) < 1e-5
+
+
+def test_wstack_fused_8192_matches_oracle(env):
+    """8192^2 planes (four-step columns of 128 x 64 in the batched FFT); three
+    planes, one of them empty, against the oracle."""
+    torch, configs, S, O = env
+    rng = numpy.random.default_rng(81)
+    N, theta, n = 8192, 0.05, 20000
+    lam = N / theta
+    r = rng.uniform(0, 0.4 * lam, n)
+    ph = rng.uniform(0, 2 * numpy.pi, n)
+    uvw = numpy.column_stack([r * numpy.cos(ph), r * numpy.sin(ph), rng.uniform(-400, 400, n)])
+    vis = rng.normal(size=n) + 1j * rng.normal(size=n)
+    plane = numpy.where(uvw[:, 2] < 0, 0, 2)  # plane 1 stays empty
+    kv = O.kernel_oversample(O.anti_aliasing_function(N, 0, 8), 8, 8)
+    ref = O.w_stack_imaging(theta, lam, uvw, None, vis, kv, plane)
+    got = S.w_stack_imaging(theta, lam, uvw, None, vis, kv, plane)
+    assert rel(got, ref) < 1e-5
