@@ -6,10 +6,10 @@
 //
 // Passes over HBM per plane:
 //   rows:    N / 16 threads per row, whole rows per CTA, in place;
-//   columns up to 2048: up to 512 threads per CTA transform a tile of C
+//   columns up to 1024: up to 512 threads per CTA transform a tile of C
 //            adjacent columns (C x 8 bytes of every row, H x C <= 8192
 //            elements), in place;
-//   columns from 4096: two four-step passes over tiles of 32 columns
+//   columns from 2048: two four-step passes over tiles of 32 columns
 //            (H = H1 x H2, lines of H1 then H2 elements), the second out of
 //            place (through a scratch stack, or into the dirty image).
 // Each line runs the register-blocked Stockham stages of fft32.h (radix 16,
@@ -37,8 +37,11 @@ namespace f32 {
 
 constexpr int MIN_LOG = 6, MAX_LOG = 13;
 constexpr int COL_THREADS = 512;
-// columns from this length on run as the four-step passes (both >= 64)
-constexpr int STEP_MIN = 4096;
+// columns from this length on run as the four-step passes (lines of
+// H1 >= 64 and H2 >= 32 elements; at 1024 the column tiles are faster:
+// 0.032 against 0.039 ms for a 1024^2 plane, at 2048 the four-step passes:
+// 0.064 against 0.066 ms)
+constexpr int STEP_MIN = 2048;
 
 __device__ __forceinline__ int pad(int e) { return e + (e >> 5); }  // bank spread
 
@@ -368,8 +371,11 @@ struct StepBImage {
 
 // One pass of the four-step columns: lines of L = 2^LOGL, 32 columns per
 // tile, T = L / 16 threads per column (thread (t, c), c fastest).
+// CTAs per SM the step kernels are built for (80 registers a thread)
+constexpr int step_minb(int logl) { return 768 / (32 << (logl - 4)); }
+
 template <int LOGL, class IO>
-__global__ void __launch_bounds__(32 * (1 << (LOGL - 4)), 6 >> (LOGL - 6))
+__global__ void __launch_bounds__(32 * (1 << (LOGL - 4)), step_minb(LOGL))
     k_fft32_step(IO io, int64_t units, const float2 *__restrict__ tw, int sign,
                  float *max_out) {
   constexpr int L = 1 << LOGL, T = L / 16, C = 32, NS = (LOGL + 3) / 4;
@@ -463,6 +469,7 @@ template <class IO>
 int launch_step(int logl, const IO &io, int64_t units, int sign, float *max_out,
                 cudaStream_t st) {
   switch (logl) {
+    case 5: return launch_step_as<5>(io, units, sign, max_out, st);
     case 6: return launch_step_as<6>(io, units, sign, max_out, st);
     case 7: return launch_step_as<7>(io, units, sign, max_out, st);
   }

@@ -2,7 +2,7 @@
 // stages (radix 16, one first stage of radix 2, 4 or 8), run thread by
 // thread as the kernels run them (all threads' loads of a stage before any
 // store, one buffer, twiddles from the per-stage tables), against a direct
-// DFT in double precision for N = 64 .. 8192 and both signs; and every
+// DFT in double precision for N = 32 .. 8192 and both signs; and every
 // twiddle of the per-stage tables against the exact value (at most 2^-22
 // off: one rounding, or the product of two rounded entries).  Prints the worst
 // error relative to the transform's norm; exit status 0 when it is below
@@ -22,7 +22,7 @@ int main() {
     seed = seed * 1664525u + 1013904223u;
     return (float)((seed >> 8) * (1.0 / 16777216.0) - 0.5);
   };
-  for (int logn = 6; logn <= 13; ++logn) {
+  for (int logn = 5; logn <= 13; ++logn) {
     const int N = 1 << logn, T = N / 16;
     for (int sign = -1; sign <= 1; sign += 2) {
       std::vector<cf> in(N), buf(N), tw(N);

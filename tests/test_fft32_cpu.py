@@ -1,6 +1,6 @@
 """The register-blocked Stockham line transform of the FP32 FFTs
 (crocodile_gb300/csrc/fft32.h, plain C++ compiled for the host) against a
-direct DFT in double precision for N = 64 .. 8192 and both signs, and its
+direct DFT in double precision for N = 32 .. 8192 and both signs, and its
 per-stage twiddle tables against the exact values (tests/fft32_check.cpp)."""
 
 import os

@@ -45,7 +45,7 @@ def test_centred_fft32_matches_numpy(env, H, W):
 
 @pytest.mark.parametrize("shape", [(3, 256, 512), (3, 4096, 512), (9, 4096, 4096)])
 def test_batched_and_raw_fft32(env, shape):
-    """Column tiles (256 x 512) and, for columns of 4096 and up, the four-step
+    """Column tiles (256 x 512) and, for columns of 2048 and up, the four-step
     column passes (9 planes of 4096^2 go through the 1 GiB scratch stack in
     two chunks)."""
     torch, E, S, O = env
