@@ -373,9 +373,16 @@ def _table_and_groups(gcf, src, n, dtype):
 
 
 def _grid_into(ktab, kidx, uvw, lam, shape, vis, prec, weight=None, out=None, status=None):
-    """Grid on the device; returns the device grid (c64 or c128)."""
+    """Grid on the device; returns the device grid (c64 or c128) and the plan (which
+    also takes ``ktab`` when it was built for the table's even-support padding)."""
     mode = _lib.CG_PLAN_TILED if prec == "fp32" else _lib.CG_PLAN_GROUPS
+    src = ktab
+    if prec == "fp32":
+        uvw = E.cuda_tensor(uvw, torch.float64)
+        ktab = ktab.padded_even(uvw, lam, shape)  # same results, lane gridder
     plan = E.Plan(uvw, lam, shape, ktab, kidx, mode, status)
+    if ktab is not src:
+        plan.accept(src, ktab)
     if prec == "fp32":
         g = out if out is not None else torch.zeros(shape, dtype=E.CF, device="cuda")
         if weight is None:
@@ -397,6 +404,9 @@ def _degrid_from(ktab, kidx, uvw, lam, guv, prec):
     mode = _lib.CG_PLAN_TILED if prec == "fp32" else _lib.CG_PLAN_GROUPS
     dt = E.CF if prec == "fp32" else E.CD
     g = E.cuda_tensor(guv, dt)
+    if prec == "fp32":
+        uvw = E.cuda_tensor(uvw, torch.float64)
+        ktab = ktab.padded_even(uvw, lam, tuple(g.shape))  # same results, lane gridder
     plan = E.Plan(uvw, lam, tuple(g.shape), ktab, kidx, mode)
     out = plan.degrid(ktab, g) if prec == "fp32" else plan.degrid_fp64(ktab, g)
     plan.check()

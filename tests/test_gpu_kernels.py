@@ -116,6 +116,40 @@ def test_gridder_shapes_match_oracle(env, cfg):
     assert rel(vgot, vref) < FP32_TOL
 
 
+@pytest.mark.parametrize("layout", [1, 2, 3])
+def test_odd_support_unpadded_and_padded(env, layout):
+    """An S 15 table straight through a plan (lane layout: slices padded to a
+    16-byte multiple) and its zero-padded S 16 form (padded_even, which the FP32
+    drivers use), each against the oracle; a footprint reaching the grid edge
+    keeps the table as it is."""
+    torch, E, S, A, O = env
+    theta, lam, uvw, vis = _wproj_case(O, n=8000)
+    N = int(round(theta * lam))
+    kw = dict(NpixFF=32, NpixKern=15, Qpx=4)
+    ref = O.w_cache_imaging(theta, lam, uvw, None, vis, wstep=20.0, **kw)
+    uvw_t = E.cuda_tensor(uvw, torch.float64)
+    st = E.Status()
+    kidx, kmin, kmax = E.w_bins(uvw_t, 20.0, st)
+    ws_ = 20.0 * numpy.arange(kmin, kmax + 1).astype(float)
+    kt = E.KernelTable(E.w_kernels(theta, ws_, 32, 15, 4).reshape(-1), False, 4, 15)
+    kt16 = kt.padded_even(uvw_t, lam, (N, N))
+    assert kt16.S == 16 and kt16 is not kt
+    v = E.cuda_tensor(vis, E.CF)
+    A.set_tuning(layout=layout)
+    try:
+        for table in (kt, kt16):
+            g = torch.zeros((N, N), dtype=E.CF, device="cuda")
+            plan = E.Plan(uvw_t, lam, (N, N), table, kidx, status=st)
+            plan.grid(table, v, g)
+            plan.check()
+            assert rel(g.cpu().numpy(), ref) < FP32_TOL, (layout, table.S)
+    finally:
+        A.set_tuning()
+    edge = uvw_t.clone()
+    edge[0, 0] = -0.5 * lam * (1 - 8.0 / N)  # footprint starts 4 cells from the edge
+    assert kt.padded_even(edge, lam, (N, N)) is kt
+
+
 @pytest.mark.parametrize("S_,sep", [(8, True), (8, False), (7, False), (16, False), (16, True),
                                     (3, False), (12, False)])
 def test_supports_and_separable(env, S_, sep):
