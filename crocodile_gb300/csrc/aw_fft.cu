@@ -10,8 +10,9 @@
 // costs 256 x (taps <= 256) complex MACs per output sub-kernel; this one a
 // 1024-point product and a pruned 32 x 32 inverse transform.
 //
-// k_aw_fftconv: one CTA per AW key, FA_k in shared memory, each warp takes
-// sub-kernels f in turn.  Lane = column k2: the warp loads FW_wf row by row
+// k_aw_fftconv (complex128 tables; complex64 ones run k_aw_fftconv_f below):
+// one CTA per AW key, FA_k in shared memory, each warp takes sub-kernels f
+// in turn.  Lane = column k2: the warp loads FW_wf row by row
 // (coalesced), multiplies by FA_k, runs a 32-point decimation-in-frequency
 // inverse FFT over k1 in registers (twiddle indices compile-time, table in
 // constant memory), keeps the 16 rows n1 of the crop, and transforms each of
@@ -22,6 +23,7 @@
 #include <cmath>
 
 #include "cg_internal.cuh"
+#include "fft32.h"
 
 namespace cg {
 
@@ -183,6 +185,76 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 1) k_aw_fftconv(
   }
 }
 
+// The complex64 form with 16-point register transforms (fft32.h) and one
+// transpose through shared memory in place of the shuffled row pass: per
+// sub-kernel about 800 warp instructions against 1,794.  Column pass (lane =
+// column k2): the 32-point inverse transform over k1 as two 16-point
+// transforms of the even and odd rows, Y[n] = E[n mod 16] + w32^n O[n mod 16]
+// (w32^(n + 16) = -w32^n), evaluated for the 16 kept rows n = o .. o + 15
+// only; they go to shared memory.  Row pass: lane 2r + h takes kept row r and
+// the outputs n2 = 2m + h: Out[2m + h] = DFT16_m[(z[k] + (-1)^h z[k + 16])
+// w32^(k h)], of which the 8 kept ones (n2 in o .. o + 15) are stored.
+template <int S>
+__global__ void __launch_bounds__(256, 2) k_aw_fftconv_f(
+    const float2 *__restrict__ fa, const float2 *__restrict__ fw, int nW, int QQ,
+    const int32_t *__restrict__ wi, float2 *__restrict__ out, int32_t *status) {
+  using f32::cf;
+  __shared__ float2 sfa[32][33];
+  __shared__ float2 srow[8][16][33];  // per warp: the kept rows of the column pass
+  constexpr int o = (S - 1) / 2;
+  const int k = blockIdx.x;
+  const int w = wi[k];
+  if (w < 0 || w >= nW) {
+    if (threadIdx.x == 0) atomicAdd(&status[ST_INDEX], 1);
+    return;
+  }
+  if ((status[ST_RANGE] | status[ST_INDEX]) != 0) return;
+  for (int t = threadIdx.x; t < 1024; t += blockDim.x)
+    sfa[t >> 5][t & 31] = fa[(int64_t)k * 1024 + t];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int r = lane >> 1, h = lane & 1;
+  auto mul = [](cf a, float2 b) { return cf{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; };
+  for (int f = warp; f < QQ; f += 8) {
+    const float2 *src = fw + ((int64_t)w * QQ + f) * 1024;
+    cf e[16], od[16];
+#pragma unroll
+    for (int b = 0; b < 16; ++b) {
+      const float2 x0 = src[(2 * b) * 32 + lane], a0 = sfa[2 * b][lane];
+      const float2 x1 = src[(2 * b + 1) * 32 + lane], a1 = sfa[2 * b + 1][lane];
+      e[b] = mul(cf{a0.x, a0.y}, x0);
+      od[b] = mul(cf{a1.x, a1.y}, x1);
+    }
+    f32::dft16(e, 1);  // inverse: exp(+2 pi i / 16); output q in slot out_slot(4, q)
+    f32::dft16(od, 1);
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const int n = o + t, q = n < 16 ? n : n - 16;
+      const cf E = e[f32::out_slot(4, q)], O = mul(od[f32::out_slot(4, q)], c_tw32[q]);
+      const cf y = n < 16 ? f32::cf_add(E, O) : f32::cf_sub(E, O);
+      srow[warp][t][lane] = make_float2(y.x, y.y);
+    }
+    __syncwarp();
+    cf u[16];
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      const float2 z0 = srow[warp][r][kk], z1 = srow[warp][r][kk + 16];
+      const cf sum = {z0.x + z1.x, z0.y + z1.y}, dif = {z0.x - z1.x, z0.y - z1.y};
+      u[kk] = h ? mul(dif, c_tw32[kk]) : sum;
+    }
+    __syncwarp();  // srow is rewritten by the next sub-kernel
+    f32::dft16(u, 1);
+    float2 *dst = out + ((int64_t)k * QQ + f) * 256 + r * 16;
+    constexpr int m0e = (o + 1) >> 1, m0o = o >> 1;  // first kept m for h = 0 and 1
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int me = m0e + j, mo = m0o + j;  // n2 = 2 me, or 2 mo + 1
+      const cf v = h ? u[f32::out_slot(4, mo)] : u[f32::out_slot(4, me)];
+      dst[(h ? 2 * mo + 1 : 2 * me) - o] = make_float2(v.x, v.y);
+    }
+  }
+}
+
 }  // namespace
 
 bool aw_fft_supported(int SA, int S) { return SA == 16 && S >= 1 && S <= 16; }
@@ -241,9 +313,12 @@ int aw_fft_run(const typename Cx<R>::T *akern, int nk, const void *W, int nW, in
       return set_error(CG_ERR_CUDA, "cuFFT failed (AW FFT convolution)");
   }
   const int QQ = Q * Q;
-#define CG_AW_FFT_CASE(SS)                                                               \
-  case SS:                                                                               \
-    k_aw_fftconv<T, SS><<<nk, 256, 0, st>>>(fa, fw, nW, QQ, wi, (T *)out, d_status);     \
+#define CG_AW_FFT_CASE(SS)                                                                 \
+  case SS:                                                                                 \
+    if constexpr (sizeof(R) == 4)                                                          \
+      k_aw_fftconv_f<SS><<<nk, 256, 0, st>>>(fa, fw, nW, QQ, wi, (float2 *)out, d_status);  \
+    else                                                                                   \
+      k_aw_fftconv<T, SS><<<nk, 256, 0, st>>>(fa, fw, nW, QQ, wi, (T *)out, d_status);     \
     break;
   switch (S) {
     CG_AW_FFT_CASE(1) CG_AW_FFT_CASE(2) CG_AW_FFT_CASE(3) CG_AW_FFT_CASE(4)
