@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 1) k_aw_fftconv(
 // the outputs n2 = 2m + h: Out[2m + h] = DFT16_m[(z[k] + (-1)^h z[k + 16])
 // w32^(k h)], of which the 8 kept ones (n2 in o .. o + 15) are stored.
 template <int S>
-__global__ void __launch_bounds__(256, 2) k_aw_fftconv_f(
+__global__ void __launch_bounds__(256, 3) k_aw_fftconv_f(
     const float2 *__restrict__ fa, const float2 *__restrict__ fw, int nW, int QQ,
     const int32_t *__restrict__ wi, float2 *__restrict__ out, int32_t *status) {
   using f32::cf;
