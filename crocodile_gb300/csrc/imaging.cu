@@ -3,8 +3,11 @@
 //
 // Replaces doweight (crocodile/synthesis.py:535-549), mirror_uvw (:831-852),
 // make_grid_hermitian (:855-880), fft/ifft (:83-106) and the image half of
-// do_imaging (:904-911).  FFTs run in cuFFT; the shifts of the centred
-// transform are folded into the neighbouring passes: for even sizes
+// do_imaging (:904-911).  FFTs run in the library's own transforms (FP32,
+// fft32.cu, for complex64 planes with power-of-two sides 64..8192;
+// double-float, dfft.cu, for complex128 planes 64..2048) and in cuFFT for
+// other shapes; the shifts of the centred transform are folded into the
+// neighbouring passes: for even sizes
 //   fftshift(F(ifftshift(a)))[k, l] = (-1)^(k + l + (H + W)/2) F(a * (-1)^(m + n))[k, l]
 // so no data movement is spent on them.
 #include <cufft.h>
@@ -18,7 +21,7 @@
 
 namespace cg {
 
-// ---------------------------------------------------------------- cuFFT plans
+// ---------------------------------------------------------------- cuFFT plans (other shapes)
 static std::mutex g_fft_mu;
 static std::map<std::tuple<int, int, int, int, int>, cufftHandle> g_fft_plans;
 
