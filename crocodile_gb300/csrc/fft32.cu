@@ -11,7 +11,9 @@
 //            elements), in place;
 //   columns from 2048: two four-step passes over tiles of 32 columns
 //            (H = H1 x H2, lines of H1 then H2 elements), the second out of
-//            place (through a scratch stack, or into the dirty image).
+//            place (through a scratch stack, or into the dirty image); each
+//            unit's 32 x H1 (or H2) input tile arrives by one tiled tensor
+//            copy (TMA), double-buffered against the previous unit's stages.
 // Each line runs the register-blocked Stockham stages of fft32.h (radix 16,
 // 16 values per thread): the first stage reads global memory and the last
 // writes it, coalesced; the stages between exchange through one padded
@@ -31,6 +33,9 @@
 
 #include "cg_internal.cuh"
 #include "fft32.h"
+#include "mbar.cuh"
+
+#include <cudaTypedefs.h>
 
 namespace cg {
 namespace f32 {
@@ -419,6 +424,103 @@ __global__ void __launch_bounds__(32 * (1 << (LOGL - 4)), step_minb(LOGL))
   }
 }
 
+// The column passes with their input tiles brought by the tensor-memory
+// accelerator: the 32-column x L-row box of a unit is one tiled tensor copy
+// (cp.async.bulk.tensor) into shared memory, double-buffered, so that the
+// next unit's tile is in flight while this one's stages run; the stages
+// work in place in the tile (its rows are 256 contiguous bytes and a warp
+// always touches one row: no bank conflicts without padding) and the last
+// stage writes global memory as in k_fft32_step.  The tensor map spans the
+// planes as (W, H2, H1, planes); pass A's box is (32, 1, H1, 1) at (col0, n2,
+// 0, plane), pass B's (32, H2, 1, 1) at (col0, 0, k1, plane).  Every wait is
+// bounded (about two seconds); on expiry the CTA counts the timeout in
+// g_fft32_timeouts, waits (bounded) for its other copy in flight and stops.
+constexpr long long FFT_WAIT_CYCLES = 4000000000ll;
+__device__ int g_fft32_timeouts;
+
+template <int LOGL>
+struct TmaShape {
+  static constexpr int L = 1 << LOGL, C = 32, THREADS = C * (L / 16);
+  static constexpr size_t tile_bytes() { return (size_t)L * C * sizeof(float2); }
+  static constexpr size_t smem() {  // 128 bytes of alignment slack, two tiles, twiddles, bars
+    return 128 + 2 * tile_bytes() + (size_t)tw_entries(LOGL) * sizeof(float2) + 16;
+  }
+};
+
+template <int LOGL, class IO>
+__global__ void __launch_bounds__(TmaShape<LOGL>::THREADS, step_minb(LOGL))
+    k_fft32_step_tma(const __grid_constant__ CUtensorMap tmap, IO io, int64_t units,
+                     int box_a, const float2 *__restrict__ tw, int sign, float *max_out) {
+  using TS = TmaShape<LOGL>;
+  constexpr int L = TS::L, T = L / 16, C = TS::C, NS = (LOGL + 3) / 4;
+  extern __shared__ unsigned char f32_tsm[];
+  float2 *tiles = (float2 *)(((uintptr_t)f32_tsm + 127) & ~(uintptr_t)127);
+  float2 *stw = tiles + 2 * L * C;
+  uint64_t *bar = (uint64_t *)(stw + tw_entries(LOGL));
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  for (int k = threadIdx.x; k < tw_entries(LOGL); k += TS::THREADS) stw[k] = tw[k];
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  const SmTw<LOGL> twf{stw};
+  auto issue = [&](int64_t u, int b) {  // one thread
+    int64_t pl;
+    int j, col0;
+    io.sh.unit(u, pl, j, col0);
+    if (box_a)
+      tma_load_4d(tiles + b * L * C, &tmap, col0, j, 0, (int)pl, &bar[b], (uint32_t)TS::tile_bytes());
+    else
+      tma_load_4d(tiles + b * L * C, &tmap, col0, 0, j, (int)pl, &bar[b], (uint32_t)TS::tile_bytes());
+  };
+  float mx = -FLT_MAX;
+  int64_t u = blockIdx.x;
+  if (threadIdx.x == 0 && u < units) issue(u, 0);
+  for (int it = 0; u < units; u += gridDim.x, ++it) {
+    const int b = it & 1;
+    const bool next = u + gridDim.x < units;
+    // the other tile's last reads were before the previous unit's last barrier
+    if (threadIdx.x == 0 && next) issue(u + gridDim.x, b ^ 1);
+    const bool ok = mbar_wait_cycles(&bar[b], (it >> 1) & 1, FFT_WAIT_CYCLES);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicAdd(&g_fft32_timeouts, 1);
+        if (next) mbar_wait_cycles(&bar[b ^ 1], ((it + 1) >> 1) & 1, FFT_WAIT_CYCLES);
+      }
+      return;
+    }
+    float2 *buf = tiles + b * L * C;
+    auto lds = [&](int e) {
+      const float2 v = buf[e * C + c];
+      return cf{v.x, v.y};
+    };
+    auto sts = [&](int e, cf v) { buf[e * C + c] = make_float2(v.x, v.y); };
+    const StepCtx x = io.ctx(u, c);
+    cf v[16];
+    stage_load(LOGL, 0, t, lds, twf, v);
+    __syncthreads();  // all reads before any write
+    stage_dft(LOGL, 0, sign, v);
+    stage_store(LOGL, 0, t, sts, v);
+#pragma unroll
+    for (int s = 1; s < NS; ++s) {
+      __syncthreads();
+      stage_load(LOGL, s, t, lds, twf, v);
+      __syncthreads();
+      stage_dft(LOGL, s, sign, v);
+      if (s + 1 < NS)
+        stage_store(LOGL, s, t, sts, v);
+      else
+        stage_store(LOGL, s, t, [&](int e, cf y) { io.st(x, e, y, mx); }, v);
+    }
+  }
+  if (IO::kMax && max_out) {
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomic_max_f(max_out, mx);
+  }
+}
+
 // w_H^j for j < H, correctly rounded, cached per device, log H and sign
 std::map<std::tuple<int, int, int>, float2 *> g_twfull;
 
@@ -462,6 +564,79 @@ int launch_step_as(const IO &io, int64_t units, int sign, float *max_out, cudaSt
   const unsigned grid = (unsigned)std::min<int64_t>(units, (int64_t)num_sms() * per_sm);
   k_fft32_step<LOGL, IO><<<grid, threads, smem, st>>>(io, units, tw, sign, max_out);
   CG_LAUNCH("FP32 FFT column step");
+  return CG_OK;
+}
+
+// cuTensorMapEncodeTiled from the driver (no link against libcuda)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }();
+  return fn;
+}
+
+// The TMA-fed column pass over `in` (nplanes planes of H1 H2 x W): box_a for
+// pass A.  *used = false (and nothing launched) when the tensor map cannot
+// describe the input: an unaligned base, an odd width, or no encoder.
+template <int LOGL, class IO>
+int launch_step_tma_as(const IO &io, const float2 *in, int W, int H1, int H2, int64_t nplanes,
+                       bool box_a, int64_t units, int sign, float *max_out, cudaStream_t st,
+                       bool *used) {
+  using TS = TmaShape<LOGL>;
+  *used = false;
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc || ((uintptr_t)in & 15) || W % 2 || nplanes < 1 || nplanes > INT32_MAX) return CG_OK;
+  if ((box_a ? H1 : H2) != TS::L) return CG_OK;
+  CUtensorMap map;
+  const cuuint64_t dims[4] = {(cuuint64_t)W, (cuuint64_t)H2, (cuuint64_t)H1, (cuuint64_t)nplanes};
+  const cuuint64_t strides[3] = {(cuuint64_t)W * 8, (cuuint64_t)H2 * W * 8,
+                                 (cuuint64_t)H1 * H2 * W * 8};
+  const cuuint32_t box[4] = {32, box_a ? 1u : (cuuint32_t)H2, box_a ? (cuuint32_t)H1 : 1u, 1};
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_INT64, 4, (void *)in, dims, strides, box, es,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return CG_OK;
+  const float2 *tw;
+  int rc = twiddles(LOGL, sign, &tw);
+  if (rc) return rc;
+  const size_t smem = TS::smem();
+  CG_CUDA(cudaFuncSetAttribute(k_fft32_step_tma<LOGL, IO>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft32_step_tma<LOGL, IO>,
+                                                        TS::THREADS, smem));
+  if (per_sm < 1) return CG_OK;
+  const unsigned grid = (unsigned)std::min<int64_t>(units, (int64_t)num_sms() * per_sm);
+  k_fft32_step_tma<LOGL, IO><<<grid, TS::THREADS, smem, st>>>(map, io, units, box_a ? 1 : 0, tw,
+                                                              sign, max_out);
+  CG_LAUNCH("FP32 FFT column step (TMA)");
+  *used = true;
+  return CG_OK;
+}
+
+template <class IO>
+int launch_step_tma(int logl, const IO &io, const float2 *in, int W, int H1, int H2,
+                    int64_t nplanes, bool box_a, int64_t units, int sign, float *max_out,
+                    cudaStream_t st, bool *used) {
+  switch (logl) {
+    case 5:
+      return launch_step_tma_as<5>(io, in, W, H1, H2, nplanes, box_a, units, sign, max_out, st,
+                                   used);
+    case 6:
+      return launch_step_tma_as<6>(io, in, W, H1, H2, nplanes, box_a, units, sign, max_out, st,
+                                   used);
+    case 7:
+      return launch_step_tma_as<7>(io, in, W, H1, H2, nplanes, box_a, units, sign, max_out, st,
+                                   used);
+  }
+  *used = false;
   return CG_OK;
 }
 
@@ -639,12 +814,17 @@ int fft32_planes(float2 *data, int64_t batch, int H, int W, bool inverse, bool c
       float2 *d = data + b0 * plane;
       f32::StepShape sa{W, 1 << l1, 1 << l2, W / 32, 1 << l2, plane};
       f32::StepA A{sa, d, scratch, twH};
-      rc = f32::launch_step(l1, A, nb * sa.nj * sa.tiles, sign, nullptr, st);
+      bool used;
+      rc = f32::launch_step_tma(l1, A, d, W, 1 << l1, 1 << l2, nb, true, nb * sa.nj * sa.tiles,
+                                sign, nullptr, st, &used);
+      if (!rc && !used) rc = f32::launch_step(l1, A, nb * sa.nj * sa.tiles, sign, nullptr, st);
       if (rc) break;
       f32::StepShape sb = sa;
       sb.nj = 1 << l1;
       f32::StepB B{sb, scratch, d, centred ? 1 : 0, phase & 1, (float)scale};
-      rc = f32::launch_step(l2, B, nb * sb.nj * sb.tiles, sign, nullptr, st);
+      rc = f32::launch_step_tma(l2, B, scratch, W, 1 << l1, 1 << l2, nb, false,
+                                nb * sb.nj * sb.tiles, sign, nullptr, st, &used);
+      if (!rc && !used) rc = f32::launch_step(l2, B, nb * sb.nj * sb.tiles, sign, nullptr, st);
     }
     const cudaError_t fe = cudaFreeAsync(scratch, st);
     if (rc) return rc;
@@ -678,10 +858,19 @@ int fft32_image(const float2 *grid_premod, int H, int W, float *image, float *ma
     float2 *g = (float2 *)grid_premod;
     f32::StepShape sa{W, 1 << l1, 1 << l2, W / 32, 1 << l2, (int64_t)H * W};
     f32::StepA A{sa, g, g, twH};
-    if ((rc = f32::launch_step(l1, A, (int64_t)sa.nj * sa.tiles, 1, nullptr, st))) return rc;
+    bool used;
+    if ((rc = f32::launch_step_tma(l1, A, g, W, 1 << l1, 1 << l2, 1, true,
+                                   (int64_t)sa.nj * sa.tiles, 1, nullptr, st, &used)))
+      return rc;
+    if (!used && (rc = f32::launch_step(l1, A, (int64_t)sa.nj * sa.tiles, 1, nullptr, st)))
+      return rc;
     f32::StepShape sb = sa;
     sb.nj = 1 << l1;
     f32::StepBImage B{sb, g, image, (H / 2 + W / 2) & 1, (float)(1.0 / ((double)H * W))};
+    if ((rc = f32::launch_step_tma(l2, B, g, W, 1 << l1, 1 << l2, 1, false,
+                                   (int64_t)sb.nj * sb.tiles, 1, max_out, st, &used)))
+      return rc;
+    if (used) return CG_OK;
     return f32::launch_step(l2, B, (int64_t)sb.nj * sb.tiles, 1, max_out, st);
   }
   f32::ColImageIO io{grid_premod, image, W, H, (H / 2 + W / 2) & 1,

@@ -26,6 +26,7 @@
 // status word, waits (bounded) for its copies in flight and stops.
 #include <algorithm>
 
+#include "mbar.cuh"
 #include "tiled.cuh"
 
 namespace cg {
@@ -51,21 +52,6 @@ struct LaneArgs {
   int stage_off, meta_off, val_off, bar_off;  // byte offsets inside a warp's region
 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
-               : "memory");
-}
-
-// Makes initialised mbarriers visible to the bulk-copy (async) proxy.
-__device__ __forceinline__ void mbar_fence_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
 // On lanes with p set: order the warp's earlier shared-memory reads before
 // the async proxy, then one bulk copy of `bytes` (multiple of 16, both
 // addresses 16-byte aligned) from global to shared memory completing on `bar`.
@@ -82,37 +68,9 @@ __device__ __forceinline__ void bulk_load_if(bool p, void *dst, const void *src,
       : "memory");
 }
 
-// Non-blocking poll of a phase (test_wait returns at once; try_wait may
-// suspend the thread for a while until the phase completes).
-__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
 // Waits for the phase of `bar` with the given parity; false after ~2 s.
-__device__ __noinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  if (mbar_try(bar, parity)) return true;
-  const long long t0 = clock64();
-  while (!mbar_try(bar, parity))
-    if (clock64() - t0 > LANE_WAIT_CYCLES) return false;
-  return true;
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  return mbar_wait_cycles(bar, parity, LANE_WAIT_CYCLES);
 }
 
 // FULLT: S * S == 32 * MAXT, every lane owns MAXT taps (no per-tap checks).
