@@ -118,6 +118,7 @@ SIGNATURES = {
     "cg_degrid_grid": (c_int, [P, P, P, P, c_int, P, P, P]),
     "cg_update_peak": (c_int, [c_int, c_int, P, c_size_t, ctypes.POINTER(c_double), P]),
     "cg_set_wait_limit": (c_int, [ctypes.c_longlong]),
+    "cg_fft_timeouts": (c_int, [P, c_int]),
     "cg_get_wait_limit": (ctypes.c_longlong, []),
     "cg_grid_noalloc": (c_int, [ctypes.POINTER(KernelDesc), c_int, c_int, P, c_int64, c_double,
                                 P, c_int64, P, P, P, P, P]),

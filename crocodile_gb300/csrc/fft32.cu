@@ -433,10 +433,16 @@ __global__ void __launch_bounds__(32 * (1 << (LOGL - 4)), step_minb(LOGL))
 // stage writes global memory as in k_fft32_step.  The tensor map spans the
 // planes as (W, H2, H1, planes); pass A's box is (32, 1, H1, 1) at (col0, n2,
 // 0, plane), pass B's (32, H2, 1, 1) at (col0, 0, k1, plane).  Every wait is
-// bounded (about two seconds); on expiry the CTA counts the timeout in
-// g_fft32_timeouts, waits (bounded) for its other copy in flight and stops.
+// bounded by the process-wide wait limit (cg_set_wait_limit; 0 polls once
+// without blocking); on expiry the CTA counts the timeout in
+// g_fft32_timeouts (cg_fft_timeouts), waits for its copies in flight (at
+// most the default limit each) and stops, leaving its units' output undefined.
 constexpr long long FFT_WAIT_CYCLES = 4000000000ll;
 __device__ int g_fft32_timeouts;
+
+__device__ __forceinline__ bool tile_wait(uint64_t *bar, uint32_t parity, long long cycles) {
+  return cycles ? mbar_wait_cycles(bar, parity, cycles) : mbar_test(bar, parity);
+}
 
 template <int LOGL>
 struct TmaShape {
@@ -450,7 +456,8 @@ struct TmaShape {
 template <int LOGL, class IO>
 __global__ void __launch_bounds__(TmaShape<LOGL>::THREADS, step_minb(LOGL))
     k_fft32_step_tma(const __grid_constant__ CUtensorMap tmap, IO io, int64_t units,
-                     int box_a, const float2 *__restrict__ tw, int sign, float *max_out) {
+                     int box_a, const float2 *__restrict__ tw, int sign, float *max_out,
+                     long long wait) {
   using TS = TmaShape<LOGL>;
   constexpr int L = TS::L, T = L / 16, C = TS::C, NS = (LOGL + 3) / 4;
   extern __shared__ unsigned char f32_tsm[];
@@ -483,12 +490,16 @@ __global__ void __launch_bounds__(TmaShape<LOGL>::THREADS, step_minb(LOGL))
     const bool next = u + gridDim.x < units;
     // the other tile's last reads were before the previous unit's last barrier
     if (threadIdx.x == 0 && next) issue(u + gridDim.x, b ^ 1);
-    const bool ok = mbar_wait_cycles(&bar[b], (it >> 1) & 1, FFT_WAIT_CYCLES);
+    const bool ok = tile_wait(&bar[b], (it >> 1) & 1, wait);
     if (__syncthreads_or(!ok)) {
+      // let this tile's copy and the next one's land before the CTA (and its
+      // shared memory) goes away
       if (threadIdx.x == 0) {
         atomicAdd(&g_fft32_timeouts, 1);
+        mbar_wait_cycles(&bar[b], (it >> 1) & 1, FFT_WAIT_CYCLES);
         if (next) mbar_wait_cycles(&bar[b ^ 1], ((it + 1) >> 1) & 1, FFT_WAIT_CYCLES);
       }
+      __syncthreads();
       return;
     }
     float2 *buf = tiles + b * L * C;
@@ -615,7 +626,7 @@ int launch_step_tma_as(const IO &io, const float2 *in, int W, int H1, int H2, in
   if (per_sm < 1) return CG_OK;
   const unsigned grid = (unsigned)std::min<int64_t>(units, (int64_t)num_sms() * per_sm);
   k_fft32_step_tma<LOGL, IO><<<grid, TS::THREADS, smem, st>>>(map, io, units, box_a ? 1 : 0, tw,
-                                                              sign, max_out);
+                                                              sign, max_out, wait_cycles());
   CG_LAUNCH("FP32 FFT column step (TMA)");
   *used = true;
   return CG_OK;
@@ -879,3 +890,15 @@ int fft32_image(const float2 *grid_premod, int H, int W, float *image, float *ma
 }
 
 }  // namespace cg
+
+extern "C" int cg_fft_timeouts(int32_t *count, int reset) {
+  CG_REQUIRE(count, "NULL argument");
+  int v = 0;
+  CG_CUDA(cudaMemcpyFromSymbol(&v, cg::f32::g_fft32_timeouts, sizeof(int)));
+  *count = v;
+  if (reset) {
+    const int zero = 0;
+    CG_CUDA(cudaMemcpyToSymbol(cg::f32::g_fft32_timeouts, &zero, sizeof(int)));
+  }
+  return CG_OK;
+}

@@ -425,6 +425,14 @@ def fft_df_(t, inverse):
     return t
 
 
+def fft_timeouts(reset=True):
+    """Waits of the FP32 FFT's column passes that ran out (cg_fft_timeouts), since
+    the last reset; synchronises the device."""
+    c = (ctypes.c_int32 * 1)()
+    L.call("cg_fft_timeouts", c, int(bool(reset)))
+    return int(c[0])
+
+
 def fft_raw(t, inverse):
     """Unshifted, unnormalised (i)fft of the last two dims of t, in place."""
     H, W = t.shape[-2], t.shape[-1]

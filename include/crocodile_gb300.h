@@ -128,11 +128,16 @@ int cg_get_tuning(cg_tuning *out);
  * many SM clock cycles (default 4e9, about two seconds); a wait that runs out
  * counts CG_ERR_TIMEOUT in the status block, the warp lets its copies in
  * flight land (waiting at most the default limit) and stops, and the call
- * returns.  No counterpart in the reference: a test hook that makes a wait
- * run out on purpose (a limit of 0 fails every copy not yet landed when it
- * is first polled).  Process-wide. */
+ * returns.  The FP32 FFT's column passes wait for their tensor copies under
+ * the same limit; a wait that runs out there is counted in a device-wide
+ * counter that cg_fft_timeouts reads (after synchronising the device; reset
+ * nonzero: set it back to 0), and the transform's output is undefined.  No
+ * counterpart in the reference: a test hook that makes a wait run out on
+ * purpose (a limit of 0 fails every copy not yet landed when it is first
+ * polled).  Process-wide. */
 int cg_set_wait_limit(long long cycles);
 long long cg_get_wait_limit(void);
+int cg_fft_timeouts(int32_t *count, int reset);
 
 /* A plan holds the visibilities' bit-exact cell assignment, their order
  * (sorted into grid tiles, or into kernel groups for the plain FP64 form)

@@ -71,3 +71,30 @@ def test_lane_wait_runs_out_and_context_survives(env):
     O.convgrid(gcf, ref, uvw[:, :2], kidx[:, None], vis)
     got = grid.cpu().numpy()
     assert numpy.linalg.norm(got - ref) / numpy.linalg.norm(ref) < 1e-5
+
+
+def test_fft_tile_wait_runs_out_and_next_transform_is_exact(env):
+    """The FP32 FFT's column passes (tensor copies of their tiles, from 2048
+    rows) wait under the same limit: at 0 the first poll of a copy not yet
+    landed gives up, the timeout is counted, and the call returns; with the
+    default limit the next transform matches numpy."""
+    torch, L, E, O, autotune = env
+    lib = L.lib()
+    rng = numpy.random.default_rng(32)
+    a = rng.normal(size=(4096, 4096)) + 1j * rng.normal(size=(4096, 4096))
+    E.fft_timeouts(reset=True)
+    default = lib.cg_get_wait_limit()
+    try:
+        assert lib.cg_set_wait_limit(0) == L.CG_OK
+        t = E.cuda_tensor(a, E.CF)
+        E.fft_(t, True)
+        torch.cuda.synchronize()
+        assert E.fft_timeouts(reset=True) > 0
+    finally:
+        lib.cg_set_wait_limit(default)
+    t = E.cuda_tensor(a, E.CF)
+    E.fft_(t, True)
+    assert E.fft_timeouts(reset=True) == 0
+    ref = O.ifft(a)
+    got = t.cpu().numpy()
+    assert numpy.linalg.norm(got - ref) / numpy.linalg.norm(ref) < 2e-6
