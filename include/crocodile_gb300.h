@@ -326,7 +326,7 @@ int cg_make_hermitian(void *grid, int H, int W, int is_c64,
  * H x W arrays (H = 1: 1-D), in place; the inverse includes 1/(H*W).
  * Grids with H and W even need no workspace; otherwise workspace must hold
  * one array of the same size.  complex64 with power-of-two sides 64..8192
- * run the library's own FP32 FFT; from H = 4096 its column passes go
+ * run the library's own FP32 FFT; from H = 2048 its column passes go
  * through a scratch stack of at most 1 GiB taken from a memory pool the
  * library keeps per device (stream-ordered, retained after the first use). */
 int cg_fft(void *data, int batch, int H, int W, int is_c64, int inverse,
