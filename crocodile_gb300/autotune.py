@@ -87,15 +87,18 @@ def _store(sig, entry):
 def candidates(S, quick=False):
     """Launch shapes to try: the warp layout over tile edge, work-item size and
     warps per CTA; the owner layout over tile edge, rows per thread and groups;
-    the lane layout (S <= 16) over tile edge and work-item size."""
+    the lane layout (S <= 16) over tile edge, work-item size and degridder."""
     tiles = [t for t in ((32, 48) if quick else (16, 24, 32, 48, 64)) if t >= min(S, 16)]
     chunks = (0, 1024) if quick else (0, 512, 2048)
     out = []
     if S <= 16:
-        for tile, chunk in itertools.product((16, 32) if quick else (16, 24, 32),
-                                             (512, 1024) if quick else (0, 512, 1024)):
+        # the lane layout, each with the tiled degridder (dvis 0) and the ring
+        # degridder (dvis 3)
+        for tile, chunk, dvis in itertools.product((16, 32) if quick else (16, 24, 32),
+                                                   (512, 1024) if quick else (0, 512, 1024),
+                                                   (0, 3)):
             out.append({"tile": tile, "chunk": chunk, "rows": 0, "groups": 0,
-                        "layout": L.CG_LAYOUT_LANE})
+                        "layout": L.CG_LAYOUT_LANE, "dvis": dvis})
     for tile, chunk in itertools.product(tiles, chunks):
         for warps in ((8,) if quick else (4, 8)):
             out.append({"tile": tile, "chunk": chunk, "rows": 0, "groups": warps,

@@ -70,8 +70,7 @@ int cg_set_tuning(const cg_tuning *t) {
   CG_REQUIRE(t->chunk >= 0 && t->chunk <= (1 << 20), "chunk %d out of range", t->chunk);
   CG_REQUIRE(t->rows >= 0 && t->rows <= 8, "rows %d out of range [0, 8]", t->rows);
   CG_REQUIRE(t->layout >= 0 && t->layout <= CG_LAYOUT_LANE, "layout %d unknown", t->layout);
-  CG_REQUIRE(t->dvis >= 0 && t->dvis <= 4 && t->dvis != 3, "dvis %d must be 0, 1, 2 or 4",
-             t->dvis);
+  CG_REQUIRE(t->dvis >= 0 && t->dvis <= 4, "dvis %d must be 0..4", t->dvis);
   const int gmax = t->layout == CG_LAYOUT_LANE ? 16 : 8;
   CG_REQUIRE(t->groups >= 0 && t->groups <= gmax, "groups %d out of range [0, %d]", t->groups,
              gmax);

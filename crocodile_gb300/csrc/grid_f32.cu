@@ -704,6 +704,12 @@ int cg_degrid(const cg_plan *p, const void *ktab, const void *grid, void *out,
   if (dvis == 1 && layout_for(p->kd) == CG_LAYOUT_LANE)
     return lane_launch(p, (const float2 *)ktab, nullptr, nullptr, 0, nullptr,
                        (const float2 *)grid, (float2 *)out, 0, true, s);
+  // dvis 3: the shared window with per-warp slice rings, where the table streams
+  if (dvis == 3) {
+    const int rc = ring_degrid_launch(p, (const float2 *)ktab, (const float2 *)grid,
+                                      (float2 *)out, s);
+    if (rc != CG_ERR_ARG) return rc;
+  }
   TiledArgs A = tiled_args(p);
   const int SS = p->kd.S * p->kd.S;
   const int need = (SS + 31) / 32;

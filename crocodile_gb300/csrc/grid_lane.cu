@@ -353,6 +353,21 @@ __global__ void k_pad_slices(const float2 *__restrict__ src, int64_t nslices, in
   }
 }
 
+// Odd S * S: the table with slices padded to an even element count (a
+// 16-byte multiple), copied into the plan's workspace; ktab then points at it.
+static int padded_table(const cg_plan *p, const float2 *&ktab, cudaStream_t s) {
+  const int SS = p->kd.S * p->kd.S, KS = p->kd.sep ? p->kd.S : p->slice_stride;
+  if (p->kd.sep || KS == SS) return CG_OK;
+  CG_REQUIRE(p->kpad && KS == SS + 1, "plan has no padded kernel table");
+  const int64_t total = p->kpad_slices * KS;
+  const unsigned blocks = (unsigned)std::max<int64_t>(
+      1, std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16));
+  k_pad_slices<<<blocks, 256, 0, s>>>(ktab, p->kpad_slices, SS, KS, p->kpad);
+  CG_LAUNCH("kernel slice padding");
+  ktab = p->kpad;
+  return CG_OK;
+}
+
 template <bool SEP, bool BULK, bool FUSED>
 static void *lane_kernel_for(int maxt, int SS, int pitch) {
   if (maxt == 8 && SS == 256 && pitch == 32) return (void *)k_lane<SEP, BULK, FUSED, 8, true, 16, 32>;
@@ -378,18 +393,9 @@ int lane_launch(const cg_plan *p, const float2 *ktab, const float2 *vis, const f
   const int need = (SS + 31) / 32;
   int maxt = 1;
   while (maxt < need) maxt *= 2;
-  // odd S * S: the table with slices padded to an even element count (a
-  // 16-byte multiple), copied into the plan's workspace
   const int KS = p->kd.sep ? S : p->slice_stride;
-  if (!p->kd.sep && KS != SS) {
-    CG_REQUIRE(p->kpad && KS == SS + 1, "plan has no padded kernel table");
-    const int64_t total = p->kpad_slices * KS;
-    const unsigned blocks = (unsigned)std::max<int64_t>(
-        1, std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16));
-    k_pad_slices<<<blocks, 256, 0, s>>>(ktab, p->kpad_slices, SS, KS, p->kpad);
-    CG_LAUNCH("kernel slice padding");
-    ktab = p->kpad;
-  }
+  const int prc = padded_table(p, ktab, s);
+  if (prc) return prc;
   const bool bulk = !p->kd.sep && (KS * 8) % 16 == 0 && ((uintptr_t)ktab & 15) == 0;
 
   const cg_tuning t = tuning();
@@ -446,6 +452,217 @@ int lane_launch(const cg_plan *p, const float2 *ktab, const float2 *vis, const f
   TiledArgs A = tiled_args(p);
   CG_CUDA(cudaMemsetAsync(p->ticket, 0, sizeof(int32_t), s));
   void *args[] = {&A, &P};
+  CG_CUDA(cudaLaunchKernel(fn, dim3((unsigned)blocks), dim3(threads), args, smem, s));
+  return CG_OK;
+}
+
+// ---------------------------------------------------------------- ring degridder
+// Degridding (convdegrid, synthesis.py:484-503) of lane-layout plans with the
+// tiled degridder's CTA-shared window and the lane gridder's slice streaming:
+// the CTA stages one work item's grid window in shared memory, warp w takes
+// the item's visibilities w, w + warps, ..., and each warp streams its
+// visibilities' S x S slices through its own ring of D shared-memory stages
+// (bulk copies issued D - 1 visibilities ahead by lane 0, completion counted
+// in bytes on one mbarrier per stage), so ~D slices per warp are in flight
+// without holding registers.  Lane l sums taps l + 32 i against the window
+// and the warp reduces with shuffles.  The item's records are staged per warp
+// in shared memory before its first copies are issued.  Waits are bounded: a
+// warp whose copy does not land in time counts the timeout, lets its copies
+// in flight land, and the whole CTA stops at the next item boundary.
+struct RingArgs {
+  const float2 *ktab;
+  const float2 *grid;
+  float2 *out;
+  long long wait_cycles;
+  int kstride;                   // elements between slices
+  int depth;                     // stages per warp
+  int win_bytes;                 // window region (16-byte multiple)
+  int warp_bytes;                // per-warp region: stages, records, barriers
+  int meta_off, bar_off;         // offsets inside a warp's region
+};
+
+template <int MAXT, bool FULLT, int SC = 0, int PC = 0>
+__global__ void __launch_bounds__(256) k_degrid_ring(TiledArgs A, RingArgs R) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_item, s_fail;
+  if (status_failed(A.status)) return;
+  const int S = SC ? SC : A.S, SS = S * S, pitch = PC ? PC : A.pitch;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  float2 *win = (float2 *)smem;
+  unsigned char *region = smem + R.win_bytes + (size_t)warp * R.warp_bytes;
+  float2 *stages = (float2 *)region;
+  int4 *meta = (int4 *)(region + R.meta_off);
+  uint64_t *bar = (uint64_t *)(region + R.bar_off);
+  const int QQ = A.Q * A.Q, KS = R.kstride, D = R.depth;
+  const uint32_t slice_bytes = (uint32_t)KS * 8u;
+  const float2 zero = make_float2(0.f, 0.f);
+
+  int soff[MAXT];
+  bool own[MAXT];
+  constexpr bool STEP = SC > 0 && 32 % (SC > 0 ? SC : 1) == 0;
+#pragma unroll
+  for (int i = 0; i < MAXT; ++i) {
+    const int t = lane + 32 * i;
+    const int dy = STEP ? lane / S + i * (32 / S) : t / S;
+    const int dx = STEP ? lane % S : t - dy * S;
+    own[i] = FULLT || t < SS;
+    soff[i] = dy * pitch + dx;
+  }
+  if (lane == 0) {
+    for (int d = 0; d < D; ++d) mbar_init(&bar[d], 1);
+    mbar_fence_init();
+  }
+  if (threadIdx.x == 0) s_fail = 0;
+
+  // consumer position in this warp's ring (persists across items)
+  int cst = 0;
+  uint32_t cpar = 0;
+  for (;;) {
+    __syncthreads();  // the last item's window reads; s_fail
+    if (threadIdx.x == 0) s_item = atomicAdd(A.ticket, 1);
+    __syncthreads();
+    if (s_fail) return;  // a warp's wait ran out: its copies have landed
+    const int it = s_item;
+    if (it >= *A.nitems) break;
+    const WorkItem w = A.items[it];
+    const TileOrigin org = tile_origin(A, w.tile);
+    const int n = w.count;
+    const int mine = n > warp ? (n - warp + nw - 1) / nw : 0;
+
+    // this warp's records: footprint base in the window, slice, destination
+    for (int q = lane; q < mine; q += 32) {
+      const int j = w.start + warp + q * nw;
+      const VisRec r = A.recs[j];
+      meta[q] = make_int4((r.y0 - org.wy0) * pitch + (r.x0 - org.wx0), r.k0 * QQ + r.k1,
+                          A.perm[j], 0);
+    }
+    __syncwarp();
+    int issued = 0;
+    for (int ist = cst; issued < min(mine, D - 1); ++issued) {
+      bulk_load_if(lane == 0, stages + (size_t)ist * KS, R.ktab + (size_t)meta[issued].y * KS,
+                   slice_bytes, &bar[ist]);
+      ist = ist + 1 == D ? 0 : ist + 1;
+    }
+    // the window, while the first copies are in flight
+    for (int c = threadIdx.x; c < A.win * A.win; c += blockDim.x) {
+      const int r = c / A.win, q = c - r * A.win;
+      const int gy = org.wy0 + r, gx = org.wx0 + q;
+      win[r * pitch + q] = (gy < A.H && gx < A.W)
+                               ? __ldg(&R.grid[org.layer_off + (size_t)gy * A.W + gx])
+                               : zero;
+    }
+    __syncthreads();
+
+    int q = 0;
+    bool failed = false;
+    for (; q < mine; ++q) {
+      if (issued < mine) {  // into the stage visibility q - 1 used
+        const int ist = cst == 0 ? D - 1 : cst - 1;
+        bulk_load_if(lane == 0, stages + (size_t)ist * KS, R.ktab + (size_t)meta[issued].y * KS,
+                     slice_bytes, &bar[ist]);
+        ++issued;
+      }
+      // a limit of 0 (a test of the timeout path) polls without blocking
+      bool ok = R.wait_cycles ? mbar_try(&bar[cst], cpar) : mbar_test(&bar[cst], cpar);
+      if (!__all_sync(FULL_MASK, ok)) {  // warp-uniform slow path, bounded
+        const long long t0 = clock64();
+        while (!ok && clock64() - t0 <= R.wait_cycles) ok = mbar_try(&bar[cst], cpar);
+        if (__any_sync(FULL_MASK, !ok)) {
+          failed = true;
+          break;
+        }
+      }
+      const int4 m = meta[q];
+      const float2 *kp = stages + (size_t)cst * KS + lane;
+      float2 sum = zero;
+#pragma unroll
+      for (int i = 0; i < MAXT; ++i)
+        if (own[i]) cfma(sum, win[m.x + soff[i]], kp[32 * i]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        sum.x += __shfl_xor_sync(FULL_MASK, sum.x, o);
+        sum.y += __shfl_xor_sync(FULL_MASK, sum.y, o);
+      }
+      if (lane == 0) R.out[m.z] = sum;
+      if (++cst == D) {
+        cst = 0;
+        cpar ^= 1u;
+      }
+      __syncwarp();  // this stage's reads before a copy reuses it
+    }
+    if (failed) {
+      // record the timeout, let this warp's copies in flight land; the CTA
+      // stops at the next item boundary
+      if (lane == 0) {
+        atomicAdd((int32_t *)&A.status[ST_TIMEOUT], 1);
+        s_fail = 1;
+        int st = cst;
+        uint32_t par = cpar;
+        for (int jx = q; jx < issued; ++jx) {
+          mbar_wait(&bar[st], par);
+          if (++st == D) {
+            st = 0;
+            par ^= 1u;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+int ring_degrid_launch(const cg_plan *p, const float2 *ktab, const float2 *grid, float2 *out,
+                       cudaStream_t s) {
+  const int S = p->kd.S, SS = S * S;
+  if (p->kd.sep || S > 16) return CG_ERR_ARG;
+  const int KS = p->slice_stride;
+  const int prc = padded_table(p, ktab, s);
+  if (prc) return prc;
+  if ((KS * 8) % 16 != 0 || ((uintptr_t)ktab & 15) != 0) return CG_ERR_ARG;
+  const int need = (SS + 31) / 32;
+  int maxt = 1;
+  while (maxt < need) maxt *= 2;
+  // 8 warps and 2 stages: 4 CTAs per SM with 512-visibility items, which
+  // measured fastest on the AW set (3.79 ms against 3.86 with 5 CTAs, 4.29
+  // with 3 stages and 3 CTAs, 4.95 with 16 warps per CTA)
+  const int warps = 8;
+  auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+  RingArgs R;
+  R.ktab = ktab;
+  R.grid = grid;
+  R.out = out;
+  R.wait_cycles = wait_cycles();
+  R.kstride = KS;
+  R.depth = 2;
+  R.win_bytes = (int)up16((size_t)p->pitch * p->win * sizeof(float2));
+  const int per_warp = (p->chunk + warps - 1) / warps;
+  size_t off = (size_t)R.depth * KS * sizeof(float2);
+  R.meta_off = (int)off;
+  off += (size_t)per_warp * sizeof(int4);
+  R.bar_off = (int)off;
+  R.warp_bytes = (int)up16(off + R.depth * sizeof(uint64_t));
+  const size_t smem = (size_t)R.win_bytes + (size_t)warps * R.warp_bytes;
+  CG_REQUIRE(smem <= (227u << 10), "ring degridder does not fit in shared memory (%zu bytes)",
+             smem);
+  void *fn = nullptr;
+  if (maxt == 8 && SS == 256 && p->pitch == 32) fn = (void *)k_degrid_ring<8, true, 16, 32>;
+  else if (maxt == 8 && SS == 256) fn = (void *)k_degrid_ring<8, true>;
+  else if (maxt == 2 && SS == 64) fn = (void *)k_degrid_ring<2, true>;
+  else if (maxt == 1) fn = (void *)k_degrid_ring<1, false>;
+  else if (maxt == 2) fn = (void *)k_degrid_ring<2, false>;
+  else if (maxt == 4) fn = (void *)k_degrid_ring<4, false>;
+  else if (maxt == 8) fn = (void *)k_degrid_ring<8, false>;
+  CG_REQUIRE(fn, "no ring degridder for support %d", S);
+  const int threads = 32 * warps;
+  CG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+  CG_REQUIRE(per_sm > 0, "ring degridder does not fit on an SM (smem %zu)", smem);
+  const int64_t blocks =
+      std::max<int64_t>(1, std::min<int64_t>((int64_t)per_sm * num_sms(), p->max_items));
+  TiledArgs A = tiled_args(p);
+  CG_CUDA(cudaMemsetAsync(p->ticket, 0, sizeof(int32_t), s));
+  void *args[] = {&A, &R};
   CG_CUDA(cudaLaunchKernel(fn, dim3((unsigned)blocks), dim3(threads), args, smem, s));
   return CG_OK;
 }

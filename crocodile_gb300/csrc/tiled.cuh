@@ -82,4 +82,10 @@ int lane_launch(const cg_plan *p, const float2 *ktab, const float2 *vis, const f
                 int gmode, float2 *grid, const float2 *grid_in, float2 *vis_out, int residual,
                 bool fused, cudaStream_t s);
 
+// Degridding of lane-layout plans with per-warp slice rings (grid_lane.cu);
+// CG_ERR_ARG (nothing launched) when the plan's table cannot stream by bulk
+// copies (separable, S > 16, or a table that is not 16-byte aligned).
+int ring_degrid_launch(const cg_plan *p, const float2 *ktab, const float2 *grid, float2 *out,
+                       cudaStream_t s);
+
 }  // namespace cg

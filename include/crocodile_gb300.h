@@ -107,7 +107,10 @@ typedef struct {
  * groups, or warp-layout warps, per CTA (1..8), or lane-layout warps per
  * CTA (1..16); dvis: the degridder: 0 (automatic) or 2 runs the tiled
  * degridder with 2 visibilities per warp step, 4 with 4; 1 runs lane-layout
- * plans through the lane kernel's degridding traversal (others as 0).  layout 0 picks CG_LAYOUT_LANE (with 16-cell tiles) for
+ * plans through the lane kernel's degridding traversal (others as 0); 3 runs
+ * plans whose table streams by bulk copies (non-separable, S <= 16, 16-byte
+ * slices) through the ring degridder: the item's window in shared memory,
+ * each warp's slices by bulk copies through a 2-stage ring (others as 0).  layout 0 picks CG_LAYOUT_LANE (with 16-cell tiles) for
  * non-separable tables with even S <= 16, whose slices stream by bulk
  * copies as they are, and CG_LAYOUT_WARP otherwise.  Process-wide. */
 #define CG_LAYOUT_WARP 1

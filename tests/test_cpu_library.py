@@ -107,7 +107,7 @@ def test_tuning_roundtrip_and_validation(libpath):
         assert autotune.get_tuning() == {"tile": 32, "chunk": 700, "rows": 3, "groups": 2,
                                          "layout": 2, "dvis": 4}
         for bad in ({"tile": 30}, {"tile": 68}, {"rows": 9}, {"groups": 9}, {"layout": 4},
-                    {"layout": 3, "groups": 17}, {"dvis": 3}):
+                    {"layout": 3, "groups": 17}, {"dvis": 5}):
             with pytest.raises(ValueError):
                 autotune.set_tuning(**bad)
     finally:

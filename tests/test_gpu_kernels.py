@@ -98,6 +98,9 @@ def _wproj_case(O, n=20000, N=256, seed=5):
     {"layout": 3, "rows": 3, "groups": 14, "tile": 16, "chunk": 64},
     {"layout": 3, "tile": 16, "dvis": 4},            # degridder: four visibilities a warp
     {"layout": 3, "tile": 16, "dvis": 1},            # degridder: the lane kernel's traversal
+    {"layout": 3, "tile": 16, "dvis": 3},            # degridder: window + slice rings
+    {"layout": 3, "tile": 16, "rows": 2, "chunk": 40, "dvis": 3},
+    {"layout": 1, "tile": 32, "chunk": 100, "dvis": 3},  # warp layout, odd S: tiled
     {"layout": 1, "groups": 8, "tile": 32, "chunk": 100, "dvis": 4},
 ])
 def test_gridder_shapes_match_oracle(env, cfg):

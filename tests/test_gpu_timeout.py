@@ -98,3 +98,50 @@ def test_fft_tile_wait_runs_out_and_next_transform_is_exact(env):
     ref = O.ifft(a)
     got = t.cpu().numpy()
     assert numpy.linalg.norm(got - ref) / numpy.linalg.norm(ref) < 2e-6
+
+
+def test_ring_degrid_polls_under_zero_limit_and_next_call_is_exact(env):
+    """The ring degridder (tuning dvis 3) waits for its slices' bulk copies under
+    the same limit.  Its first copies fly while the CTA stages the grid window,
+    so at a limit of 0 a poll may or may not find its copy landed: the call
+    returns either way, and either counts timeouts (code -7) or gives the
+    oracle's visibilities; with the default limit the same plan degrids to the
+    oracle's visibilities."""
+    torch, L, E, O, autotune = env
+    lib = L.lib()
+    rng = numpy.random.default_rng(33)
+    N, S, Q, G, n = 512, 16, 4, 2, 20_000
+    r = rng.uniform(0, 0.4, n)
+    ph = rng.uniform(0, 2 * numpy.pi, n)
+    uvw = numpy.column_stack([r * numpy.cos(ph), r * numpy.sin(ph), numpy.zeros(n)])
+    gcf = rng.normal(size=(G, Q, Q, S, S)) + 1j * rng.normal(size=(G, Q, Q, S, S))
+    kidx = rng.integers(0, G, n).astype(numpy.int32)
+    a = rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N))
+    kt = E.KernelTable.from_gcf(gcf, 1, E.CF)
+    assert autotune.effective_layout(kt) == L.CG_LAYOUT_LANE
+    st = E.Status()
+    st.reset()
+    plan = E.Plan(uvw, 1.0, (N, N), kt, kidx, status=st)
+    plan.check()
+    g = E.cuda_tensor(a, E.CF)
+    default = lib.cg_get_wait_limit()
+    autotune.set_tuning(dvis=3)
+    try:
+        try:
+            assert lib.cg_set_wait_limit(0) == L.CG_OK
+            first = plan.degrid(kt, g).cpu().numpy()  # returns: every wait is bounded
+            timed_out = st.counts()[3] > 0
+            if timed_out:
+                with pytest.raises(RuntimeError, match="code -7"):
+                    st.check()
+        finally:
+            lib.cg_set_wait_limit(default)
+        st.reset()
+        got = plan.degrid(kt, g).cpu().numpy()
+        plan.check()
+    finally:
+        autotune.set_tuning()
+    ref = O.convdegrid(gcf, a, uvw[:, :2], kidx[:, None])
+    assert numpy.linalg.norm(got - ref) / numpy.linalg.norm(ref) < 1e-5
+    if not timed_out:
+        assert numpy.linalg.norm(first - ref) / numpy.linalg.norm(ref) < 1e-5
