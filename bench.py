@@ -843,7 +843,7 @@ def run_ours(args):
         kname = {L.CG_LAYOUT_LANE: "k_lane", L.CG_LAYOUT_OWNER: "k_grid_tiled"}.get(lay,
                                                                                    "k_grid_warp")
     else:
-        kname = "k_degrid_tiled"
+        kname = "k_degrid_ring" if tuned.get("dvis") == 3 else "k_degrid_tiled"
     peaks = {}
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk):
