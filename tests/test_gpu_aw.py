@@ -61,6 +61,13 @@ def test_aw_subset_matches_oracle(aw_workload):
     assert rel(g_host, ref) < 1e-5
     vref = O.w_cache_predict(w.theta, w.lam, uvw, src, ref, wstep=wstep, kernel_cache=fn)
     assert rel(v.cpu().numpy(), vref) < 1e-5
+    from crocodile_gb300 import autotune
+    autotune.set_tuning(dvis=3)  # the ring degridder
+    try:
+        vr = op.degrid(g)
+    finally:
+        autotune.set_tuning()
+    assert rel(vr.cpu().numpy(), vref) < 1e-5
 
 
 def test_aw_full_size_fp32_vs_fp64(aw_workload):
@@ -79,6 +86,16 @@ def test_aw_full_size_fp32_vs_fp64(aw_workload):
     v32 = op.degrid(g64.to(torch.complex64))
     v64 = op.degrid_fp64(g64)
     err = float(torch.linalg.vector_norm(v32.to(torch.complex128) - v64) /
+                torch.linalg.vector_norm(v64))
+    assert err < 1e-5, err
+    # the ring degridder (dvis 3, the autotuner's pick for this workload)
+    from crocodile_gb300 import autotune
+    autotune.set_tuning(dvis=3)
+    try:
+        vr = op.degrid(g64.to(torch.complex64))
+    finally:
+        autotune.set_tuning()
+    err = float(torch.linalg.vector_norm(vr.to(torch.complex128) - v64) /
                 torch.linalg.vector_norm(v64))
     assert err < 1e-5, err
     # the fused pass (each AW slice read once) gives both results at once
