@@ -117,6 +117,10 @@ def test_tuning_roundtrip_and_validation(libpath):
     cands = autotune.candidates(15)
     assert any(c["layout"] == 1 for c in cands) and any(c["layout"] == 2 for c in cands)
     assert any(c["layout"] == 3 for c in cands)
+    # every lane-layout shape is tried with the tiled and the ring degridder
+    lane = [c for c in cands if c["layout"] == 3]
+    assert {c.get("dvis", 0) for c in lane} == {0, 3}
+    assert all(c.get("dvis", 0) == 0 for c in cands if c["layout"] != 3)
     assert not any(c["layout"] == 3 for c in autotune.candidates(24))
     for c in cands:
         if c["layout"] == 2:
