@@ -850,12 +850,17 @@ def run_ours(args):
         peaks = json.load(open(pk))
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg / (dom_ms * 1e-3) / 1e9
-    traffic = None
+    traffic = traffic_src = None
     tf = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tf):
-        entry = json.load(open(tf)).get(args.workload, {}).get(kname)
+        # captures are keyed by kernel and work-item size (the plan's chunk)
+        chunk = info_plan["chunk"]
+        recs = json.load(open(tf)).get(args.workload, {})
+        entry = recs.get("%s/chunk%d" % (kname, chunk)) or next(
+            (v for k, v in recs.items() if k.split("/")[0] == kname), None)
         if entry:
             traffic = entry["bytes_per_launch"]
+            traffic_src = entry["source"]
 
     # ---- update rate: 2 n S^2 grid-point updates per step against the measured
     # shared-memory update and L2 atomic peaks (microbenchmarks of cg_update_peak)
@@ -956,6 +961,7 @@ def run_ours(args):
                      "streamed_bytes_def": "n*(16 record + 4 index + 8 value + %d kernel slice) + "
                                            "N^2*8: what this gridder reads per launch" % kbytes,
                      "traffic_over_algorithmic": traffic / alg if traffic else None,
+                     "traffic_source": traffic_src,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks
                      else "fallback 6800 GB/s"},
         "update_roofline": {"updates_per_s": urate, "updates_per_step": 2 * n * S * S,

@@ -52,15 +52,18 @@ struct LaneArgs {
   int stage_off, meta_off, val_off, bar_off;  // byte offsets inside a warp's region
 };
 
-// On lanes with p set: order the warp's earlier shared-memory reads before
-// the async proxy, then one bulk copy of `bytes` (multiple of 16, both
+// On lanes with p set: one bulk copy of `bytes` (multiple of 16, both
 // addresses 16-byte aligned) from global to shared memory completing on `bar`.
-// Predicated rather than branched, so the warp does not diverge.
+// Predicated rather than branched, so the warp does not diverge.  No proxy
+// fence before it: generic code only ever reads the stages these copies fill
+// (nothing generic writes them), and every read of a stage has returned its
+// value, which the reading lane has consumed, before the warp barrier that
+// precedes the copy reusing the stage; a fence here measured 4.33 against
+// 4.13 ms for the AW gridder and 3.79 against 3.66 ms for the ring degridder.
 __device__ __forceinline__ void bulk_load_if(bool p, void *dst, const void *src, uint32_t bytes,
                                              uint64_t *bar) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "@p fence.proxy.async.shared::cta;\n\t"
       "@p mbarrier.arrive.expect_tx.shared::cta.b64 _, [%3], %2;\n\t"
       "@p cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
       "\n\t}" ::"r"(smem_u32(dst)),
