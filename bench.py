@@ -37,6 +37,12 @@ import time
 
 import numpy
 
+# One hardware work queue per stream for this process (read when CUDA
+# initialises): with the default 8, the end-to-end pipeline's kernel stream
+# and copy-out stream can share a queue, and each step's kernels then wait
+# behind the last step's copy-out.  A value the caller set is kept.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
