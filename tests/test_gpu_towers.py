@@ -115,3 +115,23 @@ def test_w_towers_predict_single_plane_is_w_cache_predict(env):
     got = S.w_towers_predict(theta, lam, uvw, None, guv, 64, 16, 100.0, 10.0, **kw)
     ref = O.w_cache_predict(theta, lam, uvw, None, guv, wstep=10.0, **kw)
     assert rel(got, ref) < TOL
+
+
+@pytest.mark.parametrize("kern", [7, 8])
+def test_w_towers_predict_ring_degridder_matches_oracle(env, kern):
+    """The layered (chunk, plane) plans of w-towers predict through the ring
+    degridder (tuning dvis 3): layer offsets, sparse items, padded odd slices."""
+    torch, E, S, O = env
+    from crocodile_gb300 import autotune
+    theta, lam, uvw, vis = _case(n=20000, seed=55)
+    N = int(round(theta * lam))
+    rng = numpy.random.default_rng(8)
+    guv = rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N))
+    kw = dict(NpixFF=32, NpixKern=kern, Qpx=4)
+    autotune.set_tuning(dvis=3)
+    try:
+        got = S.w_towers_predict(theta, lam, uvw, None, guv, 64, 16, 60.0, 10.0, **kw)
+    finally:
+        autotune.set_tuning()
+    ref = O.w_towers_predict(theta, lam, uvw, None, guv, 64, 16, 60.0, 10.0, **kw)
+    assert rel(got, ref) < TOL
