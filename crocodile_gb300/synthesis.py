@@ -579,23 +579,34 @@ def _spec_w_cache(theta, uvw_t, uvw_host, src, wstep, kernel_cache, kernel_fn, k
 
 
 def _int_columns(src, n, nsrc):
-    """The src columns as an int32 [n, nsrc] host array with per-column minima and
-    ranges, or None when a column is not integer-valued or the ranges are too wide
-    for packed keys."""
-    s = src.cpu().numpy() if isinstance(src, torch.Tensor) else numpy.asarray(src)
-    s = s.reshape(n, nsrc)
-    if s.dtype.kind in "iu":
-        si = s
-    elif s.dtype.kind == "f":
-        if not numpy.all(numpy.isfinite(s)) or not numpy.array_equal(numpy.floor(s), s):
+    """The src columns as an int32 [n, nsrc] device tensor with per-column minima
+    and ranges (host int64 arrays), or None when a column is not integer-valued or
+    the ranges are too wide for packed keys.  The integrality test and the column
+    minima and maxima run on the device (on the host they took most of a 16M-row
+    do_imaging call)."""
+    if isinstance(src, torch.Tensor):
+        t = src.reshape(n, nsrc)
+        if t.dtype == torch.bool or t.dtype.is_complex:
             return None
-        si = s
     else:
-        return None
-    lo, hi = si.min(axis=0), si.max(axis=0)
+        a = numpy.asarray(src).reshape(n, nsrc)
+        if a.dtype.kind == "u":
+            if a.dtype.itemsize == 8 and a.size and a.max() >= 2 ** 63:
+                return None
+            a = a.astype(numpy.int64)  # unsigned tensors have partial support in torch
+        elif a.dtype.kind not in "if":
+            return None
+        t = torch.from_numpy(numpy.ascontiguousarray(a))
+    t = t.to("cuda")
+    if t.dtype.is_floating_point:
+        if not bool(torch.isfinite(t).all()) or not bool((torch.floor(t) == t).all()):
+            return None
+    lo, hi = torch.aminmax(t, dim=0)
+    lo, hi = lo.double().cpu().numpy(), hi.double().cpu().numpy()
     if numpy.any(lo < -2 ** 31) or numpy.any(hi >= 2 ** 31):
         return None
-    return si.astype(numpy.int32), lo.astype(numpy.int64), (hi - lo + 1).astype(numpy.int64)
+    lo, hi = lo.astype(numpy.int64), hi.astype(numpy.int64)
+    return t.to(torch.int32), lo, hi - lo + 1
 
 
 def _device_keys(theta, uvw_t, src, nsrc, wstep, fn, kwargs, dtype):
@@ -619,7 +630,7 @@ def _device_keys(theta, uvw_t, src, nsrc, wstep, fn, kwargs, dtype):
     space = int(nb) * int(numpy.prod(rng))
     if space >= 2 ** 31 - 1 or space > 64 * n + (1 << 24):
         return None
-    key = E.row_keys(uvw_t, wstep, kmin, nb, torch.from_numpy(si), lo, rng, st)
+    key = E.row_keys(uvw_t, wstep, kmin, nb, si, lo, rng, st)
     rows, kor = E.compact_keys(key, space, st)
     st.check()
     kor = kor.cpu().numpy().astype(numpy.int64)
