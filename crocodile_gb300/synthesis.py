@@ -73,14 +73,16 @@ def _nrows(x):
 
 
 def _src_cols(src, n):
+    """Columns of src as an [n, k] array (0 for None or empty); a tensor's shape is
+    read without copying it to the host."""
     if src is None:
         return 0
-    if isinstance(src, torch.Tensor):
-        src = src.cpu().numpy()
-    s = numpy.asarray(src)
-    if s.size == 0:
+    size = src.numel() if isinstance(src, torch.Tensor) else numpy.size(src)
+    if size == 0:
         return 0
-    return s.reshape(n, -1).shape[1]
+    if n == 0 or size % n:
+        raise ValueError("src has %d values, not a multiple of the %d rows" % (size, n))
+    return size // n
 
 
 # --------------------------------------------------------------------------
