@@ -81,6 +81,22 @@ def test_kernel_layout_and_groups():
     assert E.kernel_groups((), None, 5) is None
 
 
+def test_src_columns_counted_from_the_shape():
+    """The src argument's column count (the reference's src[:, i] indexing),
+    from numpy, lists or tensors without a host copy; a size that is not a
+    multiple of the rows is refused."""
+    import torch
+    from crocodile_gb300 import synthesis as S
+    assert S._src_cols(None, 4) == 0
+    assert S._src_cols(numpy.ndarray((4, 0)), 4) == 0
+    assert S._src_cols(numpy.zeros((4, 2)), 4) == 2
+    assert S._src_cols([[1, 2, 3]] * 4, 4) == 3
+    assert S._src_cols(numpy.zeros(4), 4) == 1
+    assert S._src_cols(torch.zeros(4, 2, dtype=torch.int32), 4) == 2
+    with pytest.raises(ValueError):
+        S._src_cols(numpy.zeros(7), 4)
+
+
 def test_host_helpers_match_oracle():
     from crocodile_gb300 import synthesis as S
     from oracle import crocodile_oracle as O
